@@ -1,0 +1,182 @@
+"""Seeded synthetic scenes for the DFPSR triangle path.
+
+Every scene is plain numpy data laid out like the reference's Model
+(Source/DFPSR/implementation/render/model/Model.h:54-64): indexed positions,
+polygons of 3 or 4 corners with a texture coordinate (u1, v1, u2, v2) and an
+RGBA colour per corner, one part with an optional diffuse and light texture.
+The same arrays feed the GPU renderer, the CPU oracle and the reference build,
+so the three render identical inputs.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Scene:
+    width: int
+    height: int
+    positions: np.ndarray          # (N, 3) float32, model space
+    poly_indices: np.ndarray       # (P, 4) int32, index 3 is -1 for triangles
+    tex_coords: np.ndarray         # (P, 4, 4) float32 (u1, v1, u2, v2) per corner
+    colors: np.ndarray             # (P, 4, 4) float32 RGBA per corner
+    diffuse: Optional[np.ndarray]  # (H, W) uint32 level-0 texels, RGBA bytes in memory order
+    diffuse_levels: int
+    light: Optional[np.ndarray]
+    light_levels: int
+    filter: int                    # 0 Solid, 1 Alpha
+    camera_location: np.ndarray    # (12,) float32: position, xAxis, yAxis, zAxis
+    perspective: bool
+    slope: float                   # widthSlope (perspective) or halfWidth (orthogonal)
+    near_clip: float
+    far_clip: float
+    model_to_world: np.ndarray     # (12,) float32
+
+    @property
+    def triangle_count(self) -> int:
+        return int(np.sum(np.where(self.poly_indices[:, 3] < 0, 1, 2)))
+
+
+IDENTITY = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1], dtype=np.float32)
+
+
+def _normalize(v):
+    v = np.asarray(v, dtype=np.float64)
+    n = np.linalg.norm(v)
+    return v / n if n > 0 else np.array([0.0, 0.0, 1.0])
+
+
+def axis_system(forward, up):
+    """Camera axes like FMatrix3x3::makeAxisSystem (math/FMatrix3x3.h:46-53), in float64."""
+    z = _normalize(forward)
+    x = _normalize(np.cross(_normalize(up), z))
+    y = _normalize(np.cross(z, x))
+    return x, y, z
+
+
+def camera_location(position, forward, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    x, y, z = axis_system(forward, up)
+    return np.concatenate([np.asarray(position, np.float64), x, y, z]).astype(np.float32)
+
+
+def noise_texture(rng: np.random.Generator, size: int) -> np.ndarray:
+    return rng.integers(0, 2**32, size=(size, size), dtype=np.uint64).astype(np.uint32)
+
+
+def random_triangles(seed: int = 1234, triangles: int = 20000, width: int = 800, height: int = 600,
+                     texture_size: int = 256, fov_degrees: float = 60.0) -> Scene:
+    """Independent triangles with corners uniform in [-1, 1]^3, seen from distance 3.
+
+    Per-vertex RGBA colours are uniform bytes divided by 255, texture coordinates
+    uniform in [0, 1], and one uniform-noise texture with a full mip chain.
+    """
+    rng = np.random.default_rng(seed)
+    positions = rng.uniform(-1.0, 1.0, size=(triangles * 3, 3)).astype(np.float32)
+    idx = np.arange(triangles * 3, dtype=np.int32).reshape(triangles, 3)
+    poly = np.concatenate([idx, -np.ones((triangles, 1), np.int32)], axis=1)
+    colors = np.zeros((triangles, 4, 4), np.float32)
+    colors[:, :3, :] = rng.integers(0, 256, size=(triangles, 3, 4)).astype(np.float32) / np.float32(255.0)
+    tex = np.zeros((triangles, 4, 4), np.float32)
+    tex[:, :3, :] = rng.uniform(0.0, 1.0, size=(triangles, 3, 4)).astype(np.float32)
+    diffuse = noise_texture(rng, texture_size) if texture_size else None
+    slope = np.float32(math.tan(math.radians(fov_degrees) * 0.5))
+    return Scene(width, height, positions, poly, tex, colors, diffuse, 16, None, 1, 0,
+                 camera_location((0.0, 0.0, -3.0), (0.0, 0.0, 1.0)), True, float(slope), 0.01, 1000.0,
+                 IDENTITY.copy())
+
+
+def value_noise(rng: np.random.Generator, size: int, octaves: int = 6, base_cells: int = 4) -> np.ndarray:
+    """Sum of `octaves` layers of bilinearly smoothed lattice noise in [0, 1), float64."""
+    result = np.zeros((size, size), np.float64)
+    amplitude, total = 1.0, 0.0
+    coords = np.arange(size, dtype=np.float64) / size
+    for o in range(octaves):
+        cells = base_cells << o
+        lattice = rng.uniform(0.0, 1.0, size=(cells + 1, cells + 1))
+        f = coords * cells
+        i0 = np.floor(f).astype(np.int64)
+        t = f - i0
+        t = t * t * (3.0 - 2.0 * t)
+        a = lattice[np.ix_(i0, i0)]
+        b = lattice[np.ix_(i0, i0 + 1)]
+        c = lattice[np.ix_(i0 + 1, i0)]
+        d = lattice[np.ix_(i0 + 1, i0 + 1)]
+        ty, tx = t[:, None], t[None, :]
+        layer = (a * (1 - tx) + b * tx) * (1 - ty) + (c * (1 - tx) + d * tx) * ty
+        result += amplitude * layer
+        total += amplitude
+        amplitude *= 0.5
+    return result / total
+
+
+def terrain(seed: int = 1234, grid: int = 512, width: int = 1920, height: int = 1080, texture_size: int = 1024,
+            height_scale: float = 48.0, pitch_degrees: float = 30.0, camera_height: float = 120.0,
+            width_slope: float = 1.0) -> Scene:
+    """A grid x grid height field of quads (A-B-C-D with alternating diagonals, as the
+    reference's terrain sample builds it: Source/SDK/terrain/main.cpp:121-171), textured
+    with seeded noise and coloured with seeded per-point colours, seen from above at a pitch."""
+    rng = np.random.default_rng(seed)
+    heights = (value_noise(rng, grid) * height_scale).astype(np.float32)
+    zs, xs = np.meshgrid(np.arange(grid, dtype=np.float32), np.arange(grid, dtype=np.float32), indexing="ij")
+    positions = np.stack([xs, heights, -zs], axis=-1).reshape(-1, 3).astype(np.float32)
+    point_colors = np.concatenate([rng.uniform(0.55, 1.0, size=(grid * grid, 3)), np.ones((grid * grid, 1))], axis=1).astype(np.float32)
+    px, pz = np.meshgrid(np.arange(1, grid), np.arange(1, grid), indexing="xy")
+    px = px.reshape(-1).astype(np.int64); pz = pz.reshape(-1).astype(np.int64)
+    x0, z0 = px - 1, pz - 1
+    ia = x0 + z0 * grid
+    ib = px + z0 * grid
+    ic = px + pz * grid
+    idd = x0 + pz * grid
+    scale = np.float32(1.0) / np.float32(grid - 1.0)
+    ta = np.stack([x0 * scale, z0 * scale], -1)
+    tb = np.stack([px * scale, z0 * scale], -1)
+    tc = np.stack([px * scale, pz * scale], -1)
+    td = np.stack([x0 * scale, pz * scale], -1)
+    even = ((px + pz) % 2) == 0
+    idx = np.where(even[:, None], np.stack([ia, ib, ic, idd], -1), np.stack([ib, ic, idd, ia], -1)).astype(np.int32)
+    uv = np.where(even[:, None, None], np.stack([ta, tb, tc, td], 1), np.stack([tb, tc, td, ta], 1)).astype(np.float32)
+    tex = np.zeros((idx.shape[0], 4, 4), np.float32)
+    tex[:, :, :2] = uv
+    colors = point_colors[idx]
+    diffuse = noise_texture(rng, texture_size)
+    pitch = math.radians(pitch_degrees)
+    center = grid * 0.5
+    position = (center, camera_height, camera_height / math.tan(pitch) * 0.5)
+    forward = (0.0, -math.sin(pitch), -math.cos(pitch))
+    return Scene(width, height, positions, idx, tex, colors, diffuse, 16, None, 1, 0,
+                 camera_location(position, forward), True, float(width_slope), 0.01, 1000.0, IDENTITY.copy())
+
+
+def with_variant(scene: Scene, *, texture: bool = True, light: bool = False, colors: str = "random",
+                 seed: int = 7, pyramid: bool = True) -> Scene:
+    """Same geometry with another RgbaMultiply variant (Source/DFPSR/implementation/render/shader/RgbaMultiply.h:110-173).
+
+    colors: "random" (vertex fading), "white" (colorless), "constant" (one colour per triangle).
+    """
+    rng = np.random.default_rng(seed)
+    s = dataclasses.replace(scene)
+    p = scene.colors.shape[0]
+    if colors == "white":
+        s.colors = np.ones_like(scene.colors)
+    elif colors == "constant":
+        c = rng.integers(0, 256, size=(p, 1, 4)).astype(np.float32) / np.float32(255.0)
+        s.colors = np.repeat(c, 4, axis=1).astype(np.float32)
+    if not texture:
+        s.diffuse = None
+    elif s.diffuse is None:
+        s.diffuse = noise_texture(rng, 64)
+    if not pyramid:
+        s.diffuse_levels = 1
+    if light:
+        s.light = noise_texture(rng, 32)
+        s.light_levels = 1
+        t = s.tex_coords.copy()
+        t[:, :, 2:] = rng.uniform(0.0, 1.0, size=t[:, :, 2:].shape).astype(np.float32)
+        s.tex_coords = t
+    else:
+        s.light = None
+    return s

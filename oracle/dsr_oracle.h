@@ -1,0 +1,98 @@
+/*
+ * CPU oracle for the DFPSR triangle-rendering hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain, scalar C restatement of the reference's algorithm, used as the
+ * checker for the CUDA path (tests, smoke() and bench.py's CPU-baseline leg).
+ * The product never links, loads or calls it.  Every function cites the
+ * reference file:line it restates (paths relative to the reference's Source/).
+ *
+ * Float arithmetic is IEEE binary32 in source order; the build must use
+ * -ffp-contract=off so that a*b+c is never fused (the reference's exact build
+ * is scalar with contraction off, see oracle/Makefile.ref).
+ */
+#ifndef DSR_ORACLE_H
+#define DSR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* TextureRgbaU8 (DFPSR/implementation/image/Texture.h:42-102). */
+typedef struct {
+	uint32_t log2width, log2height, maxMipLevel;
+	uint32_t startOffset, maxLevelMask;
+	uint32_t minWidthOrMask, minHeightOrMask, maxWidthAndMask, maxHeightAndMask;
+	float floatMaxWidth, floatMaxHeight;
+	uint32_t pixelCount;
+	uint32_t *pixels; /* pyramid, smallest level first, RGBA bytes in memory order */
+} or_texture;
+
+/* A model with one part (DFPSR/implementation/render/model/Model.h:54-64,
+ * Model.cpp:150-162).  polyIndices: polyCount x 4 (index 3 < 0 for triangles).
+ * texCoords, colors: polyCount x 4 corners x 4 floats. */
+typedef struct {
+	const float *positions;
+	int32_t pointCount;
+	const int32_t *polyIndices;
+	const float *texCoords;
+	const float *colors;
+	int32_t polyCount;
+	const or_texture *diffuse; /* may be null */
+	const or_texture *light;   /* may be null */
+	int32_t filter;            /* 0 Solid, 1 Alpha */
+} or_model;
+
+/* Camera description shared by every entry point: location = position(3),
+ * xAxis(3), yAxis(3), zAxis(3); slope = widthSlope (perspective) or halfWidth
+ * (orthogonal). */
+typedef struct {
+	float location[12];
+	int32_t perspective;
+	float slope, nearClip, farClip;
+	int32_t width, height;
+} or_camera_desc;
+
+/* Optional instrumentation collected while rendering. */
+typedef struct {
+	uint64_t fragments;      /* (pixel, triangle) pairs inside the row intervals, before the depth test */
+	uint64_t trianglesDrawn; /* draw commands executed (after cull/clip/front-face) */
+	uint32_t *coverage;      /* optional per-pixel fragment count */
+	uint32_t *winner;        /* optional per-pixel order key of the last colour/depth write */
+} or_stats;
+
+/* ---- textures ---- */
+int or_texture_init_empty(or_texture *t, uint32_t log2w, uint32_t log2h, uint32_t maxMipLevel);
+int or_texture_create_from_image(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions);
+void or_texture_free(or_texture *t);
+void or_texture_generate_pyramid(or_texture *t);
+uint32_t or_texture_pixel_offset_to_layer(const or_texture *t, uint32_t mipLevel);
+uint32_t or_texture_pixel_offset(const or_texture *t, uint32_t x, uint32_t y, uint32_t mipLevel);
+uint32_t or_texture_read_pixel(const or_texture *t, uint32_t x, uint32_t y, uint32_t mipLevel);
+void or_texture_write_pixel(or_texture *t, uint32_t x, uint32_t y, uint32_t mipLevel, uint32_t color);
+uint32_t or_interpolate_color_linear(uint32_t a, uint32_t b, uint32_t weight);
+uint32_t or_interpolate_color_bilinear(uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t wx, uint32_t wy);
+uint32_t or_sample_bilinear(const or_texture *t, float u, float v, uint32_t mipLevel, int highestResolution);
+uint32_t or_sample_nearest(const or_texture *t, float u, float v, uint32_t mipLevel, int highestResolution);
+uint32_t or_mip_level_index(const or_texture *t, const float u[4], const float v[4]);
+
+/* ---- geometry ---- */
+void or_camera_to_screen(const or_camera_desc *cam, const float cs[3], float outIs[2], int64_t outFlat[2]);
+int32_t or_triangle_rows(const int64_t flat[6], const int32_t clip[4], int32_t *startRow, int32_t *lefts, int32_t *rights, int32_t maxRows);
+
+/* ---- rendering ---- */
+/* model_render (DFPSR/api/modelAPI.cpp:197-201) when bands == 1, and the
+ * band-split renderer_* path (renderCore.cpp:449-480) when bands > 1, run on
+ * `threads` worker threads.  color (packOrder 0..3) and depth may be null. */
+int or_model_render(const or_model *model, const float modelToWorld[12], const or_camera_desc *cam,
+                    uint32_t *color, float *depth, int32_t packOrder, int32_t bands, int32_t threads,
+                    or_stats *stats);
+/* model_renderDepth (DFPSR/api/modelAPI.cpp:202-206). */
+int or_model_render_depth(const or_model *model, const float modelToWorld[12], const or_camera_desc *cam,
+                          float *depth, or_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,221 @@
+"""ctypes front end of the C oracle (oracle/dsr_oracle.c) -- test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "dsr_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+                               src, "-o", LIB_PATH, "-lm"])
+    return LIB_PATH
+
+
+class Texture(C.Structure):
+    _fields_ = [("log2width", C.c_uint32), ("log2height", C.c_uint32), ("maxMipLevel", C.c_uint32),
+                ("startOffset", C.c_uint32), ("maxLevelMask", C.c_uint32),
+                ("minWidthOrMask", C.c_uint32), ("minHeightOrMask", C.c_uint32),
+                ("maxWidthAndMask", C.c_uint32), ("maxHeightAndMask", C.c_uint32),
+                ("floatMaxWidth", C.c_float), ("floatMaxHeight", C.c_float),
+                ("pixelCount", C.c_uint32), ("pixels", C.POINTER(C.c_uint32))]
+
+    def array(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.pixels, shape=(self.pixelCount,)).copy()
+
+    def fields(self):
+        return [self.log2width, self.log2height, self.maxMipLevel, self.startOffset, self.maxLevelMask,
+                self.minWidthOrMask, self.minHeightOrMask, self.maxWidthAndMask, self.maxHeightAndMask]
+
+
+class Model(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("pointCount", C.c_int32), ("polyIndices", C.c_void_p),
+                ("texCoords", C.c_void_p), ("colors", C.c_void_p), ("polyCount", C.c_int32),
+                ("diffuse", C.POINTER(Texture)), ("light", C.POINTER(Texture)), ("filter", C.c_int32)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("location", C.c_float * 12), ("perspective", C.c_int32), ("slope", C.c_float),
+                ("nearClip", C.c_float), ("farClip", C.c_float), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("fragments", C.c_uint64), ("trianglesDrawn", C.c_uint64),
+                ("coverage", C.c_void_p), ("winner", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        l = C.CDLL(path)
+        P = C.c_void_p
+        l.or_texture_init_empty.argtypes = [C.POINTER(Texture), C.c_uint32, C.c_uint32, C.c_uint32]
+        l.or_texture_create_from_image.argtypes = [C.POINTER(Texture), P, C.c_int32, C.c_int32, C.c_int32]
+        l.or_texture_free.argtypes = [C.POINTER(Texture)]
+        l.or_texture_generate_pyramid.argtypes = [C.POINTER(Texture)]
+        for name in ("or_texture_pixel_offset_to_layer",):
+            getattr(l, name).argtypes = [C.POINTER(Texture), C.c_uint32]
+            getattr(l, name).restype = C.c_uint32
+        for name in ("or_texture_pixel_offset", "or_texture_read_pixel"):
+            getattr(l, name).argtypes = [C.POINTER(Texture), C.c_uint32, C.c_uint32, C.c_uint32]
+            getattr(l, name).restype = C.c_uint32
+        l.or_texture_write_pixel.argtypes = [C.POINTER(Texture), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+        l.or_interpolate_color_linear.argtypes = [C.c_uint32] * 3
+        l.or_interpolate_color_linear.restype = C.c_uint32
+        l.or_interpolate_color_bilinear.argtypes = [C.c_uint32] * 6
+        l.or_interpolate_color_bilinear.restype = C.c_uint32
+        l.or_sample_bilinear.argtypes = [C.POINTER(Texture), C.c_float, C.c_float, C.c_uint32, C.c_int]
+        l.or_sample_bilinear.restype = C.c_uint32
+        l.or_sample_nearest.argtypes = [C.POINTER(Texture), C.c_float, C.c_float, C.c_uint32, C.c_int]
+        l.or_sample_nearest.restype = C.c_uint32
+        l.or_camera_to_screen.argtypes = [C.POINTER(CameraDesc), P, P, P]
+        l.or_triangle_rows.argtypes = [P, P, P, P, P, C.c_int32]
+        l.or_triangle_rows.restype = C.c_int32
+        l.or_model_render.argtypes = [C.POINTER(Model), P, C.POINTER(CameraDesc), P, P, C.c_int32, C.c_int32,
+                                      C.c_int32, C.POINTER(Stats)]
+        l.or_model_render.restype = C.c_int
+        l.or_model_render_depth.argtypes = [C.POINTER(Model), P, C.POINTER(CameraDesc), P, C.POINTER(Stats)]
+        l.or_model_render_depth.restype = C.c_int
+        _lib = l
+    return _lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleTexture:
+    def __init__(self, pixels: Optional[np.ndarray] = None, resolutions: int = 16, empty=None):
+        self.t = Texture()
+        if empty is not None:
+            if lib().or_texture_init_empty(C.byref(self.t), *empty):
+                raise MemoryError
+        else:
+            pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
+            h, w = pixels.shape
+            if lib().or_texture_create_from_image(C.byref(self.t), _ptr(pixels), w, h, resolutions):
+                raise ValueError("texture dimensions must be powers of two")
+
+    def __del__(self):
+        try:
+            lib().or_texture_free(C.byref(self.t))
+        except Exception:
+            pass
+
+    def ref(self):
+        return C.pointer(self.t)
+
+
+def camera_desc(scene) -> CameraDesc:
+    d = CameraDesc()
+    for i in range(12):
+        d.location[i] = float(scene.camera_location[i])
+    d.perspective = 1 if scene.perspective else 0
+    d.slope = scene.slope
+    d.nearClip = scene.near_clip
+    d.farClip = scene.far_clip
+    d.width = scene.width
+    d.height = scene.height
+    return d
+
+
+class PreparedModel:
+    """Keeps the numpy buffers and textures of one scene alive for repeated renders."""
+
+    def __init__(self, scene):
+        self.scene = scene
+        self.positions = np.ascontiguousarray(scene.positions, np.float32)
+        self.poly = np.ascontiguousarray(scene.poly_indices, np.int32)
+        self.tex = np.ascontiguousarray(scene.tex_coords, np.float32)
+        self.colors = np.ascontiguousarray(scene.colors, np.float32)
+        self.diffuse = OracleTexture(scene.diffuse, scene.diffuse_levels) if scene.diffuse is not None else None
+        self.light = OracleTexture(scene.light, scene.light_levels) if scene.light is not None else None
+        m = Model()
+        m.positions = _ptr(self.positions)
+        m.pointCount = self.positions.shape[0]
+        m.polyIndices = _ptr(self.poly)
+        m.texCoords = _ptr(self.tex)
+        m.colors = _ptr(self.colors)
+        m.polyCount = self.poly.shape[0]
+        m.diffuse = self.diffuse.ref() if self.diffuse else None
+        m.light = self.light.ref() if self.light else None
+        m.filter = scene.filter
+        self.model = m
+        self.cam = camera_desc(scene)
+        self.transform = np.ascontiguousarray(scene.model_to_world, np.float32)
+
+
+def render(scene, color: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None, *, pack_order: int = 0,
+           bands: int = 1, threads: int = 1, use_color: bool = True, use_depth: bool = True,
+           coverage: bool = False, winner: bool = False, prepared: Optional[PreparedModel] = None):
+    """model_render (bands == 1) or the band-split renderer (bands > 1) on the CPU oracle.
+
+    Returns (color, depth, info) where info holds fragments, trianglesDrawn and the optional
+    per-pixel coverage counts and winner keys."""
+    pm = prepared or PreparedModel(scene)
+    h, w = scene.height, scene.width
+    if use_color:
+        color = np.zeros((h, w), np.uint32) if color is None else np.ascontiguousarray(color, np.uint32).copy()
+    else:
+        color = None
+    if use_depth:
+        depth = np.zeros((h, w), np.float32) if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+    else:
+        depth = None
+    st = Stats()
+    cov = np.zeros((h, w), np.uint32) if coverage else None
+    win = np.full((h, w), 0xFFFFFFFF, np.uint32) if winner else None
+    st.coverage = _ptr(cov)
+    st.winner = _ptr(win)
+    lib().or_model_render(C.byref(pm.model), _ptr(pm.transform), C.byref(pm.cam), _ptr(color), _ptr(depth),
+                          pack_order, bands, threads, C.byref(st))
+    info = {"fragments": int(st.fragments), "triangles_drawn": int(st.trianglesDrawn), "coverage": cov, "winner": win}
+    return color, depth, info
+
+
+def render_depth(scene, depth: Optional[np.ndarray] = None, *, coverage: bool = False, winner: bool = False,
+                 prepared: Optional[PreparedModel] = None):
+    pm = prepared or PreparedModel(scene)
+    h, w = scene.height, scene.width
+    depth = np.zeros((h, w), np.float32) if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+    st = Stats()
+    cov = np.zeros((h, w), np.uint32) if coverage else None
+    win = np.full((h, w), 0xFFFFFFFF, np.uint32) if winner else None
+    st.coverage = _ptr(cov)
+    st.winner = _ptr(win)
+    lib().or_model_render_depth(C.byref(pm.model), _ptr(pm.transform), C.byref(pm.cam), _ptr(depth), C.byref(st))
+    return depth, {"fragments": int(st.fragments), "triangles_drawn": int(st.trianglesDrawn), "coverage": cov,
+                   "winner": win}
+
+
+def triangle_rows(flat, clip, max_rows: int = 1 << 16):
+    flat = np.ascontiguousarray(flat, np.int64)
+    clip = np.ascontiguousarray(clip, np.int32)
+    start = np.zeros(1, np.int32)
+    lefts = np.zeros(max_rows, np.int32)
+    rights = np.zeros(max_rows, np.int32)
+    n = lib().or_triangle_rows(_ptr(flat), _ptr(clip), _ptr(start), _ptr(lefts), _ptr(rights), max_rows)
+    if n <= 0:
+        return int(start[0]), lefts[:0], rights[:0]
+    return int(start[0]), lefts[:n].copy(), rights[:n].copy()
+
+
+def camera_to_screen(scene, cs):
+    d = camera_desc(scene)
+    cs = np.ascontiguousarray(cs, np.float32)
+    out_is = np.zeros(2, np.float32)
+    out_flat = np.zeros(2, np.int64)
+    lib().or_camera_to_screen(C.byref(d), _ptr(cs), _ptr(out_is), _ptr(out_flat))
+    return out_is, out_flat

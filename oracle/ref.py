@@ -1,0 +1,149 @@
+"""ctypes front end of the reference itself, built out-of-tree into oracle/_ref/ -- test infrastructure only.
+
+`available()` is False wherever the reference sources were not present to
+build from (for example on a machine that only received this repository).
+"""
+from __future__ import annotations
+
+import atexit
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+REFERENCE_ROOT = os.environ.get("DFPSR_REFERENCE", "/root/reference")
+
+
+def lib_path(variant: str = "exact") -> str:
+    return os.path.join(REF_DIR, f"libdsr_ref_{variant}.so")
+
+
+def build(jobs: int = 8) -> bool:
+    """Builds both reference variants when the reference sources exist; returns availability."""
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "Source", "DFPSR")):
+        return available()
+    repo = os.path.dirname(HERE)
+    subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={REFERENCE_ROOT}", f"-j{jobs}"],
+                          cwd=repo)
+    return available()
+
+
+def available(variant: str = "exact") -> bool:
+    if not os.path.exists(lib_path(variant)):
+        return False
+    try:
+        _load(variant)
+        return True
+    except OSError:
+        return False
+
+
+_libs = {}
+
+
+def _load(variant: str):
+    if variant not in _libs:
+        l = C.CDLL(lib_path(variant))
+        P = C.c_void_p
+        l.refh_texture_create.argtypes = [P, C.c_int, C.c_int, C.c_int]
+        l.refh_texture_create.restype = P
+        l.refh_texture_info.argtypes = [P, P, P, C.c_int]
+        l.refh_texture_info.restype = C.c_int
+        l.refh_texture_free.argtypes = [P]
+        l.refh_model_create.argtypes = [P, C.c_int, P, P, P, C.c_int, P, P, C.c_int]
+        l.refh_model_create.restype = P
+        l.refh_model_free.argtypes = [P]
+        l.refh_model_render.argtypes = [P, P, P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, P, P,
+                                        C.c_int, C.c_int]
+        l.refh_model_render.restype = C.c_int
+        l.refh_model_render_depth.argtypes = [P, P, P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, P]
+        l.refh_model_render_depth.restype = C.c_int
+        l.refh_camera_to_screen.argtypes = [P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, P, P, P]
+        l.refh_triangle_rows.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_int]
+        l.refh_triangle_rows.restype = C.c_int
+        atexit.register(l.refh_shutdown)
+        _libs[variant] = l
+    return _libs[variant]
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class RefTexture:
+    def __init__(self, lib, pixels: np.ndarray, resolutions: int):
+        self.lib = lib
+        self.pixels = np.ascontiguousarray(pixels, np.uint32)
+        h, w = self.pixels.shape
+        self.handle = lib.refh_texture_create(_ptr(self.pixels), w, h, resolutions)
+
+    def info(self):
+        fields = np.zeros(9, np.uint32)
+        n = self.lib.refh_texture_info(self.handle, _ptr(fields), None, 0)
+        pixels = np.zeros(n, np.uint32)
+        self.lib.refh_texture_info(self.handle, _ptr(fields), _ptr(pixels), n)
+        return fields, pixels
+
+    def __del__(self):
+        try:
+            self.lib.refh_texture_free(self.handle)
+        except Exception:
+            pass
+
+
+class RefModel:
+    def __init__(self, scene, variant: str = "exact"):
+        self.lib = _load(variant)
+        self.scene = scene
+        self.positions = np.ascontiguousarray(scene.positions, np.float32)
+        self.poly = np.ascontiguousarray(scene.poly_indices, np.int32)
+        self.tex = np.ascontiguousarray(scene.tex_coords, np.float32)
+        self.colors = np.ascontiguousarray(scene.colors, np.float32)
+        self.diffuse = RefTexture(self.lib, scene.diffuse, scene.diffuse_levels) if scene.diffuse is not None else None
+        self.light = RefTexture(self.lib, scene.light, scene.light_levels) if scene.light is not None else None
+        self.handle = self.lib.refh_model_create(
+            _ptr(self.positions), self.positions.shape[0], _ptr(self.poly), _ptr(self.tex), _ptr(self.colors),
+            self.poly.shape[0], self.diffuse.handle if self.diffuse else None,
+            self.light.handle if self.light else None, scene.filter)
+        self.camera = np.ascontiguousarray(scene.camera_location, np.float32)
+        self.transform = np.ascontiguousarray(scene.model_to_world, np.float32)
+
+    def __del__(self):
+        try:
+            self.lib.refh_model_free(self.handle)
+        except Exception:
+            pass
+
+    def render(self, color=None, depth=None, *, pack_order: int = 0, threaded: bool = False,
+               use_color: bool = True, use_depth: bool = True):
+        s = self.scene
+        h, w = s.height, s.width
+        color = (np.zeros((h, w), np.uint32) if color is None else np.ascontiguousarray(color, np.uint32).copy()) if use_color else None
+        depth = (np.zeros((h, w), np.float32) if depth is None else np.ascontiguousarray(depth, np.float32).copy()) if use_depth else None
+        self.lib.refh_model_render(self.handle, _ptr(self.transform), _ptr(self.camera), int(s.perspective), s.slope,
+                                   s.near_clip, s.far_clip, w, h, _ptr(color), _ptr(depth), pack_order, 1 if threaded else 0)
+        return color, depth
+
+    def render_depth(self, depth=None):
+        s = self.scene
+        depth = np.zeros((s.height, s.width), np.float32) if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+        self.lib.refh_model_render_depth(self.handle, _ptr(self.transform), _ptr(self.camera), int(s.perspective), s.slope,
+                                         s.near_clip, s.far_clip, s.width, s.height, _ptr(depth))
+        return depth
+
+
+def triangle_rows(flat, clip, variant: str = "exact", max_rows: int = 1 << 16):
+    l = _load(variant)
+    flat = np.ascontiguousarray(flat, np.int64)
+    clip = np.ascontiguousarray(clip, np.int32)
+    start = np.zeros(1, np.int32)
+    lefts = np.zeros(max_rows, np.int32)
+    rights = np.zeros(max_rows, np.int32)
+    n = l.refh_triangle_rows(_ptr(flat), _ptr(clip), 2, 2, _ptr(start), _ptr(lefts), _ptr(rights), max_rows)
+    if n <= 0:
+        return int(start[0]), lefts[:0], rights[:0]
+    return int(start[0]), lefts[:n].copy(), rights[:n].copy()

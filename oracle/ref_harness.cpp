@@ -1,0 +1,213 @@
+// Test-infrastructure harness around the UNMODIFIED DFPSR reference library.
+//
+// This file is part of the oracle (test infrastructure only). It is compiled
+// together with the reference's own sources (built out-of-tree by
+// oracle/Makefile.ref into oracle/_ref/) and exposes a small extern "C" surface
+// so that Python tests can drive the reference's public API on seeded inputs:
+//   * model_render / model_renderDepth        (Source/DFPSR/api/modelAPI.h:285-291)
+//   * renderer_create/begin/giveTask/end      (Source/DFPSR/api/rendererAPI.h:56-135, modelAPI.h:299)
+//   * texture_create_RgbaU8(image, levels)    (Source/DFPSR/api/textureAPI.h:450-465)
+//   * rasterizeTriangle row intervals         (Source/DFPSR/implementation/render/ITriangle2D.h:52)
+//   * addPointLight / setDirectedLight / blendLight (Source/SDK/SpriteEngine/lightAPI.h:27-31)
+//   * draw_higher                              (Source/DFPSR/api/drawAPI.h:142-150)
+// Nothing in the product links this file.
+
+#include "DFPSR/includeFramework.h"
+#include "DFPSR/implementation/render/ITriangle2D.h"
+#include "DFPSR/implementation/render/renderCore.h"
+#include "SDK/SpriteEngine/lightAPI.h"
+#include "SDK/SpriteEngine/orthoAPI.h"
+#include <cstring>
+#include <cstdint>
+
+using namespace dsr;
+
+namespace {
+
+Transform3D makeTransform(const float* t) {
+	// t = position(3), xAxis(3), yAxis(3), zAxis(3)
+	return Transform3D(FVector3D(t[0], t[1], t[2]),
+	  FMatrix3x3(FVector3D(t[3], t[4], t[5]), FVector3D(t[6], t[7], t[8]), FVector3D(t[9], t[10], t[11])));
+}
+
+Camera makeCamera(const float* location, int perspective, float slope, int width, int height, float nearClip, float farClip) {
+	if (perspective) {
+		return Camera::createPerspective(makeTransform(location), float(width), float(height), slope, nearClip, farClip);
+	} else {
+		return Camera::createOrthogonal(makeTransform(location), float(width), float(height), slope);
+	}
+}
+
+struct TextureBox { TextureRgbaU8 texture; };
+struct ModelBox { Model model; };
+
+void copyInRgba(const ImageRgbaU8& image, const uint32_t* src, int width, int height) {
+	for (int y = 0; y < height; y++) {
+		uint32_t* row = image_getSafePointer<uint32_t>(image, y).getUnsafe();
+		std::memcpy(row, src + (size_t)y * width, sizeof(uint32_t) * width);
+	}
+}
+void copyOutRgba(const ImageRgbaU8& image, uint32_t* dst, int width, int height) {
+	for (int y = 0; y < height; y++) {
+		const uint32_t* row = image_getSafePointer<uint32_t>(image, y).getUnsafe();
+		std::memcpy(dst + (size_t)y * width, row, sizeof(uint32_t) * width);
+	}
+}
+void copyInF32(const ImageF32& image, const float* src, int width, int height) {
+	for (int y = 0; y < height; y++) {
+		float* row = image_getSafePointer<float>(image, y).getUnsafe();
+		std::memcpy(row, src + (size_t)y * width, sizeof(float) * width);
+	}
+}
+void copyOutF32(const ImageF32& image, float* dst, int width, int height) {
+	for (int y = 0; y < height; y++) {
+		const float* row = image_getSafePointer<float>(image, y).getUnsafe();
+		std::memcpy(dst + (size_t)y * width, row, sizeof(float) * width);
+	}
+}
+
+} // namespace
+
+extern "C" {
+
+// Tells the reference's heap that the process is ending (base/heap.h:161), so that its
+// leak report at exit stays quiet when the harness is unloaded with live allocations.
+void refh_shutdown() { heap_terminatingApplication(); }
+
+// Creates a texture pyramid from a width x height RGBA image (bytes R,G,B,A in memory).
+void* refh_texture_create(const uint32_t* pixels, int width, int height, int resolutions) {
+	OrderedImageRgbaU8 image = image_create_RgbaU8(width, height);
+	copyInRgba(image, pixels, width, height);
+	TextureBox* box = new TextureBox();
+	box->texture = texture_create_RgbaU8(image, resolutions);
+	return box;
+}
+
+// Reads the texture's pyramid buffer and fields.
+// fields = log2width, log2height, maxMipLevel, startOffset, maxLevelMask, minWidthOrMask,
+//          minHeightOrMask, maxWidthAndMask, maxHeightAndMask; returns the pixel count.
+int refh_texture_info(void* handle, uint32_t* fields, uint32_t* pixels, int maxPixels) {
+	TextureRgbaU8& t = ((TextureBox*)handle)->texture;
+	fields[0] = t.impl_log2width; fields[1] = t.impl_log2height; fields[2] = t.impl_maxMipLevel;
+	fields[3] = t.impl_startOffset; fields[4] = t.impl_maxLevelMask; fields[5] = t.impl_minWidthOrMask;
+	fields[6] = t.impl_minHeightOrMask; fields[7] = t.impl_maxWidthAndMask; fields[8] = t.impl_maxHeightAndMask;
+	int count = (int)(t.impl_startOffset + (uint32_t(1) << (t.impl_log2width + t.impl_log2height)));
+	if (pixels) {
+		const uint32_t* data = t.impl_buffer.getSafe<uint32_t>("harness").getUnsafe();
+		std::memcpy(pixels, data, sizeof(uint32_t) * (count < maxPixels ? count : maxPixels));
+	}
+	return count;
+}
+
+void refh_texture_free(void* handle) { delete (TextureBox*)handle; }
+
+// polyIndices: polyCount x 4 (index 3 = -1 for triangles); texCoords, colors: polyCount x 4 x 4 floats.
+void* refh_model_create(const float* positions, int pointCount, const int* polyIndices,
+                        const float* texCoords, const float* colors, int polyCount,
+                        void* diffuse, void* light, int filter) {
+	ModelBox* box = new ModelBox();
+	box->model = model_create();
+	model_setFilter(box->model, filter ? Filter::Alpha : Filter::Solid);
+	int part = model_addEmptyPart(box->model, U"part");
+	if (diffuse) model_setDiffuseMap(box->model, part, ((TextureBox*)diffuse)->texture);
+	if (light) model_setLightMap(box->model, part, ((TextureBox*)light)->texture);
+	for (int p = 0; p < pointCount; p++) {
+		model_addPoint(box->model, FVector3D(positions[p * 3], positions[p * 3 + 1], positions[p * 3 + 2]));
+	}
+	for (int p = 0; p < polyCount; p++) {
+		const int* idx = polyIndices + p * 4;
+		int poly;
+		int corners;
+		if (idx[3] < 0) {
+			poly = model_addTriangle(box->model, part, idx[0], idx[1], idx[2]);
+			corners = 3;
+		} else {
+			poly = model_addQuad(box->model, part, idx[0], idx[1], idx[2], idx[3]);
+			corners = 4;
+		}
+		for (int v = 0; v < corners; v++) {
+			const float* tc = texCoords + (p * 4 + v) * 4;
+			const float* co = colors + (p * 4 + v) * 4;
+			model_setTexCoord(box->model, part, poly, v, FVector4D(tc[0], tc[1], tc[2], tc[3]));
+			model_setVertexColor(box->model, part, poly, v, FVector4D(co[0], co[1], co[2], co[3]));
+		}
+	}
+	return box;
+}
+
+void refh_model_free(void* handle) { delete (ModelBox*)handle; }
+
+// mode 0: model_render (single thread).  mode 1: renderer_begin/giveTask/end (threaded bands).
+// color may be null (depth-only target through model_render), depth may be null.
+// packOrder: PackOrderIndex of the colour target (0 RGBA, 1 BGRA, 2 ARGB, 3 ABGR).
+int refh_model_render(void* modelHandle, const float* modelToWorld, const float* cameraLocation,
+                      int perspective, float slope, float nearClip, float farClip,
+                      int width, int height, uint32_t* color, float* depth, int packOrder, int mode) {
+	Model& model = ((ModelBox*)modelHandle)->model;
+	Transform3D transform = makeTransform(modelToWorld);
+	Camera camera = makeCamera(cameraLocation, perspective, slope, width, height, nearClip, farClip);
+	ImageRgbaU8 colorImage;
+	ImageF32 depthImage;
+	if (color) {
+		colorImage = image_create_RgbaU8_native(width, height, PackOrderIndex(packOrder));
+		copyInRgba(colorImage, color, width, height);
+	}
+	if (depth) {
+		depthImage = image_create_F32(width, height);
+		copyInF32(depthImage, depth, width, height);
+	}
+	if (mode == 0) {
+		model_render(model, transform, colorImage, depthImage, camera);
+	} else {
+		Renderer renderer = renderer_create();
+		renderer_begin(renderer, colorImage, depthImage);
+		renderer_giveTask(renderer, model, transform, camera);
+		renderer_end(renderer);
+	}
+	if (color) copyOutRgba(colorImage, color, width, height);
+	if (depth) copyOutF32(depthImage, depth, width, height);
+	return 0;
+}
+
+int refh_model_render_depth(void* modelHandle, const float* modelToWorld, const float* cameraLocation,
+                            int perspective, float slope, float nearClip, float farClip,
+                            int width, int height, float* depth) {
+	Model& model = ((ModelBox*)modelHandle)->model;
+	Transform3D transform = makeTransform(modelToWorld);
+	Camera camera = makeCamera(cameraLocation, perspective, slope, width, height, nearClip, farClip);
+	ImageF32 depthImage = image_create_F32(width, height);
+	copyInF32(depthImage, depth, width, height);
+	model_renderDepth(model, transform, depthImage, camera);
+	copyOutF32(depthImage, depth, width, height);
+	return 0;
+}
+
+// Projects one camera-space point the way the reference does (Camera::cameraToScreen).
+// out = is.x, is.y ; outFlat = flat.x, flat.y
+void refh_camera_to_screen(const float* cameraLocation, int perspective, float slope, float nearClip, float farClip,
+                           int width, int height, const float* cs, float* outIs, int64_t* outFlat) {
+	Camera camera = makeCamera(cameraLocation, perspective, slope, width, height, nearClip, farClip);
+	ProjectedPoint p = camera.cameraToScreen(FVector3D(cs[0], cs[1], cs[2]));
+	outIs[0] = p.is.x; outIs[1] = p.is.y;
+	outFlat[0] = p.flat.x; outFlat[1] = p.flat.y;
+}
+
+// Row intervals from the reference's own rasterizer for one triangle given its sub-pixel corners.
+// clip = left, top, width, height. Returns the row count (or 0 if outside) and writes startRow.
+int refh_triangle_rows(const int64_t* flat, const int* clip, int alignX, int alignY,
+                       int* startRow, int* lefts, int* rights, int maxRows) {
+	ProjectedPoint a(FVector3D(), FVector2D(), LVector2D(flat[0], flat[1]));
+	ProjectedPoint b(FVector3D(), FVector2D(), LVector2D(flat[2], flat[3]));
+	ProjectedPoint c(FVector3D(), FVector2D(), LVector2D(flat[4], flat[5]));
+	ITriangle2D triangle(a, b, c);
+	IRect clipBound(clip[0], clip[1], clip[2], clip[3]);
+	int rowCount = triangle.getBufferSize(clipBound, alignX, alignY);
+	if (rowCount <= 0 || rowCount > maxRows) return rowCount > maxRows ? -rowCount : 0;
+	RowInterval* rows = new RowInterval[rowCount];
+	triangle.getShape(*startRow, rows, clipBound, alignX, alignY);
+	for (int r = 0; r < rowCount; r++) { lefts[r] = rows[r].left; rights[r] = rows[r].right; }
+	delete[] rows;
+	return rowCount;
+}
+
+} // extern "C"
