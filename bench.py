@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the GB300 DFPSR triangle path.
+
+One step renders one frame of the workload (default: the 1920x1080 terrain, a
+512x512 height grid of 522k triangles with a 1024x1024 mip-mapped texture and
+texture x vertex-colour shading, depth tested) through dsrg_model_render.
+
+  value  fragments/s with the colour and depth targets resident in HBM, CUDA events
+         on the renderer's stream around each frame, L2 flushed before every frame.
+  e2e    the same through the C ABI with page-locked HOST images: each frame copies
+         the targets to the GPU and back inside the timed region.
+
+`python bench.py --impl reference` times the reference's CPU renderer on this
+host's cores instead (the reference built from source where available, otherwise
+the oracle's C restatement of it).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mfrag/s & frames/s plain vs batched; fwd+bwd views/s at grad rel err ≤1e-3"
+BYTES_PER_FRAGMENT = 28  # depth read + depth write + colour write + 4 bilinear RGBA8 texels
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["terrain", "random"], default="terrain")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
+    return p.parse_args()
+
+
+def workload(name):
+    from dfpsr_gb300 import scenes
+    if name == "terrain":
+        s = scenes.terrain(seed=1234)
+        cfg = {"workload": "terrain 1920x1080, 512x512 height grid (522,242 triangles), 1024x1024 RGBA8 texture with mips, "
+                           "texture x vertex colour, depth tested", "width": 1920, "height": 1080,
+               "triangles": s.triangle_count, "seed": 1234}
+    else:
+        s = scenes.random_triangles(seed=1234)
+        cfg = {"workload": "800x600, 20,000 random triangles, 256x256 RGBA8 texture with mips, vertex colour x texture, "
+                           "depth tested", "width": 800, "height": 600, "triangles": s.triangle_count, "seed": 1234}
+    return s, cfg
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.file:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, seconds: float):
+    """The oracle's C restatement of the reference renderer on all host cores (band split like
+    renderer_end, CommandQueue::execute with 12 bands), over a bounded number of frames."""
+    from oracle import port
+    threads = os.cpu_count() or 1
+    pm = port.PreparedModel(scene)
+    _, _, info = port.render(scene, bands=12, threads=threads, prepared=pm)
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        port.render(scene, bands=12, threads=threads, prepared=pm)
+        frames += 1
+        if time.perf_counter() - t0 > seconds or frames >= 50:
+            break
+    dt = (time.perf_counter() - t0) / frames
+    return {"value": info["fragments"] / dt / 1e6, "unit": "Mfrag/s", "cores": min(threads, 12), "kind": "port",
+            "sample": f"{frames} frame(s) of the same workload, oracle C port, 12 row bands on {min(threads, 12)} threads",
+            "frames_per_s": 1.0 / dt}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene, cfg = workload(args.workload)
+    from oracle import port, ref
+    threads = os.cpu_count() or 1
+    use_ref = ref.available("shipped")
+    if use_ref:
+        model = ref.RefModel(scene, "shipped")
+        frame = lambda: model.render(threaded=True)
+        kind, sample = "reference", "reference renderer_begin/giveTask/end (as shipped, -O2 -march=native), threaded bands"
+    else:
+        pm = port.PreparedModel(scene)
+        frame = lambda: port.render(scene, bands=12, threads=threads, prepared=pm)
+        kind, sample = "port", "oracle C port of the reference renderer, 12 row bands"
+    _, _, info = port.render(scene)
+    fragments = info["fragments"]
+    for _ in range(max(1, min(args.warmup, 2))):
+        frame()
+    times = []
+    budget = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        frame()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - budget > 120:
+            break
+    dt = sum(times) / len(times)
+    value = fragments / dt / 1e6
+    cores = min(threads - 1 if use_ref else threads, 12) or 1
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mfrag/s", "n_gpus": args.gpus,
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64", "data": "synthetic (seeded)", "config": cfg,
+            "frames_per_s": 1.0 / dt,
+            "cpu_baseline": {"value": value, "unit": "Mfrag/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "Mfrag/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    sys.stderr.flush()
+    # The reference library's own heap bookkeeping reports spuriously when Python tears it down.
+    os._exit(0)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import dfpsr_gb300 as d
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    scene, cfg = workload(args.workload)
+    h, w = scene.height, scene.width
+    ctx = d.Context(local)
+    model = d.Model(ctx, scene)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    color = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    depth = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB of L2
+
+    # fragments per frame: deterministic, counted once by the kernels themselves
+    ctx.set_counting(True)
+    ctx.render(model, model.camera, color, depth)
+    fragments = ctx.stats()["fragments"]
+    ctx.set_counting(False)
+
+    def frame_device():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            color.zero_()
+            depth.zero_()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        ctx.render(model, model.camera, color, depth)
+        stop.record(stream)
+        return start, stop
+
+    for _ in range(args.warmup):
+        frame_device()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.stats()["kernel_launches"]
+    events, raster_ms = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            events.append(frame_device())
+            raster_ms.append(ctx.stats()["raster_milliseconds"])
+        torch.cuda.synchronize()
+    launches = ctx.stats()["kernel_launches"] - launches0
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        if dist:
+            dist.barrier()
+
+    # end to end through the C ABI with page-locked host images
+    host_color = torch.zeros((h, w), dtype=torch.int32).pin_memory().numpy()
+    host_depth = torch.zeros((h, w), dtype=torch.float32).pin_memory().numpy()
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.render(model, model.camera, host_color, host_depth)
+    e2e_times = []
+    for _ in range(args.steps):
+        host_color.fill(0)
+        host_depth.fill(0.0)
+        t0 = time.perf_counter()
+        ctx.render(model, model.camera, host_color, host_depth)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank == 0:
+        peaks, peak_kind = measured_peaks()
+        raster_avg_s = (sum(raster_ms) / len(raster_ms)) / 1e3
+        achieved = BYTES_PER_FRAGMENT * fragments / raster_avg_s / 1e9
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        traffic = None
+        try:
+            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+                traffic = json.load(f).get(args.workload)
+        except Exception:
+            pass
+        value = world * fragments * args.steps / total_s / 1e6
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mfrag/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64", "data": "synthetic (seeded)",
+            "config": dict(cfg, l2="flushed before every frame (256 MB write)", parallelism="replicas" if world > 1 else "single GPU"),
+            "frames_per_s": world * args.steps / total_s,
+            "fragments_per_frame": fragments,
+            "e2e": {"value": world * fragments * args.steps / e2e_s / 1e6, "unit": "Mfrag/s",
+                    "h2d_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
+                    "d2h_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
+                    "frames_per_s": world * args.steps / e2e_s},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": traffic, "kernel": "raster_kernel",
+                         "kernel_ms": raster_avg_s * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+        }
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,295 @@
+"""GB300 (sm_103a) implementation of DFPSR's triangle-rendering path.
+
+The product is the in-tree CUDA library libdsrg.so behind the C ABI in
+include/dsrg.h.  This module is a thin ctypes front end over that ABI for Python
+callers (tests, benchmarks, the gradient harness).  There is no fallback: if the
+library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdsrg.so")
+
+DSRG_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "CALL_ORDER", 5: "UNSUPPORTED", 6: "DEVICE"}
+
+# Every entry point declared in include/dsrg.h.
+EXPORTED = [
+    "dsrg_context_create", "dsrg_context_destroy", "dsrg_context_last_error", "dsrg_context_stream",
+    "dsrg_context_set_counting", "dsrg_context_get_stats",
+    "dsrg_texture_create", "dsrg_texture_destroy", "dsrg_texture_read",
+    "dsrg_model_create", "dsrg_model_destroy",
+    "dsrg_model_render", "dsrg_model_render_depth",
+    "dsrg_renderer_create", "dsrg_renderer_destroy", "dsrg_renderer_begin", "dsrg_renderer_give_task",
+    "dsrg_renderer_end", "dsrg_renderer_takes_triangles",
+]
+
+
+class DsrgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Camera(C.Structure):
+    _fields_ = [("location", C.c_float * 12), ("perspective", C.c_int32), ("slope", C.c_float),
+                ("nearClip", C.c_float), ("farClip", C.c_float), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("strideBytes", C.c_int32),
+                ("packOrder", C.c_int32), ("onDevice", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("fragments", C.c_uint64), ("drawRecords", C.c_uint64), ("binEntries", C.c_uint64),
+                ("milliseconds", C.c_float), ("rasterMilliseconds", C.c_float), ("kernelLaunches", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libdsrg.so (built by __graft_entry__.build() or dfpsr_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        l = C.CDLL(LIB_PATH)
+        P, I = C.c_void_p, C.c_int32
+        l.dsrg_context_create.argtypes = [I, C.POINTER(P)]
+        l.dsrg_context_destroy.argtypes = [P]
+        l.dsrg_context_last_error.argtypes = [P]
+        l.dsrg_context_last_error.restype = C.c_char_p
+        l.dsrg_context_stream.argtypes = [P]
+        l.dsrg_context_stream.restype = P
+        l.dsrg_context_set_counting.argtypes = [P, I, P]
+        l.dsrg_context_get_stats.argtypes = [P, C.POINTER(Stats)]
+        l.dsrg_texture_create.argtypes = [P, P, I, I, I, C.POINTER(P)]
+        l.dsrg_texture_destroy.argtypes = [P]
+        l.dsrg_texture_read.argtypes = [P, P, I, P, C.POINTER(I)]
+        l.dsrg_model_create.argtypes = [P, P, I, P, P, P, I, P, P, I, C.POINTER(P)]
+        l.dsrg_model_destroy.argtypes = [P]
+        l.dsrg_model_render.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image), C.POINTER(Image)]
+        l.dsrg_model_render_depth.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
+        l.dsrg_renderer_create.argtypes = [P, C.POINTER(P)]
+        l.dsrg_renderer_destroy.argtypes = [P]
+        l.dsrg_renderer_begin.argtypes = [P, C.POINTER(Image), C.POINTER(Image)]
+        l.dsrg_renderer_give_task.argtypes = [P, P, P, C.POINTER(Camera)]
+        l.dsrg_renderer_end.argtypes = [P]
+        l.dsrg_renderer_takes_triangles.argtypes = [P]
+        _lib = l
+    return _lib
+
+
+def _ptr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())  # torch tensor
+
+
+def camera_struct(scene) -> Camera:
+    c = Camera()
+    for i in range(12):
+        c.location[i] = float(scene.camera_location[i])
+    c.perspective = 1 if scene.perspective else 0
+    c.slope = scene.slope
+    c.nearClip = scene.near_clip
+    c.farClip = scene.far_clip
+    c.width = scene.width
+    c.height = scene.height
+    return c
+
+
+def image_struct(array, pack_order: int = 0) -> Optional[Image]:
+    """A dsrg_image over a 2-D numpy array (host) or torch CUDA tensor (device) of 4-byte pixels."""
+    if array is None:
+        return None
+    img = Image()
+    if isinstance(array, np.ndarray):
+        assert array.dtype.itemsize == 4 and array.ndim == 2 and array.strides[1] == 4
+        img.data = array.ctypes.data
+        img.height, img.width = array.shape
+        img.strideBytes = array.strides[0]
+        img.onDevice = 0
+    else:
+        assert array.element_size() == 4 and array.dim() == 2 and array.stride(1) == 1 and array.is_cuda
+        img.data = array.data_ptr()
+        img.height, img.width = array.shape
+        img.strideBytes = array.stride(0) * 4
+        img.onDevice = 1
+    img.packOrder = pack_order
+    return img
+
+
+class Context:
+    """A dsrg_context on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._l = lib()
+        h = C.c_void_p()
+        self._check(self._l.dsrg_context_create(device, C.byref(h)), None)
+        self.handle = h
+
+    def _check(self, status: int, handle=None):
+        if status != DSRG_OK:
+            msg = self._l.dsrg_context_last_error(handle if handle is not None else getattr(self, "handle", None))
+            raise DsrgError(status, (msg or b"").decode())
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._l.dsrg_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self._l.dsrg_context_stream(self.handle) or 0)
+
+    def texture(self, pixels: np.ndarray, resolutions: int = 16) -> "Texture":
+        return Texture(self, pixels, resolutions)
+
+    def model(self, scene, diffuse: Optional["Texture"] = None, light: Optional["Texture"] = None) -> "Model":
+        return Model(self, scene, diffuse, light)
+
+    def set_counting(self, on: bool, coverage=None):
+        self._check(self._l.dsrg_context_set_counting(self.handle, 1 if on else 0, _ptr(coverage)))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self._l.dsrg_context_get_stats(self.handle, C.byref(s)))
+        return {"fragments": int(s.fragments), "draw_records": int(s.drawRecords), "bin_entries": int(s.binEntries),
+                "milliseconds": float(s.milliseconds), "raster_milliseconds": float(s.rasterMilliseconds),
+                "kernel_launches": int(s.kernelLaunches)}
+
+    def render(self, model: "Model", camera: Camera, color=None, depth=None, transform=None, pack_order: int = 0):
+        """dsrg_model_render into the given host (numpy) or device (torch) images, in place."""
+        t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
+        ci, di = image_struct(color, pack_order), image_struct(depth)
+        self._check(self._l.dsrg_model_render(self.handle, model.handle, t.ctypes.data, C.byref(camera),
+                                              C.byref(ci) if ci else None, C.byref(di) if di else None))
+
+    def render_depth(self, model: "Model", camera: Camera, depth, transform=None):
+        t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
+        di = image_struct(depth)
+        self._check(self._l.dsrg_model_render_depth(self.handle, model.handle, t.ctypes.data, C.byref(camera), C.byref(di)))
+
+    def renderer(self) -> "Renderer":
+        return Renderer(self)
+
+
+class Texture:
+    def __init__(self, ctx: Context, pixels: np.ndarray, resolutions: int = 16):
+        self.ctx = ctx
+        pixels = np.ascontiguousarray(pixels, np.uint32)
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_texture_create(ctx.handle, pixels.ctypes.data, pixels.shape[1], pixels.shape[0],
+                                              resolutions, C.byref(h)))
+        self.handle = h
+
+    def read(self):
+        fields = np.zeros(9, np.uint32)
+        count = C.c_int32()
+        self.ctx._check(self.ctx._l.dsrg_texture_read(self.handle, None, 0, fields.ctypes.data, C.byref(count)))
+        pixels = np.zeros(count.value, np.uint32)
+        self.ctx._check(self.ctx._l.dsrg_texture_read(self.handle, pixels.ctypes.data, count.value, None, None))
+        return fields, pixels
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.ctx._l.dsrg_texture_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+class Model:
+    def __init__(self, ctx: Context, scene, diffuse: Optional[Texture] = None, light: Optional[Texture] = None):
+        self.ctx = ctx
+        self.scene = scene
+        if diffuse is None and scene.diffuse is not None:
+            diffuse = Texture(ctx, scene.diffuse, scene.diffuse_levels)
+        if light is None and scene.light is not None:
+            light = Texture(ctx, scene.light, scene.light_levels)
+        self.diffuse, self.light = diffuse, light
+        pos = np.ascontiguousarray(scene.positions, np.float32)
+        poly = np.ascontiguousarray(scene.poly_indices, np.int32)
+        tex = np.ascontiguousarray(scene.tex_coords, np.float32)
+        col = np.ascontiguousarray(scene.colors, np.float32)
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_model_create(ctx.handle, pos.ctypes.data, pos.shape[0], poly.ctypes.data, tex.ctypes.data,
+                                            col.ctypes.data, poly.shape[0], diffuse.handle if diffuse else None,
+                                            light.handle if light else None, scene.filter, C.byref(h)))
+        self.handle = h
+        self.transform = np.ascontiguousarray(scene.model_to_world, np.float32)
+        self.camera = camera_struct(scene)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.ctx._l.dsrg_model_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+class Renderer:
+    """dsrg_renderer: renderer_begin / renderer_giveTask / renderer_end."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_renderer_create(ctx.handle, C.byref(h)))
+        self.handle = h
+        self._images = None
+
+    def begin(self, color=None, depth=None, pack_order: int = 0):
+        ci, di = image_struct(color, pack_order), image_struct(depth)
+        self._images = (color, depth, ci, di)
+        self.ctx._check(self.ctx._l.dsrg_renderer_begin(self.handle, C.byref(ci) if ci else None, C.byref(di) if di else None))
+
+    def give_task(self, model: Model, camera: Optional[Camera] = None, transform=None):
+        t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
+        cam = model.camera if camera is None else camera
+        self.ctx._check(self.ctx._l.dsrg_renderer_give_task(self.handle, model.handle, t.ctypes.data, C.byref(cam)))
+
+    def end(self):
+        self.ctx._check(self.ctx._l.dsrg_renderer_end(self.handle))
+        self._images = None
+
+    @property
+    def takes_triangles(self) -> bool:
+        return bool(self.ctx._l.dsrg_renderer_takes_triangles(self.handle))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.ctx._l.dsrg_renderer_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+def render_scene(ctx: Context, scene, color: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None, *,
+                 use_color: bool = True, use_depth: bool = True, pack_order: int = 0, model: Optional[Model] = None):
+    """Renders a scene into fresh (or given) host images through dsrg_model_render; returns (color, depth)."""
+    m = model or Model(ctx, scene)
+    h, w = scene.height, scene.width
+    c = (np.zeros((h, w), np.uint32) if color is None else np.array(color, np.uint32)) if use_color else None
+    d = (np.zeros((h, w), np.float32) if depth is None else np.array(depth, np.float32)) if use_depth else None
+    ctx.render(m, m.camera, c, d, pack_order=pack_order)
+    return c, d

@@ -1,0 +1,83 @@
+"""Builds the in-tree CUDA library of the DFPSR triangle path (libdsrg.so) for sm_103a.
+
+Device code is compiled with -fmad=false and host code with -ffp-contract=off: the
+renderer's results are defined by binary32 operations in a fixed order, and a fused
+multiply-add anywhere would change them.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libdsrg.so")
+SOURCES = ["dsrg_kernels.cu", "dsrg_api.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+              "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-Xptxas", "-O3"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def headers():
+    out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    out.append(os.path.join(os.path.dirname(HERE), "include", "dsrg.h"))
+    return out
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    hdrs = headers()
+    objs = []
+    jobs = []
+    for src in SOURCES:
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(obj)
+        if force or _stale(obj, [path] + hdrs):
+            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, "-c", path, "-o", obj])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        subprocess.check_call(cmd)
+
+    with ThreadPoolExecutor(max_workers=len(jobs) or 1) as pool:
+        for f in [pool.submit(run, j) for j in jobs]:
+            f.result()
+    if force or jobs or _stale(LIB, objs):
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"])
+    return LIB
+
+
+HOSTCHECK_LIB = os.path.join(HERE, "libdsrg_hostcheck.so")
+
+
+def build_hostcheck(force: bool = False) -> str:
+    """Host build of the kernels' exact arithmetic, for CPU-side checks."""
+    src = os.path.join(CSRC, "dsrg_hostcheck.cpp")
+    if force or _stale(HOSTCHECK_LIB, [src] + headers()):
+        cxx = os.environ.get("CXX", "g++")
+        subprocess.check_call([cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", HOSTCHECK_LIB])
+    return HOSTCHECK_LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    build_hostcheck(force="--force" in sys.argv)

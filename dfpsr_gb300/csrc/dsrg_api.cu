@@ -1,0 +1,715 @@
+// Host side of the dsrg C ABI: contexts, textures, models and the renderer state machine
+// around the kernels in dsrg_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/dsrg.h"
+#include "dsrg_geometry.h"
+#include "dsrg_kernels.h"
+
+using namespace dsrg;
+
+namespace {
+
+template <typename T>
+struct DeviceBuffer {
+	T *ptr = nullptr;
+	size_t capacity = 0;
+	cudaError_t reserve(size_t n, bool keep = false, size_t keepCount = 0, cudaStream_t stream = 0) {
+		if (n <= capacity) return cudaSuccess;
+		size_t newCapacity = capacity ? capacity : 1024;
+		while (newCapacity < n) newCapacity *= 2;
+		T *fresh = nullptr;
+		cudaError_t err = cudaMalloc((void **)&fresh, newCapacity * sizeof(T));
+		if (err != cudaSuccess) return err;
+		if (keep && ptr && keepCount) {
+			err = cudaMemcpyAsync(fresh, ptr, keepCount * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+			if (err != cudaSuccess) { cudaFree(fresh); return err; }
+			cudaStreamSynchronize(stream);
+		}
+		if (ptr) cudaFree(ptr);
+		ptr = fresh;
+		capacity = newCapacity;
+		return cudaSuccess;
+	}
+	void release() {
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		capacity = 0;
+	}
+};
+
+// Camera::createPerspective / createOrthogonal and ViewFrustum (implementation/render/Camera.h:55-156),
+// computed on the host in the reference's order (this file is built with -ffp-contract=off).
+Plane make_plane(float x, float y, float z, float offset) {
+	Plane p;
+	float l = sqrtf(x * x + y * y + z * z);
+	if (l == 0.0f) { p.nx = 0.0f; p.ny = 0.0f; p.nz = 1.0f; }
+	else { p.nx = x / l; p.ny = y / l; p.nz = z / l; }
+	p.offset = offset;
+	return p;
+}
+
+int frustum_perspective(Plane *planes, float nearClip, float farClip, float ws, float hs) {
+	planes[0] = make_plane(-1.0f, 0.0f, -ws, 0.0f);
+	planes[1] = make_plane(1.0f, 0.0f, -ws, 0.0f);
+	planes[2] = make_plane(0.0f, 1.0f, -hs, 0.0f);
+	planes[3] = make_plane(0.0f, -1.0f, -hs, 0.0f);
+	planes[4] = make_plane(0.0f, 0.0f, -1.0f, -nearClip);
+	planes[5] = make_plane(0.0f, 0.0f, 1.0f, farClip);
+	return std::isinf(farClip) && farClip > 0 ? 5 : 6;
+}
+
+int frustum_orthogonal(Plane *planes, float hw, float hh) {
+	planes[0] = make_plane(-1.0f, 0.0f, 0.0f, hw);
+	planes[1] = make_plane(1.0f, 0.0f, 0.0f, hw);
+	planes[2] = make_plane(0.0f, 1.0f, 0.0f, hh);
+	planes[3] = make_plane(0.0f, -1.0f, 0.0f, hh);
+	return 4;
+}
+
+CameraData make_camera(const dsrg_camera &d) {
+	CameraData c;
+	memset(&c, 0, sizeof(c));
+	for (int i = 0; i < 3; i++) {
+		c.position[i] = d.location[i];
+		c.xAxis[i] = d.location[3 + i];
+		c.yAxis[i] = d.location[6 + i];
+		c.zAxis[i] = d.location[9 + i];
+	}
+	c.imageWidth = (float)d.width;
+	c.imageHeight = (float)d.height;
+	c.perspective = d.perspective ? 1 : 0;
+	float ws = d.slope;
+	float hs = ws * c.imageHeight / c.imageWidth;
+	if (d.perspective) {
+		c.cullCount = frustum_perspective(c.cull, d.nearClip, d.farClip, ws * 1.0001f, hs * 1.0001f);
+		c.clipCount = frustum_perspective(c.clip, d.nearClip, d.farClip, ws * 2.0f, hs * 2.0f);
+	} else {
+		c.cullCount = frustum_orthogonal(c.cull, ws * 1.0001f, hs * 1.0001f);
+		c.clipCount = frustum_orthogonal(c.clip, ws * 2.0f, hs * 2.0f);
+	}
+	c.invWidthSlope = 0.5f / ws;
+	c.invHeightSlope = 0.5f / hs;
+	return c;
+}
+
+// Camera::isBoxSeen (implementation/render/Camera.h:202-217).
+bool box_seen(const CameraData &c, const float *mn, const float *mx, const float *modelToWorld) {
+	const float corners[8][3] = {{mn[0], mn[1], mn[2]}, {mx[0], mn[1], mn[2]}, {mn[0], mx[1], mn[2]}, {mx[0], mx[1], mn[2]},
+	                             {mn[0], mn[1], mx[2]}, {mx[0], mn[1], mx[2]}, {mn[0], mx[1], mx[2]}, {mx[0], mx[1], mx[2]}};
+	Vec3 cs[8];
+	for (int i = 0; i < 8; i++) cs[i] = world_to_camera(c, transform_point(modelToWorld, vec3(corners[i][0], corners[i][1], corners[i][2])));
+	for (int s = 0; s < c.cullCount; s++) {
+		bool anyInside = false;
+		for (int i = 0; i < 8; i++) if (plane_inside(c.cull[s], cs[i])) anyInside = true;
+		if (!anyInside) return false;
+	}
+	return true;
+}
+
+} // namespace
+
+struct dsrg_context_s {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	std::string lastError;
+	// frame scratch, grown on demand and reused
+	DeviceBuffer<float> csx, csy, csz, isx, isy;
+	DeviceBuffer<int64_t> flatx, flaty;
+	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
+	DeviceBuffer<DrawRecord> records;
+	DeviceBuffer<ShadeRecord> shades;
+	DeviceBuffer<uint32_t> control;      // [0] record count, [1] error flag
+	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
+	DeviceBuffer<TextureData> textureTable;
+	DeviceBuffer<uint32_t> stagingColor;
+	DeviceBuffer<float> stagingDepth;
+	DeviceBuffer<unsigned long long> fragmentCounter;
+	int32_t counting = 0;
+	uint32_t *coverage = nullptr;
+	dsrg_stats stats;
+	cudaEvent_t eventStart = nullptr, eventStop = nullptr, eventRasterStart = nullptr, eventRasterStop = nullptr;
+	dsrg_renderer implicitRenderer = nullptr;
+};
+
+struct dsrg_texture_s {
+	dsrg_context context;
+	uint32_t *pixels = nullptr;
+	uint32_t fields[9];
+	uint32_t pixelCount = 0;
+	TextureData data;
+};
+
+struct dsrg_model_s {
+	dsrg_context context;
+	float *positions = nullptr;
+	int32_t *polygons = nullptr;
+	float *texCoords = nullptr;
+	float *colors = nullptr;
+	int32_t *triSource = nullptr;
+	int32_t pointCount = 0, polygonCount = 0, triangleCount = 0;
+	float minBound[3], maxBound[3];
+	dsrg_texture diffuse = nullptr, light = nullptr;
+	int32_t filter = 0;
+};
+
+struct dsrg_renderer_s {
+	dsrg_context context;
+	bool receiving = false;
+	dsrg_image color, depth;
+	bool hasColor = false, hasDepth = false;
+	int32_t width = 0, height = 0;
+	uint32_t *deviceColor = nullptr;
+	float *deviceDepth = nullptr;
+	int32_t colorStride = 0, depthStride = 0;
+	uint32_t triangleCount = 0;   // fan triangles submitted this frame
+	uint32_t recordCapacity = 0;
+	bool depthOnly = false;
+	bool affine = false;
+	bool cameraKnown = false;
+	std::vector<TextureData> textures;
+	std::vector<dsrg_texture> textureHandles;
+};
+
+#define CUDA_TRY(ctx, expr)                                                                      \
+	do {                                                                                         \
+		cudaError_t _e = (expr);                                                                 \
+		if (_e != cudaSuccess) {                                                                 \
+			(ctx)->lastError = std::string("CUDA error in " #expr ": ") + cudaGetErrorString(_e); \
+			return _e == cudaErrorMemoryAllocation ? DSRG_ERROR_OUT_OF_MEMORY : DSRG_ERROR_CUDA; \
+		}                                                                                        \
+	} while (0)
+
+static int fail(dsrg_context ctx, int code, const std::string &message) {
+	if (ctx) ctx->lastError = message;
+	return code;
+}
+
+extern "C" {
+
+int dsrg_context_create(int32_t device, dsrg_context *out) {
+	if (!out) return DSRG_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) return DSRG_ERROR_CUDA;
+	if (cudaSetDevice(device) != cudaSuccess) return DSRG_ERROR_CUDA;
+	dsrg_context ctx = new (std::nothrow) dsrg_context_s();
+	if (!ctx) return DSRG_ERROR_OUT_OF_MEMORY;
+	ctx->device = device;
+	memset(&ctx->stats, 0, sizeof(ctx->stats));
+	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
+	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
+	    ctx->control.reserve(4) != cudaSuccess || ctx->fragmentCounter.reserve(1) != cudaSuccess) {
+		delete ctx;
+		return DSRG_ERROR_CUDA;
+	}
+	cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream);
+	*out = ctx;
+	return DSRG_OK;
+}
+
+int dsrg_renderer_destroy(dsrg_renderer renderer);
+
+int dsrg_context_destroy(dsrg_context ctx) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	if (ctx->implicitRenderer) dsrg_renderer_destroy(ctx->implicitRenderer);
+	DeviceBuffer<float> *fbufs[] = {&ctx->csx, &ctx->csy, &ctx->csz, &ctx->isx, &ctx->isy, &ctx->stagingDepth};
+	for (auto *b : fbufs) b->release();
+	ctx->flatx.release(); ctx->flaty.release();
+	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
+	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
+	for (auto *b : ubufs) b->release();
+	ctx->records.release(); ctx->shades.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
+	cudaEventDestroy(ctx->eventStart);
+	cudaEventDestroy(ctx->eventStop);
+	cudaEventDestroy(ctx->eventRasterStart);
+	cudaEventDestroy(ctx->eventRasterStop);
+	cudaStreamDestroy(ctx->stream);
+	delete ctx;
+	return DSRG_OK;
+}
+
+const char *dsrg_context_last_error(dsrg_context ctx) { return ctx ? ctx->lastError.c_str() : "null context"; }
+
+void *dsrg_context_stream(dsrg_context ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int dsrg_context_set_counting(dsrg_context ctx, int32_t counting, uint32_t *deviceCoverage) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	ctx->counting = counting;
+	ctx->coverage = counting ? deviceCoverage : nullptr;
+	return DSRG_OK;
+}
+
+int dsrg_context_get_stats(dsrg_context ctx, dsrg_stats *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	*out = ctx->stats;
+	return DSRG_OK;
+}
+
+// ------------------------------------------------------------------ textures
+
+int dsrg_texture_create(dsrg_context ctx, const uint32_t *pixels, int32_t width, int32_t height, int32_t resolutions,
+                        dsrg_texture *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	if (resolutions < 1) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture without any resolutions stored, which would be empty!");
+	if (width < 1 || height < 1 || !pixels) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture of an empty image!");
+	if (width > 32768 || height > 32768) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture exceeding the maximum texture dimensions of 32768 x 32768 pixels!");
+	uint32_t lw = 0, lh = 0;
+	while ((1u << lw) < (uint32_t)width) lw++;
+	while ((1u << lh) < (uint32_t)height) lh++;
+	if ((1u << lw) != (uint32_t)width || (1u << lh) != (uint32_t)height)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "Texture dimensions must be powers of two (other sizes are resampled by filter_resize, which is not part of the GPU path)");
+	// Texture constructor (implementation/image/Texture.h:66-101)
+	uint32_t maxMip = (uint32_t)(resolutions - 1);
+	if (maxMip > lw) maxMip = lw;
+	if (maxMip > lh) maxMip = lh;
+	if (maxMip > 15u) maxMip = 15u;
+	uint32_t highest = 1u << (lw + lh);
+	uint64_t pixelCount = 0;
+	uint32_t levelCount = highest;
+	for (int32_t level = (int32_t)maxMip; level >= 0; level--) { pixelCount |= levelCount; levelCount >>= 2; }
+	dsrg_texture tex = new (std::nothrow) dsrg_texture_s();
+	if (!tex) return DSRG_ERROR_OUT_OF_MEMORY;
+	tex->context = ctx;
+	tex->pixelCount = (uint32_t)pixelCount;
+	uint32_t startOffset = (uint32_t)pixelCount & ~highest;
+	uint32_t f[9] = {lw, lh, maxMip, startOffset, highest - 1, (1u << (lw - maxMip)) - 1, (1u << (lh - maxMip)) - 1,
+	                 (1u << lw) - 1, (1u << lh) - 1};
+	memcpy(tex->fields, f, sizeof(f));
+	// texture_generatePyramid: integer 2x2 box average level by level (api/textureAPI.cpp:44-87)
+	std::vector<uint32_t> pyramid(pixelCount, 0u);
+	memcpy(pyramid.data() + startOffset, pixels, sizeof(uint32_t) * (size_t)width * height);
+	auto layer = [&](uint32_t mip) { return startOffset & ((highest - 1) >> (mip << 1)); };
+	for (uint32_t level = 1; level <= maxMip; level++) {
+		uint32_t w = 1u << (lw - level), h = 1u << (lh - level);
+		uint32_t sw = w * 2;
+		const uint32_t *src = pyramid.data() + layer(level - 1);
+		uint32_t *dst = pyramid.data() + layer(level);
+		for (uint32_t y = 0; y < h; y++) {
+			for (uint32_t x = 0; x < w; x++) {
+				uint32_t c[4] = {src[(y * 2) * sw + x * 2], src[(y * 2) * sw + x * 2 + 1], src[(y * 2 + 1) * sw + x * 2],
+				                 src[(y * 2 + 1) * sw + x * 2 + 1]};
+				uint32_t o = 0;
+				for (int ch = 0; ch < 4; ch++) {
+					uint32_t s = 0;
+					for (int i = 0; i < 4; i++) s += (c[i] >> (ch * 8)) & 0xFFu;
+					o |= (s / 4) << (ch * 8);
+				}
+				dst[y * w + x] = o;
+			}
+		}
+	}
+	cudaSetDevice(ctx->device);
+	if (cudaMalloc((void **)&tex->pixels, sizeof(uint32_t) * pixelCount) != cudaSuccess) {
+		delete tex;
+		return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "cudaMalloc failed for a texture pyramid");
+	}
+	if (cudaMemcpy(tex->pixels, pyramid.data(), sizeof(uint32_t) * pixelCount, cudaMemcpyHostToDevice) != cudaSuccess) {
+		cudaFree(tex->pixels);
+		delete tex;
+		return fail(ctx, DSRG_ERROR_CUDA, "cudaMemcpy failed for a texture pyramid");
+	}
+	TextureData &d = tex->data;
+	d.pixels = tex->pixels;
+	d.log2width = lw; d.log2height = lh; d.maxMipLevel = maxMip; d.startOffset = startOffset; d.maxLevelMask = highest - 1;
+	d.maxWidthAndMask = (1u << lw) - 1; d.maxHeightAndMask = (1u << lh) - 1;
+	d.floatMaxWidth = (float)(1u << lw); d.floatMaxHeight = (float)(1u << lh);
+	d.exists = 1;
+	*out = tex;
+	return DSRG_OK;
+}
+
+int dsrg_texture_destroy(dsrg_texture tex) {
+	if (!tex) return DSRG_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(tex->context->device);
+	cudaStreamSynchronize(tex->context->stream);
+	cudaFree(tex->pixels);
+	delete tex;
+	return DSRG_OK;
+}
+
+int dsrg_texture_read(dsrg_texture tex, uint32_t *pixels, int32_t maxPixels, uint32_t *fields, int32_t *count) {
+	if (!tex) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (fields) memcpy(fields, tex->fields, sizeof(tex->fields));
+	if (count) *count = (int32_t)tex->pixelCount;
+	if (pixels && maxPixels > 0) {
+		size_t n = (size_t)maxPixels < tex->pixelCount ? (size_t)maxPixels : tex->pixelCount;
+		CUDA_TRY(tex->context, cudaMemcpy(pixels, tex->pixels, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+	}
+	return DSRG_OK;
+}
+
+// ------------------------------------------------------------------ models
+
+int dsrg_model_create(dsrg_context ctx, const float *positions, int32_t pointCount, const int32_t *polygonIndices,
+                      const float *texCoords, const float *colors, int32_t polygonCount, dsrg_texture diffuse,
+                      dsrg_texture light, int32_t filter, dsrg_model *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	if (pointCount < 0 || polygonCount < 0 || (pointCount > 0 && !positions) ||
+	    (polygonCount > 0 && (!polygonIndices || !texCoords || !colors)))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_create: missing arrays");
+	if (filter != DSRG_FILTER_SOLID && filter != DSRG_FILTER_ALPHA)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_create: unknown filter");
+	std::vector<int32_t> triSource;
+	triSource.reserve((size_t)polygonCount * 2);
+	for (int32_t p = 0; p < polygonCount; p++) {
+		const int32_t *idx = polygonIndices + p * 4;
+		int corners = idx[3] < 0 ? 3 : 4;
+		for (int i = 0; i < corners; i++)
+			if (idx[i] < 0 || idx[i] >= pointCount)
+				return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_create: polygon point index out of range");
+		triSource.push_back(p * 2);
+		if (corners == 4) triSource.push_back(p * 2 + 1);
+	}
+	dsrg_model m = new (std::nothrow) dsrg_model_s();
+	if (!m) return DSRG_ERROR_OUT_OF_MEMORY;
+	m->context = ctx;
+	m->pointCount = pointCount;
+	m->polygonCount = polygonCount;
+	m->triangleCount = (int32_t)triSource.size();
+	m->diffuse = diffuse;
+	m->light = light;
+	m->filter = filter;
+	// ModelImpl::expandBound starting from a zero bound (model/Model.cpp:281-288)
+	for (int i = 0; i < 3; i++) { m->minBound[i] = 0.0f; m->maxBound[i] = 0.0f; }
+	for (int32_t i = 0; i < pointCount; i++) {
+		for (int a = 0; a < 3; a++) {
+			float v = positions[i * 3 + a];
+			if (m->minBound[a] > v) m->minBound[a] = v;
+			if (m->maxBound[a] < v) m->maxBound[a] = v;
+		}
+	}
+	cudaSetDevice(ctx->device);
+	size_t np = (size_t)(pointCount > 0 ? pointCount : 1), ng = (size_t)(polygonCount > 0 ? polygonCount : 1);
+	bool ok = cudaMalloc((void **)&m->positions, np * 3 * sizeof(float)) == cudaSuccess &&
+	          cudaMalloc((void **)&m->polygons, ng * 4 * sizeof(int32_t)) == cudaSuccess &&
+	          cudaMalloc((void **)&m->texCoords, ng * 16 * sizeof(float)) == cudaSuccess &&
+	          cudaMalloc((void **)&m->colors, ng * 16 * sizeof(float)) == cudaSuccess &&
+	          cudaMalloc((void **)&m->triSource, (triSource.size() + 1) * sizeof(int32_t)) == cudaSuccess;
+	if (ok && pointCount > 0) ok = cudaMemcpy(m->positions, positions, (size_t)pointCount * 3 * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+	if (ok && polygonCount > 0) {
+		ok = cudaMemcpy(m->polygons, polygonIndices, (size_t)polygonCount * 4 * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+		     cudaMemcpy(m->texCoords, texCoords, (size_t)polygonCount * 16 * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+		     cudaMemcpy(m->colors, colors, (size_t)polygonCount * 16 * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+		     cudaMemcpy(m->triSource, triSource.data(), triSource.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess;
+	}
+	if (!ok) {
+		cudaFree(m->positions); cudaFree(m->polygons); cudaFree(m->texCoords); cudaFree(m->colors); cudaFree(m->triSource);
+		delete m;
+		return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "dsrg_model_create: device allocation or copy failed");
+	}
+	*out = m;
+	return DSRG_OK;
+}
+
+int dsrg_model_destroy(dsrg_model m) {
+	if (!m) return DSRG_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(m->context->device);
+	cudaStreamSynchronize(m->context->stream);
+	cudaFree(m->positions); cudaFree(m->polygons); cudaFree(m->texCoords); cudaFree(m->colors); cudaFree(m->triSource);
+	delete m;
+	return DSRG_OK;
+}
+
+// ------------------------------------------------------------------ renderer
+
+int dsrg_renderer_create(dsrg_context ctx, dsrg_renderer *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_renderer r = new (std::nothrow) dsrg_renderer_s();
+	if (!r) return DSRG_ERROR_OUT_OF_MEMORY;
+	r->context = ctx;
+	*out = r;
+	return DSRG_OK;
+}
+
+int dsrg_renderer_destroy(dsrg_renderer r) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	delete r;
+	return DSRG_OK;
+}
+
+int dsrg_renderer_takes_triangles(dsrg_renderer r) { return (r && r->receiving) ? 1 : 0; }
+
+static bool image_valid(const dsrg_image *img, int elementSize) {
+	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * elementSize &&
+	       img->strideBytes % elementSize == 0;
+}
+
+static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_image *depth, bool depthOnly) {
+	dsrg_context ctx = r->context;
+	// RendererImpl::beginFrame (api/rendererAPI.cpp:151-168)
+	if (r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_begin on the same renderer twice without ending the previous batch!");
+	if (color && !image_valid(color, 4)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: invalid colour image");
+	if (depth && !image_valid(depth, 4)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: invalid depth image");
+	if (color && (color->packOrder < 0 || color->packOrder > 3)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: unknown pack order");
+	if (color && depth && (color->width != depth->width || color->height != depth->height))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: colour and depth images must have the same dimensions");
+	cudaSetDevice(ctx->device);
+	r->hasColor = color != nullptr;
+	r->hasDepth = depth != nullptr;
+	r->depthOnly = depthOnly;
+	if (color) r->color = *color;
+	if (depth) r->depth = *depth;
+	r->width = color ? color->width : (depth ? depth->width : 0);
+	r->height = color ? color->height : (depth ? depth->height : 0);
+	size_t pixels = (size_t)r->width * r->height;
+	r->deviceColor = nullptr;
+	r->deviceDepth = nullptr;
+	if (color) {
+		if (color->onDevice) {
+			r->deviceColor = (uint32_t *)color->data;
+			r->colorStride = color->strideBytes / 4;
+		} else {
+			CUDA_TRY(ctx, ctx->stagingColor.reserve(pixels));
+			r->deviceColor = ctx->stagingColor.ptr;
+			r->colorStride = r->width;
+			CUDA_TRY(ctx, cudaMemcpy2DAsync(r->deviceColor, (size_t)r->width * 4, color->data, color->strideBytes,
+			                                (size_t)r->width * 4, r->height, cudaMemcpyHostToDevice, ctx->stream));
+		}
+	}
+	if (depth) {
+		if (depth->onDevice) {
+			r->deviceDepth = (float *)depth->data;
+			r->depthStride = depth->strideBytes / 4;
+		} else {
+			CUDA_TRY(ctx, ctx->stagingDepth.reserve(pixels));
+			r->deviceDepth = ctx->stagingDepth.ptr;
+			r->depthStride = r->width;
+			CUDA_TRY(ctx, cudaMemcpy2DAsync(r->deviceDepth, (size_t)r->width * 4, depth->data, depth->strideBytes,
+			                                (size_t)r->width * 4, r->height, cudaMemcpyHostToDevice, ctx->stream));
+		}
+	}
+	r->triangleCount = 0;
+	r->recordCapacity = (uint32_t)ctx->records.capacity;
+	r->cameraKnown = false;
+	r->textures.clear();
+	r->textureHandles.clear();
+	CUDA_TRY(ctx, cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream));
+	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStart, ctx->stream));
+	r->receiving = true;
+	return DSRG_OK;
+}
+
+int dsrg_renderer_begin(dsrg_renderer r, const dsrg_image *color, const dsrg_image *depth) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	return begin_frame(r, color, depth, false);
+}
+
+static int32_t texture_slot(dsrg_renderer r, dsrg_texture t) {
+	if (!t) return -1;
+	for (size_t i = 0; i < r->textureHandles.size(); i++) if (r->textureHandles[i] == t) return (int32_t)i;
+	r->textureHandles.push_back(t);
+	r->textures.push_back(t->data);
+	return (int32_t)r->textures.size() - 1;
+}
+
+static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera) {
+	dsrg_context ctx = r->context;
+	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Cannot call renderer_giveTask before renderer_begin!");
+	if (!m || !modelToWorld || !camera) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: null argument");
+	if (camera->width <= 0 || camera->height <= 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: camera without image size");
+	if (m->filter == DSRG_FILTER_ALPHA && r->hasColor)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: the alpha filter is not available on the GPU path yet");
+	CameraData cam = make_camera(*camera);
+	if (r->cameraKnown && r->affine != !camera->perspective)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: perspective and orthogonal cameras cannot share one frame");
+	r->affine = !camera->perspective;
+	r->cameraKnown = true;
+	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld)) return DSRG_OK;
+	if (m->triangleCount == 0) return DSRG_OK;
+	TaskParams task;
+	memset(&task, 0, sizeof(task));
+	task.positions = m->positions;
+	task.polygons = m->polygons;
+	task.texCoords = m->texCoords;
+	task.colors = m->colors;
+	task.triSource = m->triSource;
+	task.pointCount = m->pointCount;
+	task.triangleCount = m->triangleCount;
+	task.orderBase = r->triangleCount;
+	task.shadeBase = r->triangleCount;
+	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
+	task.camera = cam;
+	task.width = r->width;
+	task.height = r->height;
+	task.hasColor = r->hasColor ? 1 : 0;
+	task.hasDepth = r->hasDepth ? 1 : 0;
+	task.filter = m->filter;
+	task.diffuse = r->depthOnly ? -1 : texture_slot(r, m->diffuse);
+	task.light = r->depthOnly ? -1 : texture_slot(r, m->light);
+	task.depthOnly = r->depthOnly ? 1 : 0;
+	size_t np = (size_t)m->pointCount, nt = (size_t)m->triangleCount;
+	CUDA_TRY(ctx, ctx->csx.reserve(np)); CUDA_TRY(ctx, ctx->csy.reserve(np)); CUDA_TRY(ctx, ctx->csz.reserve(np));
+	CUDA_TRY(ctx, ctx->isx.reserve(np)); CUDA_TRY(ctx, ctx->isy.reserve(np));
+	CUDA_TRY(ctx, ctx->flatx.reserve(np)); CUDA_TRY(ctx, ctx->flaty.reserve(np));
+	CUDA_TRY(ctx, ctx->triCounts.reserve(nt + 2));
+	CUDA_TRY(ctx, ctx->triOffsets.reserve(nt + 2));
+	size_t scanElems = scan_scratch_elems((uint32_t)(nt + 2));
+	CUDA_TRY(ctx, ctx->scanScratch.reserve(scanElems));
+	// A triangle clipped against six planes is a fan of at most seven triangles.
+	size_t needed = (size_t)r->triangleCount * 7 + nt * 7;
+	CUDA_TRY(ctx, ctx->records.reserve(needed, true, (size_t)r->triangleCount * 7, ctx->stream));
+	CUDA_TRY(ctx, ctx->shades.reserve((size_t)r->triangleCount + nt, true, r->triangleCount, ctx->stream));
+	r->recordCapacity = (uint32_t)ctx->records.capacity;
+	FrameBuffers fb;
+	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
+	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
+	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
+	fb.triCounts = ctx->triCounts.ptr;
+	fb.triOffsets = ctx->triOffsets.ptr;
+	fb.records = ctx->records.ptr;
+	fb.shades = ctx->shades.ptr;
+	fb.recordCount = ctx->control.ptr;
+	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
+	fb.scanScratch = ctx->scanScratch.ptr;
+	fb.scanScratchElems = ctx->scanScratch.capacity;
+	launch_project(task, fb, ctx->stream);
+	launch_setup(task, fb, r->recordCapacity, ctx->stream);
+	CUDA_TRY(ctx, cudaGetLastError());
+	r->triangleCount += (uint32_t)nt;
+	return DSRG_OK;
+}
+
+int dsrg_renderer_give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	return give_task(r, m, modelToWorld, camera);
+}
+
+static int end_frame(dsrg_renderer r) {
+	dsrg_context ctx = r->context;
+	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
+	r->receiving = false;
+	uint32_t control[2] = {0, 0};
+	CUDA_TRY(ctx, cudaMemcpyAsync(control, ctx->control.ptr, sizeof(control), cudaMemcpyDeviceToHost, ctx->stream));
+	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	if (control[1] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(control[1]));
+	const uint32_t recordCount = control[0];
+	TileBins bins;
+	bins.tilesX = (r->width + TILE_W - 1) / TILE_W;
+	bins.tilesY = (r->height + TILE_H - 1) / TILE_H;
+	size_t tiles = (size_t)bins.tilesX * bins.tilesY;
+	CUDA_TRY(ctx, ctx->binCounts.reserve(tiles));
+	CUDA_TRY(ctx, ctx->binOffsets.reserve(tiles + 1));
+	CUDA_TRY(ctx, ctx->binCursors.reserve(tiles));
+	CUDA_TRY(ctx, ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)tiles)));
+	CUDA_TRY(ctx, ctx->textureTable.reserve(r->textures.size() + 1));
+	if (!r->textures.empty())
+		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->textureTable.ptr, r->textures.data(), r->textures.size() * sizeof(TextureData),
+		                              cudaMemcpyHostToDevice, ctx->stream));
+	bins.counts = ctx->binCounts.ptr;
+	bins.offsets = ctx->binOffsets.ptr;
+	bins.cursors = ctx->binCursors.ptr;
+	bins.lists = ctx->binLists.ptr;
+	bins.listCapacity = ctx->binLists.capacity;
+	FrameBuffers fb;
+	memset(&fb, 0, sizeof(fb));
+	fb.records = ctx->records.ptr;
+	fb.shades = ctx->shades.ptr;
+	fb.recordCount = ctx->control.ptr;
+	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
+	fb.scanScratch = ctx->scanScratch.ptr;
+	fb.scanScratchElems = ctx->scanScratch.capacity;
+	uint32_t entries = launch_bin_count(fb, recordCount, bins, ctx->stream);
+	CUDA_TRY(ctx, cudaGetLastError());
+	CUDA_TRY(ctx, ctx->binLists.reserve((size_t)entries + 1));
+	bins.lists = ctx->binLists.ptr;
+	bins.listCapacity = ctx->binLists.capacity;
+	launch_bin_fill(fb, recordCount, bins, ctx->stream);
+	TargetParams tg;
+	memset(&tg, 0, sizeof(tg));
+	tg.color = r->hasColor ? r->deviceColor : nullptr;
+	tg.colorStride = r->colorStride;
+	tg.packOrder = r->hasColor ? r->color.packOrder : 0;
+	tg.depth = r->hasDepth ? r->deviceDepth : nullptr;
+	tg.depthStride = r->depthStride;
+	tg.width = r->width;
+	tg.height = r->height;
+	tg.affine = r->affine ? 1 : 0;
+	if (ctx->counting) {
+		CUDA_TRY(ctx, cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), ctx->stream));
+		tg.fragments = ctx->fragmentCounter.ptr;
+		tg.coverage = ctx->coverage;
+	}
+	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStart, ctx->stream));
+	if (r->depthOnly) launch_raster_depth_only(fb, bins, tg, ctx->stream);
+	else launch_raster(fb, ctx->textureTable.ptr, bins, tg, ctx->stream);
+	CUDA_TRY(ctx, cudaGetLastError());
+	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStop, ctx->stream));
+	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStop, ctx->stream));
+	if (r->hasColor && !r->color.onDevice)
+		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->color.data, r->color.strideBytes, r->deviceColor, (size_t)r->width * 4,
+		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
+	if (r->hasDepth && !r->depth.onDevice)
+		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->depth.data, r->depth.strideBytes, r->deviceDepth, (size_t)r->width * 4,
+		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
+	unsigned long long fragments = 0;
+	if (ctx->counting)
+		CUDA_TRY(ctx, cudaMemcpyAsync(&fragments, ctx->fragmentCounter.ptr, sizeof(fragments), cudaMemcpyDeviceToHost, ctx->stream));
+	uint32_t errorBits = 0;
+	CUDA_TRY(ctx, cudaMemcpyAsync(&errorBits, ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "rasterisation reported device error bits " + std::to_string(errorBits));
+	float ms = 0.0f, rasterMs = 0.0f;
+	cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
+	cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);
+	ctx->stats.fragments = fragments;
+	ctx->stats.drawRecords = recordCount;
+	ctx->stats.binEntries = entries;
+	ctx->stats.milliseconds = ms;
+	ctx->stats.rasterMilliseconds = rasterMs;
+	ctx->stats.kernelLaunches = launch_count();
+	return DSRG_OK;
+}
+
+int dsrg_renderer_end(dsrg_renderer r) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	return end_frame(r);
+}
+
+// ------------------------------------------------------------------ single-call rendering
+
+static int render_once(dsrg_context ctx, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera,
+                       const dsrg_image *color, const dsrg_image *depth, bool depthOnly) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!m) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "model_render: null model");
+	if (!color && !depth) return DSRG_OK; // renderTriangleFromData: no target buffer to draw on
+	if (!ctx->implicitRenderer) {
+		int s = dsrg_renderer_create(ctx, &ctx->implicitRenderer);
+		if (s != DSRG_OK) return s;
+	}
+	dsrg_renderer r = ctx->implicitRenderer;
+	int s = begin_frame(r, color, depth, depthOnly);
+	if (s != DSRG_OK) return s;
+	s = give_task(r, m, modelToWorld, camera);
+	if (s != DSRG_OK) {
+		r->receiving = false;
+		cudaStreamSynchronize(ctx->stream);
+		return s;
+	}
+	return end_frame(r);
+}
+
+int dsrg_model_render(dsrg_context ctx, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera,
+                      const dsrg_image *color, const dsrg_image *depth) {
+	return render_once(ctx, m, modelToWorld, camera, color, depth, false);
+}
+
+int dsrg_model_render_depth(dsrg_context ctx, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera,
+                            const dsrg_image *depth) {
+	if (!depth) return DSRG_OK;
+	return render_once(ctx, m, modelToWorld, camera, nullptr, depth, true);
+}
+
+} // extern "C"

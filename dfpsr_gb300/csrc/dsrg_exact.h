@@ -1,0 +1,223 @@
+// Exact arithmetic shared by the CUDA kernels and their host-side checks.
+//
+// Everything here is plain binary32 / int64 arithmetic in a fixed order, so the
+// same source compiled by nvcc for sm_103a (with -fmad=false) and by a host C++
+// compiler (with -ffp-contract=off) gives identical bits.  These are the
+// operations the reference renderer performs one pixel at a time; the GPU needs
+// them in a form that any thread can evaluate for any pixel independently.
+#ifndef DSRG_EXACT_H
+#define DSRG_EXACT_H
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define DSRG_HD __host__ __device__ __forceinline__
+#else
+#define DSRG_HD inline
+#endif
+
+namespace dsrg {
+
+DSRG_HD float fadd(float a, float b) {
+#if defined(__CUDA_ARCH__)
+	return __fadd_rn(a, b);
+#else
+	return a + b;
+#endif
+}
+DSRG_HD float fmul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+	return __fmul_rn(a, b);
+#else
+	return a * b;
+#endif
+}
+DSRG_HD float fdiv(float a, float b) {
+#if defined(__CUDA_ARCH__)
+	return __fdiv_rn(a, b);
+#else
+	return a / b;
+#endif
+}
+DSRG_HD uint32_t fbits(float f) {
+#if defined(__CUDA_ARCH__)
+	return __float_as_uint(f);
+#else
+	union { float f; uint32_t u; } v; v.f = f; return v.u;
+#endif
+}
+DSRG_HD float bitsf(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+	return __uint_as_float(u);
+#else
+	union { float f; uint32_t u; } v; v.u = u; return v.f;
+#endif
+}
+DSRG_HD float i64_to_float(int64_t v) {
+#if defined(__CUDA_ARCH__)
+	return __ll2float_rn(v);
+#else
+	return (float)v;
+#endif
+}
+
+// Result of adding d to s, n times in a row, each sum rounded to binary32 nearest-even:
+//   for (i = 0; i < n; i++) s = s + d;
+// The reference accumulates its depth and vertex weights this way along each
+// row pair (implementation/render/shader/fillerTemplates.h:196-244, 339-372).
+// Evaluated in O(binades visited) instead of O(n): inside one binade of s the
+// representable values are the multiples of ulp(s), the exact sum s + d always
+// has the same remainder modulo ulp(s), so every step rounds by the same
+// increment until the running value leaves the binade (or a tie needs a parity
+// that the current value does not have).  Those boundary steps are taken one at
+// a time with a real float addition.
+DSRG_HD float chain_add(float s, float d, int32_t n) {
+	for (int guard = 0; n > 0 && guard < 96; guard++) {
+		uint32_t sb = fbits(s), db = fbits(d);
+		int32_t se = (int32_t)((sb >> 23) & 0xFFu), de = (int32_t)((db >> 23) & 0xFFu);
+		if (se == 0 || se >= 254 || de == 0 || de == 255) {
+			// zero, subnormal, near-overflow, infinity or NaN: one plain step
+			s = fadd(s, d); n--; continue;
+		}
+		const bool negative = (sb >> 31) != 0;
+		const int64_t M = (int64_t)((sb & 0x7FFFFFu) | 0x800000u);     // |s| = M * 2^(se-150)
+		int64_t Dm = (int64_t)((db & 0x7FFFFFu) | 0x800000u);         // |d| = Dm * 2^(de-150)
+		if (((db >> 31) != 0) != negative) Dm = -Dm;                     // d relative to the sign of s
+		if (de > se + 26) { s = fadd(s, d); n--; continue; }             // leaves the binade at once
+		if (se > de + 26) {
+			// |d| < ulp(s) / 4: s never changes unless it sits on the bottom of its binade and d
+			// points down, where the next binade has a finer ulp.
+			if (M == 0x800000 && Dm < 0) { s = fadd(s, d); n--; continue; }
+			return s;
+		}
+		const int32_t e0 = se < de ? se : de;
+		const int64_t U = (int64_t)1 << (se - e0);       // ulp(s) in units of 2^(e0-150)
+		const int64_t S = M << (se - e0);                 // s in those units
+		const int64_t D = Dm * ((int64_t)1 << (de - e0)); // d in those units
+		const int64_t lo = (int64_t)1 << (23 + se - e0);  // bottom of the binade of |s|
+		const int64_t hi = lo << 1;
+		// floor division of D by U (U is a power of two)
+		int64_t a = D >= 0 ? D / U : -((-D + U - 1) / U);
+		int64_t r = D - a * U;                            // 0 <= r < U
+		int64_t inc;
+		if (U == 1) {
+			inc = a;
+		} else {
+			const int64_t half = U >> 1;
+			if (r < half) {
+				inc = a;
+			} else if (r > half) {
+				inc = a + 1;
+			} else {
+				// tie: rounds to the even multiple; constant only once s itself is an even multiple
+				if ((M & 1) != 0) { s = fadd(s, d); n--; continue; }
+				inc = ((a & 1) == 0) ? a : a + 1;
+			}
+		}
+		const int64_t X0 = S + D;
+		if (X0 < lo || X0 >= hi) { s = fadd(s, d); n--; continue; }
+		const int64_t INC = inc * U;
+		if (INC == 0) return s;
+		int64_t m;
+		if (INC > 0) {
+			m = (hi - X0 + INC - 1) / INC;
+		} else {
+			m = (X0 - lo) / (-INC) + 1;
+		}
+		const int64_t steps = m < (int64_t)n ? m : (int64_t)n;
+		const int64_t S2 = S + steps * INC;
+		n -= (int32_t)steps;
+		int64_t M2 = S2 >> (se - e0);
+		uint32_t bits;
+		if (M2 >= ((int64_t)1 << 24)) {
+			bits = ((uint32_t)(se + 1) << 23);
+		} else {
+			bits = ((uint32_t)se << 23) | ((uint32_t)M2 & 0x7FFFFFu);
+		}
+		s = bitsf(bits | (negative ? 0x80000000u : 0u));
+		if (n > 0) { s = fadd(s, d); n--; }
+	}
+	while (n > 0) { s = fadd(s, d); n--; }
+	return s;
+}
+
+// min(max(L, (int32_t)(a / b + 1)), R) with C's truncating int64 division, as the
+// reference's cutConvexEdge computes each row's bound (implementation/render/ITriangle2D.cpp:122,130).
+// A binary32 estimate of the quotient settles the clamp when it is far outside
+// [L, R]; near the clamp range an exact int64 remainder check corrects it; only
+// quotients beyond +-2^30 (where the int32 cast may wrap) take the 64-bit division.
+// Requires b != 0 and -2^20 < L <= R < 2^20.
+DSRG_HD int32_t clamp_quotient_plus_one(int64_t a, int64_t b, int32_t L, int32_t R) {
+	float qf = fdiv(i64_to_float(a), i64_to_float(b));
+	int32_t v;
+	if (qf > -1.0e9f && qf < 1.0e9f) {
+		if (qf < -2097152.0f) return L;
+		if (qf > 2097152.0f) return R;
+		int64_t q = (int64_t)qf;
+		// make the divisor positive; truncating and floor quotients are unchanged by negating both
+		int64_t aa = a, bb = b;
+		if (bb < 0) { aa = -aa; bb = -bb; }
+		// floor quotient: q * bb <= aa < (q + 1) * bb
+		while (q * bb > aa) q--;
+		while ((q + 1) * bb <= aa) q++;
+		if (aa < 0 && q * bb != aa) q++; // truncation toward zero
+		v = (int32_t)(q + 1);
+	} else {
+		v = (int32_t)(a / b + 1);
+	}
+	return v < L ? L : (v > R ? R : v);
+}
+
+// One triangle edge in sub-pixel units, from cutConvexEdge (implementation/render/ITriangle2D.cpp:86-148).
+struct Edge {
+	int64_t sx, sy;      // start corner
+	int64_t nx, ny;      // normal: (end.y - start.y, start.x - end.x)
+	int64_t threshold;   // -1 or 0 by edge direction
+};
+
+DSRG_HD Edge make_edge(int64_t sx, int64_t sy, int64_t ex, int64_t ey) {
+	Edge e;
+	e.sx = sx; e.sy = sy;
+	e.nx = ey - sy;
+	e.ny = sx - ex;
+	e.threshold = (sx > ex || (sx == ex && sy > ey)) ? -1 : 0;
+	return e;
+}
+
+// Applies one edge to the interval of pixel row y, clamped to [L, R).
+// The per-row limit of cutConvexEdge, limit(y) = threshold - (128 - sx)*nx - (128 + 256*y - sy)*ny,
+// does not depend on the clip rectangle's corner, so any row can be cut on its own.
+DSRG_HD void cut_row(const Edge &e, int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {
+	if (e.nx != 0) {
+		int64_t limit = e.threshold - (128 - e.sx) * e.nx - (128 + 256 * (int64_t)y - e.sy) * e.ny;
+		int64_t offsetX = e.nx * 256;
+		if (e.nx < 0) {
+			int32_t side = clamp_quotient_plus_one(limit + 1, offsetX, L, R);
+			if (side > left) left = side;
+		} else {
+			int32_t side = clamp_quotient_plus_one(limit, offsetX, L, R);
+			if (side < right) right = side;
+		}
+	} else if (e.ny != 0) {
+		int64_t value = (128 + 256 * (int64_t)y - e.sy) * e.ny;
+		if (value > e.threshold) { left = R; right = L; }
+	}
+}
+
+// Row interval [left, right) of pixel row y for a triangle with sub-pixel corners,
+// clamped to [L, R): rasterizeTriangle (implementation/render/ITriangle2D.cpp:150-169).
+DSRG_HD void row_interval(const int32_t *flat, int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {
+	const bool degenerate = (flat[0] == flat[2] && flat[1] == flat[3]) || (flat[2] == flat[4] && flat[3] == flat[5]) ||
+	                        (flat[4] == flat[0] && flat[5] == flat[1]);
+	if (degenerate) { left = R; right = L; return; }
+	left = L; right = R;
+	for (int i = 0; i < 3; i++) {
+		int j = (i + 1) % 3;
+		Edge e = make_edge(flat[i * 2], flat[i * 2 + 1], flat[j * 2], flat[j * 2 + 1]);
+		cut_row(e, y, L, R, left, right);
+	}
+}
+
+} // namespace dsrg
+
+#endif

@@ -1,0 +1,589 @@
+// CUDA kernels of the DFPSR triangle path for sm_103a.
+//
+// Pipeline per frame:
+//   project_kernel      Camera::worldToScreen for every model point (implementation/render/Camera.h:157-190)
+//   setup_kernel<false> per fan triangle: cull, clip, front-face; counts its draw records
+//   scan                record offsets, so that records land in submission order
+//   setup_kernel<true>  writes DrawRecords (bound, sub-pixel corners, projection) and ShadeRecords
+//   bin kernels         per 16x16 tile lists of the records whose raster bound touches it
+//   raster kernels      one CTA per tile: exact row intervals, exact accumulated depth, depth
+//                       test resolved with 64-bit shared-memory atomicMax keys, then deferred
+//                       shading of the winning fragment of every pixel.
+//
+// Why the depth test can run out of order: the reference writes a fragment when its depth is
+// strictly greater (1/W, perspective) or smaller (linear, orthogonal) than the stored one
+// (implementation/render/shader/fillerTemplates.h:108-152).  After any sequence of opaque
+// triangles the stored value is the extreme depth over all fragments that beat the initial
+// value, and the colour is the earliest fragment reaching it.  Packing (depth, ~record index)
+// into one 64-bit key and taking the maximum reproduces exactly that, in any order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dsrg_exact.h"
+#include "dsrg_geometry.h"
+#include "dsrg_shade.h"
+#include "dsrg_kernels.h"
+
+namespace dsrg {
+
+static uint64_t g_launches = 0;
+uint64_t launch_count() { return g_launches; }
+#define COUNT_LAUNCH() (g_launches++)
+
+// ------------------------------------------------------------------ projection
+
+__global__ void project_kernel(TaskParams task, ProjectedPoints out) {
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= task.pointCount) return;
+	Vec3 p = vec3(task.positions[i * 3], task.positions[i * 3 + 1], task.positions[i * 3 + 2]);
+	Projected pr = camera_to_screen(task.camera, world_to_camera(task.camera, transform_point(task.modelToWorld, p)));
+	out.csx[i] = pr.cs.x; out.csy[i] = pr.cs.y; out.csz[i] = pr.cs.z;
+	out.isx[i] = pr.isx; out.isy[i] = pr.isy;
+	out.flatx[i] = pr.flatx; out.flaty[i] = pr.flaty;
+}
+
+void launch_project(const TaskParams &task, const FrameBuffers &fb, cudaStream_t stream) {
+	if (task.pointCount <= 0) return;
+	COUNT_LAUNCH();
+	project_kernel<<<(task.pointCount + 255) / 256, 256, 0, stream>>>(task, fb.points);
+}
+
+// ------------------------------------------------------------------ triangle setup
+
+struct Corner {
+	Vec3 cs;
+	float isx, isy;
+	int64_t fx, fy;
+};
+
+// Emits one draw command (renderCore.cpp:203-217 executeTriangleDrawing against the whole target):
+// the triangle bound cut to the target with rows aligned to pairs (ITriangle2D.cpp:70-75).
+template <bool WRITE>
+__device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity,
+                            const Corner *c, const float *subB, const float *subC, uint32_t order, uint32_t shade,
+                            uint32_t base, uint32_t &emitted) {
+	int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
+	int32_t b[4];
+	triangle_bound(fx, fy, b);
+	if (!(b[0] < task.width && b[2] > 0 && b[1] < task.height && b[3] > 0)) return;
+	int32_t left = b[0] > 0 ? b[0] : 0, top = b[1] > 0 ? b[1] : 0;
+	int32_t right = b[2] < task.width ? b[2] : task.width, bottom = b[3] < task.height ? b[3] : task.height;
+	top = top & ~1;                 // roundDown(top, 2) for top >= 0
+	bottom = (bottom + 1) & ~1;     // roundUp(bottom, 2)
+	if (WRITE) {
+		uint32_t index = base + emitted;
+		if (index >= recordCapacity) {
+			atomicOr(fb.errorFlag, ERROR_RECORD_OVERFLOW);
+		} else {
+			DrawRecord r;
+			bool inRange = true;
+			for (int i = 0; i < 3; i++) {
+				if (fx[i] < -(1ll << 30) || fx[i] > (1ll << 30) || fy[i] < -(1ll << 30) || fy[i] > (1ll << 30)) inRange = false;
+				r.flat[i * 2] = (int32_t)fx[i];
+				r.flat[i * 2 + 1] = (int32_t)fy[i];
+			}
+			if (!inRange) atomicOr(fb.errorFlag, ERROR_COORDINATE_RANGE);
+			r.left = left; r.top = top; r.right = right; r.bottom = bottom;
+			float isx[3] = {c[0].isx, c[1].isx, c[2].isx}, isy[3] = {c[0].isy, c[1].isy, c[2].isy};
+			float csz[3] = {c[0].cs.z, c[1].cs.z, c[2].cs.z};
+			triangle_projection(isx, isy, csz, subB, subC, task.camera.perspective != 0, r.start, r.dx, r.dy);
+			r.order = order;
+			r.shade = shade;
+			r.flags = task.camera.perspective ? 0u : RECORD_AFFINE;
+			r.pad = 0;
+			fb.records[index] = r;
+		}
+	}
+	emitted++;
+}
+
+// renderTriangleFromData / renderTriangleFromDataDepth for one fan triangle (renderCore.cpp:220-341, 400-443).
+template <bool WRITE>
+__global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCapacity) {
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= task.triangleCount) return;
+	uint32_t emitted = 0;
+	const uint32_t base = WRITE ? fb.triOffsets[t] + fb.triOffsets[task.triangleCount + 1] : 0u;
+	const int32_t src = task.triSource[t];
+	const int32_t p = src >> 1, k = src & 1;
+	const int corner[3] = {0, 1 + k, 2 + k}; // fan 0-1-2, 0-2-3 (model/Model.cpp:135-162, 164-183)
+	Corner c[3];
+	for (int i = 0; i < 3; i++) {
+		int32_t pi = task.polygons[p * 4 + corner[i]];
+		c[i].cs = vec3(fb.points.csx[pi], fb.points.csy[pi], fb.points.csz[pi]);
+		c[i].isx = fb.points.isx[pi]; c[i].isy = fb.points.isy[pi];
+		c[i].fx = fb.points.flatx[pi]; c[i].fy = fb.points.flaty[pi];
+	}
+	const uint32_t order = (task.orderBase + (uint32_t)t) * 8u;
+	const uint32_t shadeIndex = task.shadeBase + (uint32_t)t;
+	bool visible = triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, false) != 0;
+	if (visible && !task.depthOnly) {
+		const float *col[3];
+		for (int i = 0; i < 3; i++) col[i] = task.colors + (p * 4 + corner[i]) * 4;
+		if (task.filter == 1 && almost_zero(col[0][3]) && almost_zero(col[1][3]) && almost_zero(col[2][3])) visible = false;
+		if (visible && WRITE) {
+			// RgbaMultiply_data and the variant choice (shader/RgbaMultiply.h:37-58, 110-173).
+			ShadeRecord s;
+			float scale = 255.0f;
+			if (task.diffuse >= 0) scale = fmul(scale, 1.0f / 255.0f);
+			if (task.light >= 0) scale = fmul(scale, 1.0f / 255.0f);
+			for (int i = 0; i < 3; i++) {
+				s.red[i] = fmul(col[i][0], scale); s.green[i] = fmul(col[i][1], scale);
+				s.blue[i] = fmul(col[i][2], scale); s.alpha[i] = fmul(col[i][3], scale);
+				const float *tc = task.texCoords + (p * 4 + corner[i]) * 4;
+				s.u1[i] = tc[0]; s.v1[i] = tc[1]; s.u2[i] = tc[2]; s.v2[i] = tc[3];
+			}
+			bool fade = !(almost_same3(s.red) && almost_same3(s.green) && almost_same3(s.blue) && almost_same3(s.alpha));
+			bool colorless = almost_one3(s.red) && almost_one3(s.green) && almost_one3(s.blue) && almost_one3(s.alpha);
+			bool hasDiffuse = task.diffuse >= 0, hasLight = task.light >= 0;
+			if (fade || (hasDiffuse == hasLight)) colorless = false;
+			s.flags = (hasDiffuse ? SHADE_DIFFUSE : 0u) | (hasLight ? SHADE_LIGHT : 0u) | (fade ? SHADE_VERTEX_FADE : 0u) |
+			          (colorless ? SHADE_COLORLESS : 0u) | (task.filter == 1 ? SHADE_ALPHA_FILTER : 0u);
+			s.diffuse = task.diffuse;
+			s.light = task.light;
+			s.pad = 0;
+			fb.shades[shadeIndex] = s;
+		}
+	}
+	if (visible && (task.hasColor || task.hasDepth)) {
+		const float defaultB[3] = {0.0f, 1.0f, 0.0f}, defaultC[3] = {0.0f, 0.0f, 1.0f};
+		const float zero3[3] = {0.0f, 0.0f, 0.0f};
+		if (triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, true) == 1) {
+			int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
+			if (is_frontfacing(fx, fy)) {
+				emit_record<WRITE>(task, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
+				                   task.depthOnly ? zero3 : defaultC, order, shadeIndex, base, emitted);
+			}
+		} else {
+			ClippedPolygon poly;
+			poly.count = 3;
+			for (int i = 0; i < 3; i++) { poly.v[i].cs = c[i].cs; poly.v[i].state = 0; poly.v[i].value = 0.0f; }
+			poly.v[0].subB = 0.0f; poly.v[0].subC = 0.0f;
+			poly.v[1].subB = 1.0f; poly.v[1].subC = 0.0f;
+			poly.v[2].subB = 0.0f; poly.v[2].subC = 1.0f;
+			for (int s = 0; s < task.camera.clipCount; s++) poly.clip(task.camera.clip[s]);
+			for (int f = 0; f < poly.count - 2; f++) {
+				const SubVertex *sv[3] = {&poly.v[0], &poly.v[1 + f], &poly.v[2 + f]};
+				Corner sc[3];
+				for (int i = 0; i < 3; i++) {
+					Projected pr = camera_to_screen(task.camera, sv[i]->cs);
+					sc[i].cs = pr.cs; sc[i].isx = pr.isx; sc[i].isy = pr.isy; sc[i].fx = pr.flatx; sc[i].fy = pr.flaty;
+				}
+				int64_t fx[3] = {sc[0].fx, sc[1].fx, sc[2].fx}, fy[3] = {sc[0].fy, sc[1].fy, sc[2].fy};
+				if (is_frontfacing(fx, fy)) {
+					float sb[3] = {sv[0]->subB, sv[1]->subB, sv[2]->subB};
+					float scc[3] = {sv[0]->subC, sv[1]->subC, sv[2]->subC};
+					emit_record<WRITE>(task, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
+					                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, shadeIndex, base, emitted);
+				}
+			}
+		}
+	}
+	if (!WRITE) fb.triCounts[t] = emitted;
+}
+
+__global__ void advance_record_count_kernel(FrameBuffers fb, int32_t triangleCount) {
+	// triOffsets[triangleCount] holds this task's total; [triangleCount + 1] the records before it.
+	uint32_t before = fb.triOffsets[triangleCount + 1];
+	*fb.recordCount = before + fb.triOffsets[triangleCount];
+}
+
+__global__ void load_record_base_kernel(FrameBuffers fb, int32_t triangleCount) {
+	fb.triOffsets[triangleCount + 1] = *fb.recordCount;
+}
+
+void launch_setup(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream) {
+	if (task.triangleCount <= 0) return;
+	int blocks = (task.triangleCount + 255) / 256;
+	COUNT_LAUNCH();
+	setup_kernel<false><<<blocks, 256, 0, stream>>>(task, fb, recordCapacity);
+	launch_scan(fb.triCounts, fb.triOffsets, (uint32_t)task.triangleCount, fb.scanScratch, fb.scanScratchElems, stream);
+	COUNT_LAUNCH();
+	load_record_base_kernel<<<1, 1, 0, stream>>>(fb, task.triangleCount);
+	COUNT_LAUNCH();
+	setup_kernel<true><<<blocks, 256, 0, stream>>>(task, fb, recordCapacity);
+	COUNT_LAUNCH();
+	advance_record_count_kernel<<<1, 1, 0, stream>>>(fb, task.triangleCount);
+}
+
+// ------------------------------------------------------------------ scan
+
+static const int SCAN_BLOCK = 1024;
+
+__global__ void scan_blocks_kernel(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *blockSums) {
+	__shared__ uint32_t warpSums[32];
+	uint32_t i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+	uint32_t v = i < n ? in[i] : 0u;
+	uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t x = v;
+	for (int o = 1; o < 32; o <<= 1) {
+		uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+		if (lane >= (uint32_t)o) x += y;
+	}
+	if (lane == 31) warpSums[warp] = x;
+	__syncthreads();
+	if (warp == 0) {
+		uint32_t s = warpSums[lane];
+		for (int o = 1; o < 32; o <<= 1) {
+			uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+			if (lane >= (uint32_t)o) s += y;
+		}
+		warpSums[lane] = s;
+	}
+	__syncthreads();
+	uint32_t prefix = (warp > 0 ? warpSums[warp - 1] : 0u) + x - v;
+	if (i < n) out[i] = prefix;
+	if (threadIdx.x == SCAN_BLOCK - 1) blockSums[blockIdx.x] = prefix + v;
+}
+
+__global__ void scan_add_kernel(uint32_t *out, uint32_t n, const uint32_t *blockOffsets) {
+	uint32_t i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+	if (i < n) out[i] += blockOffsets[blockIdx.x];
+}
+
+__global__ void scan_total_kernel(const uint32_t *blockOffsets, const uint32_t *blockSums, uint32_t blocks, uint32_t *out, uint32_t n) {
+	out[n] = blockOffsets[blocks - 1] + blockSums[blocks - 1];
+}
+
+size_t scan_scratch_elems(uint32_t n) {
+	size_t total = 0;
+	uint32_t blocks = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+	while (true) {
+		total += 2 * (size_t)(blocks + 1);
+		if (blocks <= 1) break;
+		blocks = (blocks + SCAN_BLOCK - 1) / SCAN_BLOCK;
+	}
+	return total + 16;
+}
+
+void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream) {
+	if (n == 0) {
+		cudaMemsetAsync(out, 0, sizeof(uint32_t), stream);
+		return;
+	}
+	uint32_t blocks = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+	uint32_t *blockSums = scratch;
+	uint32_t *blockOffsets = scratch + blocks + 1;
+	(void)scratchElems;
+	COUNT_LAUNCH();
+	scan_blocks_kernel<<<blocks, SCAN_BLOCK, 0, stream>>>(in, out, n, blockSums);
+	if (blocks > 1) {
+		launch_scan(blockSums, blockOffsets, blocks, scratch + 2 * (blocks + 1), scratchElems - 2 * (blocks + 1), stream);
+		COUNT_LAUNCH();
+		scan_add_kernel<<<blocks, SCAN_BLOCK, 0, stream>>>(out, n, blockOffsets);
+	} else {
+		cudaMemsetAsync(blockOffsets, 0, sizeof(uint32_t), stream);
+	}
+	COUNT_LAUNCH();
+	scan_total_kernel<<<1, 1, 0, stream>>>(blockOffsets, blockSums, blocks, out, n);
+}
+
+// ------------------------------------------------------------------ binning
+
+__device__ __forceinline__ void record_tiles(const DrawRecord &r, const TileBins &bins, int32_t &tx0, int32_t &tx1,
+                                             int32_t &ty0, int32_t &ty1) {
+	tx0 = r.left >> 4; tx1 = (r.right - 1) >> 4;
+	ty0 = r.top >> 4; ty1 = (r.bottom - 1) >> 4;
+	if (tx1 >= bins.tilesX) tx1 = bins.tilesX - 1;
+	if (ty1 >= bins.tilesY) ty1 = bins.tilesY - 1;
+}
+
+template <bool FILL>
+__global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, TileBins bins, int32_t *errorFlag) {
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+	int32_t tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1;
+	if (r < recordCount) record_tiles(records[r], bins, tx0, tx1, ty0, ty1);
+	const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
+	const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
+	const bool big = tiles > 4;
+	// small records: each thread walks its own few tiles, with the atomics of threads that hit
+	// the same tile merged into one (neighbouring triangles of a mesh usually share tiles)
+	{
+		for (int32_t i = 0; i < 4; i++) {
+			bool active = !big && i < tiles;
+			uint32_t tile = active ? (uint32_t)((ty0 + i / w) * bins.tilesX + tx0 + i % w) : 0xFFFFFFFFu;
+			uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
+			if (active) {
+				uint32_t leader = __ffs(peers) - 1;
+				uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+				uint32_t count = __popc(peers);
+				uint32_t baseSlot = 0;
+				if (lane == leader) baseSlot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], count);
+				baseSlot = __shfl_sync(peers, baseSlot, leader);
+				if (FILL) {
+					uint32_t slot = bins.offsets[tile] + baseSlot + rank;
+					if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+				}
+			}
+		}
+	}
+	// big records: the whole warp walks each one's tiles together
+	uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
+	while (bigMask) {
+		uint32_t src = __ffs(bigMask) - 1;
+		bigMask &= bigMask - 1;
+		int32_t bx0 = __shfl_sync(0xFFFFFFFFu, tx0, src), by0 = __shfl_sync(0xFFFFFFFFu, ty0, src);
+		int32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bt = __shfl_sync(0xFFFFFFFFu, tiles, src);
+		uint32_t br = __shfl_sync(0xFFFFFFFFu, r, src);
+		for (int32_t i = (int32_t)lane; i < bt; i += 32) {
+			uint32_t tile = (uint32_t)((by0 + i / bw) * bins.tilesX + bx0 + i % bw);
+			uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
+			if (FILL) {
+				slot += bins.offsets[tile];
+				if (slot < bins.listCapacity) bins.lists[slot] = br; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+			}
+		}
+	}
+}
+
+uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
+	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * tiles, stream);
+	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag); }
+	launch_scan(bins.counts, bins.offsets, tiles, fb.scanScratch, fb.scanScratchElems, stream);
+	uint32_t total = 0;
+	cudaMemcpyAsync(&total, bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+	cudaStreamSynchronize(stream);
+	return total;
+}
+
+void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
+	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * tiles, stream);
+	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag); }
+}
+
+// ------------------------------------------------------------------ rasterisation
+
+// Block bounds of one row pair (fillerTemplates.h:273-293).
+struct RowPair {
+	int32_t obs, obe, ibs, ibe;
+	int32_t upperLeft, upperRight, lowerLeft, lowerRight;
+	bool any;
+};
+
+__device__ __forceinline__ RowPair make_row_pair(int32_t uL, int32_t uR, int32_t lL, int32_t lR, int32_t y2, int32_t maxHeight) {
+	RowPair rp;
+	int32_t outerStart = min(uL, lL), outerEnd = max(uR, lR);
+	int32_t innerStart = max(uL, lL), innerEnd = min(uR, lR);
+	rp.obs = (int32_t)((uint32_t)outerStart & ~1u);
+	rp.obe = (int32_t)(((uint32_t)outerEnd + 1u) & ~1u);
+	rp.ibs = (int32_t)(((uint32_t)innerStart + 1u) & ~1u);
+	rp.ibe = (int32_t)((uint32_t)innerEnd & ~1u);
+	if (y2 >= maxHeight) lR = lL;
+	rp.upperLeft = uL; rp.upperRight = uR; rp.lowerLeft = lL; rp.lowerRight = lR;
+	rp.any = (uR > uL) || (lR > lL);
+	return rp;
+}
+
+// The four lane values of one component (1/W or W, U/W, V/W) for the quad at x, following the
+// reference's accumulation: edge quads step pWeightUpper/Lower by 2*dx one quad at a time, the
+// run of full quads steps every lane on its own from where the left edge stopped, and the right
+// edge restarts from the left edge's value plus 2*dx times the run length
+// (fillerTemplates.h:196-244, 328-373).
+__device__ __forceinline__ void quad_lanes(float start, float dx, float dy, const RowPair &rp, int32_t y1, int32_t x, float *out) {
+	const float P0 = fadd(fadd(start, fmul(dx, (float)rp.obs + 0.5f)), fmul(dy, (float)y1 + 0.5f));
+	const float L0 = fadd(P0, dy);
+	const float d2 = fmul(dx, 2.0f);
+	if (rp.ibe <= rp.ibs || x < rp.ibs) {
+		int32_t k = (x - rp.obs) >> 1;
+		float U = chain_add(P0, d2, k), L = chain_add(L0, d2, k);
+		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
+		return;
+	}
+	const int32_t nL = (rp.ibs - rp.obs) >> 1;
+	const float Ub = chain_add(P0, d2, nL), Lb = chain_add(L0, d2, nL);
+	if (x < rp.ibe) {
+		int32_t j = (x - rp.ibs) >> 1;
+		out[0] = chain_add(Ub, d2, j);
+		out[1] = chain_add(fadd(Ub, dx), d2, j);
+		out[2] = chain_add(Lb, d2, j);
+		out[3] = chain_add(fadd(Lb, dx), d2, j);
+	} else {
+		int32_t nI = (rp.ibe - rp.ibs) >> 1, r = (x - rp.ibe) >> 1;
+		float m = fmul(d2, (float)nI);
+		float U = chain_add(fadd(Ub, m), d2, r), L = chain_add(fadd(Lb, m), d2, r);
+		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
+	}
+}
+
+// Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106).
+__device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, int l) {
+	const bool edge = (rp.ibe <= rp.ibs) || x < rp.ibs || x >= rp.ibe;
+	const int32_t xx = x + (l & 1);
+	if (l < 2) return edge ? (xx >= rp.upperLeft && xx < rp.upperRight) : true;
+	// Inner quads draw both rows unconditionally.
+	return edge ? (xx >= rp.lowerLeft && xx < rp.lowerRight) : true;
+}
+
+__device__ __forceinline__ uint32_t ordered_depth(float z) {
+	uint32_t b = fbits(z);
+	if (b == 0x80000000u) b = 0u; // -0 and +0 compare equal
+	return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ unsigned long long make_key(float z, uint32_t record, bool depthTest, bool affine) {
+	if (!depthTest) return (unsigned long long)(record + 1u); // no depth buffer: the last triangle drawn wins
+	uint32_t hi = ordered_depth(z);
+	if (affine) hi = ~hi;
+	return ((unsigned long long)hi << 32) | (unsigned long long)(~record);
+}
+
+__device__ __forceinline__ uint32_t key_record(unsigned long long key, bool depthTest) {
+	return depthTest ? ~(uint32_t)(key & 0xFFFFFFFFull) : (uint32_t)key - 1u;
+}
+
+// Row pair of record r for the rows y1, y1 + 1.
+__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, int32_t y1, int32_t height) {
+	int32_t uL, uR, lL, lR;
+	row_interval(r.flat, y1, r.left, r.right, uL, uR);
+	row_interval(r.flat, y1 + 1, r.left, r.right, lL, lR);
+	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
+}
+
+template <bool DEPTH_ONLY_1X1>
+__global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restrict__ records, const ShadeRecord *__restrict__ shades,
+                                                     const TextureData *__restrict__ textures, TileBins bins, TargetParams tg) {
+	__shared__ unsigned long long keys[TILE_PIXELS];
+	__shared__ float initialDepth[TILE_PIXELS];
+	__shared__ uint32_t coverage[TILE_PIXELS];
+	__shared__ unsigned long long fragmentSum;
+	const int tile = blockIdx.x;
+	const int32_t tx0 = (tile % bins.tilesX) * TILE_W, ty0 = (tile / bins.tilesX) * TILE_H;
+	const int tid = threadIdx.x;
+	const int32_t px = tx0 + (tid & 15), py = ty0 + (tid >> 4);
+	const bool inside = px < tg.width && py < tg.height;
+	const bool depthTest = tg.depth != nullptr;
+	const bool affine = tg.affine != 0;
+	initialDepth[tid] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
+	keys[tid] = 0ull;
+	coverage[tid] = 0u;
+	if (tid == 0) fragmentSum = 0ull;
+	__syncthreads();
+
+	const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
+	const int warp = tid >> 5, lane = tid & 31;
+	uint32_t fragments = 0;
+	for (uint32_t e = begin + warp; e < end; e += 8) {
+		const uint32_t ri = bins.lists[e];
+		const DrawRecord r = records[ri];
+		// every lane cuts one of the tile's 16 rows (lanes 16..31 repeat 0..15)
+		int32_t rowLeft, rowRight;
+		row_interval(r.flat, ty0 + (lane & 15), r.left, r.right, rowLeft, rowRight);
+		if (DEPTH_ONLY_1X1) {
+			// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
+			// pixel and grows by dx one pixel at a time.
+			const int32_t y = ty0 + (lane & 15);
+			if (y >= r.top && y < r.bottom && y < tg.height && rowRight > rowLeft) {
+				const int32_t xs = tx0 + (lane >> 4) * 8;
+				int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
+				if (x0 < x1) {
+					float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)rowLeft + 0.5f)), fmul(r.dy[0], (float)y + 0.5f));
+					value = chain_add(value, r.dx[0], x0 - rowLeft);
+					for (int32_t x = x0; x < x1; x++) {
+						const int pix = (y - ty0) * TILE_W + (x - tx0);
+						fragments++;
+						if (tg.coverage) atomicAdd(&coverage[pix], 1u);
+						bool pass = affine ? (value < initialDepth[pix]) : (value > initialDepth[pix]);
+						if (pass) {
+							unsigned long long key = make_key(value, ri, true, affine);
+							if (key > keys[pix]) atomicMax(&keys[pix], key);
+						}
+						value = fadd(value, r.dx[0]);
+					}
+				}
+			}
+			continue;
+		}
+		const int rp = lane >> 2;
+		const int32_t y1 = ty0 + 2 * rp;
+		const int32_t uL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp), uR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp);
+		const int32_t lL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp + 1), lR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp + 1);
+		if (y1 < r.top || y1 >= r.bottom) continue;
+		const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, tg.height);
+		if (!pair.any) continue;
+		for (int q = 0; q < 2; q++) {
+			const int32_t x = tx0 + 4 * (lane & 3) + 2 * q;
+			if (x < pair.obs || x >= pair.obe) continue;
+			float z[4];
+			quad_lanes(r.start[0], r.dx[0], r.dy[0], pair, y1, x, z);
+			for (int l = 0; l < 4; l++) {
+				if (!lane_covered(pair, x, l)) continue;
+				const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+				if (yy >= tg.height || xx >= tg.width) continue;
+				const int pix = (yy - ty0) * TILE_W + (xx - tx0);
+				fragments++;
+				if (tg.coverage) atomicAdd(&coverage[pix], 1u);
+				bool pass = !depthTest || (affine ? (z[l] < initialDepth[pix]) : (z[l] > initialDepth[pix]));
+				if (pass) {
+					unsigned long long key = make_key(z[l], ri, depthTest, affine);
+					if (key > keys[pix]) atomicMax(&keys[pix], key);
+				}
+			}
+		}
+	}
+	if (tg.fragments) {
+		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
+		if (lane == 0) atomicAdd(&fragmentSum, (unsigned long long)fragments);
+	}
+	__syncthreads();
+
+	// Resolve: every pixel re-evaluates its winning fragment exactly and shades it.
+	if (inside) {
+		if (tg.coverage) tg.coverage[(size_t)py * tg.width + px] = coverage[tid];
+		const unsigned long long key = keys[tid];
+		if (key != 0ull) {
+			const uint32_t ri = key_record(key, depthTest);
+			const DrawRecord r = records[ri];
+			if (DEPTH_ONLY_1X1) {
+				int32_t left, right;
+				row_interval(r.flat, py, r.left, r.right, left, right);
+				float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
+				value = chain_add(value, r.dx[0], px - left);
+				tg.depth[(size_t)py * tg.depthStride + px] = value;
+			} else {
+				const int32_t y1 = py & ~1, x = px & ~1;
+				const int lane4 = ((py & 1) << 1) | (px & 1);
+				const RowPair pair = record_row_pair(r, y1, tg.height);
+				float w[3][4];
+				for (int c = 0; c < 3; c++) {
+					if (c > 0 && tg.color == nullptr) break;
+					quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
+				}
+				if (tg.color) {
+					float wa[4], wb[4], wc[4];
+					for (int l = 0; l < 4; l++) {
+						if (affine) {
+							wb[l] = w[1][l];
+							wc[l] = w[2][l];
+						} else {
+							const float linearDepth = fdiv(1.0f, w[0][l]);
+							wb[l] = fmul(w[1][l], linearDepth);
+							wc[l] = fmul(w[2][l], linearDepth);
+						}
+						wa[l] = 1.0f - fadd(wb[l], wc[l]);
+					}
+					float rgba[4];
+					shade_lane(shades[r.shade], textures, wa, wb, wc, lane4, rgba);
+					tg.color[(size_t)py * tg.colorStride + px] = pack_saturated(rgba, tg.packOrder);
+				}
+				if (depthTest) tg.depth[(size_t)py * tg.depthStride + px] = w[0][lane4];
+			}
+		}
+	}
+	if (tg.fragments && tid == 0) atomicAdd(tg.fragments, fragmentSum);
+}
+
+void launch_raster(const FrameBuffers &fb, const TextureData *textures, const TileBins &bins, const TargetParams &target,
+                   cudaStream_t stream) {
+	int tiles = bins.tilesX * bins.tilesY;
+	if (tiles > 0) { COUNT_LAUNCH(); raster_kernel<false><<<tiles, 256, 0, stream>>>(fb.records, fb.shades, textures, bins, target); }
+}
+
+void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream) {
+	int tiles = bins.tilesX * bins.tilesY;
+	if (tiles > 0) { COUNT_LAUNCH(); raster_kernel<true><<<tiles, 256, 0, stream>>>(fb.records, fb.shades, nullptr, bins, target); }
+}
+
+} // namespace dsrg

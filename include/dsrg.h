@@ -1,0 +1,139 @@
+/*
+ * dsrg: C ABI of the GB300 (sm_103a) implementation of DFPSR's triangle-rendering path.
+ *
+ * Plain C types only: pointers, sizes and status codes.  Every entry point names the
+ * reference interface it replaces (paths relative to the reference's Source/ directory).
+ * Every call returns DSRG_OK (0) or a nonzero status; dsrg_context_last_error() then holds
+ * a message whose prefix matches the reference's error text where the reference has one.
+ *
+ * Threading: a context, and everything created from it, is driven by one host thread at a
+ * time, like a dsr::Renderer (api/rendererAPI.h:54-55).  All work runs on the context's
+ * CUDA stream; the render calls return when their results are in the target images.
+ */
+#ifndef DSRG_H
+#define DSRG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define DSRG_OK 0
+#define DSRG_ERROR_INVALID_ARGUMENT 1
+#define DSRG_ERROR_CUDA 2
+#define DSRG_ERROR_OUT_OF_MEMORY 3
+#define DSRG_ERROR_CALL_ORDER 4
+#define DSRG_ERROR_UNSUPPORTED 5
+#define DSRG_ERROR_DEVICE 6
+
+/* Filter of a model (implementation/render/constants.h:33). */
+#define DSRG_FILTER_SOLID 0
+#define DSRG_FILTER_ALPHA 1
+
+/* PackOrderIndex of a colour image (implementation/image/PackOrder.h:37-42). */
+#define DSRG_PACK_RGBA 0
+#define DSRG_PACK_BGRA 1
+#define DSRG_PACK_ARGB 2
+#define DSRG_PACK_ABGR 3
+
+typedef struct dsrg_context_s *dsrg_context;
+typedef struct dsrg_texture_s *dsrg_texture;
+typedef struct dsrg_model_s *dsrg_model;
+typedef struct dsrg_renderer_s *dsrg_renderer;
+
+/* A camera as Camera::createPerspective / Camera::createOrthogonal build it
+ * (implementation/render/Camera.h:144-156).  location = position(3), xAxis(3), yAxis(3),
+ * zAxis(3) of the camera's Transform3D; slope = widthSlope (perspective) or halfWidth
+ * (orthogonal); nearClip/farClip are ignored for orthogonal cameras. */
+typedef struct {
+	float location[12];
+	int32_t perspective;
+	float slope;
+	float nearClip;
+	float farClip;
+	int32_t width;
+	int32_t height;
+} dsrg_camera;
+
+/* A target image: ImageRgbaU8 (4 bytes per pixel in packOrder) or ImageF32/AlignedImageF32
+ * (float per pixel) (implementation/image/Image.h:249-289).  data points to row 0;
+ * strideBytes is the distance between rows.  onDevice = 1 when data is device memory of the
+ * context's GPU; 0 when it is host memory (copied to the GPU and back inside the call;
+ * page-locked memory makes those copies asynchronous and faster). */
+typedef struct {
+	void *data;
+	int32_t width;
+	int32_t height;
+	int32_t strideBytes;
+	int32_t packOrder;
+	int32_t onDevice;
+} dsrg_image;
+
+/* Counters of the last render call (the unit of work of the benchmarks). */
+typedef struct {
+	uint64_t fragments;      /* (pixel, triangle) pairs inside the row intervals, before the depth test; 0 unless counting is on */
+	uint64_t drawRecords;    /* triangles left after culling, clipping and the front-face test */
+	uint64_t binEntries;     /* (tile, triangle) pairs */
+	float milliseconds;      /* GPU time of the last render from its first kernel to its last (CUDA events) */
+	float rasterMilliseconds;/* GPU time of the last render's tile raster kernel alone (CUDA events) */
+	uint64_t kernelLaunches; /* kernels this library has launched in this process so far */
+} dsrg_stats;
+
+/* ---- context ---- */
+int dsrg_context_create(int32_t device, dsrg_context *out);
+int dsrg_context_destroy(dsrg_context context);
+const char *dsrg_context_last_error(dsrg_context context);
+/* The cudaStream_t all work of the context is ordered on. */
+void *dsrg_context_stream(dsrg_context context);
+/* counting: 1 makes render calls count fragments (and, when coverage is a device buffer of
+ * width*height uint32, write the per-pixel fragment count there); 0 turns it off. */
+int dsrg_context_set_counting(dsrg_context context, int32_t counting, uint32_t *deviceCoverage);
+int dsrg_context_get_stats(dsrg_context context, dsrg_stats *out);
+
+/* ---- textures: texture_create_RgbaU8(image, resolutions) (api/textureAPI.h:450-465,
+ * api/textureAPI.cpp:89-131) for power-of-two images; the mip pyramid is the integer 2x2 box
+ * average of texture_generatePyramid (api/textureAPI.cpp:44-87). pixels: width*height RGBA
+ * bytes in memory order, host memory. ---- */
+int dsrg_texture_create(dsrg_context context, const uint32_t *pixels, int32_t width, int32_t height,
+                        int32_t resolutions, dsrg_texture *out);
+int dsrg_texture_destroy(dsrg_texture texture);
+/* Copies the pyramid (smallest level first) to host memory; fields = log2width, log2height,
+ * maxMipLevel, startOffset, maxLevelMask, minWidthOrMask, minHeightOrMask, maxWidthAndMask,
+ * maxHeightAndMask (implementation/image/Texture.h:42-61). Returns the texel count in *count. */
+int dsrg_texture_read(dsrg_texture texture, uint32_t *pixels, int32_t maxPixels, uint32_t *fields, int32_t *count);
+
+/* ---- models: model_create + model_addPoint/addTriangle/addQuad/setTexCoord/setVertexColor/
+ * setDiffuseMap/setLightMap/setFilter (api/modelAPI.h:62-258) in one call, one part.
+ * positions: pointCount x 3 floats; polygonIndices: polygonCount x 4 (index 3 = -1 for a
+ * triangle); texCoords and colors: polygonCount x 4 corners x 4 floats. Host memory. ---- */
+int dsrg_model_create(dsrg_context context, const float *positions, int32_t pointCount, const int32_t *polygonIndices,
+                      const float *texCoords, const float *colors, int32_t polygonCount, dsrg_texture diffuse,
+                      dsrg_texture light, int32_t filter, dsrg_model *out);
+int dsrg_model_destroy(dsrg_model model);
+
+/* ---- rendering ---- */
+/* model_render (api/modelAPI.h:285, api/modelAPI.cpp:197-201): draws the model into the colour
+ * and depth images; either may be null.  modelToWorld as in dsrg_camera.location. */
+int dsrg_model_render(dsrg_context context, dsrg_model model, const float *modelToWorld, const dsrg_camera *camera,
+                      const dsrg_image *color, const dsrg_image *depth);
+/* model_renderDepth (api/modelAPI.h:291, api/modelAPI.cpp:202-206). */
+int dsrg_model_render_depth(dsrg_context context, dsrg_model model, const float *modelToWorld,
+                            const dsrg_camera *camera, const dsrg_image *depth);
+
+/* renderer_create / renderer_begin / renderer_giveTask / renderer_end (api/rendererAPI.h:56-135,
+ * api/modelAPI.h:299-301): triangles of every task are drawn at renderer_end in submission
+ * order, with the same result as model_render of the tasks one after another. */
+int dsrg_renderer_create(dsrg_context context, dsrg_renderer *out);
+int dsrg_renderer_destroy(dsrg_renderer renderer);
+int dsrg_renderer_begin(dsrg_renderer renderer, const dsrg_image *color, const dsrg_image *depth);
+int dsrg_renderer_give_task(dsrg_renderer renderer, dsrg_model model, const float *modelToWorld, const dsrg_camera *camera);
+int dsrg_renderer_end(dsrg_renderer renderer);
+/* renderer_takesTriangles (api/rendererAPI.h:67): 1 between begin and end. */
+int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

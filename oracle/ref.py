@@ -43,6 +43,12 @@ def available(variant: str = "exact") -> bool:
 
 
 _libs = {}
+_shut_down = []
+
+
+def _shutdown(l):
+    _shut_down.append(True)
+    l.refh_shutdown()
 
 
 def _load(variant: str):
@@ -65,7 +71,7 @@ def _load(variant: str):
         l.refh_camera_to_screen.argtypes = [P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, P, P, P]
         l.refh_triangle_rows.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_int]
         l.refh_triangle_rows.restype = C.c_int
-        atexit.register(l.refh_shutdown)
+        atexit.register(_shutdown, l)
         _libs[variant] = l
     return _libs[variant]
 
@@ -89,6 +95,8 @@ class RefTexture:
         return fields, pixels
 
     def __del__(self):
+        if _shut_down:
+            return
         try:
             self.lib.refh_texture_free(self.handle)
         except Exception:
@@ -113,6 +121,8 @@ class RefModel:
         self.transform = np.ascontiguousarray(scene.model_to_world, np.float32)
 
     def __del__(self):
+        if _shut_down:
+            return
         try:
             self.lib.refh_model_free(self.handle)
         except Exception:
