@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -138,6 +139,10 @@ class Context:
         h = C.c_void_p()
         self._check(self._l.dsrg_context_create(device, C.byref(h)), None)
         self.handle = h
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, child):
+        self._children.add(child)
 
     def _check(self, status: int, handle=None):
         if status != DSRG_OK:
@@ -145,7 +150,13 @@ class Context:
             raise DsrgError(status, (msg or b"").decode())
 
     def close(self):
+        """Destroys the context after every model, texture and renderer made from it."""
         if getattr(self, "handle", None):
+            kids = list(self._children)
+            for kind in (Renderer, Model, Texture):
+                for child in kids:
+                    if isinstance(child, kind):
+                        child.destroy()
             self._l.dsrg_context_destroy(self.handle)
             self.handle = None
 
@@ -199,6 +210,7 @@ class Texture:
         ctx._check(ctx._l.dsrg_texture_create(ctx.handle, pixels.ctypes.data, pixels.shape[1], pixels.shape[0],
                                               resolutions, C.byref(h)))
         self.handle = h
+        ctx._adopt(self)
 
     def read(self):
         fields = np.zeros(9, np.uint32)
@@ -208,11 +220,14 @@ class Texture:
         self.ctx._check(self.ctx._l.dsrg_texture_read(self.handle, pixels.ctypes.data, count.value, None, None))
         return fields, pixels
 
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_texture_destroy(self.handle)
+        self.handle = None
+
     def __del__(self):
         try:
-            if self.handle:
-                self.ctx._l.dsrg_texture_destroy(self.handle)
-                self.handle = None
+            self.destroy()
         except Exception:
             pass
 
@@ -235,14 +250,18 @@ class Model:
                                             col.ctypes.data, poly.shape[0], diffuse.handle if diffuse else None,
                                             light.handle if light else None, scene.filter, C.byref(h)))
         self.handle = h
+        ctx._adopt(self)
         self.transform = np.ascontiguousarray(scene.model_to_world, np.float32)
         self.camera = camera_struct(scene)
 
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_model_destroy(self.handle)
+        self.handle = None
+
     def __del__(self):
         try:
-            if self.handle:
-                self.ctx._l.dsrg_model_destroy(self.handle)
-                self.handle = None
+            self.destroy()
         except Exception:
             pass
 
@@ -256,6 +275,7 @@ class Renderer:
         ctx._check(ctx._l.dsrg_renderer_create(ctx.handle, C.byref(h)))
         self.handle = h
         self._images = None
+        ctx._adopt(self)
 
     def begin(self, color=None, depth=None, pack_order: int = 0):
         ci, di = image_struct(color, pack_order), image_struct(depth)
@@ -275,11 +295,14 @@ class Renderer:
     def takes_triangles(self) -> bool:
         return bool(self.ctx._l.dsrg_renderer_takes_triangles(self.handle))
 
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_renderer_destroy(self.handle)
+        self.handle = None
+
     def __del__(self):
         try:
-            if self.handle:
-                self.ctx._l.dsrg_renderer_destroy(self.handle)
-                self.handle = None
+            self.destroy()
         except Exception:
             pass
 

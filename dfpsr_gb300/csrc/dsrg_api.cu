@@ -132,6 +132,8 @@ struct dsrg_context_s {
 	DeviceBuffer<uint32_t> stagingColor;
 	DeviceBuffer<float> stagingDepth;
 	DeviceBuffer<unsigned long long> fragmentCounter;
+	DeviceBuffer<unsigned long long> keys;
+	int32_t smallRows = 8, smallWidth = 16; // thread-per-triangle path for raster bounds up to 8 x 16 pixels
 	int32_t counting = 0;
 	uint32_t *coverage = nullptr;
 	dsrg_stats stats;
@@ -230,6 +232,7 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();
 	ctx->records.release(); ctx->shades.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
+	ctx->keys.release();
 	cudaEventDestroy(ctx->eventStart);
 	cudaEventDestroy(ctx->eventStop);
 	cudaEventDestroy(ctx->eventRasterStart);
@@ -621,12 +624,13 @@ static int end_frame(dsrg_renderer r) {
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	fb.scanScratch = ctx->scanScratch.ptr;
 	fb.scanScratchElems = ctx->scanScratch.capacity;
-	uint32_t entries = launch_bin_count(fb, recordCount, bins, ctx->stream);
+	const int32_t smallRows = r->depthOnly ? 0 : ctx->smallRows, smallWidth = ctx->smallWidth;
+	uint32_t entries = launch_bin_count(fb, recordCount, bins, smallRows, smallWidth, ctx->stream);
 	CUDA_TRY(ctx, cudaGetLastError());
 	CUDA_TRY(ctx, ctx->binLists.reserve((size_t)entries + 1));
 	bins.lists = ctx->binLists.ptr;
 	bins.listCapacity = ctx->binLists.capacity;
-	launch_bin_fill(fb, recordCount, bins, ctx->stream);
+	launch_bin_fill(fb, recordCount, bins, smallRows, smallWidth, ctx->stream);
 	TargetParams tg;
 	memset(&tg, 0, sizeof(tg));
 	tg.color = r->hasColor ? r->deviceColor : nullptr;
@@ -637,14 +641,25 @@ static int end_frame(dsrg_renderer r) {
 	tg.width = r->width;
 	tg.height = r->height;
 	tg.affine = r->affine ? 1 : 0;
+	tg.smallRows = smallRows;
+	tg.smallWidth = smallWidth;
+	const size_t pixels = (size_t)r->width * r->height;
+	CUDA_TRY(ctx, ctx->keys.reserve(pixels));
+	CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
+	tg.keys = ctx->keys.ptr;
 	if (ctx->counting) {
 		CUDA_TRY(ctx, cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), ctx->stream));
 		tg.fragments = ctx->fragmentCounter.ptr;
 		tg.coverage = ctx->coverage;
+		if (tg.coverage) CUDA_TRY(ctx, cudaMemsetAsync(tg.coverage, 0, pixels * sizeof(uint32_t), ctx->stream));
 	}
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStart, ctx->stream));
-	if (r->depthOnly) launch_raster_depth_only(fb, bins, tg, ctx->stream);
-	else launch_raster(fb, ctx->textureTable.ptr, bins, tg, ctx->stream);
+	if (r->depthOnly) {
+		launch_raster_depth_only(fb, bins, tg, ctx->stream);
+	} else {
+		launch_small_raster(fb, recordCount, tg, ctx->stream);
+		launch_raster(fb, ctx->textureTable.ptr, bins, tg, ctx->stream);
+	}
 	CUDA_TRY(ctx, cudaGetLastError());
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStop, ctx->stream));
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStop, ctx->stream));

@@ -72,6 +72,11 @@ DSRG_HD float i64_to_float(int64_t v) {
 // that the current value does not have).  Those boundary steps are taken one at
 // a time with a real float addition.
 DSRG_HD float chain_add(float s, float d, int32_t n) {
+	if (n <= 6) {
+		// short chains (small triangles, quads near a row's start) are cheaper step by step
+		for (int32_t i = 0; i < n; i++) s = fadd(s, d);
+		return s;
+	}
 	for (int guard = 0; n > 0 && guard < 96; guard++) {
 		uint32_t sb = fbits(s), db = fbits(d);
 		int32_t se = (int32_t)((sb >> 23) & 0xFFu), de = (int32_t)((db >> 23) & 0xFFu);

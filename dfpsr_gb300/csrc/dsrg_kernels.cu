@@ -289,11 +289,15 @@ __device__ __forceinline__ void record_tiles(const DrawRecord &r, const TileBins
 }
 
 template <bool FILL>
-__global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, TileBins bins, int32_t *errorFlag) {
+__global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, TileBins bins, int32_t *errorFlag,
+                           int32_t smallRows, int32_t smallWidth) {
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
 	int32_t tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1;
-	if (r < recordCount) record_tiles(records[r], bins, tx0, tx1, ty0, ty1);
+	if (r < recordCount) {
+		const DrawRecord rec = records[r];
+		if (!record_is_small(rec, smallRows, smallWidth)) record_tiles(rec, bins, tx0, tx1, ty0, ty1);
+	}
 	const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
 	const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
 	const bool big = tiles > 4;
@@ -337,10 +341,11 @@ __global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, Tile
 	}
 }
 
-uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                          cudaStream_t stream) {
 	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
 	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * tiles, stream);
-	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag); }
+	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth); }
 	launch_scan(bins.counts, bins.offsets, tiles, fb.scanScratch, fb.scanScratchElems, stream);
 	uint32_t total = 0;
 	cudaMemcpyAsync(&total, bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
@@ -348,10 +353,11 @@ uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins
 	return total;
 }
 
-void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                     cudaStream_t stream) {
 	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
 	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * tiles, stream);
-	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag); }
+	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth); }
 }
 
 // ------------------------------------------------------------------ rasterisation
@@ -457,8 +463,9 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 	const bool depthTest = tg.depth != nullptr;
 	const bool affine = tg.affine != 0;
 	initialDepth[tid] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
-	keys[tid] = 0ull;
-	coverage[tid] = 0u;
+	// small triangles were already resolved into the global keys by small_raster_kernel
+	keys[tid] = (inside && tg.keys) ? tg.keys[(size_t)py * tg.width + px] : 0ull;
+	coverage[tid] = (inside && tg.coverage) ? tg.coverage[(size_t)py * tg.width + px] : 0u;
 	if (tid == 0) fragmentSum = 0ull;
 	__syncthreads();
 
@@ -573,6 +580,83 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 		}
 	}
 	if (tg.fragments && tid == 0) atomicAdd(tg.fragments, fragmentSum);
+}
+
+// One thread draws one small record, walking its row pairs and quads exactly as fillShapeSuper
+// does (fillerTemplates.h:246-385), so that every value is the reference's own running sum.
+// Depth tests resolve through the same 64-bit keys as the tile kernel, in global memory.
+__device__ __forceinline__ void small_quad(const TargetParams &tg, const RowPair &pair, int32_t x, int32_t y1, bool edge,
+                                           const float *z, uint32_t record, bool depthTest, bool affine, uint32_t &fragments) {
+	for (int l = 0; l < 4; l++) {
+		const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+		bool covered;
+		if (l < 2) covered = !edge || (xx >= pair.upperLeft && xx < pair.upperRight);
+		else covered = !edge || (xx >= pair.lowerLeft && xx < pair.lowerRight);
+		if (!covered || yy >= tg.height || xx >= tg.width) continue;
+		fragments++;
+		const size_t pix = (size_t)yy * tg.width + xx;
+		if (tg.coverage) atomicAdd(&tg.coverage[pix], 1u);
+		bool pass = true;
+		if (depthTest) {
+			const float old = tg.depth[(size_t)yy * tg.depthStride + xx];
+			pass = affine ? (z[l] < old) : (z[l] > old);
+		}
+		if (pass) {
+			const unsigned long long key = make_key(z[l], record, depthTest, affine);
+			if (key > tg.keys[pix]) atomicMax(&tg.keys[pix], key);
+		}
+	}
+}
+
+__global__ void __launch_bounds__(256) small_raster_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, TargetParams tg) {
+	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t fragments = 0;
+	if (ri < recordCount) {
+		const DrawRecord r = records[ri];
+		if (record_is_small(r, tg.smallRows, tg.smallWidth)) {
+			const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
+			const float dx = r.dx[0], d2 = fmul(dx, 2.0f);
+			for (int32_t y1 = r.top; y1 < r.bottom; y1 += 2) {
+				const RowPair pair = record_row_pair(r, y1, tg.height);
+				if (!pair.any) continue;
+				float U = fadd(fadd(r.start[0], fmul(dx, (float)pair.obs + 0.5f)), fmul(r.dy[0], (float)y1 + 0.5f));
+				float L = fadd(U, r.dy[0]);
+				float z[4];
+				const bool allEdge = pair.ibe <= pair.ibs;
+				const int32_t leftEnd = allEdge ? pair.obe : pair.ibs;
+				int32_t x = pair.obs;
+				for (; x < leftEnd; x += 2) {
+					z[0] = U; z[1] = fadd(U, dx); z[2] = L; z[3] = fadd(L, dx);
+					small_quad(tg, pair, x, y1, true, z, ri, depthTest, affine, fragments);
+					U = fadd(U, d2); L = fadd(L, d2);
+				}
+				if (!allEdge) {
+					float v[4] = {U, fadd(U, dx), L, fadd(L, dx)};
+					for (; x < pair.ibe; x += 2) {
+						small_quad(tg, pair, x, y1, false, v, ri, depthTest, affine, fragments);
+						for (int l = 0; l < 4; l++) v[l] = fadd(v[l], d2);
+					}
+					const float m = fmul(d2, (float)((pair.ibe - pair.ibs) >> 1));
+					U = fadd(U, m); L = fadd(L, m);
+					for (; x < pair.obe; x += 2) {
+						z[0] = U; z[1] = fadd(U, dx); z[2] = L; z[3] = fadd(L, dx);
+						small_quad(tg, pair, x, y1, true, z, ri, depthTest, affine, fragments);
+						U = fadd(U, d2); L = fadd(L, d2);
+					}
+				}
+			}
+		}
+	}
+	if (tg.fragments) {
+		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
+		if ((threadIdx.x & 31) == 0 && fragments) atomicAdd(tg.fragments, (unsigned long long)fragments);
+	}
+}
+
+void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream) {
+	if (recordCount == 0 || target.smallRows <= 0) return;
+	COUNT_LAUNCH();
+	small_raster_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, target);
 }
 
 void launch_raster(const FrameBuffers &fb, const TextureData *textures, const TileBins &bins, const TargetParams &target,

@@ -57,9 +57,17 @@ struct TargetParams {
 	int32_t depthStride;
 	int32_t width, height;
 	int32_t affine;           // orthogonal camera: depth test '<' on linear depth
-	uint32_t *coverage;       // optional per-pixel fragment counts
+	uint32_t *coverage;       // optional per-pixel fragment counts (width * height, dense)
 	unsigned long long *fragments; // optional fragment total
+	unsigned long long *keys; // width * height depth keys shared by the small-triangle and tile kernels
+	int32_t smallRows;        // records whose raster bound is at most smallRows x smallWidth pixels are
+	int32_t smallWidth;       // drawn by one thread each instead of one warp per covered tile
 };
+
+// True when one thread draws the whole record (dsrg small-triangle path).
+__host__ __device__ inline bool record_is_small(const DrawRecord &r, int32_t smallRows, int32_t smallWidth) {
+	return (r.bottom - r.top) <= smallRows && (r.right - r.left) <= smallWidth;
+}
 
 enum ErrorBits : int32_t {
 	ERROR_RECORD_OVERFLOW = 1,
@@ -72,10 +80,16 @@ void launch_project(const TaskParams &task, const FrameBuffers &fb, cudaStream_t
 void launch_setup(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream);
 // Bins the first *recordCount records into tiles.  Returns the number of list entries needed
 // (reads it back, synchronising the stream) so that the caller can grow the list buffer.
-uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
-void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
+// Small records (record_is_small with smallRows/smallWidth) are left out of the bins; pass
+// smallRows = 0 to bin every record.
+uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                          cudaStream_t stream);
+void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                     cudaStream_t stream);
 void launch_raster(const FrameBuffers &fb, const TextureData *textures, const TileBins &bins,
                    const TargetParams &target, cudaStream_t stream);
+// Draws every small record with one thread each into target.keys (before launch_raster).
+void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream);
 void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total).
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);
