@@ -125,7 +125,7 @@ struct dsrg_context_s {
 	DeviceBuffer<int64_t> flatx, flaty;
 	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
 	DeviceBuffer<DrawRecord> records;
-	DeviceBuffer<ShadeRecord> shades;
+	DeviceBuffer<TaskData> taskTable;
 	DeviceBuffer<uint32_t> control;      // [0] record count, [1] error flag
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
 	DeviceBuffer<TextureData> textureTable;
@@ -178,6 +178,7 @@ struct dsrg_renderer_s {
 	bool cameraKnown = false;
 	std::vector<TextureData> textures;
 	std::vector<dsrg_texture> textureHandles;
+	std::vector<TaskData> tasks;
 };
 
 #define CUDA_TRY(ctx, expr)                                                                      \
@@ -231,7 +232,7 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();
-	ctx->records.release(); ctx->shades.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
+	ctx->records.release(); ctx->taskTable.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
 	ctx->keys.release();
 	cudaEventDestroy(ctx->eventStart);
 	cudaEventDestroy(ctx->eventStop);
@@ -499,6 +500,7 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 	r->cameraKnown = false;
 	r->textures.clear();
 	r->textureHandles.clear();
+	r->tasks.clear();
 	CUDA_TRY(ctx, cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream));
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStart, ctx->stream));
 	r->receiving = true;
@@ -542,7 +544,7 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	task.pointCount = m->pointCount;
 	task.triangleCount = m->triangleCount;
 	task.orderBase = r->triangleCount;
-	task.shadeBase = r->triangleCount;
+	task.taskIndex = (uint32_t)r->tasks.size();
 	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
 	task.camera = cam;
 	task.width = r->width;
@@ -553,6 +555,15 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	task.diffuse = r->depthOnly ? -1 : texture_slot(r, m->diffuse);
 	task.light = r->depthOnly ? -1 : texture_slot(r, m->light);
 	task.depthOnly = r->depthOnly ? 1 : 0;
+	TaskData td;
+	td.polygons = m->polygons;
+	td.texCoords = m->texCoords;
+	td.colors = m->colors;
+	td.triSource = m->triSource;
+	td.diffuse = task.diffuse;
+	td.light = task.light;
+	td.filter = m->filter;
+	td.pad = 0;
 	size_t np = (size_t)m->pointCount, nt = (size_t)m->triangleCount;
 	CUDA_TRY(ctx, ctx->csx.reserve(np)); CUDA_TRY(ctx, ctx->csy.reserve(np)); CUDA_TRY(ctx, ctx->csz.reserve(np));
 	CUDA_TRY(ctx, ctx->isx.reserve(np)); CUDA_TRY(ctx, ctx->isy.reserve(np));
@@ -564,7 +575,6 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	// A triangle clipped against six planes is a fan of at most seven triangles.
 	size_t needed = (size_t)r->triangleCount * 7 + nt * 7;
 	CUDA_TRY(ctx, ctx->records.reserve(needed, true, (size_t)r->triangleCount * 7, ctx->stream));
-	CUDA_TRY(ctx, ctx->shades.reserve((size_t)r->triangleCount + nt, true, r->triangleCount, ctx->stream));
 	r->recordCapacity = (uint32_t)ctx->records.capacity;
 	FrameBuffers fb;
 	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
@@ -573,11 +583,11 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	fb.triCounts = ctx->triCounts.ptr;
 	fb.triOffsets = ctx->triOffsets.ptr;
 	fb.records = ctx->records.ptr;
-	fb.shades = ctx->shades.ptr;
 	fb.recordCount = ctx->control.ptr;
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	fb.scanScratch = ctx->scanScratch.ptr;
 	fb.scanScratchElems = ctx->scanScratch.capacity;
+	r->tasks.push_back(td);
 	launch_project(task, fb, ctx->stream);
 	launch_setup(task, fb, r->recordCapacity, ctx->stream);
 	CUDA_TRY(ctx, cudaGetLastError());
@@ -611,6 +621,10 @@ static int end_frame(dsrg_renderer r) {
 	if (!r->textures.empty())
 		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->textureTable.ptr, r->textures.data(), r->textures.size() * sizeof(TextureData),
 		                              cudaMemcpyHostToDevice, ctx->stream));
+	CUDA_TRY(ctx, ctx->taskTable.reserve(r->tasks.size() + 1));
+	if (!r->tasks.empty())
+		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->taskTable.ptr, r->tasks.data(), r->tasks.size() * sizeof(TaskData),
+		                              cudaMemcpyHostToDevice, ctx->stream));
 	bins.counts = ctx->binCounts.ptr;
 	bins.offsets = ctx->binOffsets.ptr;
 	bins.cursors = ctx->binCursors.ptr;
@@ -619,7 +633,6 @@ static int end_frame(dsrg_renderer r) {
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
 	fb.records = ctx->records.ptr;
-	fb.shades = ctx->shades.ptr;
 	fb.recordCount = ctx->control.ptr;
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	fb.scanScratch = ctx->scanScratch.ptr;
@@ -658,7 +671,8 @@ static int end_frame(dsrg_renderer r) {
 		launch_raster_depth_only(fb, bins, tg, ctx->stream);
 	} else {
 		launch_small_raster(fb, recordCount, tg, ctx->stream);
-		launch_raster(fb, ctx->textureTable.ptr, bins, tg, ctx->stream);
+		launch_raster(fb, ctx->taskTable.ptr, ctx->textureTable.ptr, bins, tg, ctx->stream);
+		launch_small_shade(fb, recordCount, ctx->taskTable.ptr, ctx->textureTable.ptr, tg, ctx->stream);
 	}
 	CUDA_TRY(ctx, cudaGetLastError());
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStop, ctx->stream));

@@ -96,14 +96,15 @@ DSRG_HD float chain_add(float s, float d, int32_t n) {
 			return s;
 		}
 		const int32_t e0 = se < de ? se : de;
-		const int64_t U = (int64_t)1 << (se - e0);       // ulp(s) in units of 2^(e0-150)
-		const int64_t S = M << (se - e0);                 // s in those units
+		const int32_t ushift = se - e0;
+		const int64_t U = (int64_t)1 << ushift;           // ulp(s) in units of 2^(e0-150)
+		const int64_t S = M << ushift;                    // s in those units
 		const int64_t D = Dm * ((int64_t)1 << (de - e0)); // d in those units
-		const int64_t lo = (int64_t)1 << (23 + se - e0);  // bottom of the binade of |s|
+		const int64_t lo = (int64_t)1 << (23 + ushift);   // bottom of the binade of |s|
 		const int64_t hi = lo << 1;
-		// floor division of D by U (U is a power of two)
-		int64_t a = D >= 0 ? D / U : -((-D + U - 1) / U);
-		int64_t r = D - a * U;                            // 0 <= r < U
+		// floor division of D by the power of two U
+		int64_t a = D >> ushift;
+		int64_t r = D - (a << ushift);                    // 0 <= r < U
 		int64_t inc;
 		if (U == 1) {
 			inc = a;
@@ -123,11 +124,25 @@ DSRG_HD float chain_add(float s, float d, int32_t n) {
 		if (X0 < lo || X0 >= hi) { s = fadd(s, d); n--; continue; }
 		const int64_t INC = inc * U;
 		if (INC == 0) return s;
+		// m = number of steps that stay in the binade: the largest m with every k < m valid.
+		// A binary32 estimate of the quotient, corrected with exact products (no 64-bit division).
 		int64_t m;
-		if (INC > 0) {
-			m = (hi - X0 + INC - 1) / INC;
-		} else {
-			m = (X0 - lo) / (-INC) + 1;
+		{
+			const int64_t room = INC > 0 ? hi - X0 : X0 - lo; // > 0 for INC > 0, >= 0 for INC < 0
+			const int64_t step = INC > 0 ? INC : -INC;
+			int64_t q = (int64_t)fdiv(i64_to_float(room), i64_to_float(step));
+			if (q < 0) q = 0;
+			// INC > 0: count of k >= 0 with k * step < room, i.e. ceil(room / step)
+			// INC < 0: count of k >= 0 with k * step <= room, i.e. floor(room / step) + 1
+			if (INC > 0) {
+				while (q > 0 && (q - 1) * step >= room) q--;
+				while (q * step < room) q++;
+			} else {
+				while (q > 0 && q * step > room) q--;
+				while ((q + 1) * step <= room) q++;
+				q += 1;
+			}
+			m = q;
 		}
 		const int64_t steps = m < (int64_t)n ? m : (int64_t)n;
 		const int64_t S2 = S + steps * INC;

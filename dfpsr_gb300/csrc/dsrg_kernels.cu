@@ -1,21 +1,23 @@
 // CUDA kernels of the DFPSR triangle path for sm_103a.
 //
 // Pipeline per frame:
-//   project_kernel      Camera::worldToScreen for every model point (implementation/render/Camera.h:157-190)
-//   setup_kernel<false> per fan triangle: cull, clip, front-face; counts its draw records
-//   scan                record offsets, so that records land in submission order
-//   setup_kernel<true>  writes DrawRecords (bound, sub-pixel corners, projection) and ShadeRecords
-//   bin kernels         per 16x16 tile lists of the records whose raster bound touches it
-//   raster kernels      one CTA per tile: exact row intervals, exact accumulated depth, depth
-//                       test resolved with 64-bit shared-memory atomicMax keys, then deferred
-//                       shading of the winning fragment of every pixel.
+//   project_kernel       Camera::worldToScreen for every model point (implementation/render/Camera.h:157-190)
+//   setup_kernel<false>  per fan triangle: cull, clip, front-face; counts its draw records
+//   scan                 record offsets, so that records land in submission order
+//   setup_kernel<true>   writes the DrawRecords (bound, sub-pixel corners, projection)
+//   bin kernels          per 16x16 tile lists of the large records whose raster bound touches it
+//   small_raster_kernel  one thread per small record: depth keys into a global key image
+//   raster_kernel        one CTA per tile: depth keys of the large records in shared memory, merged
+//                        with the global keys; shades the pixels that large records won
+//   small_shade_kernel   one thread per small record: shades the pixels that small records won
 //
 // Why the depth test can run out of order: the reference writes a fragment when its depth is
 // strictly greater (1/W, perspective) or smaller (linear, orthogonal) than the stored one
 // (implementation/render/shader/fillerTemplates.h:108-152).  After any sequence of opaque
 // triangles the stored value is the extreme depth over all fragments that beat the initial
 // value, and the colour is the earliest fragment reaching it.  Packing (depth, ~record index)
-// into one 64-bit key and taking the maximum reproduces exactly that, in any order.
+// into one 64-bit key and taking the maximum reproduces exactly that, in any order, because
+// records are stored in submission order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -59,17 +61,13 @@ struct Corner {
 // Emits one draw command (renderCore.cpp:203-217 executeTriangleDrawing against the whole target):
 // the triangle bound cut to the target with rows aligned to pairs (ITriangle2D.cpp:70-75).
 template <bool WRITE>
-__device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity,
-                            const Corner *c, const float *subB, const float *subC, uint32_t order, uint32_t shade,
-                            uint32_t base, uint32_t &emitted) {
+__device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, const Corner *c,
+                            const float *subB, const float *subC, uint32_t order, uint32_t tri, uint32_t base,
+                            uint32_t &emitted) {
 	int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
 	int32_t b[4];
 	triangle_bound(fx, fy, b);
 	if (!(b[0] < task.width && b[2] > 0 && b[1] < task.height && b[3] > 0)) return;
-	int32_t left = b[0] > 0 ? b[0] : 0, top = b[1] > 0 ? b[1] : 0;
-	int32_t right = b[2] < task.width ? b[2] : task.width, bottom = b[3] < task.height ? b[3] : task.height;
-	top = top & ~1;                 // roundDown(top, 2) for top >= 0
-	bottom = (bottom + 1) & ~1;     // roundUp(bottom, 2)
 	if (WRITE) {
 		uint32_t index = base + emitted;
 		if (index >= recordCapacity) {
@@ -83,14 +81,17 @@ __device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint
 				r.flat[i * 2 + 1] = (int32_t)fy[i];
 			}
 			if (!inRange) atomicOr(fb.errorFlag, ERROR_COORDINATE_RANGE);
-			r.left = left; r.top = top; r.right = right; r.bottom = bottom;
+			r.left = b[0] > 0 ? b[0] : 0;
+			r.top = (b[1] > 0 ? b[1] : 0) & ~1;                                       // roundDown(top, 2)
+			r.right = b[2] < task.width ? b[2] : task.width;
+			r.bottom = ((b[3] < task.height ? b[3] : task.height) + 1) & ~1;          // roundUp(bottom, 2)
 			float isx[3] = {c[0].isx, c[1].isx, c[2].isx}, isy[3] = {c[0].isy, c[1].isy, c[2].isy};
 			float csz[3] = {c[0].cs.z, c[1].cs.z, c[2].cs.z};
 			triangle_projection(isx, isy, csz, subB, subC, task.camera.perspective != 0, r.start, r.dx, r.dy);
 			r.order = order;
-			r.shade = shade;
+			r.tri = tri;
+			r.task = task.taskIndex;
 			r.flags = task.camera.perspective ? 0u : RECORD_AFFINE;
-			r.pad = 0;
 			fb.records[index] = r;
 		}
 	}
@@ -99,7 +100,7 @@ __device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint
 
 // renderTriangleFromData / renderTriangleFromDataDepth for one fan triangle (renderCore.cpp:220-341, 400-443).
 template <bool WRITE>
-__global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCapacity) {
+__global__ void __launch_bounds__(256) setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCapacity) {
 	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= task.triangleCount) return;
 	uint32_t emitted = 0;
@@ -115,35 +116,12 @@ __global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCa
 		c[i].fx = fb.points.flatx[pi]; c[i].fy = fb.points.flaty[pi];
 	}
 	const uint32_t order = (task.orderBase + (uint32_t)t) * 8u;
-	const uint32_t shadeIndex = task.shadeBase + (uint32_t)t;
 	bool visible = triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, false) != 0;
-	if (visible && !task.depthOnly) {
-		const float *col[3];
-		for (int i = 0; i < 3; i++) col[i] = task.colors + (p * 4 + corner[i]) * 4;
-		if (task.filter == 1 && almost_zero(col[0][3]) && almost_zero(col[1][3]) && almost_zero(col[2][3])) visible = false;
-		if (visible && WRITE) {
-			// RgbaMultiply_data and the variant choice (shader/RgbaMultiply.h:37-58, 110-173).
-			ShadeRecord s;
-			float scale = 255.0f;
-			if (task.diffuse >= 0) scale = fmul(scale, 1.0f / 255.0f);
-			if (task.light >= 0) scale = fmul(scale, 1.0f / 255.0f);
-			for (int i = 0; i < 3; i++) {
-				s.red[i] = fmul(col[i][0], scale); s.green[i] = fmul(col[i][1], scale);
-				s.blue[i] = fmul(col[i][2], scale); s.alpha[i] = fmul(col[i][3], scale);
-				const float *tc = task.texCoords + (p * 4 + corner[i]) * 4;
-				s.u1[i] = tc[0]; s.v1[i] = tc[1]; s.u2[i] = tc[2]; s.v2[i] = tc[3];
-			}
-			bool fade = !(almost_same3(s.red) && almost_same3(s.green) && almost_same3(s.blue) && almost_same3(s.alpha));
-			bool colorless = almost_one3(s.red) && almost_one3(s.green) && almost_one3(s.blue) && almost_one3(s.alpha);
-			bool hasDiffuse = task.diffuse >= 0, hasLight = task.light >= 0;
-			if (fade || (hasDiffuse == hasLight)) colorless = false;
-			s.flags = (hasDiffuse ? SHADE_DIFFUSE : 0u) | (hasLight ? SHADE_LIGHT : 0u) | (fade ? SHADE_VERTEX_FADE : 0u) |
-			          (colorless ? SHADE_COLORLESS : 0u) | (task.filter == 1 ? SHADE_ALPHA_FILTER : 0u);
-			s.diffuse = task.diffuse;
-			s.light = task.light;
-			s.pad = 0;
-			fb.shades[shadeIndex] = s;
-		}
+	if (visible && !task.depthOnly && task.filter == 1) {
+		// renderTriangleFromData skips alpha-filtered triangles whose three alphas are almost zero (renderCore.cpp:319)
+		const float *col = task.colors + p * 16;
+		if (almost_zero(col[corner[0] * 4 + 3]) && almost_zero(col[corner[1] * 4 + 3]) && almost_zero(col[corner[2] * 4 + 3]))
+			visible = false;
 	}
 	if (visible && (task.hasColor || task.hasDepth)) {
 		const float defaultB[3] = {0.0f, 1.0f, 0.0f}, defaultC[3] = {0.0f, 0.0f, 1.0f};
@@ -152,7 +130,7 @@ __global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCa
 			int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
 			if (is_frontfacing(fx, fy)) {
 				emit_record<WRITE>(task, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
-				                   task.depthOnly ? zero3 : defaultC, order, shadeIndex, base, emitted);
+				                   task.depthOnly ? zero3 : defaultC, order, (uint32_t)t, base, emitted);
 			}
 		} else {
 			ClippedPolygon poly;
@@ -174,7 +152,7 @@ __global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCa
 					float sb[3] = {sv[0]->subB, sv[1]->subB, sv[2]->subB};
 					float scc[3] = {sv[0]->subC, sv[1]->subC, sv[2]->subC};
 					emit_record<WRITE>(task, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
-					                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, shadeIndex, base, emitted);
+					                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, (uint32_t)t, base, emitted);
 				}
 			}
 		}
@@ -184,8 +162,7 @@ __global__ void setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCa
 
 __global__ void advance_record_count_kernel(FrameBuffers fb, int32_t triangleCount) {
 	// triOffsets[triangleCount] holds this task's total; [triangleCount + 1] the records before it.
-	uint32_t before = fb.triOffsets[triangleCount + 1];
-	*fb.recordCount = before + fb.triOffsets[triangleCount];
+	*fb.recordCount = fb.triOffsets[triangleCount + 1] + fb.triOffsets[triangleCount];
 }
 
 __global__ void load_record_base_kernel(FrameBuffers fb, int32_t triangleCount) {
@@ -264,7 +241,6 @@ void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratc
 	uint32_t blocks = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
 	uint32_t *blockSums = scratch;
 	uint32_t *blockOffsets = scratch + blocks + 1;
-	(void)scratchElems;
 	COUNT_LAUNCH();
 	scan_blocks_kernel<<<blocks, SCAN_BLOCK, 0, stream>>>(in, out, n, blockSums);
 	if (blocks > 1) {
@@ -288,6 +264,9 @@ __device__ __forceinline__ void record_tiles(const DrawRecord &r, const TileBins
 	if (ty1 >= bins.tilesY) ty1 = bins.tilesY - 1;
 }
 
+// Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs of the large records.
+// Records touching at most 4 tiles are walked by their own thread, with the atomics of threads
+// that hit the same tile merged into one; larger ones are walked by the whole warp.
 template <bool FILL>
 __global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, TileBins bins, int32_t *errorFlag,
                            int32_t smallRows, int32_t smallWidth) {
@@ -301,28 +280,22 @@ __global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, Tile
 	const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
 	const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
 	const bool big = tiles > 4;
-	// small records: each thread walks its own few tiles, with the atomics of threads that hit
-	// the same tile merged into one (neighbouring triangles of a mesh usually share tiles)
-	{
-		for (int32_t i = 0; i < 4; i++) {
-			bool active = !big && i < tiles;
-			uint32_t tile = active ? (uint32_t)((ty0 + i / w) * bins.tilesX + tx0 + i % w) : 0xFFFFFFFFu;
-			uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
-			if (active) {
-				uint32_t leader = __ffs(peers) - 1;
-				uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-				uint32_t count = __popc(peers);
-				uint32_t baseSlot = 0;
-				if (lane == leader) baseSlot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], count);
-				baseSlot = __shfl_sync(peers, baseSlot, leader);
-				if (FILL) {
-					uint32_t slot = bins.offsets[tile] + baseSlot + rank;
-					if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
-				}
+	for (int32_t i = 0; i < 4; i++) {
+		bool active = !big && i < tiles;
+		uint32_t tile = active ? (uint32_t)((ty0 + i / w) * bins.tilesX + tx0 + i % w) : 0xFFFFFFFFu;
+		uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
+		if (active) {
+			uint32_t leader = __ffs(peers) - 1;
+			uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+			uint32_t baseSlot = 0;
+			if (lane == leader) baseSlot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], (uint32_t)__popc(peers));
+			baseSlot = __shfl_sync(peers, baseSlot, leader);
+			if (FILL) {
+				uint32_t slot = bins.offsets[tile] + baseSlot + rank;
+				if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
 			}
 		}
 	}
-	// big records: the whole warp walks each one's tiles together
 	uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
 	while (bigMask) {
 		uint32_t src = __ffs(bigMask) - 1;
@@ -345,7 +318,10 @@ uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins
                           cudaStream_t stream) {
 	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
 	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * tiles, stream);
-	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth); }
+	if (recordCount > 0) {
+		COUNT_LAUNCH();
+		bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth);
+	}
 	launch_scan(bins.counts, bins.offsets, tiles, fb.scanScratch, fb.scanScratchElems, stream);
 	uint32_t total = 0;
 	cudaMemcpyAsync(&total, bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
@@ -357,10 +333,13 @@ void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bin
                      cudaStream_t stream) {
 	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
 	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * tiles, stream);
-	if (recordCount > 0) { COUNT_LAUNCH(); bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth); }
+	if (recordCount > 0) {
+		COUNT_LAUNCH();
+		bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth);
+	}
 }
 
-// ------------------------------------------------------------------ rasterisation
+// ------------------------------------------------------------------ shared raster pieces
 
 // Block bounds of one row pair (fillerTemplates.h:273-293).
 struct RowPair {
@@ -381,6 +360,14 @@ __device__ __forceinline__ RowPair make_row_pair(int32_t uL, int32_t uR, int32_t
 	rp.upperLeft = uL; rp.upperRight = uR; rp.lowerLeft = lL; rp.lowerRight = lR;
 	rp.any = (uR > uL) || (lR > lL);
 	return rp;
+}
+
+// Row pair of record r for the rows y1, y1 + 1.
+__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, int32_t y1, int32_t height) {
+	int32_t uL, uR, lL, lR;
+	row_interval(r.flat, y1, r.left, r.right, uL, uR);
+	row_interval(r.flat, y1 + 1, r.left, r.right, lL, lR);
+	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
 }
 
 // The four lane values of one component (1/W or W, U/W, V/W) for the quad at x, following the
@@ -414,13 +401,15 @@ __device__ __forceinline__ void quad_lanes(float start, float dx, float dy, cons
 	}
 }
 
-// Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106).
-__device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, int l) {
-	const bool edge = (rp.ibe <= rp.ibs) || x < rp.ibs || x >= rp.ibe;
+__device__ __forceinline__ bool quad_is_edge(const RowPair &rp, int32_t x) {
+	return (rp.ibe <= rp.ibs) || x < rp.ibs || x >= rp.ibe;
+}
+
+// Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106); full quads draw all four.
+__device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, bool edge, int l) {
+	if (!edge) return true;
 	const int32_t xx = x + (l & 1);
-	if (l < 2) return edge ? (xx >= rp.upperLeft && xx < rp.upperRight) : true;
-	// Inner quads draw both rows unconditionally.
-	return edge ? (xx >= rp.lowerLeft && xx < rp.lowerRight) : true;
+	return (l < 2) ? (xx >= rp.upperLeft && xx < rp.upperRight) : (xx >= rp.lowerLeft && xx < rp.lowerRight);
 }
 
 __device__ __forceinline__ uint32_t ordered_depth(float z) {
@@ -440,48 +429,225 @@ __device__ __forceinline__ uint32_t key_record(unsigned long long key, bool dept
 	return depthTest ? ~(uint32_t)(key & 0xFFFFFFFFull) : (uint32_t)key - 1u;
 }
 
-// Row pair of record r for the rows y1, y1 + 1.
-__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, int32_t y1, int32_t height) {
-	int32_t uL, uR, lL, lR;
-	row_interval(r.flat, y1, r.left, r.right, uL, uR);
-	row_interval(r.flat, y1 + 1, r.left, r.right, lL, lR);
-	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
+// RgbaMultiply_data and its variant (shader/RgbaMultiply.h:37-58, 110-173) for fan triangle `tri`.
+__device__ __forceinline__ void make_shade(const TaskData &task, uint32_t tri, ShadeRecord &s) {
+	const int32_t src = task.triSource[tri];
+	const int32_t p = src >> 1, k = src & 1;
+	const int corner[3] = {0, 1 + k, 2 + k};
+	float scale = 255.0f;
+	if (task.diffuse >= 0) scale = fmul(scale, 1.0f / 255.0f);
+	if (task.light >= 0) scale = fmul(scale, 1.0f / 255.0f);
+	for (int i = 0; i < 3; i++) {
+		const float4 col = *reinterpret_cast<const float4 *>(task.colors + (p * 4 + corner[i]) * 4);
+		const float4 tc = *reinterpret_cast<const float4 *>(task.texCoords + (p * 4 + corner[i]) * 4);
+		s.red[i] = fmul(col.x, scale); s.green[i] = fmul(col.y, scale);
+		s.blue[i] = fmul(col.z, scale); s.alpha[i] = fmul(col.w, scale);
+		s.u1[i] = tc.x; s.v1[i] = tc.y; s.u2[i] = tc.z; s.v2[i] = tc.w;
+	}
+	bool fade = !(almost_same3(s.red) && almost_same3(s.green) && almost_same3(s.blue) && almost_same3(s.alpha));
+	bool colorless = almost_one3(s.red) && almost_one3(s.green) && almost_one3(s.blue) && almost_one3(s.alpha);
+	const bool hasDiffuse = task.diffuse >= 0, hasLight = task.light >= 0;
+	if (fade || (hasDiffuse == hasLight)) colorless = false;
+	s.flags = (hasDiffuse ? SHADE_DIFFUSE : 0u) | (hasLight ? SHADE_LIGHT : 0u) | (fade ? SHADE_VERTEX_FADE : 0u) |
+	          (colorless ? SHADE_COLORLESS : 0u) | (task.filter == 1 ? SHADE_ALPHA_FILTER : 0u);
+	s.diffuse = task.diffuse;
+	s.light = task.light;
 }
 
+// Vertex weights of the four lanes from (1/W, U/W, V/W) or (W, U, V) (fillerTemplates.h:197-233).
+__device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, float *wa, float *wb, float *wc) {
+	for (int l = 0; l < 4; l++) {
+		if (affine) {
+			wb[l] = w[1][l];
+			wc[l] = w[2][l];
+		} else {
+			const float linearDepth = fdiv(1.0f, w[0][l]); // reciprocal of the scalar build (noSimd.h:187)
+			wb[l] = fmul(w[1][l], linearDepth);
+			wc[l] = fmul(w[2][l], linearDepth);
+		}
+		wa[l] = 1.0f - fadd(wb[l], wc[l]);
+	}
+}
+
+// ------------------------------------------------------------------ small records, one thread each
+
+// Walks the row pairs and quads of a record exactly as fillShapeSuper does (fillerTemplates.h:246-385),
+// so every value is the reference's own running sum.  COMPONENTS = 1 for depth only, 3 for shading.
+// visit(x, y1, edge, lanes[component][lane]) is called for every quad in order.
+template <int COMPONENTS, typename Visit>
+__device__ __forceinline__ void walk_record(const DrawRecord &r, int32_t height, Visit visit) {
+	for (int32_t y1 = r.top; y1 < r.bottom; y1 += 2) {
+		const RowPair pair = record_row_pair(r, y1, height);
+		if (!pair.any) continue;
+		float U[COMPONENTS], L[COMPONENTS], v[COMPONENTS][4];
+		for (int c = 0; c < COMPONENTS; c++) {
+			U[c] = fadd(fadd(r.start[c], fmul(r.dx[c], (float)pair.obs + 0.5f)), fmul(r.dy[c], (float)y1 + 0.5f));
+			L[c] = fadd(U[c], r.dy[c]);
+		}
+		const bool allEdge = pair.ibe <= pair.ibs;
+		const int32_t leftEnd = allEdge ? pair.obe : pair.ibs;
+		int32_t x = pair.obs;
+		for (; x < leftEnd; x += 2) {
+			for (int c = 0; c < COMPONENTS; c++) {
+				v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
+				const float d2 = fmul(r.dx[c], 2.0f);
+				U[c] = fadd(U[c], d2); L[c] = fadd(L[c], d2);
+			}
+			visit(pair, x, y1, true, v);
+		}
+		if (!allEdge) {
+			for (int c = 0; c < COMPONENTS; c++) {
+				v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
+			}
+			for (; x < pair.ibe; x += 2) {
+				visit(pair, x, y1, false, v);
+				for (int c = 0; c < COMPONENTS; c++) {
+					const float d2 = fmul(r.dx[c], 2.0f);
+					for (int l = 0; l < 4; l++) v[c][l] = fadd(v[c][l], d2);
+				}
+			}
+			for (int c = 0; c < COMPONENTS; c++) {
+				const float m = fmul(fmul(r.dx[c], 2.0f), (float)((pair.ibe - pair.ibs) >> 1));
+				U[c] = fadd(U[c], m); L[c] = fadd(L[c], m);
+			}
+			for (; x < pair.obe; x += 2) {
+				for (int c = 0; c < COMPONENTS; c++) {
+					v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
+					const float d2 = fmul(r.dx[c], 2.0f);
+					U[c] = fadd(U[c], d2); L[c] = fadd(L[c], d2);
+				}
+				visit(pair, x, y1, true, v);
+			}
+		}
+	}
+}
+
+__global__ void __launch_bounds__(256) small_raster_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, TargetParams tg) {
+	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t fragments = 0;
+	if (ri < recordCount) {
+		const DrawRecord r = records[ri];
+		if (record_is_small(r, tg.smallRows, tg.smallWidth)) {
+			const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
+			walk_record<1>(r, tg.height, [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
+				for (int l = 0; l < 4; l++) {
+					const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+					if (!lane_covered(pair, x, edge, l) || yy >= tg.height || xx >= tg.width) continue;
+					fragments++;
+					const size_t pix = (size_t)yy * tg.width + xx;
+					if (tg.coverage) atomicAdd(&tg.coverage[pix], 1u);
+					bool pass = true;
+					if (depthTest) {
+						const float old = __ldg(&tg.depth[(size_t)yy * tg.depthStride + xx]);
+						pass = affine ? (v[0][l] < old) : (v[0][l] > old);
+					}
+					if (pass) {
+						const unsigned long long key = make_key(v[0][l], ri, depthTest, affine);
+						if (key > tg.keys[pix]) atomicMax(&tg.keys[pix], key);
+					}
+				}
+			});
+		}
+	}
+	if (tg.fragments) {
+		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
+		if ((threadIdx.x & 31) == 0 && fragments) atomicAdd(tg.fragments, (unsigned long long)fragments);
+	}
+}
+
+__global__ void __launch_bounds__(256) small_shade_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
+                                                          const TaskData *__restrict__ tasks, const TextureData *__restrict__ textures,
+                                                          TargetParams tg) {
+	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
+	if (ri >= recordCount) return;
+	const DrawRecord r = records[ri];
+	if (!record_is_small(r, tg.smallRows, tg.smallWidth)) return;
+	const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
+	ShadeRecord shade;
+	bool shadeReady = false;
+	auto visit = [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
+		bool won[4];
+		bool any = false;
+		for (int l = 0; l < 4; l++) {
+			const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+			won[l] = false;
+			if (!lane_covered(pair, x, edge, l) || yy >= tg.height || xx >= tg.width) continue;
+			const unsigned long long key = tg.keys[(size_t)yy * tg.width + xx];
+			won[l] = key != 0ull && key_record(key, depthTest) == ri;
+			any = any || won[l];
+		}
+		if (!any) return;
+		float wa[4], wb[4], wc[4];
+		if (tg.color) {
+			if (!shadeReady) { make_shade(tasks[r.task], r.tri, shade); shadeReady = true; }
+			lane_weights(v, affine, wa, wb, wc);
+		}
+		for (int l = 0; l < 4; l++) {
+			if (!won[l]) continue;
+			const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+			if (tg.color) {
+				float rgba[4];
+				shade_lane(shade, textures, wa, wb, wc, l, rgba);
+				tg.color[(size_t)yy * tg.colorStride + xx] = pack_saturated(rgba, tg.packOrder);
+			}
+			if (depthTest) tg.depth[(size_t)yy * tg.depthStride + xx] = v[0][l];
+		}
+	};
+	if (tg.color) walk_record<3>(r, tg.height, visit);
+	else walk_record<1>(r, tg.height, visit);
+}
+
+void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream) {
+	if (recordCount == 0 || target.smallRows <= 0) return;
+	COUNT_LAUNCH();
+	small_raster_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, target);
+}
+
+void launch_small_shade(const FrameBuffers &fb, uint32_t recordCount, const TaskData *tasks, const TextureData *textures,
+                        const TargetParams &target, cudaStream_t stream) {
+	if (recordCount == 0 || target.smallRows <= 0) return;
+	COUNT_LAUNCH();
+	small_shade_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, tasks, textures, target);
+}
+
+// ------------------------------------------------------------------ large records, one CTA per tile
+
 template <bool DEPTH_ONLY_1X1>
-__global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restrict__ records, const ShadeRecord *__restrict__ shades,
+__global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
                                                      const TextureData *__restrict__ textures, TileBins bins, TargetParams tg) {
 	__shared__ unsigned long long keys[TILE_PIXELS];
 	__shared__ float initialDepth[TILE_PIXELS];
 	__shared__ uint32_t coverage[TILE_PIXELS];
 	__shared__ unsigned long long fragmentSum;
 	const int tile = blockIdx.x;
+	const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
+	if (begin == end) return; // no large triangle here: the small-record passes own every pixel
 	const int32_t tx0 = (tile % bins.tilesX) * TILE_W, ty0 = (tile / bins.tilesX) * TILE_H;
 	const int tid = threadIdx.x;
 	const int32_t px = tx0 + (tid & 15), py = ty0 + (tid >> 4);
 	const bool inside = px < tg.width && py < tg.height;
 	const bool depthTest = tg.depth != nullptr;
 	const bool affine = tg.affine != 0;
+	const size_t pixel = (size_t)py * tg.width + px;
 	initialDepth[tid] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
-	// small triangles were already resolved into the global keys by small_raster_kernel
-	keys[tid] = (inside && tg.keys) ? tg.keys[(size_t)py * tg.width + px] : 0ull;
-	coverage[tid] = (inside && tg.coverage) ? tg.coverage[(size_t)py * tg.width + px] : 0u;
+	keys[tid] = (inside && tg.keys) ? tg.keys[pixel] : 0ull;
+	coverage[tid] = 0u;
 	if (tid == 0) fragmentSum = 0ull;
 	__syncthreads();
 
-	const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
 	const int warp = tid >> 5, lane = tid & 31;
 	uint32_t fragments = 0;
 	for (uint32_t e = begin + warp; e < end; e += 8) {
 		const uint32_t ri = bins.lists[e];
 		const DrawRecord r = records[ri];
 		// every lane cuts one of the tile's 16 rows (lanes 16..31 repeat 0..15)
-		int32_t rowLeft, rowRight;
-		row_interval(r.flat, ty0 + (lane & 15), r.left, r.right, rowLeft, rowRight);
+		int32_t rowLeft = 0, rowRight = 0;
+		const int32_t ry = ty0 + (lane & 15);
+		if (ry >= r.top && ry < r.bottom) row_interval(r.flat, ry, r.left, r.right, rowLeft, rowRight);
 		if (DEPTH_ONLY_1X1) {
 			// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
 			// pixel and grows by dx one pixel at a time.
-			const int32_t y = ty0 + (lane & 15);
+			const int32_t y = ry;
 			if (y >= r.top && y < r.bottom && y < tg.height && rowRight > rowLeft) {
 				const int32_t xs = tx0 + (lane >> 4) * 8;
 				int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
@@ -513,10 +679,11 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 		for (int q = 0; q < 2; q++) {
 			const int32_t x = tx0 + 4 * (lane & 3) + 2 * q;
 			if (x < pair.obs || x >= pair.obe) continue;
+			const bool edge = quad_is_edge(pair, x);
 			float z[4];
 			quad_lanes(r.start[0], r.dx[0], r.dy[0], pair, y1, x, z);
 			for (int l = 0; l < 4; l++) {
-				if (!lane_covered(pair, x, l)) continue;
+				if (!lane_covered(pair, x, edge, l)) continue;
 				const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
 				if (yy >= tg.height || xx >= tg.width) continue;
 				const int pix = (yy - ty0) * TILE_W + (xx - tx0);
@@ -536,10 +703,10 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 	}
 	__syncthreads();
 
-	// Resolve: every pixel re-evaluates its winning fragment exactly and shades it.
 	if (inside) {
-		if (tg.coverage) tg.coverage[(size_t)py * tg.width + px] = coverage[tid];
+		if (tg.coverage) tg.coverage[pixel] += coverage[tid];
 		const unsigned long long key = keys[tid];
+		if (tg.keys) tg.keys[pixel] = key;
 		if (key != 0ull) {
 			const uint32_t ri = key_record(key, depthTest);
 			const DrawRecord r = records[ri];
@@ -549,30 +716,21 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 				float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
 				value = chain_add(value, r.dx[0], px - left);
 				tg.depth[(size_t)py * tg.depthStride + px] = value;
-			} else {
+			} else if (!record_is_small(r, tg.smallRows, tg.smallWidth)) {
+				// the winner is a large record: re-evaluate its quad exactly and shade this pixel
 				const int32_t y1 = py & ~1, x = px & ~1;
 				const int lane4 = ((py & 1) << 1) | (px & 1);
 				const RowPair pair = record_row_pair(r, y1, tg.height);
 				float w[3][4];
-				for (int c = 0; c < 3; c++) {
-					if (c > 0 && tg.color == nullptr) break;
-					quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
-				}
+				const int components = tg.color ? 3 : 1;
+				for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
 				if (tg.color) {
 					float wa[4], wb[4], wc[4];
-					for (int l = 0; l < 4; l++) {
-						if (affine) {
-							wb[l] = w[1][l];
-							wc[l] = w[2][l];
-						} else {
-							const float linearDepth = fdiv(1.0f, w[0][l]);
-							wb[l] = fmul(w[1][l], linearDepth);
-							wc[l] = fmul(w[2][l], linearDepth);
-						}
-						wa[l] = 1.0f - fadd(wb[l], wc[l]);
-					}
+					lane_weights(w, affine, wa, wb, wc);
+					ShadeRecord shade;
+					make_shade(tasks[r.task], r.tri, shade);
 					float rgba[4];
-					shade_lane(shades[r.shade], textures, wa, wb, wc, lane4, rgba);
+					shade_lane(shade, textures, wa, wb, wc, lane4, rgba);
 					tg.color[(size_t)py * tg.colorStride + px] = pack_saturated(rgba, tg.packOrder);
 				}
 				if (depthTest) tg.depth[(size_t)py * tg.depthStride + px] = w[0][lane4];
@@ -582,92 +740,21 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 	if (tg.fragments && tid == 0) atomicAdd(tg.fragments, fragmentSum);
 }
 
-// One thread draws one small record, walking its row pairs and quads exactly as fillShapeSuper
-// does (fillerTemplates.h:246-385), so that every value is the reference's own running sum.
-// Depth tests resolve through the same 64-bit keys as the tile kernel, in global memory.
-__device__ __forceinline__ void small_quad(const TargetParams &tg, const RowPair &pair, int32_t x, int32_t y1, bool edge,
-                                           const float *z, uint32_t record, bool depthTest, bool affine, uint32_t &fragments) {
-	for (int l = 0; l < 4; l++) {
-		const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-		bool covered;
-		if (l < 2) covered = !edge || (xx >= pair.upperLeft && xx < pair.upperRight);
-		else covered = !edge || (xx >= pair.lowerLeft && xx < pair.lowerRight);
-		if (!covered || yy >= tg.height || xx >= tg.width) continue;
-		fragments++;
-		const size_t pix = (size_t)yy * tg.width + xx;
-		if (tg.coverage) atomicAdd(&tg.coverage[pix], 1u);
-		bool pass = true;
-		if (depthTest) {
-			const float old = tg.depth[(size_t)yy * tg.depthStride + xx];
-			pass = affine ? (z[l] < old) : (z[l] > old);
-		}
-		if (pass) {
-			const unsigned long long key = make_key(z[l], record, depthTest, affine);
-			if (key > tg.keys[pix]) atomicMax(&tg.keys[pix], key);
-		}
-	}
-}
-
-__global__ void __launch_bounds__(256) small_raster_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, TargetParams tg) {
-	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
-	uint32_t fragments = 0;
-	if (ri < recordCount) {
-		const DrawRecord r = records[ri];
-		if (record_is_small(r, tg.smallRows, tg.smallWidth)) {
-			const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
-			const float dx = r.dx[0], d2 = fmul(dx, 2.0f);
-			for (int32_t y1 = r.top; y1 < r.bottom; y1 += 2) {
-				const RowPair pair = record_row_pair(r, y1, tg.height);
-				if (!pair.any) continue;
-				float U = fadd(fadd(r.start[0], fmul(dx, (float)pair.obs + 0.5f)), fmul(r.dy[0], (float)y1 + 0.5f));
-				float L = fadd(U, r.dy[0]);
-				float z[4];
-				const bool allEdge = pair.ibe <= pair.ibs;
-				const int32_t leftEnd = allEdge ? pair.obe : pair.ibs;
-				int32_t x = pair.obs;
-				for (; x < leftEnd; x += 2) {
-					z[0] = U; z[1] = fadd(U, dx); z[2] = L; z[3] = fadd(L, dx);
-					small_quad(tg, pair, x, y1, true, z, ri, depthTest, affine, fragments);
-					U = fadd(U, d2); L = fadd(L, d2);
-				}
-				if (!allEdge) {
-					float v[4] = {U, fadd(U, dx), L, fadd(L, dx)};
-					for (; x < pair.ibe; x += 2) {
-						small_quad(tg, pair, x, y1, false, v, ri, depthTest, affine, fragments);
-						for (int l = 0; l < 4; l++) v[l] = fadd(v[l], d2);
-					}
-					const float m = fmul(d2, (float)((pair.ibe - pair.ibs) >> 1));
-					U = fadd(U, m); L = fadd(L, m);
-					for (; x < pair.obe; x += 2) {
-						z[0] = U; z[1] = fadd(U, dx); z[2] = L; z[3] = fadd(L, dx);
-						small_quad(tg, pair, x, y1, true, z, ri, depthTest, affine, fragments);
-						U = fadd(U, d2); L = fadd(L, d2);
-					}
-				}
-			}
-		}
-	}
-	if (tg.fragments) {
-		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
-		if ((threadIdx.x & 31) == 0 && fragments) atomicAdd(tg.fragments, (unsigned long long)fragments);
-	}
-}
-
-void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream) {
-	if (recordCount == 0 || target.smallRows <= 0) return;
-	COUNT_LAUNCH();
-	small_raster_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, target);
-}
-
-void launch_raster(const FrameBuffers &fb, const TextureData *textures, const TileBins &bins, const TargetParams &target,
-                   cudaStream_t stream) {
+void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureData *textures, const TileBins &bins,
+                   const TargetParams &target, cudaStream_t stream) {
 	int tiles = bins.tilesX * bins.tilesY;
-	if (tiles > 0) { COUNT_LAUNCH(); raster_kernel<false><<<tiles, 256, 0, stream>>>(fb.records, fb.shades, textures, bins, target); }
+	if (tiles > 0) {
+		COUNT_LAUNCH();
+		raster_kernel<false><<<tiles, 256, 0, stream>>>(fb.records, tasks, textures, bins, target);
+	}
 }
 
 void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream) {
 	int tiles = bins.tilesX * bins.tilesY;
-	if (tiles > 0) { COUNT_LAUNCH(); raster_kernel<true><<<tiles, 256, 0, stream>>>(fb.records, fb.shades, nullptr, bins, target); }
+	if (tiles > 0) {
+		COUNT_LAUNCH();
+		raster_kernel<true><<<tiles, 256, 0, stream>>>(fb.records, nullptr, nullptr, bins, target);
+	}
 }
 
 } // namespace dsrg

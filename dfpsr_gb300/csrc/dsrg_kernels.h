@@ -18,7 +18,7 @@ struct TaskParams {
 	int32_t pointCount;
 	int32_t triangleCount;
 	uint32_t orderBase;       // fan triangles submitted earlier in the same frame
-	uint32_t shadeBase;       // first ShadeRecord of this task
+	uint32_t taskIndex;       // this task's entry in the frame's TaskData table
 	float modelToWorld[12];
 	CameraData camera;
 	int32_t width, height;
@@ -33,7 +33,6 @@ struct FrameBuffers {
 	uint32_t *triCounts;      // per fan triangle: draw records it emits
 	uint32_t *triOffsets;     // exclusive scan of triCounts (+ running record count at [triangleCount])
 	DrawRecord *records;
-	ShadeRecord *shades;
 	uint32_t *recordCount;    // device counter of records in the frame
 	int32_t *errorFlag;       // device error bits
 	uint32_t *scanScratch;
@@ -86,10 +85,16 @@ uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins
                           cudaStream_t stream);
 void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
                      cudaStream_t stream);
-void launch_raster(const FrameBuffers &fb, const TextureData *textures, const TileBins &bins,
-                   const TargetParams &target, cudaStream_t stream);
-// Draws every small record with one thread each into target.keys (before launch_raster).
+// The three raster passes of a frame, in this order:
+//   launch_small_raster  depth keys of every small record (one thread per record) into target.keys
+//   launch_raster        per tile: keys of the large records, merged into target.keys; shades the
+//                        pixels that large records won
+//   launch_small_shade   shades the pixels that small records won (one thread per record)
 void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream);
+void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureData *textures, const TileBins &bins,
+                   const TargetParams &target, cudaStream_t stream);
+void launch_small_shade(const FrameBuffers &fb, uint32_t recordCount, const TaskData *tasks, const TextureData *textures,
+                        const TargetParams &target, cudaStream_t stream);
 void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total).
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);

@@ -4,6 +4,10 @@
 
 #include <stdint.h>
 
+#if !defined(__CUDACC__) && !defined(__align__)
+#define __align__(n) alignas(n)
+#endif
+
 namespace dsrg {
 
 // Tiles of the screen that one CTA owns while rasterising.
@@ -54,27 +58,37 @@ enum ShadeFlags : uint32_t {
 };
 
 // Per source triangle: scaled vertex colours and texture coordinates (shader/Shader.h:36-60,
-// RgbaMultiply.h:37-58) plus the variant and its textures.
+// RgbaMultiply.h:37-58) plus the variant and its textures, computed where a pixel is shaded.
 struct ShadeRecord {
 	float red[3], green[3], blue[3], alpha[3];
 	float u1[3], v1[3], u2[3], v2[3];
 	uint32_t flags;
 	int32_t diffuse; // index into the frame's texture table, -1 for none
 	int32_t light;
-	int32_t pad;
+};
+
+// One model submitted to a frame (renderer_giveTask): where its polygon data lives and which
+// textures of the frame's table it uses.
+struct TaskData {
+	const int32_t *polygons;
+	const float *texCoords;
+	const float *colors;
+	const int32_t *triSource;
+	int32_t diffuse, light, filter, pad;
 };
 
 // One draw command after culling, clipping and the front-face test
 // (implementation/render/renderCore.h:52-70): sub-pixel corners, the row-aligned
 // raster bound inside the target, and the vertex-weight projection (ITriangle2D.h:63-78).
-struct DrawRecord {
+// 96 bytes, 16-byte aligned so that it moves in six 128-bit accesses.
+struct __align__(16) DrawRecord {
 	int32_t flat[6];
 	int32_t left, top, right, bottom; // getAlignedRasterBound against the whole target
 	float start[3], dx[3], dy[3];     // pWeightStart, pWeightDx, pWeightDy
 	uint32_t order;                   // submission order: triangle index * 8 + clipped sub-triangle index
-	uint32_t shade;                   // index of the ShadeRecord
-	uint32_t flags;                   // bit 0: affine (orthogonal camera)
-	uint32_t pad;
+	uint32_t tri;                     // fan triangle of its task (polygon data for shading)
+	uint32_t task;                    // index into the frame's TaskData table
+	uint32_t flags;                   // RECORD_AFFINE for orthogonal cameras
 };
 
 static const uint32_t RECORD_AFFINE = 1u;
