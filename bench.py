@@ -210,7 +210,8 @@ def main():
     # fragments per frame: deterministic, counted once by the kernels themselves
     ctx.set_counting(True)
     ctx.render(model, model.camera, color, depth)
-    fragments = ctx.stats()["fragments"]
+    frame_stats = ctx.stats()
+    fragments = frame_stats["fragments"]
     ctx.set_counting(False)
 
     def frame_device():
@@ -284,6 +285,7 @@ def main():
             "config": dict(cfg, l2="flushed before every frame (256 MB write)", parallelism="replicas" if world > 1 else "single GPU"),
             "frames_per_s": world * args.steps / total_s,
             "fragments_per_frame": fragments,
+            "frame_stats": {"draw_records": frame_stats["draw_records"], "bin_entries": frame_stats["bin_entries"]},
             "e2e": {"value": world * fragments * args.steps / e2e_s / 1e6, "unit": "Mfrag/s",
                     "h2d_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
                     "d2h_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),

@@ -133,7 +133,8 @@ struct dsrg_context_s {
 	DeviceBuffer<float> stagingDepth;
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;
-	int32_t smallRows = 8, smallWidth = 16; // thread-per-triangle path for raster bounds up to 8 x 16 pixels
+	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;
+	int32_t smallRows = 8, smallWidth = 16; // one lane walks records whose raster bound is at most 8 x 16 pixels
 	int32_t counting = 0;
 	uint32_t *coverage = nullptr;
 	dsrg_stats stats;
@@ -232,8 +233,8 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();
-	ctx->records.release(); ctx->taskTable.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
-	ctx->keys.release();
+	ctx->records.release(); ctx->taskTable.release(); ctx->keys.release();
+	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
 	cudaEventDestroy(ctx->eventStart);
 	cudaEventDestroy(ctx->eventStop);
 	cudaEventDestroy(ctx->eventRasterStart);
@@ -460,6 +461,8 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 	if (color && (color->packOrder < 0 || color->packOrder > 3)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: unknown pack order");
 	if (color && depth && (color->width != depth->width || color->height != depth->height))
 		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_begin: colour and depth images must have the same dimensions");
+	if ((color && (color->width > 32767 || color->height > 32767)) || (depth && (depth->width > 32767 || depth->height > 32767)))
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_begin: targets are limited to 32767 x 32767 pixels");
 	cudaSetDevice(ctx->device);
 	r->hasColor = color != nullptr;
 	r->hasDepth = depth != nullptr;
@@ -616,7 +619,9 @@ static int end_frame(dsrg_renderer r) {
 	CUDA_TRY(ctx, ctx->binCounts.reserve(tiles));
 	CUDA_TRY(ctx, ctx->binOffsets.reserve(tiles + 1));
 	CUDA_TRY(ctx, ctx->binCursors.reserve(tiles));
-	CUDA_TRY(ctx, ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)tiles)));
+	CUDA_TRY(ctx, ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(tiles > recordCount ? tiles : recordCount) + 2)));
+	CUDA_TRY(ctx, ctx->rowCounts.reserve((size_t)recordCount + 2));
+	CUDA_TRY(ctx, ctx->rowOffsets.reserve((size_t)recordCount + 2));
 	CUDA_TRY(ctx, ctx->textureTable.reserve(r->textures.size() + 1));
 	if (!r->textures.empty())
 		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->textureTable.ptr, r->textures.data(), r->textures.size() * sizeof(TextureData),
@@ -633,17 +638,27 @@ static int end_frame(dsrg_renderer r) {
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
 	fb.records = ctx->records.ptr;
+	fb.rowOffsets = ctx->rowOffsets.ptr;
 	fb.recordCount = ctx->control.ptr;
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	fb.scanScratch = ctx->scanScratch.ptr;
 	fb.scanScratchElems = ctx->scanScratch.capacity;
 	const int32_t smallRows = r->depthOnly ? 0 : ctx->smallRows, smallWidth = ctx->smallWidth;
-	uint32_t entries = launch_bin_count(fb, recordCount, bins, smallRows, smallWidth, ctx->stream);
+	launch_row_offsets(fb, recordCount, ctx->rowCounts.ptr, ctx->stream);
+	launch_bin_count(fb, recordCount, bins, 0, 0, ctx->stream);
 	CUDA_TRY(ctx, cudaGetLastError());
+	uint32_t totals[2] = {0, 0};
+	CUDA_TRY(ctx, cudaMemcpyAsync(&totals[0], bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+	CUDA_TRY(ctx, cudaMemcpyAsync(&totals[1], ctx->rowOffsets.ptr + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	const uint32_t entries = totals[0];
 	CUDA_TRY(ctx, ctx->binLists.reserve((size_t)entries + 1));
+	CUDA_TRY(ctx, ctx->rows.reserve((size_t)totals[1] + 2));
+	fb.rows = ctx->rows.ptr;
 	bins.lists = ctx->binLists.ptr;
 	bins.listCapacity = ctx->binLists.capacity;
-	launch_bin_fill(fb, recordCount, bins, smallRows, smallWidth, ctx->stream);
+	launch_rows(fb, recordCount, ctx->stream);
+	launch_bin_fill(fb, recordCount, bins, 0, 0, ctx->stream);
 	TargetParams tg;
 	memset(&tg, 0, sizeof(tg));
 	tg.color = r->hasColor ? r->deviceColor : nullptr;
@@ -660,6 +675,8 @@ static int end_frame(dsrg_renderer r) {
 	CUDA_TRY(ctx, ctx->keys.reserve(pixels));
 	CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
 	tg.keys = ctx->keys.ptr;
+	tg.rowOffsets = ctx->rowOffsets.ptr;
+	tg.rows = ctx->rows.ptr;
 	if (ctx->counting) {
 		CUDA_TRY(ctx, cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), ctx->stream));
 		tg.fragments = ctx->fragmentCounter.ptr;
@@ -670,9 +687,7 @@ static int end_frame(dsrg_renderer r) {
 	if (r->depthOnly) {
 		launch_raster_depth_only(fb, bins, tg, ctx->stream);
 	} else {
-		launch_small_raster(fb, recordCount, tg, ctx->stream);
 		launch_raster(fb, ctx->taskTable.ptr, ctx->textureTable.ptr, bins, tg, ctx->stream);
-		launch_small_shade(fb, recordCount, ctx->taskTable.ptr, ctx->textureTable.ptr, tg, ctx->stream);
 	}
 	CUDA_TRY(ctx, cudaGetLastError());
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStop, ctx->stream));

@@ -12,8 +12,11 @@
 
 #if defined(__CUDACC__)
 #define DSRG_HD __host__ __device__ __forceinline__
+// Large helpers stay out of line on the device so that the kernels fit the instruction cache.
+#define DSRG_HD_CALL static __host__ __device__ __noinline__
 #else
 #define DSRG_HD inline
+#define DSRG_HD_CALL inline
 #endif
 
 namespace dsrg {
@@ -71,7 +74,7 @@ DSRG_HD float i64_to_float(int64_t v) {
 // increment until the running value leaves the binade (or a tie needs a parity
 // that the current value does not have).  Those boundary steps are taken one at
 // a time with a real float addition.
-DSRG_HD float chain_add(float s, float d, int32_t n) {
+DSRG_HD_CALL float chain_add(float s, float d, int32_t n) {
 	if (n <= 6) {
 		// short chains (small triangles, quads near a row's start) are cheaper step by step
 		for (int32_t i = 0; i < n; i++) s = fadd(s, d);
@@ -226,7 +229,7 @@ DSRG_HD void cut_row(const Edge &e, int32_t y, int32_t L, int32_t R, int32_t &le
 
 // Row interval [left, right) of pixel row y for a triangle with sub-pixel corners,
 // clamped to [L, R): rasterizeTriangle (implementation/render/ITriangle2D.cpp:150-169).
-DSRG_HD void row_interval(const int32_t *flat, int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {
+DSRG_HD_CALL void row_interval(const int32_t *flat, int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {
 	const bool degenerate = (flat[0] == flat[2] && flat[1] == flat[3]) || (flat[2] == flat[4] && flat[3] == flat[5]) ||
 	                        (flat[4] == flat[0] && flat[5] == flat[1]);
 	if (degenerate) { left = R; right = L; return; }

@@ -5,11 +5,9 @@
 //   setup_kernel<false>  per fan triangle: cull, clip, front-face; counts its draw records
 //   scan                 record offsets, so that records land in submission order
 //   setup_kernel<true>   writes the DrawRecords (bound, sub-pixel corners, projection)
-//   bin kernels          per 16x16 tile lists of the large records whose raster bound touches it
-//   small_raster_kernel  one thread per small record: depth keys into a global key image
-//   raster_kernel        one CTA per tile: depth keys of the large records in shared memory, merged
-//                        with the global keys; shades the pixels that large records won
-//   small_shade_kernel   one thread per small record: shades the pixels that small records won
+//   bin kernels          per 16x16 tile lists of the records whose raster bound touches it
+//   raster_kernel        one CTA per tile: every fragment competes for 64-bit depth keys in shared
+//                        memory, then every pixel shades its winning fragment
 //
 // Why the depth test can run out of order: the reference writes a fragment when its depth is
 // strictly greater (1/W, perspective) or smaller (linear, orthogonal) than the stored one
@@ -264,6 +262,44 @@ __device__ __forceinline__ void record_tiles(const DrawRecord &r, const TileBins
 	if (ty1 >= bins.tilesY) ty1 = bins.tilesY - 1;
 }
 
+// Conservative test of whether any pixel of tile (tx, ty) can be inside the record's row
+// intervals: a pixel (x, y) passes edge i of cutConvexEdge when
+//   (128 + 256x - sx)*nx + (128 + 256y - sy)*ny <= threshold      (ITriangle2D.cpp:96-146)
+// and that linear function is largest at a corner of any rectangle, so a tile is out when one
+// edge rejects all four corners of the tile grown by two pixels (the growth covers the rows
+// where the reference's truncating division admits a pixel just outside an edge).
+__device__ __forceinline__ bool tile_may_overlap(const DrawRecord &r, int32_t tx, int32_t ty) {
+	const int64_t X0 = 128 + 256 * (int64_t)(tx * TILE_W - 2), X1 = 128 + 256 * (int64_t)(tx * TILE_W + TILE_W + 1);
+	const int64_t Y0 = 128 + 256 * (int64_t)(ty * TILE_H - 2), Y1 = 128 + 256 * (int64_t)(ty * TILE_H + TILE_H + 1);
+	for (int i = 0; i < 3; i++) {
+		const int j = (i + 1) % 3;
+		const Edge e = make_edge(r.flat[i * 2], r.flat[i * 2 + 1], r.flat[j * 2], r.flat[j * 2 + 1]);
+		const int64_t a = (X0 - e.sx) * e.nx, b = (X1 - e.sx) * e.nx;
+		const int64_t c = (Y0 - e.sy) * e.ny, d = (Y1 - e.sy) * e.ny;
+		const int64_t lowest = (a < b ? a : b) + (c < d ? c : d);
+		if (lowest > e.threshold) return false;
+	}
+	return true;
+}
+
+// The corner test above is exact only when no row of the record makes the reference cast a
+// quotient beyond 32 bits (a nearly horizontal edge whose row crossings lie 2^30 pixels away),
+// because such a row's interval comes from the wrapped value, not from the edge.
+__device__ __forceinline__ bool tile_test_is_exact(const DrawRecord &r) {
+	for (int i = 0; i < 3; i++) {
+		const int j = (i + 1) % 3;
+		const Edge e = make_edge(r.flat[i * 2], r.flat[i * 2 + 1], r.flat[j * 2], r.flat[j * 2 + 1]);
+		if (e.nx == 0) continue;
+		const float den = fabsf(i64_to_float(e.nx * 256));
+		for (int k = 0; k < 2; k++) {
+			const int64_t y = k ? (int64_t)r.bottom : (int64_t)r.top;
+			const int64_t limit = e.threshold - (128 - e.sx) * e.nx - (128 + 256 * y - e.sy) * e.ny;
+			if (fabsf(i64_to_float(limit)) >= 5.0e8f * den) return false;
+		}
+	}
+	return true;
+}
+
 // Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs of the large records.
 // Records touching at most 4 tiles are walked by their own thread, with the atomics of threads
 // that hit the same tile merged into one; larger ones are walked by the whole warp.
@@ -303,8 +339,12 @@ __global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, Tile
 		int32_t bx0 = __shfl_sync(0xFFFFFFFFu, tx0, src), by0 = __shfl_sync(0xFFFFFFFFu, ty0, src);
 		int32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bt = __shfl_sync(0xFFFFFFFFu, tiles, src);
 		uint32_t br = __shfl_sync(0xFFFFFFFFu, r, src);
+		const DrawRecord rec = records[br];
+		const bool exact = tile_test_is_exact(rec);
 		for (int32_t i = (int32_t)lane; i < bt; i += 32) {
-			uint32_t tile = (uint32_t)((by0 + i / bw) * bins.tilesX + bx0 + i % bw);
+			const int32_t tx = bx0 + i % bw, ty = by0 + i / bw;
+			if (exact && !tile_may_overlap(rec, tx, ty)) continue;
+			uint32_t tile = (uint32_t)(ty * bins.tilesX + tx);
 			uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
 			if (FILL) {
 				slot += bins.offsets[tile];
@@ -314,8 +354,8 @@ __global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, Tile
 	}
 }
 
-uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
-                          cudaStream_t stream) {
+void launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                      cudaStream_t stream) {
 	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
 	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * tiles, stream);
 	if (recordCount > 0) {
@@ -323,10 +363,66 @@ uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins
 		bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth);
 	}
 	launch_scan(bins.counts, bins.offsets, tiles, fb.scanScratch, fb.scanScratchElems, stream);
-	uint32_t total = 0;
-	cudaMemcpyAsync(&total, bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
-	cudaStreamSynchronize(stream);
-	return total;
+}
+
+// ------------------------------------------------------------------ row intervals
+
+__global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, uint32_t *counts) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < recordCount) counts[i] = (uint32_t)(records[i].bottom - records[i].top);
+}
+
+void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream) {
+	if (recordCount > 0) {
+		COUNT_LAUNCH();
+		row_count_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, rowCounts);
+	}
+	launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
+}
+
+// Rows of records up to 16 rows tall are cut by their own thread, taller ones by the whole warp.
+__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
+                                                   const uint32_t *__restrict__ rowOffsets, uint32_t *rows) {
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	int32_t count = 0;
+	DrawRecord r;
+	if (i < recordCount) {
+		r = records[i];
+		count = r.bottom - r.top;
+		if (count <= 16) {
+			uint32_t *out = rows + rowOffsets[i];
+			for (int32_t k = 0; k < count; k++) {
+				int32_t left, right;
+				row_interval(r.flat, r.top + k, r.left, r.right, left, right);
+				out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+			}
+		}
+	}
+	uint32_t tall = __ballot_sync(0xFFFFFFFFu, count > 16);
+	while (tall) {
+		const int src = __ffs(tall) - 1;
+		tall &= tall - 1;
+		const uint32_t ri = __shfl_sync(0xFFFFFFFFu, i, src);
+		const DrawRecord t = records[ri];
+		uint32_t *out = rows + rowOffsets[ri];
+		for (int32_t k = (int32_t)lane; k < t.bottom - t.top; k += 32) {
+			int32_t left, right;
+			row_interval(t.flat, t.top + k, t.left, t.right, left, right);
+			out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+		}
+	}
+}
+
+void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream) {
+	if (recordCount == 0) return;
+	COUNT_LAUNCH();
+	rows_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets, fb.rows);
+}
+
+__device__ __forceinline__ void unpack_row(uint32_t packed, int32_t &left, int32_t &right) {
+	left = (int32_t)(packed & 0xFFFFu);
+	right = (int32_t)(packed >> 16);
 }
 
 void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
@@ -362,11 +458,12 @@ __device__ __forceinline__ RowPair make_row_pair(int32_t uL, int32_t uR, int32_t
 	return rp;
 }
 
-// Row pair of record r for the rows y1, y1 + 1.
-__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, int32_t y1, int32_t height) {
+// Row pair of a record for the rows y1, y1 + 1 from its row intervals (recordRows = its first row).
+__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, const uint32_t *recordRows, int32_t y1, int32_t height) {
 	int32_t uL, uR, lL, lR;
-	row_interval(r.flat, y1, r.left, r.right, uL, uR);
-	row_interval(r.flat, y1 + 1, r.left, r.right, lL, lR);
+	const uint2 two = *reinterpret_cast<const uint2 *>(recordRows + (y1 - r.top)) ;
+	unpack_row(two.x, uL, uR);
+	unpack_row(two.y, lL, lR);
 	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
 }
 
@@ -469,15 +566,16 @@ __device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, f
 	}
 }
 
-// ------------------------------------------------------------------ small records, one thread each
+// ------------------------------------------------------------------ the reference's walk over one record
 
 // Walks the row pairs and quads of a record exactly as fillShapeSuper does (fillerTemplates.h:246-385),
 // so every value is the reference's own running sum.  COMPONENTS = 1 for depth only, 3 for shading.
 // visit(x, y1, edge, lanes[component][lane]) is called for every quad in order.
 template <int COMPONENTS, typename Visit>
-__device__ __forceinline__ void walk_record(const DrawRecord &r, int32_t height, Visit visit) {
-	for (int32_t y1 = r.top; y1 < r.bottom; y1 += 2) {
-		const RowPair pair = record_row_pair(r, y1, height);
+__device__ __forceinline__ void walk_record(const DrawRecord &r, const uint32_t *recordRows, int32_t rowStart, int32_t rowEnd,
+                                            int32_t height, Visit visit) {
+	for (int32_t y1 = rowStart; y1 < rowEnd; y1 += 2) {
+		const RowPair pair = record_row_pair(r, recordRows, y1, height);
 		if (!pair.any) continue;
 		float U[COMPONENTS], L[COMPONENTS], v[COMPONENTS][4];
 		for (int c = 0; c < COMPONENTS; c++) {
@@ -522,177 +620,154 @@ __device__ __forceinline__ void walk_record(const DrawRecord &r, int32_t height,
 	}
 }
 
-__global__ void __launch_bounds__(256) small_raster_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, TargetParams tg) {
-	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
-	uint32_t fragments = 0;
-	if (ri < recordCount) {
-		const DrawRecord r = records[ri];
-		if (record_is_small(r, tg.smallRows, tg.smallWidth)) {
-			const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
-			walk_record<1>(r, tg.height, [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
-				for (int l = 0; l < 4; l++) {
-					const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-					if (!lane_covered(pair, x, edge, l) || yy >= tg.height || xx >= tg.width) continue;
-					fragments++;
-					const size_t pix = (size_t)yy * tg.width + xx;
-					if (tg.coverage) atomicAdd(&tg.coverage[pix], 1u);
-					bool pass = true;
-					if (depthTest) {
-						const float old = __ldg(&tg.depth[(size_t)yy * tg.depthStride + xx]);
-						pass = affine ? (v[0][l] < old) : (v[0][l] > old);
-					}
-					if (pass) {
-						const unsigned long long key = make_key(v[0][l], ri, depthTest, affine);
-						if (key > tg.keys[pix]) atomicMax(&tg.keys[pix], key);
-					}
-				}
-			});
-		}
-	}
-	if (tg.fragments) {
-		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
-		if ((threadIdx.x & 31) == 0 && fragments) atomicAdd(tg.fragments, (unsigned long long)fragments);
-	}
-}
-
-__global__ void __launch_bounds__(256) small_shade_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
-                                                          const TaskData *__restrict__ tasks, const TextureData *__restrict__ textures,
-                                                          TargetParams tg) {
-	const uint32_t ri = blockIdx.x * blockDim.x + threadIdx.x;
-	if (ri >= recordCount) return;
-	const DrawRecord r = records[ri];
-	if (!record_is_small(r, tg.smallRows, tg.smallWidth)) return;
-	const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
-	ShadeRecord shade;
-	bool shadeReady = false;
-	auto visit = [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
-		bool won[4];
-		bool any = false;
-		for (int l = 0; l < 4; l++) {
-			const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-			won[l] = false;
-			if (!lane_covered(pair, x, edge, l) || yy >= tg.height || xx >= tg.width) continue;
-			const unsigned long long key = tg.keys[(size_t)yy * tg.width + xx];
-			won[l] = key != 0ull && key_record(key, depthTest) == ri;
-			any = any || won[l];
-		}
-		if (!any) return;
-		float wa[4], wb[4], wc[4];
-		if (tg.color) {
-			if (!shadeReady) { make_shade(tasks[r.task], r.tri, shade); shadeReady = true; }
-			lane_weights(v, affine, wa, wb, wc);
-		}
-		for (int l = 0; l < 4; l++) {
-			if (!won[l]) continue;
-			const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-			if (tg.color) {
-				float rgba[4];
-				shade_lane(shade, textures, wa, wb, wc, l, rgba);
-				tg.color[(size_t)yy * tg.colorStride + xx] = pack_saturated(rgba, tg.packOrder);
-			}
-			if (depthTest) tg.depth[(size_t)yy * tg.depthStride + xx] = v[0][l];
-		}
-	};
-	if (tg.color) walk_record<3>(r, tg.height, visit);
-	else walk_record<1>(r, tg.height, visit);
-}
-
-void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream) {
-	if (recordCount == 0 || target.smallRows <= 0) return;
-	COUNT_LAUNCH();
-	small_raster_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, target);
-}
-
-void launch_small_shade(const FrameBuffers &fb, uint32_t recordCount, const TaskData *tasks, const TextureData *textures,
-                        const TargetParams &target, cudaStream_t stream) {
-	if (recordCount == 0 || target.smallRows <= 0) return;
-	COUNT_LAUNCH();
-	small_shade_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, tasks, textures, target);
-}
-
 // ------------------------------------------------------------------ large records, one CTA per tile
 
+// Depth test of one fragment against the tile's shared keys.
+__device__ __forceinline__ void tile_fragment(unsigned long long *keys, const float *initialDepth, uint32_t *coverage,
+                                              const TargetParams &tg, int pix, float z, uint32_t record, bool depthTest,
+                                              bool affine, uint32_t &fragments) {
+	fragments++;
+	if (tg.coverage) atomicAdd(&coverage[pix], 1u);
+	const bool pass = !depthTest || (affine ? (z < initialDepth[pix]) : (z > initialDepth[pix]));
+	if (pass) {
+		const unsigned long long key = make_key(z, record, depthTest, affine);
+		if (key > keys[pix]) atomicMax(&keys[pix], key);
+	}
+}
+
+// One CTA per 16x16 tile.  Each warp takes 32 list entries at a time: a lane walks a small record
+// by itself (the reference's sequential walk, only the quads inside the tile are tested); large
+// records are rasterised by the whole warp, one lane per (row pair, 4 columns).  After all
+// fragments have competed for the shared keys, every thread resolves one pixel: it re-evaluates
+// the winning fragment's quad exactly and shades it (deferred shading).
 template <bool DEPTH_ONLY_1X1>
-__global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
-                                                     const TextureData *__restrict__ textures, TileBins bins, TargetParams tg) {
-	__shared__ unsigned long long keys[TILE_PIXELS];
-	__shared__ float initialDepth[TILE_PIXELS];
-	__shared__ uint32_t coverage[TILE_PIXELS];
+__global__ void __launch_bounds__(256, 4) raster_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
+                                                        const TextureData *__restrict__ textures, TileBins bins, TargetParams tg) {
+	__shared__ unsigned long long keys[TILE_H * TILE_STRIDE];
+	__shared__ float initialDepth[TILE_H * TILE_STRIDE];
+	__shared__ uint32_t coverage[TILE_H * TILE_STRIDE];
 	__shared__ unsigned long long fragmentSum;
 	const int tile = blockIdx.x;
 	const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
-	if (begin == end) return; // no large triangle here: the small-record passes own every pixel
+	if (begin == end) return; // nothing covers this tile (its keys were cleared before the launch)
 	const int32_t tx0 = (tile % bins.tilesX) * TILE_W, ty0 = (tile / bins.tilesX) * TILE_H;
 	const int tid = threadIdx.x;
 	const int32_t px = tx0 + (tid & 15), py = ty0 + (tid >> 4);
 	const bool inside = px < tg.width && py < tg.height;
 	const bool depthTest = tg.depth != nullptr;
 	const bool affine = tg.affine != 0;
-	const size_t pixel = (size_t)py * tg.width + px;
-	initialDepth[tid] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
-	keys[tid] = (inside && tg.keys) ? tg.keys[pixel] : 0ull;
-	coverage[tid] = 0u;
+	const int me = (tid >> 4) * TILE_STRIDE + (tid & 15); // this thread's pixel in the padded tile arrays
+	initialDepth[me] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
+	keys[me] = 0ull;
+	coverage[me] = 0u;
 	if (tid == 0) fragmentSum = 0ull;
 	__syncthreads();
 
 	const int warp = tid >> 5, lane = tid & 31;
 	uint32_t fragments = 0;
-	for (uint32_t e = begin + warp; e < end; e += 8) {
-		const uint32_t ri = bins.lists[e];
-		const DrawRecord r = records[ri];
-		// every lane cuts one of the tile's 16 rows (lanes 16..31 repeat 0..15)
-		int32_t rowLeft = 0, rowRight = 0;
-		const int32_t ry = ty0 + (lane & 15);
-		if (ry >= r.top && ry < r.bottom) row_interval(r.flat, ry, r.left, r.right, rowLeft, rowRight);
-		if (DEPTH_ONLY_1X1) {
-			// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
-			// pixel and grows by dx one pixel at a time.
-			const int32_t y = ry;
-			if (y >= r.top && y < r.bottom && y < tg.height && rowRight > rowLeft) {
-				const int32_t xs = tx0 + (lane >> 4) * 8;
-				int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
-				if (x0 < x1) {
-					float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)rowLeft + 0.5f)), fmul(r.dy[0], (float)y + 0.5f));
-					value = chain_add(value, r.dx[0], x0 - rowLeft);
-					for (int32_t x = x0; x < x1; x++) {
-						const int pix = (y - ty0) * TILE_W + (x - tx0);
-						fragments++;
-						if (tg.coverage) atomicAdd(&coverage[pix], 1u);
-						bool pass = affine ? (value < initialDepth[pix]) : (value > initialDepth[pix]);
-						if (pass) {
-							unsigned long long key = make_key(value, ri, true, affine);
-							if (key > keys[pix]) atomicMax(&keys[pix], key);
+	// entries are dealt round-robin over the warps (warp w takes w, w + 8, w + 16, ...), so that
+	// short lists still keep every warp of the tile busy
+	for (uint32_t chunk = begin; chunk < end; chunk += 32u * 8u) {
+		const uint32_t e = chunk + (uint32_t)warp + 8u * (uint32_t)lane;
+		const bool valid = e < end;
+		const uint32_t myRecord = valid ? bins.lists[e] : 0u;
+		bool small = false;
+		if (valid && !DEPTH_ONLY_1X1) {
+			const DrawRecord r = records[myRecord];
+			small = record_is_small(r, tg.smallRows, tg.smallWidth);
+			if (small) {
+				const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
+				walk_record<1>(r, tg.rows + tg.rowOffsets[myRecord], rowStart, rowEnd, tg.height, [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
+					if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
+					for (int l = 0; l < 4; l++) {
+						const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+						if (xx < tx0 || xx >= tx0 + TILE_W || yy >= tg.height || xx >= tg.width) continue;
+						if (!lane_covered(pair, x, edge, l)) continue;
+						tile_fragment(keys, initialDepth, coverage, tg, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l], myRecord,
+						              depthTest, affine, fragments);
+					}
+				});
+			}
+		}
+		uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small);
+		while (largeMask) {
+			const int src = __ffs(largeMask) - 1;
+			largeMask &= largeMask - 1;
+			const uint32_t ri = __shfl_sync(0xFFFFFFFFu, myRecord, src);
+			const DrawRecord r = records[ri];
+			// every lane cuts one of the tile's 16 rows (lanes 16..31 repeat 0..15)
+			int32_t rowLeft = 0, rowRight = 0;
+			const int32_t ry = ty0 + (lane & 15);
+			if (ry >= r.top && ry < r.bottom) unpack_row(tg.rows[tg.rowOffsets[ri] + (ry - r.top)], rowLeft, rowRight);
+			if (DEPTH_ONLY_1X1) {
+				// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
+				// pixel and grows by dx one pixel at a time.
+				if (ry >= r.top && ry < r.bottom && ry < tg.height && rowRight > rowLeft) {
+					const int32_t xs = tx0 + (lane >> 4) * 8;
+					const int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
+					if (x0 < x1) {
+						float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)rowLeft + 0.5f)), fmul(r.dy[0], (float)ry + 0.5f));
+						value = chain_add(value, r.dx[0], x0 - rowLeft);
+						for (int32_t x = x0; x < x1; x++) {
+							tile_fragment(keys, initialDepth, coverage, tg, (ry - ty0) * TILE_STRIDE + (x - tx0), value, ri, true, affine, fragments);
+							value = fadd(value, r.dx[0]);
 						}
-						value = fadd(value, r.dx[0]);
 					}
 				}
+				continue;
 			}
-			continue;
-		}
-		const int rp = lane >> 2;
-		const int32_t y1 = ty0 + 2 * rp;
-		const int32_t uL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp), uR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp);
-		const int32_t lL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp + 1), lR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp + 1);
-		if (y1 < r.top || y1 >= r.bottom) continue;
-		const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, tg.height);
-		if (!pair.any) continue;
-		for (int q = 0; q < 2; q++) {
-			const int32_t x = tx0 + 4 * (lane & 3) + 2 * q;
-			if (x < pair.obs || x >= pair.obe) continue;
-			const bool edge = quad_is_edge(pair, x);
-			float z[4];
-			quad_lanes(r.start[0], r.dx[0], r.dy[0], pair, y1, x, z);
-			for (int l = 0; l < 4; l++) {
-				if (!lane_covered(pair, x, edge, l)) continue;
-				const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-				if (yy >= tg.height || xx >= tg.width) continue;
-				const int pix = (yy - ty0) * TILE_W + (xx - tx0);
-				fragments++;
-				if (tg.coverage) atomicAdd(&coverage[pix], 1u);
-				bool pass = !depthTest || (affine ? (z[l] < initialDepth[pix]) : (z[l] > initialDepth[pix]));
-				if (pass) {
-					unsigned long long key = make_key(z[l], ri, depthTest, affine);
-					if (key > keys[pix]) atomicMax(&keys[pix], key);
+			// lane = (row pair, position in the 2x2 quad); it walks its position across the tile's quads
+			const int rp = lane >> 2, pos = lane & 3;
+			const int32_t y1 = ty0 + 2 * rp;
+			const int32_t uL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp), uR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp);
+			const int32_t lL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp + 1), lR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp + 1);
+			if (y1 < r.top || y1 >= r.bottom) continue;
+			const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, tg.height);
+			if (!pair.any) continue;
+			const int32_t x0 = max(tx0, pair.obs), x1 = min(tx0 + TILE_W, pair.obe);
+			if (x0 >= x1) continue;
+			const int32_t yy = y1 + (pos >> 1);
+			if (yy >= tg.height) continue;
+			const bool odd = (pos & 1) != 0;
+			const int32_t rowL = (pos < 2) ? pair.upperLeft : pair.lowerLeft, rowR = (pos < 2) ? pair.upperRight : pair.lowerRight;
+			const float dx = r.dx[0], d2 = fmul(dx, 2.0f);
+			const float P0 = fadd(fadd(r.start[0], fmul(dx, (float)pair.obs + 0.5f)), fmul(r.dy[0], (float)y1 + 0.5f));
+			const float R0 = (pos < 2) ? P0 : fadd(P0, r.dy[0]);
+			const bool allEdge = pair.ibe <= pair.ibs;
+			const int32_t nL = (pair.ibs - pair.obs) >> 1;
+			const float m = fmul(d2, (float)((pair.ibe - pair.ibs) >> 1));
+			// state of the reference's running sums at quad x0 (fillerTemplates.h:328-373)
+			int region; // 0 left edge, 1 full quads, 2 right edge
+			float R, V = 0.0f, Rb = 0.0f;
+			if (allEdge || x0 < pair.ibs) {
+				region = 0;
+				R = chain_add(R0, d2, (x0 - pair.obs) >> 1);
+			} else {
+				Rb = chain_add(R0, d2, nL);
+				if (x0 < pair.ibe) {
+					region = 1;
+					R = Rb;
+					V = chain_add(odd ? fadd(Rb, dx) : Rb, d2, (x0 - pair.ibs) >> 1);
+				} else {
+					region = 2;
+					R = chain_add(fadd(Rb, m), d2, (x0 - pair.ibe) >> 1);
+				}
+			}
+			const int pixRow = (yy - ty0) * TILE_STRIDE;
+			for (int32_t x = x0; x < x1; x += 2) {
+				const int32_t xx = x + (odd ? 1 : 0);
+				const float z = (region == 1) ? V : (odd ? fadd(R, dx) : R);
+				const bool covered = (region == 1) || (xx >= rowL && xx < rowR);
+				if (covered && xx < tg.width)
+					tile_fragment(keys, initialDepth, coverage, tg, pixRow + (xx - tx0), z, ri, depthTest, affine, fragments);
+				if (region == 0) {
+					R = fadd(R, d2);
+					if (!allEdge && x + 2 == pair.ibs) { region = 1; Rb = R; V = odd ? fadd(R, dx) : R; }
+				} else if (region == 1) {
+					V = fadd(V, d2);
+					if (x + 2 == pair.ibe) { region = 2; R = fadd(Rb, m); }
+				} else {
+					R = fadd(R, d2);
 				}
 			}
 		}
@@ -704,40 +779,51 @@ __global__ void __launch_bounds__(256) raster_kernel(const DrawRecord *__restric
 	__syncthreads();
 
 	if (inside) {
-		if (tg.coverage) tg.coverage[pixel] += coverage[tid];
-		const unsigned long long key = keys[tid];
-		if (tg.keys) tg.keys[pixel] = key;
-		if (key != 0ull) {
-			const uint32_t ri = key_record(key, depthTest);
-			const DrawRecord r = records[ri];
-			if (DEPTH_ONLY_1X1) {
-				int32_t left, right;
-				row_interval(r.flat, py, r.left, r.right, left, right);
-				float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
-				value = chain_add(value, r.dx[0], px - left);
-				tg.depth[(size_t)py * tg.depthStride + px] = value;
-			} else if (!record_is_small(r, tg.smallRows, tg.smallWidth)) {
-				// the winner is a large record: re-evaluate its quad exactly and shade this pixel
-				const int32_t y1 = py & ~1, x = px & ~1;
-				const int lane4 = ((py & 1) << 1) | (px & 1);
-				const RowPair pair = record_row_pair(r, y1, tg.height);
-				float w[3][4];
-				const int components = tg.color ? 3 : 1;
-				for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
-				if (tg.color) {
-					float wa[4], wb[4], wc[4];
-					lane_weights(w, affine, wa, wb, wc);
-					ShadeRecord shade;
-					make_shade(tasks[r.task], r.tri, shade);
-					float rgba[4];
-					shade_lane(shade, textures, wa, wb, wc, lane4, rgba);
-					tg.color[(size_t)py * tg.colorStride + px] = pack_saturated(rgba, tg.packOrder);
-				}
-				if (depthTest) tg.depth[(size_t)py * tg.depthStride + px] = w[0][lane4];
-			}
-		}
+		if (tg.coverage) tg.coverage[(size_t)py * tg.width + px] = coverage[me];
+		tg.keys[(size_t)py * tg.width + px] = keys[me];
 	}
 	if (tg.fragments && tid == 0) atomicAdd(tg.fragments, fragmentSum);
+}
+
+// One thread per pixel: the winning fragment's quad is re-evaluated exactly (its row pair's
+// intervals and the reference's running sums at that quad) and the pixel is shaded (deferred
+// shading: only winners are shaded, one per pixel).
+template <bool DEPTH_ONLY_1X1>
+__global__ void __launch_bounds__(256) resolve_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
+                                                      const TextureData *__restrict__ textures, TargetParams tg) {
+	const int32_t px = blockIdx.x * TILE_W + (threadIdx.x & 15), py = blockIdx.y * TILE_H + (threadIdx.x >> 4);
+	if (px >= tg.width || py >= tg.height) return;
+	const unsigned long long key = tg.keys[(size_t)py * tg.width + px];
+	if (key == 0ull) return;
+	const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
+	const uint32_t ri = key_record(key, depthTest);
+	const DrawRecord r = records[ri];
+	const uint32_t *recordRows = tg.rows + tg.rowOffsets[ri];
+	if (DEPTH_ONLY_1X1) {
+		int32_t left, right;
+		unpack_row(recordRows[py - r.top], left, right);
+		float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
+		value = chain_add(value, r.dx[0], px - left);
+		tg.depth[(size_t)py * tg.depthStride + px] = value;
+		return;
+	}
+	const int32_t y1 = py & ~1, x = px & ~1;
+	const int lane4 = ((py & 1) << 1) | (px & 1);
+	const RowPair pair = record_row_pair(r, recordRows, y1, tg.height);
+	float w[3][4];
+	const int components = tg.color ? 3 : 1;
+	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
+	const float depthValue = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
+	if (tg.color) {
+		float wa[4], wb[4], wc[4];
+		lane_weights(w, affine, wa, wb, wc);
+		ShadeRecord shade;
+		make_shade(tasks[r.task], r.tri, shade);
+		float rgba[4];
+		shade_lane(shade, textures, wa, wb, wc, lane4, rgba);
+		tg.color[(size_t)py * tg.colorStride + px] = pack_saturated(rgba, tg.packOrder);
+	}
+	if (depthTest) tg.depth[(size_t)py * tg.depthStride + px] = depthValue;
 }
 
 void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureData *textures, const TileBins &bins,
@@ -746,6 +832,8 @@ void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureD
 	if (tiles > 0) {
 		COUNT_LAUNCH();
 		raster_kernel<false><<<tiles, 256, 0, stream>>>(fb.records, tasks, textures, bins, target);
+		COUNT_LAUNCH();
+		resolve_kernel<false><<<dim3(bins.tilesX, bins.tilesY), 256, 0, stream>>>(fb.records, tasks, textures, target);
 	}
 }
 
@@ -754,6 +842,8 @@ void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, cons
 	if (tiles > 0) {
 		COUNT_LAUNCH();
 		raster_kernel<true><<<tiles, 256, 0, stream>>>(fb.records, nullptr, nullptr, bins, target);
+		COUNT_LAUNCH();
+		resolve_kernel<true><<<dim3(bins.tilesX, bins.tilesY), 256, 0, stream>>>(fb.records, nullptr, nullptr, target);
 	}
 }
 

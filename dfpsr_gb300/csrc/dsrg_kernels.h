@@ -33,6 +33,8 @@ struct FrameBuffers {
 	uint32_t *triCounts;      // per fan triangle: draw records it emits
 	uint32_t *triOffsets;     // exclusive scan of triCounts (+ running record count at [triangleCount])
 	DrawRecord *records;
+	uint32_t *rowOffsets;     // per record: first entry of its rows in `rows` (+ total at [recordCount])
+	uint32_t *rows;           // row intervals of every record, left | right << 16
 	uint32_t *recordCount;    // device counter of records in the frame
 	int32_t *errorFlag;       // device error bits
 	uint32_t *scanScratch;
@@ -58,12 +60,14 @@ struct TargetParams {
 	int32_t affine;           // orthogonal camera: depth test '<' on linear depth
 	uint32_t *coverage;       // optional per-pixel fragment counts (width * height, dense)
 	unsigned long long *fragments; // optional fragment total
-	unsigned long long *keys; // width * height depth keys shared by the small-triangle and tile kernels
+	unsigned long long *keys; // width * height winning (depth, record) keys, written by the tile pass
+	const uint32_t *rowOffsets; // see FrameBuffers
+	const uint32_t *rows;
 	int32_t smallRows;        // records whose raster bound is at most smallRows x smallWidth pixels are
-	int32_t smallWidth;       // drawn by one thread each instead of one warp per covered tile
+	int32_t smallWidth;       // walked by one lane each instead of by the whole warp
 };
 
-// True when one thread draws the whole record (dsrg small-triangle path).
+// True when one lane walks the whole record inside a tile (small-triangle path).
 __host__ __device__ inline bool record_is_small(const DrawRecord &r, int32_t smallRows, int32_t smallWidth) {
 	return (r.bottom - r.top) <= smallRows && (r.right - r.left) <= smallWidth;
 }
@@ -79,22 +83,18 @@ void launch_project(const TaskParams &task, const FrameBuffers &fb, cudaStream_t
 void launch_setup(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream);
 // Bins the first *recordCount records into tiles.  Returns the number of list entries needed
 // (reads it back, synchronising the stream) so that the caller can grow the list buffer.
-// Small records (record_is_small with smallRows/smallWidth) are left out of the bins; pass
-// smallRows = 0 to bin every record.
-uint32_t launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
-                          cudaStream_t stream);
+// Counts the (tile, record) pairs and scans them into bins.offsets (total at offsets[tiles]).
+void launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
+                      cudaStream_t stream);
+// Row counts of the records scanned into fb.rowOffsets (total at rowOffsets[recordCount]).
+void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream);
+// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176) into fb.rows.
+void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream);
 void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
                      cudaStream_t stream);
-// The three raster passes of a frame, in this order:
-//   launch_small_raster  depth keys of every small record (one thread per record) into target.keys
-//   launch_raster        per tile: keys of the large records, merged into target.keys; shades the
-//                        pixels that large records won
-//   launch_small_shade   shades the pixels that small records won (one thread per record)
-void launch_small_raster(const FrameBuffers &fb, uint32_t recordCount, const TargetParams &target, cudaStream_t stream);
+// One CTA per tile rasterises, depth-tests and shades every record binned to it.
 void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureData *textures, const TileBins &bins,
                    const TargetParams &target, cudaStream_t stream);
-void launch_small_shade(const FrameBuffers &fb, uint32_t recordCount, const TaskData *tasks, const TextureData *textures,
-                        const TargetParams &target, cudaStream_t stream);
 void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total).
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);

@@ -44,7 +44,7 @@ DSRG_HD uint32_t texel_load(const uint32_t *p, uint32_t index) {
 }
 
 // texture_sample_bilinear with MIP_INSIDE (api/textureAPI.h:320-430).
-DSRG_HD uint32_t sample_bilinear(const TextureData &t, float u, float v, uint32_t mip, bool highest) {
+DSRG_HD_CALL uint32_t sample_bilinear(const TextureData &t, float u, float v, uint32_t mip, bool highest) {
 	uint32_t scaleU = 256u << t.log2width, scaleV = 256u << t.log2height;
 	uint32_t maskX = t.maxWidthAndMask, maskY = t.maxHeightAndMask;
 	uint32_t log2Stride = t.log2width;
@@ -97,7 +97,7 @@ DSRG_HD void unpack_rgba(uint32_t c, float *out) {
 
 // getPixels_2x2 (shader/RgbaMultiply.h:74-106) for lane `lane` of a quad whose four lanes have
 // vertex weights wa/wb/wc.  The mip level of each texture comes from lanes 0..2.
-DSRG_HD void shade_lane(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
+DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
                         const float *wc, int lane, float *rgba) {
 	const bool hasDiffuse = (s.flags & SHADE_DIFFUSE) != 0, hasLight = (s.flags & SHADE_LIGHT) != 0;
 	const bool colorless = (s.flags & SHADE_COLORLESS) != 0, fade = (s.flags & SHADE_VERTEX_FADE) != 0;

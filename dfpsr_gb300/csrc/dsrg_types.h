@@ -14,6 +14,9 @@ namespace dsrg {
 static const int32_t TILE_W = 16;
 static const int32_t TILE_H = 16;
 static const int32_t TILE_PIXELS = TILE_W * TILE_H;
+// Row stride of the shared tile arrays: one word of padding keeps the 16 rows of a column in
+// different shared-memory banks.
+static const int32_t TILE_STRIDE = TILE_W + 1;
 
 // A plane a*x + b*y + c*z - offset <= 0 means inside (math/FPlane3D.h:38-46).
 struct Plane {
