@@ -1,0 +1,207 @@
+// Internal declarations shared by the host-side translation units of libdsrg
+// (objects behind the C ABI handles and host helpers); not part of the public ABI.
+#ifndef DSRG_INTERNAL_H
+#define DSRG_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dsrg.h"
+#include "dsrg_geometry.h"
+#include "dsrg_kernels.h"
+
+namespace dsrg {
+
+
+template <typename T>
+struct DeviceBuffer {
+	T *ptr = nullptr;
+	size_t capacity = 0;
+	cudaError_t reserve(size_t n, bool keep = false, size_t keepCount = 0, cudaStream_t stream = 0) {
+		if (n <= capacity) return cudaSuccess;
+		size_t newCapacity = capacity ? capacity : 1024;
+		while (newCapacity < n) newCapacity *= 2;
+		T *fresh = nullptr;
+		cudaError_t err = cudaMalloc((void **)&fresh, newCapacity * sizeof(T));
+		if (err != cudaSuccess) return err;
+		if (keep && ptr && keepCount) {
+			err = cudaMemcpyAsync(fresh, ptr, keepCount * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+			if (err != cudaSuccess) { cudaFree(fresh); return err; }
+			cudaStreamSynchronize(stream);
+		}
+		if (ptr) cudaFree(ptr);
+		ptr = fresh;
+		capacity = newCapacity;
+		return cudaSuccess;
+	}
+	void release() {
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		capacity = 0;
+	}
+};
+
+// Camera::createPerspective / createOrthogonal and ViewFrustum (implementation/render/Camera.h:55-156),
+// computed on the host in the reference's order (this file is built with -ffp-contract=off).
+inline Plane make_plane(float x, float y, float z, float offset) {
+	Plane p;
+	float l = sqrtf(x * x + y * y + z * z);
+	if (l == 0.0f) { p.nx = 0.0f; p.ny = 0.0f; p.nz = 1.0f; }
+	else { p.nx = x / l; p.ny = y / l; p.nz = z / l; }
+	p.offset = offset;
+	return p;
+}
+
+inline int frustum_perspective(Plane *planes, float nearClip, float farClip, float ws, float hs) {
+	planes[0] = make_plane(-1.0f, 0.0f, -ws, 0.0f);
+	planes[1] = make_plane(1.0f, 0.0f, -ws, 0.0f);
+	planes[2] = make_plane(0.0f, 1.0f, -hs, 0.0f);
+	planes[3] = make_plane(0.0f, -1.0f, -hs, 0.0f);
+	planes[4] = make_plane(0.0f, 0.0f, -1.0f, -nearClip);
+	planes[5] = make_plane(0.0f, 0.0f, 1.0f, farClip);
+	return std::isinf(farClip) && farClip > 0 ? 5 : 6;
+}
+
+inline int frustum_orthogonal(Plane *planes, float hw, float hh) {
+	planes[0] = make_plane(-1.0f, 0.0f, 0.0f, hw);
+	planes[1] = make_plane(1.0f, 0.0f, 0.0f, hw);
+	planes[2] = make_plane(0.0f, 1.0f, 0.0f, hh);
+	planes[3] = make_plane(0.0f, -1.0f, 0.0f, hh);
+	return 4;
+}
+
+inline CameraData make_camera(const dsrg_camera &d) {
+	CameraData c;
+	memset(&c, 0, sizeof(c));
+	for (int i = 0; i < 3; i++) {
+		c.position[i] = d.location[i];
+		c.xAxis[i] = d.location[3 + i];
+		c.yAxis[i] = d.location[6 + i];
+		c.zAxis[i] = d.location[9 + i];
+	}
+	c.imageWidth = (float)d.width;
+	c.imageHeight = (float)d.height;
+	c.perspective = d.perspective ? 1 : 0;
+	float ws = d.slope;
+	float hs = ws * c.imageHeight / c.imageWidth;
+	if (d.perspective) {
+		c.cullCount = frustum_perspective(c.cull, d.nearClip, d.farClip, ws * 1.0001f, hs * 1.0001f);
+		c.clipCount = frustum_perspective(c.clip, d.nearClip, d.farClip, ws * 2.0f, hs * 2.0f);
+	} else {
+		c.cullCount = frustum_orthogonal(c.cull, ws * 1.0001f, hs * 1.0001f);
+		c.clipCount = frustum_orthogonal(c.clip, ws * 2.0f, hs * 2.0f);
+	}
+	c.invWidthSlope = 0.5f / ws;
+	c.invHeightSlope = 0.5f / hs;
+	return c;
+}
+
+// Camera::isBoxSeen (implementation/render/Camera.h:202-217).
+inline bool box_seen(const CameraData &c, const float *mn, const float *mx, const float *modelToWorld) {
+	const float corners[8][3] = {{mn[0], mn[1], mn[2]}, {mx[0], mn[1], mn[2]}, {mn[0], mx[1], mn[2]}, {mx[0], mx[1], mn[2]},
+	                             {mn[0], mn[1], mx[2]}, {mx[0], mn[1], mx[2]}, {mn[0], mx[1], mx[2]}, {mx[0], mx[1], mx[2]}};
+	Vec3 cs[8];
+	for (int i = 0; i < 8; i++) cs[i] = world_to_camera(c, transform_point(modelToWorld, vec3(corners[i][0], corners[i][1], corners[i][2])));
+	for (int s = 0; s < c.cullCount; s++) {
+		bool anyInside = false;
+		for (int i = 0; i < 8; i++) if (plane_inside(c.cull[s], cs[i])) anyInside = true;
+		if (!anyInside) return false;
+	}
+	return true;
+}
+
+
+} // namespace dsrg
+
+using dsrg::DeviceBuffer;
+using dsrg::DrawRecord;
+using dsrg::TaskData;
+using dsrg::TextureData;
+using dsrg::CameraData;
+
+struct dsrg_context_s {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	std::string lastError;
+	// frame scratch, grown on demand and reused
+	DeviceBuffer<float> csx, csy, csz, isx, isy;
+	DeviceBuffer<int64_t> flatx, flaty;
+	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
+	DeviceBuffer<DrawRecord> records;
+	DeviceBuffer<TaskData> taskTable;
+	DeviceBuffer<uint32_t> control;      // [0] record count, [1] error flag
+	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
+	DeviceBuffer<TextureData> textureTable;
+	DeviceBuffer<uint32_t> stagingColor;
+	DeviceBuffer<float> stagingDepth;
+	DeviceBuffer<unsigned long long> fragmentCounter;
+	DeviceBuffer<unsigned long long> keys;
+	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;
+	int32_t smallRows = 8, smallWidth = 16; // one lane walks records whose raster bound is at most 8 x 16 pixels
+	int32_t counting = 0;
+	uint32_t *coverage = nullptr;
+	dsrg_stats stats;
+	cudaEvent_t eventStart = nullptr, eventStop = nullptr, eventRasterStart = nullptr, eventRasterStop = nullptr;
+	dsrg_renderer implicitRenderer = nullptr;
+};
+
+struct dsrg_texture_s {
+	dsrg_context context;
+	uint32_t *pixels = nullptr;
+	uint32_t fields[9];
+	uint32_t pixelCount = 0;
+	TextureData data;
+};
+
+struct dsrg_model_s {
+	dsrg_context context;
+	float *positions = nullptr;
+	int32_t *polygons = nullptr;
+	float *texCoords = nullptr;
+	float *colors = nullptr;
+	int32_t *triSource = nullptr;
+	int32_t pointCount = 0, polygonCount = 0, triangleCount = 0;
+	float minBound[3], maxBound[3];
+	dsrg_texture diffuse = nullptr, light = nullptr;
+	int32_t filter = 0;
+};
+
+struct dsrg_renderer_s {
+	dsrg_context context;
+	bool receiving = false;
+	dsrg_image color, depth;
+	bool hasColor = false, hasDepth = false;
+	int32_t width = 0, height = 0;
+	uint32_t *deviceColor = nullptr;
+	float *deviceDepth = nullptr;
+	int32_t colorStride = 0, depthStride = 0;
+	uint32_t triangleCount = 0;   // fan triangles submitted this frame
+	uint32_t recordCapacity = 0;
+	bool depthOnly = false;
+	bool affine = false;
+	bool cameraKnown = false;
+	std::vector<TextureData> textures;
+	std::vector<dsrg_texture> textureHandles;
+	std::vector<TaskData> tasks;
+};
+
+#define DSRG_CUDA_TRY(ctx, expr)                                                                      \
+	do {                                                                                         \
+		cudaError_t _e = (expr);                                                                 \
+		if (_e != cudaSuccess) {                                                                 \
+			(ctx)->lastError = std::string("CUDA error in " #expr ": ") + cudaGetErrorString(_e); \
+			return _e == cudaErrorMemoryAllocation ? DSRG_ERROR_OUT_OF_MEMORY : DSRG_ERROR_CUDA; \
+		}                                                                                        \
+	} while (0)
+
+inline int fail(dsrg_context ctx, int code, const std::string &message) {
+	if (ctx) ctx->lastError = message;
+	return code;
+}
+
+
+#endif
