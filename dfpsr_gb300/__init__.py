@@ -28,7 +28,7 @@ EXPORTED = [
     "dsrg_model_create", "dsrg_model_destroy",
     "dsrg_model_render", "dsrg_model_render_depth",
     "dsrg_renderer_create", "dsrg_renderer_destroy", "dsrg_renderer_begin", "dsrg_renderer_give_task",
-    "dsrg_renderer_end", "dsrg_renderer_takes_triangles",
+    "dsrg_renderer_end", "dsrg_renderer_takes_triangles", "dsrg_model_render_depth_noalloc",
 ]
 
 
@@ -85,6 +85,7 @@ def lib():
         l.dsrg_renderer_give_task.argtypes = [P, P, P, C.POINTER(Camera)]
         l.dsrg_renderer_end.argtypes = [P]
         l.dsrg_renderer_takes_triangles.argtypes = [P]
+        l.dsrg_model_render_depth_noalloc.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
         _lib = l
     return _lib
 

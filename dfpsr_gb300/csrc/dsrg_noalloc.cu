@@ -1,0 +1,182 @@
+// dsrg_model_render_depth_noalloc: model_renderDepth for callers that must not allocate GPU
+// memory while they render, such as a frame loop that runs under a strict no-allocation
+// policy after start-up (cudaMalloc and cudaFree synchronise the whole device and can stall
+// other work), or a host that hands the renderer a fixed memory budget up front.
+//
+// Every buffer the depth path needs between its kernels (projected points, draw records,
+// row intervals, tile lists, depth keys, counters) is carved out of one file-scope device
+// array of DSRG_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds until the
+// process exits.  The caller passes the inputs (a model created earlier) and the output
+// (a depth image in device memory).
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "dsrg_internal.h"
+
+using namespace dsrg;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[DSRG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+// Per-device device address of g_noallocScratch, looked up once per device.
+std::mutex g_scratchMutex;
+void *g_scratchAddress[64] = {};
+
+int scratch_address(dsrg_context ctx, unsigned char **out) {
+	if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: device index above 63");
+	std::lock_guard<std::mutex> lock(g_scratchMutex);
+	if (!g_scratchAddress[ctx->device]) {
+		// The array's name is only a host-side stand-in; its device address must be asked for,
+		// with the device current.
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+		if (e != cudaSuccess || !p)
+			return fail(ctx, DSRG_ERROR_CUDA, std::string("dsrg_model_render_depth_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+		g_scratchAddress[ctx->device] = p;
+	}
+	*out = (unsigned char *)g_scratchAddress[ctx->device];
+	return DSRG_OK;
+}
+
+// Bump allocator over the static array (nothing is ever freed; the layout is rebuilt per call).
+struct Carver {
+	unsigned char *base;
+	size_t used;
+	template <typename T>
+	T *take(size_t count) {
+		size_t at = (used + 255) & ~(size_t)255;
+		used = at + count * sizeof(T);
+		return (T *)(base + at);
+	}
+};
+
+const uint32_t MAX_RECORDS = 7u * DSRG_NOALLOC_MAX_TRIANGLES; // a clipped triangle is a fan of at most 7
+const uint32_t MAX_TILES = (uint32_t)((DSRG_NOALLOC_MAX_SIDE + 15) / 16) * (uint32_t)((DSRG_NOALLOC_MAX_SIDE + 15) / 16);
+
+} // namespace
+
+extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, const float *modelToWorld,
+                                               const dsrg_camera *camera, const dsrg_image *depth) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!m || !modelToWorld || !camera || !depth || !depth->data)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_render_depth_noalloc: null argument");
+	if (!depth->onDevice)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_render_depth_noalloc: the depth image must be device memory (onDevice = 1)");
+	if (depth->width <= 0 || depth->height <= 0 || depth->strideBytes < depth->width * 4 || depth->strideBytes % 4 != 0)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_render_depth_noalloc: invalid depth image");
+	if (depth->width > DSRG_NOALLOC_MAX_SIDE || depth->height > DSRG_NOALLOC_MAX_SIDE)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: depth image larger than DSRG_NOALLOC_MAX_SIDE (1024) pixels on a side");
+	if (m->pointCount > DSRG_NOALLOC_MAX_POINTS)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: model has more than DSRG_NOALLOC_MAX_POINTS (49152) points");
+	if (m->triangleCount > DSRG_NOALLOC_MAX_TRIANGLES)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: model has more than DSRG_NOALLOC_MAX_TRIANGLES (16384) triangles");
+	if (camera->width <= 0 || camera->height <= 0)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_model_render_depth_noalloc: camera without image size");
+	DSRG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+	unsigned char *base = nullptr;
+	int status = scratch_address(ctx, &base);
+	if (status != DSRG_OK) return status;
+
+	CameraData cam = make_camera(*camera);
+	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld)) return DSRG_OK; // ModelImpl::renderDepth (Model.cpp:199-211)
+	if (m->triangleCount == 0) return DSRG_OK;
+	cudaStream_t stream = ctx->stream;
+	const int32_t width = depth->width, height = depth->height;
+
+	// carve the scratch
+	Carver carve{base, 0};
+	const size_t np = (size_t)DSRG_NOALLOC_MAX_POINTS;
+	FrameBuffers fb;
+	memset(&fb, 0, sizeof(fb));
+	fb.points.csx = carve.take<float>(np); fb.points.csy = carve.take<float>(np); fb.points.csz = carve.take<float>(np);
+	fb.points.isx = carve.take<float>(np); fb.points.isy = carve.take<float>(np);
+	fb.points.flatx = carve.take<int64_t>(np); fb.points.flaty = carve.take<int64_t>(np);
+	fb.triCounts = carve.take<uint32_t>(DSRG_NOALLOC_MAX_TRIANGLES + 2);
+	fb.triOffsets = carve.take<uint32_t>(DSRG_NOALLOC_MAX_TRIANGLES + 2);
+	fb.records = carve.take<DrawRecord>(MAX_RECORDS);
+	uint32_t *rowCounts = carve.take<uint32_t>(MAX_RECORDS + 2);
+	fb.rowOffsets = carve.take<uint32_t>(MAX_RECORDS + 2);
+	fb.rows = carve.take<uint32_t>(DSRG_NOALLOC_MAX_ROWS);
+	uint32_t *control = carve.take<uint32_t>(4);
+	fb.recordCount = control;
+	fb.errorFlag = (int32_t *)(control + 1);
+	fb.scanScratchElems = scan_scratch_elems(MAX_RECORDS + 2);
+	fb.scanScratch = carve.take<uint32_t>(fb.scanScratchElems);
+	TileBins bins;
+	bins.tilesX = (width + TILE_W - 1) / TILE_W;
+	bins.tilesY = (height + TILE_H - 1) / TILE_H;
+	bins.counts = carve.take<uint32_t>(MAX_TILES);
+	bins.offsets = carve.take<uint32_t>(MAX_TILES + 1);
+	bins.cursors = carve.take<uint32_t>(MAX_TILES);
+	bins.lists = carve.take<uint32_t>(DSRG_NOALLOC_MAX_BIN_ENTRIES);
+	bins.listCapacity = DSRG_NOALLOC_MAX_BIN_ENTRIES;
+	unsigned long long *keys = carve.take<unsigned long long>((size_t)DSRG_NOALLOC_MAX_SIDE * DSRG_NOALLOC_MAX_SIDE);
+	if (carve.used > (size_t)DSRG_NOALLOC_SCRATCH_BYTES)
+		return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: scratch layout exceeds DSRG_NOALLOC_SCRATCH_BYTES");
+
+	// projection and triangle setup (renderTriangleFromDataDepth, renderCore.cpp:400-443)
+	TaskParams task;
+	memset(&task, 0, sizeof(task));
+	task.positions = m->positions;
+	task.polygons = m->polygons;
+	task.texCoords = m->texCoords;
+	task.colors = m->colors;
+	task.triSource = m->triSource;
+	task.pointCount = m->pointCount;
+	task.triangleCount = m->triangleCount;
+	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
+	task.camera = cam;
+	task.width = width;
+	task.height = height;
+	task.hasDepth = 1;
+	task.diffuse = -1;
+	task.light = -1;
+	task.depthOnly = 1;
+	// the counters start at zero on every call: the array keeps whatever the previous call left
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(control, 0, 4 * sizeof(uint32_t), stream));
+	launch_project(task, fb, stream);
+	launch_setup(task, fb, MAX_RECORDS, stream);
+	uint32_t counts[2] = {0, 0};
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(counts, control, sizeof(counts), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
+	if (counts[1] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: triangle setup reported device error bits " + std::to_string(counts[1]));
+	const uint32_t recordCount = counts[0];
+
+	// row intervals and tile lists
+	launch_row_offsets(fb, recordCount, rowCounts, stream);
+	launch_bin_count(fb, recordCount, bins, 0, 0, stream);
+	uint32_t totals[2] = {0, 0};
+	const uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totals[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totals[1], bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
+	if (totals[0] > DSRG_NOALLOC_MAX_ROWS)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles span more than DSRG_NOALLOC_MAX_ROWS (2097152) pixel rows");
+	if (totals[1] > DSRG_NOALLOC_MAX_BIN_ENTRIES)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles touch more than DSRG_NOALLOC_MAX_BIN_ENTRIES (1048576) tiles in total");
+	launch_rows(fb, recordCount, stream);
+	launch_bin_fill(fb, recordCount, bins, 0, 0, stream);
+
+	// depth raster (executeTriangleDrawingDepth, renderCore.cpp:343-387) and resolve
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(keys, 0, (size_t)width * height * sizeof(unsigned long long), stream));
+	TargetParams tg;
+	memset(&tg, 0, sizeof(tg));
+	tg.depth = (float *)depth->data;
+	tg.depthStride = depth->strideBytes / 4;
+	tg.width = width;
+	tg.height = height;
+	tg.affine = camera->perspective ? 0 : 1;
+	tg.keys = keys;
+	tg.rowOffsets = fb.rowOffsets;
+	tg.rows = fb.rows;
+	launch_raster_depth_only(fb, bins, tg, stream);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	uint32_t errorBits = 0;
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&errorBits, control + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
+	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: device error bits " + std::to_string(errorBits));
+	return DSRG_OK;
+}

@@ -133,6 +133,34 @@ int dsrg_renderer_end(dsrg_renderer renderer);
 /* renderer_takesTriangles (api/rendererAPI.h:67): 1 between begin and end. */
 int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
 
+/* ---- depth rendering without allocation; this entry point has no counterpart in the reference.
+ *
+ * For callers that must not allocate GPU memory while they render: a frame loop held to a
+ * no-allocation rule after start-up (cudaMalloc and cudaFree synchronise the whole device and
+ * can stall unrelated work), or a host that gives the renderer a fixed memory budget up front.
+ * It draws what dsrg_model_render_depth draws (model_renderDepth, api/modelAPI.h:291) and calls
+ * no cudaMalloc, cudaFree or other allocating routine.  Its intermediate buffers live in one
+ * static device array of DSRG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
+ * until the process exits.
+ *   - depth must be device memory (onDevice = 1) of at most DSRG_NOALLOC_MAX_SIDE pixels on a
+ *     side; the model at most DSRG_NOALLOC_MAX_POINTS points and DSRG_NOALLOC_MAX_TRIANGLES fan
+ *     triangles.  Larger inputs, or a view whose visible triangles need more than
+ *     DSRG_NOALLOC_MAX_ROWS pixel rows or DSRG_NOALLOC_MAX_BIN_ENTRIES (tile, triangle) pairs,
+ *     are rejected with DSRG_ERROR_UNSUPPORTED and a message naming the limit.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress);
+ *     make that first call before any stream capture.
+ *   - Every call on a device shares the same array and leaves its contents behind (each call
+ *     clears what it needs cleared); calls whose GPU work overlaps, from any context or thread,
+ *     race on it, so they must be serialised. */
+#define DSRG_NOALLOC_SCRATCH_BYTES (36u * 1024u * 1024u)
+#define DSRG_NOALLOC_MAX_SIDE 1024
+#define DSRG_NOALLOC_MAX_POINTS 49152
+#define DSRG_NOALLOC_MAX_TRIANGLES 16384
+#define DSRG_NOALLOC_MAX_ROWS 2097152u
+#define DSRG_NOALLOC_MAX_BIN_ENTRIES 1048576u
+int dsrg_model_render_depth_noalloc(dsrg_context context, dsrg_model model, const float *modelToWorld,
+                                    const dsrg_camera *camera, const dsrg_image *depth);
+
 #ifdef __cplusplus
 }
 #endif
