@@ -534,16 +534,15 @@ uint32_t or_sample_bilinear(const or_texture *t, float u, float v, uint32_t mipL
 	return or_interpolate_color_bilinear(a, b, c, d, weightX, weightY);
 }
 
-/* texture_sample_nearest (textureAPI.h:218-236) with MIP_INSIDE as used by the shaders. */
+/* texture_sample_nearest with its default template arguments (api/textureAPI.h:218-236): the mip level
+ * is not assumed inside the pyramid, so texel coordinates are tiled with the clamped masks of
+ * texture_getPixelOffset. */
 uint32_t or_sample_nearest(const or_texture *t, float u, float v, uint32_t mipLevel, int highestResolution) {
 	uint32_t scaleU = 1u << t->log2width, scaleV = 1u << t->log2height;
 	if (!highestResolution) { scaleU >>= mipLevel; scaleV >>= mipLevel; }
 	uint32_t x = trunc_u32((u + 256.0f) * (float)scaleU);
 	uint32_t y = trunc_u32((v + 256.0f) * (float)scaleV);
-	uint32_t mip = highestResolution ? 0u : mipLevel;
-	uint32_t maskX = t->maxWidthAndMask >> mip, maskY = t->maxHeightAndMask >> mip;
-	uint32_t off = ((y & maskY) << (t->log2width - mip)) | (x & maskX);
-	return t->pixels[(highestResolution ? t->startOffset : or_texture_pixel_offset_to_layer(t, mip)) + off];
+	return or_texture_read_pixel(t, x, y, highestResolution ? 0u : mipLevel);
 }
 
 /* texture_getMipLevelIndex (textureAPI.h:471-495) on lanes 0 (upper left), 1 (upper right), 2 (lower left). */

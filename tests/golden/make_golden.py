@@ -1,0 +1,219 @@
+#!/usr/bin/env python3
+"""Regenerates the golden fixtures in tests/golden/ (run where the reference sources exist).
+
+texture_kats.json
+    The known-answer assertions of the reference's own texture test
+    (Source/test/tests/TextureTest.cpp), read from that file as text: pyramid fields,
+    texel offsets, pixel reads after writes, nearest sampling and the 8-bit linear mix.
+render_*.npz
+    Small seeded scenes (inputs stored in the file) rendered by the reference itself, built
+    from its sources as the exact (scalar, no-FMA) variant by oracle/Makefile.ref, through
+    model_render / renderer_* / model_renderDepth.
+
+Usage: python tests/golden/make_golden.py [reference root, default $DFPSR_REFERENCE or /root/reference]
+"""
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def f32_expr(text):
+    """Evaluates a C float expression of literals, +, -, *, / and parentheses in binary32."""
+    tokens = re.findall(r"\d+\.\d*f?|\d+f|\d+u?|[-+*/()]", text.replace(" ", ""))
+
+    def literal(tok):
+        return np.float32(float(tok.rstrip("fu")))
+
+    pos = 0
+
+    def expr():
+        nonlocal pos
+        value = term()
+        while pos < len(tokens) and tokens[pos] in "+-":
+            op = tokens[pos]; pos += 1
+            rhs = term()
+            value = np.float32(value + rhs) if op == "+" else np.float32(value - rhs)
+        return value
+
+    def term():
+        nonlocal pos
+        value = factor()
+        while pos < len(tokens) and tokens[pos] in "*/":
+            op = tokens[pos]; pos += 1
+            rhs = factor()
+            value = np.float32(value * rhs) if op == "*" else np.float32(value / rhs)
+        return value
+
+    def factor():
+        nonlocal pos
+        tok = tokens[pos]
+        if tok == "-":
+            pos += 1
+            return np.float32(-factor())
+        if tok == "(":
+            pos += 1
+            v = expr()
+            pos += 1
+            return v
+        pos += 1
+        return literal(tok)
+
+    return float(expr())
+
+
+def split_args(text):
+    depth, cur, out = 0, "", []
+    for ch in text:
+        if ch == "," and depth == 0:
+            out.append(cur.strip()); cur = ""
+            continue
+        depth += ch == "("
+        depth -= ch == ")"
+        cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def int_literal(tok):
+    tok = tok.strip().rstrip("u")
+    return int(tok, 2) if tok.startswith("0b") else int(tok)
+
+
+def lanes(tok):
+    m = re.match(r"U32x(\d+)\((.*)\)$", tok.strip())
+    vals = [int_literal(v) for v in split_args(m.group(2))]
+    n = int(m.group(1))
+    return vals * n if len(vals) == 1 else vals
+
+
+def texture_kats(reference_root):
+    path = os.path.join(reference_root, "Source", "test", "tests", "TextureTest.cpp")
+    blocks, current, mix = [], None, []
+    for raw in open(path, encoding="utf-8-sig"):
+        line = raw.strip()
+        m = re.match(r"TextureRgbaU8 texture = TextureRgbaU8\((.*)\);", line)
+        if m:
+            args = [int(a) for a in split_args(m.group(1))]
+            current = {"log2w": args[0], "log2h": args[1], "maxMip": args[2] if len(args) > 2 else 15,
+                       "fields": {}, "layer": [], "offset": [], "writes": [], "read": [], "nearest": []}
+            blocks.append(current)
+            continue
+        if line.startswith("U32x4 mixedColor = texture_interpolate_color_linear"):
+            mix.append(line)
+            continue
+        if mix and len(mix) < 8 and not line.startswith("ASSERT_EQUAL_SIMD(mixedColor"):
+            mix.append(line)
+            continue
+        if current is None:
+            continue
+        m = re.match(r"ASSERT_EQUAL\(texture\.impl_(\w+)\s*,\s*(\w+)\);", line)
+        if m:
+            current["fields"][m.group(1)] = int_literal(m.group(2)); continue
+        m = re.match(r"ASSERT_EQUAL\(texture_get(MaxWidth|MaxHeight|SmallestMipLevel)\(texture\),\s*(\d+)\);", line)
+        if m:
+            current["fields"][m.group(1)] = int(m.group(2)); continue
+        m = re.match(r"ASSERT\((!?)texture_hasPyramid\(texture\)\);", line)
+        if m:
+            current["fields"]["hasPyramid"] = 0 if m.group(1) else 1; continue
+        m = re.match(r"ASSERT_EQUAL\(texture_getPixelOffsetToLayer\(texture,\s*(\w+)\),\s*(\w+)\);", line)
+        if m:
+            current["layer"].append([int_literal(m.group(1)), int_literal(m.group(2))]); continue
+        m = re.match(r"ASSERT_EQUAL\(texture_getPixelOffset\(texture,(.*)\),\s*(\w+)\);", line)
+        if m:
+            a = [int_literal(v) for v in split_args(m.group(1))]
+            current["offset"].append(a + [int_literal(m.group(2))]); continue
+        m = re.match(r"ASSERT_EQUAL_SIMD\(texture_getPixelOffset\(texture, (.*)\), (U32x\d+\(.*\))\);", line)
+        if m:
+            xs, ys, ms = [lanes(v) for v in split_args(m.group(1))]
+            expected = lanes(m.group(2))
+            for x, y, mm, e in zip(xs, ys, ms, expected):
+                current["offset"].append([x, y, mm, e])
+            continue
+        m = re.match(r"texture_writePixel\(texture,(.*)\);", line)
+        if m:
+            current["writes"].append([int_literal(v) for v in split_args(m.group(1))]); continue
+        m = re.match(r"ASSERT_EQUAL\(texture_readPixel\(texture,(.*)\),\s*(\w+)\);", line)
+        if m:
+            current["read"].append([int_literal(v) for v in split_args(m.group(1))] + [int_literal(m.group(2))]); continue
+        m = re.match(r"ASSERT_EQUAL\(texture_sample_nearest\(texture,(.*)\),\s*(\w+)\);", line)
+        if m:
+            a = split_args(m.group(1))
+            current["nearest"].append([f32_expr(a[0]), f32_expr(a[1]), int_literal(a[2]), int_literal(m.group(2))]); continue
+    # the 8-bit linear mix: four packed lanes of colour A, colour B, weight and the expected result
+    text = " ".join(mix)
+    packs = re.findall(r"packOrder_packBytes\((U32x4\([^)]*\)), (U32x4\([^)]*\)), (U32x4\([^)]*\)), (U32x4\([^)]*\))\)", text)
+    weight = lanes(re.search(r"\),\s*(U32x4\([^)]*\))\s*\);", text).group(1))
+    expect_text = open(path, encoding="utf-8-sig").read()
+    em = re.search(r"U32x4 expectedColor = packOrder_packBytes\((U32x4\([^)]*\)), (U32x4\([^)]*\)), (U32x4\([^)]*\)), (U32x4\([^)]*\))\);", expect_text)
+
+    def pack(groups):
+        ch = [lanes(g) for g in groups]
+        return [ch[0][i] | (ch[1][i] << 8) | (ch[2][i] << 16) | (ch[3][i] << 24) for i in range(4)]
+
+    linear = {"a": pack(packs[0]), "b": pack(packs[1]), "weight": weight, "expected": pack(em.groups())}
+    return {"source": "Source/test/tests/TextureTest.cpp", "textures": blocks, "linear_mix": linear}
+
+
+def render_cases():
+    from dfpsr_gb300 import scenes
+    cases = {}
+    cases["random_small"] = scenes.random_triangles(seed=101, triangles=260, width=128, height=96, texture_size=64)
+    cases["terrain_small"] = scenes.terrain(seed=102, grid=48, width=160, height=96, texture_size=64, camera_height=40.0)
+    clip = scenes.random_triangles(seed=103, triangles=400, width=128, height=96, texture_size=32)
+    clip.camera_location = scenes.camera_location((0.1, 0.2, -0.3), (0.0, 0.0, 1.0))
+    cases["near_clipping"] = clip
+    base = scenes.random_triangles(seed=104, triangles=200, width=96, height=72, texture_size=32)
+    cases["variant_untextured"] = scenes.with_variant(base, texture=False)
+    cases["variant_colorless"] = scenes.with_variant(base, colors="white")
+    cases["variant_lightmap"] = scenes.with_variant(base, light=True)
+    ortho = scenes.random_triangles(seed=105, triangles=240, width=96, height=80, texture_size=32)
+    ortho.perspective = False
+    ortho.slope = 1.3
+    cases["orthogonal"] = ortho
+    return cases
+
+
+def save_case(name, scene, variant="exact"):
+    from oracle import ref
+    model = ref.RefModel(scene, variant)
+    color, depth = model.render()
+    threaded_color, threaded_depth = model.render(threaded=True)
+    assert np.array_equal(color, threaded_color) and np.array_equal(depth.view(np.uint32), threaded_depth.view(np.uint32))
+    bgra, _ = model.render(pack_order=1)
+    depth_only = model.render_depth()
+    payload = dict(width=scene.width, height=scene.height, positions=scene.positions, poly_indices=scene.poly_indices,
+                   tex_coords=scene.tex_coords, colors=scene.colors, filter=scene.filter,
+                   camera_location=scene.camera_location, perspective=int(scene.perspective), slope=scene.slope,
+                   near_clip=scene.near_clip, far_clip=scene.far_clip, model_to_world=scene.model_to_world,
+                   diffuse_levels=scene.diffuse_levels, light_levels=scene.light_levels,
+                   color=color, depth=depth, color_bgra=bgra, depth_only=depth_only)
+    if scene.diffuse is not None:
+        payload["diffuse"] = scene.diffuse
+    if scene.light is not None:
+        payload["light"] = scene.light
+    np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), **payload)
+
+
+def main():
+    reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DFPSR_REFERENCE", "/root/reference")
+    from oracle import ref
+    os.environ["DFPSR_REFERENCE"] = reference_root
+    if not ref.build():
+        raise SystemExit("the reference could not be built from " + reference_root)
+    with open(os.path.join(HERE, "texture_kats.json"), "w") as f:
+        json.dump(texture_kats(reference_root), f, indent=0)
+    for name, scene in render_cases().items():
+        save_case(name, scene)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

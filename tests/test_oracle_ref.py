@@ -1,0 +1,69 @@
+"""The oracle against the reference itself, run here where the reference was built from its
+sources (skipped elsewhere): bit-exact against the exact (scalar, no-FMA) build on seeded
+scenes, including the full 800x600 random-triangle configuration and the threaded renderer."""
+import numpy as np
+import pytest
+
+from dfpsr_gb300 import scenes
+
+
+@pytest.fixture(scope="module")
+def ref_lib(built):
+    from oracle import ref
+    if not ref.available("exact"):
+        pytest.skip("the reference was not built from source on this machine")
+    return ref
+
+
+CASES = {
+    "random_800x600": lambda: scenes.random_triangles(seed=1234),
+    "terrain_grid128": lambda: scenes.terrain(seed=3, grid=128, width=640, height=360, texture_size=256),
+    "clipping": lambda: _clipping(),
+    "orthogonal": lambda: _ortho(),
+    "lightmap": lambda: scenes.with_variant(scenes.random_triangles(seed=8, triangles=1500, width=256, height=192), light=True),
+}
+
+
+def _clipping():
+    s = scenes.random_triangles(seed=9, triangles=3000, width=400, height=300)
+    s.camera_location = scenes.camera_location((0.1, 0.2, -0.3), (0.0, 0.0, 1.0))
+    return s
+
+
+def _ortho():
+    s = scenes.random_triangles(seed=23, triangles=1500, width=256, height=200)
+    s.perspective = False
+    s.slope = 1.3
+    return s
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_equals_reference_exact_build(ref_lib, name):
+    from oracle import port
+    scene = CASES[name]()
+    model = ref_lib.RefModel(scene, "exact")
+    rc, rd = model.render()
+    oc, od, _ = port.render(scene)
+    assert np.array_equal(rc, oc)
+    assert np.array_equal(rd.view(np.uint32), od.view(np.uint32))
+    tc, td = model.render(threaded=True)
+    bc, bd, _ = port.render(scene, bands=12, threads=4)
+    assert np.array_equal(tc, bc) and np.array_equal(td.view(np.uint32), bd.view(np.uint32))
+    depth_ref = model.render_depth()
+    depth_oracle, _ = port.render_depth(scene)
+    assert np.array_equal(depth_ref.view(np.uint32), depth_oracle.view(np.uint32))
+
+
+def test_row_intervals_equal_reference(ref_lib):
+    """rasterizeTriangle's row intervals (ITriangle2D.cpp:150-176) for random and extreme triangles."""
+    from oracle import port
+    r = np.random.default_rng(77)
+    for i in range(3000):
+        f = r.integers(-200 * 256, 1000 * 256, 6).astype(np.int64)
+        if i % 3 == 1:
+            f[1] = f[3] + r.integers(-2, 3)
+        clip = [0, 0, 800, 600]
+        a = ref_lib.triangle_rows(f, clip)
+        b = port.triangle_rows(f, clip)
+        assert a[0] == b[0] or len(a[1]) == 0
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
