@@ -44,6 +44,7 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=["terrain", "random"], default="terrain")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
+    p.add_argument("--batch-frames", type=int, default=256, help="frames of the mixed-size batch (0 skips it)")
     return p.parse_args()
 
 
@@ -117,6 +118,112 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def batched_section(ctx, args, flush):
+    """The mixed-size batch: 256 frames of random triangles (resolutions uniform over 64x64,
+    256x256, 640x480 and 1024x768, 1k-200k triangles log-uniform, a 256x256 texture each),
+    drawn per frame through dsrg_model_render (plain) and all at once through dsrg_batch_render
+    (batched, after the autotuner picked the tile kernel's launch shape), targets in HBM."""
+    import torch
+    import dfpsr_gb300 as d
+    from dfpsr_gb300 import scenes
+    frames = scenes.batch_frames(seed=4321, frames=args.batch_frames)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    models = [d.Model(ctx, s) for s in frames]
+    colors = [torch.zeros((s.height, s.width), dtype=torch.int32, device="cuda") for s in frames]
+    depths = [torch.zeros((s.height, s.width), dtype=torch.float32, device="cuda") for s in frames]
+    batch = d.Batch(ctx)
+    for i, m in enumerate(models):
+        batch.add_frame(colors[i], depths[i])
+        batch.give_task(i, m)
+
+    def clear():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            for c, z in zip(colors, depths):
+                c.zero_()
+                z.zero_()
+
+    tuning = batch.autotune(rounds=1)
+    ctx.set_counting(True)
+    clear()
+    batch.render()
+    stats = ctx.stats()
+    fragments = stats["fragments"]
+    ctx.set_counting(False)
+    for _ in range(3):
+        clear()
+        batch.render()
+    steps = max(1, min(args.steps, 10))
+    batch_ms, raster_ms = [], []
+    for _ in range(steps):
+        clear()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        batch.render()
+        b.record(stream)
+        raster_ms.append(ctx.stats()["raster_milliseconds"])
+        batch_ms.append((a, b))
+    torch.cuda.synchronize()
+    batch_s = statistics.median([a.elapsed_time(b) for a, b in batch_ms]) / 1e3
+
+    def plain_pass():
+        total = 0.0
+        for i, m in enumerate(models):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                colors[i].zero_()
+                depths[i].zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render(m, m.camera, colors[i], depths[i])
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b) / 1e3
+        return total
+
+    plain_pass()
+    plain_s = min(plain_pass() for _ in range(2))
+    # end to end: host images (page-locked) through the batch API
+    host = [(torch.zeros((s.height, s.width), dtype=torch.int32).pin_memory().numpy(),
+             torch.zeros((s.height, s.width), dtype=torch.float32).pin_memory().numpy()) for s in frames]
+    hbatch = d.Batch(ctx)
+    for i, m in enumerate(models):
+        hbatch.add_frame(*host[i])
+        hbatch.give_task(i, m)
+    hbatch.render()
+    e2e = []
+    for _ in range(steps):
+        for c, z in host:
+            c.fill(0)
+            z.fill(0.0)
+        t0 = time.perf_counter()
+        hbatch.render()
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e)
+    host_bytes = int(sum(c.nbytes + z.nbytes for c, z in host))
+    n = len(frames)
+    out = {
+        "workload": f"{n} frames, resolutions uniform over 64x64/256x256/640x480/1024x768, 1k-200k random triangles "
+                    "(log-uniform) per frame, own 256x256 RGBA8 texture per frame, depth tested",
+        "frames": n, "triangles": int(sum(s.triangle_count for s in frames)),
+        "pixels": int(sum(s.width * s.height for s in frames)), "fragments": fragments,
+        "draw_records": stats["draw_records"], "bin_entries": stats["bin_entries"],
+        "batched": {"frames_per_s": n / batch_s, "Mfrag_per_s": fragments / batch_s / 1e6, "ms_per_batch": batch_s * 1e3,
+                    "raster_ms": statistics.median(raster_ms)},
+        "plain": {"frames_per_s": n / plain_s, "Mfrag_per_s": fragments / plain_s / 1e6, "ms_per_batch": plain_s * 1e3},
+        "batched_over_plain": plain_s / batch_s,
+        "e2e": {"frames_per_s": n / e2e_s, "Mfrag_per_s": fragments / e2e_s / 1e6, "h2d_bytes_per_batch": host_bytes,
+                "d2h_bytes_per_batch": host_bytes},
+        "tuning": tuning,
+        "l2": "flushed before every batch and before every plain frame (256 MB write)",
+    }
+    hbatch.destroy()
+    batch.destroy()
+    for m in models:
+        m.destroy()
+    return out
 
 
 def cpu_baseline(scene, seconds: float):
@@ -296,6 +403,8 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
+        if args.batch_frames > 0:
+            line["batch"] = batched_section(ctx, args, flush)
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
         print(json.dumps(line), flush=True)

@@ -29,6 +29,8 @@ EXPORTED = [
     "dsrg_model_render", "dsrg_model_render_depth",
     "dsrg_renderer_create", "dsrg_renderer_destroy", "dsrg_renderer_begin", "dsrg_renderer_give_task",
     "dsrg_renderer_end", "dsrg_renderer_takes_triangles", "dsrg_model_render_depth_noalloc",
+    "dsrg_batch_create", "dsrg_batch_destroy", "dsrg_batch_clear", "dsrg_batch_add_frame", "dsrg_batch_give_task",
+    "dsrg_batch_render", "dsrg_context_get_tuning", "dsrg_context_set_tuning", "dsrg_batch_autotune",
 ]
 
 
@@ -51,6 +53,15 @@ class Image(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("fragments", C.c_uint64), ("drawRecords", C.c_uint64), ("binEntries", C.c_uint64),
                 ("milliseconds", C.c_float), ("rasterMilliseconds", C.c_float), ("kernelLaunches", C.c_uint64)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("threadsPerTile", C.c_int32), ("ctasPerSm", C.c_int32), ("smallRows", C.c_int32),
+                ("smallWidth", C.c_int32), ("graphs", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"threads_per_tile": self.threadsPerTile, "ctas_per_sm": self.ctasPerSm, "small_rows": self.smallRows,
+                "small_width": self.smallWidth, "graphs": self.graphs}
 
 
 _lib = None
@@ -86,6 +97,15 @@ def lib():
         l.dsrg_renderer_end.argtypes = [P]
         l.dsrg_renderer_takes_triangles.argtypes = [P]
         l.dsrg_model_render_depth_noalloc.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
+        l.dsrg_batch_create.argtypes = [P, C.POINTER(P)]
+        l.dsrg_batch_destroy.argtypes = [P]
+        l.dsrg_batch_clear.argtypes = [P]
+        l.dsrg_batch_add_frame.argtypes = [P, C.POINTER(Image), C.POINTER(Image), C.POINTER(I)]
+        l.dsrg_batch_give_task.argtypes = [P, I, P, P, C.POINTER(Camera)]
+        l.dsrg_batch_render.argtypes = [P]
+        l.dsrg_context_get_tuning.argtypes = [P, C.POINTER(Tuning)]
+        l.dsrg_context_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+        l.dsrg_batch_autotune.argtypes = [P, I, C.POINTER(Tuning)]
         _lib = l
     return _lib
 
@@ -154,7 +174,7 @@ class Context:
         """Destroys the context after every model, texture and renderer made from it."""
         if getattr(self, "handle", None):
             kids = list(self._children)
-            for kind in (Renderer, Model, Texture):
+            for kind in (Batch, Renderer, Model, Texture):
                 for child in kids:
                     if isinstance(child, kind):
                         child.destroy()
@@ -201,6 +221,30 @@ class Context:
 
     def renderer(self) -> "Renderer":
         return Renderer(self)
+
+    def batch(self) -> "Batch":
+        return Batch(self)
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self._check(self._l.dsrg_context_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, threads_per_tile: Optional[int] = None, ctas_per_sm: Optional[int] = None,
+                   small_rows: Optional[int] = None, small_width: Optional[int] = None, graphs: Optional[bool] = None):
+        t = Tuning()
+        self._check(self._l.dsrg_context_get_tuning(self.handle, C.byref(t)))
+        if threads_per_tile is not None:
+            t.threadsPerTile = threads_per_tile
+        if ctas_per_sm is not None:
+            t.ctasPerSm = ctas_per_sm
+        if small_rows is not None:
+            t.smallRows = small_rows
+        if small_width is not None:
+            t.smallWidth = small_width
+        if graphs is not None:
+            t.graphs = 1 if graphs else 0
+        self._check(self._l.dsrg_context_set_tuning(self.handle, C.byref(t)))
 
 
 class Texture:
@@ -299,6 +343,55 @@ class Renderer:
     def destroy(self):
         if getattr(self, "handle", None) and self.ctx.handle:
             self.ctx._l.dsrg_renderer_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Batch:
+    """dsrg_batch: many frames, each its own renderer_begin ... renderer_end, drawn in one pass."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_batch_create(ctx.handle, C.byref(h)))
+        self.handle = h
+        self._keep = []  # images and structs the library points at until the batch is cleared
+        ctx._adopt(self)
+
+    def add_frame(self, color=None, depth=None, pack_order: int = 0) -> int:
+        ci, di = image_struct(color, pack_order), image_struct(depth)
+        index = C.c_int32()
+        self.ctx._check(self.ctx._l.dsrg_batch_add_frame(self.handle, C.byref(ci) if ci else None,
+                                                         C.byref(di) if di else None, C.byref(index)))
+        self._keep.append((color, depth))
+        return index.value
+
+    def give_task(self, frame: int, model: Model, camera: Optional[Camera] = None, transform=None):
+        t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
+        cam = model.camera if camera is None else camera
+        self.ctx._check(self.ctx._l.dsrg_batch_give_task(self.handle, frame, model.handle, t.ctypes.data, C.byref(cam)))
+        self._keep.append(model)
+
+    def render(self):
+        self.ctx._check(self.ctx._l.dsrg_batch_render(self.handle))
+
+    def autotune(self, rounds: int = 2) -> dict:
+        t = Tuning()
+        self.ctx._check(self.ctx._l.dsrg_batch_autotune(self.handle, rounds, C.byref(t)))
+        return t.as_dict()
+
+    def clear(self):
+        self.ctx._check(self.ctx._l.dsrg_batch_clear(self.handle))
+        self._keep = []
+
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_batch_destroy(self.handle)
         self.handle = None
 
     def __del__(self):

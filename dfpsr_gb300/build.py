@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdsrg.so")
-SOURCES = ["dsrg_kernels.cu", "dsrg_api.cu", "dsrg_noalloc.cu"]
+SOURCES = ["dsrg_kernels.cu", "dsrg_api.cu", "dsrg_noalloc.cu", "dsrg_pipeline.cu", "dsrg_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-Xptxas", "-O3"]
@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for f in [pool.submit(run, j) for j in jobs]:
             f.result()
     if force or jobs or _stale(LIB, objs):
-        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"])
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread", "-Xlinker", "--no-undefined"])
     return LIB
 
 

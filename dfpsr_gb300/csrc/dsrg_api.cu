@@ -52,8 +52,10 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();
-	ctx->records.release(); ctx->taskTable.release(); ctx->keys.release();
+	ctx->records.release(); ctx->tables.release(); ctx->keys.release();
+	if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
 	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
+	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);
 	cudaEventDestroy(ctx->eventStop);
 	cudaEventDestroy(ctx->eventRasterStart);
@@ -318,12 +320,10 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 		}
 	}
 	r->triangleCount = 0;
-	r->recordCapacity = (uint32_t)ctx->records.capacity;
 	r->cameraKnown = false;
 	r->textures.clear();
 	r->textureHandles.clear();
 	r->tasks.clear();
-	CUDA_TRY(ctx, cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream));
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStart, ctx->stream));
 	r->receiving = true;
 	return DSRG_OK;
@@ -366,54 +366,15 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	task.pointCount = m->pointCount;
 	task.triangleCount = m->triangleCount;
 	task.orderBase = r->triangleCount;
-	task.taskIndex = (uint32_t)r->tasks.size();
+	task.frame = 0;
 	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
 	task.camera = cam;
-	task.width = r->width;
-	task.height = r->height;
-	task.hasColor = r->hasColor ? 1 : 0;
-	task.hasDepth = r->hasDepth ? 1 : 0;
 	task.filter = m->filter;
 	task.diffuse = r->depthOnly ? -1 : texture_slot(r, m->diffuse);
 	task.light = r->depthOnly ? -1 : texture_slot(r, m->light);
 	task.depthOnly = r->depthOnly ? 1 : 0;
-	TaskData td;
-	td.polygons = m->polygons;
-	td.texCoords = m->texCoords;
-	td.colors = m->colors;
-	td.triSource = m->triSource;
-	td.diffuse = task.diffuse;
-	td.light = task.light;
-	td.filter = m->filter;
-	td.pad = 0;
-	size_t np = (size_t)m->pointCount, nt = (size_t)m->triangleCount;
-	CUDA_TRY(ctx, ctx->csx.reserve(np)); CUDA_TRY(ctx, ctx->csy.reserve(np)); CUDA_TRY(ctx, ctx->csz.reserve(np));
-	CUDA_TRY(ctx, ctx->isx.reserve(np)); CUDA_TRY(ctx, ctx->isy.reserve(np));
-	CUDA_TRY(ctx, ctx->flatx.reserve(np)); CUDA_TRY(ctx, ctx->flaty.reserve(np));
-	CUDA_TRY(ctx, ctx->triCounts.reserve(nt + 2));
-	CUDA_TRY(ctx, ctx->triOffsets.reserve(nt + 2));
-	size_t scanElems = scan_scratch_elems((uint32_t)(nt + 2));
-	CUDA_TRY(ctx, ctx->scanScratch.reserve(scanElems));
-	// A triangle clipped against six planes is a fan of at most seven triangles.
-	size_t needed = (size_t)r->triangleCount * 7 + nt * 7;
-	CUDA_TRY(ctx, ctx->records.reserve(needed, true, (size_t)r->triangleCount * 7, ctx->stream));
-	r->recordCapacity = (uint32_t)ctx->records.capacity;
-	FrameBuffers fb;
-	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
-	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
-	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
-	fb.triCounts = ctx->triCounts.ptr;
-	fb.triOffsets = ctx->triOffsets.ptr;
-	fb.records = ctx->records.ptr;
-	fb.recordCount = ctx->control.ptr;
-	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
-	fb.scanScratch = ctx->scanScratch.ptr;
-	fb.scanScratchElems = ctx->scanScratch.capacity;
-	r->tasks.push_back(td);
-	launch_project(task, fb, ctx->stream);
-	launch_setup(task, fb, r->recordCapacity, ctx->stream);
-	CUDA_TRY(ctx, cudaGetLastError());
-	r->triangleCount += (uint32_t)nt;
+	r->tasks.push_back(task);
+	r->triangleCount += (uint32_t)m->triangleCount;
 	return DSRG_OK;
 }
 
@@ -426,114 +387,38 @@ static int end_frame(dsrg_renderer r) {
 	dsrg_context ctx = r->context;
 	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
 	r->receiving = false;
-	uint32_t control[2] = {0, 0};
-	CUDA_TRY(ctx, cudaMemcpyAsync(control, ctx->control.ptr, sizeof(control), cudaMemcpyDeviceToHost, ctx->stream));
-	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	if (control[1] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(control[1]));
-	const uint32_t recordCount = control[0];
-	TileBins bins;
-	bins.tilesX = (r->width + TILE_W - 1) / TILE_W;
-	bins.tilesY = (r->height + TILE_H - 1) / TILE_H;
-	size_t tiles = (size_t)bins.tilesX * bins.tilesY;
-	CUDA_TRY(ctx, ctx->binCounts.reserve(tiles));
-	CUDA_TRY(ctx, ctx->binOffsets.reserve(tiles + 1));
-	CUDA_TRY(ctx, ctx->binCursors.reserve(tiles));
-	CUDA_TRY(ctx, ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(tiles > recordCount ? tiles : recordCount) + 2)));
-	CUDA_TRY(ctx, ctx->rowCounts.reserve((size_t)recordCount + 2));
-	CUDA_TRY(ctx, ctx->rowOffsets.reserve((size_t)recordCount + 2));
-	CUDA_TRY(ctx, ctx->textureTable.reserve(r->textures.size() + 1));
-	if (!r->textures.empty())
-		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->textureTable.ptr, r->textures.data(), r->textures.size() * sizeof(TextureData),
-		                              cudaMemcpyHostToDevice, ctx->stream));
-	CUDA_TRY(ctx, ctx->taskTable.reserve(r->tasks.size() + 1));
-	if (!r->tasks.empty())
-		CUDA_TRY(ctx, cudaMemcpyAsync(ctx->taskTable.ptr, r->tasks.data(), r->tasks.size() * sizeof(TaskData),
-		                              cudaMemcpyHostToDevice, ctx->stream));
-	bins.counts = ctx->binCounts.ptr;
-	bins.offsets = ctx->binOffsets.ptr;
-	bins.cursors = ctx->binCursors.ptr;
-	bins.lists = ctx->binLists.ptr;
-	bins.listCapacity = ctx->binLists.capacity;
-	FrameBuffers fb;
-	memset(&fb, 0, sizeof(fb));
-	fb.records = ctx->records.ptr;
-	fb.rowOffsets = ctx->rowOffsets.ptr;
-	fb.recordCount = ctx->control.ptr;
-	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
-	fb.scanScratch = ctx->scanScratch.ptr;
-	fb.scanScratchElems = ctx->scanScratch.capacity;
-	const int32_t smallRows = r->depthOnly ? 0 : ctx->smallRows, smallWidth = ctx->smallWidth;
-	launch_row_offsets(fb, recordCount, ctx->rowCounts.ptr, ctx->stream);
-	launch_bin_count(fb, recordCount, bins, 0, 0, ctx->stream);
-	CUDA_TRY(ctx, cudaGetLastError());
-	uint32_t totals[2] = {0, 0};
-	CUDA_TRY(ctx, cudaMemcpyAsync(&totals[0], bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-	CUDA_TRY(ctx, cudaMemcpyAsync(&totals[1], ctx->rowOffsets.ptr + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	const uint32_t entries = totals[0];
-	CUDA_TRY(ctx, ctx->binLists.reserve((size_t)entries + 1));
-	CUDA_TRY(ctx, ctx->rows.reserve((size_t)totals[1] + 2));
-	fb.rows = ctx->rows.ptr;
-	bins.lists = ctx->binLists.ptr;
-	bins.listCapacity = ctx->binLists.capacity;
-	launch_rows(fb, recordCount, ctx->stream);
-	launch_bin_fill(fb, recordCount, bins, 0, 0, ctx->stream);
-	TargetParams tg;
-	memset(&tg, 0, sizeof(tg));
-	tg.color = r->hasColor ? r->deviceColor : nullptr;
-	tg.colorStride = r->colorStride;
-	tg.packOrder = r->hasColor ? r->color.packOrder : 0;
-	tg.depth = r->hasDepth ? r->deviceDepth : nullptr;
-	tg.depthStride = r->depthStride;
-	tg.width = r->width;
-	tg.height = r->height;
-	tg.affine = r->affine ? 1 : 0;
-	tg.smallRows = smallRows;
-	tg.smallWidth = smallWidth;
-	const size_t pixels = (size_t)r->width * r->height;
-	CUDA_TRY(ctx, ctx->keys.reserve(pixels));
-	CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
-	tg.keys = ctx->keys.ptr;
-	tg.rowOffsets = ctx->rowOffsets.ptr;
-	tg.rows = ctx->rows.ptr;
-	if (ctx->counting) {
-		CUDA_TRY(ctx, cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), ctx->stream));
-		tg.fragments = ctx->fragmentCounter.ptr;
-		tg.coverage = ctx->coverage;
-		if (tg.coverage) CUDA_TRY(ctx, cudaMemsetAsync(tg.coverage, 0, pixels * sizeof(uint32_t), ctx->stream));
+	BatchJob &job = ctx->frameJob;
+	job.tasks.swap(r->tasks);
+	job.textures.swap(r->textures);
+	job.frames.resize(1);
+	FrameTarget &f = job.frames[0];
+	memset(&f, 0, sizeof(f));
+	f.color = r->hasColor ? r->deviceColor : nullptr;
+	f.colorStride = r->colorStride;
+	f.packOrder = r->hasColor ? r->color.packOrder : 0;
+	f.depth = r->hasDepth ? r->deviceDepth : nullptr;
+	f.depthStride = r->depthStride;
+	f.width = r->width;
+	f.height = r->height;
+	f.affine = r->affine ? 1 : 0;
+	f.coverage = ctx->counting ? ctx->coverage : nullptr;
+	job.depthOnly = r->depthOnly;
+	job.resolve = true;
+	BatchTotals totals;
+	int status = batch_enqueue(ctx, job, totals);
+	job.tasks.swap(r->tasks);
+	job.textures.swap(r->textures);
+	if (status != DSRG_OK) {
+		cudaStreamSynchronize(ctx->stream);
+		return status;
 	}
-	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStart, ctx->stream));
-	if (r->depthOnly) {
-		launch_raster_depth_only(fb, bins, tg, ctx->stream);
-	} else {
-		launch_raster(fb, ctx->taskTable.ptr, ctx->textureTable.ptr, bins, tg, ctx->stream);
-	}
-	CUDA_TRY(ctx, cudaGetLastError());
-	CUDA_TRY(ctx, cudaEventRecord(ctx->eventRasterStop, ctx->stream));
-	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStop, ctx->stream));
 	if (r->hasColor && !r->color.onDevice)
 		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->color.data, r->color.strideBytes, r->deviceColor, (size_t)r->width * 4,
 		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
 	if (r->hasDepth && !r->depth.onDevice)
 		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->depth.data, r->depth.strideBytes, r->deviceDepth, (size_t)r->width * 4,
 		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
-	unsigned long long fragments = 0;
-	if (ctx->counting)
-		CUDA_TRY(ctx, cudaMemcpyAsync(&fragments, ctx->fragmentCounter.ptr, sizeof(fragments), cudaMemcpyDeviceToHost, ctx->stream));
-	uint32_t errorBits = 0;
-	CUDA_TRY(ctx, cudaMemcpyAsync(&errorBits, ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-	CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "rasterisation reported device error bits " + std::to_string(errorBits));
-	float ms = 0.0f, rasterMs = 0.0f;
-	cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
-	cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);
-	ctx->stats.fragments = fragments;
-	ctx->stats.drawRecords = recordCount;
-	ctx->stats.binEntries = entries;
-	ctx->stats.milliseconds = ms;
-	ctx->stats.rasterMilliseconds = rasterMs;
-	ctx->stats.kernelLaunches = launch_count();
-	return DSRG_OK;
+	return batch_finish(ctx, totals);
 }
 
 int dsrg_renderer_end(dsrg_renderer r) {

@@ -1,0 +1,285 @@
+// Batched rendering (dsrg_batch_*) and the tile kernel's autotuner.
+//
+// A batch is a list of frames, each what one renderer_begin ... renderer_end would draw
+// (api/rendererAPI.cpp:151-168, 351-358), rendered by one pass of the kernels over all frames.
+// The reference has no batched form; its renderer draws one target at a time.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "dsrg_internal.h"
+
+using namespace dsrg;
+
+struct dsrg_batch_s {
+	dsrg_context context;
+	struct Frame {
+		dsrg_image color, depth;
+		bool hasColor = false, hasDepth = false;
+		int32_t width = 0, height = 0;
+		uint32_t triangles = 0; // fan triangles given so far (the next task's orderBase)
+		int32_t affine = -1;    // -1 no camera yet, 0 perspective, 1 orthogonal
+	};
+	std::vector<Frame> frames;
+	std::vector<TaskParams> tasks;
+	std::vector<TextureData> textures;
+	std::unordered_map<dsrg_texture, int32_t> textureSlots;
+	DeviceBuffer<uint32_t> stagingColor; // frames whose images are in host memory
+	DeviceBuffer<float> stagingDepth;
+	BatchJob job;
+};
+
+static bool image_ok(const dsrg_image *img) {
+	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 && img->strideBytes % 4 == 0;
+}
+
+extern "C" {
+
+int dsrg_batch_create(dsrg_context ctx, dsrg_batch *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_batch b = new (std::nothrow) dsrg_batch_s();
+	if (!b) return DSRG_ERROR_OUT_OF_MEMORY;
+	b->context = ctx;
+	*out = b;
+	return DSRG_OK;
+}
+
+int dsrg_batch_destroy(dsrg_batch b) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(b->context->device);
+	cudaStreamSynchronize(b->context->stream);
+	b->stagingColor.release();
+	b->stagingDepth.release();
+	delete b;
+	return DSRG_OK;
+}
+
+int dsrg_batch_clear(dsrg_batch b) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	b->frames.clear();
+	b->tasks.clear();
+	b->textures.clear();
+	b->textureSlots.clear();
+	return DSRG_OK;
+}
+
+int dsrg_batch_add_frame(dsrg_batch b, const dsrg_image *color, const dsrg_image *depth, int32_t *frameIndex) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_context ctx = b->context;
+	if (!color && !depth) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_add_frame: a frame needs a colour or a depth image");
+	if (color && !image_ok(color)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_add_frame: invalid colour image");
+	if (depth && !image_ok(depth)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_add_frame: invalid depth image");
+	if (color && (color->packOrder < 0 || color->packOrder > 3)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_add_frame: unknown pack order");
+	if (color && depth && (color->width != depth->width || color->height != depth->height))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_add_frame: colour and depth images must have the same dimensions");
+	const int32_t w = color ? color->width : depth->width, h = color ? color->height : depth->height;
+	if (w > 32767 || h > 32767) return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_batch_add_frame: targets are limited to 32767 x 32767 pixels");
+	dsrg_batch_s::Frame f;
+	f.hasColor = color != nullptr;
+	f.hasDepth = depth != nullptr;
+	if (color) f.color = *color;
+	if (depth) f.depth = *depth;
+	f.width = w;
+	f.height = h;
+	b->frames.push_back(f);
+	if (frameIndex) *frameIndex = (int32_t)b->frames.size() - 1;
+	return DSRG_OK;
+}
+
+int dsrg_batch_give_task(dsrg_batch b, int32_t frameIndex, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_context ctx = b->context;
+	if (frameIndex < 0 || frameIndex >= (int32_t)b->frames.size())
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_give_task: no such frame");
+	if (!m || !modelToWorld || !camera) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_give_task: null argument");
+	if (camera->width <= 0 || camera->height <= 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_give_task: camera without image size");
+	dsrg_batch_s::Frame &f = b->frames[frameIndex];
+	if (m->filter == DSRG_FILTER_ALPHA && f.hasColor)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_batch_give_task: the alpha filter is not available on the GPU path yet");
+	const int32_t affine = camera->perspective ? 0 : 1;
+	if (f.affine >= 0 && f.affine != affine)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_batch_give_task: perspective and orthogonal cameras cannot share one frame");
+	f.affine = affine;
+	CameraData cam = make_camera(*camera);
+	// ModelImpl::render skips models whose bound is outside the view (model/Model.cpp:186-197)
+	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld) || m->triangleCount == 0) return DSRG_OK;
+	TaskParams task;
+	memset(&task, 0, sizeof(task));
+	task.positions = m->positions;
+	task.polygons = m->polygons;
+	task.texCoords = m->texCoords;
+	task.colors = m->colors;
+	task.triSource = m->triSource;
+	task.pointCount = m->pointCount;
+	task.triangleCount = m->triangleCount;
+	task.orderBase = f.triangles;
+	task.frame = frameIndex;
+	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
+	task.camera = cam;
+	task.filter = m->filter;
+	auto slot = [&](dsrg_texture t) -> int32_t {
+		if (!t) return -1;
+		auto it = b->textureSlots.find(t);
+		if (it != b->textureSlots.end()) return it->second;
+		const int32_t index = (int32_t)b->textures.size();
+		b->textures.push_back(t->data);
+		b->textureSlots[t] = index;
+		return index;
+	};
+	task.diffuse = slot(m->diffuse);
+	task.light = slot(m->light);
+	task.depthOnly = 0;
+	b->tasks.push_back(task);
+	f.triangles += (uint32_t)m->triangleCount;
+	return DSRG_OK;
+}
+
+int dsrg_batch_render(dsrg_batch b) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_context ctx = b->context;
+	cudaSetDevice(ctx->device);
+	cudaStream_t stream = ctx->stream;
+	// frames in host memory are drawn in staging buffers
+	size_t colorPixels = 0, depthPixels = 0;
+	for (const auto &f : b->frames) {
+		if (f.hasColor && !f.color.onDevice) colorPixels += (size_t)f.width * f.height;
+		if (f.hasDepth && !f.depth.onDevice) depthPixels += (size_t)f.width * f.height;
+	}
+	if (colorPixels) DSRG_CUDA_TRY(ctx, b->stagingColor.reserve(colorPixels));
+	if (depthPixels) DSRG_CUDA_TRY(ctx, b->stagingDepth.reserve(depthPixels));
+	DSRG_CUDA_TRY(ctx, cudaEventRecord(ctx->eventStart, stream));
+	BatchJob &job = b->job;
+	job.frames.resize(b->frames.size());
+	colorPixels = depthPixels = 0;
+	for (size_t i = 0; i < b->frames.size(); i++) {
+		const auto &f = b->frames[i];
+		FrameTarget &t = job.frames[i];
+		memset(&t, 0, sizeof(t));
+		t.width = f.width;
+		t.height = f.height;
+		t.affine = f.affine == 1 ? 1 : 0;
+		if (f.hasColor) {
+			t.packOrder = f.color.packOrder;
+			if (f.color.onDevice) {
+				t.color = (uint32_t *)f.color.data;
+				t.colorStride = f.color.strideBytes / 4;
+			} else {
+				t.color = b->stagingColor.ptr + colorPixels;
+				t.colorStride = f.width;
+				colorPixels += (size_t)f.width * f.height;
+				DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(t.color, (size_t)f.width * 4, f.color.data, f.color.strideBytes, (size_t)f.width * 4,
+				                                     f.height, cudaMemcpyHostToDevice, stream));
+			}
+		}
+		if (f.hasDepth) {
+			if (f.depth.onDevice) {
+				t.depth = (float *)f.depth.data;
+				t.depthStride = f.depth.strideBytes / 4;
+			} else {
+				t.depth = b->stagingDepth.ptr + depthPixels;
+				t.depthStride = f.width;
+				depthPixels += (size_t)f.width * f.height;
+				DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(t.depth, (size_t)f.width * 4, f.depth.data, f.depth.strideBytes, (size_t)f.width * 4,
+				                                     f.height, cudaMemcpyHostToDevice, stream));
+			}
+		}
+	}
+	job.tasks.swap(b->tasks);
+	job.textures.swap(b->textures);
+	job.depthOnly = false;
+	job.resolve = true;
+	BatchTotals totals;
+	const int status = batch_enqueue(ctx, job, totals);
+	job.tasks.swap(b->tasks);
+	job.textures.swap(b->textures);
+	if (status != DSRG_OK) {
+		cudaStreamSynchronize(stream);
+		return status;
+	}
+	for (size_t i = 0; i < b->frames.size(); i++) {
+		const auto &f = b->frames[i];
+		const FrameTarget &t = job.frames[i];
+		if (f.hasColor && !f.color.onDevice)
+			DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(f.color.data, f.color.strideBytes, t.color, (size_t)f.width * 4, (size_t)f.width * 4,
+			                                     f.height, cudaMemcpyDeviceToHost, stream));
+		if (f.hasDepth && !f.depth.onDevice)
+			DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(f.depth.data, f.depth.strideBytes, t.depth, (size_t)f.width * 4, (size_t)f.width * 4,
+			                                     f.height, cudaMemcpyDeviceToHost, stream));
+	}
+	return batch_finish(ctx, totals);
+}
+
+int dsrg_context_get_tuning(dsrg_context ctx, dsrg_tuning *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	out->threadsPerTile = ctx->threadsPerTile;
+	out->ctasPerSm = ctx->ctasPerSm;
+	out->smallRows = ctx->smallRows;
+	out->smallWidth = ctx->smallWidth;
+	out->graphs = ctx->useGraphs;
+	return DSRG_OK;
+}
+
+int dsrg_context_set_tuning(dsrg_context ctx, const dsrg_tuning *t) {
+	if (!ctx || !t) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (t->threadsPerTile != 128 && t->threadsPerTile != 256)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: threadsPerTile must be 128 or 256");
+	if (t->ctasPerSm < 1 || t->ctasPerSm > 1024 / t->threadsPerTile)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: ctasPerSm must be between 1 and 1024 / threadsPerTile");
+	if (t->smallRows < 0 || t->smallWidth < 0 || t->smallRows > 16 || t->smallWidth > 64)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: small-triangle bound out of range (rows 0..16, width 0..64)");
+	ctx->threadsPerTile = t->threadsPerTile;
+	ctx->ctasPerSm = t->ctasPerSm;
+	ctx->smallRows = t->smallRows;
+	ctx->smallWidth = t->smallWidth;
+	ctx->useGraphs = t->graphs ? 1 : 0;
+	return DSRG_OK;
+}
+
+int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_context ctx = b->context;
+	if (rounds < 1) rounds = 1;
+	dsrg_tuning start;
+	dsrg_context_get_tuning(ctx, &start);
+	struct Shape { int32_t threads, perSm; };
+	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}};
+	const int32_t smalls[][2] = {{8, 16}, {0, 0}};
+	dsrg_tuning chosen = start;
+	double bestSeconds = -1.0;
+	for (const Shape &s : shapes) {
+		for (const auto &sm : smalls) {
+			dsrg_tuning t = start;
+			t.threadsPerTile = s.threads;
+			t.ctasPerSm = s.perSm;
+			t.smallRows = sm[0];
+			t.smallWidth = sm[1];
+			int status = dsrg_context_set_tuning(ctx, &t);
+			if (status != DSRG_OK) return status;
+			status = dsrg_batch_render(b); // warm-up: scratch sizes and graphs for this shape
+			if (status != DSRG_OK) { dsrg_context_set_tuning(ctx, &start); return status; }
+			double seconds = -1.0;
+			for (int32_t r = 0; r < rounds; r++) {
+				const auto t0 = std::chrono::steady_clock::now();
+				status = dsrg_batch_render(b);
+				const auto t1 = std::chrono::steady_clock::now();
+				if (status != DSRG_OK) { dsrg_context_set_tuning(ctx, &start); return status; }
+				const double d = std::chrono::duration<double>(t1 - t0).count();
+				if (seconds < 0.0 || d < seconds) seconds = d;
+			}
+			if (bestSeconds < 0.0 || seconds < bestSeconds) {
+				bestSeconds = seconds;
+				chosen = t;
+			}
+		}
+	}
+	dsrg_context_set_tuning(ctx, &chosen);
+	if (best) *best = chosen;
+	return DSRG_OK;
+}
+
+} // extern "C"

@@ -115,11 +115,45 @@ inline bool box_seen(const CameraData &c, const float *mn, const float *mx, cons
 }
 
 
+// One batch for the kernels: frames (targets in device memory) and the tasks drawing into them.
+// The tasks of one frame must appear in submission order; their orderBase counts the fan
+// triangles given to the same frame before them.
+struct BatchJob {
+	std::vector<TaskParams> tasks;
+	std::vector<FrameTarget> frames;  // color, depth, strides, packOrder, size, affine and coverage set by the caller
+	std::vector<TextureData> textures;
+	bool depthOnly = false;
+	bool resolve = true;
+};
+
+// The launches of one phase between two host synchronisations, kept as a CUDA graph.  A phase
+// whose launch parameters (key) repeat those of the previous call is captured on the repeat and
+// replayed from then on; a phase whose parameters change every call is launched directly.
+struct PhaseGraph {
+	std::vector<unsigned char> key;
+	cudaGraphExec_t exec = nullptr;
+	uint64_t launches = 0; // kernels in the graph
+	void reset() {
+		if (exec) cudaGraphExecDestroy(exec);
+		exec = nullptr;
+		key.clear();
+		launches = 0;
+	}
+};
+
+struct BatchTotals {
+	uint32_t points = 0, triangles = 0, tiles = 0;
+	size_t pixels = 0;
+	uint32_t records = 0, rows = 0, binEntries = 0;
+};
+
 } // namespace dsrg
 
 using dsrg::DeviceBuffer;
 using dsrg::DrawRecord;
-using dsrg::TaskData;
+using dsrg::TaskParams;
+using dsrg::FrameTarget;
+using dsrg::BatchParams;
 using dsrg::TextureData;
 using dsrg::CameraData;
 
@@ -132,8 +166,10 @@ struct dsrg_context_s {
 	DeviceBuffer<int64_t> flatx, flaty;
 	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
 	DeviceBuffer<DrawRecord> records;
-	DeviceBuffer<TaskData> taskTable;
-	DeviceBuffer<uint32_t> control;      // [0] record count, [1] error flag
+	DeviceBuffer<unsigned char> tables;  // the batch's task, frame and texture tables
+	unsigned char *pinnedTables = nullptr; // host staging of the tables (page-locked)
+	size_t pinnedCapacity = 0;
+	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
 	DeviceBuffer<TextureData> textureTable;
 	DeviceBuffer<uint32_t> stagingColor;
@@ -142,11 +178,16 @@ struct dsrg_context_s {
 	DeviceBuffer<unsigned long long> keys;
 	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;
 	int32_t smallRows = 8, smallWidth = 16; // one lane walks records whose raster bound is at most 8 x 16 pixels
+	int32_t ctasPerSm = 4;                  // resident CTAs per SM of the persistent tile kernel
+	int32_t threadsPerTile = 256;           // threads of one tile's CTA
+	int32_t useGraphs = 1;                  // replay unchanged phases as CUDA graphs
+	dsrg::PhaseGraph graphs[4];             // phases A, B, C (lists) and D (raster)
 	int32_t counting = 0;
 	uint32_t *coverage = nullptr;
 	dsrg_stats stats;
 	cudaEvent_t eventStart = nullptr, eventStop = nullptr, eventRasterStart = nullptr, eventRasterStop = nullptr;
 	dsrg_renderer implicitRenderer = nullptr;
+	dsrg::BatchJob frameJob;                // reused by renderer_end
 };
 
 struct dsrg_texture_s {
@@ -180,13 +221,12 @@ struct dsrg_renderer_s {
 	float *deviceDepth = nullptr;
 	int32_t colorStride = 0, depthStride = 0;
 	uint32_t triangleCount = 0;   // fan triangles submitted this frame
-	uint32_t recordCapacity = 0;
 	bool depthOnly = false;
 	bool affine = false;
 	bool cameraKnown = false;
 	std::vector<TextureData> textures;
 	std::vector<dsrg_texture> textureHandles;
-	std::vector<TaskData> tasks;
+	std::vector<TaskParams> tasks;
 };
 
 #define DSRG_CUDA_TRY(ctx, expr)                                                                      \
@@ -202,6 +242,27 @@ inline int fail(dsrg_context ctx, int code, const std::string &message) {
 	if (ctx) ctx->lastError = message;
 	return code;
 }
+
+namespace dsrg {
+
+
+// Fills the tasks' point and triangle bases and the frames' tile ranges and key images
+// (keysBase + the frame's first pixel), and lays the tables out for a device copy at deviceBase:
+// writes them to `host` when it is not null and points `params` at their device addresses.
+// Returns the bytes the tables take.
+size_t layout_tables(BatchJob &job, unsigned long long *keysBase, unsigned char *host, unsigned char *deviceBase,
+                     BatchParams &params, BatchTotals &totals);
+size_t layout_tables(TaskParams *tasks, size_t taskCount, FrameTarget *frames, size_t frameCount, const TextureData *textures,
+                     size_t textureCount, bool depthOnly, unsigned long long *keysBase, unsigned char *host,
+                     unsigned char *deviceBase, BatchParams &params, BatchTotals &totals);
+
+// Runs phases A to C of the batch on the context's stream (growing its scratch as needed) and
+// returns with the raster queued; the caller queues its copies and then calls batch_finish.
+int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals);
+// Waits for the stream, checks the device error bits and fills the context's statistics.
+int batch_finish(dsrg_context ctx, const BatchTotals &totals);
+
+} // namespace dsrg
 
 
 #endif

@@ -1,13 +1,17 @@
 // CUDA kernels of the DFPSR triangle path for sm_103a.
 //
-// Pipeline per frame:
-//   project_kernel       Camera::worldToScreen for every model point (implementation/render/Camera.h:157-190)
-//   setup_kernel<false>  per fan triangle: cull, clip, front-face; counts its draw records
-//   scan                 record offsets, so that records land in submission order
-//   setup_kernel<true>   writes the DrawRecords (bound, sub-pixel corners, projection)
-//   bin kernels          per 16x16 tile lists of the records whose raster bound touches it
-//   raster_kernel        one CTA per tile: every fragment competes for 64-bit depth keys in shared
-//                        memory, then every pixel shades its winning fragment
+// Every launch covers a whole batch of frames (see dsrg_kernels.h).  Per batch:
+//   A  project_kernel       Camera::worldToScreen for every model point (implementation/render/Camera.h:157-190)
+//      setup_kernel<false>  per fan triangle: cull, clip, front-face; counts its draw records
+//      scan                 record offsets, so that records land in submission order
+//      setup_kernel<true>   writes the DrawRecords (bound, sub-pixel corners, projection)
+//   B  row_count_kernel     + scan: where each record's row intervals go
+//      bin_kernel<false>    + scan: (tile, record) pair counts per tile
+//   C  rows_kernel          row intervals of every record (rasterizeTriangle)
+//      bin_kernel<true>     per-tile record lists
+//      raster_kernel        persistent CTAs pull tiles from a queue; every fragment competes for
+//                           64-bit depth keys in shared memory; the winners go to the key image
+//      resolve_kernel       every pixel re-evaluates and shades its winning fragment
 //
 // Why the depth test can run out of order: the reference writes a fragment when its depth is
 // strictly greater (1/W, perspective) or smaller (linear, orthogonal) than the stored one
@@ -15,7 +19,7 @@
 // triangles the stored value is the extreme depth over all fragments that beat the initial
 // value, and the colour is the earliest fragment reaching it.  Packing (depth, ~record index)
 // into one 64-bit key and taking the maximum reproduces exactly that, in any order, because
-// records are stored in submission order.
+// the records of a frame are stored in submission order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -28,24 +32,56 @@ namespace dsrg {
 
 static uint64_t g_launches = 0;
 uint64_t launch_count() { return g_launches; }
+void add_launches(uint64_t n) { g_launches += n; }
 #define COUNT_LAUNCH() (g_launches++)
+
+int32_t sm_count() {
+	static int32_t count = 0;
+	if (count == 0) {
+		int device = 0, value = 0;
+		cudaGetDevice(&device);
+		cudaDeviceGetAttribute(&value, cudaDevAttrMultiProcessorCount, device);
+		count = value > 0 ? value : 1;
+	}
+	return count;
+}
+
+// Grid of a grid-stride kernel over n items: enough CTAs to fill the GPU, never more than needed.
+static int grid_for(uint64_t n, int threads) {
+	uint64_t blocks = (n + threads - 1) / threads;
+	const uint64_t cap = (uint64_t)sm_count() * 16;
+	if (blocks > cap) blocks = cap;
+	return (int)(blocks > 0 ? blocks : 1);
+}
+
+// Largest k in [0, count) with base[k] <= i (base[0] = 0, ascending).
+__device__ __forceinline__ int32_t find_segment(const uint32_t *base, int32_t count, uint32_t i) {
+	int32_t lo = 0, hi = count - 1;
+	while (lo < hi) {
+		const int32_t mid = (lo + hi + 1) >> 1;
+		if (__ldg(&base[mid]) <= i) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
 
 // ------------------------------------------------------------------ projection
 
-__global__ void project_kernel(TaskParams task, ProjectedPoints out) {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= task.pointCount) return;
-	Vec3 p = vec3(task.positions[i * 3], task.positions[i * 3 + 1], task.positions[i * 3 + 2]);
-	Projected pr = camera_to_screen(task.camera, world_to_camera(task.camera, transform_point(task.modelToWorld, p)));
-	out.csx[i] = pr.cs.x; out.csy[i] = pr.cs.y; out.csz[i] = pr.cs.z;
-	out.isx[i] = pr.isx; out.isy[i] = pr.isy;
-	out.flatx[i] = pr.flatx; out.flaty[i] = pr.flaty;
+__global__ void project_kernel(BatchParams b, ProjectedPoints out) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < b.totalPoints; i += gridDim.x * blockDim.x) {
+		const TaskParams &task = b.tasks[find_segment(b.taskPointBase, b.taskCount, i)];
+		const uint32_t local = i - task.pointBase;
+		Vec3 p = vec3(task.positions[local * 3], task.positions[local * 3 + 1], task.positions[local * 3 + 2]);
+		Projected pr = camera_to_screen(task.camera, world_to_camera(task.camera, transform_point(task.modelToWorld, p)));
+		out.csx[i] = pr.cs.x; out.csy[i] = pr.cs.y; out.csz[i] = pr.cs.z;
+		out.isx[i] = pr.isx; out.isy[i] = pr.isy;
+		out.flatx[i] = pr.flatx; out.flaty[i] = pr.flaty;
+	}
 }
 
-void launch_project(const TaskParams &task, const FrameBuffers &fb, cudaStream_t stream) {
-	if (task.pointCount <= 0) return;
+void launch_project(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
+	if (b.totalPoints == 0) return;
 	COUNT_LAUNCH();
-	project_kernel<<<(task.pointCount + 255) / 256, 256, 0, stream>>>(task, fb.points);
+	project_kernel<<<grid_for(b.totalPoints, 256), 256, 0, stream>>>(b, fb.points);
 }
 
 // ------------------------------------------------------------------ triangle setup
@@ -59,15 +95,15 @@ struct Corner {
 // Emits one draw command (renderCore.cpp:203-217 executeTriangleDrawing against the whole target):
 // the triangle bound cut to the target with rows aligned to pairs (ITriangle2D.cpp:70-75).
 template <bool WRITE>
-__device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, const Corner *c,
-                            const float *subB, const float *subC, uint32_t order, uint32_t tri, uint32_t base,
-                            uint32_t &emitted) {
+__device__ void emit_record(const TaskParams &task, uint32_t taskIndex, int32_t width, int32_t height, const FrameBuffers &fb,
+                            uint32_t recordCapacity, const Corner *c, const float *subB, const float *subC, uint32_t order,
+                            uint32_t tri, uint32_t base, uint32_t &emitted) {
 	int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
-	int32_t b[4];
-	triangle_bound(fx, fy, b);
-	if (!(b[0] < task.width && b[2] > 0 && b[1] < task.height && b[3] > 0)) return;
+	int32_t bd[4];
+	triangle_bound(fx, fy, bd);
+	if (!(bd[0] < width && bd[2] > 0 && bd[1] < height && bd[3] > 0)) return;
 	if (WRITE) {
-		uint32_t index = base + emitted;
+		const uint32_t index = base + emitted;
 		if (index >= recordCapacity) {
 			atomicOr(fb.errorFlag, ERROR_RECORD_OVERFLOW);
 		} else {
@@ -79,17 +115,17 @@ __device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint
 				r.flat[i * 2 + 1] = (int32_t)fy[i];
 			}
 			if (!inRange) atomicOr(fb.errorFlag, ERROR_COORDINATE_RANGE);
-			r.left = b[0] > 0 ? b[0] : 0;
-			r.top = (b[1] > 0 ? b[1] : 0) & ~1;                                       // roundDown(top, 2)
-			r.right = b[2] < task.width ? b[2] : task.width;
-			r.bottom = ((b[3] < task.height ? b[3] : task.height) + 1) & ~1;          // roundUp(bottom, 2)
+			r.left = bd[0] > 0 ? bd[0] : 0;
+			r.top = (bd[1] > 0 ? bd[1] : 0) & ~1;                           // roundDown(top, 2)
+			r.right = bd[2] < width ? bd[2] : width;
+			r.bottom = ((bd[3] < height ? bd[3] : height) + 1) & ~1;        // roundUp(bottom, 2)
 			float isx[3] = {c[0].isx, c[1].isx, c[2].isx}, isy[3] = {c[0].isy, c[1].isy, c[2].isy};
 			float csz[3] = {c[0].cs.z, c[1].cs.z, c[2].cs.z};
 			triangle_projection(isx, isy, csz, subB, subC, task.camera.perspective != 0, r.start, r.dx, r.dy);
 			r.order = order;
 			r.tri = tri;
-			r.task = task.taskIndex;
-			r.flags = task.camera.perspective ? 0u : RECORD_AFFINE;
+			r.task = taskIndex;
+			r.frame = (uint32_t)task.frame;
 			fb.records[index] = r;
 		}
 	}
@@ -98,87 +134,86 @@ __device__ void emit_record(const TaskParams &task, const FrameBuffers &fb, uint
 
 // renderTriangleFromData / renderTriangleFromDataDepth for one fan triangle (renderCore.cpp:220-341, 400-443).
 template <bool WRITE>
-__global__ void __launch_bounds__(256) setup_kernel(TaskParams task, FrameBuffers fb, uint32_t recordCapacity) {
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= task.triangleCount) return;
-	uint32_t emitted = 0;
-	const uint32_t base = WRITE ? fb.triOffsets[t] + fb.triOffsets[task.triangleCount + 1] : 0u;
-	const int32_t src = task.triSource[t];
-	const int32_t p = src >> 1, k = src & 1;
-	const int corner[3] = {0, 1 + k, 2 + k}; // fan 0-1-2, 0-2-3 (model/Model.cpp:135-162, 164-183)
-	Corner c[3];
-	for (int i = 0; i < 3; i++) {
-		int32_t pi = task.polygons[p * 4 + corner[i]];
-		c[i].cs = vec3(fb.points.csx[pi], fb.points.csy[pi], fb.points.csz[pi]);
-		c[i].isx = fb.points.isx[pi]; c[i].isy = fb.points.isy[pi];
-		c[i].fx = fb.points.flatx[pi]; c[i].fy = fb.points.flaty[pi];
-	}
-	const uint32_t order = (task.orderBase + (uint32_t)t) * 8u;
-	bool visible = triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, false) != 0;
-	if (visible && !task.depthOnly && task.filter == 1) {
-		// renderTriangleFromData skips alpha-filtered triangles whose three alphas are almost zero (renderCore.cpp:319)
-		const float *col = task.colors + p * 16;
-		if (almost_zero(col[corner[0] * 4 + 3]) && almost_zero(col[corner[1] * 4 + 3]) && almost_zero(col[corner[2] * 4 + 3]))
-			visible = false;
-	}
-	if (visible && (task.hasColor || task.hasDepth)) {
-		const float defaultB[3] = {0.0f, 1.0f, 0.0f}, defaultC[3] = {0.0f, 0.0f, 1.0f};
-		const float zero3[3] = {0.0f, 0.0f, 0.0f};
-		if (triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, true) == 1) {
-			int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
-			if (is_frontfacing(fx, fy)) {
-				emit_record<WRITE>(task, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
-				                   task.depthOnly ? zero3 : defaultC, order, (uint32_t)t, base, emitted);
-			}
-		} else {
-			ClippedPolygon poly;
-			poly.count = 3;
-			for (int i = 0; i < 3; i++) { poly.v[i].cs = c[i].cs; poly.v[i].state = 0; poly.v[i].value = 0.0f; }
-			poly.v[0].subB = 0.0f; poly.v[0].subC = 0.0f;
-			poly.v[1].subB = 1.0f; poly.v[1].subC = 0.0f;
-			poly.v[2].subB = 0.0f; poly.v[2].subC = 1.0f;
-			for (int s = 0; s < task.camera.clipCount; s++) poly.clip(task.camera.clip[s]);
-			for (int f = 0; f < poly.count - 2; f++) {
-				const SubVertex *sv[3] = {&poly.v[0], &poly.v[1 + f], &poly.v[2 + f]};
-				Corner sc[3];
-				for (int i = 0; i < 3; i++) {
-					Projected pr = camera_to_screen(task.camera, sv[i]->cs);
-					sc[i].cs = pr.cs; sc[i].isx = pr.isx; sc[i].isy = pr.isy; sc[i].fx = pr.flatx; sc[i].fy = pr.flaty;
-				}
-				int64_t fx[3] = {sc[0].fx, sc[1].fx, sc[2].fx}, fy[3] = {sc[0].fy, sc[1].fy, sc[2].fy};
+__global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers fb, uint32_t recordCapacity) {
+	for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < b.totalTriangles; g += gridDim.x * blockDim.x) {
+		const uint32_t k = (uint32_t)find_segment(b.taskTriangleBase, b.taskCount, g);
+		const TaskParams &task = b.tasks[k];
+		const FrameTarget &frame = b.frames[task.frame];
+		const int32_t width = frame.width, height = frame.height;
+		const bool hasTarget = frame.color != nullptr || frame.depth != nullptr;
+		const uint32_t t = g - task.triangleBase;
+		uint32_t emitted = 0;
+		const uint32_t base = WRITE ? fb.triOffsets[g] : 0u;
+		const int32_t src = task.triSource[t];
+		const int32_t p = src >> 1, fan = src & 1;
+		const int corner[3] = {0, 1 + fan, 2 + fan}; // fan 0-1-2, 0-2-3 (model/Model.cpp:135-162, 164-183)
+		Corner c[3];
+		for (int i = 0; i < 3; i++) {
+			const uint32_t pi = task.pointBase + (uint32_t)task.polygons[p * 4 + corner[i]];
+			c[i].cs = vec3(fb.points.csx[pi], fb.points.csy[pi], fb.points.csz[pi]);
+			c[i].isx = fb.points.isx[pi]; c[i].isy = fb.points.isy[pi];
+			c[i].fx = fb.points.flatx[pi]; c[i].fy = fb.points.flaty[pi];
+		}
+		const uint32_t order = (task.orderBase + t) * 8u;
+		bool visible = triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, false) != 0;
+		if (visible && !task.depthOnly && task.filter == 1) {
+			// renderTriangleFromData skips alpha-filtered triangles whose three alphas are almost zero (renderCore.cpp:319)
+			const float *col = task.colors + p * 16;
+			if (almost_zero(col[corner[0] * 4 + 3]) && almost_zero(col[corner[1] * 4 + 3]) && almost_zero(col[corner[2] * 4 + 3]))
+				visible = false;
+		}
+		if (visible && hasTarget) {
+			const float defaultB[3] = {0.0f, 1.0f, 0.0f}, defaultC[3] = {0.0f, 0.0f, 1.0f};
+			const float zero3[3] = {0.0f, 0.0f, 0.0f};
+			if (triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, true) == 1) {
+				int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
 				if (is_frontfacing(fx, fy)) {
-					float sb[3] = {sv[0]->subB, sv[1]->subB, sv[2]->subB};
-					float scc[3] = {sv[0]->subC, sv[1]->subC, sv[2]->subC};
-					emit_record<WRITE>(task, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
-					                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, (uint32_t)t, base, emitted);
+					emit_record<WRITE>(task, k, width, height, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
+					                   task.depthOnly ? zero3 : defaultC, order, t, base, emitted);
+				}
+			} else {
+				ClippedPolygon poly;
+				poly.count = 3;
+				for (int i = 0; i < 3; i++) { poly.v[i].cs = c[i].cs; poly.v[i].state = 0; poly.v[i].value = 0.0f; }
+				poly.v[0].subB = 0.0f; poly.v[0].subC = 0.0f;
+				poly.v[1].subB = 1.0f; poly.v[1].subC = 0.0f;
+				poly.v[2].subB = 0.0f; poly.v[2].subC = 1.0f;
+				for (int s = 0; s < task.camera.clipCount; s++) poly.clip(task.camera.clip[s]);
+				for (int f = 0; f < poly.count - 2; f++) {
+					const SubVertex *sv[3] = {&poly.v[0], &poly.v[1 + f], &poly.v[2 + f]};
+					Corner sc[3];
+					for (int i = 0; i < 3; i++) {
+						Projected pr = camera_to_screen(task.camera, sv[i]->cs);
+						sc[i].cs = pr.cs; sc[i].isx = pr.isx; sc[i].isy = pr.isy; sc[i].fx = pr.flatx; sc[i].fy = pr.flaty;
+					}
+					int64_t fx[3] = {sc[0].fx, sc[1].fx, sc[2].fx}, fy[3] = {sc[0].fy, sc[1].fy, sc[2].fy};
+					if (is_frontfacing(fx, fy)) {
+						float sb[3] = {sv[0]->subB, sv[1]->subB, sv[2]->subB};
+						float scc[3] = {sv[0]->subC, sv[1]->subC, sv[2]->subC};
+						emit_record<WRITE>(task, k, width, height, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
+						                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, t, base, emitted);
+					}
 				}
 			}
 		}
+		if (!WRITE) fb.triCounts[g] = emitted;
 	}
-	if (!WRITE) fb.triCounts[t] = emitted;
 }
 
-__global__ void advance_record_count_kernel(FrameBuffers fb, int32_t triangleCount) {
-	// triOffsets[triangleCount] holds this task's total; [triangleCount + 1] the records before it.
-	*fb.recordCount = fb.triOffsets[triangleCount + 1] + fb.triOffsets[triangleCount];
+void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
+	if (b.totalTriangles == 0) {
+		cudaMemsetAsync(fb.triOffsets, 0, sizeof(uint32_t), stream);
+		return;
+	}
+	COUNT_LAUNCH();
+	setup_kernel<false><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
+	launch_scan(fb.triCounts, fb.triOffsets, b.totalTriangles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
-__global__ void load_record_base_kernel(FrameBuffers fb, int32_t triangleCount) {
-	fb.triOffsets[triangleCount + 1] = *fb.recordCount;
-}
-
-void launch_setup(const TaskParams &task, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream) {
-	if (task.triangleCount <= 0) return;
-	int blocks = (task.triangleCount + 255) / 256;
+void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream) {
+	if (b.totalTriangles == 0) return;
 	COUNT_LAUNCH();
-	setup_kernel<false><<<blocks, 256, 0, stream>>>(task, fb, recordCapacity);
-	launch_scan(fb.triCounts, fb.triOffsets, (uint32_t)task.triangleCount, fb.scanScratch, fb.scanScratchElems, stream);
-	COUNT_LAUNCH();
-	load_record_base_kernel<<<1, 1, 0, stream>>>(fb, task.triangleCount);
-	COUNT_LAUNCH();
-	setup_kernel<true><<<blocks, 256, 0, stream>>>(task, fb, recordCapacity);
-	COUNT_LAUNCH();
-	advance_record_count_kernel<<<1, 1, 0, stream>>>(fb, task.triangleCount);
+	setup_kernel<true><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, recordCapacity);
 }
 
 // ------------------------------------------------------------------ scan
@@ -252,31 +287,86 @@ void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratc
 	scan_total_kernel<<<1, 1, 0, stream>>>(blockOffsets, blockSums, blocks, out, n);
 }
 
-// ------------------------------------------------------------------ binning
+// ------------------------------------------------------------------ row intervals
 
-__device__ __forceinline__ void record_tiles(const DrawRecord &r, const TileBins &bins, int32_t &tx0, int32_t &tx1,
-                                             int32_t &ty0, int32_t &ty1) {
-	tx0 = r.left >> 4; tx1 = (r.right - 1) >> 4;
-	ty0 = r.top >> 4; ty1 = (r.bottom - 1) >> 4;
-	if (tx1 >= bins.tilesX) tx1 = bins.tilesX - 1;
-	if (ty1 >= bins.tilesY) ty1 = bins.tilesY - 1;
+__global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, uint32_t *counts) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < recordCount; i += gridDim.x * blockDim.x)
+		counts[i] = (uint32_t)(records[i].bottom - records[i].top);
 }
 
-// Conservative test of whether any pixel of tile (tx, ty) can be inside the record's row
-// intervals: a pixel (x, y) passes edge i of cutConvexEdge when
+void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream) {
+	if (recordCount > 0) {
+		COUNT_LAUNCH();
+		row_count_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, rowCounts);
+	}
+	launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
+}
+
+// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176).  Records up to
+// 16 rows tall are cut by their own thread, taller ones by the whole warp.
+__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
+                                                   const uint32_t *__restrict__ rowOffsets, uint32_t *rows) {
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < recordCount; i0 += stride) {
+		const uint32_t i = i0 + threadIdx.x;
+		int32_t count = 0;
+		if (i < recordCount) {
+			const DrawRecord r = records[i];
+			count = r.bottom - r.top;
+			if (count <= 16) {
+				uint32_t *out = rows + rowOffsets[i];
+				for (int32_t k = 0; k < count; k++) {
+					int32_t left, right;
+					row_interval(r.flat, r.top + k, r.left, r.right, left, right);
+					out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				}
+			}
+		}
+		uint32_t tall = __ballot_sync(0xFFFFFFFFu, count > 16);
+		while (tall) {
+			const int src = __ffs(tall) - 1;
+			tall &= tall - 1;
+			const uint32_t ri = __shfl_sync(0xFFFFFFFFu, i, src);
+			const DrawRecord t = records[ri];
+			uint32_t *out = rows + rowOffsets[ri];
+			for (int32_t k = (int32_t)lane; k < t.bottom - t.top; k += 32) {
+				int32_t left, right;
+				row_interval(t.flat, t.top + k, t.left, t.right, left, right);
+				out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+			}
+		}
+	}
+}
+
+void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream) {
+	if (recordCount == 0) return;
+	COUNT_LAUNCH();
+	rows_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets, fb.rows);
+}
+
+__device__ __forceinline__ void unpack_row(uint32_t packed, int32_t &left, int32_t &right) {
+	left = (int32_t)(packed & 0xFFFFu);
+	right = (int32_t)(packed >> 16);
+}
+
+// ------------------------------------------------------------------ binning
+
+// Conservative test of whether any pixel of the tile whose top-left pixel is (px0, py0) can be
+// inside the record's row intervals: a pixel (x, y) passes edge i of cutConvexEdge when
 //   (128 + 256x - sx)*nx + (128 + 256y - sy)*ny <= threshold      (ITriangle2D.cpp:96-146)
 // and that linear function is largest at a corner of any rectangle, so a tile is out when one
 // edge rejects all four corners of the tile grown by two pixels (the growth covers the rows
 // where the reference's truncating division admits a pixel just outside an edge).
-__device__ __forceinline__ bool tile_may_overlap(const DrawRecord &r, int32_t tx, int32_t ty) {
-	const int64_t X0 = 128 + 256 * (int64_t)(tx * TILE_W - 2), X1 = 128 + 256 * (int64_t)(tx * TILE_W + TILE_W + 1);
-	const int64_t Y0 = 128 + 256 * (int64_t)(ty * TILE_H - 2), Y1 = 128 + 256 * (int64_t)(ty * TILE_H + TILE_H + 1);
+__device__ __forceinline__ bool tile_may_overlap(const DrawRecord &r, int32_t px0, int32_t py0) {
+	const int64_t X0 = 128 + 256 * (int64_t)(px0 - 2), X1 = 128 + 256 * (int64_t)(px0 + TILE_W + 1);
+	const int64_t Y0 = 128 + 256 * (int64_t)(py0 - 2), Y1 = 128 + 256 * (int64_t)(py0 + TILE_H + 1);
 	for (int i = 0; i < 3; i++) {
 		const int j = (i + 1) % 3;
 		const Edge e = make_edge(r.flat[i * 2], r.flat[i * 2 + 1], r.flat[j * 2], r.flat[j * 2 + 1]);
-		const int64_t a = (X0 - e.sx) * e.nx, b = (X1 - e.sx) * e.nx;
+		const int64_t a = (X0 - e.sx) * e.nx, bb = (X1 - e.sx) * e.nx;
 		const int64_t c = (Y0 - e.sy) * e.ny, d = (Y1 - e.sy) * e.ny;
-		const int64_t lowest = (a < b ? a : b) + (c < d ? c : d);
+		const int64_t lowest = (a < bb ? a : bb) + (c < d ? c : d);
 		if (lowest > e.threshold) return false;
 	}
 	return true;
@@ -300,138 +390,87 @@ __device__ __forceinline__ bool tile_test_is_exact(const DrawRecord &r) {
 	return true;
 }
 
-// Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs of the large records.
-// Records touching at most 4 tiles are walked by their own thread, with the atomics of threads
-// that hit the same tile merged into one; larger ones are walked by the whole warp.
+// Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs.  Records touching at
+// most 4 tiles are walked by their own thread, with the atomics of threads that hit the same tile
+// merged into one; larger ones are walked by the whole warp, tested tile by tile.  A tile's list
+// keeps submission order only per warp, which the order-free depth keys do not need.
 template <bool FILL>
-__global__ void bin_kernel(const DrawRecord *records, uint32_t recordCount, TileBins bins, int32_t *errorFlag,
-                           int32_t smallRows, int32_t smallWidth) {
+__global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records, uint32_t recordCount, TileBins bins,
+                           int32_t *errorFlag) {
 	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-	int32_t tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1;
-	if (r < recordCount) {
-		const DrawRecord rec = records[r];
-		if (!record_is_small(rec, smallRows, smallWidth)) record_tiles(rec, bins, tx0, tx1, ty0, ty1);
-	}
-	const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
-	const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
-	const bool big = tiles > 4;
-	for (int32_t i = 0; i < 4; i++) {
-		bool active = !big && i < tiles;
-		uint32_t tile = active ? (uint32_t)((ty0 + i / w) * bins.tilesX + tx0 + i % w) : 0xFFFFFFFFu;
-		uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
-		if (active) {
-			uint32_t leader = __ffs(peers) - 1;
-			uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-			uint32_t baseSlot = 0;
-			if (lane == leader) baseSlot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], (uint32_t)__popc(peers));
-			baseSlot = __shfl_sync(peers, baseSlot, leader);
-			if (FILL) {
-				uint32_t slot = bins.offsets[tile] + baseSlot + rank;
-				if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t r0 = blockIdx.x * blockDim.x; r0 < recordCount; r0 += stride) {
+		const uint32_t r = r0 + threadIdx.x;
+		int32_t tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, tilesX = 0;
+		uint32_t tileBase = 0;
+		if (r < recordCount) {
+			const DrawRecord rec = records[r];
+			const FrameTarget &f = b.frames[rec.frame];
+			tilesX = f.tilesX;
+			tileBase = f.tileBase;
+			tx0 = rec.left >> 4; tx1 = (rec.right - 1) >> 4;
+			ty0 = rec.top >> 4; ty1 = (rec.bottom - 1) >> 4;
+			if (tx1 >= f.tilesX) tx1 = f.tilesX - 1;
+			if (ty1 >= f.tilesY) ty1 = f.tilesY - 1;
+		}
+		const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
+		const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
+		const bool big = tiles > 4;
+		for (int32_t i = 0; i < 4; i++) {
+			const bool active = !big && i < tiles;
+			const uint32_t tile = active ? tileBase + (uint32_t)((ty0 + i / w) * tilesX + tx0 + i % w) : 0xFFFFFFFFu;
+			const uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
+			if (active) {
+				const uint32_t leader = __ffs(peers) - 1;
+				const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+				uint32_t baseSlot = 0;
+				if (lane == leader) baseSlot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], (uint32_t)__popc(peers));
+				baseSlot = __shfl_sync(peers, baseSlot, leader);
+				if (FILL) {
+					const uint32_t slot = bins.offsets[tile] + baseSlot + rank;
+					if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+				}
+			}
+		}
+		uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
+		while (bigMask) {
+			const uint32_t src = __ffs(bigMask) - 1;
+			bigMask &= bigMask - 1;
+			const int32_t bx0 = __shfl_sync(0xFFFFFFFFu, tx0, src), by0 = __shfl_sync(0xFFFFFFFFu, ty0, src);
+			const int32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bt = __shfl_sync(0xFFFFFFFFu, tiles, src);
+			const int32_t btx = __shfl_sync(0xFFFFFFFFu, tilesX, src);
+			const uint32_t bbase = __shfl_sync(0xFFFFFFFFu, tileBase, src);
+			const uint32_t br = __shfl_sync(0xFFFFFFFFu, r, src);
+			const DrawRecord rec = records[br];
+			const bool exact = tile_test_is_exact(rec);
+			for (int32_t i = (int32_t)lane; i < bt; i += 32) {
+				const int32_t tx = bx0 + i % bw, ty = by0 + i / bw;
+				if (exact && !tile_may_overlap(rec, tx * TILE_W, ty * TILE_H)) continue;
+				const uint32_t tile = bbase + (uint32_t)(ty * btx + tx);
+				uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
+				if (FILL) {
+					slot += bins.offsets[tile];
+					if (slot < bins.listCapacity) bins.lists[slot] = br; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+				}
 			}
 		}
 	}
-	uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
-	while (bigMask) {
-		uint32_t src = __ffs(bigMask) - 1;
-		bigMask &= bigMask - 1;
-		int32_t bx0 = __shfl_sync(0xFFFFFFFFu, tx0, src), by0 = __shfl_sync(0xFFFFFFFFu, ty0, src);
-		int32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bt = __shfl_sync(0xFFFFFFFFu, tiles, src);
-		uint32_t br = __shfl_sync(0xFFFFFFFFu, r, src);
-		const DrawRecord rec = records[br];
-		const bool exact = tile_test_is_exact(rec);
-		for (int32_t i = (int32_t)lane; i < bt; i += 32) {
-			const int32_t tx = bx0 + i % bw, ty = by0 + i / bw;
-			if (exact && !tile_may_overlap(rec, tx, ty)) continue;
-			uint32_t tile = (uint32_t)(ty * bins.tilesX + tx);
-			uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
-			if (FILL) {
-				slot += bins.offsets[tile];
-				if (slot < bins.listCapacity) bins.lists[slot] = br; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
-			}
-		}
-	}
 }
 
-void launch_bin_count(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
-                      cudaStream_t stream) {
-	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
-	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * tiles, stream);
+void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		bin_kernel<false><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth);
+		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
 	}
-	launch_scan(bins.counts, bins.offsets, tiles, fb.scanScratch, fb.scanScratchElems, stream);
+	launch_scan(bins.counts, bins.offsets, b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
-// ------------------------------------------------------------------ row intervals
-
-__global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, uint32_t *counts) {
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < recordCount) counts[i] = (uint32_t)(records[i].bottom - records[i].top);
-}
-
-void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream) {
+void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
+	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		row_count_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, rowCounts);
-	}
-	launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
-}
-
-// Rows of records up to 16 rows tall are cut by their own thread, taller ones by the whole warp.
-__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
-                                                   const uint32_t *__restrict__ rowOffsets, uint32_t *rows) {
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	int32_t count = 0;
-	DrawRecord r;
-	if (i < recordCount) {
-		r = records[i];
-		count = r.bottom - r.top;
-		if (count <= 16) {
-			uint32_t *out = rows + rowOffsets[i];
-			for (int32_t k = 0; k < count; k++) {
-				int32_t left, right;
-				row_interval(r.flat, r.top + k, r.left, r.right, left, right);
-				out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
-			}
-		}
-	}
-	uint32_t tall = __ballot_sync(0xFFFFFFFFu, count > 16);
-	while (tall) {
-		const int src = __ffs(tall) - 1;
-		tall &= tall - 1;
-		const uint32_t ri = __shfl_sync(0xFFFFFFFFu, i, src);
-		const DrawRecord t = records[ri];
-		uint32_t *out = rows + rowOffsets[ri];
-		for (int32_t k = (int32_t)lane; k < t.bottom - t.top; k += 32) {
-			int32_t left, right;
-			row_interval(t.flat, t.top + k, t.left, t.right, left, right);
-			out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
-		}
-	}
-}
-
-void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream) {
-	if (recordCount == 0) return;
-	COUNT_LAUNCH();
-	rows_kernel<<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets, fb.rows);
-}
-
-__device__ __forceinline__ void unpack_row(uint32_t packed, int32_t &left, int32_t &right) {
-	left = (int32_t)(packed & 0xFFFFu);
-	right = (int32_t)(packed >> 16);
-}
-
-void launch_bin_fill(const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, int32_t smallRows, int32_t smallWidth,
-                     cudaStream_t stream) {
-	uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
-	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * tiles, stream);
-	if (recordCount > 0) {
-		COUNT_LAUNCH();
-		bin_kernel<true><<<(recordCount + 255) / 256, 256, 0, stream>>>(fb.records, recordCount, bins, fb.errorFlag, smallRows, smallWidth);
+		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
 	}
 }
 
@@ -458,10 +497,11 @@ __device__ __forceinline__ RowPair make_row_pair(int32_t uL, int32_t uR, int32_t
 	return rp;
 }
 
-// Row pair of a record for the rows y1, y1 + 1 from its row intervals (recordRows = its first row).
+// Row pair of a record for the rows y1, y1 + 1 from its row intervals (recordRows = its first row;
+// row offsets are even because raster bounds are row-pair aligned, so two rows load as one uint2).
 __device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, const uint32_t *recordRows, int32_t y1, int32_t height) {
 	int32_t uL, uR, lL, lR;
-	const uint2 two = *reinterpret_cast<const uint2 *>(recordRows + (y1 - r.top)) ;
+	const uint2 two = *reinterpret_cast<const uint2 *>(recordRows + (y1 - r.top));
 	unpack_row(two.x, uL, uR);
 	unpack_row(two.y, lL, lR);
 	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
@@ -498,10 +538,6 @@ __device__ __forceinline__ void quad_lanes(float start, float dx, float dy, cons
 	}
 }
 
-__device__ __forceinline__ bool quad_is_edge(const RowPair &rp, int32_t x) {
-	return (rp.ibe <= rp.ibs) || x < rp.ibs || x >= rp.ibe;
-}
-
 // Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106); full quads draw all four.
 __device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, bool edge, int l) {
 	if (!edge) return true;
@@ -510,9 +546,9 @@ __device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, bool 
 }
 
 __device__ __forceinline__ uint32_t ordered_depth(float z) {
-	uint32_t b = fbits(z);
-	if (b == 0x80000000u) b = 0u; // -0 and +0 compare equal
-	return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+	uint32_t bits = fbits(z);
+	if (bits == 0x80000000u) bits = 0u; // -0 and +0 compare equal
+	return (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
 }
 
 __device__ __forceinline__ unsigned long long make_key(float z, uint32_t record, bool depthTest, bool affine) {
@@ -527,7 +563,7 @@ __device__ __forceinline__ uint32_t key_record(unsigned long long key, bool dept
 }
 
 // RgbaMultiply_data and its variant (shader/RgbaMultiply.h:37-58, 110-173) for fan triangle `tri`.
-__device__ __forceinline__ void make_shade(const TaskData &task, uint32_t tri, ShadeRecord &s) {
+__device__ __forceinline__ void make_shade(const TaskParams &task, uint32_t tri, ShadeRecord &s) {
 	const int32_t src = task.triSource[tri];
 	const int32_t p = src >> 1, k = src & 1;
 	const int corner[3] = {0, 1 + k, 2 + k};
@@ -570,7 +606,7 @@ __device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, f
 
 // Walks the row pairs and quads of a record exactly as fillShapeSuper does (fillerTemplates.h:246-385),
 // so every value is the reference's own running sum.  COMPONENTS = 1 for depth only, 3 for shading.
-// visit(x, y1, edge, lanes[component][lane]) is called for every quad in order.
+// visit(pair, x, y1, edge, lanes[component][lane]) is called for every quad in order.
 template <int COMPONENTS, typename Visit>
 __device__ __forceinline__ void walk_record(const DrawRecord &r, const uint32_t *recordRows, int32_t rowStart, int32_t rowEnd,
                                             int32_t height, Visit visit) {
@@ -620,14 +656,14 @@ __device__ __forceinline__ void walk_record(const DrawRecord &r, const uint32_t 
 	}
 }
 
-// ------------------------------------------------------------------ large records, one CTA per tile
+// ------------------------------------------------------------------ tiles
 
 // Depth test of one fragment against the tile's shared keys.
 __device__ __forceinline__ void tile_fragment(unsigned long long *keys, const float *initialDepth, uint32_t *coverage,
-                                              const TargetParams &tg, int pix, float z, uint32_t record, bool depthTest,
+                                              bool counting, int pix, float z, uint32_t record, bool depthTest,
                                               bool affine, uint32_t &fragments) {
 	fragments++;
-	if (tg.coverage) atomicAdd(&coverage[pix], 1u);
+	if (counting) atomicAdd(&coverage[pix], 1u);
 	const bool pass = !depthTest || (affine ? (z < initialDepth[pix]) : (z > initialDepth[pix]));
 	if (pass) {
 		const unsigned long long key = make_key(z, record, depthTest, affine);
@@ -635,216 +671,247 @@ __device__ __forceinline__ void tile_fragment(unsigned long long *keys, const fl
 	}
 }
 
-// One CTA per 16x16 tile.  Each warp takes 32 list entries at a time: a lane walks a small record
-// by itself (the reference's sequential walk, only the quads inside the tile are tested); large
-// records are rasterised by the whole warp, one lane per (row pair, 4 columns).  After all
-// fragments have competed for the shared keys, every thread resolves one pixel: it re-evaluates
-// the winning fragment's quad exactly and shades it (deferred shading).
-template <bool DEPTH_ONLY_1X1>
-__global__ void __launch_bounds__(256, 4) raster_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
-                                                        const TextureData *__restrict__ textures, TileBins bins, TargetParams tg) {
+// Persistent CTAs pull 16x16 tiles of the batch from a device queue.  In a tile, the warps take
+// list entries round-robin (warp w of W takes entries w, w + W, ...): a lane walks a small record by
+// itself (the reference's sequential walk; only the quads inside the tile are tested); large
+// records are rasterised by the whole warp, one lane per (row pair, position in the 2x2 quad),
+// which evaluates the reference's running sums once at the tile's left edge and then walks on.
+// All fragments compete for the tile's shared keys; the winners go to the frame's key image.
+// Tiles that nothing covers write nothing: the resolve pass skips them too.
+template <bool DEPTH_ONLY_1X1, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                                         TileBins bins, const uint32_t *__restrict__ rowOffsets,
+                                                                         const uint32_t *__restrict__ rows) {
+	constexpr int WARPS = THREADS / 32;
+	constexpr int PIXELS = TILE_W * TILE_H / THREADS; // tile pixels owned by each thread
 	__shared__ unsigned long long keys[TILE_H * TILE_STRIDE];
 	__shared__ float initialDepth[TILE_H * TILE_STRIDE];
 	__shared__ uint32_t coverage[TILE_H * TILE_STRIDE];
+	__shared__ uint32_t sharedTile;
 	__shared__ unsigned long long fragmentSum;
-	const int tile = blockIdx.x;
-	const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
-	if (begin == end) return; // nothing covers this tile (its keys were cleared before the launch)
-	const int32_t tx0 = (tile % bins.tilesX) * TILE_W, ty0 = (tile / bins.tilesX) * TILE_H;
 	const int tid = threadIdx.x;
-	const int32_t px = tx0 + (tid & 15), py = ty0 + (tid >> 4);
-	const bool inside = px < tg.width && py < tg.height;
-	const bool depthTest = tg.depth != nullptr;
-	const bool affine = tg.affine != 0;
-	const int me = (tid >> 4) * TILE_STRIDE + (tid & 15); // this thread's pixel in the padded tile arrays
-	initialDepth[me] = (inside && depthTest) ? tg.depth[(size_t)py * tg.depthStride + px] : 0.0f;
-	keys[me] = 0ull;
-	coverage[me] = 0u;
-	if (tid == 0) fragmentSum = 0ull;
-	__syncthreads();
-
 	const int warp = tid >> 5, lane = tid & 31;
-	uint32_t fragments = 0;
-	// entries are dealt round-robin over the warps (warp w takes w, w + 8, w + 16, ...), so that
-	// short lists still keep every warp of the tile busy
-	for (uint32_t chunk = begin; chunk < end; chunk += 32u * 8u) {
-		const uint32_t e = chunk + (uint32_t)warp + 8u * (uint32_t)lane;
-		const bool valid = e < end;
-		const uint32_t myRecord = valid ? bins.lists[e] : 0u;
-		bool small = false;
-		if (valid && !DEPTH_ONLY_1X1) {
-			const DrawRecord r = records[myRecord];
-			small = record_is_small(r, tg.smallRows, tg.smallWidth);
-			if (small) {
-				const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
-				walk_record<1>(r, tg.rows + tg.rowOffsets[myRecord], rowStart, rowEnd, tg.height, [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
-					if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
-					for (int l = 0; l < 4; l++) {
-						const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-						if (xx < tx0 || xx >= tx0 + TILE_W || yy >= tg.height || xx >= tg.width) continue;
-						if (!lane_covered(pair, x, edge, l)) continue;
-						tile_fragment(keys, initialDepth, coverage, tg, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l], myRecord,
-						              depthTest, affine, fragments);
-					}
-				});
-			}
+	for (;;) {
+		if (tid == 0) { sharedTile = atomicAdd(b.tileQueue, 1u); fragmentSum = 0ull; }
+		__syncthreads();
+		const uint32_t tile = sharedTile;
+		if (tile >= b.totalTiles) break;
+		const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
+		if (begin == end) { __syncthreads(); continue; }
+		const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+		const int32_t width = f.width, height = f.height;
+		const float *depthImage = f.depth;
+		const bool depthTest = depthImage != nullptr;
+		const bool affine = f.affine != 0;
+		uint32_t *coverageImage = f.coverage;
+		const bool counting = coverageImage != nullptr;
+		unsigned long long *keyImage = f.keys;
+		const int32_t local = (int32_t)(tile - f.tileBase);
+		const int32_t tx0 = (local % f.tilesX) * TILE_W, ty0 = (local / f.tilesX) * TILE_H;
+		for (int k = 0; k < PIXELS; k++) {
+			const int p = tid + k * THREADS;
+			const int32_t px = tx0 + (p & 15), py = ty0 + (p >> 4);
+			const int me = (p >> 4) * TILE_STRIDE + (p & 15); // the pixel in the padded tile arrays
+			initialDepth[me] = (depthTest && px < width && py < height) ? depthImage[(size_t)py * f.depthStride + px] : 0.0f;
+			keys[me] = 0ull;
+			coverage[me] = 0u;
 		}
-		uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small);
-		while (largeMask) {
-			const int src = __ffs(largeMask) - 1;
-			largeMask &= largeMask - 1;
-			const uint32_t ri = __shfl_sync(0xFFFFFFFFu, myRecord, src);
-			const DrawRecord r = records[ri];
-			// every lane cuts one of the tile's 16 rows (lanes 16..31 repeat 0..15)
-			int32_t rowLeft = 0, rowRight = 0;
-			const int32_t ry = ty0 + (lane & 15);
-			if (ry >= r.top && ry < r.bottom) unpack_row(tg.rows[tg.rowOffsets[ri] + (ry - r.top)], rowLeft, rowRight);
-			if (DEPTH_ONLY_1X1) {
-				// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
-				// pixel and grows by dx one pixel at a time.
-				if (ry >= r.top && ry < r.bottom && ry < tg.height && rowRight > rowLeft) {
-					const int32_t xs = tx0 + (lane >> 4) * 8;
-					const int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
-					if (x0 < x1) {
-						float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)rowLeft + 0.5f)), fmul(r.dy[0], (float)ry + 0.5f));
-						value = chain_add(value, r.dx[0], x0 - rowLeft);
-						for (int32_t x = x0; x < x1; x++) {
-							tile_fragment(keys, initialDepth, coverage, tg, (ry - ty0) * TILE_STRIDE + (x - tx0), value, ri, true, affine, fragments);
-							value = fadd(value, r.dx[0]);
+		__syncthreads();
+
+		uint32_t fragments = 0;
+		for (uint32_t chunk = begin; chunk < end; chunk += 32u * WARPS) {
+			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
+			const bool valid = e < end;
+			const uint32_t myRecord = valid ? bins.lists[e] : 0u;
+			bool small = false;
+			if (valid && !DEPTH_ONLY_1X1) {
+				const DrawRecord r = records[myRecord];
+				small = record_is_small(r, b.smallRows, b.smallWidth);
+				if (small) {
+					const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
+					walk_record<1>(r, rows + rowOffsets[myRecord], rowStart, rowEnd, height,
+					               [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
+						if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
+						for (int l = 0; l < 4; l++) {
+							const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+							if (xx < tx0 || xx >= tx0 + TILE_W || yy >= height || xx >= width) continue;
+							if (!lane_covered(pair, x, edge, l)) continue;
+							tile_fragment(keys, initialDepth, coverage, counting, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l],
+							              myRecord, depthTest, affine, fragments);
+						}
+					});
+				}
+			}
+			uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small);
+			while (largeMask) {
+				const int src = __ffs(largeMask) - 1;
+				largeMask &= largeMask - 1;
+				const uint32_t ri = __shfl_sync(0xFFFFFFFFu, myRecord, src);
+				const DrawRecord r = records[ri];
+				// every lane reads one of the tile's 16 rows (lanes 16..31 repeat 0..15)
+				int32_t rowLeft = 0, rowRight = 0;
+				const int32_t ry = ty0 + (lane & 15);
+				if (ry >= r.top && ry < r.bottom) unpack_row(rows[rowOffsets[ri] + (ry - r.top)], rowLeft, rowRight);
+				if (DEPTH_ONLY_1X1) {
+					// executeTriangleDrawingDepth (renderCore.cpp:343-387): depth starts at the row's left
+					// pixel and grows by dx one pixel at a time.
+					if (ry >= r.top && ry < r.bottom && ry < height && rowRight > rowLeft) {
+						const int32_t xs = tx0 + (lane >> 4) * 8;
+						const int32_t x0 = max(xs, rowLeft), x1 = min(xs + 8, rowRight);
+						if (x0 < x1) {
+							float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)rowLeft + 0.5f)), fmul(r.dy[0], (float)ry + 0.5f));
+							value = chain_add(value, r.dx[0], x0 - rowLeft);
+							for (int32_t x = x0; x < x1; x++) {
+								tile_fragment(keys, initialDepth, coverage, counting, (ry - ty0) * TILE_STRIDE + (x - tx0), value, ri, true,
+								              affine, fragments);
+								value = fadd(value, r.dx[0]);
+							}
 						}
 					}
+					continue;
 				}
-				continue;
-			}
-			// lane = (row pair, position in the 2x2 quad); it walks its position across the tile's quads
-			const int rp = lane >> 2, pos = lane & 3;
-			const int32_t y1 = ty0 + 2 * rp;
-			const int32_t uL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp), uR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp);
-			const int32_t lL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp + 1), lR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp + 1);
-			if (y1 < r.top || y1 >= r.bottom) continue;
-			const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, tg.height);
-			if (!pair.any) continue;
-			const int32_t x0 = max(tx0, pair.obs), x1 = min(tx0 + TILE_W, pair.obe);
-			if (x0 >= x1) continue;
-			const int32_t yy = y1 + (pos >> 1);
-			if (yy >= tg.height) continue;
-			const bool odd = (pos & 1) != 0;
-			const int32_t rowL = (pos < 2) ? pair.upperLeft : pair.lowerLeft, rowR = (pos < 2) ? pair.upperRight : pair.lowerRight;
-			const float dx = r.dx[0], d2 = fmul(dx, 2.0f);
-			const float P0 = fadd(fadd(r.start[0], fmul(dx, (float)pair.obs + 0.5f)), fmul(r.dy[0], (float)y1 + 0.5f));
-			const float R0 = (pos < 2) ? P0 : fadd(P0, r.dy[0]);
-			const bool allEdge = pair.ibe <= pair.ibs;
-			const int32_t nL = (pair.ibs - pair.obs) >> 1;
-			const float m = fmul(d2, (float)((pair.ibe - pair.ibs) >> 1));
-			// state of the reference's running sums at quad x0 (fillerTemplates.h:328-373)
-			int region; // 0 left edge, 1 full quads, 2 right edge
-			float R, V = 0.0f, Rb = 0.0f;
-			if (allEdge || x0 < pair.ibs) {
-				region = 0;
-				R = chain_add(R0, d2, (x0 - pair.obs) >> 1);
-			} else {
-				Rb = chain_add(R0, d2, nL);
-				if (x0 < pair.ibe) {
-					region = 1;
-					R = Rb;
-					V = chain_add(odd ? fadd(Rb, dx) : Rb, d2, (x0 - pair.ibs) >> 1);
+				// lane = (row pair, position in the 2x2 quad); it walks its position across the tile's quads
+				const int rp = lane >> 2, pos = lane & 3;
+				const int32_t y1 = ty0 + 2 * rp;
+				const int32_t uL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp), uR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp);
+				const int32_t lL = __shfl_sync(0xFFFFFFFFu, rowLeft, 2 * rp + 1), lR = __shfl_sync(0xFFFFFFFFu, rowRight, 2 * rp + 1);
+				if (y1 < r.top || y1 >= r.bottom) continue;
+				const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, height);
+				if (!pair.any) continue;
+				const int32_t x0 = max(tx0, pair.obs), x1 = min(tx0 + TILE_W, pair.obe);
+				if (x0 >= x1) continue;
+				const int32_t yy = y1 + (pos >> 1);
+				if (yy >= height) continue;
+				const bool odd = (pos & 1) != 0;
+				const int32_t rowL = (pos < 2) ? pair.upperLeft : pair.lowerLeft, rowR = (pos < 2) ? pair.upperRight : pair.lowerRight;
+				const float dx = r.dx[0], d2 = fmul(dx, 2.0f);
+				const float P0 = fadd(fadd(r.start[0], fmul(dx, (float)pair.obs + 0.5f)), fmul(r.dy[0], (float)y1 + 0.5f));
+				const float R0 = (pos < 2) ? P0 : fadd(P0, r.dy[0]);
+				const bool allEdge = pair.ibe <= pair.ibs;
+				const int32_t nL = (pair.ibs - pair.obs) >> 1;
+				const float m = fmul(d2, (float)((pair.ibe - pair.ibs) >> 1));
+				// state of the reference's running sums at quad x0 (fillerTemplates.h:328-373)
+				int region; // 0 left edge, 1 full quads, 2 right edge
+				float R, V = 0.0f, Rb = 0.0f;
+				if (allEdge || x0 < pair.ibs) {
+					region = 0;
+					R = chain_add(R0, d2, (x0 - pair.obs) >> 1);
 				} else {
-					region = 2;
-					R = chain_add(fadd(Rb, m), d2, (x0 - pair.ibe) >> 1);
+					Rb = chain_add(R0, d2, nL);
+					if (x0 < pair.ibe) {
+						region = 1;
+						R = Rb;
+						V = chain_add(odd ? fadd(Rb, dx) : Rb, d2, (x0 - pair.ibs) >> 1);
+					} else {
+						region = 2;
+						R = chain_add(fadd(Rb, m), d2, (x0 - pair.ibe) >> 1);
+					}
 				}
-			}
-			const int pixRow = (yy - ty0) * TILE_STRIDE;
-			for (int32_t x = x0; x < x1; x += 2) {
-				const int32_t xx = x + (odd ? 1 : 0);
-				const float z = (region == 1) ? V : (odd ? fadd(R, dx) : R);
-				const bool covered = (region == 1) || (xx >= rowL && xx < rowR);
-				if (covered && xx < tg.width)
-					tile_fragment(keys, initialDepth, coverage, tg, pixRow + (xx - tx0), z, ri, depthTest, affine, fragments);
-				if (region == 0) {
-					R = fadd(R, d2);
-					if (!allEdge && x + 2 == pair.ibs) { region = 1; Rb = R; V = odd ? fadd(R, dx) : R; }
-				} else if (region == 1) {
-					V = fadd(V, d2);
-					if (x + 2 == pair.ibe) { region = 2; R = fadd(Rb, m); }
-				} else {
-					R = fadd(R, d2);
+				const int pixRow = (yy - ty0) * TILE_STRIDE;
+				for (int32_t x = x0; x < x1; x += 2) {
+					const int32_t xx = x + (odd ? 1 : 0);
+					const float z = (region == 1) ? V : (odd ? fadd(R, dx) : R);
+					const bool covered = (region == 1) || (xx >= rowL && xx < rowR);
+					if (covered && xx < width)
+						tile_fragment(keys, initialDepth, coverage, counting, pixRow + (xx - tx0), z, ri, depthTest, affine, fragments);
+					if (region == 0) {
+						R = fadd(R, d2);
+						if (!allEdge && x + 2 == pair.ibs) { region = 1; Rb = R; V = odd ? fadd(R, dx) : R; }
+					} else if (region == 1) {
+						V = fadd(V, d2);
+						if (x + 2 == pair.ibe) { region = 2; R = fadd(Rb, m); }
+					} else {
+						R = fadd(R, d2);
+					}
 				}
 			}
 		}
+		if (b.fragments) {
+			for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
+			if (lane == 0) atomicAdd(&fragmentSum, (unsigned long long)fragments);
+		}
+		__syncthreads();
+		for (int k = 0; k < PIXELS; k++) {
+			const int p = tid + k * THREADS;
+			const int32_t px = tx0 + (p & 15), py = ty0 + (p >> 4);
+			const int me = (p >> 4) * TILE_STRIDE + (p & 15);
+			if (px < width && py < height) {
+				if (counting) coverageImage[(size_t)py * width + px] = coverage[me];
+				keyImage[(size_t)py * width + px] = keys[me];
+			}
+		}
+		if (b.fragments && tid == 0) atomicAdd(b.fragments, fragmentSum);
+		__syncthreads();
 	}
-	if (tg.fragments) {
-		for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
-		if (lane == 0) atomicAdd(&fragmentSum, (unsigned long long)fragments);
-	}
-	__syncthreads();
-
-	if (inside) {
-		if (tg.coverage) tg.coverage[(size_t)py * tg.width + px] = coverage[me];
-		tg.keys[(size_t)py * tg.width + px] = keys[me];
-	}
-	if (tg.fragments && tid == 0) atomicAdd(tg.fragments, fragmentSum);
 }
 
 // One thread per pixel: the winning fragment's quad is re-evaluated exactly (its row pair's
 // intervals and the reference's running sums at that quad) and the pixel is shaded (deferred
-// shading: only winners are shaded, one per pixel).
+// shading: only winners are shaded, one per pixel).  One CTA per tile of the batch.
 template <bool DEPTH_ONLY_1X1>
-__global__ void __launch_bounds__(256) resolve_kernel(const DrawRecord *__restrict__ records, const TaskData *__restrict__ tasks,
-                                                      const TextureData *__restrict__ textures, TargetParams tg) {
-	const int32_t px = blockIdx.x * TILE_W + (threadIdx.x & 15), py = blockIdx.y * TILE_H + (threadIdx.x >> 4);
-	if (px >= tg.width || py >= tg.height) return;
-	const unsigned long long key = tg.keys[(size_t)py * tg.width + px];
+__global__ void __launch_bounds__(256) resolve_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                      const uint32_t *__restrict__ binOffsets,
+                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	const uint32_t tile = blockIdx.x;
+	if (binOffsets[tile] == binOffsets[tile + 1]) return; // nothing drawn: the key image was not written here
+	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+	const int32_t local = (int32_t)(tile - f.tileBase);
+	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
+	if (px >= f.width || py >= f.height) return;
+	const unsigned long long key = f.keys[(size_t)py * f.width + px];
 	if (key == 0ull) return;
-	const bool depthTest = tg.depth != nullptr, affine = tg.affine != 0;
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
 	const uint32_t ri = key_record(key, depthTest);
 	const DrawRecord r = records[ri];
-	const uint32_t *recordRows = tg.rows + tg.rowOffsets[ri];
+	const uint32_t *recordRows = rows + rowOffsets[ri];
 	if (DEPTH_ONLY_1X1) {
 		int32_t left, right;
 		unpack_row(recordRows[py - r.top], left, right);
 		float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
 		value = chain_add(value, r.dx[0], px - left);
-		tg.depth[(size_t)py * tg.depthStride + px] = value;
+		f.depth[(size_t)py * f.depthStride + px] = value;
 		return;
 	}
 	const int32_t y1 = py & ~1, x = px & ~1;
 	const int lane4 = ((py & 1) << 1) | (px & 1);
-	const RowPair pair = record_row_pair(r, recordRows, y1, tg.height);
+	const RowPair pair = record_row_pair(r, recordRows, y1, f.height);
 	float w[3][4];
-	const int components = tg.color ? 3 : 1;
+	const int components = f.color ? 3 : 1;
 	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
 	const float depthValue = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
-	if (tg.color) {
+	if (f.color) {
 		float wa[4], wb[4], wc[4];
 		lane_weights(w, affine, wa, wb, wc);
 		ShadeRecord shade;
-		make_shade(tasks[r.task], r.tri, shade);
+		make_shade(b.tasks[r.task], r.tri, shade);
 		float rgba[4];
-		shade_lane(shade, textures, wa, wb, wc, lane4, rgba);
-		tg.color[(size_t)py * tg.colorStride + px] = pack_saturated(rgba, tg.packOrder);
+		shade_lane(shade, b.textures, wa, wb, wc, lane4, rgba);
+		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
 	}
-	if (depthTest) tg.depth[(size_t)py * tg.depthStride + px] = depthValue;
+	if (depthTest) f.depth[(size_t)py * f.depthStride + px] = depthValue;
 }
 
-void launch_raster(const FrameBuffers &fb, const TaskData *tasks, const TextureData *textures, const TileBins &bins,
-                   const TargetParams &target, cudaStream_t stream) {
-	int tiles = bins.tilesX * bins.tilesY;
-	if (tiles > 0) {
-		COUNT_LAUNCH();
-		raster_kernel<false><<<tiles, 256, 0, stream>>>(fb.records, tasks, textures, bins, target);
-		COUNT_LAUNCH();
-		resolve_kernel<false><<<dim3(bins.tilesX, bins.tilesY), 256, 0, stream>>>(fb.records, tasks, textures, target);
+void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,
+                   cudaStream_t stream) {
+	if (b.totalTiles == 0) return;
+	cudaMemsetAsync(b.tileQueue, 0, sizeof(uint32_t), stream);
+	const int threads = config.threadsPerTile == 128 ? 128 : 256;
+	const int maxPerSm = 1024 / threads;
+	const int perSm = config.ctasPerSm < 1 ? 1 : (config.ctasPerSm > maxPerSm ? maxPerSm : config.ctasPerSm);
+	uint32_t ctas = (uint32_t)sm_count() * (uint32_t)perSm;
+	if (ctas > b.totalTiles) ctas = b.totalTiles;
+	COUNT_LAUNCH();
+	if (threads == 128) {
+		if (b.depthOnly) raster_kernel<true, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+		else raster_kernel<false, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+	} else {
+		if (b.depthOnly) raster_kernel<true, 256><<<ctas, 256, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+		else raster_kernel<false, 256><<<ctas, 256, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
 	}
-}
-
-void launch_raster_depth_only(const FrameBuffers &fb, const TileBins &bins, const TargetParams &target, cudaStream_t stream) {
-	int tiles = bins.tilesX * bins.tilesY;
-	if (tiles > 0) {
-		COUNT_LAUNCH();
-		raster_kernel<true><<<tiles, 256, 0, stream>>>(fb.records, nullptr, nullptr, bins, target);
-		COUNT_LAUNCH();
-		resolve_kernel<true><<<dim3(bins.tilesX, bins.tilesY), 256, 0, stream>>>(fb.records, nullptr, nullptr, target);
-	}
+	if (!resolve) return;
+	COUNT_LAUNCH();
+	if (b.depthOnly) resolve_kernel<true><<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	else resolve_kernel<false><<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 }
 
 } // namespace dsrg

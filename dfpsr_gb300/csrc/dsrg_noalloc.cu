@@ -55,6 +55,7 @@ struct Carver {
 
 const uint32_t MAX_RECORDS = 7u * DSRG_NOALLOC_MAX_TRIANGLES; // a clipped triangle is a fan of at most 7
 const uint32_t MAX_TILES = (uint32_t)((DSRG_NOALLOC_MAX_SIDE + 15) / 16) * (uint32_t)((DSRG_NOALLOC_MAX_SIDE + 15) / 16);
+const size_t TABLE_BYTES = 4096; // task, frame and base tables of a batch of one
 
 } // namespace
 
@@ -100,24 +101,22 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	uint32_t *rowCounts = carve.take<uint32_t>(MAX_RECORDS + 2);
 	fb.rowOffsets = carve.take<uint32_t>(MAX_RECORDS + 2);
 	fb.rows = carve.take<uint32_t>(DSRG_NOALLOC_MAX_ROWS);
-	uint32_t *control = carve.take<uint32_t>(4);
-	fb.recordCount = control;
+	uint32_t *control = carve.take<uint32_t>(4); // [0] tile queue, [1] error flag
 	fb.errorFlag = (int32_t *)(control + 1);
 	fb.scanScratchElems = scan_scratch_elems(MAX_RECORDS + 2);
 	fb.scanScratch = carve.take<uint32_t>(fb.scanScratchElems);
 	TileBins bins;
-	bins.tilesX = (width + TILE_W - 1) / TILE_W;
-	bins.tilesY = (height + TILE_H - 1) / TILE_H;
-	bins.counts = carve.take<uint32_t>(MAX_TILES);
+	bins.counts = carve.take<uint32_t>(MAX_TILES + 1);
 	bins.offsets = carve.take<uint32_t>(MAX_TILES + 1);
-	bins.cursors = carve.take<uint32_t>(MAX_TILES);
+	bins.cursors = carve.take<uint32_t>(MAX_TILES + 1);
 	bins.lists = carve.take<uint32_t>(DSRG_NOALLOC_MAX_BIN_ENTRIES);
 	bins.listCapacity = DSRG_NOALLOC_MAX_BIN_ENTRIES;
 	unsigned long long *keys = carve.take<unsigned long long>((size_t)DSRG_NOALLOC_MAX_SIDE * DSRG_NOALLOC_MAX_SIDE);
+	unsigned char *tables = carve.take<unsigned char>(TABLE_BYTES);
 	if (carve.used > (size_t)DSRG_NOALLOC_SCRATCH_BYTES)
 		return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: scratch layout exceeds DSRG_NOALLOC_SCRATCH_BYTES");
 
-	// projection and triangle setup (renderTriangleFromDataDepth, renderCore.cpp:400-443)
+	// the task and frame tables of a batch of one (renderTriangleFromDataDepth, renderCore.cpp:400-443)
 	TaskParams task;
 	memset(&task, 0, sizeof(task));
 	task.positions = m->positions;
@@ -129,50 +128,58 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	task.triangleCount = m->triangleCount;
 	memcpy(task.modelToWorld, modelToWorld, sizeof(task.modelToWorld));
 	task.camera = cam;
-	task.width = width;
-	task.height = height;
-	task.hasDepth = 1;
 	task.diffuse = -1;
 	task.light = -1;
 	task.depthOnly = 1;
+	FrameTarget frame;
+	memset(&frame, 0, sizeof(frame));
+	frame.depth = (float *)depth->data;
+	frame.depthStride = depth->strideBytes / 4;
+	frame.width = width;
+	frame.height = height;
+	frame.affine = camera->perspective ? 0 : 1;
+	BatchParams params;
+	memset(&params, 0, sizeof(params));
+	BatchTotals totals;
+	alignas(16) unsigned char hostTables[TABLE_BYTES];
+	const size_t tableBytes = layout_tables(&task, 1, &frame, 1, nullptr, 0, true, keys, hostTables, tables, params, totals);
+	if (tableBytes > TABLE_BYTES) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: table layout exceeds its scratch");
+	params.smallRows = ctx->smallRows;
+	params.smallWidth = ctx->smallWidth;
+	params.tileQueue = control;
+	// pageable source: the copy is staged before the call returns, so the stack array may go
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(tables, hostTables, tableBytes, cudaMemcpyHostToDevice, stream));
 	// the counters start at zero on every call: the array keeps whatever the previous call left
 	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(control, 0, 4 * sizeof(uint32_t), stream));
-	launch_project(task, fb, stream);
-	launch_setup(task, fb, MAX_RECORDS, stream);
-	uint32_t counts[2] = {0, 0};
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(counts, control, sizeof(counts), cudaMemcpyDeviceToHost, stream));
+	launch_project(params, fb, stream);
+	launch_setup_count(params, fb, stream);
+	uint32_t recordCount = 0;
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&recordCount, fb.triOffsets + totals.triangles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
-	if (counts[1] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: triangle setup reported device error bits " + std::to_string(counts[1]));
-	const uint32_t recordCount = counts[0];
+	if (recordCount > MAX_RECORDS) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: more draw records than its scratch holds");
 
-	// row intervals and tile lists
+	// records, row intervals and tile lists
+	launch_setup_write(params, fb, MAX_RECORDS, stream);
 	launch_row_offsets(fb, recordCount, rowCounts, stream);
-	launch_bin_count(fb, recordCount, bins, 0, 0, stream);
-	uint32_t totals[2] = {0, 0};
-	const uint32_t tiles = (uint32_t)(bins.tilesX * bins.tilesY);
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totals[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totals[1], bins.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	launch_bin_count(params, fb, recordCount, bins, stream);
+	uint32_t totalsRead[3] = {0, 0, 0};
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[1], bins.offsets + totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[2], control + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
-	if (totals[0] > DSRG_NOALLOC_MAX_ROWS)
+	if (totalsRead[2] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: triangle setup reported device error bits " + std::to_string(totalsRead[2]));
+	if (totalsRead[0] > DSRG_NOALLOC_MAX_ROWS)
 		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles span more than DSRG_NOALLOC_MAX_ROWS (2097152) pixel rows");
-	if (totals[1] > DSRG_NOALLOC_MAX_BIN_ENTRIES)
+	if (totalsRead[1] > DSRG_NOALLOC_MAX_BIN_ENTRIES)
 		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles touch more than DSRG_NOALLOC_MAX_BIN_ENTRIES (1048576) tiles in total");
 	launch_rows(fb, recordCount, stream);
-	launch_bin_fill(fb, recordCount, bins, 0, 0, stream);
+	launch_bin_fill(params, fb, recordCount, bins, stream);
 
 	// depth raster (executeTriangleDrawingDepth, renderCore.cpp:343-387) and resolve
-	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(keys, 0, (size_t)width * height * sizeof(unsigned long long), stream));
-	TargetParams tg;
-	memset(&tg, 0, sizeof(tg));
-	tg.depth = (float *)depth->data;
-	tg.depthStride = depth->strideBytes / 4;
-	tg.width = width;
-	tg.height = height;
-	tg.affine = camera->perspective ? 0 : 1;
-	tg.keys = keys;
-	tg.rowOffsets = fb.rowOffsets;
-	tg.rows = fb.rows;
-	launch_raster_depth_only(fb, bins, tg, stream);
+	RasterConfig config;
+	config.threadsPerTile = ctx->threadsPerTile;
+	config.ctasPerSm = ctx->ctasPerSm;
+	launch_raster(params, fb, bins, config, true, stream);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
 	uint32_t errorBits = 0;
 	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&errorBits, control + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));

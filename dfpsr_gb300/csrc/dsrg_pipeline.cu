@@ -1,0 +1,287 @@
+// Host side of one batch through the kernels: table layout, scratch sizing and the three
+// launch phases, shared by the renderer (one frame), the batch API (many frames) and the
+// differentiable renderer.  Between the phases the host reads two totals (draw records, then
+// row intervals and tile-list entries) to size the next phase's buffers exactly.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "dsrg_internal.h"
+
+namespace dsrg {
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+size_t layout_tables(TaskParams *tasks, size_t taskCount, FrameTarget *frames, size_t frameCount, const TextureData *textures,
+                     size_t textureCount, bool depthOnly, unsigned long long *keysBase, unsigned char *host,
+                     unsigned char *deviceBase, BatchParams &params, BatchTotals &totals) {
+	// bases
+	uint32_t points = 0, triangles = 0, tiles = 0;
+	size_t pixels = 0;
+	for (size_t i = 0; i < taskCount; i++) {
+		TaskParams &t = tasks[i];
+		t.pointBase = points;
+		t.triangleBase = triangles;
+		points += (uint32_t)t.pointCount;
+		triangles += (uint32_t)t.triangleCount;
+	}
+	for (size_t i = 0; i < frameCount; i++) {
+		FrameTarget &f = frames[i];
+		f.tilesX = (f.width + TILE_W - 1) / TILE_W;
+		f.tilesY = (f.height + TILE_H - 1) / TILE_H;
+		f.tileBase = tiles;
+		tiles += (uint32_t)(f.tilesX * f.tilesY);
+		f.keys = keysBase ? keysBase + pixels : nullptr;
+		pixels += (size_t)f.width * f.height;
+	}
+	totals.points = points;
+	totals.triangles = triangles;
+	totals.tiles = tiles;
+	totals.pixels = pixels;
+	// layout
+	const size_t taskOffset = 0;
+	const size_t pointBaseOffset = align16(taskOffset + taskCount * sizeof(TaskParams));
+	const size_t triangleBaseOffset = align16(pointBaseOffset + (taskCount + 1) * sizeof(uint32_t));
+	const size_t frameOffset = align16(triangleBaseOffset + (taskCount + 1) * sizeof(uint32_t));
+	const size_t frameTileOffset = align16(frameOffset + frameCount * sizeof(FrameTarget));
+	const size_t textureOffset = align16(frameTileOffset + (frameCount + 1) * sizeof(uint32_t));
+	const size_t bytes = align16(textureOffset + (textureCount + 1) * sizeof(TextureData));
+	if (host) {
+		memset(host, 0, bytes);
+		if (taskCount) memcpy(host + taskOffset, tasks, taskCount * sizeof(TaskParams));
+		uint32_t *pointBase = (uint32_t *)(host + pointBaseOffset), *triangleBase = (uint32_t *)(host + triangleBaseOffset);
+		for (size_t i = 0; i < taskCount; i++) { pointBase[i] = tasks[i].pointBase; triangleBase[i] = tasks[i].triangleBase; }
+		pointBase[taskCount] = points;
+		triangleBase[taskCount] = triangles;
+		if (frameCount) memcpy(host + frameOffset, frames, frameCount * sizeof(FrameTarget));
+		uint32_t *frameTile = (uint32_t *)(host + frameTileOffset);
+		for (size_t i = 0; i < frameCount; i++) frameTile[i] = frames[i].tileBase;
+		frameTile[frameCount] = tiles;
+		if (textureCount) memcpy(host + textureOffset, textures, textureCount * sizeof(TextureData));
+	}
+	params.tasks = (const TaskParams *)(deviceBase + taskOffset);
+	params.taskPointBase = (const uint32_t *)(deviceBase + pointBaseOffset);
+	params.taskTriangleBase = (const uint32_t *)(deviceBase + triangleBaseOffset);
+	params.taskCount = (int32_t)taskCount;
+	params.frames = (const FrameTarget *)(deviceBase + frameOffset);
+	params.frameTileBase = (const uint32_t *)(deviceBase + frameTileOffset);
+	params.frameCount = (int32_t)frameCount;
+	params.textures = (const TextureData *)(deviceBase + textureOffset);
+	params.totalPoints = points;
+	params.totalTriangles = triangles;
+	params.totalTiles = tiles;
+	params.depthOnly = depthOnly ? 1 : 0;
+	return bytes;
+}
+
+size_t layout_tables(BatchJob &job, unsigned long long *keysBase, unsigned char *host, unsigned char *deviceBase,
+                     BatchParams &params, BatchTotals &totals) {
+	return layout_tables(job.tasks.data(), job.tasks.size(), job.frames.data(), job.frames.size(), job.textures.data(),
+	                     job.textures.size(), job.depthOnly, keysBase, host, deviceBase, params, totals);
+}
+
+#define TRY(expr) DSRG_CUDA_TRY(ctx, expr)
+
+// Launch parameters of one phase; compared byte for byte, so it is cleared before it is filled.
+struct PhaseKey {
+	int32_t phase;
+	int32_t resolve;
+	uint32_t recordCount;
+	RasterConfig config;
+	BatchParams params;
+	FrameBuffers fb;
+	TileBins bins;
+	uint32_t *rowCounts;
+};
+
+// Runs one phase's launches on the context's stream, through its graph when the phase repeats.
+template <typename Launches>
+static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &key, Launches launches) {
+	const unsigned char *k = reinterpret_cast<const unsigned char *>(&key);
+	const bool same = g.key.size() == sizeof(key) && memcmp(g.key.data(), k, sizeof(key)) == 0;
+	if (!ctx->useGraphs || !same) {
+		if (!same) {
+			if (g.exec) cudaGraphExecDestroy(g.exec);
+			g.exec = nullptr;
+			g.key.assign(k, k + sizeof(key));
+		}
+		launches();
+		return cudaGetLastError();
+	}
+	if (g.exec) {
+		add_launches(g.launches);
+		return cudaGraphLaunch(g.exec, ctx->stream);
+	}
+	const uint64_t before = launch_count();
+	cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+	if (e != cudaSuccess) return e;
+	launches();
+	cudaGraph_t graph = nullptr;
+	e = cudaStreamEndCapture(ctx->stream, &graph);
+	if (e != cudaSuccess) return e;
+	g.launches = launch_count() - before;
+	e = cudaGraphInstantiate(&g.exec, graph, 0);
+	cudaGraphDestroy(graph);
+	if (e != cudaSuccess) {
+		g.exec = nullptr;
+		return e;
+	}
+	return cudaGraphLaunch(g.exec, ctx->stream);
+}
+
+static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals) {
+	cudaStream_t stream = ctx->stream;
+	totals = BatchTotals();
+	BatchParams params;
+	memset(&params, 0, sizeof(params));
+	// sizes first, then the buffers, then the tables with their final device addresses
+	const size_t tableBytes = layout_tables(job, nullptr, nullptr, nullptr, params, totals);
+	if (totals.pixels > 0) TRY(ctx->keys.reserve(totals.pixels));
+	TRY(ctx->tables.reserve(tableBytes));
+	if (ctx->pinnedCapacity < tableBytes) {
+		if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
+		ctx->pinnedTables = nullptr;
+		ctx->pinnedCapacity = 0;
+		size_t capacity = 4096;
+		while (capacity < tableBytes) capacity *= 2;
+		TRY(cudaMallocHost((void **)&ctx->pinnedTables, capacity));
+		ctx->pinnedCapacity = capacity;
+	}
+	layout_tables(job, ctx->keys.ptr, ctx->pinnedTables, ctx->tables.ptr, params, totals);
+	TRY(cudaMemcpyAsync(ctx->tables.ptr, ctx->pinnedTables, tableBytes, cudaMemcpyHostToDevice, stream));
+	TRY(cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), stream));
+	params.smallRows = ctx->smallRows;
+	params.smallWidth = ctx->smallWidth;
+	params.tileQueue = ctx->control.ptr;
+	params.fragments = nullptr;
+	if (ctx->counting) {
+		TRY(cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), stream));
+		params.fragments = ctx->fragmentCounter.ptr;
+		for (const FrameTarget &f : job.frames)
+			if (f.coverage) TRY(cudaMemsetAsync(f.coverage, 0, (size_t)f.width * f.height * sizeof(uint32_t), stream));
+	}
+	if (totals.triangles == 0) return DSRG_OK; // nothing reaches the tiles: the targets stay as they are
+	RasterConfig config;
+	config.threadsPerTile = ctx->threadsPerTile;
+	config.ctasPerSm = ctx->ctasPerSm;
+	PhaseKey key;
+	memset(&key, 0, sizeof(key));
+	key.resolve = job.resolve ? 1 : 0;
+	key.config = config;
+
+	// phase A: projection and record counts
+	const size_t np = totals.points, nt = totals.triangles;
+	TRY(ctx->csx.reserve(np)); TRY(ctx->csy.reserve(np)); TRY(ctx->csz.reserve(np));
+	TRY(ctx->isx.reserve(np)); TRY(ctx->isy.reserve(np));
+	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
+	TRY(ctx->triCounts.reserve(nt + 1));
+	TRY(ctx->triOffsets.reserve(nt + 1));
+	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(nt > totals.tiles ? nt : totals.tiles) + 1)));
+	FrameBuffers fb;
+	memset(&fb, 0, sizeof(fb));
+	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
+	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
+	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
+	fb.triCounts = ctx->triCounts.ptr;
+	fb.triOffsets = ctx->triOffsets.ptr;
+	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
+	fb.scanScratch = ctx->scanScratch.ptr;
+	fb.scanScratchElems = ctx->scanScratch.capacity;
+	key.phase = 0;
+	key.params = params;
+	key.fb = fb;
+	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
+		launch_project(params, fb, stream);
+		launch_setup_count(params, fb, stream);
+	}));
+	uint32_t recordCount = 0;
+	TRY(cudaMemcpyAsync(&recordCount, fb.triOffsets + nt, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaStreamSynchronize(stream));
+	totals.records = recordCount;
+
+	// phase B: records, row offsets and tile counts
+	TRY(ctx->records.reserve((size_t)recordCount + 1));
+	TRY(ctx->rowCounts.reserve((size_t)recordCount + 1));
+	TRY(ctx->rowOffsets.reserve((size_t)recordCount + 1));
+	TRY(ctx->binCounts.reserve((size_t)totals.tiles + 1));
+	TRY(ctx->binOffsets.reserve((size_t)totals.tiles + 1));
+	TRY(ctx->binCursors.reserve((size_t)totals.tiles + 1));
+	const uint32_t largest = recordCount > totals.tiles ? recordCount : totals.tiles;
+	TRY(ctx->scanScratch.reserve(scan_scratch_elems(largest + 1)));
+	fb.records = ctx->records.ptr;
+	fb.rowOffsets = ctx->rowOffsets.ptr;
+	fb.scanScratch = ctx->scanScratch.ptr;
+	fb.scanScratchElems = ctx->scanScratch.capacity;
+	TileBins bins;
+	memset(&bins, 0, sizeof(bins));
+	bins.counts = ctx->binCounts.ptr;
+	bins.offsets = ctx->binOffsets.ptr;
+	bins.cursors = ctx->binCursors.ptr;
+	uint32_t *rowCounts = ctx->rowCounts.ptr;
+	key.phase = 1;
+	key.recordCount = recordCount;
+	key.fb = fb;
+	key.bins = bins;
+	key.rowCounts = rowCounts;
+	TRY(run_phase(ctx, ctx->graphs[1], key, [&] {
+		launch_setup_write(params, fb, recordCount, stream);
+		launch_row_offsets(fb, recordCount, rowCounts, stream);
+		launch_bin_count(params, fb, recordCount, bins, stream);
+	}));
+	uint32_t readBack[3] = {0, 0, 0};
+	TRY(cudaMemcpyAsync(&readBack[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaMemcpyAsync(&readBack[1], bins.offsets + totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaMemcpyAsync(&readBack[2], ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaStreamSynchronize(stream));
+	if (readBack[2] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(readBack[2]));
+	totals.rows = readBack[0];
+	totals.binEntries = readBack[1];
+
+	// phase C: row intervals and tile lists; phase D: raster and resolve
+	TRY(ctx->rows.reserve((size_t)totals.rows + 2));
+	TRY(ctx->binLists.reserve((size_t)totals.binEntries + 1));
+	fb.rows = ctx->rows.ptr;
+	bins.lists = ctx->binLists.ptr;
+	bins.listCapacity = ctx->binLists.capacity;
+	key.phase = 2;
+	key.fb = fb;
+	key.bins = bins;
+	TRY(run_phase(ctx, ctx->graphs[2], key, [&] {
+		launch_rows(fb, recordCount, stream);
+		launch_bin_fill(params, fb, recordCount, bins, stream);
+	}));
+	TRY(cudaEventRecord(ctx->eventRasterStart, stream));
+	key.phase = 3;
+	TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
+	TRY(cudaEventRecord(ctx->eventRasterStop, stream));
+	return DSRG_OK;
+}
+
+int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals) {
+	const int status = enqueue_phases(ctx, job, totals);
+	if (status == DSRG_OK) TRY(cudaEventRecord(ctx->eventStop, ctx->stream));
+	return status;
+}
+
+int batch_finish(dsrg_context ctx, const BatchTotals &totals) {
+	cudaStream_t stream = ctx->stream;
+	unsigned long long fragments = 0;
+	if (ctx->counting) TRY(cudaMemcpyAsync(&fragments, ctx->fragmentCounter.ptr, sizeof(fragments), cudaMemcpyDeviceToHost, stream));
+	uint32_t errorBits = 0;
+	TRY(cudaMemcpyAsync(&errorBits, ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaStreamSynchronize(stream));
+	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "rasterisation reported device error bits " + std::to_string(errorBits));
+	float ms = 0.0f, rasterMs = 0.0f;
+	cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
+	if (totals.triangles > 0) cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);
+	ctx->stats.fragments = fragments;
+	ctx->stats.drawRecords = totals.records;
+	ctx->stats.binEntries = totals.binEntries;
+	ctx->stats.milliseconds = ms;
+	ctx->stats.rasterMilliseconds = rasterMs;
+	ctx->stats.kernelLaunches = launch_count();
+	return DSRG_OK;
+}
+
+} // namespace dsrg

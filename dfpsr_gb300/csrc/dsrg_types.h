@@ -66,18 +66,8 @@ struct ShadeRecord {
 	float red[3], green[3], blue[3], alpha[3];
 	float u1[3], v1[3], u2[3], v2[3];
 	uint32_t flags;
-	int32_t diffuse; // index into the frame's texture table, -1 for none
+	int32_t diffuse; // index into the batch's texture table, -1 for none
 	int32_t light;
-};
-
-// One model submitted to a frame (renderer_giveTask): where its polygon data lives and which
-// textures of the frame's table it uses.
-struct TaskData {
-	const int32_t *polygons;
-	const float *texCoords;
-	const float *colors;
-	const int32_t *triSource;
-	int32_t diffuse, light, filter, pad;
 };
 
 // One draw command after culling, clipping and the front-face test
@@ -90,11 +80,9 @@ struct __align__(16) DrawRecord {
 	float start[3], dx[3], dy[3];     // pWeightStart, pWeightDx, pWeightDy
 	uint32_t order;                   // submission order: triangle index * 8 + clipped sub-triangle index
 	uint32_t tri;                     // fan triangle of its task (polygon data for shading)
-	uint32_t task;                    // index into the frame's TaskData table
-	uint32_t flags;                   // RECORD_AFFINE for orthogonal cameras
+	uint32_t task;                    // index into the batch's task table
+	uint32_t frame;                   // index into the batch's frame table
 };
-
-static const uint32_t RECORD_AFFINE = 1u;
 
 } // namespace dsrg
 

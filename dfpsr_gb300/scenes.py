@@ -89,6 +89,24 @@ def random_triangles(seed: int = 1234, triangles: int = 20000, width: int = 800,
                  IDENTITY.copy())
 
 
+BATCH_RESOLUTIONS = ((64, 64), (256, 256), (640, 480), (1024, 768))
+
+
+def batch_frames(seed: int = 4321, frames: int = 256, resolutions=BATCH_RESOLUTIONS, min_triangles: int = 1000,
+                 max_triangles: int = 200000, texture_size: int = 256) -> list:
+    """The mixed-size batch: every frame a random_triangles scene with its own seed and its own
+    noise texture, a resolution drawn uniformly from `resolutions` and a triangle count drawn
+    log-uniformly from [min_triangles, max_triangles]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(frames):
+        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
+        n = int(round(math.exp(rng.uniform(math.log(min_triangles), math.log(max_triangles)))))
+        out.append(random_triangles(seed=int(rng.integers(0, 2**31 - 1)), triangles=n, width=w, height=h,
+                                    texture_size=texture_size))
+    return out
+
+
 def value_noise(rng: np.random.Generator, size: int, octaves: int = 6, base_cells: int = 4) -> np.ndarray:
     """Sum of `octaves` layers of bilinearly smoothed lattice noise in [0, 1), float64."""
     result = np.zeros((size, size), np.float64)

@@ -161,6 +161,50 @@ int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
 int dsrg_model_render_depth_noalloc(dsrg_context context, dsrg_model model, const float *modelToWorld,
                                     const dsrg_camera *camera, const dsrg_image *depth);
 
+/* ---- batched rendering; no counterpart in the reference, which renders one target per
+ * renderer_begin / renderer_end (api/rendererAPI.h:54-55).
+ *
+ * A batch holds many frames, each an independent renderer_begin ... renderer_end: its own
+ * colour and depth images (any sizes, host or device memory) and its own tasks, drawn in the
+ * order given.  dsrg_batch_render draws every frame in one pass of the kernels: triangle setup
+ * and binning run over all frames' triangles at once and one persistent tile kernel pulls
+ * (frame, tile) work items from a single device queue.  Each frame's result equals
+ * dsrg_renderer_begin / give_task ... / end on that frame alone.  The launches of each phase are
+ * kept as CUDA graphs and replayed while the batch's sizes stay the same. */
+typedef struct dsrg_batch_s *dsrg_batch;
+int dsrg_batch_create(dsrg_context context, dsrg_batch *out);
+int dsrg_batch_destroy(dsrg_batch batch);
+/* Removes every frame and task (the batch can then be filled again). */
+int dsrg_batch_clear(dsrg_batch batch);
+/* Adds a frame (renderer_begin, api/rendererAPI.cpp:151-168); *frameIndex receives its index. */
+int dsrg_batch_add_frame(dsrg_batch batch, const dsrg_image *color, const dsrg_image *depth, int32_t *frameIndex);
+/* renderer_giveTask (api/modelAPI.h:299-301) for one frame of the batch. */
+int dsrg_batch_give_task(dsrg_batch batch, int32_t frameIndex, dsrg_model model, const float *modelToWorld,
+                         const dsrg_camera *camera);
+/* Draws every frame (renderer_end of each); returns when all results are in the images.  The
+ * batch keeps its frames and tasks, so rendering it again redraws the same scenes. */
+int dsrg_batch_render(dsrg_batch batch);
+
+/* Launch configuration of the tile kernel, chosen per context by dsrg_batch_autotune.
+ *   threadsPerTile   threads of one tile's CTA (128 or 256)
+ *   ctasPerSm        persistent CTAs per SM pulling tiles from the queue (1 to 4)
+ *   smallRows/Width  triangles whose raster bound is at most smallRows x smallWidth pixels are
+ *                    walked by one lane each; larger ones by a whole warp per tile
+ *   graphs           1 to replay each phase's launches as a CUDA graph, 0 to launch directly */
+typedef struct {
+	int32_t threadsPerTile;
+	int32_t ctasPerSm;
+	int32_t smallRows;
+	int32_t smallWidth;
+	int32_t graphs;
+} dsrg_tuning;
+int dsrg_context_get_tuning(dsrg_context context, dsrg_tuning *out);
+int dsrg_context_set_tuning(dsrg_context context, const dsrg_tuning *tuning);
+/* Renders the batch once per candidate configuration (rounds times each), keeps the fastest
+ * for the context and returns it in *best (may be null).  The images end up holding the batch's
+ * rendered frames. */
+int dsrg_batch_autotune(dsrg_batch batch, int32_t rounds, dsrg_tuning *best);
+
 #ifdef __cplusplus
 }
 #endif
