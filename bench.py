@@ -90,6 +90,22 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def count(self) -> int:
+        if not self.file:
+            return 0
+        self.file.flush()
+        pos = self.file.tell()
+        self.file.seek(0)
+        n = sum(1 for line in self.file.read().splitlines() if line.count(",") >= 8)
+        self.file.seek(pos)
+        return n
+
+    def wait_first(self, timeout: float = 5.0):
+        """Waits until nvidia-smi has written its first sample (it takes a moment to start)."""
+        t0 = time.perf_counter()
+        while self.proc and self.count() < 1 and time.perf_counter() - t0 < timeout:
+            time.sleep(0.02)
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -338,14 +354,21 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    launches0 = ctx.stats()["kernel_launches"]
     events, raster_ms = [], []
     with ClockSampler(local) as clocks:
+        clocks.wait_first()
+        launches0 = ctx.stats()["kernel_launches"]
         for _ in range(args.steps):
             events.append(frame_device())
             raster_ms.append(ctx.stats()["raster_milliseconds"])
         torch.cuda.synchronize()
-    launches = ctx.stats()["kernel_launches"] - launches0
+        launches = ctx.stats()["kernel_launches"] - launches0
+        # the timed region can be shorter than the sampling period: keep the same load (untimed)
+        # until a few samples under load exist
+        t0 = time.perf_counter()
+        while clocks.count() < 4 and time.perf_counter() - t0 < 3.0:
+            frame_device()
+        torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in events]
     total_s = sum(step_ms) / 1e3
     if dist:
