@@ -421,8 +421,11 @@ def main():
                     "d2h_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
                     "frames_per_s": world * args.steps / e2e_s},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": traffic, "kernel": "raster_kernel",
-                         "kernel_ms": raster_avg_s * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments},
+                         "peak_source": peak_kind, "traffic": traffic, "kernel": "raster_kernel + resolve_kernel",
+                         "kernel_ms": raster_avg_s * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments,
+                         "model": "28 B per fragment (depth read + depth write + colour write + 4 RGBA8 texels), every "
+                                  "fragment counted before the depth test; the tile kernel's early depth culling skips "
+                                  "fragments that cannot win, so frac can exceed 1 on high-overdraw scenes"},
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }

@@ -671,6 +671,59 @@ __device__ __forceinline__ void tile_fragment(unsigned long long *keys, const fl
 	}
 }
 
+// Early depth culling.  A fragment can only change a pixel when its key beats the pixel's key
+// and its depth passes the test against the initial depth buffer.  In key order (the upper 32
+// bits of make_key) the pixel therefore has a threshold max(key hi, initial depth hi), and a
+// record whose best key hi anywhere in the tile is below the smallest threshold of the tile's
+// pixels cannot change the tile.  Keys only grow while a tile is drawn, so a threshold read
+// early (or read while other warps write) is smaller than the true one: culling stays safe.
+
+// Smallest threshold over the tile's pixels inside the frame, reduced over the warp.
+__device__ __forceinline__ uint32_t warp_tile_threshold(const unsigned long long *keys, const float *initialDepth, int lane,
+                                                        int32_t validW, int32_t validH, bool affine) {
+	uint32_t m = 0xFFFFFFFFu;
+#pragma unroll
+	for (int k = 0; k < TILE_W * TILE_H / 32; k++) {
+		const int p = lane + 32 * k;
+		const int row = p >> 4, col = p & 15;
+		if (col < validW && row < validH) {
+			const int at = row * TILE_STRIDE + col;
+			const uint32_t keyHi = (uint32_t)(keys[at] >> 32);
+			uint32_t initialHi = ordered_depth(initialDepth[at]);
+			if (affine) initialHi = ~initialHi;
+			m = min(m, max(keyHi, initialHi));
+		}
+	}
+	for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+	return m;
+}
+
+// Largest key hi any fragment of the record can have inside the tile.  The reference
+// accumulates depth along rows (start + dx*(x0 + 0.5) + dy*(y + 0.5), then one addition per
+// quad or per pixel), so a fragment's depth differs from the plane's value at its centre by at
+// most (3 + steps) roundings of at most 2^-24 * M each, where M bounds every partial sum and
+// steps is the length of the row walk.  The plane's extreme over the pixel centres of the tile
+// and record bounds lies at a corner; widening it by four times that error bound is conservative.
+// Returns 0xFFFFFFFF (never culled) for non-finite planes.
+__device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
+	const int32_t xa = max(tx0, r.left), xb = min(tx0 + TILE_W, r.right) - 1;
+	const int32_t ya = max(ty0, r.top), yb = min(ty0 + TILE_H, r.bottom) - 1;
+	const float s = r.start[0], dx = r.dx[0], dy = r.dy[0];
+	const float fxa = (float)xa + 0.5f, fxb = (float)xb + 0.5f, fya = (float)ya + 0.5f, fyb = (float)yb + 0.5f;
+	const bool up = !affine; // perspective: the largest 1/W wins; orthogonal: the smallest W
+	const float px = (dx >= 0.0f) == up ? fxb : fxa;
+	const float py = (dy >= 0.0f) == up ? fyb : fya;
+	const float extreme = __fadd_rn(__fadd_rn(s, __fmul_rn(dx, px)), __fmul_rn(dy, py));
+	const float bound = __fadd_rn(__fadd_rn(fabsf(s), __fmul_rn(fabsf(dx), (float)(abs(r.right) + abs(r.left) + 2))),
+	                              __fmul_rn(fabsf(dy), (float)(abs(r.bottom) + abs(r.top) + 2)));
+	const int32_t steps = (pixelSteps ? (r.right - r.left) : ((r.right - r.left) >> 1)) + 16;
+	const float margin = __fmul_rn(__fmul_rn(bound, (float)steps), 2.384185791015625e-7f); // 2^-22 per step
+	const float best = up ? __fadd_rn(extreme, margin) : __fsub_rn(extreme, margin);
+	if (!isfinite(best) || !isfinite(margin)) return 0xFFFFFFFFu;
+	const uint32_t hi = ordered_depth(best);
+	return affine ? ~hi : hi;
+}
+
 // Persistent CTAs pull 16x16 tiles of the batch from a device queue.  In a tile, the warps take
 // list entries round-robin (warp w of W takes entries w, w + W, ...): a lane walks a small record by
 // itself (the reference's sequential walk; only the quads inside the tile are tested); large
@@ -719,15 +772,25 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		__syncthreads();
 
 		uint32_t fragments = 0;
+		// early depth culling needs a depth buffer and is off while fragments are being counted
+		const bool cull = depthTest && b.fragments == nullptr;
+		const int32_t validW = min(TILE_W, width - tx0), validH = min(TILE_H, height - ty0);
+		uint32_t tileMin = 0u; // this warp's view of the tile's depth threshold (0: nothing culled yet)
 		for (uint32_t chunk = begin; chunk < end; chunk += 32u * WARPS) {
 			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
 			const bool valid = e < end;
 			const uint32_t myRecord = valid ? bins.lists[e] : 0u;
-			bool small = false;
-			if (valid && !DEPTH_ONLY_1X1) {
+			bool small = false, culled = false;
+			uint32_t myBest = 0u;
+			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
+			if (valid) {
 				const DrawRecord r = records[myRecord];
-				small = record_is_small(r, b.smallRows, b.smallWidth);
-				if (small) {
+				if (cull) {
+					myBest = record_best_hi(r, tx0, ty0, affine, DEPTH_ONLY_1X1);
+					culled = myBest < tileMin;
+				}
+				small = !DEPTH_ONLY_1X1 && record_is_small(r, b.smallRows, b.smallWidth);
+				if (small && !culled) {
 					const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
 					walk_record<1>(r, rows + rowOffsets[myRecord], rowStart, rowEnd, height,
 					               [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
@@ -742,10 +805,19 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 					});
 				}
 			}
-			uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small);
+			uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small && !culled);
+			int sinceRefresh = 0;
 			while (largeMask) {
 				const int src = __ffs(largeMask) - 1;
 				largeMask &= largeMask - 1;
+				if (cull) {
+					// the threshold only rises while the tile is drawn: refresh it every few records
+					if (++sinceRefresh == 4) {
+						sinceRefresh = 0;
+						tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
+					}
+					if (__shfl_sync(0xFFFFFFFFu, myBest, src) < tileMin) continue;
+				}
 				const uint32_t ri = __shfl_sync(0xFFFFFFFFu, myRecord, src);
 				const DrawRecord r = records[ri];
 				// every lane reads one of the tile's 16 rows (lanes 16..31 repeat 0..15)

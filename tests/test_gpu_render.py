@@ -42,10 +42,15 @@ def assert_same(scene, gpu, ref, label=""):
 
 
 def run_case(ctx, scene, label, **kw):
+    """Renders twice: counting fragments (every fragment is walked, coverage and total are
+    compared) and not counting (the tile kernel's early depth culling is on); both must give
+    the oracle's images."""
     from oracle import port
     gpu = gpu_render(ctx, scene, **kw)
     ref = port.render(scene, coverage=True, **{k: v for k, v in kw.items() if k in ("use_color", "use_depth", "pack_order")})
     assert_same(scene, gpu, ref, label)
+    c, d, _, _ = gpu_render(ctx, scene, **dict(kw, counting=False))
+    assert_same(scene, (c, d, {"fragments": ref[2]["fragments"]}, None), ref, label + " (culling)")
     return gpu
 
 
@@ -137,6 +142,9 @@ def test_model_render_depth(ctx):
     ref, info = port.render_depth(s)
     assert np.array_equal(depth.view(np.uint32), ref.view(np.uint32))
     assert stats["fragments"] == info["fragments"]
+    culled = np.zeros((240, 320), np.float32)  # not counting: early depth culling on
+    ctx.render_depth(m, m.camera, culled)
+    assert np.array_equal(culled.view(np.uint32), ref.view(np.uint32))
 
 
 def test_renderer_tasks_equal_sequential_model_renders(ctx):
