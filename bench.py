@@ -45,6 +45,7 @@ def parse_args():
     p.add_argument("--workload", choices=["terrain", "random"], default="terrain")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     p.add_argument("--batch-frames", type=int, default=256, help="frames of the mixed-size batch (0 skips it)")
+    p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
     return p.parse_args()
 
 
@@ -242,6 +243,80 @@ def batched_section(ctx, args, flush):
     return out
 
 
+def diff_section(ctx, args):
+    """Differentiable rendering: 64 views 256x256 of a 50,000-triangle torus into float RGBA
+    targets, parameters a 512x512 float RGBA texture, per-point colours and a directional light;
+    one step = forward (with visibility buffer) + L2 loss against images rendered from
+    parameters perturbed by N(0, 0.05) + the hand-written adjoint.  The gradient is checked
+    against the FP64 host oracle, whose time is reported as a CPU figure (not a reference
+    baseline: the reference has no differentiable renderer)."""
+    import torch
+    import dfpsr_gb300 as d
+    from dfpsr_gb300 import scenes
+    problem = scenes.diff_problem(seed=99, views=args.diff_views, size=256, texture_size=512)
+    model = d.Model(ctx, problem.mesh)
+    renderer = d.Diff(ctx, model, 512, 512, problem.ambient)
+    cams = []
+    for loc in problem.cameras:
+        cam = d.camera_struct(problem.mesh)
+        for i in range(12):
+            cam.location[i] = float(loc[i])
+        cams.append(cam)
+    views, h, w = len(cams), problem.height, problem.width
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    params = [dev(problem.texture), dev(problem.vertex_colors), dev(problem.light)]
+    target_params = [dev(problem.target_texture), dev(problem.target_vertex_colors), dev(problem.target_light)]
+    images = torch.empty((views, h, w, 4), device="cuda")
+    targets = torch.empty_like(images)
+    vis = torch.empty((views, h, w, 3), dtype=torch.int32, device="cuda")
+    tvis = torch.empty_like(vis)
+    grad = torch.empty_like(images)
+    loss = torch.empty(1, device="cuda")
+    grads = [torch.empty_like(p) for p in params]
+    transform = problem.mesh.model_to_world
+    renderer.forward(cams, transform, *target_params, targets, tvis)
+
+    def step(deterministic):
+        renderer.forward(cams, transform, *params, images, vis)
+        renderer.l2_loss(images, targets, grad, loss)
+        renderer.adjoint(views, w, h, transform, *params, vis, grad, *grads, deterministic)
+
+    out = {"workload": f"{views} views {w}x{h} of a {problem.mesh.triangle_count}-triangle torus, float RGBA targets, "
+                       "parameters 512x512 float RGBA texture + per-point colours + directional light, L2 loss against "
+                       "images from parameters perturbed by N(0, 0.05)"}
+    steps = max(1, min(args.steps, 10))
+    for mode, deterministic in (("atomic", False), ("deterministic", True)):
+        for _ in range(3):
+            step(deterministic)
+        launches0 = ctx.stats()["kernel_launches"]
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step(deterministic)
+        dt = (time.perf_counter() - t0) / steps
+        out[mode] = {"views_per_s": views / dt, "ms_per_step": dt * 1e3,
+                     "launches_per_step": (ctx.stats()["kernel_launches"] - launches0) / steps}
+    # the gradient against the FP64 host oracle, at the GPU's visibility
+    from oracle import diff64
+    t0 = time.perf_counter()
+    shading = diff64.Shading(problem.mesh, vis.cpu().numpy().view(np.uint32), problem.texture.shape)
+    g64 = shading.gradients(problem.texture, problem.vertex_colors, problem.light, problem.ambient,
+                            diff64.l2_grad(images.cpu().numpy(), targets.cpu().numpy()))
+    host_s = time.perf_counter() - t0
+    errors = {}
+    for deterministic in (False, True):
+        step(deterministic)
+        for name, got, want in zip(("texture", "vertex_colors", "light"), grads, g64):
+            errors[f"{'deterministic' if deterministic else 'atomic'}_{name}"] = diff64.relative_error(got.cpu().numpy(), want)
+    out["grad_rel_err"] = errors
+    out["grad_rel_err_max"] = max(errors.values())
+    out["loss"] = float(loss.item())
+    out["fp64_host_oracle"] = {"seconds_per_step": host_s, "views_per_s": views / host_s, "cores": 1,
+                               "kind": "FP64 numpy re-shade and gradient at fixed visibility (not a reference baseline)"}
+    renderer.destroy()
+    model.destroy()
+    return out
+
+
 def cpu_baseline(scene, seconds: float):
     """The oracle's C restatement of the reference renderer on all host cores (band split like
     renderer_end, CommandQueue::execute with 12 bands), over a bounded number of frames."""
@@ -431,6 +506,8 @@ def main():
         }
         if args.batch_frames > 0:
             line["batch"] = batched_section(ctx, args, flush)
+        if args.diff_views > 0:
+            line["differentiable"] = diff_section(ctx, args)
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
         print(json.dumps(line), flush=True)

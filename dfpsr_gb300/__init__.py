@@ -31,6 +31,7 @@ EXPORTED = [
     "dsrg_renderer_end", "dsrg_renderer_takes_triangles", "dsrg_model_render_depth_noalloc",
     "dsrg_batch_create", "dsrg_batch_destroy", "dsrg_batch_clear", "dsrg_batch_add_frame", "dsrg_batch_give_task",
     "dsrg_batch_render", "dsrg_context_get_tuning", "dsrg_context_set_tuning", "dsrg_batch_autotune",
+    "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
 ]
 
 
@@ -106,8 +107,23 @@ def lib():
         l.dsrg_context_get_tuning.argtypes = [P, C.POINTER(Tuning)]
         l.dsrg_context_set_tuning.argtypes = [P, C.POINTER(Tuning)]
         l.dsrg_batch_autotune.argtypes = [P, I, C.POINTER(Tuning)]
+        l.dsrg_diff_create.argtypes = [P, P, I, I, C.c_float, C.POINTER(P)]
+        l.dsrg_diff_destroy.argtypes = [P]
+        l.dsrg_diff_forward.argtypes = [P, I, C.POINTER(Camera), P, P, P, P, P, P]
+        l.dsrg_diff_l2_loss.argtypes = [P, C.c_int64, P, P, P, P]
+        l.dsrg_diff_adjoint.argtypes = [P, I, I, I, P, P, P, P, P, P, P, P, P, I]
         _lib = l
     return _lib
+
+
+def _torch_sync():
+    """Waits for torch's current stream: device tensors handed to the library may still be being
+    written there, and the library works on its own stream.  (Every library call returns with
+    its own work finished, so torch may read the results right after.)"""
+    import sys
+    torch = sys.modules.get("torch")
+    if torch is not None and torch.cuda.is_available() and torch.cuda.is_initialized():
+        torch.cuda.current_stream().synchronize()
 
 
 def _ptr(a) -> Optional[int]:
@@ -174,7 +190,7 @@ class Context:
         """Destroys the context after every model, texture and renderer made from it."""
         if getattr(self, "handle", None):
             kids = list(self._children)
-            for kind in (Batch, Renderer, Model, Texture):
+            for kind in (Diff, Batch, Renderer, Model, Texture):
                 for child in kids:
                     if isinstance(child, kind):
                         child.destroy()
@@ -211,12 +227,14 @@ class Context:
         """dsrg_model_render into the given host (numpy) or device (torch) images, in place."""
         t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
         ci, di = image_struct(color, pack_order), image_struct(depth)
+        _torch_sync()
         self._check(self._l.dsrg_model_render(self.handle, model.handle, t.ctypes.data, C.byref(camera),
                                               C.byref(ci) if ci else None, C.byref(di) if di else None))
 
     def render_depth(self, model: "Model", camera: Camera, depth, transform=None):
         t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
         di = image_struct(depth)
+        _torch_sync()
         self._check(self._l.dsrg_model_render_depth(self.handle, model.handle, t.ctypes.data, C.byref(camera), C.byref(di)))
 
     def renderer(self) -> "Renderer":
@@ -333,6 +351,7 @@ class Renderer:
         self.ctx._check(self.ctx._l.dsrg_renderer_give_task(self.handle, model.handle, t.ctypes.data, C.byref(cam)))
 
     def end(self):
+        _torch_sync()
         self.ctx._check(self.ctx._l.dsrg_renderer_end(self.handle))
         self._images = None
 
@@ -378,10 +397,12 @@ class Batch:
         self._keep.append(model)
 
     def render(self):
+        _torch_sync()
         self.ctx._check(self.ctx._l.dsrg_batch_render(self.handle))
 
     def autotune(self, rounds: int = 2) -> dict:
         t = Tuning()
+        _torch_sync()
         self.ctx._check(self.ctx._l.dsrg_batch_autotune(self.handle, rounds, C.byref(t)))
         return t.as_dict()
 
@@ -392,6 +413,62 @@ class Batch:
     def destroy(self):
         if getattr(self, "handle", None) and self.ctx.handle:
             self.ctx._l.dsrg_batch_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Diff:
+    """dsrg_diff: float-target rendering of one model with a visibility buffer, and its adjoint.
+
+    Tensors are torch CUDA tensors (float32 / int32, contiguous): texture [th, tw, 4], vertex
+    colours [points, 4], light [4] (dir xyz, intensity), images [views, h, w, 4], visibility
+    [views, h, w, 3]."""
+
+    def __init__(self, ctx: Context, model: Model, texture_width: int, texture_height: int, ambient: float):
+        self.ctx = ctx
+        self.model = model
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_diff_create(ctx.handle, model.handle, texture_width, texture_height, C.c_float(ambient),
+                                           C.byref(h)))
+        self.handle = h
+        ctx._adopt(self)
+
+    @staticmethod
+    def _cameras(cameras):
+        arr = (Camera * len(cameras))()
+        for i, c in enumerate(cameras):
+            arr[i] = c
+        return arr
+
+    def forward(self, cameras, transform, texture, vertex_colors, light, images, visibility):
+        cams = self._cameras(cameras)
+        t = np.ascontiguousarray(transform, np.float32)
+        _torch_sync()
+        self.ctx._check(self.ctx._l.dsrg_diff_forward(self.handle, len(cameras), cams, t.ctypes.data, _ptr(texture),
+                                                      _ptr(vertex_colors), _ptr(light), _ptr(images), _ptr(visibility)))
+
+    def l2_loss(self, images, targets, grad_images, loss):
+        _torch_sync()
+        self.ctx._check(self.ctx._l.dsrg_diff_l2_loss(self.handle, images.numel(), _ptr(images), _ptr(targets),
+                                                      _ptr(grad_images), _ptr(loss)))
+
+    def adjoint(self, views, width, height, transform, texture, vertex_colors, light, visibility, grad_images,
+                grad_texture, grad_vertex_colors, grad_light, deterministic: bool = False):
+        t = np.ascontiguousarray(transform, np.float32)
+        _torch_sync()
+        self.ctx._check(self.ctx._l.dsrg_diff_adjoint(self.handle, views, width, height, t.ctypes.data, _ptr(texture),
+                                                      _ptr(vertex_colors), _ptr(light), _ptr(visibility), _ptr(grad_images),
+                                                      _ptr(grad_texture), _ptr(grad_vertex_colors), _ptr(grad_light),
+                                                      1 if deterministic else 0))
+
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_diff_destroy(self.handle)
         self.handle = None
 
     def __del__(self):

@@ -256,9 +256,17 @@ size_t layout_tables(TaskParams *tasks, size_t taskCount, FrameTarget *frames, s
                      size_t textureCount, bool depthOnly, unsigned long long *keysBase, unsigned char *host,
                      unsigned char *deviceBase, BatchParams &params, BatchTotals &totals);
 
-// Runs phases A to C of the batch on the context's stream (growing its scratch as needed) and
+// Where the kernels of an enqueued batch left their results (all null when nothing was drawn).
+struct BatchOutputs {
+	BatchParams params;
+	FrameBuffers fb;
+};
+
+// Runs the phases of the batch on the context's stream (growing its scratch as needed) and
 // returns with the raster queued; the caller queues its copies and then calls batch_finish.
-int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals);
+// Without the resolve pass (job.resolve = false) every frame's key image is complete: zero where
+// nothing was drawn.
+int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs = nullptr);
 // Waits for the stream, checks the device error bits and fills the context's statistics.
 int batch_finish(dsrg_context ctx, const BatchTotals &totals);
 

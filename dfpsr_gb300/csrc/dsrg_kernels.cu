@@ -27,6 +27,7 @@
 #include "dsrg_geometry.h"
 #include "dsrg_shade.h"
 #include "dsrg_kernels.h"
+#include "dsrg_raster.cuh"
 
 namespace dsrg {
 
@@ -52,16 +53,6 @@ static int grid_for(uint64_t n, int threads) {
 	const uint64_t cap = (uint64_t)sm_count() * 16;
 	if (blocks > cap) blocks = cap;
 	return (int)(blocks > 0 ? blocks : 1);
-}
-
-// Largest k in [0, count) with base[k] <= i (base[0] = 0, ascending).
-__device__ __forceinline__ int32_t find_segment(const uint32_t *base, int32_t count, uint32_t i) {
-	int32_t lo = 0, hi = count - 1;
-	while (lo < hi) {
-		const int32_t mid = (lo + hi + 1) >> 1;
-		if (__ldg(&base[mid]) <= i) lo = mid; else hi = mid - 1;
-	}
-	return lo;
 }
 
 // ------------------------------------------------------------------ projection
@@ -345,11 +336,6 @@ void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stre
 	rows_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets, fb.rows);
 }
 
-__device__ __forceinline__ void unpack_row(uint32_t packed, int32_t &left, int32_t &right) {
-	left = (int32_t)(packed & 0xFFFFu);
-	right = (int32_t)(packed >> 16);
-}
-
 // ------------------------------------------------------------------ binning
 
 // Conservative test of whether any pixel of the tile whose top-left pixel is (px0, py0) can be
@@ -474,94 +460,6 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 	}
 }
 
-// ------------------------------------------------------------------ shared raster pieces
-
-// Block bounds of one row pair (fillerTemplates.h:273-293).
-struct RowPair {
-	int32_t obs, obe, ibs, ibe;
-	int32_t upperLeft, upperRight, lowerLeft, lowerRight;
-	bool any;
-};
-
-__device__ __forceinline__ RowPair make_row_pair(int32_t uL, int32_t uR, int32_t lL, int32_t lR, int32_t y2, int32_t maxHeight) {
-	RowPair rp;
-	int32_t outerStart = min(uL, lL), outerEnd = max(uR, lR);
-	int32_t innerStart = max(uL, lL), innerEnd = min(uR, lR);
-	rp.obs = (int32_t)((uint32_t)outerStart & ~1u);
-	rp.obe = (int32_t)(((uint32_t)outerEnd + 1u) & ~1u);
-	rp.ibs = (int32_t)(((uint32_t)innerStart + 1u) & ~1u);
-	rp.ibe = (int32_t)((uint32_t)innerEnd & ~1u);
-	if (y2 >= maxHeight) lR = lL;
-	rp.upperLeft = uL; rp.upperRight = uR; rp.lowerLeft = lL; rp.lowerRight = lR;
-	rp.any = (uR > uL) || (lR > lL);
-	return rp;
-}
-
-// Row pair of a record for the rows y1, y1 + 1 from its row intervals (recordRows = its first row;
-// row offsets are even because raster bounds are row-pair aligned, so two rows load as one uint2).
-__device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, const uint32_t *recordRows, int32_t y1, int32_t height) {
-	int32_t uL, uR, lL, lR;
-	const uint2 two = *reinterpret_cast<const uint2 *>(recordRows + (y1 - r.top));
-	unpack_row(two.x, uL, uR);
-	unpack_row(two.y, lL, lR);
-	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
-}
-
-// The four lane values of one component (1/W or W, U/W, V/W) for the quad at x, following the
-// reference's accumulation: edge quads step pWeightUpper/Lower by 2*dx one quad at a time, the
-// run of full quads steps every lane on its own from where the left edge stopped, and the right
-// edge restarts from the left edge's value plus 2*dx times the run length
-// (fillerTemplates.h:196-244, 328-373).
-__device__ __forceinline__ void quad_lanes(float start, float dx, float dy, const RowPair &rp, int32_t y1, int32_t x, float *out) {
-	const float P0 = fadd(fadd(start, fmul(dx, (float)rp.obs + 0.5f)), fmul(dy, (float)y1 + 0.5f));
-	const float L0 = fadd(P0, dy);
-	const float d2 = fmul(dx, 2.0f);
-	if (rp.ibe <= rp.ibs || x < rp.ibs) {
-		int32_t k = (x - rp.obs) >> 1;
-		float U = chain_add(P0, d2, k), L = chain_add(L0, d2, k);
-		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
-		return;
-	}
-	const int32_t nL = (rp.ibs - rp.obs) >> 1;
-	const float Ub = chain_add(P0, d2, nL), Lb = chain_add(L0, d2, nL);
-	if (x < rp.ibe) {
-		int32_t j = (x - rp.ibs) >> 1;
-		out[0] = chain_add(Ub, d2, j);
-		out[1] = chain_add(fadd(Ub, dx), d2, j);
-		out[2] = chain_add(Lb, d2, j);
-		out[3] = chain_add(fadd(Lb, dx), d2, j);
-	} else {
-		int32_t nI = (rp.ibe - rp.ibs) >> 1, r = (x - rp.ibe) >> 1;
-		float m = fmul(d2, (float)nI);
-		float U = chain_add(fadd(Ub, m), d2, r), L = chain_add(fadd(Lb, m), d2, r);
-		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
-	}
-}
-
-// Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106); full quads draw all four.
-__device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, bool edge, int l) {
-	if (!edge) return true;
-	const int32_t xx = x + (l & 1);
-	return (l < 2) ? (xx >= rp.upperLeft && xx < rp.upperRight) : (xx >= rp.lowerLeft && xx < rp.lowerRight);
-}
-
-__device__ __forceinline__ uint32_t ordered_depth(float z) {
-	uint32_t bits = fbits(z);
-	if (bits == 0x80000000u) bits = 0u; // -0 and +0 compare equal
-	return (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
-}
-
-__device__ __forceinline__ unsigned long long make_key(float z, uint32_t record, bool depthTest, bool affine) {
-	if (!depthTest) return (unsigned long long)(record + 1u); // no depth buffer: the last triangle drawn wins
-	uint32_t hi = ordered_depth(z);
-	if (affine) hi = ~hi;
-	return ((unsigned long long)hi << 32) | (unsigned long long)(~record);
-}
-
-__device__ __forceinline__ uint32_t key_record(unsigned long long key, bool depthTest) {
-	return depthTest ? ~(uint32_t)(key & 0xFFFFFFFFull) : (uint32_t)key - 1u;
-}
-
 // RgbaMultiply_data and its variant (shader/RgbaMultiply.h:37-58, 110-173) for fan triangle `tri`.
 __device__ __forceinline__ void make_shade(const TaskParams &task, uint32_t tri, ShadeRecord &s) {
 	const int32_t src = task.triSource[tri];
@@ -585,21 +483,6 @@ __device__ __forceinline__ void make_shade(const TaskParams &task, uint32_t tri,
 	          (colorless ? SHADE_COLORLESS : 0u) | (task.filter == 1 ? SHADE_ALPHA_FILTER : 0u);
 	s.diffuse = task.diffuse;
 	s.light = task.light;
-}
-
-// Vertex weights of the four lanes from (1/W, U/W, V/W) or (W, U, V) (fillerTemplates.h:197-233).
-__device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, float *wa, float *wb, float *wc) {
-	for (int l = 0; l < 4; l++) {
-		if (affine) {
-			wb[l] = w[1][l];
-			wc[l] = w[2][l];
-		} else {
-			const float linearDepth = fdiv(1.0f, w[0][l]); // reciprocal of the scalar build (noSimd.h:187)
-			wb[l] = fmul(w[1][l], linearDepth);
-			wc[l] = fmul(w[2][l], linearDepth);
-		}
-		wa[l] = 1.0f - fadd(wb[l], wc[l]);
-	}
 }
 
 // ------------------------------------------------------------------ the reference's walk over one record

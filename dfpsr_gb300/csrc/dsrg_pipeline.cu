@@ -130,7 +130,7 @@ static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &ke
 	return cudaGraphLaunch(g.exec, ctx->stream);
 }
 
-static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals) {
+static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs) {
 	cudaStream_t stream = ctx->stream;
 	totals = BatchTotals();
 	BatchParams params;
@@ -150,6 +150,8 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals) 
 	}
 	layout_tables(job, ctx->keys.ptr, ctx->pinnedTables, ctx->tables.ptr, params, totals);
 	TRY(cudaMemcpyAsync(ctx->tables.ptr, ctx->pinnedTables, tableBytes, cudaMemcpyHostToDevice, stream));
+	// without the resolve pass the caller reads every key, also where no tile was drawn
+	if (!job.resolve && totals.pixels > 0) TRY(cudaMemsetAsync(ctx->keys.ptr, 0, totals.pixels * sizeof(unsigned long long), stream));
 	TRY(cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), stream));
 	params.smallRows = ctx->smallRows;
 	params.smallWidth = ctx->smallWidth;
@@ -255,11 +257,16 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals) 
 	key.phase = 3;
 	TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
 	TRY(cudaEventRecord(ctx->eventRasterStop, stream));
+	if (outputs) {
+		outputs->params = params;
+		outputs->fb = fb;
+	}
 	return DSRG_OK;
 }
 
-int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals) {
-	const int status = enqueue_phases(ctx, job, totals);
+int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs) {
+	if (outputs) memset(outputs, 0, sizeof(*outputs));
+	const int status = enqueue_phases(ctx, job, totals, outputs);
 	if (status == DSRG_OK) TRY(cudaEventRecord(ctx->eventStop, ctx->stream));
 	return status;
 }

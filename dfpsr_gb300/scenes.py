@@ -198,3 +198,89 @@ def with_variant(scene: Scene, *, texture: bool = True, light: bool = False, col
     else:
         s.light = None
     return s
+
+
+def torus(major_segments: int = 250, minor_segments: int = 100, major_radius: float = 1.0, minor_radius: float = 0.4,
+          uv_repeat: float = 4.0, width: int = 256, height: int = 256, inside_out: bool = False) -> Scene:
+    """A closed torus of major x minor quads (2 fan triangles each, 50,000 triangles at 250 x 100)
+    around the y axis, with texture coordinates running uv_repeat times around the ring and once
+    around the tube (per polygon corner, so the seams need no duplicated points).  The corners
+    wind so that the outer surface is front-facing (inside_out turns it around)."""
+    i = np.arange(major_segments)
+    j = np.arange(minor_segments)
+    theta = 2.0 * np.pi * i / major_segments
+    phi = 2.0 * np.pi * j / minor_segments
+    ring = major_radius + minor_radius * np.cos(phi)[None, :]
+    x = ring * np.cos(theta)[:, None]
+    z = ring * np.sin(theta)[:, None]
+    y = np.broadcast_to(minor_radius * np.sin(phi)[None, :], x.shape)
+    positions = np.stack([x, y, z], axis=-1).reshape(-1, 3).astype(np.float32)
+    ii, jj = np.meshgrid(i, j, indexing="ij")
+    ii, jj = ii.reshape(-1), jj.reshape(-1)
+    i1, j1 = (ii + 1) % major_segments, (jj + 1) % minor_segments
+    a, b, c, d = ii * minor_segments + jj, i1 * minor_segments + jj, i1 * minor_segments + j1, ii * minor_segments + j1
+    flip = not inside_out
+    corners = np.stack([a, d, c, b] if flip else [a, b, c, d], axis=1).astype(np.int32)
+    cu = np.stack([ii, ii + 1, ii + 1, ii], axis=1).astype(np.float64) * (uv_repeat / major_segments)
+    cv = np.stack([jj, jj, jj + 1, jj + 1], axis=1).astype(np.float64) / minor_segments
+    if flip:
+        cu, cv = cu[:, [0, 3, 2, 1]], cv[:, [0, 3, 2, 1]]
+    tex = np.zeros((len(corners), 4, 4), np.float32)
+    tex[:, :, 0] = cu
+    tex[:, :, 1] = cv
+    tex[:, :, 2] = cu
+    tex[:, :, 3] = cv
+    colors = np.ones((len(corners), 4, 4), np.float32)
+    slope = np.float32(math.tan(math.radians(60.0) * 0.5))
+    return Scene(width, height, positions, corners, tex, colors, None, 1, None, 1, 0,
+                 camera_location((0.0, 0.0, -3.5), (0.0, 0.0, 1.0)), True, float(slope), 0.01, 1000.0, IDENTITY.copy())
+
+
+def orbit_cameras(seed: int, views: int, distance: float = 3.2) -> list:
+    """Camera locations on a sphere around the origin, looking at it, from seeded directions."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(views):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        if abs(d[1]) > 0.95:
+            d[1] = 0.95 * np.sign(d[1])
+            d /= np.linalg.norm(d)
+        out.append(camera_location(tuple(d * distance), tuple(-d)))
+    return out
+
+
+@dataclasses.dataclass
+class DiffProblem:
+    """The differentiable-rendering workload: a mesh, views, parameters and the perturbed
+    parameters that render the target images."""
+    mesh: Scene
+    cameras: list                 # camera locations (12 floats each)
+    width: int
+    height: int
+    texture: np.ndarray           # (T, T, 4) float32
+    vertex_colors: np.ndarray     # (points, 4) float32
+    light: np.ndarray             # (4,) float32: dir xyz, intensity
+    ambient: float
+    target_texture: np.ndarray
+    target_vertex_colors: np.ndarray
+    target_light: np.ndarray
+
+
+def diff_problem(seed: int = 99, views: int = 64, size: int = 256, texture_size: int = 512, major: int = 250,
+                 minor: int = 100, sigma: float = 0.05) -> DiffProblem:
+    rng = np.random.default_rng(seed)
+    mesh = torus(major, minor, width=size, height=size)
+    cams = orbit_cameras(seed + 1, views)
+    tex = (value_noise(rng, texture_size, octaves=5, base_cells=8)[..., None] * 0.6 + 0.2
+           + rng.uniform(-0.1, 0.1, size=(texture_size, texture_size, 4))).astype(np.float32)
+    tex[..., 3] = 1.0
+    vcol = rng.uniform(0.5, 1.0, size=(len(mesh.positions), 4)).astype(np.float32)
+    vcol[:, 3] = 1.0
+    direction = rng.normal(size=3)
+    direction /= np.linalg.norm(direction)
+    light = np.array([*direction, 0.8], np.float32)
+    t_tex = (tex + rng.normal(0.0, sigma, size=tex.shape)).astype(np.float32)
+    t_vcol = (vcol + rng.normal(0.0, sigma, size=vcol.shape)).astype(np.float32)
+    t_light = (light + rng.normal(0.0, sigma, size=4)).astype(np.float32)
+    return DiffProblem(mesh, cams, size, size, tex, vcol, light, 0.3, t_tex, t_vcol, t_light)

@@ -205,6 +205,47 @@ int dsrg_context_set_tuning(dsrg_context context, const dsrg_tuning *tuning);
  * rendered frames. */
 int dsrg_batch_autotune(dsrg_batch batch, int32_t rounds, dsrg_tuning *best);
 
+/* ---- differentiable rendering; no counterpart in the reference.
+ *
+ * Views of one model rendered into float RGBA images.  Coverage and the depth test are exactly
+ * dsrg_model_render's (the same row intervals, 2x2 quads and depth keys; coverage is never
+ * smoothed).  Shading is RgbaMultiply (shader/RgbaMultiply.h:110-173) in float without U8
+ * quantisation, times a directional light:
+ *   uv     = wa*uv0 + wb*uv1 + wc*uv2      the model's texture coordinates of the corners (.xy)
+ *   vertex = wa*c0 + wb*c1 + wc*c2         per-point RGBA colours (parameters)
+ *   texel  = bilinear sample of the float RGBA texture (parameters): the reference's 1/256
+ *            sub-texel positions (api/textureAPI.h:320-430), wrapped, full resolution only
+ *   light  = ambient + intensity * max(0, -dot(N, dir))   N: unit world normal of the fan triangle
+ *                                                        (B - A) x (C - A); dir, intensity: parameters
+ *   rgb    = texel.rgb * vertex.rgb * light,   alpha = texel.a * vertex.a
+ * with (wa, wb, wc) the fragment's perspective-correct vertex weights (fillerTemplates.h:197-233)
+ * and wa = 1 - (wb + wc).  Uncovered pixels are 0.  The forward pass also writes a visibility
+ * buffer, the checkpoint the adjoint reads instead of rasterising again: per pixel the fan
+ * triangle (0xFFFFFFFF when uncovered) and the weights wb, wc as float bits.
+ * Device memory, float32, row-major: texture [textureHeight][textureWidth][4] (power-of-two
+ * sides), vertex colours [pointCount][4], light [4] = dir.x, dir.y, dir.z, intensity,
+ * images [views][height][width][4], visibility [views][height][width][3] (uint32). */
+typedef struct dsrg_diff_s *dsrg_diff;
+int dsrg_diff_create(dsrg_context context, dsrg_model model, int32_t textureWidth, int32_t textureHeight, float ambient,
+                     dsrg_diff *out);
+int dsrg_diff_destroy(dsrg_diff diff);
+/* cameras[views]: all of the same image size. */
+int dsrg_diff_forward(dsrg_diff diff, int32_t views, const dsrg_camera *cameras, const float *modelToWorld,
+                      const float *texture, const float *vertexColors, const float *light, float *images,
+                      uint32_t *visibility);
+/* loss = sum((images - targets)^2) / count into *loss (device), gradImages = 2 (images - targets) / count. */
+int dsrg_diff_l2_loss(dsrg_diff diff, int64_t count, const float *images, const float *targets, float *gradImages,
+                      float *loss);
+/* The adjoint of dsrg_diff_forward at fixed visibility: writes (does not accumulate) the gradients
+ * of the loss with respect to the texture, the vertex colours and the light from gradImages.
+ * deterministic = 0: warp-aggregated atomics (sums in a run-dependent order);
+ * deterministic = 1: every contribution sorted by its target (stable radix sort) and summed per
+ * target in pixel order, bit-identical from run to run. */
+int dsrg_diff_adjoint(dsrg_diff diff, int32_t views, int32_t width, int32_t height, const float *modelToWorld,
+                      const float *texture, const float *vertexColors, const float *light, const uint32_t *visibility,
+                      const float *gradImages, float *gradTexture, float *gradVertexColors, float *gradLight,
+                      int32_t deterministic);
+
 #ifdef __cplusplus
 }
 #endif
