@@ -1230,3 +1230,331 @@ int or_model_render_depth(const or_model *model, const float modelToWorld[12], c
 	free(proj);
 	return 0;
 }
+
+/* ================================================================== deferred light passes */
+/* SDK/SpriteEngine (orthoAPI.cpp, lightAPI.cpp) and api/drawAPI.cpp draw_higher, restated
+ * for the scalar build (4 lanes per float vector: base/simd.h:4196-4207). */
+
+typedef struct { v3 x, y, z; } m3; /* FMatrix3x3 as axes (math/FMatrix3x3.h:11-30) */
+
+/* normalize (math/FVector.h:113-119): v / length(v), length = sqrtf(squareLength). */
+static v3 normalize3(v3 v) {
+	float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+	if (l == 0.0f) return mk3(0.0f, 0.0f, 1.0f);
+	l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+	return mk3(v.x / l, v.y / l, v.z / l);
+}
+static v3 cross3(v3 a, v3 b) { return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); } /* FVector.h:101-103 */
+
+/* FMatrix3x3::makeAxisSystem (FMatrix3x3.h:24-30). */
+static m3 axis_system(v3 forward, v3 up) {
+	m3 r;
+	v3 f = normalize3(forward);
+	r.z = f;
+	r.x = normalize3(cross3(normalize3(up), f));
+	r.y = normalize3(cross3(f, r.x));
+	return r;
+}
+static v3 m3_transform(const m3 *m, v3 p) { /* FMatrix3x3.h:31-37 */
+	return mk3(p.x * m->x.x + p.y * m->y.x + p.z * m->z.x,
+	           p.x * m->x.y + p.y * m->y.y + p.z * m->z.y,
+	           p.x * m->x.z + p.y * m->y.z + p.z * m->z.z);
+}
+static v3 m3_transform_transposed(const m3 *m, v3 p) { /* FMatrix3x3.h:38-44 */
+	return mk3(p.x * m->x.x + p.y * m->x.y + p.z * m->x.z,
+	           p.x * m->y.x + p.y * m->y.y + p.z * m->y.z,
+	           p.x * m->z.x + p.y * m->z.y + p.z * m->z.z);
+}
+static m3 m3_mul(const m3 *left, const m3 *right) { /* FMatrix3x3.h:50-52 */
+	m3 r;
+	r.x = m3_transform(right, left->x);
+	r.y = m3_transform(right, left->y);
+	r.z = m3_transform(right, left->z);
+	return r;
+}
+static m3 m3_inverse(const m3 *m) { /* FMatrix3x3.h:54-80 */
+	float det = m->x.x * m->y.y * m->z.z + m->z.x * m->x.y * m->y.z + m->y.x * m->z.y * m->x.z
+	          - m->x.x * m->z.y * m->y.z - m->y.x * m->x.y * m->z.z - m->z.x * m->y.y * m->x.z;
+	float invDet = 1.0f / det;
+	m3 r;
+	r.x.x = invDet * (m->y.y * m->z.z - m->y.z * m->z.y);
+	r.x.y = -invDet * (m->x.y * m->z.z - m->x.z * m->z.y);
+	r.x.z = invDet * (m->x.y * m->y.z - m->x.z * m->y.y);
+	r.y.x = -invDet * (m->y.x * m->z.z - m->y.z * m->z.x);
+	r.y.y = invDet * (m->x.x * m->z.z - m->x.z * m->z.x);
+	r.y.z = -invDet * (m->x.x * m->y.z - m->x.z * m->y.x);
+	r.z.x = invDet * (m->y.x * m->z.y - m->y.y * m->z.x);
+	r.z.y = -invDet * (m->x.x * m->z.y - m->x.y * m->z.x);
+	r.z.z = invDet * (m->x.x * m->y.y - m->x.y * m->y.x);
+	return r;
+}
+static void m3_store(const m3 *m, float *out) {
+	out[0] = m->x.x; out[1] = m->x.y; out[2] = m->x.z;
+	out[3] = m->y.x; out[4] = m->y.y; out[5] = m->y.z;
+	out[6] = m->z.x; out[7] = m->z.y; out[8] = m->z.z;
+}
+static m3 m3_load(const float *in) {
+	m3 m;
+	m.x = mk3(in[0], in[1], in[2]); m.y = mk3(in[3], in[4], in[5]); m.z = mk3(in[6], in[7], in[8]);
+	return m;
+}
+
+/* OrthoView::OrthoView (orthoAPI.cpp:6-37) of OrthoSystem(cameraTilt, pixelsPerTile).view[index]
+ * (orthoAPI.cpp:85-123). */
+void or_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, or_ortho_view *out) {
+	const float diag = 0.707106781f;
+	/* sqrt of a float argument resolves to the double overload in the reference's build */
+	int32_t yPixelsPerTile = (int32_t)((double)(float)pixelsPerTile / sqrt((double)(cameraTilt * cameraTilt + 1)));
+	v3 up = mk3(0.0f, 1.0f, 0.0f);
+	v3 forward[8] = {mk3(diag, cameraTilt, diag), mk3(-diag, cameraTilt, diag), mk3(-diag, cameraTilt, -diag),
+	                 mk3(diag, cameraTilt, -diag), mk3(0.0f, cameraTilt, 1.0f), mk3(-1.0f, cameraTilt, 0.0f),
+	                 mk3(0.0f, cameraTilt, -1.0f), mk3(1.0f, cameraTilt, 0.0f)};
+	m3 cameraSystem = axis_system(forward[index], up);
+	v3 normalDirection = cameraSystem.z;
+	normalDirection.y = 0.0f;
+	m3 normalToWorld = axis_system(normalDirection, mk3(0.0f, 1.0f, 0.0f));
+	or_camera_desc desc;
+	memset(&desc, 0, sizeof(desc));
+	desc.location[3] = cameraSystem.x.x; desc.location[4] = cameraSystem.x.y; desc.location[5] = cameraSystem.x.z;
+	desc.location[6] = cameraSystem.y.x; desc.location[7] = cameraSystem.y.y; desc.location[8] = cameraSystem.y.z;
+	desc.location[9] = cameraSystem.z.x; desc.location[10] = cameraSystem.z.y; desc.location[11] = cameraSystem.z.z;
+	desc.perspective = 0;
+	desc.slope = 0.5f;
+	desc.width = pixelsPerTile;
+	desc.height = pixelsPerTile;
+	camera cam;
+	camera_create(&cam, &desc);
+	float halfTile = (float)pixelsPerTile * 0.5f;
+	projected px = camera_to_screen(&cam, world_to_camera(&cam, mk3(1.0f, 0.0f, 0.0f)));
+	projected pz = camera_to_screen(&cam, world_to_camera(&cam, mk3(0.0f, 0.0f, 1.0f)));
+	int32_t xAxis[2] = {(int32_t)(px.is.x - halfTile), (int32_t)(px.is.y - halfTile)};
+	int32_t zAxis[2] = {(int32_t)(pz.is.x - halfTile), (int32_t)(pz.is.y - halfTile)};
+	m3 tileToScreen;
+	tileToScreen.x = mk3((float)xAxis[0], (float)xAxis[1], 0.0f);
+	tileToScreen.y = mk3(0.0f, (float)(-yPixelsPerTile), 1.0f);
+	tileToScreen.z = mk3((float)zAxis[0], (float)zAxis[1], 0.0f);
+	m3 screenToTile = m3_inverse(&tileToScreen);
+	m3 toLight;
+	toLight.x = m3_transform_transposed(&normalToWorld, screenToTile.x);
+	toLight.y = m3_transform_transposed(&normalToWorld, screenToTile.y);
+	toLight.z = m3_transform_transposed(&normalToWorld, screenToTile.z);
+	m3 fromLight = m3_inverse(&toLight);
+	m3_store(&normalToWorld, out->normalToWorld);
+	m3_store(&toLight, out->screenDepthToLightSpace);
+	m3_store(&fromLight, out->lightSpaceToScreenDepth);
+	out->pixelOffsetPerTileX[0] = xAxis[0]; out->pixelOffsetPerTileX[1] = xAxis[1];
+	out->pixelOffsetPerTileZ[0] = zAxis[0]; out->pixelOffsetPerTileZ[1] = zAxis[1];
+	out->yPixelsPerTile = yPixelsPerTile;
+}
+
+/* Camera location of side `side` of a shadow cube map: Transform3D(origin, ShadowCubeMapSides[side] *
+ * normalToWorld) (SDK/SpriteEngine/spriteAPI.cpp:328-336, 377-381). */
+void or_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]) {
+	v3 forward[6] = {mk3(1.0f, 0.0f, 0.0f), mk3(-1.0f, 0.0f, 0.0f), mk3(0.0f, 1.0f, 0.0f),
+	                 mk3(0.0f, -1.0f, 0.0f), mk3(0.0f, 0.0f, 1.0f), mk3(0.0f, 0.0f, -1.0f)};
+	v3 up[6] = {mk3(0.0f, 1.0f, 0.0f), mk3(0.0f, 1.0f, 0.0f), mk3(0.0f, 0.0f, 1.0f),
+	            mk3(0.0f, 0.0f, 1.0f), mk3(0.0f, 1.0f, 0.0f), mk3(0.0f, 1.0f, 0.0f)};
+	m3 s = axis_system(forward[side], up[side]);
+	m3 n = m3_load(normalToWorld);
+	m3 r = m3_mul(&s, &n);
+	location[0] = 0.0f; location[1] = 0.0f; location[2] = 0.0f;
+	m3_store(&r, location + 3);
+}
+
+static inline uint32_t sat_add_bytes(uint32_t a, uint32_t b) { /* saturatedAddition of U8 lanes (base/simd.h:2670-2690) */
+	uint32_t out = 0;
+	for (int i = 0; i < 4; i++) {
+		uint32_t s = ((a >> (8 * i)) & 0xFFu) + ((b >> (8 * i)) & 0xFFu);
+		out |= (s > 255u ? 255u : s) << (8 * i);
+	}
+	return out;
+}
+static inline float vmin_ref(float left, float right) { return (right < left) ? right : left; } /* simd.h:2198-2216 */
+static inline float vmax_ref(float left, float right) { return (right > left) ? right : left; } /* simd.h:2217-2235 */
+/* reciprocalSquareRoot of the scalar build (simd.h:4084-4104): 1.0f / sqrt(x) through the double overload. */
+static inline float rsqrt_ref(float x) { return (float)(1.0 / sqrt((double)x)); }
+static inline float sqrt_ref(float x) { return (float)sqrt((double)x); } /* squareRoot (simd.h:4130-4146) */
+static inline uint32_t light_bytes(float r, float g, float b) { /* packOrder_packBytes(r, g, b) of truncated, clamped channels */
+	return trunc_u32(vmin_ref(r, 255.1f)) | (trunc_u32(vmin_ref(g, 255.1f)) << 8) | (trunc_u32(vmin_ref(b, 255.1f)) << 16);
+}
+
+/* setDirectedLight / addDirectedLight (lightAPI.cpp:23-74). */
+void or_directed_light(const or_ortho_view *view, uint32_t *light, int32_t lightStride, const uint32_t *normal,
+                       int32_t normalStride, int32_t width, int32_t height, const float direction[3], float intensity,
+                       const int32_t color[3], int32_t add) {
+	m3 n = m3_load(view->normalToWorld);
+	v3 d = normalize3(m3_transform_transposed(&n, mk3(direction[0], direction[1], direction[2])));
+	v3 rev = mk3(-d.x, -d.y, -d.z);
+	rev = scale3(rev, intensity);
+	rev = scale3(rev, 2.0f);
+	float cr = fmaxf_ref(0.0f, (float)color[0] / 255.0f), cg = fmaxf_ref(0.0f, (float)color[1] / 255.0f);
+	float cb = fmaxf_ref(0.0f, (float)color[2] / 255.0f);
+	for (int32_t y = 0; y < height; y++) {
+		for (int32_t x = 0; x < width; x++) {
+			uint32_t c = normal[(size_t)y * normalStride + x];
+			v3 neg = mk3((float)(c & 0xFFu) - 128.0f, (float)((c >> 8) & 0xFFu) - 128.0f, (float)((c >> 16) & 0xFFu) - 128.0f);
+			float i = vmax_ref(0.0f, dot3(neg, rev));
+			uint32_t bytes = light_bytes(i * cr, i * cg, i * cb);
+			uint32_t *p = light + (size_t)y * lightStride + x;
+			*p = add ? sat_add_bytes(*p, bytes) : bytes;
+		}
+	}
+}
+
+/* getShadowTransparency (lightAPI.cpp:104-138). */
+static float shadow_transparency(const float *cube, int32_t width, float halfWidth, v3 o) {
+	float absX = o.x < 0.0f ? -o.x : o.x, absY = o.y < 0.0f ? -o.y : o.y, absZ = o.z < 0.0f ? -o.z : o.z;
+	int xIsLongest = absX > absY && absX > absZ;
+	int yIsLongerThanZ = absY > absZ;
+	float depth = xIsLongest ? o.x : (yIsLongerThanZ ? o.y : o.z);
+	float slopeUp = (yIsLongerThanZ && !xIsLongest) ? o.z : o.y;
+	float slopeSide = xIsLongest ? -o.z : (yIsLongerThanZ ? -o.x : o.x);
+	int32_t viewOffset = width * (xIsLongest ? 0 : (yIsLongerThanZ ? 2 : 4));
+	int negativeSide = depth < 0.0f;
+	if (negativeSide) { depth = -depth; slopeSide = -slopeSide; viewOffset = viewOffset + width; }
+	float reciDepth = 1.0f / depth;
+	float scale = halfWidth * reciDepth;
+	int32_t sampleX = (int32_t)(halfWidth + (slopeSide * scale));
+	int32_t sampleY = (int32_t)(halfWidth - (slopeUp * scale));
+	int32_t maxPixel = width - 1;
+	if (sampleX < 0) sampleX = 0;
+	if (sampleX > maxPixel) sampleX = maxPixel;
+	if (sampleY < 0) sampleY = 0;
+	if (sampleY > maxPixel) sampleY = maxPixel;
+	float shadowReciDepth = cube[((sampleY + viewOffset) * width) + sampleX];
+	return reciDepth * 1.02f > shadowReciDepth ? 1.0f : 0.0f;
+}
+
+/* calculateBound (lightAPI.cpp:76-102) with alignment 4; returns 0 when nothing is lit. */
+int32_t or_point_light_bound(const or_ortho_view *view, int32_t centerX, int32_t centerY, int32_t width, int32_t height,
+                             const float position[3], float radius, int32_t bound[4]) {
+	m3 n = m3_load(view->normalToWorld), fromLight = m3_load(view->lightSpaceToScreenDepth);
+	v3 lightSpace = m3_transform_transposed(&n, mk3(position[0], position[1], position[2]));
+	v3 rotated = m3_transform(&fromLight, lightSpace);
+	int32_t pcx = (int32_t)rotated.x + centerX, pcy = (int32_t)rotated.y + centerY;
+	int32_t pixelRadius = (int32_t)(radius * fromLight.x.x);
+	if (pcx < -pixelRadius || pcx > width + pixelRadius || pcy < -pixelRadius || pcy > height + pixelRadius) return 0;
+	irect image = {0, 0, width, height};
+	int32_t side = (int32_t)((float)pixelRadius * 2.0f);
+	irect light = {pcx - pixelRadius, pcy - pixelRadius, pcx - pixelRadius + side, pcy - pixelRadius + side};
+	irect r = rect_cut(image, light);
+	if (!(r.right - r.left > 0 && r.bottom - r.top > 0)) return 0;
+	bound[0] = round_down(r.left, 4); bound[1] = r.top; bound[2] = round_up(r.right, 4); bound[3] = r.bottom;
+	return 1;
+}
+
+/* addPointLight (lightAPI.cpp:169-285).  Rows are split into the bands of threadedSplit
+ * (base/threading.cpp:193-263) for `threads` hardware threads: each band restarts the
+ * light-space sweep from its own top row. */
+void or_point_light(const or_ortho_view *view, int32_t centerX, int32_t centerY, uint32_t *light, int32_t lightStride,
+                    const uint32_t *normal, int32_t normalStride, const float *heightImage, int32_t heightStride,
+                    int32_t width, int32_t height, const float position[3], float radius, float intensity,
+                    const int32_t color[3], const float *shadowCube, int32_t cubeWidth, int32_t threads) {
+	int32_t b[4];
+	if (!or_point_light_bound(view, centerX, centerY, width, height, position, radius, b)) return;
+	m3 n = m3_load(view->normalToWorld), toLight = m3_load(view->screenDepthToLightSpace);
+	v3 source = m3_transform_transposed(&n, mk3(position[0], position[1], position[2]));
+	v3 face = toLight.z;
+	float cr = fmaxf_ref(0.0f, (float)color[0] * intensity), cg = fmaxf_ref(0.0f, (float)color[1] * intensity);
+	float cb = fmaxf_ref(0.0f, (float)color[2] * intensity);
+	float reciprocalRadius = 1.0f / radius;
+	float cubeCenter = (float)cubeWidth * 0.5f;
+	int32_t rows = b[3] - b[1];
+	int32_t jobs = (threads > 0 ? threads : 1) * 2;
+	if (jobs > rows / 128) jobs = rows / 128;
+	if (jobs < 1) jobs = 1;
+	v3 dx = toLight.x, dy = toLight.y;
+	v3 dxX = scale3(dx, 4.0f);
+	for (int32_t job = 0; job < jobs; job++) {
+		int32_t y1 = job == 0 ? b[1] : (job * rows) / jobs + b[1];
+		int32_t y2 = job + 1 >= jobs ? b[3] : ((job + 1) * rows) / jobs + b[1];
+		v3 base = sub3(m3_transform(&toLight, mk3(0.5f - (float)centerX + (float)b[0], 0.5f - (float)centerY + (float)y1, 0.0f)), source);
+		v3 lane[4]; /* F32xXx3::createGradient (base/simd.h:474-476, simd3D.h:211-216) */
+		lane[0] = base;
+		lane[1] = mk3(base.x + dx.x, base.y + dx.y, base.z + dx.z);
+		lane[2] = mk3(base.x + dx.x * 2.0f, base.y + dx.y * 2.0f, base.z + dx.z * 2.0f);
+		lane[3] = mk3(base.x + dx.x * 3.0f, base.y + dx.y * 3.0f, base.z + dx.z * 3.0f);
+		for (int32_t y = y1; y < y2; y++) {
+			v3 pixel[4] = {lane[0], lane[1], lane[2], lane[3]};
+			for (int32_t x = b[0]; x < b[2]; x += 4) {
+				for (int l = 0; l < 4; l++) {
+					int32_t xx = x + l;
+					if (xx < width) {
+						float depth = heightImage[(size_t)y * heightStride + xx];
+						v3 o = mk3(pixel[l].x + face.x * depth, pixel[l].y + face.y * depth, pixel[l].z + face.z * depth);
+						float squareLength = (o.x * o.x + o.y * o.y) + o.z * o.z;
+						float ratio = vmin_ref(1.0f, sqrt_ref(squareLength) * reciprocalRadius);
+						uint32_t nc = normal[(size_t)y * normalStride + xx];
+						v3 neg = mk3(((float)(nc & 0xFFu) - 128.0f) * (-1.0f / 128.0f),
+						             ((float)((nc >> 8) & 0xFFu) - 128.0f) * (-1.0f / 128.0f),
+						             ((float)((nc >> 16) & 0xFFu) - 128.0f) * (-1.0f / 128.0f));
+						float distanceIntensity = 1.0f - 2.0f * ratio + ratio * ratio;
+						float rs = rsqrt_ref(squareLength);
+						v3 unit = mk3(o.x * rs, o.y * rs, o.z * rs);
+						float angle = vmax_ref(0.0f, (unit.x * neg.x + unit.y * neg.y) + unit.z * neg.z);
+						float i = angle * distanceIntensity;
+						if (shadowCube) i = i * shadow_transparency(shadowCube, cubeWidth, cubeCenter, o);
+						uint32_t *p = light + (size_t)y * lightStride + xx;
+						*p = sat_add_bytes(*p, light_bytes(i * cr, i * cg, i * cb));
+					}
+					pixel[l] = add3(pixel[l], dxX);
+				}
+			}
+			for (int l = 0; l < 4; l++) lane[l] = add3(lane[l], dy);
+		}
+	}
+}
+
+/* blendLight (lightAPI.cpp:287-323). */
+void or_blend_light(uint32_t *target, int32_t targetStride, int32_t targetPackOrder, const uint32_t *diffuse,
+                    int32_t diffuseStride, const uint32_t *lightImage, int32_t lightStride, int32_t width, int32_t height) {
+	static const uint32_t shifts[4][3] = {{0, 8, 16}, {16, 8, 0}, {8, 16, 24}, {24, 16, 8}}; /* image/PackOrder.h:80-92 */
+	const float scale = (float)(1.0 / 128.0f);
+	for (int32_t y = 0; y < height; y++) {
+		for (int32_t x = 0; x < width; x++) {
+			uint32_t d = diffuse[(size_t)y * diffuseStride + x], l = lightImage[(size_t)y * lightStride + x];
+			uint32_t out = 0;
+			for (int ch = 0; ch < 3; ch++) {
+				float v = ((float)((d >> (8 * ch)) & 0xFFu) * (float)((l >> (8 * ch)) & 0xFFu)) * scale;
+				out |= trunc_u32(vmin_ref(v, 255.1f)) << shifts[targetPackOrder][ch];
+			}
+			target[(size_t)y * targetStride + x] = out;
+		}
+	}
+}
+
+/* Byte index of red, green, blue, alpha in memory for a PackOrderIndex (image/PackOrder.h:61-92). */
+static void pack_indices(int32_t order, int idx[4]) {
+	static const int table[4][4] = {{0, 1, 2, 3}, {2, 1, 0, 3}, {1, 2, 3, 0}, {3, 2, 1, 0}};
+	for (int i = 0; i < 4; i++) idx[i] = table[order][i];
+}
+
+/* draw_higher with two colour images (api/drawAPI.cpp:872-900, 946-981): every source pixel above
+ * -inf, raised by offset, replaces the target height and both colours when strictly higher. */
+void or_draw_higher(float *targetHeight, int32_t thStride, uint32_t *targetA, int32_t taStride, int32_t taPack,
+                    uint32_t *targetB, int32_t tbStride, int32_t tbPack, int32_t tw, int32_t th, const float *sourceHeight,
+                    int32_t shStride, const uint32_t *sourceA, int32_t saStride, int32_t saPack, const uint32_t *sourceB,
+                    int32_t sbStride, int32_t sbPack, int32_t sw, int32_t sh, int32_t left, int32_t top, float offset) {
+	int ta[4], tb[4], sa[4], sb[4];
+	pack_indices(taPack, ta); pack_indices(tbPack, tb); pack_indices(saPack, sa); pack_indices(sbPack, sb);
+	int32_t x0 = left > 0 ? left : 0, y0 = top > 0 ? top : 0;
+	int32_t x1 = left + sw < tw ? left + sw : tw, y1 = top + sh < th ? top + sh : th;
+	for (int32_t y = y0; y < y1; y++) {
+		for (int32_t x = x0; x < x1; x++) {
+			int32_t sx = x - left, sy = y - top;
+			float h = sourceHeight[(size_t)sy * shStride + sx];
+			if (h > -INFINITY) {
+				h += offset;
+				float *t = targetHeight + (size_t)y * thStride + x;
+				if (h > *t) {
+					*t = h;
+					const uint8_t *pa = (const uint8_t *)(sourceA + (size_t)sy * saStride + sx);
+					const uint8_t *pb = (const uint8_t *)(sourceB + (size_t)sy * sbStride + sx);
+					uint8_t *qa = (uint8_t *)(targetA + (size_t)y * taStride + x);
+					uint8_t *qb = (uint8_t *)(targetB + (size_t)y * tbStride + x);
+					for (int c = 0; c < 4; c++) { qa[ta[c]] = pa[sa[c]]; qb[tb[c]] = pb[sb[c]]; }
+				}
+			}
+		}
+	}
+}

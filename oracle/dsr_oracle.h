@@ -92,6 +92,32 @@ int or_model_render(const or_model *model, const float modelToWorld[12], const o
 int or_model_render_depth(const or_model *model, const float modelToWorld[12], const or_camera_desc *cam,
                           float *depth, or_stats *stats);
 
+/* ---- deferred light passes (SDK/SpriteEngine/lightAPI.h:27-31, orthoAPI.h:41-137) and draw_higher ---- */
+/* OrthoView of OrthoSystem(cameraTilt, pixelsPerTile).view[index]; matrices as x, y, z axes. */
+typedef struct {
+	float normalToWorld[9];
+	float screenDepthToLightSpace[9];
+	float lightSpaceToScreenDepth[9];
+	int32_t pixelOffsetPerTileX[2], pixelOffsetPerTileZ[2], yPixelsPerTile;
+} or_ortho_view;
+void or_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, or_ortho_view *out);
+void or_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]);
+void or_directed_light(const or_ortho_view *view, uint32_t *light, int32_t lightStride, const uint32_t *normal,
+                       int32_t normalStride, int32_t width, int32_t height, const float direction[3], float intensity,
+                       const int32_t color[3], int32_t add);
+int32_t or_point_light_bound(const or_ortho_view *view, int32_t centerX, int32_t centerY, int32_t width, int32_t height,
+                             const float position[3], float radius, int32_t bound[4]);
+void or_point_light(const or_ortho_view *view, int32_t centerX, int32_t centerY, uint32_t *light, int32_t lightStride,
+                    const uint32_t *normal, int32_t normalStride, const float *heightImage, int32_t heightStride,
+                    int32_t width, int32_t height, const float position[3], float radius, float intensity,
+                    const int32_t color[3], const float *shadowCube, int32_t cubeWidth, int32_t threads);
+void or_blend_light(uint32_t *target, int32_t targetStride, int32_t targetPackOrder, const uint32_t *diffuse,
+                    int32_t diffuseStride, const uint32_t *lightImage, int32_t lightStride, int32_t width, int32_t height);
+void or_draw_higher(float *targetHeight, int32_t thStride, uint32_t *targetA, int32_t taStride, int32_t taPack,
+                    uint32_t *targetB, int32_t tbStride, int32_t tbPack, int32_t tw, int32_t th, const float *sourceHeight,
+                    int32_t shStride, const uint32_t *sourceA, int32_t saStride, int32_t saPack, const uint32_t *sourceB,
+                    int32_t sbStride, int32_t sbPack, int32_t sw, int32_t sh, int32_t left, int32_t top, float offset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -219,3 +219,105 @@ def camera_to_screen(scene, cs):
     out_flat = np.zeros(2, np.int64)
     lib().or_camera_to_screen(C.byref(d), _ptr(cs), _ptr(out_is), _ptr(out_flat))
     return out_is, out_flat
+
+
+# ---- deferred light passes and draw_higher (oracle/dsr_oracle.c)
+
+class OrthoView(C.Structure):
+    _fields_ = [("normalToWorld", C.c_float * 9), ("screenDepthToLightSpace", C.c_float * 9),
+                ("lightSpaceToScreenDepth", C.c_float * 9), ("pixelOffsetPerTileX", C.c_int32 * 2),
+                ("pixelOffsetPerTileZ", C.c_int32 * 2), ("yPixelsPerTile", C.c_int32)]
+
+    def arrays(self):
+        m = np.concatenate([np.ctypeslib.as_array(self.normalToWorld), np.ctypeslib.as_array(self.screenDepthToLightSpace),
+                            np.ctypeslib.as_array(self.lightSpaceToScreenDepth)]).astype(np.float32)
+        i = np.array([*self.pixelOffsetPerTileX, *self.pixelOffsetPerTileZ, self.yPixelsPerTile], np.int32)
+        return m, i
+
+
+def _light_lib():
+    l = lib()
+    if not getattr(l, "_light_ready", False):
+        P, I, F = C.c_void_p, C.c_int32, C.c_float
+        l.or_ortho_view_create.argtypes = [F, I, I, C.POINTER(OrthoView)]
+        l.or_shadow_side_location.argtypes = [P, I, P]
+        l.or_directed_light.argtypes = [C.POINTER(OrthoView), P, I, P, I, I, I, P, F, P, I]
+        l.or_point_light_bound.argtypes = [C.POINTER(OrthoView), I, I, I, I, P, F, P]
+        l.or_point_light_bound.restype = I
+        l.or_point_light.argtypes = [C.POINTER(OrthoView), I, I, P, I, P, I, P, I, I, I, P, F, F, P, P, I, I]
+        l.or_blend_light.argtypes = [P, I, I, P, I, P, I, I, I]
+        l.or_draw_higher.argtypes = [P, I, P, I, I, P, I, I, I, I, P, I, P, I, I, P, I, I, I, I, I, I, F]
+        l._light_ready = True
+    return l
+
+
+def ortho_view(tilt: float, pixels_per_tile: int, index: int) -> OrthoView:
+    v = OrthoView()
+    _light_lib().or_ortho_view_create(tilt, pixels_per_tile, index, C.byref(v))
+    return v
+
+
+def shadow_side(normal_to_world, side: int):
+    out = np.zeros(12, np.float32)
+    normal_to_world = np.ascontiguousarray(normal_to_world, np.float32)
+    _light_lib().or_shadow_side_location(normal_to_world.ctypes.data, side, out.ctypes.data)
+    return out
+
+
+def directed_light(view: OrthoView, light, normal, direction, intensity, color, add):
+    light = np.ascontiguousarray(light, np.uint32).copy()
+    normal = np.ascontiguousarray(normal, np.uint32)
+    h, w = light.shape
+    direction = np.asarray(direction, np.float32)  # kept alive across the call
+    color = np.asarray(color, np.int32)
+    _light_lib().or_directed_light(C.byref(view), light.ctypes.data, w, normal.ctypes.data, w, w, h,
+                                   direction.ctypes.data, intensity, color.ctypes.data, 1 if add else 0)
+    return light
+
+
+def point_light_bound(view: OrthoView, center, width, height, position, radius):
+    b = np.zeros(4, np.int32)
+    position = np.asarray(position, np.float32)
+    ok = _light_lib().or_point_light_bound(C.byref(view), int(center[0]), int(center[1]), width, height,
+                                           position.ctypes.data, radius, b.ctypes.data)
+    return b if ok else None
+
+
+def point_light(view: OrthoView, center, light, normal, height, position, radius, intensity, color, cube=None, threads=1):
+    light = np.ascontiguousarray(light, np.uint32).copy()
+    normal = np.ascontiguousarray(normal, np.uint32)
+    height = np.ascontiguousarray(height, np.float32)
+    h, w = light.shape
+    cube_arr = None if cube is None else np.ascontiguousarray(cube, np.float32)
+    position = np.asarray(position, np.float32)
+    color = np.asarray(color, np.int32)
+    _light_lib().or_point_light(C.byref(view), int(center[0]), int(center[1]), light.ctypes.data, w, normal.ctypes.data, w,
+                                height.ctypes.data, w, w, h, position.ctypes.data, radius, intensity, color.ctypes.data,
+                                None if cube_arr is None else cube_arr.ctypes.data, 0 if cube_arr is None else cube_arr.shape[1],
+                                threads)
+    return light
+
+
+def blend_light(target_pack_order, diffuse, light):
+    diffuse = np.ascontiguousarray(diffuse, np.uint32)
+    light = np.ascontiguousarray(light, np.uint32)
+    h, w = diffuse.shape
+    out = np.zeros((h, w), np.uint32)
+    _light_lib().or_blend_light(out.ctypes.data, w, target_pack_order, diffuse.ctypes.data, w, light.ctypes.data, w, w, h)
+    return out
+
+
+def draw_higher(target, source, left, top, offset):
+    th, ta, tap, tb, tbp = target
+    sh, sa, sap, sb, sbp = source
+    th = np.ascontiguousarray(th, np.float32).copy()
+    ta = np.ascontiguousarray(ta, np.uint32).copy()
+    tb = np.ascontiguousarray(tb, np.uint32).copy()
+    sh = np.ascontiguousarray(sh, np.float32)
+    sa = np.ascontiguousarray(sa, np.uint32)
+    sb = np.ascontiguousarray(sb, np.uint32)
+    H, W = th.shape
+    h, w = sh.shape
+    _light_lib().or_draw_higher(th.ctypes.data, W, ta.ctypes.data, W, tap, tb.ctypes.data, W, tbp, W, H, sh.ctypes.data, w,
+                                sa.ctypes.data, w, sap, sb.ctypes.data, w, sbp, w, h, left, top, offset)
+    return th, ta, tb

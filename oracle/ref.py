@@ -157,3 +157,90 @@ def triangle_rows(flat, clip, variant: str = "exact", max_rows: int = 1 << 16):
     if n <= 0:
         return int(start[0]), lefts[:0], rights[:0]
     return int(start[0]), lefts[:n].copy(), rights[:n].copy()
+
+
+# ---- deferred light passes and draw_higher through the reference's own functions
+
+def _light_lib(variant: str):
+    l = _load(variant)
+    if not getattr(l, "_light_ready", False):
+        P, I, F = C.c_void_p, C.c_int, C.c_float
+        l.refh_ortho_view.argtypes = [F, I, I, P, P]
+        l.refh_thread_count.restype = I
+        l.refh_shadow_side.argtypes = [P, I, P]
+        l.refh_directed_light.argtypes = [F, I, I, P, P, I, I, P, F, P, I]
+        l.refh_point_light.argtypes = [F, I, I, I, I, P, P, P, I, I, P, F, F, P, P, I]
+        l.refh_blend_light.argtypes = [P, I, P, P, I, I]
+        l.refh_draw_higher.argtypes = [P, P, I, P, I, I, I, P, P, I, P, I, I, I, I, I, F]
+        l._light_ready = True
+    return l
+
+
+def ortho_view(tilt: float, pixels_per_tile: int, index: int, variant: str = "exact"):
+    l = _light_lib(variant)
+    m = np.zeros(27, np.float32)
+    i = np.zeros(5, np.int32)
+    l.refh_ortho_view(tilt, pixels_per_tile, index, _ptr(m), _ptr(i))
+    return m, i
+
+
+def thread_count(variant: str = "exact") -> int:
+    return int(_light_lib(variant).refh_thread_count())
+
+
+def shadow_side(normal_to_world, side: int, variant: str = "exact"):
+    out = np.zeros(12, np.float32)
+    normal_to_world = np.ascontiguousarray(normal_to_world, np.float32)
+    _light_lib(variant).refh_shadow_side(_ptr(normal_to_world), side, _ptr(out))
+    return out
+
+
+def directed_light(view, light, normal, direction, intensity, color, add, variant: str = "exact"):
+    tilt, ppt, index = view
+    light = np.ascontiguousarray(light, np.uint32).copy()
+    normal = np.ascontiguousarray(normal, np.uint32)
+    h, w = light.shape
+    direction = np.asarray(direction, np.float32)  # kept alive across the call
+    color = np.asarray(color, np.int32)
+    _light_lib(variant).refh_directed_light(tilt, ppt, index, _ptr(light), _ptr(normal), w, h, _ptr(direction), intensity,
+                                            _ptr(color), 1 if add else 0)
+    return light
+
+
+def point_light(view, center, light, normal, height, position, radius, intensity, color, cube=None, variant: str = "exact"):
+    tilt, ppt, index = view
+    light = np.ascontiguousarray(light, np.uint32).copy()
+    h, w = light.shape
+    cube_arr = None if cube is None else np.ascontiguousarray(cube, np.float32)
+    normal = np.ascontiguousarray(normal, np.uint32)
+    height = np.ascontiguousarray(height, np.float32)
+    position = np.asarray(position, np.float32)
+    color = np.asarray(color, np.int32)
+    _light_lib(variant).refh_point_light(tilt, ppt, index, int(center[0]), int(center[1]), _ptr(light), _ptr(normal), _ptr(height),
+                                         w, h, _ptr(position), radius, intensity, _ptr(color), _ptr(cube_arr),
+                                         0 if cube_arr is None else cube_arr.shape[1])
+    return light
+
+
+def blend_light(target_pack_order, diffuse, light, variant: str = "exact"):
+    diffuse = np.ascontiguousarray(diffuse, np.uint32)
+    h, w = diffuse.shape
+    out = np.zeros((h, w), np.uint32)
+    light = np.ascontiguousarray(light, np.uint32)
+    _light_lib(variant).refh_blend_light(_ptr(out), target_pack_order, _ptr(diffuse), _ptr(light), w, h)
+    return out
+
+
+def draw_higher(target, source, left, top, offset, variant: str = "exact"):
+    """target, source: (height F32, A RGBA, A pack order, B RGBA, B pack order); returns the new target arrays."""
+    th, ta, tap, tb, tbp = target
+    sh, sa, sap, sb, sbp = source
+    th, ta, tb = (np.ascontiguousarray(a).copy() for a in (th, ta, tb))
+    sh = np.ascontiguousarray(sh, np.float32)
+    sa = np.ascontiguousarray(sa, np.uint32)
+    sb = np.ascontiguousarray(sb, np.uint32)
+    H, W = th.shape
+    h, w = sh.shape
+    _light_lib(variant).refh_draw_higher(_ptr(th), _ptr(ta), tap, _ptr(tb), tbp, W, H, _ptr(sh), _ptr(sa), sap, _ptr(sb), sbp,
+                                         w, h, left, top, offset)
+    return th, ta, tb

@@ -17,6 +17,7 @@
 #include "DFPSR/implementation/render/renderCore.h"
 #include "SDK/SpriteEngine/lightAPI.h"
 #include "SDK/SpriteEngine/orthoAPI.h"
+#include "DFPSR/base/threading.h"
 #include <cstring>
 #include <cstdint>
 
@@ -208,6 +209,118 @@ int refh_triangle_rows(const int64_t* flat, const int* clip, int alignX, int ali
 	for (int r = 0; r < rowCount; r++) { lefts[r] = rows[r].left; rights[r] = rows[r].right; }
 	delete[] rows;
 	return rowCount;
+}
+
+} // extern "C"
+
+// ---- deferred light passes and draw_higher (SDK/SpriteEngine/lightAPI.h:27-31, api/drawAPI.h:142-150)
+
+namespace {
+void storeMatrix(const FMatrix3x3& m, float* out) {
+	out[0] = m.xAxis.x; out[1] = m.xAxis.y; out[2] = m.xAxis.z;
+	out[3] = m.yAxis.x; out[4] = m.yAxis.y; out[5] = m.yAxis.z;
+	out[6] = m.zAxis.x; out[7] = m.zAxis.y; out[8] = m.zAxis.z;
+}
+}
+
+extern "C" {
+
+// OrthoSystem(cameraTilt, pixelsPerTile).view[index]: normalToWorldSpace, screenDepthToLightSpace and
+// lightSpaceToScreenDepth (27 floats) and pixelOffsetPerTileX, pixelOffsetPerTileZ, yPixelsPerTile (5 ints).
+void refh_ortho_view(float cameraTilt, int pixelsPerTile, int index, float* matrices, int* ints) {
+	OrthoSystem system(cameraTilt, pixelsPerTile);
+	const OrthoView& v = system.view[index];
+	storeMatrix(v.normalToWorldSpace, matrices);
+	storeMatrix(v.screenDepthToLightSpace, matrices + 9);
+	storeMatrix(v.lightSpaceToScreenDepth, matrices + 18);
+	ints[0] = v.pixelOffsetPerTileX.x; ints[1] = v.pixelOffsetPerTileX.y;
+	ints[2] = v.pixelOffsetPerTileZ.x; ints[3] = v.pixelOffsetPerTileZ.y;
+	ints[4] = v.yPixelsPerTile;
+}
+
+// The hardware thread count that the reference's threadedSplit plans its row bands with.
+int refh_thread_count() { return getThreadCount(); }
+
+// Camera location of a shadow cube side the way PointLight::renderModelShadow builds it
+// (SDK/SpriteEngine/spriteAPI.cpp:328-336, 377-381), from the reference's own matrix code.
+void refh_shadow_side(const float* normalToWorld, int side, float* location) {
+	static const FVector3D forward[6] = {FVector3D(1.0f, 0.0f, 0.0f), FVector3D(-1.0f, 0.0f, 0.0f), FVector3D(0.0f, 1.0f, 0.0f),
+	                                     FVector3D(0.0f, -1.0f, 0.0f), FVector3D(0.0f, 0.0f, 1.0f), FVector3D(0.0f, 0.0f, -1.0f)};
+	static const FVector3D up[6] = {FVector3D(0.0f, 1.0f, 0.0f), FVector3D(0.0f, 1.0f, 0.0f), FVector3D(0.0f, 0.0f, 1.0f),
+	                                FVector3D(0.0f, 0.0f, 1.0f), FVector3D(0.0f, 1.0f, 0.0f), FVector3D(0.0f, 1.0f, 0.0f)};
+	FMatrix3x3 n(FVector3D(normalToWorld[0], normalToWorld[1], normalToWorld[2]),
+	             FVector3D(normalToWorld[3], normalToWorld[4], normalToWorld[5]),
+	             FVector3D(normalToWorld[6], normalToWorld[7], normalToWorld[8]));
+	FMatrix3x3 r = FMatrix3x3::makeAxisSystem(forward[side], up[side]) * n;
+	location[0] = 0.0f; location[1] = 0.0f; location[2] = 0.0f;
+	storeMatrix(r, location + 3);
+}
+
+// setDirectedLight (add = 0) / addDirectedLight (add = 1) on width x height RGBA images.
+void refh_directed_light(float cameraTilt, int pixelsPerTile, int index, uint32_t* light, const uint32_t* normal,
+                         int width, int height, const float* direction, float intensity, const int* color, int add) {
+	OrthoSystem system(cameraTilt, pixelsPerTile);
+	OrderedImageRgbaU8 lightImage = image_create_RgbaU8(width, height);
+	OrderedImageRgbaU8 normalImage = image_create_RgbaU8(width, height);
+	copyInRgba(lightImage, light, width, height);
+	copyInRgba(normalImage, normal, width, height);
+	FVector3D dir(direction[0], direction[1], direction[2]);
+	ColorRgbI32 c(color[0], color[1], color[2]);
+	if (add) addDirectedLight(system.view[index], lightImage, normalImage, dir, intensity, c);
+	else setDirectedLight(system.view[index], lightImage, normalImage, dir, intensity, c);
+	copyOutRgba(lightImage, light, width, height);
+}
+
+// addPointLight with a shadow cube map (cube != null: cubeWidth x 6 cubeWidth floats) or without.
+void refh_point_light(float cameraTilt, int pixelsPerTile, int index, int centerX, int centerY, uint32_t* light,
+                      const uint32_t* normal, const float* heightData, int width, int height, const float* position,
+                      float radius, float intensity, const int* color, const float* cube, int cubeWidth) {
+	OrthoSystem system(cameraTilt, pixelsPerTile);
+	OrderedImageRgbaU8 lightImage = image_create_RgbaU8(width, height);
+	OrderedImageRgbaU8 normalImage = image_create_RgbaU8(width, height);
+	AlignedImageF32 heightImage = image_create_F32(width, height);
+	copyInRgba(lightImage, light, width, height);
+	copyInRgba(normalImage, normal, width, height);
+	copyInF32(heightImage, heightData, width, height);
+	FVector3D pos(position[0], position[1], position[2]);
+	ColorRgbI32 c(color[0], color[1], color[2]);
+	if (cube) {
+		AlignedImageF32 cubeImage = image_create_F32(cubeWidth, cubeWidth * 6);
+		copyInF32(cubeImage, cube, cubeWidth, cubeWidth * 6);
+		addPointLight(system.view[index], IVector2D(centerX, centerY), lightImage, normalImage, heightImage, pos, radius, intensity, c, cubeImage);
+	} else {
+		addPointLight(system.view[index], IVector2D(centerX, centerY), lightImage, normalImage, heightImage, pos, radius, intensity, c);
+	}
+	copyOutRgba(lightImage, light, width, height);
+}
+
+// blendLight into a target of the given pack order.
+void refh_blend_light(uint32_t* target, int targetPackOrder, const uint32_t* diffuse, const uint32_t* light, int width, int height) {
+	AlignedImageRgbaU8 targetImage = image_create_RgbaU8_native(width, height, PackOrderIndex(targetPackOrder));
+	OrderedImageRgbaU8 diffuseImage = image_create_RgbaU8(width, height);
+	OrderedImageRgbaU8 lightImage = image_create_RgbaU8(width, height);
+	copyInRgba(diffuseImage, diffuse, width, height);
+	copyInRgba(lightImage, light, width, height);
+	blendLight(targetImage, diffuseImage, lightImage);
+	copyOutRgba(targetImage, target, width, height);
+}
+
+// draw_higher(F32 height, two RGBA images) with the given pack orders.
+void refh_draw_higher(float* targetHeight, uint32_t* targetA, int targetAPack, uint32_t* targetB, int targetBPack, int tw, int th,
+                      const float* sourceHeight, const uint32_t* sourceA, int sourceAPack, const uint32_t* sourceB, int sourceBPack,
+                      int sw, int sh, int left, int top, float offset) {
+	AlignedImageF32 th_ = image_create_F32(tw, th);
+	AlignedImageRgbaU8 ta = image_create_RgbaU8_native(tw, th, PackOrderIndex(targetAPack));
+	AlignedImageRgbaU8 tb = image_create_RgbaU8_native(tw, th, PackOrderIndex(targetBPack));
+	AlignedImageF32 sh_ = image_create_F32(sw, sh);
+	AlignedImageRgbaU8 sa = image_create_RgbaU8_native(sw, sh, PackOrderIndex(sourceAPack));
+	AlignedImageRgbaU8 sb = image_create_RgbaU8_native(sw, sh, PackOrderIndex(sourceBPack));
+	copyInF32(th_, targetHeight, tw, th); copyInRgba(ta, targetA, tw, th); copyInRgba(tb, targetB, tw, th);
+	copyInF32(sh_, sourceHeight, sw, sh); copyInRgba(sa, sourceA, sw, sh); copyInRgba(sb, sourceB, sw, sh);
+	ImageF32 targetHeightImage = th_;
+	ImageRgbaU8 targetAImage = ta, targetBImage = tb;
+	draw_higher(targetHeightImage, sh_, targetAImage, sa, targetBImage, sb, left, top, offset);
+	copyOutF32(th_, targetHeight, tw, th); copyOutRgba(ta, targetA, tw, th); copyOutRgba(tb, targetB, tw, th);
 }
 
 } // extern "C"
