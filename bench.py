@@ -46,6 +46,7 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="bound of the CPU-baseline sample")
     p.add_argument("--batch-frames", type=int, default=256, help="frames of the mixed-size batch (0 skips it)")
     p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
+    p.add_argument("--light-sprites", type=int, default=4096, help="sprites of the deferred-light pass (0 skips it)")
     return p.parse_args()
 
 
@@ -317,6 +318,66 @@ def diff_section(ctx, args):
     return out
 
 
+def light_section(ctx, args):
+    """Isometric deferred-light pass at 1920x1080: 4096 sprites 64x64 drawn with draw_higher into
+    diffuse, normal and height images, 16 point lights (radius 100-400 px) each with a 6 x 512 x 512
+    shadow cube map rendered from a 2,000-triangle caster model (one depth-only batch of 96 faces),
+    a directed light, the point lights, blendLight.  The CPU figure is the oracle's C restatement of
+    the same pass on one core, whose output the GPU's must equal."""
+    import torch
+    import dfpsr_gb300 as d
+    from dfpsr_gb300 import scenes
+    from dfpsr_gb300.sprite_pass import DeferredLightPass
+    m, _ = d.ortho_view(-0.7, 64, 0).arrays()
+    scene = scenes.light_scene(seed=2024, sprites=args.light_sprites, light_space=(m[9:18], m[0:9]))
+    threads = os.cpu_count() or 1
+    gpu = DeferredLightPass(ctx, scene, threads)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(3):
+        gpu.run()
+    steps = max(1, min(args.steps, 20))
+    times = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        gpu.run()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = statistics.median(times)
+    # the point-light pass alone: 20 B per lit pixel and light (normal, height, light read + write, shadow sample)
+    bounds = 0
+    from oracle import port, light_pass
+    view = port.ortho_view(scene.camera_tilt, scene.pixels_per_tile, scene.view_index)
+    for l in scene.lights:
+        b = port.point_light_bound(view, scene.center, scene.width, scene.height, l["position"], l["radius"])
+        if b is not None:
+            bounds += int((b[2] - b[0]) * (b[3] - b[1]))
+    lt = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        ctx.light_points(gpu.view, scene.center, gpu.light, gpu.normal, gpu.height, gpu.light_list, threads)
+        b.record()
+        b.synchronize()
+        lt.append(a.elapsed_time(b))
+    t0 = time.perf_counter()
+    out, *_ = light_pass.run(scene, threads)
+    cpu_s = time.perf_counter() - t0
+    got = gpu.run().cpu().numpy().view(np.uint32)
+    result = {"workload": "isometric deferred-light pass 1920x1080: 4096 sprites 64x64 (draw_higher), 16 point lights "
+                          "radius 100-400 px with 6x512x512 shadow cube maps from a 2,000-triangle caster (depth-only "
+                          "batch of 96 faces), directed light, blendLight",
+              "frames_per_s": 1e3 / ms, "ms_per_frame": ms,
+              "point_lights_ms": statistics.median(lt), "lit_pixel_lights": bounds,
+              "point_lights_GB_per_s": 20.0 * bounds / (statistics.median(lt) / 1e3) / 1e9,
+              "parity_with_oracle": bool(np.array_equal(got, out)),
+              "cpu_oracle": {"frames_per_s": 1.0 / cpu_s, "cores": 1, "kind": "port",
+                             "sample": "one frame of the same pass, oracle C restatement, one thread"}}
+    gpu.destroy()
+    return result
+
+
 def cpu_baseline(scene, seconds: float):
     """The oracle's C restatement of the reference renderer on all host cores (band split like
     renderer_end, CommandQueue::execute with 12 bands), over a bounded number of frames."""
@@ -508,6 +569,8 @@ def main():
             line["batch"] = batched_section(ctx, args, flush)
         if args.diff_views > 0:
             line["differentiable"] = diff_section(ctx, args)
+        if args.light_sprites > 0:
+            line["deferred_light"] = light_section(ctx, args)
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
         print(json.dumps(line), flush=True)

@@ -32,6 +32,8 @@ EXPORTED = [
     "dsrg_batch_create", "dsrg_batch_destroy", "dsrg_batch_clear", "dsrg_batch_add_frame", "dsrg_batch_give_task",
     "dsrg_batch_render", "dsrg_context_get_tuning", "dsrg_context_set_tuning", "dsrg_batch_autotune",
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
+    "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
+    "dsrg_draw_higher", "dsrg_batch_set_depth_only",
 ]
 
 
@@ -63,6 +65,30 @@ class Tuning(C.Structure):
     def as_dict(self) -> dict:
         return {"threads_per_tile": self.threadsPerTile, "ctas_per_sm": self.ctasPerSm, "small_rows": self.smallRows,
                 "small_width": self.smallWidth, "graphs": self.graphs}
+
+
+class OrthoView(C.Structure):
+    _fields_ = [("normalToWorld", C.c_float * 9), ("screenDepthToLightSpace", C.c_float * 9),
+                ("lightSpaceToScreenDepth", C.c_float * 9), ("pixelOffsetPerTileX", C.c_int32 * 2),
+                ("pixelOffsetPerTileZ", C.c_int32 * 2), ("yPixelsPerTile", C.c_int32)]
+
+    def arrays(self):
+        m = np.concatenate([np.ctypeslib.as_array(self.normalToWorld), np.ctypeslib.as_array(self.screenDepthToLightSpace),
+                            np.ctypeslib.as_array(self.lightSpaceToScreenDepth)]).astype(np.float32)
+        i = np.array([*self.pixelOffsetPerTileX, *self.pixelOffsetPerTileZ, self.yPixelsPerTile], np.int32)
+        return m, i
+
+
+class PointLight(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("radius", C.c_float), ("intensity", C.c_float), ("color", C.c_int32 * 3),
+                ("shadowCube", C.c_void_p), ("cubeWidth", C.c_int32)]
+
+
+class Sprite(C.Structure):
+    _fields_ = [("height", C.c_void_p), ("colorA", C.c_void_p), ("colorB", C.c_void_p), ("width", C.c_int32),
+                ("height_", C.c_int32), ("heightStrideBytes", C.c_int32), ("colorAStrideBytes", C.c_int32),
+                ("colorBStrideBytes", C.c_int32), ("colorAPackOrder", C.c_int32), ("colorBPackOrder", C.c_int32),
+                ("left", C.c_int32), ("top", C.c_int32), ("offset", C.c_float)]
 
 
 _lib = None
@@ -112,6 +138,14 @@ def lib():
         l.dsrg_diff_forward.argtypes = [P, I, C.POINTER(Camera), P, P, P, P, P, P]
         l.dsrg_diff_l2_loss.argtypes = [P, C.c_int64, P, P, P, P]
         l.dsrg_diff_adjoint.argtypes = [P, I, I, I, P, P, P, P, P, P, P, P, P, I]
+        l.dsrg_ortho_view_create.argtypes = [C.c_float, I, I, C.POINTER(OrthoView)]
+        l.dsrg_shadow_side_location.argtypes = [P, I, P]
+        l.dsrg_light_directed.argtypes = [P, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), P, C.c_float, P, I]
+        l.dsrg_light_points.argtypes = [P, C.POINTER(OrthoView), I, I, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
+                                        C.POINTER(PointLight), I, I]
+        l.dsrg_light_blend.argtypes = [P, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image)]
+        l.dsrg_draw_higher.argtypes = [P, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Sprite), I]
+        l.dsrg_batch_set_depth_only.argtypes = [P, I]
         _lib = l
     return _lib
 
@@ -242,6 +276,58 @@ class Context:
 
     def batch(self) -> "Batch":
         return Batch(self)
+
+    # ---- deferred light passes and draw_higher (device images: torch tensors)
+
+    def light_directed(self, view: "OrthoView", light, normal, direction, intensity: float, color, add: bool):
+        d = np.asarray(direction, np.float32)
+        c = np.asarray(color, np.int32)
+        li, ni = image_struct(light), image_struct(normal)
+        _torch_sync()
+        self._check(self._l.dsrg_light_directed(self.handle, C.byref(view), C.byref(li), C.byref(ni), d.ctypes.data,
+                                                C.c_float(intensity), c.ctypes.data, 1 if add else 0))
+
+    def light_points(self, view: "OrthoView", center, light, normal, height, lights, reference_threads: int = 0):
+        """lights: dicts with position, radius, intensity, color and optionally cube (device tensor cubeWidth*6 x cubeWidth)."""
+        arr = (PointLight * max(1, len(lights)))()
+        for i, l in enumerate(lights):
+            for k in range(3):
+                arr[i].position[k] = float(l["position"][k])
+                arr[i].color[k] = int(l["color"][k])
+            arr[i].radius = float(l["radius"])
+            arr[i].intensity = float(l["intensity"])
+            cube = l.get("cube")
+            arr[i].shadowCube = _ptr(cube) if cube is not None else None
+            arr[i].cubeWidth = int(cube.shape[1]) if cube is not None else 0
+        li, ni, hi = image_struct(light), image_struct(normal), image_struct(height)
+        _torch_sync()
+        self._check(self._l.dsrg_light_points(self.handle, C.byref(view), int(center[0]), int(center[1]), C.byref(li),
+                                              C.byref(ni), C.byref(hi), arr, len(lights), reference_threads))
+
+    def light_blend(self, target, diffuse, light, pack_order: int = 0):
+        ti, di, li = image_struct(target, pack_order), image_struct(diffuse), image_struct(light)
+        _torch_sync()
+        self._check(self._l.dsrg_light_blend(self.handle, C.byref(ti), C.byref(di), C.byref(li)))
+
+    def draw_higher(self, target_height, target_a, target_b, sprites, a_pack: int = 0, b_pack: int = 0):
+        """sprites: dicts with height, color_a, color_b (device tensors), left, top, offset, a_pack, b_pack."""
+        arr = (Sprite * max(1, len(sprites)))()
+        for i, sp in enumerate(sprites):
+            h = sp["height"]
+            arr[i].height = _ptr(h)
+            arr[i].colorA = _ptr(sp["color_a"])
+            arr[i].colorB = _ptr(sp["color_b"])
+            arr[i].height_, arr[i].width = int(h.shape[0]), int(h.shape[1])
+            arr[i].heightStrideBytes = int(h.stride(0)) * 4
+            arr[i].colorAStrideBytes = int(sp["color_a"].stride(0)) * 4
+            arr[i].colorBStrideBytes = int(sp["color_b"].stride(0)) * 4
+            arr[i].colorAPackOrder = int(sp.get("a_pack", 0))
+            arr[i].colorBPackOrder = int(sp.get("b_pack", 0))
+            arr[i].left, arr[i].top = int(sp["left"]), int(sp["top"])
+            arr[i].offset = float(sp["offset"])
+        hi, ai, bi = image_struct(target_height), image_struct(target_a, a_pack), image_struct(target_b, b_pack)
+        _torch_sync()
+        self._check(self._l.dsrg_draw_higher(self.handle, C.byref(hi), C.byref(ai), C.byref(bi), arr, len(sprites)))
 
     def tuning(self) -> dict:
         t = Tuning()
@@ -406,6 +492,9 @@ class Batch:
         self.ctx._check(self.ctx._l.dsrg_batch_autotune(self.handle, rounds, C.byref(t)))
         return t.as_dict()
 
+    def set_depth_only(self, on: bool):
+        self.ctx._check(self.ctx._l.dsrg_batch_set_depth_only(self.handle, 1 if on else 0))
+
     def clear(self):
         self.ctx._check(self.ctx._l.dsrg_batch_clear(self.handle))
         self._keep = []
@@ -476,6 +565,24 @@ class Diff:
             self.destroy()
         except Exception:
             pass
+
+
+def ortho_view(camera_tilt: float, pixels_per_tile: int, index: int) -> OrthoView:
+    """OrthoSystem(cameraTilt, pixelsPerTile).view[index] (host computation, no GPU)."""
+    v = OrthoView()
+    status = lib().dsrg_ortho_view_create(camera_tilt, pixels_per_tile, index, C.byref(v))
+    if status != DSRG_OK:
+        raise DsrgError(status, "dsrg_ortho_view_create")
+    return v
+
+
+def shadow_side_location(normal_to_world, side: int) -> np.ndarray:
+    n = np.ascontiguousarray(normal_to_world, np.float32)
+    out = np.zeros(12, np.float32)
+    status = lib().dsrg_shadow_side_location(n.ctypes.data, side, out.ctypes.data)
+    if status != DSRG_OK:
+        raise DsrgError(status, "dsrg_shadow_side_location")
+    return out
 
 
 def render_scene(ctx: Context, scene, color: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None, *,

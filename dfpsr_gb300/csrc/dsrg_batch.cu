@@ -31,6 +31,7 @@ struct dsrg_batch_s {
 	std::unordered_map<dsrg_texture, int32_t> textureSlots;
 	DeviceBuffer<uint32_t> stagingColor; // frames whose images are in host memory
 	DeviceBuffer<float> stagingDepth;
+	bool depthOnly = false; // model_renderDepth semantics for every frame
 	BatchJob job;
 };
 
@@ -191,8 +192,15 @@ int dsrg_batch_render(dsrg_batch b) {
 	}
 	job.tasks.swap(b->tasks);
 	job.textures.swap(b->textures);
-	job.depthOnly = false;
+	job.depthOnly = b->depthOnly;
 	job.resolve = true;
+	if (b->depthOnly) {
+		// renderTriangleFromDataDepth (renderCore.cpp:400-443): 1 x 1 walk, no shading, no colour target
+		for (TaskParams &t : job.tasks) { t.depthOnly = 1; t.diffuse = -1; t.light = -1; }
+		for (FrameTarget &f : job.frames) f.color = nullptr;
+	} else {
+		for (TaskParams &t : job.tasks) t.depthOnly = 0;
+	}
 	BatchTotals totals;
 	const int status = batch_enqueue(ctx, job, totals);
 	job.tasks.swap(b->tasks);
@@ -212,6 +220,12 @@ int dsrg_batch_render(dsrg_batch b) {
 			                                     f.height, cudaMemcpyDeviceToHost, stream));
 	}
 	return batch_finish(ctx, totals);
+}
+
+int dsrg_batch_set_depth_only(dsrg_batch b, int32_t depthOnly) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	b->depthOnly = depthOnly != 0;
+	return DSRG_OK;
 }
 
 int dsrg_context_get_tuning(dsrg_context ctx, dsrg_tuning *out) {

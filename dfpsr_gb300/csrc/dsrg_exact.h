@@ -28,6 +28,13 @@ DSRG_HD float fadd(float a, float b) {
 	return a + b;
 #endif
 }
+DSRG_HD float fsub(float a, float b) {
+#if defined(__CUDA_ARCH__)
+	return __fsub_rn(a, b);
+#else
+	return a - b;
+#endif
+}
 DSRG_HD float fmul(float a, float b) {
 #if defined(__CUDA_ARCH__)
 	return __fmul_rn(a, b);

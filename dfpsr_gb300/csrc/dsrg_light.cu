@@ -1,0 +1,558 @@
+// Deferred light passes of the isometric sprite engine and draw_higher, on the GPU.
+//
+//   light_directed_kernel   setDirectedLight / addDirectedLight (SDK/SpriteEngine/lightAPI.cpp:23-74)
+//   light_points_kernel     addPointLight for many lights in one pass (lightAPI.cpp:76-285)
+//   light_blend_kernel      blendLight (lightAPI.cpp:287-323)
+//   higher_keys_kernel      draw_higher for many sprites: the winning (height, sprite) per pixel ...
+//   higher_resolve_kernel   ... and the copy of its height and colours (api/drawAPI.cpp:872-900)
+//
+// The reference's scalar build works on 4-lane float vectors (base/simd.h:4196-4207).  The point
+// light sweeps light space along each row with running sums: every lane starts at the band's first
+// row (F32xXx3::createGradient), adds the screen's y axis once per row and the x axis times four once
+// per 4-pixel step.  Each pixel here reproduces its own lane's sums with chain_add, so the values
+// are the reference's bit for bit.  Rows are cut into the bands of the reference's threadedSplit,
+// which restart the sweep.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "dsrg_internal.h"
+#include "dsrg_shade.h"
+
+using namespace dsrg;
+
+namespace {
+
+// ------------------------------------------------------------------ host: ortho views (host code is built with
+// -ffp-contract=off, so every expression below is the reference's sequence of binary32 operations)
+
+struct M3 { Vec3 x, y, z; };
+
+Vec3 v3(float x, float y, float z) { return vec3(x, y, z); }
+
+// normalize (math/FVector.h:113-119)
+Vec3 normalize_ref(Vec3 v) {
+	const float l = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+	if (l == 0.0f) return v3(0.0f, 0.0f, 1.0f);
+	return v3(v.x / l, v.y / l, v.z / l);
+}
+Vec3 cross_ref(Vec3 a, Vec3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+// FMatrix3x3::makeAxisSystem (math/FMatrix3x3.h:24-30)
+M3 axis_system(Vec3 forward, Vec3 up) {
+	M3 r;
+	const Vec3 f = normalize_ref(forward);
+	r.z = f;
+	r.x = normalize_ref(cross_ref(normalize_ref(up), f));
+	r.y = normalize_ref(cross_ref(f, r.x));
+	return r;
+}
+Vec3 transform_ref(const M3 &m, Vec3 p) { // FMatrix3x3.h:31-37
+	return v3(p.x * m.x.x + p.y * m.y.x + p.z * m.z.x, p.x * m.x.y + p.y * m.y.y + p.z * m.z.y, p.x * m.x.z + p.y * m.y.z + p.z * m.z.z);
+}
+Vec3 transform_transposed_ref(const M3 &m, Vec3 p) { // FMatrix3x3.h:38-44
+	return v3(p.x * m.x.x + p.y * m.x.y + p.z * m.x.z, p.x * m.y.x + p.y * m.y.y + p.z * m.y.z, p.x * m.z.x + p.y * m.z.y + p.z * m.z.z);
+}
+M3 inverse_ref(const M3 &m) { // FMatrix3x3.h:54-80
+	const float det = m.x.x * m.y.y * m.z.z + m.z.x * m.x.y * m.y.z + m.y.x * m.z.y * m.x.z - m.x.x * m.z.y * m.y.z -
+	                  m.y.x * m.x.y * m.z.z - m.z.x * m.y.y * m.x.z;
+	const float invDet = 1.0f / det;
+	M3 r;
+	r.x.x = invDet * (m.y.y * m.z.z - m.y.z * m.z.y);
+	r.x.y = -invDet * (m.x.y * m.z.z - m.x.z * m.z.y);
+	r.x.z = invDet * (m.x.y * m.y.z - m.x.z * m.y.y);
+	r.y.x = -invDet * (m.y.x * m.z.z - m.y.z * m.z.x);
+	r.y.y = invDet * (m.x.x * m.z.z - m.x.z * m.z.x);
+	r.y.z = -invDet * (m.x.x * m.y.z - m.x.z * m.y.x);
+	r.z.x = invDet * (m.y.x * m.z.y - m.y.y * m.z.x);
+	r.z.y = -invDet * (m.x.x * m.z.y - m.x.y * m.z.x);
+	r.z.z = invDet * (m.x.x * m.y.y - m.x.y * m.y.x);
+	return r;
+}
+void store_m3(const M3 &m, float *out) {
+	const float v[9] = {m.x.x, m.x.y, m.x.z, m.y.x, m.y.y, m.y.z, m.z.x, m.z.y, m.z.z};
+	memcpy(out, v, sizeof(v));
+}
+M3 load_m3(const float *in) {
+	M3 m;
+	m.x = v3(in[0], in[1], in[2]);
+	m.y = v3(in[3], in[4], in[5]);
+	m.z = v3(in[6], in[7], in[8]);
+	return m;
+}
+
+// ------------------------------------------------------------------ device
+
+// truncated, clamped channels packed as the reference's packOrder_packBytes(r, g, b) (alpha 0)
+__device__ __forceinline__ uint32_t light_channel(float v) { return trunc_u32((255.1f < v) ? 255.1f : v); }
+
+__device__ __forceinline__ float vmin_ref(float left, float right) { return (right < left) ? right : left; } // simd.h:2198-2216
+__device__ __forceinline__ float vmax_ref(float left, float right) { return (right > left) ? right : left; } // simd.h:2217-2235
+
+__device__ __forceinline__ uint32_t sat_add_bytes(uint32_t a, uint32_t b) { // saturatedAddition (simd.h:2670-2690)
+	uint32_t out = 0;
+	for (int i = 0; i < 4; i++) {
+		const uint32_t s = ((a >> (8 * i)) & 0xFFu) + ((b >> (8 * i)) & 0xFFu);
+		out |= (s > 255u ? 255u : s) << (8 * i);
+	}
+	return out;
+}
+
+struct DirectedParams {
+	float rev[3]; // -normalize(N^T dir) * intensity * 2
+	float color[3];
+	int32_t add;
+};
+
+__global__ void light_directed_kernel(uint32_t *light, int32_t lightStride, const uint32_t *__restrict__ normal, int32_t normalStride,
+                                      int32_t width, int32_t height, DirectedParams p) {
+	const int32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+	if (x >= width || y >= height) return;
+	const uint32_t c = normal[(size_t)y * normalStride + x];
+	const float nx = fadd((float)(c & 0xFFu), -128.0f), ny = fadd((float)((c >> 8) & 0xFFu), -128.0f);
+	const float nz = fadd((float)((c >> 16) & 0xFFu), -128.0f);
+	const float dot = fadd(fadd(fmul(nx, p.rev[0]), fmul(ny, p.rev[1])), fmul(nz, p.rev[2]));
+	const float i = vmax_ref(0.0f, dot);
+	const uint32_t bytes = light_channel(fmul(i, p.color[0])) | (light_channel(fmul(i, p.color[1])) << 8) |
+	                       (light_channel(fmul(i, p.color[2])) << 16);
+	uint32_t *q = light + (size_t)y * lightStride + x;
+	*q = p.add ? sat_add_bytes(*q, bytes) : bytes;
+}
+
+// One point light, as prepared on the host (calculateBound and the uniforms of addPointLightSuper).
+struct PointLightParams {
+	int32_t left, top, right, bottom; // bound, left and right aligned to 4 pixels
+	int32_t jobs;                     // threadedSplit bands of the bound's rows
+	float source[3];                  // light-space position
+	float color[3];
+	float reciprocalRadius;
+	const float *cube;                // shadow cube map or null
+	int32_t cubeWidth;
+	float cubeCenter;
+};
+
+struct PointFrame {
+	float toLight[9];     // screenDepthToLightSpace (x, y, z axes)
+	int32_t centerX, centerY;
+	int32_t lightCount;
+	const PointLightParams *lights;
+};
+
+// getShadowTransparency (lightAPI.cpp:104-138)
+__device__ __forceinline__ float shadow_transparency(const float *cube, int32_t width, float halfWidth, float ox, float oy, float oz) {
+	const float absX = ox < 0.0f ? -ox : ox, absY = oy < 0.0f ? -oy : oy, absZ = oz < 0.0f ? -oz : oz;
+	const bool xIsLongest = absX > absY && absX > absZ;
+	const bool yIsLongerThanZ = absY > absZ;
+	float depth = xIsLongest ? ox : (yIsLongerThanZ ? oy : oz);
+	const float slopeUp = (yIsLongerThanZ && !xIsLongest) ? oz : oy;
+	float slopeSide = xIsLongest ? -oz : (yIsLongerThanZ ? -ox : ox);
+	int32_t viewOffset = width * (xIsLongest ? 0 : (yIsLongerThanZ ? 2 : 4));
+	if (depth < 0.0f) {
+		depth = -depth;
+		slopeSide = -slopeSide;
+		viewOffset += width;
+	}
+	const float reciDepth = fdiv(1.0f, depth);
+	const float scale = fmul(halfWidth, reciDepth);
+	int32_t sampleX = (int32_t)fadd(halfWidth, fmul(slopeSide, scale));
+	int32_t sampleY = (int32_t)fsub(halfWidth, fmul(slopeUp, scale));
+	const int32_t maxPixel = width - 1;
+	sampleX = sampleX < 0 ? 0 : (sampleX > maxPixel ? maxPixel : sampleX);
+	sampleY = sampleY < 0 ? 0 : (sampleY > maxPixel ? maxPixel : sampleY);
+	const float shadowReciDepth = __ldg(&cube[(size_t)(sampleY + viewOffset) * width + sampleX]);
+	return fmul(reciDepth, 1.02f) > shadowReciDepth ? 1.0f : 0.0f;
+}
+
+// One thread per pixel of the light image: the bytes of every light whose bound holds the pixel
+// are summed and added to the pixel with saturation (equal to the reference's saturated additions
+// light after light, because every added byte is non-negative).
+__global__ void __launch_bounds__(256) light_points_kernel(uint32_t *light, int32_t lightStride, const uint32_t *__restrict__ normal,
+                                                           int32_t normalStride, const float *__restrict__ heightImage,
+                                                           int32_t heightStride, int32_t width, int32_t height, PointFrame f) {
+	const int32_t x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+	if (x >= width || y >= height) return;
+	uint32_t sum[3] = {0u, 0u, 0u};
+	bool any = false;
+	const float depthOffset = heightImage[(size_t)y * heightStride + x];
+	const uint32_t nc = normal[(size_t)y * normalStride + x];
+	const float negN[3] = {fmul(fadd((float)(nc & 0xFFu), -128.0f), -0.0078125f),
+	                       fmul(fadd((float)((nc >> 8) & 0xFFu), -128.0f), -0.0078125f),
+	                       fmul(fadd((float)((nc >> 16) & 0xFFu), -128.0f), -0.0078125f)};
+	const float *m = f.toLight;
+	for (int32_t k = 0; k < f.lightCount; k++) {
+		const PointLightParams &p = f.lights[k];
+		if (x < p.left || x >= p.right || y < p.top || y >= p.bottom) continue;
+		// the band holding this row (splitStartIndex, base/threading.cpp:209-221)
+		const int32_t rows = p.bottom - p.top;
+		int32_t bandTop = p.top;
+		for (int32_t j = 1; j < p.jobs; j++) {
+			const int32_t start = (j * rows) / p.jobs + p.top;
+			if (start <= y) bandTop = start;
+		}
+		// lightBaseRow = screenDepthToLightSpace.transform((0.5 - cx + left, 0.5 - cy + bandTop, 0)) - source
+		const float px = fadd(fsub(0.5f, (float)f.centerX), (float)p.left);
+		const float py = fadd(fsub(0.5f, (float)f.centerY), (float)bandTop);
+		const int32_t lane = (x - p.left) & 3, steps = (x - p.left) >> 2;
+		const int32_t rowSteps = y - bandTop;
+		float o[3];
+		for (int c = 0; c < 3; c++) {
+			const float base = fsub(fadd(fadd(fmul(px, m[c]), fmul(py, m[3 + c])), fmul(0.0f, m[6 + c])), p.source[c]);
+			const float dx = m[c], dy = m[3 + c];
+			// F32x4::createGradient (base/simd.h:474-476)
+			const float start = lane == 0 ? base : fadd(base, lane == 1 ? dx : fmul(dx, (float)lane));
+			const float row = chain_add(start, dy, rowSteps);
+			const float value = chain_add(row, fmul(dx, 4.0f), steps);
+			o[c] = fadd(value, fmul(m[6 + c], depthOffset));
+		}
+		const float squareLength = fadd(fadd(fmul(o[0], o[0]), fmul(o[1], o[1])), fmul(o[2], o[2]));
+		// squareRoot and reciprocalSquareRoot of the scalar build go through the double overload of sqrt
+		const float length = __double2float_rn(__dsqrt_rn((double)squareLength));
+		const float ratio = vmin_ref(1.0f, fmul(length, p.reciprocalRadius));
+		const float distanceIntensity = fadd(fsub(1.0f, fmul(2.0f, ratio)), fmul(ratio, ratio));
+		const float rs = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)squareLength)));
+		const float angle = vmax_ref(0.0f, fadd(fadd(fmul(fmul(o[0], rs), negN[0]), fmul(fmul(o[1], rs), negN[1])),
+		                                        fmul(fmul(o[2], rs), negN[2])));
+		float intensity = fmul(angle, distanceIntensity);
+		if (p.cube) intensity = fmul(intensity, shadow_transparency(p.cube, p.cubeWidth, p.cubeCenter, o[0], o[1], o[2]));
+		for (int c = 0; c < 3; c++) sum[c] += light_channel(fmul(intensity, p.color[c]));
+		any = true;
+	}
+	if (!any) return;
+	uint32_t *q = light + (size_t)y * lightStride + x;
+	uint32_t v = *q;
+	for (int c = 0; c < 3; c++) {
+		const uint32_t s = ((v >> (8 * c)) & 0xFFu) + sum[c];
+		v = (v & ~(0xFFu << (8 * c))) | ((s > 255u ? 255u : s) << (8 * c));
+	}
+	*q = v;
+}
+
+__global__ void light_blend_kernel(uint32_t *target, int32_t targetStride, int32_t packOrder, const uint32_t *__restrict__ diffuse,
+                                   int32_t diffuseStride, const uint32_t *__restrict__ light, int32_t lightStride, int32_t width,
+                                   int32_t height) {
+	const int32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+	if (x >= width || y >= height) return;
+	const uint32_t d = diffuse[(size_t)y * diffuseStride + x], l = light[(size_t)y * lightStride + x];
+	uint32_t out = 0;
+	for (int c = 0; c < 3; c++) {
+		const float v = fmul(fmul((float)((d >> (8 * c)) & 0xFFu), (float)((l >> (8 * c)) & 0xFFu)), 0.0078125f);
+		out |= light_channel(v) << pack_shift(packOrder, c);
+	}
+	target[(size_t)y * targetStride + x] = out;
+}
+
+struct SpriteData {
+	const float *height;
+	const uint32_t *colorA, *colorB;
+	int32_t width, height_;
+	int32_t heightStride, aStride, bStride; // in elements
+	int32_t aPack, bPack;
+	int32_t left, top;
+	float offset;
+};
+
+__device__ __forceinline__ uint32_t ordered_height(float h) {
+	uint32_t bits = fbits(h);
+	if (bits == 0x80000000u) bits = 0u; // -0 equals +0
+	return (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
+}
+
+// Every source pixel raised above the initial target height bids (height, ~sprite) for its pixel.
+__global__ void higher_keys_kernel(const SpriteData *__restrict__ sprites, int32_t first, int32_t count,
+                                   const float *__restrict__ targetHeight, int32_t thStride, int32_t width, int32_t height,
+                                   unsigned long long *keys) {
+	const int32_t s = first + (int32_t)blockIdx.y;
+	if (s >= count) return;
+	const SpriteData sp = sprites[s];
+	const int32_t pixels = sp.width * sp.height_;
+	for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
+		const int32_t sx = i % sp.width, sy = i / sp.width;
+		const int32_t x = sp.left + sx, y = sp.top + sy;
+		if (x < 0 || y < 0 || x >= width || y >= height) continue;
+		float h = sp.height[(size_t)sy * sp.heightStride + sx];
+		if (!(h > -INFINITY)) continue;
+		h = fadd(h, sp.offset);
+		if (!(h > targetHeight[(size_t)y * thStride + x])) continue;
+		const unsigned long long key = ((unsigned long long)ordered_height(h) << 32) | (unsigned long long)(~(uint32_t)s);
+		atomicMax(&keys[(size_t)y * width + x], key);
+	}
+}
+
+// Byte index of red, green, blue, alpha in memory for a PackOrderIndex (image/PackOrder.h:61-92).
+__device__ __forceinline__ int pack_index(int32_t order, int channel) {
+	const int table[4][4] = {{0, 1, 2, 3}, {2, 1, 0, 3}, {1, 2, 3, 0}, {3, 2, 1, 0}};
+	return table[order & 3][channel];
+}
+
+__device__ __forceinline__ uint32_t reorder(uint32_t source, int32_t from, int32_t to) {
+	uint32_t out = 0;
+	for (int c = 0; c < 4; c++) out |= ((source >> (8 * pack_index(from, c))) & 0xFFu) << (8 * pack_index(to, c));
+	return out;
+}
+
+__global__ void higher_resolve_kernel(const SpriteData *__restrict__ sprites, const unsigned long long *__restrict__ keys,
+                                      float *targetHeight, int32_t thStride, uint32_t *targetA, int32_t taStride, int32_t taPack,
+                                      uint32_t *targetB, int32_t tbStride, int32_t tbPack, int32_t width, int32_t height) {
+	const int32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+	if (x >= width || y >= height) return;
+	const unsigned long long key = keys[(size_t)y * width + x];
+	if (key == 0ull) return;
+	const SpriteData sp = sprites[~(uint32_t)(key & 0xFFFFFFFFull)];
+	const int32_t sx = x - sp.left, sy = y - sp.top;
+	targetHeight[(size_t)y * thStride + x] = fadd(sp.height[(size_t)sy * sp.heightStride + sx], sp.offset);
+	targetA[(size_t)y * taStride + x] = reorder(sp.colorA[(size_t)sy * sp.aStride + sx], sp.aPack, taPack);
+	targetB[(size_t)y * tbStride + x] = reorder(sp.colorB[(size_t)sy * sp.bStride + sx], sp.bPack, tbPack);
+}
+
+bool device_image(const dsrg_image *img) {
+	return img && img->data && img->onDevice && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 &&
+	       img->strideBytes % 4 == 0;
+}
+
+int32_t hardware_threads() {
+	const unsigned n = std::thread::hardware_concurrency();
+	return n > 0 ? (int32_t)n : 1;
+}
+
+} // namespace
+
+extern "C" {
+
+int dsrg_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, dsrg_ortho_view *out) {
+	if (!out || index < 0 || index > 7 || pixelsPerTile < 1) return DSRG_ERROR_INVALID_ARGUMENT;
+	const float diag = 0.707106781f;
+	// the reference's unqualified sqrt of a float argument resolves to the double overload
+	const int32_t yPixelsPerTile = (int32_t)((double)(float)pixelsPerTile / sqrt((double)(cameraTilt * cameraTilt + 1)));
+	const Vec3 forward[8] = {v3(diag, cameraTilt, diag), v3(-diag, cameraTilt, diag), v3(-diag, cameraTilt, -diag),
+	                         v3(diag, cameraTilt, -diag), v3(0.0f, cameraTilt, 1.0f), v3(-1.0f, cameraTilt, 0.0f),
+	                         v3(0.0f, cameraTilt, -1.0f), v3(1.0f, cameraTilt, 0.0f)};
+	const M3 system = axis_system(forward[index], v3(0.0f, 1.0f, 0.0f));
+	Vec3 normalDirection = system.z;
+	normalDirection.y = 0.0f;
+	const M3 normalToWorld = axis_system(normalDirection, v3(0.0f, 1.0f, 0.0f));
+	// Camera::createOrthogonal(Transform3D(origin, system), ppt, ppt, 0.5) and worldToScreen of the x and z axes
+	dsrg_camera cam;
+	memset(&cam, 0, sizeof(cam));
+	const float loc[12] = {0.0f, 0.0f, 0.0f, system.x.x, system.x.y, system.x.z, system.y.x, system.y.y, system.y.z,
+	                       system.z.x, system.z.y, system.z.z};
+	memcpy(cam.location, loc, sizeof(loc));
+	cam.perspective = 0;
+	cam.slope = 0.5f;
+	cam.width = pixelsPerTile;
+	cam.height = pixelsPerTile;
+	const CameraData c = make_camera(cam);
+	const float halfTile = (float)pixelsPerTile * 0.5f;
+	const Projected px = camera_to_screen(c, world_to_camera(c, v3(1.0f, 0.0f, 0.0f)));
+	const Projected pz = camera_to_screen(c, world_to_camera(c, v3(0.0f, 0.0f, 1.0f)));
+	const int32_t xAxis[2] = {(int32_t)(px.isx - halfTile), (int32_t)(px.isy - halfTile)};
+	const int32_t zAxis[2] = {(int32_t)(pz.isx - halfTile), (int32_t)(pz.isy - halfTile)};
+	// OrthoView::OrthoView (orthoAPI.cpp:6-37)
+	M3 tileToScreen;
+	tileToScreen.x = v3((float)xAxis[0], (float)xAxis[1], 0.0f);
+	tileToScreen.y = v3(0.0f, (float)(-yPixelsPerTile), 1.0f);
+	tileToScreen.z = v3((float)zAxis[0], (float)zAxis[1], 0.0f);
+	const M3 screenToTile = inverse_ref(tileToScreen);
+	M3 toLight;
+	toLight.x = transform_transposed_ref(normalToWorld, screenToTile.x);
+	toLight.y = transform_transposed_ref(normalToWorld, screenToTile.y);
+	toLight.z = transform_transposed_ref(normalToWorld, screenToTile.z);
+	const M3 fromLight = inverse_ref(toLight);
+	store_m3(normalToWorld, out->normalToWorld);
+	store_m3(toLight, out->screenDepthToLightSpace);
+	store_m3(fromLight, out->lightSpaceToScreenDepth);
+	out->pixelOffsetPerTileX[0] = xAxis[0]; out->pixelOffsetPerTileX[1] = xAxis[1];
+	out->pixelOffsetPerTileZ[0] = zAxis[0]; out->pixelOffsetPerTileZ[1] = zAxis[1];
+	out->yPixelsPerTile = yPixelsPerTile;
+	return DSRG_OK;
+}
+
+int dsrg_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]) {
+	if (!normalToWorld || !location || side < 0 || side > 5) return DSRG_ERROR_INVALID_ARGUMENT;
+	const Vec3 forward[6] = {v3(1.0f, 0.0f, 0.0f), v3(-1.0f, 0.0f, 0.0f), v3(0.0f, 1.0f, 0.0f),
+	                         v3(0.0f, -1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f), v3(0.0f, 0.0f, -1.0f)};
+	const Vec3 up[6] = {v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f),
+	                    v3(0.0f, 0.0f, 1.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f)};
+	const M3 s = axis_system(forward[side], up[side]);
+	const M3 n = load_m3(normalToWorld);
+	M3 r; // FMatrix3x3 product (FMatrix3x3.h:50-52)
+	r.x = transform_ref(n, s.x);
+	r.y = transform_ref(n, s.y);
+	r.z = transform_ref(n, s.z);
+	location[0] = 0.0f; location[1] = 0.0f; location[2] = 0.0f;
+	store_m3(r, location + 3);
+	return DSRG_OK;
+}
+
+int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
+                        const float direction[3], float intensity, const int32_t color[3], int32_t add) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!view || !direction || !color) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: null argument");
+	if (!device_image(light) || !device_image(normal) || light->width != normal->width || light->height != normal->height)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: light and normal must be device images of one size");
+	cudaSetDevice(ctx->device);
+	const M3 n = load_m3(view->normalToWorld);
+	const Vec3 d = normalize_ref(transform_transposed_ref(n, v3(direction[0], direction[1], direction[2])));
+	DirectedParams p;
+	p.rev[0] = -d.x * intensity * 2.0f;
+	p.rev[1] = -d.y * intensity * 2.0f;
+	p.rev[2] = -d.z * intensity * 2.0f;
+	for (int c = 0; c < 3; c++) {
+		const float v = (float)color[c] / 255.0f;
+		p.color[c] = 0.0f > v ? 0.0f : v;
+	}
+	p.add = add ? 1 : 0;
+	const dim3 grid((light->width + 255) / 256, light->height);
+	light_directed_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)light->data, light->strideBytes / 4, (const uint32_t *)normal->data,
+	                                                     normal->strideBytes / 4, light->width, light->height, p);
+	add_launches(1);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return DSRG_OK;
+}
+
+int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY, const dsrg_image *light,
+                      const dsrg_image *normal, const dsrg_image *height, const dsrg_point_light *lights, int32_t count,
+                      int32_t referenceThreads) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!view || (count > 0 && !lights) || count < 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: null argument");
+	if (!device_image(light) || !device_image(normal) || !device_image(height) || light->width != normal->width ||
+	    light->height != normal->height || light->width != height->width || light->height != height->height)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: light, normal and height must be device images of one size");
+	cudaSetDevice(ctx->device);
+	const int32_t width = light->width, imageHeight = light->height;
+	const int32_t threads = referenceThreads > 0 ? referenceThreads : hardware_threads();
+	const M3 n = load_m3(view->normalToWorld), fromLight = load_m3(view->lightSpaceToScreenDepth);
+	std::vector<PointLightParams> params;
+	for (int32_t k = 0; k < count; k++) {
+		const dsrg_point_light &l = lights[k];
+		if (l.shadowCube && l.cubeWidth < 1) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: shadow cube without a width");
+		// calculateBound (lightAPI.cpp:76-102)
+		const Vec3 source = transform_transposed_ref(n, v3(l.position[0], l.position[1], l.position[2]));
+		const Vec3 rotated = transform_ref(fromLight, source);
+		const int32_t pcx = (int32_t)rotated.x + centerX, pcy = (int32_t)rotated.y + centerY;
+		const int32_t pixelRadius = (int32_t)(l.radius * fromLight.x.x);
+		if (pcx < -pixelRadius || pcx > width + pixelRadius || pcy < -pixelRadius || pcy > imageHeight + pixelRadius) continue;
+		const int32_t side = (int32_t)((float)pixelRadius * 2.0f);
+		const int32_t bl = pcx - pixelRadius, bt = pcy - pixelRadius, br = bl + side, bb = bt + side;
+		if (!(0 < br && width > bl && 0 < bb && imageHeight > bt)) continue; // IRect::overlaps (IRect.h:77-79)
+		const int32_t left = bl > 0 ? bl : 0, top = bt > 0 ? bt : 0;
+		const int32_t right = br < width ? br : width, bottom = bb < imageHeight ? bb : imageHeight;
+		if (right - left <= 0 || bottom - top <= 0) continue;
+		PointLightParams p;
+		p.left = left - (left % 4);                  // roundDown(left, 4) for left >= 0
+		p.right = right + 3 - ((right - 1) % 4);     // roundUp(right, 4) for right >= 1
+		p.top = top;
+		p.bottom = bottom;
+		const int32_t rows = bottom - top;
+		int32_t jobs = threads * 2; // getJobCount (base/threading.cpp:193-206) with 128 rows per job, 2 jobs per thread
+		if (jobs > rows / 128) jobs = rows / 128;
+		if (jobs < 1) jobs = 1;
+		p.jobs = jobs;
+		p.source[0] = source.x; p.source[1] = source.y; p.source[2] = source.z;
+		for (int c = 0; c < 3; c++) {
+			const float v = (float)l.color[c] * l.intensity;
+			p.color[c] = 0.0f > v ? 0.0f : v;
+		}
+		p.reciprocalRadius = 1.0f / l.radius;
+		p.cube = l.shadowCube;
+		p.cubeWidth = l.cubeWidth;
+		p.cubeCenter = (float)l.cubeWidth * 0.5f;
+		params.push_back(p);
+	}
+	if (params.empty()) return DSRG_OK;
+	// the light table travels in the context's table buffer
+	const size_t bytes = params.size() * sizeof(PointLightParams);
+	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(bytes));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, params.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+	PointFrame f;
+	memcpy(f.toLight, view->screenDepthToLightSpace, sizeof(f.toLight));
+	f.centerX = centerX;
+	f.centerY = centerY;
+	f.lightCount = (int32_t)params.size();
+	f.lights = reinterpret_cast<const PointLightParams *>(ctx->tables.ptr);
+	const dim3 grid((width + 15) / 16, (imageHeight + 15) / 16);
+	light_points_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)light->data, light->strideBytes / 4, (const uint32_t *)normal->data,
+	                                                   normal->strideBytes / 4, (const float *)height->data, height->strideBytes / 4,
+	                                                   width, imageHeight, f);
+	add_launches(1);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return DSRG_OK;
+}
+
+int dsrg_light_blend(dsrg_context ctx, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!device_image(target) || !device_image(diffuse) || !device_image(light) || target->width != diffuse->width ||
+	    target->height != diffuse->height || target->width != light->width || target->height != light->height ||
+	    target->packOrder < 0 || target->packOrder > 3)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_blend: target, diffuse and light must be device images of one size");
+	cudaSetDevice(ctx->device);
+	const dim3 grid((target->width + 255) / 256, target->height);
+	light_blend_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)target->data, target->strideBytes / 4, target->packOrder,
+	                                                  (const uint32_t *)diffuse->data, diffuse->strideBytes / 4,
+	                                                  (const uint32_t *)light->data, light->strideBytes / 4, target->width,
+	                                                  target->height);
+	add_launches(1);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return DSRG_OK;
+}
+
+int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsrg_image *targetA, const dsrg_image *targetB,
+                     const dsrg_sprite *sprites, int32_t count) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (count < 0 || (count > 0 && !sprites)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: null sprites");
+	if (!device_image(targetHeight) || !device_image(targetA) || !device_image(targetB) || targetHeight->width != targetA->width ||
+	    targetHeight->height != targetA->height || targetHeight->width != targetB->width || targetHeight->height != targetB->height ||
+	    targetA->packOrder < 0 || targetA->packOrder > 3 || targetB->packOrder < 0 || targetB->packOrder > 3)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: targets must be device images of one size");
+	cudaSetDevice(ctx->device);
+	if (count == 0) return DSRG_OK;
+	std::vector<SpriteData> table(count);
+	int32_t largest = 1;
+	for (int32_t i = 0; i < count; i++) {
+		const dsrg_sprite &s = sprites[i];
+		if (!s.height || !s.colorA || !s.colorB || s.width < 0 || s.height_ < 0 || s.heightStrideBytes < s.width * 4 ||
+		    s.colorAStrideBytes < s.width * 4 || s.colorBStrideBytes < s.width * 4 || s.heightStrideBytes % 4 ||
+		    s.colorAStrideBytes % 4 || s.colorBStrideBytes % 4 || s.colorAPackOrder < 0 || s.colorAPackOrder > 3 ||
+		    s.colorBPackOrder < 0 || s.colorBPackOrder > 3)
+			return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: invalid sprite " + std::to_string(i));
+		SpriteData &d = table[i];
+		d.height = s.height; d.colorA = s.colorA; d.colorB = s.colorB;
+		d.width = s.width; d.height_ = s.height_;
+		d.heightStride = s.heightStrideBytes / 4; d.aStride = s.colorAStrideBytes / 4; d.bStride = s.colorBStrideBytes / 4;
+		d.aPack = s.colorAPackOrder; d.bPack = s.colorBPackOrder;
+		d.left = s.left; d.top = s.top; d.offset = s.offset;
+		if (s.width * s.height_ > largest) largest = s.width * s.height_;
+	}
+	const int32_t width = targetHeight->width, height = targetHeight->height;
+	const size_t pixels = (size_t)width * height;
+	DSRG_CUDA_TRY(ctx, ctx->keys.reserve(pixels));
+	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(sizeof(SpriteData) * table.size()));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, table.data(), sizeof(SpriteData) * table.size(), cudaMemcpyHostToDevice, ctx->stream));
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
+	const SpriteData *deviceTable = reinterpret_cast<const SpriteData *>(ctx->tables.ptr);
+	const int32_t blocksPerSprite = (largest + 255) / 256 < 64 ? (largest + 255) / 256 : 64;
+	for (int32_t first = 0; first < count; first += 65535) { // grid y is limited to 65535 sprites per launch
+		const int32_t n = count - first < 65535 ? count - first : 65535;
+		higher_keys_kernel<<<dim3(blocksPerSprite, n), 256, 0, ctx->stream>>>(deviceTable, first, count, (const float *)targetHeight->data,
+		                                                                     targetHeight->strideBytes / 4, width, height, ctx->keys.ptr);
+		add_launches(1);
+	}
+	const dim3 grid((width + 255) / 256, height);
+	higher_resolve_kernel<<<grid, 256, 0, ctx->stream>>>(deviceTable, ctx->keys.ptr, (float *)targetHeight->data,
+	                                                     targetHeight->strideBytes / 4, (uint32_t *)targetA->data,
+	                                                     targetA->strideBytes / 4, targetA->packOrder, (uint32_t *)targetB->data,
+	                                                     targetB->strideBytes / 4, targetB->packOrder, width, height);
+	add_launches(1);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return DSRG_OK;
+}
+
+} // extern "C"

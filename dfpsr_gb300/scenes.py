@@ -284,3 +284,98 @@ def diff_problem(seed: int = 99, views: int = 64, size: int = 256, texture_size:
     t_vcol = (vcol + rng.normal(0.0, sigma, size=vcol.shape)).astype(np.float32)
     t_light = (light + rng.normal(0.0, sigma, size=4)).astype(np.float32)
     return DiffProblem(mesh, cams, size, size, tex, vcol, light, 0.3, t_tex, t_vcol, t_light)
+
+
+@dataclasses.dataclass
+class LightScene:
+    """The isometric deferred-light workload: sprite images drawn with draw_higher, point lights with
+    shadow cube maps rendered from a caster model, a directed light and blendLight."""
+    width: int
+    height: int
+    camera_tilt: float
+    pixels_per_tile: int
+    view_index: int
+    center: tuple                  # worldCenter in pixels
+    sprite_heights: list           # (s, s) float32 per sprite type
+    sprite_diffuse: list           # (s, s) uint32 RGBA per sprite type
+    sprite_normals: list           # (s, s) uint32 RGBA per sprite type
+    placements: np.ndarray         # (n, 4): type, left, top, and the height offset's bits (float32 viewed as int32)
+    lights: list                   # dicts: position, radius, intensity, color
+    sun_direction: tuple
+    sun_intensity: float
+    sun_color: tuple
+    caster: Scene                  # shadow caster model (positions in tiles, relative to the camera)
+    cube_resolution: int
+
+
+def _sprite_type(rng, size):
+    yy, xx = np.mgrid[0:size, 0:size].astype(np.float64)
+    c = (size - 1) / 2.0
+    r = np.sqrt((xx - c) ** 2 + (yy - c) ** 2) / (size / 2.0)
+    dome = np.clip(1.0 - r * r, 0.0, None)
+    height = (dome * rng.uniform(1.0, 3.0) + rng.uniform(0.0, 0.15, size=(size, size)) * (dome > 0)).astype(np.float32)
+    height[r > 1.0] = -np.inf  # transparent corners
+    gy, gx = np.gradient(np.where(r <= 1.0, height.astype(np.float64), 0.0))
+    n = np.stack([-gx, -gy, np.ones_like(gx)], axis=-1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    nb = np.clip(n * 127.0 + 128.0, 0, 255).astype(np.uint32)
+    normal = nb[..., 0] | (nb[..., 1] << 8) | (nb[..., 2] << 16) | (np.uint32(255) << 24)
+    diffuse = rng.integers(0, 2**32, size=(size, size), dtype=np.uint64).astype(np.uint32) | np.uint32(0xFF000000)
+    return height, diffuse, normal.astype(np.uint32)
+
+
+def light_scene(seed: int = 2024, width: int = 1920, height: int = 1080, sprites: int = 4096, sprite_size: int = 64,
+                sprite_types: int = 32, lights: int = 16, radius_px=(100, 400), caster_triangles: int = 2000,
+                cube_resolution: int = 512, camera_tilt: float = -0.7, pixels_per_tile: int = 64, view_index: int = 0,
+                light_space=None) -> LightScene:
+    """Sprites on a grid covering the image (seeded noise images with domed heights), point lights at
+    seeded pixel positions with radii uniform in radius_px, and a caster model of small random
+    triangles around the lights.  light_space = (screenDepthToLightSpace, normalToWorld) as 3x3 axes
+    (row per axis) places the lights; the library's ortho_view provides them."""
+    rng = np.random.default_rng(seed)
+    types = [_sprite_type(rng, sprite_size) for _ in range(sprite_types)]
+    cols = int(math.ceil(math.sqrt(sprites * width / height)))
+    rows = int(math.ceil(sprites / cols))
+    place = np.zeros((sprites, 4), np.int32)
+    for k in range(sprites):
+        i, j = k % cols, k // cols
+        left = int(round(i * (width + sprite_size) / cols)) - sprite_size // 2 + int(rng.integers(-4, 5))
+        top = int(round(j * (height + sprite_size) / rows)) - sprite_size // 2 + int(rng.integers(-4, 5))
+        offset = np.float32(j * 0.02 + rng.uniform(0.0, 0.5))
+        place[k] = (int(rng.integers(0, sprite_types)), left, top, np.array([offset], np.float32).view(np.int32)[0])
+    center = (width // 2, height // 2)
+    light_list = []
+    if light_space is not None:
+        to_light, normal_to_world = (np.asarray(m, np.float64).reshape(3, 3) for m in light_space)
+        for _ in range(lights):
+            px, py = rng.uniform(0, width), rng.uniform(0, height)
+            h = rng.uniform(1.0, 3.0)
+            screen = np.array([px - center[0], py - center[1], h])
+            ls = screen[0] * to_light[0] + screen[1] * to_light[1] + screen[2] * to_light[2]
+            pos = ls[0] * normal_to_world[0] + ls[1] * normal_to_world[1] + ls[2] * normal_to_world[2]
+            scale = np.linalg.norm(to_light[0])  # tiles per pixel along the screen's x axis
+            radius = float(rng.uniform(*radius_px) * scale)
+            color = tuple(int(c) for c in rng.integers(128, 256, size=3))
+            light_list.append({"position": tuple(float(v) for v in pos), "radius": radius,
+                               "intensity": float(rng.uniform(0.6, 1.2)), "color": color})
+    # casters: small triangles scattered around the lights (tile units, relative to the camera)
+    anchors = np.array([l["position"] for l in light_list]) if light_list else np.zeros((1, 3))
+    a = anchors[rng.integers(0, len(anchors), size=caster_triangles)]
+    centers = a + rng.normal(0.0, 1.5, size=(caster_triangles, 3))
+    corners = centers[:, None, :] + rng.normal(0.0, 0.35, size=(caster_triangles, 3, 3))
+    positions = corners.reshape(-1, 3).astype(np.float32)
+    idx = np.arange(caster_triangles * 3, dtype=np.int32).reshape(-1, 3)
+    poly = np.concatenate([idx, -np.ones((caster_triangles, 1), np.int32)], axis=1)
+    zeros = np.zeros((caster_triangles, 4, 4), np.float32)
+    caster = Scene(cube_resolution, cube_resolution, positions, poly, zeros, np.ones_like(zeros), None, 1, None, 1, 0,
+                   camera_location((0.0, 0.0, 0.0), (0.0, 0.0, 1.0)), True, 1.0, 0.01, 1000.0, IDENTITY.copy())
+    # the sun shines down and away from the camera in light space, so that flat sprite pixels are lit
+    sun_light_space = np.array([rng.uniform(-0.4, 0.4), -0.6, -0.75])
+    if light_space is not None:
+        n = np.asarray(light_space[1], np.float64).reshape(3, 3)
+        sun = sun_light_space[0] * n[0] + sun_light_space[1] * n[1] + sun_light_space[2] * n[2]
+    else:
+        sun = sun_light_space
+    return LightScene(width, height, camera_tilt, pixels_per_tile, view_index, center,
+                      [t[0] for t in types], [t[1] for t in types], [t[2] for t in types], place, light_list,
+                      tuple(float(v) for v in sun / np.linalg.norm(sun)), 0.35, (200, 210, 255), caster, cube_resolution)

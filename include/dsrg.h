@@ -246,6 +246,72 @@ int dsrg_diff_adjoint(dsrg_diff diff, int32_t views, int32_t width, int32_t heig
                       const float *gradImages, float *gradTexture, float *gradVertexColors, float *gradLight,
                       int32_t deterministic);
 
+/* ---- deferred light passes of the isometric sprite engine (SDK/SpriteEngine/lightAPI.h:27-31,
+ * orthoAPI.h:41-137) and draw_higher (api/drawAPI.h:142-150).
+ * Images are device memory (onDevice = 1).  RGBA images other than blend targets and draw_higher
+ * images are in the standard RGBA order, like the reference's OrderedImageRgbaU8. */
+
+/* OrthoView (orthoAPI.h:41-91) with its matrices as x, y, z axes. */
+typedef struct {
+	float normalToWorld[9];
+	float screenDepthToLightSpace[9];
+	float lightSpaceToScreenDepth[9];
+	int32_t pixelOffsetPerTileX[2];
+	int32_t pixelOffsetPerTileZ[2];
+	int32_t yPixelsPerTile;
+} dsrg_ortho_view;
+/* OrthoSystem(cameraTilt, pixelsPerTile).view[index] (orthoAPI.cpp:79-123); host only, no GPU call. */
+int dsrg_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, dsrg_ortho_view *out);
+/* Camera location (as dsrg_camera.location) of side 0..5 of a point light's shadow cube map, the
+ * rotation ShadowCubeMapSides[side] * normalToWorld at the origin (spriteAPI.cpp:328-336, 377-381);
+ * its camera is perspective with slope 1 at the cube's resolution.  Host only. */
+int dsrg_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]);
+
+/* setDirectedLight (add = 0) / addDirectedLight (add = 1) (lightAPI.cpp:23-74). */
+int dsrg_light_directed(dsrg_context context, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
+                        const float direction[3], float intensity, const int32_t color[3], int32_t add);
+
+/* One addPointLight call (lightAPI.cpp:169-285).  shadowCube: device image of cubeWidth x 6 cubeWidth
+ * floats (six reciprocal-depth faces, no row padding) or null for a light without shadows. */
+typedef struct {
+	float position[3]; /* relative to the camera, as the reference takes it */
+	float radius;
+	float intensity;
+	int32_t color[3];
+	const float *shadowCube;
+	int32_t cubeWidth;
+} dsrg_point_light;
+/* addPointLight for every light of the array, all in one pass: the sum of saturated additions of
+ * non-negative bytes does not depend on their order.  referenceThreads is the hardware thread count
+ * whose row bands the reference's threadedSplit would use (base/threading.cpp:193-263); each band
+ * restarts the reference's light-space sweep, so results depend on it.  0 = this machine's count. */
+int dsrg_light_points(dsrg_context context, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY,
+                      const dsrg_image *light, const dsrg_image *normal, const dsrg_image *height,
+                      const dsrg_point_light *lights, int32_t count, int32_t referenceThreads);
+/* blendLight (lightAPI.cpp:287-323): target (any pack order) = diffuse * light / 128 per channel. */
+int dsrg_light_blend(dsrg_context context, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light);
+
+/* One draw_higher source (F32 height + two RGBA images of the same size, device memory). */
+typedef struct {
+	const float *height;
+	const uint32_t *colorA;
+	const uint32_t *colorB;
+	int32_t width, height_;
+	int32_t heightStrideBytes, colorAStrideBytes, colorBStrideBytes;
+	int32_t colorAPackOrder, colorBPackOrder;
+	int32_t left, top;
+	float offset;
+} dsrg_sprite;
+/* draw_higher(targetHeight, sourceHeight, targetA, sourceA, targetB, sourceB, left, top, offset)
+ * (api/drawAPI.cpp:872-900, 946-981) for every sprite in order, in one pass: a pixel ends with the
+ * highest raised source height that is strictly above the target's, the earliest sprite on ties. */
+int dsrg_draw_higher(dsrg_context context, const dsrg_image *targetHeight, const dsrg_image *targetA,
+                     const dsrg_image *targetB, const dsrg_sprite *sprites, int32_t count);
+
+/* model_renderDepth semantics for every frame of a batch (1 x 1 depth walk, no colour), for
+ * shadow cube maps and other depth-only views: depthOnly = 1.  Frames need depth images only. */
+int dsrg_batch_set_depth_only(dsrg_batch batch, int32_t depthOnly);
+
 #ifdef __cplusplus
 }
 #endif

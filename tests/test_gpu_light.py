@@ -1,0 +1,128 @@
+"""GPU parity of the deferred light passes and draw_higher against the oracle (oracle/dsr_oracle.c,
+itself pinned to the reference build): every byte and every float bit must be identical."""
+import numpy as np
+import pytest
+
+from dfpsr_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+THREADS = 8  # the reference thread count whose row bands both sides use
+
+
+def dev(a, dtype):
+    import torch
+    return torch.tensor(np.ascontiguousarray(a).view(dtype), device="cuda")
+
+
+def host(t, dtype):
+    return t.cpu().numpy().view(dtype)
+
+
+def random_images(rng, h, w):
+    normal = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    light = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32) & np.uint32(0x7F7F7F7F)
+    height = rng.uniform(-2, 2, size=(h, w)).astype(np.float32)
+    return normal, light, height
+
+
+def test_directed_light(ctx):
+    import dfpsr_gb300 as d
+    from oracle import port
+    rng = np.random.default_rng(1)
+    normal, light, _ = random_images(rng, 157, 203)
+    for index, add in ((3, False), (5, True)):
+        view, oview = d.ortho_view(-0.8, 64, index), port.ortho_view(-0.8, 64, index)
+        want = port.directed_light(oview, light, normal, (0.3, -1.0, 0.2), 0.9, (255, 200, 100), add)
+        got = dev(light, np.int32)
+        ctx.light_directed(view, got, dev(normal, np.int32), (0.3, -1.0, 0.2), 0.9, (255, 200, 100), add)
+        assert np.array_equal(host(got, np.uint32), want)
+
+
+@pytest.mark.parametrize("shadows", [False, True])
+def test_point_lights_with_row_bands(ctx, shadows):
+    """Several lights in one pass against the oracle light after light; tall bounds exercise the
+    reference's row bands, which restart its running sums."""
+    import dfpsr_gb300 as d
+    from oracle import port
+    rng = np.random.default_rng(2)
+    h, w = 600, 360
+    normal, light, height = random_images(rng, h, w)
+    view, oview = d.ortho_view(-0.8, 64, 2), port.ortho_view(-0.8, 64, 2)
+    lights = []
+    for _ in range(4):
+        lights.append({"position": (rng.uniform(-2, 2), rng.uniform(0, 2), rng.uniform(-2, 2)), "radius": float(rng.uniform(2, 6)),
+                       "intensity": float(rng.uniform(0.5, 1.5)), "color": tuple(int(c) for c in rng.integers(64, 256, 3))})
+    cubes = [rng.uniform(0, 0.6, size=(6 * 64, 64)).astype(np.float32) for _ in lights] if shadows else [None] * 4
+    want = light
+    for l, cube in zip(lights, cubes):
+        want = port.point_light(oview, (w // 2, h // 2), want, normal, height, l["position"], l["radius"], l["intensity"],
+                                l["color"], cube, THREADS)
+    assert (want != light).sum() > 20000
+    got = dev(light, np.int32)
+    gpu_lights = [dict(l, cube=dev(c, np.float32)) if c is not None else l for l, c in zip(lights, cubes)]
+    ctx.light_points(view, (w // 2, h // 2), got, dev(normal, np.int32), dev(height, np.float32), gpu_lights, THREADS)
+    assert np.array_equal(host(got, np.uint32), want)
+
+
+def test_blend_light_every_pack_order(ctx):
+    import torch
+    from oracle import port
+    rng = np.random.default_rng(3)
+    diffuse, light, _ = random_images(rng, 97, 131)
+    for order in range(4):
+        target = torch.empty((97, 131), dtype=torch.int32, device="cuda")
+        ctx.light_blend(target, dev(diffuse, np.int32), dev(light, np.int32), order)
+        assert np.array_equal(host(target, np.uint32), port.blend_light(order, diffuse, light))
+
+
+def test_draw_higher_many_sprites(ctx):
+    """Overlapping sprites with transparent pixels, equal heights (the earliest wins), clipped
+    placements and mixed pack orders, against the oracle's draw_higher sprite after sprite."""
+    from oracle import port
+    rng = np.random.default_rng(4)
+    H, W = 120, 170
+    th = rng.uniform(-1, 0.5, size=(H, W)).astype(np.float32)
+    ta = rng.integers(0, 2**32, size=(H, W), dtype=np.uint64).astype(np.uint32)
+    tb = rng.integers(0, 2**32, size=(H, W), dtype=np.uint64).astype(np.uint32)
+    sprites, want = [], (th, ta, tb)
+    for k in range(40):
+        sh_, sw_ = int(rng.integers(8, 50)), int(rng.integers(8, 50))
+        hgt = np.round(rng.uniform(-1, 1, size=(sh_, sw_)) * 4).astype(np.float32) / 4  # many equal heights
+        hgt[rng.uniform(size=hgt.shape) < 0.15] = -np.inf
+        a = rng.integers(0, 2**32, size=(sh_, sw_), dtype=np.uint64).astype(np.uint32)
+        b = rng.integers(0, 2**32, size=(sh_, sw_), dtype=np.uint64).astype(np.uint32)
+        left, top = int(rng.integers(-30, W)), int(rng.integers(-30, H))
+        offset = float(np.float32(rng.choice([0.0, 0.25, -0.25])))
+        ap, bp = int(rng.integers(0, 4)), int(rng.integers(0, 4))
+        want = port.draw_higher((want[0], want[1], 1, want[2], 2), (hgt, a, ap, b, bp), left, top, offset)
+        sprites.append({"height": dev(hgt, np.float32), "color_a": dev(a, np.int32), "color_b": dev(b, np.int32),
+                        "left": left, "top": top, "offset": offset, "a_pack": ap, "b_pack": bp})
+    gh, ga, gb = dev(th, np.float32), dev(ta, np.int32), dev(tb, np.int32)
+    ctx.draw_higher(gh, ga, gb, sprites, a_pack=1, b_pack=2)
+    assert np.array_equal(host(gh, np.uint32), want[0].view(np.uint32))
+    assert np.array_equal(host(ga, np.uint32), want[1])
+    assert np.array_equal(host(gb, np.uint32), want[2])
+
+
+def test_deferred_light_pass_end_to_end(ctx):
+    """Sprites, shadow cube maps from a depth-only batch, directed and point lights, blendLight."""
+    import dfpsr_gb300 as d
+    from dfpsr_gb300.sprite_pass import DeferredLightPass
+    from oracle import light_pass
+    m, _ = d.ortho_view(-0.7, 64, 0).arrays()
+    scene = scenes.light_scene(seed=3, width=320, height=300, sprites=150, sprite_types=6, lights=4, radius_px=(60, 150),
+                               caster_triangles=300, cube_resolution=64, light_space=(m[9:18], m[0:9]))
+    out, light, height, diffuse, normal, cubes = light_pass.run(scene, THREADS)
+    gpu = DeferredLightPass(ctx, scene, THREADS)
+    got = gpu.run()
+    assert np.array_equal(host(gpu.height, np.uint32), height.view(np.uint32))
+    assert np.array_equal(host(gpu.diffuse, np.uint32), diffuse)
+    assert np.array_equal(host(gpu.normal, np.uint32), normal)
+    for k, cube in enumerate(cubes):
+        assert np.array_equal(host(gpu.cubes[k], np.uint32), cube.view(np.uint32)), f"shadow cube {k}"
+        assert (cube > 0).sum() > 100
+    assert np.array_equal(host(gpu.light, np.uint32), light)
+    assert np.array_equal(host(got, np.uint32), out)
+    assert (out != 0).mean() > 0.3
+    gpu.destroy()
