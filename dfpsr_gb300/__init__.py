@@ -310,24 +310,12 @@ class Context:
         self._check(self._l.dsrg_light_blend(self.handle, C.byref(ti), C.byref(di), C.byref(li)))
 
     def draw_higher(self, target_height, target_a, target_b, sprites, a_pack: int = 0, b_pack: int = 0):
-        """sprites: dicts with height, color_a, color_b (device tensors), left, top, offset, a_pack, b_pack."""
-        arr = (Sprite * max(1, len(sprites)))()
-        for i, sp in enumerate(sprites):
-            h = sp["height"]
-            arr[i].height = _ptr(h)
-            arr[i].colorA = _ptr(sp["color_a"])
-            arr[i].colorB = _ptr(sp["color_b"])
-            arr[i].height_, arr[i].width = int(h.shape[0]), int(h.shape[1])
-            arr[i].heightStrideBytes = int(h.stride(0)) * 4
-            arr[i].colorAStrideBytes = int(sp["color_a"].stride(0)) * 4
-            arr[i].colorBStrideBytes = int(sp["color_b"].stride(0)) * 4
-            arr[i].colorAPackOrder = int(sp.get("a_pack", 0))
-            arr[i].colorBPackOrder = int(sp.get("b_pack", 0))
-            arr[i].left, arr[i].top = int(sp["left"]), int(sp["top"])
-            arr[i].offset = float(sp["offset"])
+        """sprites: a SpriteArray, or dicts with height, color_a, color_b (device tensors), left, top,
+        offset, a_pack, b_pack."""
+        array = sprites if isinstance(sprites, SpriteArray) else SpriteArray(sprites)
         hi, ai, bi = image_struct(target_height), image_struct(target_a, a_pack), image_struct(target_b, b_pack)
         _torch_sync()
-        self._check(self._l.dsrg_draw_higher(self.handle, C.byref(hi), C.byref(ai), C.byref(bi), arr, len(sprites)))
+        self._check(self._l.dsrg_draw_higher(self.handle, C.byref(hi), C.byref(ai), C.byref(bi), array.array, array.count))
 
     def tuning(self) -> dict:
         t = Tuning()
@@ -455,6 +443,31 @@ class Renderer:
             self.destroy()
         except Exception:
             pass
+
+
+class SpriteArray:
+    """A dsrg_sprite array built once from sprite dicts (see Context.draw_higher); it keeps the
+    tensors it points at alive."""
+
+    def __init__(self, sprites):
+        self.count = len(sprites)
+        self.array = (Sprite * max(1, self.count))()
+        self._keep = []
+        for i, sp in enumerate(sprites):
+            h = sp["height"]
+            a = self.array[i]
+            a.height = _ptr(h)
+            a.colorA = _ptr(sp["color_a"])
+            a.colorB = _ptr(sp["color_b"])
+            a.height_, a.width = int(h.shape[0]), int(h.shape[1])
+            a.heightStrideBytes = int(h.stride(0)) * 4
+            a.colorAStrideBytes = int(sp["color_a"].stride(0)) * 4
+            a.colorBStrideBytes = int(sp["color_b"].stride(0)) * 4
+            a.colorAPackOrder = int(sp.get("a_pack", 0))
+            a.colorBPackOrder = int(sp.get("b_pack", 0))
+            a.left, a.top = int(sp["left"]), int(sp["top"])
+            a.offset = float(sp["offset"])
+            self._keep.append((h, sp["color_a"], sp["color_b"]))
 
 
 class Batch:

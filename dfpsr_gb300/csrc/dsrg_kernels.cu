@@ -293,38 +293,61 @@ void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *
 	launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
-// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176).  Records up to
-// 16 rows tall are cut by their own thread, taller ones by the whole warp.
+// Row interval of row y for corners held in registers (row_interval without the corner array).
+__device__ __forceinline__ void row_interval_regs(int32_t x0, int32_t y0, int32_t x1, int32_t y1, int32_t x2, int32_t y2,
+                                                  int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {
+	if ((x0 == x1 && y0 == y1) || (x1 == x2 && y1 == y2) || (x2 == x0 && y2 == y0)) { left = R; right = L; return; }
+	left = L; right = R;
+	cut_row(make_edge(x0, y0, x1, y1), y, L, R, left, right);
+	cut_row(make_edge(x1, y1, x2, y2), y, L, R, left, right);
+	cut_row(make_edge(x2, y2, x0, y0), y, L, R, left, right);
+}
+
+// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176).  Each warp takes
+// 32 records and spreads the concatenation of their rows over its lanes, so tall and short
+// triangles keep every lane busy: a lane finds the record of its row by a binary search over the
+// warp's prefix sums of row counts and fetches that record's corners with shuffles.
 __global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
                                                    const uint32_t *__restrict__ rowOffsets, uint32_t *rows) {
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t stride = gridDim.x * blockDim.x;
-	for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < recordCount; i0 += stride) {
-		const uint32_t i = i0 + threadIdx.x;
-		int32_t count = 0;
+	const int lane = threadIdx.x & 31;
+	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32u < recordCount; w += warps) {
+		const uint32_t i = w * 32u + (uint32_t)lane;
+		int32_t count = 0, top = 0, L = 0, R = 0;
+		int32_t f0 = 0, f1 = 0, f2 = 0, f3 = 0, f4 = 0, f5 = 0;
+		uint32_t out = 0;
 		if (i < recordCount) {
-			const DrawRecord r = records[i];
-			count = r.bottom - r.top;
-			if (count <= 16) {
-				uint32_t *out = rows + rowOffsets[i];
-				for (int32_t k = 0; k < count; k++) {
-					int32_t left, right;
-					row_interval(r.flat, r.top + k, r.left, r.right, left, right);
-					out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
-				}
-			}
+			const int4 a = __ldg(reinterpret_cast<const int4 *>(&records[i].flat[0]));   // flat[0..3]
+			const int4 b = __ldg(reinterpret_cast<const int4 *>(&records[i].flat[4]));   // flat[4..5], left, top
+			const int2 c = __ldg(reinterpret_cast<const int2 *>(&records[i].right));     // right, bottom
+			f0 = a.x; f1 = a.y; f2 = a.z; f3 = a.w; f4 = b.x; f5 = b.y;
+			L = b.z; top = b.w; R = c.x;
+			count = c.y - top;
+			out = rowOffsets[i];
 		}
-		uint32_t tall = __ballot_sync(0xFFFFFFFFu, count > 16);
-		while (tall) {
-			const int src = __ffs(tall) - 1;
-			tall &= tall - 1;
-			const uint32_t ri = __shfl_sync(0xFFFFFFFFu, i, src);
-			const DrawRecord t = records[ri];
-			uint32_t *out = rows + rowOffsets[ri];
-			for (int32_t k = (int32_t)lane; k < t.bottom - t.top; k += 32) {
+		int32_t inclusive = count;
+		for (int o = 1; o < 32; o <<= 1) {
+			const int32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
+			if (lane >= o) inclusive += v;
+		}
+		const int32_t total = __shfl_sync(0xFFFFFFFFu, inclusive, 31);
+		for (int32_t base = 0; base < total; base += 32) {
+			const int32_t j = base + lane;
+			int k = 0; // first lane whose inclusive sum exceeds j
+			for (int step = 16; step >= 1; step >>= 1)
+				if (__shfl_sync(0xFFFFFFFFu, inclusive, k + step - 1) <= j) k += step;
+			const int32_t start = __shfl_sync(0xFFFFFFFFu, inclusive, k) - __shfl_sync(0xFFFFFFFFu, count, k);
+			const int32_t kx0 = __shfl_sync(0xFFFFFFFFu, f0, k), ky0 = __shfl_sync(0xFFFFFFFFu, f1, k);
+			const int32_t kx1 = __shfl_sync(0xFFFFFFFFu, f2, k), ky1 = __shfl_sync(0xFFFFFFFFu, f3, k);
+			const int32_t kx2 = __shfl_sync(0xFFFFFFFFu, f4, k), ky2 = __shfl_sync(0xFFFFFFFFu, f5, k);
+			const int32_t kTop = __shfl_sync(0xFFFFFFFFu, top, k), kL = __shfl_sync(0xFFFFFFFFu, L, k);
+			const int32_t kR = __shfl_sync(0xFFFFFFFFu, R, k);
+			const uint32_t kOut = __shfl_sync(0xFFFFFFFFu, out, k);
+			if (j < total) {
+				const int32_t row = j - start;
 				int32_t left, right;
-				row_interval(t.flat, t.top + k, t.left, t.right, left, right);
-				out[k] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				row_interval_regs(kx0, ky0, kx1, ky1, kx2, ky2, kTop + row, kL, kR, left, right);
+				rows[kOut + (uint32_t)row] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
 			}
 		}
 	}
@@ -333,7 +356,9 @@ __global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict_
 void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream) {
 	if (recordCount == 0) return;
 	COUNT_LAUNCH();
-	rows_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets, fb.rows);
+	// one warp per 32 records
+	rows_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets,
+	                                                                                        fb.rows);
 }
 
 // ------------------------------------------------------------------ binning
@@ -800,15 +825,37 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 	}
 }
 
-// One thread per pixel: the winning fragment's quad is re-evaluated exactly (its row pair's
-// intervals and the reference's running sums at that quad) and the pixel is shaded (deferred
-// shading: only winners are shaded, one per pixel).  One CTA per tile of the batch.
-template <bool DEPTH_ONLY_1X1>
-__global__ void __launch_bounds__(256) resolve_kernel(BatchParams b, const DrawRecord *__restrict__ records,
-                                                      const uint32_t *__restrict__ binOffsets,
-                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+// model_renderDepth resolve, one thread per pixel: the winner's depth is the reference's 1 x 1
+// walk from its row's left end (executeTriangleDrawingDepth, renderCore.cpp:343-387).
+__global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                            const uint32_t *__restrict__ binOffsets,
+                                                            const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[tile] == binOffsets[tile + 1]) return; // nothing drawn: the key image was not written here
+	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+	const int32_t local = (int32_t)(tile - f.tileBase);
+	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
+	if (px >= f.width || py >= f.height) return;
+	const unsigned long long key = f.keys[(size_t)py * f.width + px];
+	if (key == 0ull) return;
+	const uint32_t ri = key_record(key, true);
+	const DrawRecord r = records[ri];
+	int32_t left, right;
+	unpack_row(rows[rowOffsets[ri] + (py - r.top)], left, right);
+	float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
+	value = chain_add(value, r.dx[0], px - left);
+	f.depth[(size_t)py * f.depthStride + px] = value;
+}
+
+// One thread per pixel: the winning fragment's quad is re-evaluated exactly (its row pair's
+// intervals and the reference's running sums at that quad) and the pixel is shaded.  Used for
+// frames of small triangles, where the pixels of a quad mostly have different winners.  One CTA
+// of 256 threads per 16x16 tile.
+__global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                             const uint32_t *__restrict__ binOffsets,
+                                                             const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	const uint32_t tile = blockIdx.x;
+	if (binOffsets[tile] == binOffsets[tile + 1]) return;
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
 	const int32_t local = (int32_t)(tile - f.tileBase);
 	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
@@ -818,18 +865,9 @@ __global__ void __launch_bounds__(256) resolve_kernel(BatchParams b, const DrawR
 	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
 	const uint32_t ri = key_record(key, depthTest);
 	const DrawRecord r = records[ri];
-	const uint32_t *recordRows = rows + rowOffsets[ri];
-	if (DEPTH_ONLY_1X1) {
-		int32_t left, right;
-		unpack_row(recordRows[py - r.top], left, right);
-		float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
-		value = chain_add(value, r.dx[0], px - left);
-		f.depth[(size_t)py * f.depthStride + px] = value;
-		return;
-	}
 	const int32_t y1 = py & ~1, x = px & ~1;
 	const int lane4 = ((py & 1) << 1) | (px & 1);
-	const RowPair pair = record_row_pair(r, recordRows, y1, f.height);
+	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
 	float w[3][4];
 	const int components = f.color ? 3 : 1;
 	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
@@ -844,6 +882,64 @@ __global__ void __launch_bounds__(256) resolve_kernel(BatchParams b, const DrawR
 		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
 	}
 	if (depthTest) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+}
+
+// One thread per 2x2 quad: the winners of its pixels are grouped by record, and for each record
+// the reference's running sums of the quad (its row pair's intervals and chains), the vertex
+// weights, the shader inputs and the mip level are evaluated once for all the pixels it won
+// (deferred shading: only winners are shaded).  Used for frames of larger triangles, where a
+// quad's pixels mostly share their winner.  One CTA of 64 threads per 16x16 tile.
+__global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                     const uint32_t *__restrict__ binOffsets,
+                                                     const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	const uint32_t tile = blockIdx.x;
+	if (binOffsets[tile] == binOffsets[tile + 1]) return;
+	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+	const int32_t local = (int32_t)(tile - f.tileBase);
+	const int32_t x = (local % f.tilesX) * TILE_W + 2 * (threadIdx.x & 7), y1 = (local / f.tilesX) * TILE_H + 2 * (threadIdx.x >> 3);
+	const int32_t width = f.width, height = f.height;
+	if (x >= width || y1 >= height) return;
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
+	uint32_t record[4];
+	uint32_t pending = 0;
+	for (int l = 0; l < 4; l++) {
+		const int32_t px = x + (l & 1), py = y1 + (l >> 1);
+		record[l] = 0;
+		if (px < width && py < height) {
+			const unsigned long long key = f.keys[(size_t)py * width + px];
+			if (key != 0ull) {
+				record[l] = key_record(key, depthTest);
+				pending |= 1u << l;
+			}
+		}
+	}
+	while (pending) {
+		const int first = __ffs(pending) - 1;
+		const uint32_t ri = record[first];
+		uint32_t mask = 0;
+		for (int l = first; l < 4; l++)
+			if ((pending & (1u << l)) && record[l] == ri) mask |= 1u << l;
+		pending &= ~mask;
+		const DrawRecord r = records[ri];
+		const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, height);
+		float w[3][4];
+		const int components = f.color ? 3 : 1;
+		for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
+		if (f.color) {
+			float wa[4], wb[4], wc[4];
+			lane_weights(w, affine, wa, wb, wc);
+			ShadeRecord shade;
+			make_shade(b.tasks[r.task], r.tri, shade);
+			float rgba[4][4];
+			shade_quad(shade, b.textures, wa, wb, wc, mask, rgba);
+			for (int l = 0; l < 4; l++)
+				if (mask & (1u << l))
+					f.color[(size_t)(y1 + (l >> 1)) * f.colorStride + x + (l & 1)] = pack_saturated(rgba[l], f.packOrder);
+		}
+		if (depthTest)
+			for (int l = 0; l < 4; l++)
+				if (mask & (1u << l)) f.depth[(size_t)(y1 + (l >> 1)) * f.depthStride + x + (l & 1)] = w[0][l];
+	}
 }
 
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,
@@ -865,8 +961,9 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	}
 	if (!resolve) return;
 	COUNT_LAUNCH();
-	if (b.depthOnly) resolve_kernel<true><<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-	else resolve_kernel<false><<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	if (b.depthOnly) resolve_depth_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	else if (config.resolveQuads) resolve_quads_kernel<<<b.totalTiles, 64, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	else resolve_pixels_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 }
 
 } // namespace dsrg

@@ -112,6 +112,7 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 struct RasterConfig {
 	int32_t threadsPerTile; // 128 or 256
 	int32_t ctasPerSm;      // resident CTAs per SM pulling tiles (at most 1024 / threadsPerTile)
+	int32_t resolveQuads;   // resolve one 2x2 quad per thread (large triangles) instead of one pixel
 };
 // resolve = false leaves the winners in the key images (the differentiable renderer reads them).
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,

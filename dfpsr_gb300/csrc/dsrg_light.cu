@@ -168,68 +168,96 @@ __device__ __forceinline__ float shadow_transparency(const float *cube, int32_t 
 	return fmul(reciDepth, 1.02f) > shadowReciDepth ? 1.0f : 0.0f;
 }
 
-// One thread per pixel of the light image: the bytes of every light whose bound holds the pixel
-// are summed and added to the pixel with saturation (equal to the reference's saturated additions
-// light after light, because every added byte is non-negative).
+// Contribution bytes (r, g, b) of one light at one pixel from its light-space offset o.
+__device__ __forceinline__ void point_light_bytes(const PointLightParams &p, const float *o, uint32_t normalWord, uint32_t *sum) {
+	const float negN[3] = {fmul(fadd((float)(normalWord & 0xFFu), -128.0f), -0.0078125f),
+	                       fmul(fadd((float)((normalWord >> 8) & 0xFFu), -128.0f), -0.0078125f),
+	                       fmul(fadd((float)((normalWord >> 16) & 0xFFu), -128.0f), -0.0078125f)};
+	const float squareLength = fadd(fadd(fmul(o[0], o[0]), fmul(o[1], o[1])), fmul(o[2], o[2]));
+	// squareRoot and reciprocalSquareRoot of the scalar build go through the double overload of sqrt
+	const double root = __dsqrt_rn((double)squareLength);
+	const float length = __double2float_rn(root);
+	const float ratio = vmin_ref(1.0f, fmul(length, p.reciprocalRadius));
+	const float distanceIntensity = fadd(fsub(1.0f, fmul(2.0f, ratio)), fmul(ratio, ratio));
+	const float rs = __double2float_rn(__ddiv_rn(1.0, root));
+	const float angle = vmax_ref(0.0f, fadd(fadd(fmul(fmul(o[0], rs), negN[0]), fmul(fmul(o[1], rs), negN[1])),
+	                                        fmul(fmul(o[2], rs), negN[2])));
+	float intensity = fmul(angle, distanceIntensity);
+	if (p.cube) intensity = fmul(intensity, shadow_transparency(p.cube, p.cubeWidth, p.cubeCenter, o[0], o[1], o[2]));
+	for (int c = 0; c < 3; c++) sum[c] += light_channel(fmul(intensity, p.color[c]));
+}
+
+// Every thread owns one lane (x mod 4) of one row and eight of its 4-pixel groups, spread 8 groups
+// apart so that a warp's loads for one step are 32 consecutive pixels: the reference's running
+// sums are evaluated with chain_add once per light at the first group, then advanced 8 steps of
+// dx*4 at a time with plain additions.  The bytes of every light whose bound holds a pixel are
+// summed and added to the pixel with saturation (equal to the reference's saturated additions
+// light after light, because every added byte is non-negative).  Blocks of 32 x 8 threads cover
+// 256 x 8 pixels.
 __global__ void __launch_bounds__(256) light_points_kernel(uint32_t *light, int32_t lightStride, const uint32_t *__restrict__ normal,
                                                            int32_t normalStride, const float *__restrict__ heightImage,
                                                            int32_t heightStride, int32_t width, int32_t height, PointFrame f) {
-	const int32_t x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
-	if (x >= width || y >= height) return;
-	uint32_t sum[3] = {0u, 0u, 0u};
-	bool any = false;
-	const float depthOffset = heightImage[(size_t)y * heightStride + x];
-	const uint32_t nc = normal[(size_t)y * normalStride + x];
-	const float negN[3] = {fmul(fadd((float)(nc & 0xFFu), -128.0f), -0.0078125f),
-	                       fmul(fadd((float)((nc >> 8) & 0xFFu), -128.0f), -0.0078125f),
-	                       fmul(fadd((float)((nc >> 16) & 0xFFu), -128.0f), -0.0078125f)};
+	const int32_t lane = threadIdx.x & 3, seg = (threadIdx.x >> 2) & 7;
+	const int32_t y = blockIdx.y * 8 + (threadIdx.x >> 5);
+	const int32_t g0 = blockIdx.x * 64 + seg; // first group; the thread's groups are g0, g0 + 8, ..., g0 + 56
+	if (y >= height) return;
+	uint32_t sum[8][3];
+	for (int j = 0; j < 8; j++) sum[j][0] = sum[j][1] = sum[j][2] = 0u;
+	uint32_t touched = 0;
 	const float *m = f.toLight;
 	for (int32_t k = 0; k < f.lightCount; k++) {
 		const PointLightParams &p = f.lights[k];
-		if (x < p.left || x >= p.right || y < p.top || y >= p.bottom) continue;
+		if (y < p.top || y >= p.bottom) continue;
+		const int32_t gl = p.left >> 2, gr = p.right >> 2; // groups of the bound (left and right are multiples of 4)
+		// the thread's groups inside [gl, gr): j from jFirst while g0 + 8j < gr
+		int32_t jFirst = gl > g0 ? (gl - g0 + 7) >> 3 : 0;
+		if (jFirst > 7 || g0 + 8 * jFirst >= gr) continue;
 		// the band holding this row (splitStartIndex, base/threading.cpp:209-221)
 		const int32_t rows = p.bottom - p.top;
 		int32_t bandTop = p.top;
-		for (int32_t j = 1; j < p.jobs; j++) {
-			const int32_t start = (j * rows) / p.jobs + p.top;
+		for (int32_t b = 1; b < p.jobs; b++) {
+			const int32_t start = (b * rows) / p.jobs + p.top;
 			if (start <= y) bandTop = start;
 		}
 		// lightBaseRow = screenDepthToLightSpace.transform((0.5 - cx + left, 0.5 - cy + bandTop, 0)) - source
 		const float px = fadd(fsub(0.5f, (float)f.centerX), (float)p.left);
 		const float py = fadd(fsub(0.5f, (float)f.centerY), (float)bandTop);
-		const int32_t lane = (x - p.left) & 3, steps = (x - p.left) >> 2;
-		const int32_t rowSteps = y - bandTop;
-		float o[3];
+		float value[3], stepX[3];
 		for (int c = 0; c < 3; c++) {
 			const float base = fsub(fadd(fadd(fmul(px, m[c]), fmul(py, m[3 + c])), fmul(0.0f, m[6 + c])), p.source[c]);
 			const float dx = m[c], dy = m[3 + c];
-			// F32x4::createGradient (base/simd.h:474-476)
+			// F32x4::createGradient (base/simd.h:474-476), then one += dy per row of the band
 			const float start = lane == 0 ? base : fadd(base, lane == 1 ? dx : fmul(dx, (float)lane));
-			const float row = chain_add(start, dy, rowSteps);
-			const float value = chain_add(row, fmul(dx, 4.0f), steps);
-			o[c] = fadd(value, fmul(m[6 + c], depthOffset));
+			const float row = chain_add(start, dy, y - bandTop);
+			stepX[c] = fmul(dx, 4.0f);
+			value[c] = chain_add(row, stepX[c], g0 + 8 * jFirst - gl);
 		}
-		const float squareLength = fadd(fadd(fmul(o[0], o[0]), fmul(o[1], o[1])), fmul(o[2], o[2]));
-		// squareRoot and reciprocalSquareRoot of the scalar build go through the double overload of sqrt
-		const float length = __double2float_rn(__dsqrt_rn((double)squareLength));
-		const float ratio = vmin_ref(1.0f, fmul(length, p.reciprocalRadius));
-		const float distanceIntensity = fadd(fsub(1.0f, fmul(2.0f, ratio)), fmul(ratio, ratio));
-		const float rs = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn((double)squareLength)));
-		const float angle = vmax_ref(0.0f, fadd(fadd(fmul(fmul(o[0], rs), negN[0]), fmul(fmul(o[1], rs), negN[1])),
-		                                        fmul(fmul(o[2], rs), negN[2])));
-		float intensity = fmul(angle, distanceIntensity);
-		if (p.cube) intensity = fmul(intensity, shadow_transparency(p.cube, p.cubeWidth, p.cubeCenter, o[0], o[1], o[2]));
-		for (int c = 0; c < 3; c++) sum[c] += light_channel(fmul(intensity, p.color[c]));
-		any = true;
+		for (int32_t j = jFirst; j < 8; j++) {
+			const int32_t g = g0 + 8 * j;
+			if (g >= gr) break;
+			if (j > jFirst)
+				for (int c = 0; c < 3; c++)
+					for (int s = 0; s < 8; s++) value[c] = fadd(value[c], stepX[c]);
+			const int32_t x = 4 * g + lane;
+			if (x >= width) continue;
+			const float depthOffset = heightImage[(size_t)y * heightStride + x];
+			const float o[3] = {fadd(value[0], fmul(m[6], depthOffset)), fadd(value[1], fmul(m[7], depthOffset)),
+			                    fadd(value[2], fmul(m[8], depthOffset))};
+			point_light_bytes(p, o, normal[(size_t)y * normalStride + x], sum[j]);
+			touched |= 1u << j;
+		}
 	}
-	if (!any) return;
-	uint32_t *q = light + (size_t)y * lightStride + x;
-	uint32_t v = *q;
-	for (int c = 0; c < 3; c++) {
-		const uint32_t s = ((v >> (8 * c)) & 0xFFu) + sum[c];
-		v = (v & ~(0xFFu << (8 * c))) | ((s > 255u ? 255u : s) << (8 * c));
+	for (int32_t j = 0; j < 8; j++) {
+		if (!(touched & (1u << j))) continue;
+		const int32_t x = 4 * (g0 + 8 * j) + lane;
+		uint32_t *q = light + (size_t)y * lightStride + x;
+		uint32_t v = *q;
+		for (int c = 0; c < 3; c++) {
+			const uint32_t s = ((v >> (8 * c)) & 0xFFu) + sum[j][c];
+			v = (v & ~(0xFFu << (8 * c))) | ((s > 255u ? 255u : s) << (8 * c));
+		}
+		*q = v;
 	}
-	*q = v;
 }
 
 __global__ void light_blend_kernel(uint32_t *target, int32_t targetStride, int32_t packOrder, const uint32_t *__restrict__ diffuse,
@@ -475,7 +503,7 @@ int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
 	f.centerY = centerY;
 	f.lightCount = (int32_t)params.size();
 	f.lights = reinterpret_cast<const PointLightParams *>(ctx->tables.ptr);
-	const dim3 grid((width + 15) / 16, (imageHeight + 15) / 16);
+	const dim3 grid((width + 255) / 256, (imageHeight + 7) / 8);
 	light_points_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)light->data, light->strideBytes / 4, (const uint32_t *)normal->data,
 	                                                   normal->strideBytes / 4, (const float *)height->data, height->strideBytes / 4,
 	                                                   width, imageHeight, f);

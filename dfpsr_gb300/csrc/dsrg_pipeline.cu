@@ -167,6 +167,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	RasterConfig config;
 	config.threadsPerTile = ctx->threadsPerTile;
 	config.ctasPerSm = ctx->ctasPerSm;
+	config.resolveQuads = 0; // set once the record count is known
 	PhaseKey key;
 	memset(&key, 0, sizeof(key));
 	key.resolve = job.resolve ? 1 : 0;
@@ -254,6 +255,10 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_bin_fill(params, fb, recordCount, bins, stream);
 	}));
 	TRY(cudaEventRecord(ctx->eventRasterStart, stream));
+	// small triangles (more than one record per 8 pixels) leave most quads with several winners:
+	// resolve per pixel; otherwise a quad's pixels mostly share their winner: resolve per quad
+	config.resolveQuads = (uint64_t)recordCount * 8u <= (uint64_t)totals.pixels ? 1 : 0;
+	key.config = config;
 	key.phase = 3;
 	TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
 	TRY(cudaEventRecord(ctx->eventRasterStop, stream));

@@ -2,6 +2,7 @@
 #ifndef DSRG_TYPES_H
 #define DSRG_TYPES_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #if !defined(__CUDACC__) && !defined(__align__)
@@ -83,6 +84,10 @@ struct __align__(16) DrawRecord {
 	uint32_t task;                    // index into the batch's task table
 	uint32_t frame;                   // index into the batch's frame table
 };
+// The row kernel loads corners and bounds as int4 (flat[0..3]), int4 (flat[4..5], left, top) and int2 (right, bottom).
+static_assert(sizeof(DrawRecord) == 96, "DrawRecord is 96 bytes");
+static_assert(offsetof(DrawRecord, left) == 24 && offsetof(DrawRecord, top) == 28 && offsetof(DrawRecord, right) == 32 &&
+              offsetof(DrawRecord, bottom) == 36, "DrawRecord field offsets");
 
 } // namespace dsrg
 

@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import DsrgError, Model, camera_struct, ortho_view, shadow_side_location
+from . import Model, SpriteArray, camera_struct, ortho_view, shadow_side_location
 
 BACKGROUND_HEIGHT = -1000.0
 
@@ -22,11 +22,12 @@ class DeferredLightPass:
         self.view = ortho_view(scene.camera_tilt, scene.pixels_per_tile, scene.view_index)
         self.types = [(dev(h, np.float32), dev(c, np.int32), dev(n, np.int32))
                       for h, c, n in zip(scene.sprite_heights, scene.sprite_diffuse, scene.sprite_normals)]
-        self.sprites = []
+        sprites = []
         for t, left, top, offset_bits in scene.placements:
             h, c, n = self.types[int(t)]
-            self.sprites.append({"height": h, "color_a": c, "color_b": n, "left": int(left), "top": int(top),
-                                 "offset": float(np.array([offset_bits], np.int32).view(np.float32)[0])})
+            sprites.append({"height": h, "color_a": c, "color_b": n, "left": int(left), "top": int(top),
+                            "offset": float(np.array([offset_bits], np.int32).view(np.float32)[0])})
+        self.sprites = SpriteArray(sprites)  # built once: the call only passes the array
         H, W = scene.height, scene.width
         self.height = torch.empty((H, W), dtype=torch.float32, device="cuda")
         self.diffuse = torch.empty((H, W), dtype=torch.int32, device="cuda")
