@@ -466,6 +466,14 @@ def main():
     depth = torch.zeros((h, w), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB of L2
 
+    # the tile kernel's launch shape for this workload, chosen by the library's autotuner on a
+    # one-frame batch of it (the plain path below uses the context's tuning)
+    tune_batch = ctx.batch()
+    tune_batch.add_frame(color, depth)
+    tune_batch.give_task(0, model)
+    tuning = tune_batch.autotune(rounds=3)
+    tune_batch.destroy()
+
     # fragments per frame: deterministic, counted once by the kernels themselves
     ctx.set_counting(True)
     ctx.render(model, model.camera, color, depth)
@@ -563,6 +571,7 @@ def main():
                                   "fragment counted before the depth test; the tile kernel's early depth culling skips "
                                   "fragments that cannot win, so frac can exceed 1 on high-overdraw scenes"},
             "gpu_launches": launches,
+            "tuning": tuning,
             "clocks": clocks.summary(),
         }
         if args.batch_frames > 0:

@@ -262,7 +262,7 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	dsrg_context_get_tuning(ctx, &start);
 	struct Shape { int32_t threads, perSm; };
 	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}};
-	const int32_t smalls[][2] = {{8, 16}, {0, 0}};
+	const int32_t smalls[][2] = {{8, 16}, {0, 0}, {4, 8}};
 	dsrg_tuning chosen = start;
 	double bestSeconds = -1.0;
 	for (const Shape &s : shapes) {

@@ -401,10 +401,12 @@ __device__ __forceinline__ bool tile_test_is_exact(const DrawRecord &r) {
 	return true;
 }
 
-// Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs.  Records touching at
-// most 4 tiles are walked by their own thread, with the atomics of threads that hit the same tile
-// merged into one; larger ones are walked by the whole warp, tested tile by tile.  A tile's list
-// keeps submission order only per warp, which the order-free depth keys do not need.
+// Counts (FILL = false) or writes (FILL = true) the (tile, record) pairs.  Every tile has two lists,
+// slot 2 * tile for the records the tile kernel walks one lane each (small) and slot 2 * tile + 1
+// for the ones it walks with a whole warp (large).  Records touching at most 4 tiles are binned by
+// their own thread, with the atomics of threads that hit the same slot merged into one; larger
+// ones by the whole warp, tested tile by tile.  A list keeps submission order only per warp, which
+// the order-free depth keys do not need.
 template <bool FILL>
 __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records, uint32_t recordCount, TileBins bins,
                            int32_t *errorFlag) {
@@ -413,10 +415,11 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 	for (uint32_t r0 = blockIdx.x * blockDim.x; r0 < recordCount; r0 += stride) {
 		const uint32_t r = r0 + threadIdx.x;
 		int32_t tx0 = 0, tx1 = -1, ty0 = 0, ty1 = -1, tilesX = 0;
-		uint32_t tileBase = 0;
+		uint32_t tileBase = 0, large = 1;
 		if (r < recordCount) {
 			const DrawRecord rec = records[r];
 			const FrameTarget &f = b.frames[rec.frame];
+			large = (b.depthOnly || !record_is_small(rec, b.smallRows, b.smallWidth)) ? 1u : 0u;
 			tilesX = f.tilesX;
 			tileBase = f.tileBase;
 			tx0 = rec.left >> 4; tx1 = (rec.right - 1) >> 4;
@@ -429,7 +432,7 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 		const bool big = tiles > 4;
 		for (int32_t i = 0; i < 4; i++) {
 			const bool active = !big && i < tiles;
-			const uint32_t tile = active ? tileBase + (uint32_t)((ty0 + i / w) * tilesX + tx0 + i % w) : 0xFFFFFFFFu;
+			const uint32_t tile = active ? 2u * (tileBase + (uint32_t)((ty0 + i / w) * tilesX + tx0 + i % w)) + large : 0xFFFFFFFFu;
 			const uint32_t peers = __match_any_sync(0xFFFFFFFFu, tile);
 			if (active) {
 				const uint32_t leader = __ffs(peers) - 1;
@@ -452,12 +455,13 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 			const int32_t btx = __shfl_sync(0xFFFFFFFFu, tilesX, src);
 			const uint32_t bbase = __shfl_sync(0xFFFFFFFFu, tileBase, src);
 			const uint32_t br = __shfl_sync(0xFFFFFFFFu, r, src);
+			const uint32_t blarge = __shfl_sync(0xFFFFFFFFu, large, src);
 			const DrawRecord rec = records[br];
 			const bool exact = tile_test_is_exact(rec);
 			for (int32_t i = (int32_t)lane; i < bt; i += 32) {
 				const int32_t tx = bx0 + i % bw, ty = by0 + i / bw;
 				if (exact && !tile_may_overlap(rec, tx * TILE_W, ty * TILE_H)) continue;
-				const uint32_t tile = bbase + (uint32_t)(ty * btx + tx);
+				const uint32_t tile = 2u * (bbase + (uint32_t)(ty * btx + tx)) + blarge;
 				uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
 				if (FILL) {
 					slot += bins.offsets[tile];
@@ -469,16 +473,16 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 }
 
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
-	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * b.totalTiles, stream);
+	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
 		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
 	}
-	launch_scan(bins.counts, bins.offsets, b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
+	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
-	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * b.totalTiles, stream);
+	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
 		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
@@ -632,11 +636,12 @@ __device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t 
 	return affine ? ~hi : hi;
 }
 
-// Persistent CTAs pull 16x16 tiles of the batch from a device queue.  In a tile, the warps take
-// list entries round-robin (warp w of W takes entries w, w + W, ...): a lane walks a small record by
-// itself (the reference's sequential walk; only the quads inside the tile are tested); large
-// records are rasterised by the whole warp, one lane per (row pair, position in the 2x2 quad),
-// which evaluates the reference's running sums once at the tile's left edge and then walks on.
+// Persistent CTAs pull 16x16 tiles of the batch from a device queue.  The binning split every
+// tile's list into small and large records.  Both are dealt round-robin over the warps (warp w of
+// W takes entries w, w + W, ...): a lane walks a small record by itself (the reference's sequential
+// walk; only the quads inside the tile are tested); large records are rasterised by the whole warp,
+// one lane per (row pair, position in the 2x2 quad), which evaluates the reference's running sums
+// once at the tile's left edge and then walks on.
 // All fragments compete for the tile's shared keys; the winners go to the frame's key image.
 // Tiles that nothing covers write nothing: the resolve pass skips them too.
 template <bool DEPTH_ONLY_1X1, int THREADS>
@@ -657,8 +662,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		__syncthreads();
 		const uint32_t tile = sharedTile;
 		if (tile >= b.totalTiles) break;
-		const uint32_t begin = bins.offsets[tile], end = bins.offsets[tile + 1];
-		if (begin == end) { __syncthreads(); continue; }
+		const uint32_t smallBegin = bins.offsets[2 * tile], smallEnd = bins.offsets[2 * tile + 1], end = bins.offsets[2 * tile + 2];
+		if (smallBegin == end) { __syncthreads(); continue; }
 		const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
 		const int32_t width = f.width, height = f.height;
 		const float *depthImage = f.depth;
@@ -684,36 +689,43 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		const bool cull = depthTest && b.fragments == nullptr;
 		const int32_t validW = min(TILE_W, width - tx0), validH = min(TILE_H, height - ty0);
 		uint32_t tileMin = 0u; // this warp's view of the tile's depth threshold (0: nothing culled yet)
-		for (uint32_t chunk = begin; chunk < end; chunk += 32u * WARPS) {
+		// small records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...), each
+		// walked by one lane in the reference's order; spreading them keeps a short list's walks in
+		// parallel on all warps rather than queued on a few
+		for (uint32_t chunk = smallBegin; chunk < smallEnd; chunk += (uint32_t)THREADS) {
+			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
+			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
+			if (e >= smallEnd) continue;
+			const uint32_t ri = bins.lists[e];
+			const DrawRecord r = records[ri];
+			if (cull && record_best_hi(r, tx0, ty0, affine, false) < tileMin) continue;
+			const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
+			walk_record<1>(r, rows + rowOffsets[ri], rowStart, rowEnd, height,
+			               [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
+				if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
+				for (int l = 0; l < 4; l++) {
+					const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
+					if (xx < tx0 || xx >= tx0 + TILE_W || yy >= height || xx >= width) continue;
+					if (!lane_covered(pair, x, edge, l)) continue;
+					tile_fragment(keys, initialDepth, coverage, counting, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l], ri,
+					              depthTest, affine, fragments);
+				}
+			});
+		}
+		// large records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...),
+		// each rasterised by the whole warp
+		for (uint32_t chunk = smallEnd; chunk < end; chunk += 32u * WARPS) {
 			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
 			const bool valid = e < end;
 			const uint32_t myRecord = valid ? bins.lists[e] : 0u;
-			bool small = false, culled = false;
+			bool culled = false;
 			uint32_t myBest = 0u;
 			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
-			if (valid) {
-				const DrawRecord r = records[myRecord];
-				if (cull) {
-					myBest = record_best_hi(r, tx0, ty0, affine, DEPTH_ONLY_1X1);
-					culled = myBest < tileMin;
-				}
-				small = !DEPTH_ONLY_1X1 && record_is_small(r, b.smallRows, b.smallWidth);
-				if (small && !culled) {
-					const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
-					walk_record<1>(r, rows + rowOffsets[myRecord], rowStart, rowEnd, height,
-					               [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
-						if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
-						for (int l = 0; l < 4; l++) {
-							const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-							if (xx < tx0 || xx >= tx0 + TILE_W || yy >= height || xx >= width) continue;
-							if (!lane_covered(pair, x, edge, l)) continue;
-							tile_fragment(keys, initialDepth, coverage, counting, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l],
-							              myRecord, depthTest, affine, fragments);
-						}
-					});
-				}
+			if (valid && cull) {
+				myBest = record_best_hi(records[myRecord], tx0, ty0, affine, DEPTH_ONLY_1X1);
+				culled = myBest < tileMin;
 			}
-			uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !small && !culled);
+			uint32_t largeMask = __ballot_sync(0xFFFFFFFFu, valid && !culled);
 			int sinceRefresh = 0;
 			while (largeMask) {
 				const int src = __ffs(largeMask) - 1;
@@ -831,7 +843,7 @@ __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const
                                                             const uint32_t *__restrict__ binOffsets,
                                                             const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
 	const uint32_t tile = blockIdx.x;
-	if (binOffsets[tile] == binOffsets[tile + 1]) return; // nothing drawn: the key image was not written here
+	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return; // nothing drawn: the key image was not written here
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
 	const int32_t local = (int32_t)(tile - f.tileBase);
 	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
@@ -855,7 +867,7 @@ __global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, cons
                                                              const uint32_t *__restrict__ binOffsets,
                                                              const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
 	const uint32_t tile = blockIdx.x;
-	if (binOffsets[tile] == binOffsets[tile + 1]) return;
+	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
 	const int32_t local = (int32_t)(tile - f.tileBase);
 	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
@@ -893,7 +905,7 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
                                                      const uint32_t *__restrict__ binOffsets,
                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
 	const uint32_t tile = blockIdx.x;
-	if (binOffsets[tile] == binOffsets[tile + 1]) return;
+	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
 	const int32_t local = (int32_t)(tile - f.tileBase);
 	const int32_t x = (local % f.tilesX) * TILE_W + 2 * (threadIdx.x & 7), y1 = (local / f.tilesX) * TILE_H + 2 * (threadIdx.x >> 3);

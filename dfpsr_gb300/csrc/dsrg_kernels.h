@@ -77,10 +77,12 @@ struct FrameBuffers {
 	size_t scanScratchElems;
 };
 
+// Two lists per tile: slot 2 * tile holds the records walked one lane each (small), slot
+// 2 * tile + 1 the ones walked by a whole warp (large).
 struct TileBins {
-	uint32_t *counts;   // totalTiles
-	uint32_t *offsets;  // totalTiles + 1
-	uint32_t *cursors;  // totalTiles
+	uint32_t *counts;   // 2 * totalTiles
+	uint32_t *offsets;  // 2 * totalTiles + 1
+	uint32_t *cursors;  // 2 * totalTiles
 	uint32_t *lists;
 	size_t listCapacity;
 };
@@ -101,7 +103,7 @@ enum ErrorBits : int32_t {
 void launch_project(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream);
 void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream);
 // Phase B: the records, in submission order (per frame: the order of its tasks, then of their
-// triangles), row offsets (total at rowOffsets[recordCount]) and tile counts (total at offsets[totalTiles]).
+// triangles), row offsets (total at rowOffsets[recordCount]) and tile counts (total at offsets[2 * totalTiles]).
 void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream);
 void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream);
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);

@@ -106,9 +106,9 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	fb.scanScratchElems = scan_scratch_elems(MAX_RECORDS + 2);
 	fb.scanScratch = carve.take<uint32_t>(fb.scanScratchElems);
 	TileBins bins;
-	bins.counts = carve.take<uint32_t>(MAX_TILES + 1);
-	bins.offsets = carve.take<uint32_t>(MAX_TILES + 1);
-	bins.cursors = carve.take<uint32_t>(MAX_TILES + 1);
+	bins.counts = carve.take<uint32_t>(2 * MAX_TILES + 1);
+	bins.offsets = carve.take<uint32_t>(2 * MAX_TILES + 1);
+	bins.cursors = carve.take<uint32_t>(2 * MAX_TILES + 1);
 	bins.lists = carve.take<uint32_t>(DSRG_NOALLOC_MAX_BIN_ENTRIES);
 	bins.listCapacity = DSRG_NOALLOC_MAX_BIN_ENTRIES;
 	unsigned long long *keys = carve.take<unsigned long long>((size_t)DSRG_NOALLOC_MAX_SIDE * DSRG_NOALLOC_MAX_SIDE);
@@ -164,7 +164,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	launch_bin_count(params, fb, recordCount, bins, stream);
 	uint32_t totalsRead[3] = {0, 0, 0};
 	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[1], bins.offsets + totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[1], bins.offsets + 2 * (size_t)totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&totalsRead[2], control + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(stream));
 	if (totalsRead[2] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "dsrg_model_render_depth_noalloc: triangle setup reported device error bits " + std::to_string(totalsRead[2]));

@@ -180,7 +180,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
 	TRY(ctx->triCounts.reserve(nt + 1));
 	TRY(ctx->triOffsets.reserve(nt + 1));
-	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(nt > totals.tiles ? nt : totals.tiles) + 1)));
+	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(nt > 2 * (size_t)totals.tiles ? nt : 2 * (size_t)totals.tiles) + 1)));
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
 	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
@@ -207,10 +207,10 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(ctx->records.reserve((size_t)recordCount + 1));
 	TRY(ctx->rowCounts.reserve((size_t)recordCount + 1));
 	TRY(ctx->rowOffsets.reserve((size_t)recordCount + 1));
-	TRY(ctx->binCounts.reserve((size_t)totals.tiles + 1));
-	TRY(ctx->binOffsets.reserve((size_t)totals.tiles + 1));
-	TRY(ctx->binCursors.reserve((size_t)totals.tiles + 1));
-	const uint32_t largest = recordCount > totals.tiles ? recordCount : totals.tiles;
+	TRY(ctx->binCounts.reserve(2 * (size_t)totals.tiles + 1));
+	TRY(ctx->binOffsets.reserve(2 * (size_t)totals.tiles + 1));
+	TRY(ctx->binCursors.reserve(2 * (size_t)totals.tiles + 1));
+	const uint32_t largest = recordCount > 2 * totals.tiles ? recordCount : 2 * totals.tiles;
 	TRY(ctx->scanScratch.reserve(scan_scratch_elems(largest + 1)));
 	fb.records = ctx->records.ptr;
 	fb.rowOffsets = ctx->rowOffsets.ptr;
@@ -234,7 +234,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	}));
 	uint32_t readBack[3] = {0, 0, 0};
 	TRY(cudaMemcpyAsync(&readBack[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	TRY(cudaMemcpyAsync(&readBack[1], bins.offsets + totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	TRY(cudaMemcpyAsync(&readBack[1], bins.offsets + 2 * (size_t)totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaMemcpyAsync(&readBack[2], ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaStreamSynchronize(stream));
 	if (readBack[2] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(readBack[2]));
