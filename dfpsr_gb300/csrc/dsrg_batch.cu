@@ -240,8 +240,8 @@ int dsrg_context_get_tuning(dsrg_context ctx, dsrg_tuning *out) {
 
 int dsrg_context_set_tuning(dsrg_context ctx, const dsrg_tuning *t) {
 	if (!ctx || !t) return DSRG_ERROR_INVALID_ARGUMENT;
-	if (t->threadsPerTile != 128 && t->threadsPerTile != 256)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: threadsPerTile must be 128 or 256");
+	if (t->threadsPerTile != 64 && t->threadsPerTile != 128 && t->threadsPerTile != 256)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: threadsPerTile must be 64, 128 or 256");
 	if (t->ctasPerSm < 1 || t->ctasPerSm > 1024 / t->threadsPerTile)
 		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: ctasPerSm must be between 1 and 1024 / threadsPerTile");
 	if (t->smallRows < 0 || t->smallWidth < 0 || t->smallRows > 16 || t->smallWidth > 64)
@@ -261,7 +261,7 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	dsrg_tuning start;
 	dsrg_context_get_tuning(ctx, &start);
 	struct Shape { int32_t threads, perSm; };
-	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}};
+	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}, {64, 16}};
 	const int32_t smalls[][2] = {{8, 16}, {0, 0}, {4, 8}};
 	dsrg_tuning chosen = start;
 	double bestSeconds = -1.0;

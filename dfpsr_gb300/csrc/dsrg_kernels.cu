@@ -958,13 +958,16 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
                    cudaStream_t stream) {
 	if (b.totalTiles == 0) return;
 	cudaMemsetAsync(b.tileQueue, 0, sizeof(uint32_t), stream);
-	const int threads = config.threadsPerTile == 128 ? 128 : 256;
+	const int threads = config.threadsPerTile == 64 ? 64 : (config.threadsPerTile == 128 ? 128 : 256);
 	const int maxPerSm = 1024 / threads;
 	const int perSm = config.ctasPerSm < 1 ? 1 : (config.ctasPerSm > maxPerSm ? maxPerSm : config.ctasPerSm);
 	uint32_t ctas = (uint32_t)sm_count() * (uint32_t)perSm;
 	if (ctas > b.totalTiles) ctas = b.totalTiles;
 	COUNT_LAUNCH();
-	if (threads == 128) {
+	if (threads == 64) {
+		if (b.depthOnly) raster_kernel<true, 64><<<ctas, 64, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+		else raster_kernel<false, 64><<<ctas, 64, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+	} else if (threads == 128) {
 		if (b.depthOnly) raster_kernel<true, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
 		else raster_kernel<false, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
 	} else {

@@ -112,7 +112,7 @@ void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stre
 void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
 // Launch shape of the persistent tile kernel.
 struct RasterConfig {
-	int32_t threadsPerTile; // 128 or 256
+	int32_t threadsPerTile; // 64, 128 or 256
 	int32_t ctasPerSm;      // resident CTAs per SM pulling tiles (at most 1024 / threadsPerTile)
 	int32_t resolveQuads;   // resolve one 2x2 quad per thread (large triangles) instead of one pixel
 };

@@ -186,8 +186,8 @@ int dsrg_batch_give_task(dsrg_batch batch, int32_t frameIndex, dsrg_model model,
 int dsrg_batch_render(dsrg_batch batch);
 
 /* Launch configuration of the tile kernel, chosen per context by dsrg_batch_autotune.
- *   threadsPerTile   threads of one tile's CTA (128 or 256)
- *   ctasPerSm        persistent CTAs per SM pulling tiles from the queue (1 to 4)
+ *   threadsPerTile   threads of one tile's CTA (64, 128 or 256)
+ *   ctasPerSm        persistent CTAs per SM pulling tiles from the queue (1 to 1024 / threadsPerTile)
  *   smallRows/Width  triangles whose raster bound is at most smallRows x smallWidth pixels are
  *                    walked by one lane each; larger ones by a whole warp per tile
  *   graphs           1 to replay each phase's launches as a CUDA graph, 0 to launch directly */

@@ -116,7 +116,8 @@ def test_batch_interleaved_tasks_keep_each_frames_submission_order(ctx):
         assert _same(c, ec) and _same(z, ez)
 
 
-@pytest.mark.parametrize("threads,per_sm,small", [(256, 4, (8, 16)), (256, 1, (0, 0)), (128, 8, (16, 32)), (128, 2, (4, 8))])
+@pytest.mark.parametrize("threads,per_sm,small", [(256, 4, (8, 16)), (256, 1, (0, 0)), (128, 8, (16, 32)), (128, 2, (4, 8)),
+                                                   (64, 16, (8, 16)), (64, 3, (0, 0))])
 def test_every_launch_shape_gives_the_same_frames(ctx, threads, per_sm, small):
     import dfpsr_gb300 as d
     frame_scenes = _frames(seed=13, frames=4, max_triangles=2500)
@@ -156,7 +157,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(ctx):
             batch.add_frame(*imgs[-1])
             batch.give_task(i, m)
         best = batch.autotune(rounds=1)
-        assert best["threads_per_tile"] in (128, 256)
+        assert best["threads_per_tile"] in (64, 128, 256)
         assert 1 <= best["ctas_per_sm"] <= 1024 // best["threads_per_tile"]
         assert ctx.tuning() == best
         for c, z in imgs:
