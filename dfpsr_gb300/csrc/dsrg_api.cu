@@ -347,8 +347,6 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Cannot call renderer_giveTask before renderer_begin!");
 	if (!m || !modelToWorld || !camera) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: null argument");
 	if (camera->width <= 0 || camera->height <= 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: camera without image size");
-	if (m->filter == DSRG_FILTER_ALPHA && r->hasColor)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: the alpha filter is not available on the GPU path yet");
 	CameraData cam = make_camera(*camera);
 	if (r->cameraKnown && r->affine != !camera->perspective)
 		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: perspective and orthogonal cameras cannot share one frame");
@@ -405,7 +403,41 @@ static int end_frame(dsrg_renderer r) {
 	job.depthOnly = r->depthOnly;
 	job.resolve = true;
 	BatchTotals totals;
-	int status = batch_enqueue(ctx, job, totals);
+	int status = DSRG_OK;
+	// Alpha-filtered tasks blend in submission order and write no depth (fillShape,
+	// fillerTemplates.h:387-441), so a frame runs as consecutive runs of alpha-filtered and other
+	// tasks, each through the whole pipeline, one after another on the stream.  Without a colour
+	// target an alpha-filtered task draws like a solid one.
+	auto isAlpha = [&](const TaskParams &t) { return r->hasColor && !r->depthOnly && t.filter == 1; };
+	bool anyAlpha = false;
+	for (const TaskParams &t : job.tasks) anyAlpha = anyAlpha || isAlpha(t);
+	if (!anyAlpha) {
+		job.alpha = false;
+		job.clearCounters = true;
+		status = batch_enqueue(ctx, job, totals);
+	} else {
+		std::vector<TaskParams> &all = r->runTasks;
+		all.swap(job.tasks);
+		size_t begin = 0;
+		while (begin < all.size() && status == DSRG_OK) {
+			const bool alpha = isAlpha(all[begin]);
+			size_t end = begin + 1;
+			while (end < all.size() && isAlpha(all[end]) == alpha) end++;
+			job.tasks.assign(all.begin() + begin, all.begin() + end);
+			job.alpha = alpha;
+			job.clearCounters = begin == 0;
+			BatchTotals run;
+			status = batch_enqueue(ctx, job, run);
+			totals.triangles += run.triangles;
+			totals.records += run.records;
+			totals.rows += run.rows;
+			totals.binEntries += run.binEntries;
+			begin = end;
+		}
+		all.swap(job.tasks);
+		job.alpha = false;
+		job.clearCounters = true;
+	}
 	job.tasks.swap(r->tasks);
 	job.textures.swap(r->textures);
 	if (status != DSRG_OK) {

@@ -353,64 +353,6 @@ __global__ void __launch_bounds__(256) adjoint_emit_kernel(DiffModel m, DiffPara
 	block_light_sums(light, blockLight);
 }
 
-// ------------------------------------------------------------------ stable radix sort of (key, id)
-
-const int SORT_TILE = 4096;   // items per block
-const int SORT_THREADS = 256;
-
-__global__ void __launch_bounds__(SORT_THREADS) radix_histogram_kernel(const uint32_t *__restrict__ keys, uint64_t n, int shift,
-                                                                       uint32_t *hist, uint32_t blocks) {
-	__shared__ uint32_t counts[256];
-	counts[threadIdx.x] = 0u;
-	__syncthreads();
-	const uint64_t begin = (uint64_t)blockIdx.x * SORT_TILE;
-	for (int j = threadIdx.x; j < SORT_TILE; j += SORT_THREADS) {
-		const uint64_t i = begin + j;
-		if (i < n) atomicAdd(&counts[(keys[i] >> shift) & 0xFFu], 1u);
-	}
-	__syncthreads();
-	hist[(size_t)threadIdx.x * blocks + blockIdx.x] = counts[threadIdx.x]; // digit-major
-}
-
-// Writes the block's items to their digit's slots in input order: 256 items at a time, ranks
-// within a warp from __match_any_sync, across warps from per-warp digit counts, across steps
-// from running per-digit counts.
-__global__ void __launch_bounds__(SORT_THREADS) radix_scatter_kernel(const uint32_t *__restrict__ keysIn, const uint32_t *__restrict__ idsIn,
-                                                                     uint64_t n, int shift, const uint32_t *__restrict__ offsets,
-                                                                     uint32_t blocks, uint32_t *keysOut, uint32_t *idsOut) {
-	__shared__ uint32_t running[256];
-	__shared__ uint32_t warpCounts[SORT_THREADS / 32][256];
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	running[threadIdx.x] = offsets[(size_t)threadIdx.x * blocks + blockIdx.x];
-	for (int w = 0; w < SORT_THREADS / 32; w++) warpCounts[w][threadIdx.x] = 0u;
-	__syncthreads();
-	const uint64_t begin = (uint64_t)blockIdx.x * SORT_TILE;
-	for (int j0 = 0; j0 < SORT_TILE; j0 += SORT_THREADS) {
-		const uint64_t i = begin + j0 + threadIdx.x;
-		const bool valid = i < n;
-		const uint32_t key = valid ? keysIn[i] : 0u;
-		const uint32_t digit = valid ? (key >> shift) & 0xFFu : 0x100u; // invalid lanes form their own group
-		const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
-		const uint32_t rankInWarp = __popc(peers & ((1u << lane) - 1u));
-		if (valid && rankInWarp == 0) warpCounts[warp][digit] = __popc(peers);
-		__syncthreads();
-		if (valid) {
-			uint32_t before = running[digit] + rankInWarp;
-			for (int w = 0; w < warp; w++) before += warpCounts[w][digit];
-			keysOut[before] = key;
-			idsOut[before] = idsIn ? idsIn[i] : (uint32_t)i;
-		}
-		__syncthreads();
-		uint32_t add = 0;
-		for (int w = 0; w < SORT_THREADS / 32; w++) {
-			add += warpCounts[w][threadIdx.x];
-			warpCounts[w][threadIdx.x] = 0u;
-		}
-		running[threadIdx.x] += add;
-		__syncthreads();
-	}
-}
-
 // One warp per target key k: the values of the ids sorted into [segment[k], segment[k + 1]),
 // lane l summing entries l, l + 32, ... in order, then a butterfly over the lanes.  Float
 // addition is commutative, so every lane of the butterfly ends with the same bits; the shape of
@@ -480,7 +422,7 @@ static DiffModel diff_model(dsrg_diff d) {
 // Scratch of segmented_sum for n entries and keys below keyEnd, reserved before any launch.
 static int reserve_segmented_sum(dsrg_diff d, uint64_t n, uint32_t keyEnd) {
 	dsrg_context ctx = d->context;
-	const uint32_t blocks = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
+	const uint32_t blocks = sort_blocks(n);
 	TRY(d->keysA.reserve(n)); TRY(d->keysB.reserve(n)); TRY(d->idsA.reserve(n)); TRY(d->idsB.reserve(n));
 	TRY(d->hist.reserve((size_t)256 * blocks + 1));
 	TRY(d->offsets.reserve((size_t)256 * blocks + 1));
@@ -497,30 +439,20 @@ static int reserve_segmented_sum(dsrg_diff d, uint64_t n, uint32_t keyEnd) {
 static int segmented_sum(dsrg_diff d, const uint32_t *keys, const float4 *values, uint64_t n, uint32_t keyEnd, float4 *out) {
 	dsrg_context ctx = d->context;
 	cudaStream_t stream = ctx->stream;
-	const uint32_t blocks = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
 	int bits = 1;
 	while ((1ull << bits) <= (uint64_t)keyEnd) bits++;
-	const int passes = (bits + 7) / 8;
 	// segment starts per key
 	TRY(cudaMemsetAsync(d->counts.ptr, 0, sizeof(uint32_t) * keyEnd, stream));
 	key_count_kernel<<<grid_for(n, 256), 256, 0, stream>>>(keys, n, keyEnd, d->counts.ptr);
 	add_launches(1);
 	launch_scan(d->counts.ptr, d->segments.ptr, keyEnd, ctx->scanScratch.ptr, ctx->scanScratch.capacity, stream);
-	// stable LSD radix sort of the entry ids by key, 8 bits per pass
-	const uint32_t *kin = keys;
-	const uint32_t *iin = nullptr; // first pass: ids are the entry indices
-	uint32_t *kout = d->keysA.ptr, *iout = d->idsA.ptr;
-	for (int p = 0; p < passes; p++) {
-		const int shift = 8 * p;
-		radix_histogram_kernel<<<blocks, SORT_THREADS, 0, stream>>>(kin, n, shift, d->hist.ptr, blocks);
-		launch_scan(d->hist.ptr, d->offsets.ptr, 256u * blocks, ctx->scanScratch.ptr, ctx->scanScratch.capacity, stream);
-		radix_scatter_kernel<<<blocks, SORT_THREADS, 0, stream>>>(kin, iin, n, shift, d->offsets.ptr, blocks, kout, iout);
-		add_launches(2);
-		kin = kout;
-		iin = iout;
-		kout = (kout == d->keysA.ptr) ? d->keysB.ptr : d->keysA.ptr;
-		iout = (iout == d->idsA.ptr) ? d->idsB.ptr : d->idsA.ptr;
-	}
+	// the entry ids sorted by key, entries of one key in entry order
+	SortBuffers sb;
+	sb.keysA = d->keysA.ptr; sb.keysB = d->keysB.ptr; sb.idsA = d->idsA.ptr; sb.idsB = d->idsB.ptr;
+	sb.hist = d->hist.ptr; sb.offsets = d->offsets.ptr;
+	sb.scanScratch = ctx->scanScratch.ptr; sb.scanScratchElems = ctx->scanScratch.capacity;
+	const uint32_t *sortedKeys = nullptr, *iin = nullptr;
+	launch_stable_sort(keys, nullptr, n, bits, sb, stream, &sortedKeys, &iin);
 	segment_sum_kernel<<<grid_for((uint64_t)keyEnd * 32, 256), 256, 0, stream>>>(d->segments.ptr, iin, values, keyEnd, out);
 	add_launches(1);
 	TRY(cudaGetLastError());

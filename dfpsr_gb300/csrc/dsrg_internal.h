@@ -124,6 +124,8 @@ struct BatchJob {
 	std::vector<TextureData> textures;
 	bool depthOnly = false;
 	bool resolve = true;
+	bool alpha = false;         // every task is alpha-filtered and every frame has a colour target
+	bool clearCounters = true;  // false for the later runs of one frame: fragment counts accumulate
 };
 
 // The launches of one phase between two host synchronisations, kept as a CUDA graph.  A phase
@@ -177,6 +179,8 @@ struct dsrg_context_s {
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;
 	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;
+	DeviceBuffer<uint32_t> alphaEntryTile, alphaTileKeys, alphaRecords; // the alpha filter's list order
+	DeviceBuffer<uint32_t> sortKeysA, sortKeysB, sortIdsA, sortIdsB, sortHist, sortOffsets;
 	int32_t smallRows = 8, smallWidth = 16; // one lane walks records whose raster bound is at most 8 x 16 pixels
 	int32_t ctasPerSm = 4;                  // resident CTAs per SM of the persistent tile kernel
 	int32_t threadsPerTile = 256;           // threads of one tile's CTA
@@ -227,6 +231,7 @@ struct dsrg_renderer_s {
 	std::vector<TextureData> textures;
 	std::vector<dsrg_texture> textureHandles;
 	std::vector<TaskParams> tasks;
+	std::vector<TaskParams> runTasks; // the frame's tasks while it runs as alpha-filtered and other runs
 };
 
 #define DSRG_CUDA_TRY(ctx, expr)                                                                      \

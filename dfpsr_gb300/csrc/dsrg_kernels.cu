@@ -828,7 +828,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 			const int32_t px = tx0 + (p & 15), py = ty0 + (p >> 4);
 			const int me = (p >> 4) * TILE_STRIDE + (p & 15);
 			if (px < width && py < height) {
-				if (counting) coverageImage[(size_t)py * width + px] = coverage[me];
+				if (counting) coverageImage[(size_t)py * width + px] += coverage[me]; // zeroed before a frame's first run
 				keyImage[(size_t)py * width + px] = keys[me];
 			}
 		}
@@ -952,6 +952,104 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
 			for (int l = 0; l < 4; l++)
 				if (mask & (1u << l)) f.depth[(size_t)(y1 + (l >> 1)) * f.depthStride + x + (l & 1)] = w[0][l];
 	}
+}
+
+// ------------------------------------------------------------------ alpha filter
+
+// Tile of every list entry (the entries of tile t are [offsets[2t], offsets[2t + 2])).
+__global__ void entry_tile_kernel(const uint32_t *__restrict__ binOffsets, uint32_t *entryTile) {
+	const uint32_t tile = blockIdx.x;
+	const uint32_t begin = binOffsets[2 * tile], end = binOffsets[2 * tile + 2];
+	for (uint32_t e = begin + threadIdx.x; e < end; e += blockDim.x) entryTile[e] = tile;
+}
+
+// After the sort by record: the tile of each sorted entry (key of the second sort) and its record.
+__global__ void tile_keys_kernel(const uint32_t *__restrict__ entryTile, const uint32_t *__restrict__ sortedRecords,
+                                 const uint32_t *__restrict__ sortedEntries, uint32_t n, uint32_t *tileKeys, uint32_t *records) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		tileKeys[i] = entryTile[sortedEntries[i]];
+		records[i] = sortedRecords[i];
+	}
+}
+
+// Alpha-filtered triangles (fillQuadSuper with Filter::Alpha, fillerTemplates.h:160-186, read-only
+// depth: fillerTemplates.h:386-441): every covered fragment that passes the depth test blends its
+// colour over the pixel, source * (alpha / 255) + target * (1 - alpha / 255), packed with
+// saturation after each blend, and writes no depth.  The order matters, so one thread per pixel
+// takes the tile's records in submission order (lists sorted by record).  The fragment's value is
+// re-evaluated exactly as the resolve pass does.  One CTA of 256 threads per 16x16 tile.
+__global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                    const uint32_t *__restrict__ binOffsets, const uint32_t *__restrict__ sorted,
+                                                    const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	const uint32_t tile = blockIdx.x;
+	const uint32_t begin = binOffsets[2 * tile], end = binOffsets[2 * tile + 2];
+	if (begin == end) return;
+	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+	const int32_t local = (int32_t)(tile - f.tileBase);
+	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
+	if (px >= f.width || py >= f.height || !f.color) return;
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
+	const float stored = depthTest ? f.depth[(size_t)py * f.depthStride + px] : 0.0f;
+	uint32_t *target = f.color + (size_t)py * f.colorStride + px;
+	uint32_t packed = *target;
+	const int32_t y1 = py & ~1, x = px & ~1;
+	const int lane4 = ((py & 1) << 1) | (px & 1);
+	uint32_t fragments = 0;
+	for (uint32_t e = begin; e < end; e++) {
+		const uint32_t ri = sorted[e];
+		const DrawRecord r = records[ri];
+		if (py < r.top || py >= r.bottom || px < r.left || px >= r.right) continue;
+		int32_t left, right;
+		unpack_row(rows[rowOffsets[ri] + (py - r.top)], left, right);
+		if (px < left || px >= right) continue;
+		fragments++;
+		const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
+		float w[3][4];
+		for (int c = 0; c < 3; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
+		const float z = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
+		if (depthTest && !(affine ? (z < stored) : (z > stored))) continue;
+		float wa[4], wb[4], wc[4];
+		lane_weights(w, affine, wa, wb, wc);
+		ShadeRecord shade;
+		make_shade(b.tasks[r.task], r.tri, shade);
+		float rgba[4];
+		shade_lane(shade, b.textures, wa, wb, wc, lane4, rgba);
+		const float opacity = fmul(rgba[3], 1.0f / 255.0f);
+		const float keep = fsub(1.0f, opacity);
+		float blended[4];
+		for (int c = 0; c < 4; c++) {
+			const float t = (float)((packed >> pack_shift(f.packOrder, c)) & 0xFFu);
+			blended[c] = fadd(fmul(rgba[c], opacity), fmul(t, keep));
+		}
+		packed = pack_saturated(blended, f.packOrder);
+	}
+	*target = packed;
+	if (f.coverage) f.coverage[(size_t)py * f.width + px] += fragments;
+	if (b.fragments && fragments) atomicAdd(b.fragments, (unsigned long long)fragments);
+}
+
+void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, uint32_t entries, uint32_t recordCount,
+                  const AlphaBuffers &a, cudaStream_t stream) {
+	if (b.totalTiles == 0) return;
+	const uint32_t *sorted = bins.lists;
+	if (entries > 1) {
+		// every tile's list in submission order: a stable sort of the entries by record, then a
+		// stable sort of that order by tile (a tile's entries keep their offsets, which only
+		// depend on the tile's count)
+		COUNT_LAUNCH();
+		entry_tile_kernel<<<b.totalTiles, 128, 0, stream>>>(bins.offsets, a.entryTile);
+		int recordBits = 1, tileBits = 1;
+		while ((1ull << recordBits) < (uint64_t)recordCount) recordBits++;
+		while ((1ull << tileBits) < (uint64_t)b.totalTiles) tileBits++;
+		const uint32_t *records = nullptr, *order = nullptr;
+		launch_stable_sort(bins.lists, nullptr, entries, recordBits, a.sort, stream, &records, &order);
+		COUNT_LAUNCH();
+		tile_keys_kernel<<<grid_for(entries, 256), 256, 0, stream>>>(a.entryTile, records, order, entries, a.tileKeys, a.records);
+		const uint32_t *tiles = nullptr;
+		launch_stable_sort(a.tileKeys, a.records, entries, tileBits, a.sort, stream, &tiles, &sorted);
+	}
+	COUNT_LAUNCH();
+	alpha_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, sorted, fb.rowOffsets, fb.rows);
 }
 
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,

@@ -119,6 +119,28 @@ struct RasterConfig {
 // resolve = false leaves the winners in the key images (the differentiable renderer reads them).
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,
                    cudaStream_t stream);
+// Buffers of launch_stable_sort for n items: keys and ids twice n; hist and offsets
+// 256 * sort_blocks(n) + 1; scan scratch for 256 * sort_blocks(n) + 1 values.
+struct SortBuffers {
+	uint32_t *keysA, *keysB, *idsA, *idsB, *hist, *offsets;
+	uint32_t *scanScratch;
+	size_t scanScratchElems;
+};
+uint32_t sort_blocks(uint64_t n);
+// Stable LSD radix sort of the ids (the item indices when ids is null) by the low keyBits bits of
+// their keys; *sortedKeys and *sortedIds point at the buffers holding the result (the inputs when n is 0).
+void launch_stable_sort(const uint32_t *keys, const uint32_t *ids, uint64_t n, int keyBits, const SortBuffers &b,
+                        cudaStream_t stream, const uint32_t **sortedKeys, const uint32_t **sortedIds);
+// Scratch of launch_alpha for `entries` list entries: entryTile, tileKeys and records hold
+// `entries` values each; sort as launch_stable_sort needs for `entries` items.
+struct AlphaBuffers {
+	uint32_t *entryTile, *tileKeys, *records;
+	SortBuffers sort;
+};
+// The alpha filter over the binned records (in place of launch_raster): colour blends in
+// submission order, depth read only.
+void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, uint32_t entries, uint32_t recordCount,
+                  const AlphaBuffers &a, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total).
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);
 size_t scan_scratch_elems(uint32_t n);

@@ -87,7 +87,10 @@ size_t layout_tables(BatchJob &job, unsigned long long *keysBase, unsigned char 
 struct PhaseKey {
 	int32_t phase;
 	int32_t resolve;
+	int32_t alpha;
 	uint32_t recordCount;
+	uint32_t entries;
+	AlphaBuffers alphaBuffers;
 	RasterConfig config;
 	BatchParams params;
 	FrameBuffers fb;
@@ -157,7 +160,9 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	params.smallWidth = ctx->smallWidth;
 	params.tileQueue = ctx->control.ptr;
 	params.fragments = nullptr;
-	if (ctx->counting) {
+	if (ctx->counting && !job.clearCounters) {
+		params.fragments = ctx->fragmentCounter.ptr;
+	} else if (ctx->counting) {
 		TRY(cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, sizeof(unsigned long long), stream));
 		params.fragments = ctx->fragmentCounter.ptr;
 		for (const FrameTarget &f : job.frames)
@@ -171,6 +176,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	PhaseKey key;
 	memset(&key, 0, sizeof(key));
 	key.resolve = job.resolve ? 1 : 0;
+	key.alpha = job.alpha ? 1 : 0;
 	key.config = config;
 
 	// phase A: projection and record counts
@@ -255,6 +261,33 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_bin_fill(params, fb, recordCount, bins, stream);
 	}));
 	TRY(cudaEventRecord(ctx->eventRasterStart, stream));
+	if (job.alpha) {
+		// blending in submission order: sorted tile lists, one thread per pixel
+		const uint64_t n = totals.binEntries;
+		const uint32_t blocks = sort_blocks(n);
+		TRY(ctx->alphaEntryTile.reserve(n + 1)); TRY(ctx->alphaTileKeys.reserve(n + 1)); TRY(ctx->alphaRecords.reserve(n + 1));
+		TRY(ctx->sortKeysA.reserve(n + 1)); TRY(ctx->sortKeysB.reserve(n + 1));
+		TRY(ctx->sortIdsA.reserve(n + 1)); TRY(ctx->sortIdsB.reserve(n + 1));
+		TRY(ctx->sortHist.reserve((size_t)256 * blocks + 1)); TRY(ctx->sortOffsets.reserve((size_t)256 * blocks + 1));
+		TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)((size_t)256 * blocks) + 1)));
+		AlphaBuffers a;
+		memset(&a, 0, sizeof(a));
+		a.entryTile = ctx->alphaEntryTile.ptr; a.tileKeys = ctx->alphaTileKeys.ptr; a.records = ctx->alphaRecords.ptr;
+		a.sort.keysA = ctx->sortKeysA.ptr; a.sort.keysB = ctx->sortKeysB.ptr;
+		a.sort.idsA = ctx->sortIdsA.ptr; a.sort.idsB = ctx->sortIdsB.ptr;
+		a.sort.hist = ctx->sortHist.ptr; a.sort.offsets = ctx->sortOffsets.ptr;
+		a.sort.scanScratch = ctx->scanScratch.ptr; a.sort.scanScratchElems = ctx->scanScratch.capacity;
+		key.phase = 3;
+		key.entries = totals.binEntries;
+		key.alphaBuffers = a;
+		TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_alpha(params, fb, bins, totals.binEntries, recordCount, a, stream); }));
+		TRY(cudaEventRecord(ctx->eventRasterStop, stream));
+		if (outputs) {
+			outputs->params = params;
+			outputs->fb = fb;
+		}
+		return DSRG_OK;
+	}
 	// small triangles (more than one record per 8 pixels) leave most quads with several winners:
 	// resolve per pixel; otherwise a quad's pixels mostly share their winner: resolve per quad
 	config.resolveQuads = (uint64_t)recordCount * 8u <= (uint64_t)totals.pixels ? 1 : 0;

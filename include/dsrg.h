@@ -124,7 +124,9 @@ int dsrg_model_render_depth(dsrg_context context, dsrg_model model, const float 
 
 /* renderer_create / renderer_begin / renderer_giveTask / renderer_end (api/rendererAPI.h:56-135,
  * api/modelAPI.h:299-301): triangles of every task are drawn at renderer_end in submission
- * order, with the same result as model_render of the tasks one after another. */
+ * order, with the same result as model_render of the tasks one after another.  Models with
+ * DSRG_FILTER_ALPHA blend over the colour target in submission order and only read depth; a
+ * frame mixing them with solid models runs as consecutive runs of each kind. */
 int dsrg_renderer_create(dsrg_context context, dsrg_renderer *out);
 int dsrg_renderer_destroy(dsrg_renderer renderer);
 int dsrg_renderer_begin(dsrg_renderer renderer, const dsrg_image *color, const dsrg_image *depth);
@@ -178,7 +180,9 @@ int dsrg_batch_destroy(dsrg_batch batch);
 int dsrg_batch_clear(dsrg_batch batch);
 /* Adds a frame (renderer_begin, api/rendererAPI.cpp:151-168); *frameIndex receives its index. */
 int dsrg_batch_add_frame(dsrg_batch batch, const dsrg_image *color, const dsrg_image *depth, int32_t *frameIndex);
-/* renderer_giveTask (api/modelAPI.h:299-301) for one frame of the batch. */
+/* renderer_giveTask (api/modelAPI.h:299-301) for one frame of the batch.  Alpha-filtered models
+ * on a frame with a colour target are rejected with DSRG_ERROR_UNSUPPORTED (draw them with
+ * dsrg_renderer_* or dsrg_model_render). */
 int dsrg_batch_give_task(dsrg_batch batch, int32_t frameIndex, dsrg_model model, const float *modelToWorld,
                          const dsrg_camera *camera);
 /* Draws every frame (renderer_end of each); returns when all results are in the images.  The
