@@ -34,6 +34,8 @@ EXPORTED = [
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
     "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
     "dsrg_draw_higher", "dsrg_batch_set_depth_only",
+    "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
+    "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
 ]
 
 
@@ -123,6 +125,12 @@ def lib():
         l.dsrg_renderer_give_task.argtypes = [P, P, P, C.POINTER(Camera)]
         l.dsrg_renderer_end.argtypes = [P]
         l.dsrg_renderer_takes_triangles.argtypes = [P]
+        l.dsrg_renderer_occlude_from_box.argtypes = [P, P, P, P, C.POINTER(Camera), I]
+        l.dsrg_renderer_occlude_from_existing_triangles.argtypes = [P]
+        l.dsrg_renderer_occlude_from_top_rows.argtypes = [P, C.POINTER(Camera)]
+        l.dsrg_renderer_is_box_visible.argtypes = [P, P, P, P, C.POINTER(Camera), C.POINTER(I)]
+        l.dsrg_renderer_has_occluders.argtypes = [P]
+        l.dsrg_renderer_get_occlusion_grid.argtypes = [P, P, I, C.POINTER(I), C.POINTER(I)]
         l.dsrg_model_render_depth_noalloc.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
         l.dsrg_batch_create.argtypes = [P, C.POINTER(P)]
         l.dsrg_batch_destroy.argtypes = [P]
@@ -432,6 +440,40 @@ class Renderer:
     @property
     def takes_triangles(self) -> bool:
         return bool(self.ctx._l.dsrg_renderer_takes_triangles(self.handle))
+
+    # the occlusion grid (renderer_occludeFromBox / FromExistingTriangles / FromTopRows, isBoxVisible)
+    def occlude_from_box(self, minimum, maximum, transform, camera: Camera, debug_silhouette: bool = False):
+        a, b = np.ascontiguousarray(minimum, np.float32), np.ascontiguousarray(maximum, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        self.ctx._check(self.ctx._l.dsrg_renderer_occlude_from_box(self.handle, a.ctypes.data, b.ctypes.data, t.ctypes.data,
+                                                                   C.byref(camera), 1 if debug_silhouette else 0))
+
+    def occlude_from_existing_triangles(self):
+        self.ctx._check(self.ctx._l.dsrg_renderer_occlude_from_existing_triangles(self.handle))
+
+    def occlude_from_top_rows(self, camera: Camera):
+        _torch_sync()
+        self.ctx._check(self.ctx._l.dsrg_renderer_occlude_from_top_rows(self.handle, C.byref(camera)))
+
+    def is_box_visible(self, minimum, maximum, transform, camera: Camera) -> bool:
+        a, b = np.ascontiguousarray(minimum, np.float32), np.ascontiguousarray(maximum, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        v = C.c_int32(0)
+        self.ctx._check(self.ctx._l.dsrg_renderer_is_box_visible(self.handle, a.ctypes.data, b.ctypes.data, t.ctypes.data,
+                                                                 C.byref(camera), C.byref(v)))
+        return bool(v.value)
+
+    @property
+    def has_occluders(self) -> bool:
+        return bool(self.ctx._l.dsrg_renderer_has_occluders(self.handle))
+
+    def occlusion_grid(self) -> np.ndarray:
+        gw, gh = C.c_int32(0), C.c_int32(0)
+        self.ctx._check(self.ctx._l.dsrg_renderer_get_occlusion_grid(self.handle, None, 0, C.byref(gw), C.byref(gh)))
+        out = np.zeros((gh.value, gw.value), np.float32)
+        self.ctx._check(self.ctx._l.dsrg_renderer_get_occlusion_grid(self.handle, out.ctypes.data, out.size, C.byref(gw),
+                                                                     C.byref(gh)))
+        return out
 
     def destroy(self):
         if getattr(self, "handle", None) and self.ctx.handle:

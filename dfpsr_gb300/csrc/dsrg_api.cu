@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "dsrg_internal.h"
+#include "dsrg_occlusion.h"
 
 using namespace dsrg;
 
@@ -292,6 +293,9 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 	if (depth) r->depth = *depth;
 	r->width = color ? color->width : (depth ? depth->width : 0);
 	r->height = color ? color->height : (depth ? depth->height : 0);
+	r->gridWidth = (r->width + (dsrg::OCCLUSION_CELL - 1)) / dsrg::OCCLUSION_CELL;
+	r->gridHeight = (r->height + (dsrg::OCCLUSION_CELL - 1)) / dsrg::OCCLUSION_CELL;
+	r->occluded = false;
 	size_t pixels = (size_t)r->width * r->height;
 	r->deviceColor = nullptr;
 	r->deviceDepth = nullptr;
@@ -353,6 +357,12 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	r->affine = !camera->perspective;
 	r->cameraKnown = true;
 	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld)) return DSRG_OK;
+	if (r->occluded) { // the whole model behind the occluders so far (modelAPI.cpp:228-233)
+		bool occluded = false;
+		const int s = renderer_box_occluded(r, m->minBound, m->maxBound, modelToWorld, cam, &occluded);
+		if (s != DSRG_OK) return s;
+		if (occluded) return DSRG_OK;
+	}
 	if (m->triangleCount == 0) return DSRG_OK;
 	TaskParams task;
 	memset(&task, 0, sizeof(task));
@@ -381,15 +391,9 @@ int dsrg_renderer_give_task(dsrg_renderer r, dsrg_model m, const float *modelToW
 	return give_task(r, m, modelToWorld, camera);
 }
 
-static int end_frame(dsrg_renderer r) {
-	dsrg_context ctx = r->context;
-	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
-	r->receiving = false;
-	BatchJob &job = ctx->frameJob;
-	job.tasks.swap(r->tasks);
-	job.textures.swap(r->textures);
-	job.frames.resize(1);
-	FrameTarget &f = job.frames[0];
+} // extern "C"
+
+void renderer_frame_target(dsrg_renderer r, FrameTarget &f) {
 	memset(&f, 0, sizeof(f));
 	f.color = r->hasColor ? r->deviceColor : nullptr;
 	f.colorStride = r->colorStride;
@@ -399,7 +403,35 @@ static int end_frame(dsrg_renderer r) {
 	f.width = r->width;
 	f.height = r->height;
 	f.affine = r->affine ? 1 : 0;
-	f.coverage = ctx->counting ? ctx->coverage : nullptr;
+	f.coverage = r->context->counting ? r->context->coverage : nullptr;
+	if (r->occluded) {
+		f.occlusion = r->gridDevice.ptr;
+		f.gridWidth = r->gridWidth;
+		f.gridHeight = r->gridHeight;
+		f.gridStride = r->gridAllocWidth;
+	}
+}
+
+extern "C" {
+
+static int end_frame(dsrg_renderer r) {
+	dsrg_context ctx = r->context;
+	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
+	r->receiving = false;
+	BatchJob &job = ctx->frameJob;
+	job.tasks.swap(r->tasks);
+	job.textures.swap(r->textures);
+	job.frames.resize(1);
+	if (r->occluded) {
+		const int s = renderer_grid_on_device(r);
+		if (s != DSRG_OK) {
+			job.tasks.swap(r->tasks);
+			job.textures.swap(r->textures);
+			return s;
+		}
+	}
+	FrameTarget &f = job.frames[0];
+	renderer_frame_target(r, f);
 	job.depthOnly = r->depthOnly;
 	job.resolve = true;
 	BatchTotals totals;

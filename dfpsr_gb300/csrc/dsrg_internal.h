@@ -232,7 +232,24 @@ struct dsrg_renderer_s {
 	std::vector<dsrg_texture> textureHandles;
 	std::vector<TaskParams> tasks;
 	std::vector<TaskParams> runTasks; // the frame's tasks while it runs as alpha-filtered and other runs
+	// occlusion grid (RendererImpl::depthGrid, api/rendererAPI.cpp:141-191): one float per 16x16
+	// cell, kept on the host for box occluders and box tests and on the device for the per-command
+	// work; whichever copy is stale is refreshed from the other before it is used
+	bool occluded = false;
+	int32_t gridWidth = 0, gridHeight = 0;           // cells covering this frame's target
+	int32_t gridAllocWidth = 0, gridAllocHeight = 0; // the grid image, grown but never shrunk; its row stride
+	std::vector<float> gridHost;
+	DeviceBuffer<float> gridDevice;
+	bool gridHostValid = false, gridDeviceValid = false;
 };
+
+// The frame target of a renderer's current frame (images, size, occlusion grid when in use).
+void renderer_frame_target(dsrg_renderer r, dsrg::FrameTarget &f);
+// Uploads the occlusion grid when the device copy is stale.
+int renderer_grid_on_device(dsrg_renderer r);
+// isBoxOccluded (api/rendererAPI.cpp:297-341) against the current grid; sets *occluded.
+int renderer_box_occluded(dsrg_renderer r, const float *minimum, const float *maximum, const float *modelToWorld,
+                          const dsrg::CameraData &camera, bool *occluded);
 
 #define DSRG_CUDA_TRY(ctx, expr)                                                                      \
 	do {                                                                                         \
@@ -274,6 +291,9 @@ struct BatchOutputs {
 int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs = nullptr);
 // Waits for the stream, checks the device error bits and fills the context's statistics.
 int batch_finish(dsrg_context ctx, const BatchTotals &totals);
+// occludeFromExistingTriangles for the job's tasks: projection and triangle setup, the setup's
+// commands lowering their frame's occlusion grid instead of becoming records; waits for the GPU.
+int occlude_enqueue(dsrg_context ctx, BatchJob &job);
 
 } // namespace dsrg
 

@@ -28,6 +28,7 @@
 #include "dsrg_shade.h"
 #include "dsrg_kernels.h"
 #include "dsrg_raster.cuh"
+#include "dsrg_occlusion.h"
 
 namespace dsrg {
 
@@ -85,15 +86,50 @@ struct Corner {
 
 // Emits one draw command (renderCore.cpp:203-217 executeTriangleDrawing against the whole target):
 // the triangle bound cut to the target with rows aligned to pairs (ITriangle2D.cpp:70-75).
-template <bool WRITE>
-__device__ void emit_record(const TaskParams &task, uint32_t taskIndex, int32_t width, int32_t height, const FrameBuffers &fb,
+enum SetupMode { SETUP_COUNT = 0, SETUP_WRITE = 1, SETUP_OCCLUDE = 2 };
+
+// Lowers a frame's occlusion grid to the command's farthest corner over the cells its triangle
+// covers (occludeFromSortedHull with the triangle as the hull, rendererAPI.cpp:216-239, 240-255).
+// Cells only ever decrease, so the order of the commands does not matter.
+__device__ void occlude_cells(const FrameTarget &f, const int64_t *fx, const int64_t *fy, const int32_t *bd, const Corner *c) {
+	if (!((bd[2] - bd[0]) > OCCLUSION_CELL && (bd[3] - bd[1]) > OCCLUSION_CELL)) return;
+	float distance = 0.0f;
+	for (int i = 0; i < 3; i++) if (c[i].cs.z > distance) distance = c[i].cs.z;
+	const CellRect cells = outer_cell_bound(bd[0], bd[1], bd[2], bd[3], f.gridWidth, f.gridHeight);
+	for (int32_t cy = cells.top; cy < cells.bottom; cy++) {
+		for (int32_t cx = cells.left; cx < cells.right; cx++) {
+			if (!cell_inside_hull(fx, fy, 3, cx, cy)) continue;
+			// float minimum by compare-and-swap; it stops as soon as the cell holds a smaller value
+			int *cell = reinterpret_cast<int *>(f.occlusion + (size_t)cy * f.gridStride + cx);
+			int old = *cell;
+			while (distance < __int_as_float(old)) {
+				const int seen = atomicCAS(cell, old, __float_as_int(distance));
+				if (seen == old) break;
+				old = seen;
+			}
+		}
+	}
+}
+
+template <int MODE>
+__device__ void emit_record(const TaskParams &task, uint32_t taskIndex, const FrameTarget &frame, const FrameBuffers &fb,
                             uint32_t recordCapacity, const Corner *c, const float *subB, const float *subC, uint32_t order,
                             uint32_t tri, uint32_t base, uint32_t &emitted) {
+	const int32_t width = frame.width, height = frame.height;
 	int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
 	int32_t bd[4];
 	triangle_bound(fx, fy, bd);
+	if (MODE == SETUP_OCCLUDE) {
+		if (task.filter == 0 && frame.occlusion) occlude_cells(frame, fx, fy, bd, c);
+		return;
+	}
+	// completeOcclusion: commands behind every cell of the grid are not drawn
+	if (frame.occlusion &&
+	    !command_survives(frame.occlusion, frame.gridWidth, frame.gridHeight, frame.gridStride, bd,
+	                      nearest_corner(c[0].cs.z, c[1].cs.z, c[2].cs.z)))
+		return;
 	if (!(bd[0] < width && bd[2] > 0 && bd[1] < height && bd[3] > 0)) return;
-	if (WRITE) {
+	if (MODE == SETUP_WRITE) {
 		const uint32_t index = base + emitted;
 		if (index >= recordCapacity) {
 			atomicOr(fb.errorFlag, ERROR_RECORD_OVERFLOW);
@@ -124,13 +160,13 @@ __device__ void emit_record(const TaskParams &task, uint32_t taskIndex, int32_t 
 }
 
 // renderTriangleFromData / renderTriangleFromDataDepth for one fan triangle (renderCore.cpp:220-341, 400-443).
-template <bool WRITE>
+template <int MODE>
 __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers fb, uint32_t recordCapacity) {
+	const bool WRITE = MODE == SETUP_WRITE;
 	for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < b.totalTriangles; g += gridDim.x * blockDim.x) {
 		const uint32_t k = (uint32_t)find_segment(b.taskTriangleBase, b.taskCount, g);
 		const TaskParams &task = b.tasks[k];
 		const FrameTarget &frame = b.frames[task.frame];
-		const int32_t width = frame.width, height = frame.height;
 		const bool hasTarget = frame.color != nullptr || frame.depth != nullptr;
 		const uint32_t t = g - task.triangleBase;
 		uint32_t emitted = 0;
@@ -159,7 +195,7 @@ __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers 
 			if (triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, true) == 1) {
 				int64_t fx[3] = {c[0].fx, c[1].fx, c[2].fx}, fy[3] = {c[0].fy, c[1].fy, c[2].fy};
 				if (is_frontfacing(fx, fy)) {
-					emit_record<WRITE>(task, k, width, height, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
+					emit_record<MODE>(task, k, frame, fb, recordCapacity, c, task.depthOnly ? zero3 : defaultB,
 					                   task.depthOnly ? zero3 : defaultC, order, t, base, emitted);
 				}
 			} else {
@@ -181,13 +217,13 @@ __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers 
 					if (is_frontfacing(fx, fy)) {
 						float sb[3] = {sv[0]->subB, sv[1]->subB, sv[2]->subB};
 						float scc[3] = {sv[0]->subC, sv[1]->subC, sv[2]->subC};
-						emit_record<WRITE>(task, k, width, height, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
+						emit_record<MODE>(task, k, frame, fb, recordCapacity, sc, task.depthOnly ? zero3 : sb,
 						                   task.depthOnly ? zero3 : scc, order + (uint32_t)f, t, base, emitted);
 					}
 				}
 			}
 		}
-		if (!WRITE) fb.triCounts[g] = emitted;
+		if (MODE == SETUP_COUNT) fb.triCounts[g] = emitted;
 	}
 }
 
@@ -197,14 +233,54 @@ void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream
 		return;
 	}
 	COUNT_LAUNCH();
-	setup_kernel<false><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
+	setup_kernel<SETUP_COUNT><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
 	launch_scan(fb.triCounts, fb.triOffsets, b.totalTriangles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream) {
 	if (b.totalTriangles == 0) return;
 	COUNT_LAUNCH();
-	setup_kernel<true><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, recordCapacity);
+	setup_kernel<SETUP_WRITE><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, recordCapacity);
+}
+
+void launch_setup_occlude(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
+	if (b.totalTriangles == 0) return;
+	COUNT_LAUNCH();
+	setup_kernel<SETUP_OCCLUDE><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
+}
+
+// One thread per cell of the grid: the cell's run of the top pixel row of its cell row.  The
+// reference's runs are [0, 15) for the first cell and [16 g - 1, 16 g + 15) after it, cut at the
+// image's width; perspective depth holds 1 / distance, orthogonal depth the distance itself.
+__global__ void occlusion_top_rows_kernel(float *grid, int32_t gridWidth, int32_t gridHeight, int32_t gridStride,
+                                          const float *__restrict__ depth, int32_t depthStride, int32_t width, int32_t perspective) {
+	const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= gridWidth * gridHeight) return;
+	const int32_t gx = i % gridWidth, gy = i / gridWidth;
+	const float *row = depth + (size_t)(gy * OCCLUSION_CELL) * depthStride;
+	const int32_t start = gx == 0 ? 0 : gx * OCCLUSION_CELL - 1;
+	int32_t end = gx * OCCLUSION_CELL + OCCLUSION_CELL - 1;
+	if (end >= width) end = width;
+	float value;
+	if (perspective) {
+		float maxInv = __int_as_float(0x7F800000);
+		for (int32_t x = start; x < end; x++) if (row[x] < maxInv) maxInv = row[x];
+		value = __fdiv_rn(1.0f, maxInv);
+	} else {
+		value = 0.0f;
+		for (int32_t x = start; x < end; x++) if (row[x] > value) value = row[x];
+	}
+	float &cell = grid[(size_t)gy * gridStride + gx];
+	if (value < cell) cell = value;
+}
+
+void launch_occlusion_top_rows(float *grid, int32_t gridWidth, int32_t gridHeight, int32_t gridStride, const float *depth,
+                               int32_t depthStride, int32_t width, bool perspective, cudaStream_t stream) {
+	const int32_t cells = gridWidth * gridHeight;
+	if (cells <= 0) return;
+	COUNT_LAUNCH();
+	occlusion_top_rows_kernel<<<(cells + 127) / 128, 128, 0, stream>>>(grid, gridWidth, gridHeight, gridStride, depth, depthStride,
+	                                                                 width, perspective ? 1 : 0);
 }
 
 // ------------------------------------------------------------------ scan

@@ -45,6 +45,8 @@ struct FrameTarget {
 	uint32_t *coverage;       // optional per-pixel fragment counts (width * height, dense)
 	uint32_t tileBase;        // the frame's first tile in the batch
 	int32_t tilesX, tilesY;
+	float *occlusion;         // the renderer's occlusion grid (gridWidth x gridHeight cells) or null
+	int32_t gridWidth, gridHeight, gridStride;
 };
 
 // Device tables of a batch.
@@ -105,6 +107,12 @@ void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream
 // Phase B: the records, in submission order (per frame: the order of its tasks, then of their
 // triangles), row offsets (total at rowOffsets[recordCount]) and tile counts (total at offsets[2 * totalTiles]).
 void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream);
+// occludeFromExistingTriangles (api/rendererAPI.cpp:240-255): every solid draw command of the batch
+// whose bound exceeds one cell lowers the occlusion grid of its frame over the cells it covers.
+void launch_setup_occlude(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream);
+// occludeFromTopRows (api/rendererAPI.cpp:417-476) from a device depth image.
+void launch_occlusion_top_rows(float *grid, int32_t gridWidth, int32_t gridHeight, int32_t gridStride, const float *depth,
+                               int32_t depthStride, int32_t width, bool perspective, cudaStream_t stream);
 void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream);
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
 // Phase C: row intervals, tile lists, the persistent tile raster and the per-pixel resolve.

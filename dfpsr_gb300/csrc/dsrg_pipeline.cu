@@ -309,6 +309,43 @@ int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOut
 	return status;
 }
 
+int occlude_enqueue(dsrg_context ctx, BatchJob &job) {
+	cudaStream_t stream = ctx->stream;
+	BatchTotals totals;
+	BatchParams params;
+	memset(&params, 0, sizeof(params));
+	const size_t tableBytes = layout_tables(job, nullptr, nullptr, nullptr, params, totals);
+	if (totals.triangles == 0) return DSRG_OK;
+	TRY(ctx->tables.reserve(tableBytes));
+	if (ctx->pinnedCapacity < tableBytes) {
+		if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
+		ctx->pinnedTables = nullptr;
+		ctx->pinnedCapacity = 0;
+		size_t capacity = 4096;
+		while (capacity < tableBytes) capacity *= 2;
+		TRY(cudaMallocHost((void **)&ctx->pinnedTables, capacity));
+		ctx->pinnedCapacity = capacity;
+	}
+	layout_tables(job, nullptr, ctx->pinnedTables, ctx->tables.ptr, params, totals);
+	TRY(cudaMemcpyAsync(ctx->tables.ptr, ctx->pinnedTables, tableBytes, cudaMemcpyHostToDevice, stream));
+	const size_t np = totals.points;
+	TRY(ctx->csx.reserve(np)); TRY(ctx->csy.reserve(np)); TRY(ctx->csz.reserve(np));
+	TRY(ctx->isx.reserve(np)); TRY(ctx->isy.reserve(np));
+	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
+	FrameBuffers fb;
+	memset(&fb, 0, sizeof(fb));
+	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
+	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
+	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
+	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
+	launch_project(params, fb, stream);
+	launch_setup_occlude(params, fb, stream);
+	TRY(cudaGetLastError());
+	// the page-locked tables are rewritten by the next batch: wait for their copy (and the grid)
+	TRY(cudaStreamSynchronize(stream));
+	return DSRG_OK;
+}
+
 int batch_finish(dsrg_context ctx, const BatchTotals &totals) {
 	cudaStream_t stream = ctx->stream;
 	unsigned long long fragments = 0;

@@ -379,3 +379,107 @@ def light_scene(seed: int = 2024, width: int = 1920, height: int = 1080, sprites
     return LightScene(width, height, camera_tilt, pixels_per_tile, view_index, center,
                       [t[0] for t in types], [t[1] for t in types], [t[2] for t in types], place, light_list,
                       tuple(float(v) for v in sun / np.linalg.norm(sun)), 0.35, (200, 210, 255), caster, cube_resolution)
+
+
+BOX_FACES = np.array([[0, 2, 3, 1], [4, 5, 7, 6], [0, 1, 5, 4], [2, 6, 7, 3], [0, 4, 6, 2], [1, 3, 7, 5]], np.int32)
+
+
+def box_model(rng: np.random.Generator, minimum, maximum, camera: Scene, texture_size: int = 32) -> Scene:
+    """A box of six quads facing outwards, random corner colours and texture coordinates, drawn
+    with `camera`'s camera and target size."""
+    x0, y0, z0 = minimum
+    x1, y1, z1 = maximum
+    positions = np.array([[x0, y0, z0], [x1, y0, z0], [x0, y1, z0], [x1, y1, z0],
+                          [x0, y0, z1], [x1, y0, z1], [x0, y1, z1], [x1, y1, z1]], np.float32)
+    colors = rng.integers(64, 256, size=(6, 4, 4)).astype(np.float32) / np.float32(255.0)
+    colors[:, :, 3] = 1.0
+    tex = rng.uniform(0.0, 1.0, size=(6, 4, 4)).astype(np.float32)
+    return dataclasses.replace(camera, positions=positions, poly_indices=BOX_FACES.copy(), tex_coords=tex, colors=colors,
+                               diffuse=noise_texture(rng, texture_size), diffuse_levels=16, light=None, filter=0,
+                               model_to_world=IDENTITY.copy())
+
+
+def placed(scene: Scene, translation, rotation=None) -> Scene:
+    """The scene with a model-to-world transform (position, then the rotation's x, y and z axes)."""
+    r = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32)
+    t = np.concatenate([np.asarray(translation, np.float32), r[0], r[1], r[2]]).astype(np.float32)
+    return dataclasses.replace(scene, model_to_world=t)
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+    q = q * np.sign(np.diag(r))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q.astype(np.float32)
+
+
+@dataclasses.dataclass
+class OcclusionScene:
+    """A renderer frame for the occlusion grid: a wall in front of the camera, a field of small
+    triangles partly behind it, boxes all over, and a depth image from an earlier pass whose top
+    rows can occlude (renderer_occludeFromTopRows)."""
+    camera: Scene           # camera and target size (no geometry)
+    wall: Scene
+    panel: Scene            # a tilted quad that only occludes through its triangles
+    field: Scene
+    props: list
+    depth: np.ndarray       # (height, width) float32 initial depth buffer
+    color: np.ndarray       # (height, width) uint32 initial colour buffer
+
+    @staticmethod
+    def bound(scene: Scene):
+        """The model's bound as the reference keeps it: grown from the origin (Model.cpp:281-288)."""
+        p = scene.positions
+        return np.minimum(p.min(axis=0), 0.0).astype(np.float32), np.maximum(p.max(axis=0), 0.0).astype(np.float32)
+
+
+def occlusion_scene(seed: int = 77, width: int = 320, height: int = 240, props: int = 24, field_triangles: int = 1500,
+                    perspective: bool = True) -> OcclusionScene:
+    rng = np.random.default_rng(seed)
+    if perspective:
+        slope = float(np.float32(math.tan(math.radians(30.0))))
+        cam = Scene(width, height, np.zeros((0, 3), np.float32), np.zeros((0, 4), np.int32), np.zeros((0, 4, 4), np.float32),
+                    np.zeros((0, 4, 4), np.float32), None, 16, None, 1, 0, camera_location((0.0, 0.0, -6.0), (0.0, 0.0, 1.0)),
+                    True, slope, 0.01, 1000.0, IDENTITY.copy())
+    else:
+        cam = Scene(width, height, np.zeros((0, 3), np.float32), np.zeros((0, 4), np.int32), np.zeros((0, 4, 4), np.float32),
+                    np.zeros((0, 4, 4), np.float32), None, 16, None, 1, 0, camera_location((0.0, 0.0, -6.0), (0.0, 0.0, 1.0)),
+                    False, 4.0, 0.01, 1000.0, IDENTITY.copy())
+    wall = placed(box_model(rng, (-1.5, -1.0, -0.2), (1.5, 1.0, 0.2), cam), (0.0, -0.2, 0.0))
+    panel_points = np.array([[-4.5, 0.6, 2.0], [-1.8, 0.6, 3.5], [-4.5, 3.2, 2.5], [-1.8, 3.2, 4.0]], np.float32)
+    panel = dataclasses.replace(cam, positions=panel_points, poly_indices=np.array([[0, 2, 3, 1]], np.int32),
+                                tex_coords=rng.uniform(0.0, 1.0, size=(1, 4, 4)).astype(np.float32),
+                                colors=np.ones((1, 4, 4), np.float32), diffuse=noise_texture(rng, 32), diffuse_levels=16,
+                                filter=0, model_to_world=IDENTITY.copy())
+    # the field: small triangles scattered over a slab behind and beside the wall
+    n = field_triangles
+    centers = np.stack([rng.uniform(-5.0, 5.0, n), rng.uniform(-3.5, 3.5, n), rng.uniform(1.0, 8.0, n)], axis=1)
+    corners = centers[:, None, :] + rng.uniform(-0.35, 0.35, size=(n, 3, 3))
+    positions = corners.reshape(-1, 3).astype(np.float32)
+    idx = np.arange(n * 3, dtype=np.int32).reshape(n, 3)
+    poly = np.concatenate([idx, -np.ones((n, 1), np.int32)], axis=1)
+    colors = np.zeros((n, 4, 4), np.float32)
+    colors[:, :3, :] = rng.integers(0, 256, size=(n, 3, 4)).astype(np.float32) / np.float32(255.0)
+    tex = np.zeros((n, 4, 4), np.float32)
+    tex[:, :3, :] = rng.uniform(0.0, 1.0, size=(n, 3, 4)).astype(np.float32)
+    field = dataclasses.replace(cam, positions=positions, poly_indices=poly, tex_coords=tex, colors=colors,
+                                diffuse=noise_texture(rng, 32), diffuse_levels=16, filter=0, model_to_world=IDENTITY.copy())
+    prop_list = []
+    for _ in range(props):
+        h = rng.uniform(0.15, 0.4, 3)
+        box = box_model(rng, tuple(-h), tuple(h), cam)
+        where = (rng.uniform(-4.0, 4.0), rng.uniform(-2.5, 2.5), rng.uniform(-2.5, 9.0))
+        prop_list.append(placed(box, where, random_rotation(rng)))
+    # depth of an earlier pass: a near band over the upper left, and near stripes on the top pixel row
+    # of every cell of the right half (only those rows occlude from the top rows, so what lies behind
+    # the stripes is culled although it shows between them); nothing (0, or the far clear value) elsewhere
+    ys, xs = np.mgrid[0:height, 0:width]
+    near = ((ys < height * 0.45) & (xs < width * 0.55)) | ((ys % 16 == 0) & (xs >= width * 0.55))
+    distance = (3.0 + 4.0 * xs / width).astype(np.float32)
+    if perspective:
+        depth = np.where(near, np.float32(1.0) / distance, np.float32(0.0)).astype(np.float32)
+    else:
+        depth = np.where(near, distance, np.float32(1000.0)).astype(np.float32)
+    color = rng.integers(0, 2**32, size=(height, width), dtype=np.uint64).astype(np.uint32)
+    return OcclusionScene(cam, wall, panel, field, prop_list, depth, color)

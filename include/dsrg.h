@@ -135,6 +135,34 @@ int dsrg_renderer_end(dsrg_renderer renderer);
 /* renderer_takesTriangles (api/rendererAPI.h:67): 1 between begin and end. */
 int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
 
+/* The renderer's occlusion grid (api/rendererAPI.h:69-101, rendererAPI.cpp:141-477): one value per
+ * 16x16-pixel cell, the farthest camera-space depth at which something in the cell may still be
+ * visible.  The first occluder of a frame resets it to infinity.  While a frame has occluders,
+ * renderer_give_task skips models whose bounding box is occluded, and renderer_end skips draw
+ * commands behind every cell of their bound.  minimum / maximum are model-space box corners.
+ *   occlude_from_box              renderer_occludeFromBox: the box's screen hull occludes at its
+ *                                 farthest corner (nothing when a corner lies outside the
+ *                                 narrowed view frustum).  debugSilhouette draws the hull at
+ *                                 renderer_end (cyan lines).
+ *   occlude_from_existing_triangles  renderer_occludeFromExistingTriangles: every solid draw
+ *                                 command given so far occludes the cells it covers.
+ *   occlude_from_top_rows         renderer_occludeFromTopRows: the depth image's top pixel row of
+ *                                 each cell row occludes (needs a depth image).
+ *   is_box_visible                renderer_isBoxVisible: *visible = 0 when the box is outside the
+ *                                 view or behind every cell it covers.
+ *   has_occluders                 renderer_hasOccluders: 1 once the frame has an occluder. */
+int dsrg_renderer_occlude_from_box(dsrg_renderer renderer, const float *minimum, const float *maximum,
+                                   const float *modelToWorld, const dsrg_camera *camera, int32_t debugSilhouette);
+int dsrg_renderer_occlude_from_existing_triangles(dsrg_renderer renderer);
+int dsrg_renderer_occlude_from_top_rows(dsrg_renderer renderer, const dsrg_camera *camera);
+int dsrg_renderer_is_box_visible(dsrg_renderer renderer, const float *minimum, const float *maximum,
+                                 const float *modelToWorld, const dsrg_camera *camera, int32_t *visible);
+int dsrg_renderer_has_occluders(dsrg_renderer renderer);
+/* The grid as box tests read it, gridWidth x gridHeight values row by row (no reference
+ * counterpart: the reference keeps the grid private).  out may be null to query the size. */
+int dsrg_renderer_get_occlusion_grid(dsrg_renderer renderer, float *out, int32_t capacity, int32_t *gridWidth,
+                                     int32_t *gridHeight);
+
 /* ---- depth rendering without allocation; this entry point has no counterpart in the reference.
  *
  * For callers that must not allocate GPU memory while they render: a frame loop held to a

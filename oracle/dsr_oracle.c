@@ -835,6 +835,8 @@ typedef struct {
 	shade_data shade;
 	int filter;
 	uint32_t key; /* submission order: triangle index * 8 + clipped sub-triangle index */
+	int32_t task; /* renderer task (camera) of the command */
+	int occluded; /* TriangleDrawCommand::occluded (renderCore.h:67) */
 } command;
 
 typedef struct {
@@ -1557,4 +1559,354 @@ void or_draw_higher(float *targetHeight, int32_t thStride, uint32_t *targetA, in
 			}
 		}
 	}
+}
+
+/* ------------------------------------------------------------------ renderer with an occlusion grid */
+
+/* RendererImpl (api/rendererAPI.cpp:141-477): renderer_begin / renderer_giveTask / the occlusion
+ * grid (occludeFromBox, occludeFromTopRows, occludeFromExistingTriangles, isBoxVisible,
+ * completeOcclusion) / renderer_end.  The grid holds, per 16x16 cell, the largest camera-space
+ * depth at which something may still be visible; commands whose nearest corner is behind it are
+ * not drawn.  Commands are executed in one band (the band split does not change the result). */
+#define OR_CELL 16
+
+struct or_renderer_s {
+	int receiving;
+	uint32_t *color;
+	float *depth;
+	int32_t width, height, packOrder;
+	command_list commands;
+	camera *cams;
+	int32_t camCount, camCapacity;
+	uint32_t triangles;
+	float *grid;
+	int32_t gridAllocWidth, gridAllocHeight; /* the allocated grid (its stride is gridAllocWidth) */
+	int32_t gridWidth, gridHeight;
+	int occluded;
+};
+
+or_renderer *or_renderer_create(void) { return (or_renderer *)calloc(1, sizeof(or_renderer)); }
+
+void or_renderer_destroy(or_renderer *r) {
+	if (!r) return;
+	free(r->commands.items);
+	free(r->cams);
+	free(r->grid);
+	free(r);
+}
+
+int or_renderer_begin(or_renderer *r, uint32_t *color, float *depth, int32_t width, int32_t height, int32_t packOrder) {
+	if (r->receiving) return -1;
+	r->receiving = 1;
+	r->color = color;
+	r->depth = depth;
+	r->width = width;
+	r->height = height;
+	r->packOrder = packOrder;
+	r->gridWidth = (width + (OR_CELL - 1)) / OR_CELL;
+	r->gridHeight = (height + (OR_CELL - 1)) / OR_CELL;
+	r->occluded = 0;
+	r->commands.count = 0;
+	r->camCount = 0;
+	r->triangles = 0;
+	return 0;
+}
+
+/* getOuterCellBound (rendererAPI.cpp:168-179). */
+static irect outer_cell_bound(const or_renderer *r, irect pixelBound) {
+	int32_t minX = pixelBound.left / OR_CELL, maxX = pixelBound.right / OR_CELL + 1;
+	int32_t minY = pixelBound.top / OR_CELL, maxY = pixelBound.bottom / OR_CELL + 1;
+	if (minX < 0) minX = 0;
+	if (minY < 0) minY = 0;
+	if (maxX > r->gridWidth) maxX = r->gridWidth;
+	if (maxY > r->gridHeight) maxY = r->gridHeight;
+	irect out = {minX, minY, maxX, maxY};
+	return out;
+}
+
+static float *grid_cell(const or_renderer *r, int32_t x, int32_t y) { return r->grid + (size_t)y * r->gridAllocWidth + x; }
+
+/* image_readPixel_clamp (api/imageAPI.h:276-282) of the grid image: 0 while no grid exists, and
+ * clamped to the allocated grid, which may be another frame's. */
+static float grid_read(const or_renderer *r, int32_t x, int32_t y) {
+	if (!r->grid || r->gridAllocWidth <= 0 || r->gridAllocHeight <= 0) return 0.0f;
+	if (x < 0) x = 0;
+	if (y < 0) y = 0;
+	if (x > r->gridAllocWidth - 1) x = r->gridAllocWidth - 1;
+	if (y > r->gridAllocHeight - 1) y = r->gridAllocHeight - 1;
+	return *grid_cell(r, x, y);
+}
+
+/* prepareForOcclusion (rendererAPI.cpp:181-191). */
+static void prepare_for_occlusion(or_renderer *r) {
+	if (!r->occluded) {
+		if (!(r->grid && r->gridAllocWidth >= r->gridWidth && r->gridAllocHeight >= r->gridHeight)) {
+			free(r->grid);
+			r->gridAllocWidth = r->gridWidth;
+			r->gridAllocHeight = r->gridHeight;
+			r->grid = (float *)malloc(sizeof(float) * (size_t)(r->gridWidth > 0 ? r->gridWidth : 1) * (size_t)(r->gridHeight > 0 ? r->gridHeight : 1));
+		}
+		for (size_t i = 0; i < (size_t)r->gridAllocWidth * (size_t)r->gridAllocHeight; i++) r->grid[i] = INFINITY;
+	}
+	r->occluded = 1;
+}
+
+/* pointInsideOfEdge / pointInsideOfHull / rectangleInsideOfHull (rendererAPI.cpp:100-130). */
+static int point_inside_hull(const projected *hull, int32_t count, int64_t px, int64_t py) {
+	for (int32_t c = 0; c < count; c++) {
+		int32_t nc = c + 1;
+		if (nc == count) nc = 0;
+		int64_t ex = hull[nc].flat.y - hull[c].flat.y, ey = hull[c].flat.x - hull[nc].flat.x;
+		int64_t rx = px - hull[c].flat.x, ry = py - hull[c].flat.y;
+		if (!(ex * rx + ey * ry <= 0)) return 0;
+	}
+	return 1;
+}
+
+/* occludeFromSortedHull (rendererAPI.cpp:216-239). */
+static void occlude_from_sorted_hull(or_renderer *r, const projected *hull, int32_t count, irect pixelBound) {
+	if ((pixelBound.right - pixelBound.left) > OR_CELL && (pixelBound.bottom - pixelBound.top) > OR_CELL) {
+		float distance = 0.0f;
+		for (int32_t c = 0; c < count; c++) if (hull[c].cs.z > distance) distance = hull[c].cs.z;
+		irect cells = outer_cell_bound(r, pixelBound);
+		for (int32_t cy = cells.top; cy < cells.bottom; cy++) {
+			for (int32_t cx = cells.left; cx < cells.right; cx++) {
+				int64_t left = (int64_t)(cx * OR_CELL * 256), top = (int64_t)(cy * OR_CELL * 256);
+				int64_t right = left + OR_CELL * 256, bottom = top + OR_CELL * 256;
+				if (point_inside_hull(hull, count, left, top) && point_inside_hull(hull, count, right, top) &&
+				    point_inside_hull(hull, count, left, bottom) && point_inside_hull(hull, count, right, bottom)) {
+					if (distance < grid_read(r, cx, cy)) *grid_cell(r, cx, cy) = distance;
+				}
+			}
+		}
+	}
+}
+
+/* getPixelBoundFromProjection (rendererAPI.cpp:92-98). */
+static irect pixel_bound_of(const projected *points, int32_t count) {
+	irect b;
+	b.left = (int32_t)(points[0].flat.x / 256); b.top = (int32_t)(points[0].flat.y / 256);
+	b.right = b.left + 1; b.bottom = b.top + 1;
+	for (int32_t p = 1; p < count; p++) {
+		int32_t x = (int32_t)(points[p].flat.x / 256), y = (int32_t)(points[p].flat.y / 256);
+		if (x < b.left) b.left = x;
+		if (y < b.top) b.top = y;
+		if (x + 1 > b.right) b.right = x + 1;
+		if (y + 1 > b.bottom) b.bottom = y + 1;
+	}
+	return b;
+}
+
+/* jarvisConvexHullAlgorithm (rendererAPI.cpp:38-72). */
+static int counter_clockwise(const projected *p, const projected *q, const projected *s) {
+	return (q->flat.y - p->flat.y) * (s->flat.x - q->flat.x) - (q->flat.x - p->flat.x) * (s->flat.y - q->flat.y) < 0;
+}
+static void jarvis_hull(projected *out, int32_t *outCount, const projected *in, int32_t n) {
+	if (n < 3) {
+		*outCount = n;
+		for (int32_t p = 0; p < n; p++) out[p] = in[p];
+		return;
+	}
+	int32_t l = 0;
+	*outCount = 0;
+	for (int32_t i = 1; i < n; i++) if (in[i].flat.x < in[l].flat.x) l = i;
+	int32_t p = l;
+	do {
+		if (*outCount >= n) return;
+		out[(*outCount)++] = in[p];
+		int32_t q = (p + 1) % n;
+		for (int32_t i = 0; i < n; i++) if (counter_clockwise(&in[p], &in[i], &in[q])) q = i;
+		p = q;
+	} while (p != l);
+}
+
+static void box_corners(const float mn[3], const float mx[3], v3 out[8]) { /* GENERATE_BOX_CORNERS (rendererAPI.cpp:257-265) */
+	out[0] = mk3(mn[0], mn[1], mn[2]); out[1] = mk3(mn[0], mn[1], mx[2]);
+	out[2] = mk3(mn[0], mx[1], mn[2]); out[3] = mk3(mn[0], mx[1], mx[2]);
+	out[4] = mk3(mx[0], mn[1], mn[2]); out[5] = mk3(mx[0], mn[1], mx[2]);
+	out[6] = mk3(mx[0], mx[1], mn[2]); out[7] = mk3(mx[0], mx[1], mx[2]);
+}
+
+int or_renderer_occlude_from_box(or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
+                                 const or_camera_desc *desc, projected_out *silhouette, int32_t *silhouetteCount) {
+	if (silhouetteCount) *silhouetteCount = 0;
+	if (!r->receiving) return -1;
+	prepare_for_occlusion(r);
+	camera cam;
+	camera_create(&cam, desc);
+	v3 local[8];
+	box_corners(mn, mx, local);
+	projected proj[8], hull[8];
+	for (int p = 0; p < 8; p++) { /* projectHull (rendererAPI.cpp:76-90) */
+		v3 cs = world_to_camera(&cam, transform_point(modelToWorld, local[p]));
+		v3 narrow = mk3(cs.x * 0.5f, cs.y * 0.5f, cs.z * 1.0f);
+		for (int s = 0; s < cam.cullCount; s++)
+			if (!plane_inside(&cam.cull[s], narrow)) return 0;
+		proj[p] = camera_to_screen(&cam, cs);
+	}
+	int32_t count = 0;
+	jarvis_hull(hull, &count, proj, 8);
+	occlude_from_sorted_hull(r, hull, count, pixel_bound_of(hull, count));
+	if (silhouette && silhouetteCount) {
+		for (int32_t p = 0; p < count; p++) {
+			silhouette[p].x = hull[p].flat.x; silhouette[p].y = hull[p].flat.y;
+			silhouette[p].z = proj[p].cs.z; /* the reference tests the depth of projections[p], not of the hull corner */
+		}
+		*silhouetteCount = count;
+	}
+	return 0;
+}
+
+int or_renderer_occlude_from_existing_triangles(or_renderer *r) {
+	if (!r->receiving) return -1;
+	prepare_for_occlusion(r);
+	for (size_t t = 0; t < r->commands.count; t++) {
+		const command *c = &r->commands.items[t];
+		if (c->filter == 0) occlude_from_sorted_hull(r, c->triangle.position, 3, c->triangle.wholeBound);
+	}
+	return 0;
+}
+
+/* occludeFromTopRows (rendererAPI.cpp:417-476): the top pixel row of each cell row, in cell-wide
+ * runs that start one pixel early after the first. */
+int or_renderer_occlude_from_top_rows(or_renderer *r, int perspective) {
+	prepare_for_occlusion(r);
+	if (!r->receiving) return -1;
+	if (!r->depth) return -2;
+	for (int32_t gy = 0; gy < r->gridHeight; gy++) {
+		const float *row = r->depth + (size_t)(gy * OR_CELL) * r->width;
+		int32_t x = 0, right = OR_CELL - 1;
+		for (int32_t gx = 0; gx < r->gridWidth; gx++) {
+			if (right >= r->width) right = r->width;
+			float value;
+			if (perspective) {
+				float maxInv = INFINITY;
+				while (x < right) { if (row[x] < maxInv) maxInv = row[x]; x++; }
+				value = 1.0f / maxInv;
+			} else {
+				value = 0.0f;
+				while (x < right) { if (row[x] > value) value = row[x]; x++; }
+			}
+			if (value < *grid_cell(r, gx, gy)) *grid_cell(r, gx, gy) = value;
+			right += OR_CELL;
+		}
+	}
+	return 0;
+}
+
+/* isHullOccluded / isBoxOccluded (rendererAPI.cpp:297-341); returns 1 when visible. */
+int or_renderer_is_box_visible(const or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
+                               const or_camera_desc *desc) {
+	camera cam;
+	camera_create(&cam, desc);
+	v3 local[8], cs[8];
+	projected proj[8];
+	box_corners(mn, mx, local);
+	for (int p = 0; p < 8; p++) {
+		cs[p] = world_to_camera(&cam, transform_point(modelToWorld, local[p]));
+		proj[p] = camera_to_screen(&cam, cs[p]);
+	}
+	for (int s = 0; s < cam.cullCount; s++) {
+		int allOutside = 1;
+		for (int p = 0; p < 8; p++) if (plane_inside(&cam.cull[s], cs[p])) { allOutside = 0; break; }
+		if (allOutside) return 0;
+	}
+	irect pixelBound = pixel_bound_of(proj, 8);
+	float closest = INFINITY;
+	for (int p = 0; p < 8; p++) if (proj[p].cs.z < closest) closest = proj[p].cs.z;
+	irect cells = outer_cell_bound(r, pixelBound);
+	for (int32_t cy = cells.top; cy < cells.bottom; cy++)
+		for (int32_t cx = cells.left; cx < cells.right; cx++)
+			if (closest < grid_read(r, cx, cy)) return 1;
+	return 0;
+}
+
+int or_renderer_has_occluders(const or_renderer *r) { return r->occluded; }
+
+/* model_render_threaded (modelAPI.cpp:214-275): culling, occlusion of the whole model, then one
+ * renderer_giveTask_triangle per fan triangle. */
+int or_renderer_give_task(or_renderer *r, const or_model *model, const float modelToWorld[12], const or_camera_desc *desc) {
+	if (!r->receiving) return -1;
+	camera cam;
+	camera_create(&cam, desc);
+	v3 mn, mx;
+	model_bound(model, &mn, &mx);
+	if (!box_seen(&cam, mn, mx, modelToWorld)) return 0;
+	if (r->occluded) {
+		const float bmn[3] = {mn.x, mn.y, mn.z}, bmx[3] = {mx.x, mx.y, mx.z};
+		if (!or_renderer_is_box_visible(r, bmn, bmx, modelToWorld, desc)) return 0;
+	}
+	if (r->camCount == r->camCapacity) {
+		r->camCapacity = r->camCapacity ? r->camCapacity * 2 : 16;
+		r->cams = (camera *)realloc(r->cams, sizeof(camera) * (size_t)r->camCapacity);
+	}
+	const int32_t taskIndex = r->camCount++;
+	r->cams[taskIndex] = cam;
+	projected *proj = (projected *)malloc(sizeof(projected) * (size_t)(model->pointCount > 0 ? model->pointCount : 1));
+	for (int32_t i = 0; i < model->pointCount; i++) {
+		v3 p = mk3(model->positions[i * 3], model->positions[i * 3 + 1], model->positions[i * 3 + 2]);
+		proj[i] = camera_to_screen(&cam, world_to_camera(&cam, transform_point(modelToWorld, p)));
+	}
+	const size_t before = r->commands.count;
+	for (int32_t p = 0; p < model->polyCount; p++) {
+		const int32_t *idx = model->polyIndices + p * 4;
+		int triCount = (idx[3] < 0) ? 1 : 2;
+		for (int t = 0; t < triCount; t++) {
+			int ia = 0, ib = 1 + t, ic = 2 + t;
+			submit_triangle(&r->commands, &cam, r->color != NULL, r->depth != NULL, r->width, r->height,
+			                proj[idx[ia]], proj[idx[ib]], proj[idx[ic]], model->filter, model->diffuse, model->light,
+			                model->texCoords + (p * 4 + ia) * 4, model->texCoords + (p * 4 + ib) * 4, model->texCoords + (p * 4 + ic) * 4,
+			                model->colors + (p * 4 + ia) * 4, model->colors + (p * 4 + ib) * 4, model->colors + (p * 4 + ic) * 4,
+			                r->triangles);
+			r->triangles++;
+		}
+	}
+	for (size_t i = before; i < r->commands.count; i++) { r->commands.items[i].task = taskIndex; r->commands.items[i].occluded = 0; }
+	free(proj);
+	return 0;
+}
+
+/* completeOcclusion (rendererAPI.cpp:193-214) and CommandQueue::execute of the commands left. */
+int or_renderer_end(or_renderer *r, or_stats *stats) {
+	if (!r->receiving) return -1;
+	r->receiving = 0;
+	if (r->occluded) {
+		for (size_t t = 0; t < r->commands.count; t++) {
+			command *c = &r->commands.items[t];
+			irect cells = outer_cell_bound(r, c->triangle.wholeBound);
+			float depth = c->triangle.position[0].cs.z;
+			if (c->triangle.position[1].cs.z < depth) depth = c->triangle.position[1].cs.z;
+			if (c->triangle.position[2].cs.z < depth) depth = c->triangle.position[2].cs.z;
+			int anyVisible = 0;
+			for (int32_t cy = cells.top; cy < cells.bottom; cy++)
+				for (int32_t cx = cells.left; cx < cells.right; cx++)
+					if ((double)depth < (double)grid_read(r, cx, cy) + 0.001) anyVisible = 1;
+			if (!anyVisible) c->occluded = 1;
+		}
+	}
+	target tg;
+	memset(&tg, 0, sizeof(tg));
+	tg.color = r->color; tg.depth = r->depth; tg.width = r->width; tg.height = r->height;
+	tg.packOrder = r->packOrder; tg.stats = stats;
+	irect imageBound = {0, 0, r->width, r->height};
+	row_interval *rows = NULL;
+	int32_t capacity = 0;
+	for (size_t i = 0; i < r->commands.count; i++) {
+		const command *c = &r->commands.items[i];
+		if (!c->occluded) execute_command(c, &r->cams[c->task], &tg, imageBound, imageBound, &rows, &capacity);
+	}
+	free(rows);
+	if (stats) stats->fragments += tg.fragments;
+	r->commands.count = 0;
+	return 0;
+}
+
+/* The grid as isBoxVisible reads it (for tests); returns whether an occluder was given this frame. */
+int or_renderer_grid(const or_renderer *r, float *out, int32_t *gridWidth, int32_t *gridHeight) {
+	*gridWidth = r->gridWidth;
+	*gridHeight = r->gridHeight;
+	if (!out) return r->occluded;
+	for (int32_t y = 0; y < r->gridHeight; y++)
+		for (int32_t x = 0; x < r->gridWidth; x++) out[(size_t)y * r->gridWidth + x] = grid_read(r, x, y);
+	return r->occluded;
 }

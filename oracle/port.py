@@ -88,6 +88,18 @@ def lib():
         l.or_model_render.restype = C.c_int
         l.or_model_render_depth.argtypes = [C.POINTER(Model), P, C.POINTER(CameraDesc), P, C.POINTER(Stats)]
         l.or_model_render_depth.restype = C.c_int
+        R = C.c_void_p
+        l.or_renderer_create.restype = R
+        l.or_renderer_destroy.argtypes = [R]
+        l.or_renderer_begin.argtypes = [R, P, P, C.c_int32, C.c_int32, C.c_int32]
+        l.or_renderer_give_task.argtypes = [R, C.POINTER(Model), P, C.POINTER(CameraDesc)]
+        l.or_renderer_occlude_from_box.argtypes = [R, P, P, P, C.POINTER(CameraDesc), P, P]
+        l.or_renderer_occlude_from_existing_triangles.argtypes = [R]
+        l.or_renderer_occlude_from_top_rows.argtypes = [R, C.c_int]
+        l.or_renderer_is_box_visible.argtypes = [R, P, P, P, C.POINTER(CameraDesc)]
+        l.or_renderer_has_occluders.argtypes = [R]
+        l.or_renderer_end.argtypes = [R, C.POINTER(Stats)]
+        l.or_renderer_grid.argtypes = [R, P, P, P]
         _lib = l
     return _lib
 
@@ -321,3 +333,75 @@ def draw_higher(target, source, left, top, offset):
     _light_lib().or_draw_higher(th.ctypes.data, W, ta.ctypes.data, W, tap, tb.ctypes.data, W, tbp, W, H, sh.ctypes.data, w,
                                 sa.ctypes.data, w, sap, sb.ctypes.data, w, sbp, w, h, left, top, offset)
     return th, ta, tb
+
+
+class SilhouetteCorner(C.Structure):
+    _fields_ = [("x", C.c_int64), ("y", C.c_int64), ("z", C.c_float)]
+
+
+class OracleRenderer:
+    """renderer_begin / giveTask / the occlusion grid / renderer_end on the CPU oracle
+    (api/rendererAPI.cpp:141-477).  Models are PreparedModel objects; cameras CameraDesc."""
+
+    def __init__(self):
+        self.h = C.c_void_p(lib().or_renderer_create())
+        self._keep = []
+
+    def __del__(self):
+        try:
+            lib().or_renderer_destroy(self.h)
+        except Exception:
+            pass
+
+    def begin(self, color: Optional[np.ndarray], depth: Optional[np.ndarray], pack_order: int = 0):
+        img = color if color is not None else depth
+        h, w = img.shape
+        self.color = None if color is None else np.ascontiguousarray(color, np.uint32).copy()
+        self.depth = None if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+        self._keep = []
+        assert lib().or_renderer_begin(self.h, _ptr(self.color), _ptr(self.depth), w, h, pack_order) == 0
+
+    def give_task(self, pm: "PreparedModel", transform=None, cam: Optional[CameraDesc] = None):
+        t = np.ascontiguousarray(pm.transform if transform is None else transform, np.float32)
+        self._keep.append((pm, t))
+        assert lib().or_renderer_give_task(self.h, C.byref(pm.model), _ptr(t), C.byref(cam or pm.cam)) == 0
+
+    def occlude_from_box(self, mn, mx, transform, cam: CameraDesc):
+        a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        out = (SilhouetteCorner * 8)()
+        n = C.c_int32(0)
+        assert lib().or_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), C.byref(cam), C.cast(out, C.c_void_p),
+                                                  C.cast(C.pointer(n), C.c_void_p)) == 0
+        return [(out[i].x, out[i].y, out[i].z) for i in range(n.value)]
+
+    def occlude_from_existing_triangles(self):
+        assert lib().or_renderer_occlude_from_existing_triangles(self.h) == 0
+
+    def occlude_from_top_rows(self, perspective: bool):
+        return lib().or_renderer_occlude_from_top_rows(self.h, 1 if perspective else 0)
+
+    def is_box_visible(self, mn, mx, transform, cam: CameraDesc) -> bool:
+        a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        return bool(lib().or_renderer_is_box_visible(self.h, _ptr(a), _ptr(b), _ptr(t), C.byref(cam)))
+
+    def has_occluders(self) -> bool:
+        return bool(lib().or_renderer_has_occluders(self.h))
+
+    def grid(self):
+        gw, gh = C.c_int32(0), C.c_int32(0)
+        lib().or_renderer_grid(self.h, None, C.cast(C.pointer(gw), C.c_void_p), C.cast(C.pointer(gh), C.c_void_p))
+        out = np.zeros((gh.value, gw.value), np.float32)
+        lib().or_renderer_grid(self.h, _ptr(out), C.cast(C.pointer(gw), C.c_void_p), C.cast(C.pointer(gh), C.c_void_p))
+        return out
+
+    def end(self, coverage: bool = False):
+        st = Stats()
+        cov = None
+        if coverage:
+            img = self.color if self.color is not None else self.depth
+            cov = np.zeros(img.shape, np.uint32)
+        st.coverage = _ptr(cov)
+        assert lib().or_renderer_end(self.h, C.byref(st)) == 0
+        return self.color, self.depth, {"fragments": int(st.fragments), "coverage": cov}

@@ -71,6 +71,19 @@ def _load(variant: str):
         l.refh_camera_to_screen.argtypes = [P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, P, P, P]
         l.refh_triangle_rows.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_int]
         l.refh_triangle_rows.restype = C.c_int
+        cam = [P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int]
+        l.refh_renderer_create.restype = P
+        l.refh_renderer_free.argtypes = [P]
+        l.refh_renderer_begin.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int]
+        l.refh_renderer_give_task.argtypes = [P, P, P] + cam
+        l.refh_renderer_occlude_from_box.argtypes = [P, P, P, P] + cam
+        l.refh_renderer_occlude_from_existing_triangles.argtypes = [P]
+        l.refh_renderer_occlude_from_top_rows.argtypes = [P] + cam
+        l.refh_renderer_is_box_visible.argtypes = [P, P, P, P] + cam
+        l.refh_renderer_is_box_visible.restype = C.c_int
+        l.refh_renderer_has_occluders.argtypes = [P]
+        l.refh_renderer_has_occluders.restype = C.c_int
+        l.refh_renderer_end.argtypes = [P, C.c_int]
         atexit.register(_shutdown, l)
         _libs[variant] = l
     return _libs[variant]
@@ -244,3 +257,65 @@ def draw_higher(target, source, left, top, offset, variant: str = "exact"):
     _light_lib(variant).refh_draw_higher(_ptr(th), _ptr(ta), tap, _ptr(tb), tbp, W, H, _ptr(sh), _ptr(sa), sap, _ptr(sb), sbp,
                                          w, h, left, top, offset)
     return th, ta, tb
+
+
+def _camera_args(cam):
+    """(location, perspective, slope, near, far, width, height) from a port.CameraDesc."""
+    loc = np.array([cam.location[i] for i in range(12)], np.float32)
+    return loc, [_ptr(loc), int(cam.perspective), float(cam.slope), float(cam.nearClip), float(cam.farClip),
+                 int(cam.width), int(cam.height)]
+
+
+class RefRenderer:
+    """The reference's renderer_* with its occlusion grid; models are RefModel objects and cameras
+    port.CameraDesc structures."""
+
+    def __init__(self, variant: str = "exact"):
+        self.lib = _load(variant)
+        self.h = self.lib.refh_renderer_create()
+
+    def __del__(self):
+        if _shut_down:
+            return
+        try:
+            self.lib.refh_renderer_free(self.h)
+        except Exception:
+            pass
+
+    def begin(self, color, depth, pack_order: int = 0):
+        img = color if color is not None else depth
+        h, w = img.shape
+        self.color = None if color is None else np.ascontiguousarray(color, np.uint32).copy()
+        self.depth = None if depth is None else np.ascontiguousarray(depth, np.float32).copy()
+        self.lib.refh_renderer_begin(self.h, _ptr(self.color), _ptr(self.depth), w, h, pack_order)
+
+    def give_task(self, model: "RefModel", transform, cam):
+        t = np.ascontiguousarray(transform, np.float32)
+        loc, args = _camera_args(cam)
+        self.lib.refh_renderer_give_task(self.h, model.handle, _ptr(t), *args)
+
+    def occlude_from_box(self, mn, mx, transform, cam):
+        a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        loc, args = _camera_args(cam)
+        self.lib.refh_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), *args)
+
+    def occlude_from_existing_triangles(self):
+        self.lib.refh_renderer_occlude_from_existing_triangles(self.h)
+
+    def occlude_from_top_rows(self, cam):
+        loc, args = _camera_args(cam)
+        self.lib.refh_renderer_occlude_from_top_rows(self.h, *args)
+
+    def is_box_visible(self, mn, mx, transform, cam) -> bool:
+        a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
+        t = np.ascontiguousarray(transform, np.float32)
+        loc, args = _camera_args(cam)
+        return bool(self.lib.refh_renderer_is_box_visible(self.h, _ptr(a), _ptr(b), _ptr(t), *args))
+
+    def has_occluders(self) -> bool:
+        return bool(self.lib.refh_renderer_has_occluders(self.h))
+
+    def end(self, debug_wireframe: bool = False):
+        self.lib.refh_renderer_end(self.h, 1 if debug_wireframe else 0)
+        return self.color, self.depth

@@ -183,6 +183,97 @@ int refh_model_render_depth(void* modelHandle, const float* modelToWorld, const 
 	return 0;
 }
 
+// ---- a renderer with the occlusion grid (api/rendererAPI.h:46-135, modelAPI.h:299-301)
+
+namespace {
+struct RendererBox {
+	Renderer renderer;
+	ImageRgbaU8 color;
+	ImageF32 depth;
+	uint32_t* colorOut = nullptr;
+	float* depthOut = nullptr;
+	int width = 0, height = 0;
+};
+struct CameraArgs { const float* location; int perspective; float slope, nearClip, farClip; int width, height; };
+Camera makeCamera(const CameraArgs& c) { return makeCamera(c.location, c.perspective, c.slope, c.width, c.height, c.nearClip, c.farClip); }
+} // namespace
+
+void* refh_renderer_create() {
+	RendererBox* box = new RendererBox();
+	box->renderer = renderer_create();
+	return box;
+}
+
+void refh_renderer_free(void* handle) { delete (RendererBox*)handle; }
+
+// Images are copied in at begin and out at end (color, depth: width x height, either may be null).
+void refh_renderer_begin(void* handle, uint32_t* color, float* depth, int width, int height, int packOrder) {
+	RendererBox* box = (RendererBox*)handle;
+	box->color = ImageRgbaU8();
+	box->depth = ImageF32();
+	box->colorOut = nullptr;
+	box->depthOut = nullptr;
+	box->width = width;
+	box->height = height;
+	if (color) {
+		box->color = image_create_RgbaU8_native(width, height, PackOrderIndex(packOrder));
+		copyInRgba(box->color, color, width, height);
+		box->colorOut = color;
+	}
+	if (depth) {
+		box->depth = image_create_F32(width, height);
+		copyInF32(box->depth, depth, width, height);
+		box->depthOut = depth;
+	}
+	renderer_begin(box->renderer, box->color, box->depth);
+}
+
+void refh_renderer_give_task(void* handle, void* modelHandle, const float* modelToWorld, const float* cameraLocation,
+                             int perspective, float slope, float nearClip, float farClip, int width, int height) {
+	RendererBox* box = (RendererBox*)handle;
+	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
+	renderer_giveTask(box->renderer, ((ModelBox*)modelHandle)->model, makeTransform(modelToWorld), makeCamera(c));
+}
+
+void refh_renderer_occlude_from_box(void* handle, const float* mn, const float* mx, const float* modelToWorld,
+                                    const float* cameraLocation, int perspective, float slope, float nearClip, float farClip,
+                                    int width, int height) {
+	RendererBox* box = (RendererBox*)handle;
+	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
+	renderer_occludeFromBox(box->renderer, FVector3D(mn[0], mn[1], mn[2]), FVector3D(mx[0], mx[1], mx[2]),
+	                        makeTransform(modelToWorld), makeCamera(c), false);
+}
+
+void refh_renderer_occlude_from_existing_triangles(void* handle) {
+	renderer_occludeFromExistingTriangles(((RendererBox*)handle)->renderer);
+}
+
+void refh_renderer_occlude_from_top_rows(void* handle, const float* cameraLocation, int perspective, float slope,
+                                         float nearClip, float farClip, int width, int height) {
+	RendererBox* box = (RendererBox*)handle;
+	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
+	renderer_occludeFromTopRows(box->renderer, makeCamera(c));
+}
+
+int refh_renderer_is_box_visible(void* handle, const float* mn, const float* mx, const float* modelToWorld,
+                                 const float* cameraLocation, int perspective, float slope, float nearClip, float farClip,
+                                 int width, int height) {
+	RendererBox* box = (RendererBox*)handle;
+	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
+	return renderer_isBoxVisible(box->renderer, FVector3D(mn[0], mn[1], mn[2]), FVector3D(mx[0], mx[1], mx[2]),
+	                             makeTransform(modelToWorld), makeCamera(c)) ? 1 : 0;
+}
+
+int refh_renderer_has_occluders(void* handle) { return renderer_hasOccluders(((RendererBox*)handle)->renderer) ? 1 : 0; }
+
+// renderer_end, then copies the images out.
+void refh_renderer_end(void* handle, int debugWireframe) {
+	RendererBox* box = (RendererBox*)handle;
+	renderer_end(box->renderer, debugWireframe != 0);
+	if (box->colorOut) copyOutRgba(box->color, box->colorOut, box->width, box->height);
+	if (box->depthOut) copyOutF32(box->depth, box->depthOut, box->width, box->height);
+}
+
 // Projects one camera-space point the way the reference does (Camera::cameraToScreen).
 // out = is.x, is.y ; outFlat = flat.x, flat.y
 void refh_camera_to_screen(const float* cameraLocation, int perspective, float slope, float nearClip, float farClip,

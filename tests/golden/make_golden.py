@@ -5,6 +5,10 @@ texture_kats.json
     The known-answer assertions of the reference's own texture test
     (Source/test/tests/TextureTest.cpp), read from that file as text: pyramid fields,
     texel offsets, pixel reads after writes, nearest sampling and the 8-bit linear mix.
+occlusion_sessions.json
+    The renderer session of tests/occlusion_script.py (occlusion grid: box occluders, existing
+    triangles, top rows, box tests, two frames) played by the reference: its answers and the
+    sha256 of its images, for seeded scenes whose inputs are identified by their own digest.
 render_*.npz
     Small seeded scenes (inputs stored in the file) rendered by the reference itself, built
     from its sources as the exact (scalar, no-FMA) variant by oracle/Makefile.ref, through
@@ -202,6 +206,46 @@ def save_case(name, scene, variant="exact"):
     np.savez_compressed(os.path.join(HERE, f"render_{name}.npz"), **payload)
 
 
+OCCLUSION_CASES = {"perspective": dict(seed=77, width=160, height=120, props=16, field_triangles=600, perspective=True),
+                   "orthogonal": dict(seed=78, width=160, height=120, props=16, field_triangles=600, perspective=False)}
+
+
+def scene_digest(sc):
+    """sha256 of a session's inputs, so that a change of the seeded generator is caught."""
+    import hashlib
+    h = hashlib.sha256()
+    for s in [sc.camera, sc.wall, sc.panel, sc.field] + list(sc.props):
+        for a in (s.positions, s.poly_indices, s.tex_coords, s.colors, s.camera_location, s.model_to_world):
+            h.update(np.ascontiguousarray(a).tobytes())
+        if s.diffuse is not None:
+            h.update(np.ascontiguousarray(s.diffuse).tobytes())
+    h.update(sc.depth.tobytes())
+    h.update(sc.color.tobytes())
+    return h.hexdigest()
+
+
+def image_digest(a):
+    import hashlib
+    return None if a is None else hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def occlusion_sessions():
+    """The occlusion-grid session of tests/occlusion_script.py played by the reference itself:
+    box-test answers, hasOccluders and digests of every frame's images."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import occlusion_script
+    from dfpsr_gb300 import scenes
+    out = {}
+    for name, params in OCCLUSION_CASES.items():
+        sc = scenes.occlusion_scene(**params)
+        for use_color, use_depth in ((True, True), (True, False), (False, True)):
+            r = occlusion_script.play(occlusion_script.RefEngine(), sc, use_color=use_color, use_depth=use_depth)
+            out[f"{name}_c{int(use_color)}d{int(use_depth)}"] = dict(
+                params=params, use_color=use_color, use_depth=use_depth, inputs=scene_digest(sc), visible=r["visible"],
+                has_occluders=r["has_occluders"], frames=[[image_digest(f[0]), image_digest(f[1])] for f in r["frames"]])
+    return out
+
+
 def main():
     reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DFPSR_REFERENCE", "/root/reference")
     from oracle import ref
@@ -213,6 +257,9 @@ def main():
     for name, scene in render_cases().items():
         save_case(name, scene)
         print("wrote", name)
+    with open(os.path.join(HERE, "occlusion_sessions.json"), "w") as f:
+        json.dump(occlusion_sessions(), f, indent=1)
+    print("wrote occlusion_sessions")
 
 
 if __name__ == "__main__":

@@ -121,3 +121,23 @@ def test_gpu_texture_fields_match_known_answers(ctx):
         for name in ("startOffset", "maxLevelMask"):
             if name in block["fields"]:
                 assert got[name] == block["fields"][name]
+
+
+def test_oracle_occlusion_sessions(built):
+    """The oracle plays the occlusion-grid sessions the reference played for the fixture."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_golden
+    import occlusion_script as o
+    from dfpsr_gb300 import scenes
+    with open(os.path.join(GOLDEN, "occlusion_sessions.json")) as f:
+        sessions = json.load(f)
+    assert len(sessions) == 6
+    for name, expect in sessions.items():
+        sc = scenes.occlusion_scene(**expect["params"])
+        assert make_golden.scene_digest(sc) == expect["inputs"], f"{name}: the seeded inputs changed"
+        got = o.play(o.OracleEngine(), sc, use_color=expect["use_color"], use_depth=expect["use_depth"])
+        assert got["visible"] == expect["visible"], name
+        assert got["has_occluders"] == expect["has_occluders"], name
+        frames = [[make_golden.image_digest(f[0]), make_golden.image_digest(f[1])] for f in got["frames"]]
+        assert frames == expect["frames"], name

@@ -67,3 +67,16 @@ def test_row_intervals_equal_reference(ref_lib):
         b = port.triangle_rows(f, clip)
         assert a[0] == b[0] or len(a[1]) == 0
         assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("perspective", [True, False])
+@pytest.mark.parametrize("targets", [(True, True), (True, False), (False, True)])
+def test_oracle_occlusion_session_equals_reference(ref_lib, perspective, targets):
+    """renderer_occludeFromBox / FromExistingTriangles / FromTopRows, isBoxVisible, hasOccluders and
+    renderer_end with completeOcclusion, two frames on one renderer (tests/occlusion_script.py)."""
+    import occlusion_script as o
+    sc = scenes.occlusion_scene(perspective=perspective)
+    a = o.play(o.OracleEngine(), sc, use_color=targets[0], use_depth=targets[1])
+    b = o.play(o.RefEngine(), sc, use_color=targets[0], use_depth=targets[1])
+    o.assert_same(a, b, f"perspective {perspective} targets {targets}")
+    assert 0 < sum(a["visible"]) < len(a["visible"])  # some boxes occluded, some not
