@@ -24,7 +24,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "OUT_OF_MEMORY", 4
 EXPORTED = [
     "dsrg_context_create", "dsrg_context_destroy", "dsrg_context_last_error", "dsrg_context_stream",
     "dsrg_context_set_counting", "dsrg_context_get_stats",
-    "dsrg_texture_create", "dsrg_texture_destroy", "dsrg_texture_read",
+    "dsrg_texture_create", "dsrg_texture_destroy", "dsrg_texture_read", "dsrg_texture_create_many",
     "dsrg_model_create", "dsrg_model_destroy",
     "dsrg_model_render", "dsrg_model_render_depth",
     "dsrg_renderer_create", "dsrg_renderer_destroy", "dsrg_renderer_begin", "dsrg_renderer_give_task",
@@ -115,6 +115,7 @@ def lib():
         l.dsrg_texture_create.argtypes = [P, P, I, I, I, C.POINTER(P)]
         l.dsrg_texture_destroy.argtypes = [P]
         l.dsrg_texture_read.argtypes = [P, P, I, P, C.POINTER(I)]
+        l.dsrg_texture_create_many.argtypes = [P, I, C.POINTER(Image), P, C.POINTER(P)]
         l.dsrg_model_create.argtypes = [P, P, I, P, P, P, I, P, P, I, C.POINTER(P)]
         l.dsrg_model_destroy.argtypes = [P]
         l.dsrg_model_render.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image), C.POINTER(Image)]
@@ -348,14 +349,34 @@ class Context:
 
 
 class Texture:
-    def __init__(self, ctx: Context, pixels: np.ndarray, resolutions: int = 16):
+    def __init__(self, ctx: Context, pixels: Optional[np.ndarray], resolutions: int = 16, handle=None):
         self.ctx = ctx
-        pixels = np.ascontiguousarray(pixels, np.uint32)
-        h = C.c_void_p()
-        ctx._check(ctx._l.dsrg_texture_create(ctx.handle, pixels.ctypes.data, pixels.shape[1], pixels.shape[0],
-                                              resolutions, C.byref(h)))
-        self.handle = h
+        if handle is None:
+            pixels = np.ascontiguousarray(pixels, np.uint32)
+            handle = C.c_void_p()
+            ctx._check(ctx._l.dsrg_texture_create(ctx.handle, pixels.ctypes.data, pixels.shape[1], pixels.shape[0],
+                                                  resolutions, C.byref(handle)))
+        self.handle = handle
         ctx._adopt(self)
+
+    @staticmethod
+    def create_many(ctx: Context, images, resolutions) -> list:
+        """dsrg_texture_create_many: images are (height, width) uint32 numpy arrays (host) or int32
+        torch tensors (device); resolutions an int or one per image."""
+        n = len(images)
+        res = [int(resolutions)] * n if np.isscalar(resolutions) else [int(r) for r in resolutions]
+        structs = (Image * n)()
+        keep = []
+        for i, im in enumerate(images):
+            if not hasattr(im, "data_ptr"):
+                im = np.ascontiguousarray(im, np.uint32)
+            keep.append(im)
+            structs[i] = image_struct(im, 0)
+        r = np.array(res, np.int32)
+        out = (C.c_void_p * n)()
+        _torch_sync()
+        ctx._check(ctx._l.dsrg_texture_create_many(ctx.handle, n, structs, r.ctypes.data, out))
+        return [Texture(ctx, None, handle=C.c_void_p(out[i])) for i in range(n)]
 
     def read(self):
         fields = np.zeros(9, np.uint32)

@@ -85,97 +85,7 @@ int dsrg_context_get_stats(dsrg_context ctx, dsrg_stats *out) {
 
 // ------------------------------------------------------------------ textures
 
-int dsrg_texture_create(dsrg_context ctx, const uint32_t *pixels, int32_t width, int32_t height, int32_t resolutions,
-                        dsrg_texture *out) {
-	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
-	*out = nullptr;
-	if (resolutions < 1) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture without any resolutions stored, which would be empty!");
-	if (width < 1 || height < 1 || !pixels) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture of an empty image!");
-	if (width > 32768 || height > 32768) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture exceeding the maximum texture dimensions of 32768 x 32768 pixels!");
-	uint32_t lw = 0, lh = 0;
-	while ((1u << lw) < (uint32_t)width) lw++;
-	while ((1u << lh) < (uint32_t)height) lh++;
-	if ((1u << lw) != (uint32_t)width || (1u << lh) != (uint32_t)height)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "Texture dimensions must be powers of two (other sizes are resampled by filter_resize, which is not part of the GPU path)");
-	// Texture constructor (implementation/image/Texture.h:66-101)
-	uint32_t maxMip = (uint32_t)(resolutions - 1);
-	if (maxMip > lw) maxMip = lw;
-	if (maxMip > lh) maxMip = lh;
-	if (maxMip > 15u) maxMip = 15u;
-	uint32_t highest = 1u << (lw + lh);
-	uint64_t pixelCount = 0;
-	uint32_t levelCount = highest;
-	for (int32_t level = (int32_t)maxMip; level >= 0; level--) { pixelCount |= levelCount; levelCount >>= 2; }
-	dsrg_texture tex = new (std::nothrow) dsrg_texture_s();
-	if (!tex) return DSRG_ERROR_OUT_OF_MEMORY;
-	tex->context = ctx;
-	tex->pixelCount = (uint32_t)pixelCount;
-	uint32_t startOffset = (uint32_t)pixelCount & ~highest;
-	uint32_t f[9] = {lw, lh, maxMip, startOffset, highest - 1, (1u << (lw - maxMip)) - 1, (1u << (lh - maxMip)) - 1,
-	                 (1u << lw) - 1, (1u << lh) - 1};
-	memcpy(tex->fields, f, sizeof(f));
-	// texture_generatePyramid: integer 2x2 box average level by level (api/textureAPI.cpp:44-87)
-	std::vector<uint32_t> pyramid(pixelCount, 0u);
-	memcpy(pyramid.data() + startOffset, pixels, sizeof(uint32_t) * (size_t)width * height);
-	auto layer = [&](uint32_t mip) { return startOffset & ((highest - 1) >> (mip << 1)); };
-	for (uint32_t level = 1; level <= maxMip; level++) {
-		uint32_t w = 1u << (lw - level), h = 1u << (lh - level);
-		uint32_t sw = w * 2;
-		const uint32_t *src = pyramid.data() + layer(level - 1);
-		uint32_t *dst = pyramid.data() + layer(level);
-		for (uint32_t y = 0; y < h; y++) {
-			for (uint32_t x = 0; x < w; x++) {
-				uint32_t c[4] = {src[(y * 2) * sw + x * 2], src[(y * 2) * sw + x * 2 + 1], src[(y * 2 + 1) * sw + x * 2],
-				                 src[(y * 2 + 1) * sw + x * 2 + 1]};
-				uint32_t o = 0;
-				for (int ch = 0; ch < 4; ch++) {
-					uint32_t s = 0;
-					for (int i = 0; i < 4; i++) s += (c[i] >> (ch * 8)) & 0xFFu;
-					o |= (s / 4) << (ch * 8);
-				}
-				dst[y * w + x] = o;
-			}
-		}
-	}
-	cudaSetDevice(ctx->device);
-	if (cudaMalloc((void **)&tex->pixels, sizeof(uint32_t) * pixelCount) != cudaSuccess) {
-		delete tex;
-		return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "cudaMalloc failed for a texture pyramid");
-	}
-	if (cudaMemcpy(tex->pixels, pyramid.data(), sizeof(uint32_t) * pixelCount, cudaMemcpyHostToDevice) != cudaSuccess) {
-		cudaFree(tex->pixels);
-		delete tex;
-		return fail(ctx, DSRG_ERROR_CUDA, "cudaMemcpy failed for a texture pyramid");
-	}
-	TextureData &d = tex->data;
-	d.pixels = tex->pixels;
-	d.log2width = lw; d.log2height = lh; d.maxMipLevel = maxMip; d.startOffset = startOffset; d.maxLevelMask = highest - 1;
-	d.maxWidthAndMask = (1u << lw) - 1; d.maxHeightAndMask = (1u << lh) - 1;
-	d.floatMaxWidth = (float)(1u << lw); d.floatMaxHeight = (float)(1u << lh);
-	d.exists = 1;
-	*out = tex;
-	return DSRG_OK;
-}
-
-int dsrg_texture_destroy(dsrg_texture tex) {
-	if (!tex) return DSRG_ERROR_INVALID_ARGUMENT;
-	cudaSetDevice(tex->context->device);
-	cudaStreamSynchronize(tex->context->stream);
-	cudaFree(tex->pixels);
-	delete tex;
-	return DSRG_OK;
-}
-
-int dsrg_texture_read(dsrg_texture tex, uint32_t *pixels, int32_t maxPixels, uint32_t *fields, int32_t *count) {
-	if (!tex) return DSRG_ERROR_INVALID_ARGUMENT;
-	if (fields) memcpy(fields, tex->fields, sizeof(tex->fields));
-	if (count) *count = (int32_t)tex->pixelCount;
-	if (pixels && maxPixels > 0) {
-		size_t n = (size_t)maxPixels < tex->pixelCount ? (size_t)maxPixels : tex->pixelCount;
-		CUDA_TRY(tex->context, cudaMemcpy(pixels, tex->pixels, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-	}
-	return DSRG_OK;
-}
+// texture creation, destruction and reading live in dsrg_texture.cu
 
 // ------------------------------------------------------------------ models
 

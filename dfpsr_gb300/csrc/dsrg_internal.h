@@ -175,6 +175,8 @@ struct dsrg_context_s {
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
 	DeviceBuffer<TextureData> textureTable;
 	DeviceBuffer<uint32_t> stagingColor;
+	DeviceBuffer<uint32_t> textureStaging;      // texture creation: host images and two-step resize halves
+	DeviceBuffer<unsigned char> textureTables;  // texture creation: work tables
 	DeviceBuffer<float> stagingDepth;
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;

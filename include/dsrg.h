@@ -93,11 +93,17 @@ int dsrg_context_set_counting(dsrg_context context, int32_t counting, uint32_t *
 int dsrg_context_get_stats(dsrg_context context, dsrg_stats *out);
 
 /* ---- textures: texture_create_RgbaU8(image, resolutions) (api/textureAPI.h:450-465,
- * api/textureAPI.cpp:89-131) for power-of-two images; the mip pyramid is the integer 2x2 box
- * average of texture_generatePyramid (api/textureAPI.cpp:44-87). pixels: width*height RGBA
- * bytes in memory order, host memory. ---- */
+ * api/textureAPI.cpp:89-131), built on the GPU: the image is resized linearly to the next powers
+ * of two (filter_resize with Sampler::Linear, api/filterAPI.cpp:852-859) into level 0, and the mip
+ * pyramid is the integer 2x2 box average of texture_generatePyramid (api/textureAPI.cpp:44-87).
+ * pixels: width*height RGBA bytes in memory order, host memory. ---- */
 int dsrg_texture_create(dsrg_context context, const uint32_t *pixels, int32_t width, int32_t height,
                         int32_t resolutions, dsrg_texture *out);
+/* dsrg_texture_create for count images at once (host or device memory, RGBA pack order, any
+ * stride), with resolutions[i] levels for image i; every phase (resize, each pyramid level) runs
+ * as one launch over all images.  On failure no texture is made and out[] is all null. */
+int dsrg_texture_create_many(dsrg_context context, int32_t count, const dsrg_image *images, const int32_t *resolutions,
+                             dsrg_texture *out);
 int dsrg_texture_destroy(dsrg_texture texture);
 /* Copies the pyramid (smallest level first) to host memory; fields = log2width, log2height,
  * maxMipLevel, startOffset, maxLevelMask, minWidthOrMask, minHeightOrMask, maxWidthAndMask,

@@ -472,16 +472,127 @@ void or_texture_generate_pyramid(or_texture *t) {
 	}
 }
 
-/* texture_create_RgbaU8(image, resolutions) for power-of-two images (textureAPI.cpp:89-110, 112-131).
- * Non-power-of-two inputs would go through filter_resize, which is outside this path. */
+/* ---- filter_resize(image, Sampler::Linear, width, height) of RGBA images (api/filterAPI.cpp:66-311,
+ * 852-859), for images that are neither sub-images nor of another pack order, as texture creation
+ * passes them.  Sampling positions are 16.16 fixed point: offset = 65536 * source / target pixels,
+ * start = offset / 2 - 32768, clamped at 0, the integer part the left or upper sample. */
+
+static uint32_t resize_read(const uint32_t *img, int32_t w, int32_t h, int32_t x, int32_t y) { /* image_readPixel_clamp */
+	if (x < 0) x = 0;
+	if (y < 0) y = 0;
+	if (x > w - 1) x = w - 1;
+	if (y > h - 1) y = h - 1;
+	return img[(size_t)y * w + x];
+}
+
+static int32_t resize_offset(int32_t source, int32_t target) { return (int32_t)((65536u * (uint32_t)source) / (uint32_t)target); }
+
+/* Vertical only (resize_optimized, the SIMD_ALIGNED branch): mixColorsUniform with an 8-bit weight. */
+static void resize_vertical(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sh) {
+	int32_t offsetY = resize_offset(sh, h);
+	int32_t readY = (int32_t)((uint32_t)(offsetY / 2) - 32768u);
+	for (int32_t y = 0; y < h; y++) {
+		uint32_t sampleY = (uint32_t)(readY < 0 ? 0 : readY);
+		uint32_t upperY = sampleY >> 16, lowerY = upperY + 1;
+		if (upperY >= (uint32_t)sh) upperY = (uint32_t)sh - 1;
+		if (lowerY >= (uint32_t)sh) lowerY = (uint32_t)sh - 1;
+		uint32_t ratio = (sampleY & 0xFFFFu) >> 8, inv = 256u - ratio;
+		for (int32_t x = 0; x < w; x++) {
+			uint32_t a = src[(size_t)upperY * w + x], b = src[(size_t)lowerY * w + x], out = 0;
+			for (int ch = 0; ch < 4; ch++)
+				out |= ((((a >> (ch * 8)) & 0xFFu) * inv + ((b >> (ch * 8)) & 0xFFu) * ratio) >> 8) << (ch * 8);
+			dst[(size_t)y * w + x] = out;
+		}
+		readY += offsetY;
+	}
+}
+
+static uint32_t saturate_pack(const uint32_t c[4]) { /* image_saturateAndPack, RGBA */
+	uint32_t out = 0;
+	for (int ch = 0; ch < 4; ch++) out |= (c[ch] > 255u ? 255u : c[ch]) << (ch * 8);
+	return out;
+}
+
+/* Horizontal only (resize_optimized): 16-bit weights per channel. */
+static void resize_horizontal(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw) {
+	int32_t offsetX = resize_offset(sw, w);
+	int32_t startX = (int32_t)((uint32_t)(offsetX / 2) - 32768u);
+	for (int32_t y = 0; y < h; y++) {
+		int32_t readX = startX;
+		for (int32_t x = 0; x < w; x++) {
+			uint32_t sampleX = (uint32_t)(readX < 0 ? 0 : readX);
+			uint32_t leftX = sampleX >> 16;
+			uint32_t rightRatio = sampleX & 0xFFFFu, leftRatio = 65536u - rightRatio;
+			uint32_t l = resize_read(src, sw, h, (int32_t)leftX, y), r = resize_read(src, sw, h, (int32_t)(leftX + 1), y), c[4];
+			for (int ch = 0; ch < 4; ch++) c[ch] = (((l >> (ch * 8)) & 0xFFu) * leftRatio + ((r >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
+			dst[(size_t)y * w + x] = saturate_pack(c);
+			readX += offsetX;
+		}
+	}
+}
+
+/* Both dimensions (resize_reference with samplePixel<true>): bilinear with 16-bit weights. */
+static void resize_both(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+	int32_t offsetX = resize_offset(sw, w), offsetY = resize_offset(sh, h);
+	int32_t startX = (int32_t)((uint32_t)(offsetX / 2) - 32768u);
+	int32_t readY = (int32_t)((uint32_t)(offsetY / 2) - 32768u);
+	for (int32_t y = 0; y < h; y++) {
+		uint32_t sampleY = (uint32_t)(readY < 0 ? 0 : readY);
+		uint32_t upperY = sampleY >> 16, lowerRatio = sampleY & 0xFFFFu, upperRatio = 65536u - lowerRatio;
+		int32_t readX = startX;
+		for (int32_t x = 0; x < w; x++) {
+			uint32_t sampleX = (uint32_t)(readX < 0 ? 0 : readX);
+			uint32_t leftX = sampleX >> 16, rightRatio = sampleX & 0xFFFFu, leftRatio = 65536u - rightRatio;
+			uint32_t ul = resize_read(src, sw, sh, (int32_t)leftX, (int32_t)upperY), ur = resize_read(src, sw, sh, (int32_t)(leftX + 1), (int32_t)upperY);
+			uint32_t ll = resize_read(src, sw, sh, (int32_t)leftX, (int32_t)(upperY + 1)), lr = resize_read(src, sw, sh, (int32_t)(leftX + 1), (int32_t)(upperY + 1));
+			uint32_t c[4];
+			for (int ch = 0; ch < 4; ch++) {
+				uint32_t upper = (((ul >> (ch * 8)) & 0xFFu) * leftRatio + ((ur >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
+				uint32_t lower = (((ll >> (ch * 8)) & 0xFFu) * leftRatio + ((lr >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
+				c[ch] = (upper * upperRatio + lower * lowerRatio) >> 16;
+			}
+			dst[(size_t)y * w + x] = saturate_pack(c);
+			readX += offsetX;
+		}
+		readY += offsetY;
+	}
+}
+
+/* resize_optimized's choice for one step (filterAPI.cpp:157-260). */
+static void resize_step(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+	if (sw == w && sh == h) memcpy(dst, src, sizeof(uint32_t) * (size_t)w * (size_t)h);
+	else if (sw == w) resize_vertical(dst, w, h, src, sh);
+	else if (sh == h) resize_horizontal(dst, w, h, src, sw);
+	else resize_both(dst, w, h, src, sw, sh);
+}
+
+/* resizeToTarget (filterAPI.cpp:298-314): a wider and taller target goes through a horizontal step
+ * to the target's width first. */
+void or_filter_resize_linear(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+	if (w != sw && h > sh) {
+		uint32_t *temp = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)w * (size_t)sh);
+		resize_step(temp, w, sh, src, sw, sh);
+		resize_step(dst, w, h, temp, w, sh);
+		free(temp);
+	} else {
+		resize_step(dst, w, h, src, sw, sh);
+	}
+}
+
+/* findLog2Size (textureAPI.cpp:30-40). */
+static uint32_t find_log2_size(uint32_t size) {
+	for (uint32_t l = 0; l < 15u; l++) if (((uint32_t)1 << l) >= size) return l;
+	return 15u;
+}
+
+/* texture_create_RgbaU8(image, resolutions) (textureAPI.cpp:89-110, 112-131): the image resized
+ * linearly to the next powers of two, then the pyramid. */
 int or_texture_create_from_image(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions) {
-	uint32_t lw = 0, lh = 0;
-	while (((uint32_t)1 << lw) < (uint32_t)width && lw < 15) lw++;
-	while (((uint32_t)1 << lh) < (uint32_t)height && lh < 15) lh++;
-	if (((uint32_t)1 << lw) != (uint32_t)width || ((uint32_t)1 << lh) != (uint32_t)height || resolutions < 1) return -1;
+	if (resolutions < 1 || width < 1 || height < 1 || width > 32768 || height > 32768) return -1;
+	uint32_t lw = find_log2_size((uint32_t)width), lh = find_log2_size((uint32_t)height);
 	if (or_texture_init_empty(t, lw, lh, (uint32_t)(resolutions - 1))) return -1;
 	uint32_t base = or_texture_pixel_offset_to_layer(t, 0);
-	memcpy(t->pixels + base, level0, sizeof(uint32_t) * (size_t)width * (size_t)height);
+	or_filter_resize_linear(t->pixels + base, (int32_t)1 << lw, (int32_t)1 << lh, level0, width, height);
 	or_texture_generate_pyramid(t);
 	return 0;
 }

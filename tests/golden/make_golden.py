@@ -9,6 +9,9 @@ occlusion_sessions.json
     The renderer session of tests/occlusion_script.py (occlusion grid: box occluders, existing
     triangles, top rows, box tests, two frames) played by the reference: its answers and the
     sha256 of its images, for seeded scenes whose inputs are identified by their own digest.
+texture_resize.json
+    texture_create_RgbaU8 of seeded images whose sizes are not powers of two (filter_resize to
+    the next powers of two, then the pyramid), by the reference: fields and pyramid digests.
 render_*.npz
     Small seeded scenes (inputs stored in the file) rendered by the reference itself, built
     from its sources as the exact (scalar, no-FMA) variant by oracle/Makefile.ref, through
@@ -246,6 +249,29 @@ def occlusion_sessions():
     return out
 
 
+TEXTURE_RESIZE_CASES = [(1, 1, 16), (3, 5, 16), (20, 12, 16), (12, 20, 3), (100, 60, 16), (60, 100, 2), (64, 48, 16),
+                        (48, 64, 16), (129, 31, 5), (255, 257, 16), (33, 2, 16), (300, 256, 16), (256, 300, 16)]
+
+
+def texture_resize_image(w, h):
+    rng = np.random.default_rng(1000 * w + h)
+    return rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+
+
+def texture_resizes():
+    """texture_create_RgbaU8 of images that are not powers of two (filter_resize, then the
+    pyramid) by the reference itself: fields and the sha256 of the pyramid buffer."""
+    import hashlib
+    from oracle import ref
+    lib = ref._load("exact")
+    out = []
+    for w, h, levels in TEXTURE_RESIZE_CASES:
+        fields, pixels = ref.RefTexture(lib, texture_resize_image(w, h), levels).info()
+        out.append(dict(width=w, height=h, resolutions=levels, fields=[int(v) for v in fields],
+                        pyramid=hashlib.sha256(pixels.tobytes()).hexdigest()))
+    return out
+
+
 def main():
     reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DFPSR_REFERENCE", "/root/reference")
     from oracle import ref
@@ -260,6 +286,9 @@ def main():
     with open(os.path.join(HERE, "occlusion_sessions.json"), "w") as f:
         json.dump(occlusion_sessions(), f, indent=1)
     print("wrote occlusion_sessions")
+    with open(os.path.join(HERE, "texture_resize.json"), "w") as f:
+        json.dump(texture_resizes(), f, indent=1)
+    print("wrote texture_resize")
 
 
 if __name__ == "__main__":

@@ -141,3 +141,20 @@ def test_oracle_occlusion_sessions(built):
         assert got["has_occluders"] == expect["has_occluders"], name
         frames = [[make_golden.image_digest(f[0]), make_golden.image_digest(f[1])] for f in got["frames"]]
         assert frames == expect["frames"], name
+
+
+def test_oracle_texture_resize_matches_reference_fixture(built):
+    """Images whose sizes are not powers of two: filter_resize (linear) to the next powers of two,
+    then the pyramid, as the reference made them."""
+    import hashlib
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    from oracle import port
+    with open(os.path.join(GOLDEN, "texture_resize.json")) as f:
+        cases = json.load(f)
+    assert len(cases) == len(make_golden.TEXTURE_RESIZE_CASES)
+    for case in cases:
+        t = port.OracleTexture(make_golden.texture_resize_image(case["width"], case["height"]), case["resolutions"])
+        assert list(t.t.fields()) == case["fields"], case
+        assert hashlib.sha256(t.t.array().tobytes()).hexdigest() == case["pyramid"], case

@@ -80,3 +80,20 @@ def test_oracle_occlusion_session_equals_reference(ref_lib, perspective, targets
     b = o.play(o.RefEngine(), sc, use_color=targets[0], use_depth=targets[1])
     o.assert_same(a, b, f"perspective {perspective} targets {targets}")
     assert 0 < sum(a["visible"]) < len(a["visible"])  # some boxes occluded, some not
+
+
+def test_oracle_texture_resize_equals_reference(ref_lib):
+    """filter_resize (Sampler::Linear) inside texture_create_RgbaU8: upscaling in both directions
+    (two steps), downscaling (the bilinear reference path), one dimension only (the vertical and
+    horizontal paths), tiny and large images."""
+    from oracle import port
+    lib = ref_lib._load("exact")
+    rng = np.random.default_rng(5)
+    for w, h in [(1, 1), (3, 5), (5, 3), (17, 16), (16, 17), (20, 12), (100, 60), (60, 100), (64, 48), (48, 64),
+                 (255, 257), (129, 31), (1000, 600), (33, 2), (2, 33), (513, 1)]:
+        img = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+        for levels in (1, 4, 16):
+            t = port.OracleTexture(img, levels)
+            fields, pixels = ref_lib.RefTexture(lib, img, levels).info()
+            assert list(t.t.fields()) == list(fields), (w, h, levels)
+            assert np.array_equal(t.t.array(), pixels), (w, h, levels)
