@@ -36,6 +36,7 @@ EXPORTED = [
     "dsrg_draw_higher", "dsrg_batch_set_depth_only",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
+    "dsrg_renderer_end_debug",
 ]
 
 
@@ -132,6 +133,7 @@ def lib():
         l.dsrg_renderer_is_box_visible.argtypes = [P, P, P, P, C.POINTER(Camera), C.POINTER(I)]
         l.dsrg_renderer_has_occluders.argtypes = [P]
         l.dsrg_renderer_get_occlusion_grid.argtypes = [P, P, I, C.POINTER(I), C.POINTER(I)]
+        l.dsrg_renderer_end_debug.argtypes = [P, I]
         l.dsrg_model_render_depth_noalloc.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
         l.dsrg_batch_create.argtypes = [P, C.POINTER(P)]
         l.dsrg_batch_destroy.argtypes = [P]
@@ -453,9 +455,12 @@ class Renderer:
         cam = model.camera if camera is None else camera
         self.ctx._check(self.ctx._l.dsrg_renderer_give_task(self.handle, model.handle, t.ctypes.data, C.byref(cam)))
 
-    def end(self):
+    def end(self, debug_wireframe: bool = False):
         _torch_sync()
-        self.ctx._check(self.ctx._l.dsrg_renderer_end(self.handle))
+        if debug_wireframe:
+            self.ctx._check(self.ctx._l.dsrg_renderer_end_debug(self.handle, 1))
+        else:
+            self.ctx._check(self.ctx._l.dsrg_renderer_end(self.handle))
         self._images = None
 
     @property

@@ -11,6 +11,7 @@
 
 #include "dsrg_internal.h"
 #include "dsrg_occlusion.h"
+#include "dsrg_shade.h"
 
 using namespace dsrg;
 
@@ -324,7 +325,7 @@ void renderer_frame_target(dsrg_renderer r, FrameTarget &f) {
 
 extern "C" {
 
-static int end_frame(dsrg_renderer r) {
+static int end_frame(dsrg_renderer r, bool debugWireframe) {
 	dsrg_context ctx = r->context;
 	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
 	r->receiving = false;
@@ -346,6 +347,20 @@ static int end_frame(dsrg_renderer r) {
 	job.resolve = true;
 	BatchTotals totals;
 	int status = DSRG_OK;
+	// renderer_end(debugWireframe): the edges of every drawn command, collected run by run and
+	// drawn over the finished frame (rendererAPI.cpp:354-399)
+	const bool wire = debugWireframe && r->hasColor;
+	uint32_t wireCount = 0;
+	auto enqueue = [&](BatchTotals &t) -> int {
+		BatchOutputs o;
+		int e = batch_enqueue(ctx, job, t, &o);
+		if (e != DSRG_OK || !wire || t.records == 0 || !o.fb.records) return e;
+		const size_t lines = ((size_t)wireCount + t.records) * 3;
+		CUDA_TRY(ctx, r->wireLines.reserve(lines + 1, true, (size_t)wireCount * 3, ctx->stream));
+		launch_wire_lines(o.fb.records, t.records, r->wireLines.ptr + (size_t)wireCount * 3, ctx->stream);
+		wireCount += t.records;
+		return DSRG_OK;
+	};
 	// Alpha-filtered tasks blend in submission order and write no depth (fillShape,
 	// fillerTemplates.h:387-441), so a frame runs as consecutive runs of alpha-filtered and other
 	// tasks, each through the whole pipeline, one after another on the stream.  Without a colour
@@ -356,7 +371,7 @@ static int end_frame(dsrg_renderer r) {
 	if (!anyAlpha) {
 		job.alpha = false;
 		job.clearCounters = true;
-		status = batch_enqueue(ctx, job, totals);
+		status = enqueue(totals);
 	} else {
 		std::vector<TaskParams> &all = r->runTasks;
 		all.swap(job.tasks);
@@ -369,7 +384,7 @@ static int end_frame(dsrg_renderer r) {
 			job.alpha = alpha;
 			job.clearCounters = begin == 0;
 			BatchTotals run;
-			status = batch_enqueue(ctx, job, run);
+			status = enqueue(run);
 			totals.triangles += run.triangles;
 			totals.records += run.records;
 			totals.rows += run.rows;
@@ -386,6 +401,29 @@ static int end_frame(dsrg_renderer r) {
 		cudaStreamSynchronize(ctx->stream);
 		return status;
 	}
+	if (r->hasColor) {
+		if (wire) launch_draw_lines(r->deviceColor, r->colorStride, r->width, r->height, r->wireLines.ptr, wireCount * 3, 0xFFFFFFFFu,
+		                            ctx->stream);
+		if (!r->debugLines.empty()) {
+			// silhouettes kept by occludeFromBox, in the target's pack order; a launch per colour run keeps their order
+			CUDA_TRY(ctx, r->debugLinesDevice.reserve(r->debugLines.size() + 1));
+			CUDA_TRY(ctx, cudaMemcpyAsync(r->debugLinesDevice.ptr, r->debugLines.data(), r->debugLines.size() * sizeof(int4),
+			                              cudaMemcpyHostToDevice, ctx->stream));
+			size_t begin = 0;
+			while (begin < r->debugLines.size()) {
+				size_t end = begin + 1;
+				while (end < r->debugLines.size() && r->debugColors[end] == r->debugColors[begin]) end++;
+				uint32_t packed = 0; // image_saturateAndPack in the target's pack order
+				for (int ch = 0; ch < 4; ch++) packed |= ((r->debugColors[begin] >> (ch * 8)) & 0xFFu) << dsrg::pack_shift(r->color.packOrder, ch);
+				launch_draw_lines(r->deviceColor, r->colorStride, r->width, r->height, r->debugLinesDevice.ptr + begin,
+				                  (uint32_t)(end - begin), packed, ctx->stream);
+				begin = end;
+			}
+			CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream)); // the host list is cleared next
+			r->debugLines.clear();
+			r->debugColors.clear();
+		}
+	}
 	if (r->hasColor && !r->color.onDevice)
 		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->color.data, r->color.strideBytes, r->deviceColor, (size_t)r->width * 4,
 		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
@@ -397,7 +435,12 @@ static int end_frame(dsrg_renderer r) {
 
 int dsrg_renderer_end(dsrg_renderer r) {
 	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
-	return end_frame(r);
+	return end_frame(r, false);
+}
+
+int dsrg_renderer_end_debug(dsrg_renderer r, int32_t debugWireframe) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	return end_frame(r, debugWireframe != 0);
 }
 
 // ------------------------------------------------------------------ single-call rendering
@@ -420,7 +463,7 @@ static int render_once(dsrg_context ctx, dsrg_model m, const float *modelToWorld
 		cudaStreamSynchronize(ctx->stream);
 		return s;
 	}
-	return end_frame(r);
+	return end_frame(r, false);
 }
 
 int dsrg_model_render(dsrg_context ctx, dsrg_model m, const float *modelToWorld, const dsrg_camera *camera,

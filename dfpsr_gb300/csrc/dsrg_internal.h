@@ -243,6 +243,12 @@ struct dsrg_renderer_s {
 	std::vector<float> gridHost;
 	DeviceBuffer<float> gridDevice;
 	bool gridHostValid = false, gridDeviceValid = false;
+	// debug overlays (DebugLine, rendererAPI.cpp:132-137): silhouettes kept until a renderer_end
+	// with a colour target draws them (colour as RGBA bytes), and the frame's wireframe lines
+	std::vector<int4> debugLines;
+	std::vector<uint32_t> debugColors;
+	DeviceBuffer<int4> wireLines;
+	DeviceBuffer<int4> debugLinesDevice;
 };
 
 // The frame target of a renderer's current frame (images, size, occlusion grid when in use).

@@ -149,6 +149,11 @@ struct AlphaBuffers {
 // submission order, depth read only.
 void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, uint32_t entries, uint32_t recordCount,
                   const AlphaBuffers &a, cudaStream_t stream);
+// Debug overlays: the three edges of every record as lines in pixels (flat / 256), and draw_line
+// (api/drawAPI.cpp:176-279) of many lines of one packed colour into a device image.
+void launch_wire_lines(const DrawRecord *records, uint32_t count, int4 *lines, cudaStream_t stream);
+void launch_draw_lines(uint32_t *image, int32_t stride, int32_t width, int32_t height, const int4 *lines, uint32_t count,
+                       uint32_t color, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total).
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);
 size_t scan_scratch_elems(uint32_t n);

@@ -189,7 +189,6 @@ int dsrg_renderer_occlude_from_box(dsrg_renderer r, const float *minimum, const 
 	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Cannot call renderer_occludeFromBox without first calling renderer_begin!");
 	if (!minimum || !maximum || !modelToWorld || !camera)
 		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_occludeFromBox: null argument");
-	(void)debugSilhouette;
 	prepare_for_occlusion(r);
 	int s = grid_on_host(r);
 	if (s != DSRG_OK) return s;
@@ -208,6 +207,18 @@ int dsrg_renderer_occlude_from_box(dsrg_renderer r, const float *minimum, const 
 	convex_hull(proj, 8, hull);
 	occlude_from_hull(r, hull);
 	r->gridDeviceValid = false;
+	if (debugSilhouette) {
+		// cyan lines around the hull, drawn at renderer_end; the reference tests the depth of the
+		// unsorted projection p, not of the hull corner it draws from (rendererAPI.cpp:277-291)
+		for (int32_t p = 0; p < hull.count; p++) {
+			const int32_t q = (p + 1) % hull.count;
+			if (proj[p].cs.z > camera->nearClip) {
+				r->debugLines.push_back(make_int4((int32_t)(hull.x[p] / 256), (int32_t)(hull.y[p] / 256), (int32_t)(hull.x[q] / 256),
+				                                  (int32_t)(hull.y[q] / 256)));
+				r->debugColors.push_back(0xFFFFFF00u); // red 0, green 255, blue 255, alpha 255
+			}
+		}
+	}
 	return DSRG_OK;
 }
 

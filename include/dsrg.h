@@ -138,6 +138,13 @@ int dsrg_renderer_destroy(dsrg_renderer renderer);
 int dsrg_renderer_begin(dsrg_renderer renderer, const dsrg_image *color, const dsrg_image *depth);
 int dsrg_renderer_give_task(dsrg_renderer renderer, dsrg_model model, const float *modelToWorld, const dsrg_camera *camera);
 int dsrg_renderer_end(dsrg_renderer renderer);
+/* renderer_end(renderer, debugWireframe) (api/rendererAPI.h:111-112, rendererAPI.cpp:343-415):
+ * with debugWireframe, white lines (draw_line, api/drawAPI.h) along the edges of every drawn
+ * triangle over the finished colour image; the silhouettes kept by occlude_from_box with
+ * debugSilhouette are drawn after them, by either form of renderer_end that has a colour image
+ * (without one they stay for the next frame's).  dsrg_renderer_end(r) is
+ * dsrg_renderer_end_debug(r, 0). */
+int dsrg_renderer_end_debug(dsrg_renderer renderer, int32_t debugWireframe);
 /* renderer_takesTriangles (api/rendererAPI.h:67): 1 between begin and end. */
 int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
 

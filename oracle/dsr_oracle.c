@@ -1681,6 +1681,46 @@ void or_draw_higher(float *targetHeight, int32_t thStride, uint32_t *targetA, in
  * not drawn.  Commands are executed in one band (the band split does not change the result). */
 #define OR_CELL 16
 
+typedef struct { int32_t x1, y1, x2, y2; uint32_t color; } debug_line; /* DebugLine (rendererAPI.cpp:132-137), colour as RGBA bytes */
+
+/* drawLineSuper (api/drawAPI.cpp:176-279) of a packed colour: horizontal and vertical runs, else
+ * the reference's integer error walk along the longer axis; only pixels inside the image are written. */
+static void draw_line(uint32_t *image, int32_t width, int32_t height, int32_t x1, int32_t y1, int32_t x2, int32_t y2, uint32_t color) {
+	if ((x1 < 0 && x2 < 0) || (y1 < 0 && y2 < 0) || (x1 >= width && x2 >= width) || (y1 >= height && y2 >= height)) return;
+#define PUT(X, Y) do { int32_t px_ = (X), py_ = (Y); if (px_ >= 0 && py_ >= 0 && px_ < width && py_ < height) image[(size_t)py_ * width + px_] = color; } while (0)
+	if (y1 == y2) {
+		int32_t l = x1 < x2 ? x1 : x2, r = x1 < x2 ? x2 : x1;
+		for (int32_t x = l; x <= r; x++) PUT(x, y1);
+	} else if (x1 == x2) {
+		int32_t t = y1 < y2 ? y1 : y2, b = y1 < y2 ? y2 : y1;
+		for (int32_t y = t; y <= b; y++) PUT(x1, y);
+	} else {
+		int32_t adx = x2 > x1 ? x2 - x1 : x1 - x2, ady = y2 > y1 ? y2 - y1 : y1 - y2;
+		if (ady >= adx) {
+			if (y2 < y1) { int32_t t = x1; x1 = x2; x2 = t; t = y1; y1 = y2; y2 = t; }
+			int32_t step = x2 > x1 ? 1 : -1, tilt = (x2 > x1 ? x2 - x1 : x1 - x2) * 2, maxError = y2 - y1, error = 0, x = x1;
+			for (int32_t y = y1; y <= y2; y++) {
+				PUT(x, y);
+				error += tilt;
+				if (error >= maxError) { x += step; error -= maxError * 2; }
+			}
+		} else {
+			if (x2 < x1) { int32_t t = x1; x1 = x2; x2 = t; t = y1; y1 = y2; y2 = t; }
+			int32_t step = y2 > y1 ? 1 : -1, tilt = (y2 > y1 ? y2 - y1 : y1 - y2) * 2, maxError = x2 - x1, error = 0, y = y1;
+			for (int32_t x = x1; x <= x2; x++) {
+				PUT(x, y);
+				error += tilt;
+				if (error >= maxError) { y += step; error -= maxError * 2; }
+			}
+		}
+	}
+#undef PUT
+}
+
+void or_draw_line(uint32_t *image, int32_t width, int32_t height, int32_t x1, int32_t y1, int32_t x2, int32_t y2, uint32_t color) {
+	draw_line(image, width, height, x1, y1, x2, y2, color);
+}
+
 struct or_renderer_s {
 	int receiving;
 	uint32_t *color;
@@ -1694,6 +1734,8 @@ struct or_renderer_s {
 	int32_t gridAllocWidth, gridAllocHeight; /* the allocated grid (its stride is gridAllocWidth) */
 	int32_t gridWidth, gridHeight;
 	int occluded;
+	debug_line *debugLines;
+	int32_t debugCount, debugCapacity;
 };
 
 or_renderer *or_renderer_create(void) { return (or_renderer *)calloc(1, sizeof(or_renderer)); }
@@ -1703,6 +1745,7 @@ void or_renderer_destroy(or_renderer *r) {
 	free(r->commands.items);
 	free(r->cams);
 	free(r->grid);
+	free(r->debugLines);
 	free(r);
 }
 
@@ -1838,9 +1881,17 @@ static void box_corners(const float mn[3], const float mx[3], v3 out[8]) { /* GE
 	out[6] = mk3(mx[0], mx[1], mn[2]); out[7] = mk3(mx[0], mx[1], mx[2]);
 }
 
+static void push_debug_line(or_renderer *r, int32_t x1, int32_t y1, int32_t x2, int32_t y2, uint32_t color) {
+	if (r->debugCount == r->debugCapacity) {
+		r->debugCapacity = r->debugCapacity ? r->debugCapacity * 2 : 64;
+		r->debugLines = (debug_line *)realloc(r->debugLines, sizeof(debug_line) * (size_t)r->debugCapacity);
+	}
+	debug_line l = {x1, y1, x2, y2, color};
+	r->debugLines[r->debugCount++] = l;
+}
+
 int or_renderer_occlude_from_box(or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
-                                 const or_camera_desc *desc, projected_out *silhouette, int32_t *silhouetteCount) {
-	if (silhouetteCount) *silhouetteCount = 0;
+                                 const or_camera_desc *desc, int debugSilhouette) {
 	if (!r->receiving) return -1;
 	prepare_for_occlusion(r);
 	camera cam;
@@ -1858,12 +1909,15 @@ int or_renderer_occlude_from_box(or_renderer *r, const float mn[3], const float 
 	int32_t count = 0;
 	jarvis_hull(hull, &count, proj, 8);
 	occlude_from_sorted_hull(r, hull, count, pixel_bound_of(hull, count));
-	if (silhouette && silhouetteCount) {
+	if (debugSilhouette) {
+		/* cyan lines around the hull, kept until renderer_end; the reference tests the depth of
+		 * projections[p] (unsorted), not of the hull corner it draws from (rendererAPI.cpp:277-291) */
 		for (int32_t p = 0; p < count; p++) {
-			silhouette[p].x = hull[p].flat.x; silhouette[p].y = hull[p].flat.y;
-			silhouette[p].z = proj[p].cs.z; /* the reference tests the depth of projections[p], not of the hull corner */
+			int32_t q = (p + 1) % count;
+			if (proj[p].cs.z > cam.nearClip)
+				push_debug_line(r, (int32_t)(hull[p].flat.x / 256), (int32_t)(hull[p].flat.y / 256), (int32_t)(hull[q].flat.x / 256),
+				                (int32_t)(hull[q].flat.y / 256), 0xFFFFFF00u /* red 0, green, blue, alpha 255 */);
 		}
-		*silhouetteCount = count;
 	}
 	return 0;
 }
@@ -1977,8 +2031,10 @@ int or_renderer_give_task(or_renderer *r, const or_model *model, const float mod
 	return 0;
 }
 
-/* completeOcclusion (rendererAPI.cpp:193-214) and CommandQueue::execute of the commands left. */
-int or_renderer_end(or_renderer *r, or_stats *stats) {
+/* completeOcclusion (rendererAPI.cpp:193-214), CommandQueue::execute of the commands left, then the
+ * debug overlays of endFrame (rendererAPI.cpp:354-415): white lines around every drawn command
+ * when debugWireframe, then the silhouettes kept by occludeFromBox. */
+int or_renderer_end(or_renderer *r, or_stats *stats, int debugWireframe) {
 	if (!r->receiving) return -1;
 	r->receiving = 0;
 	if (r->occluded) {
@@ -2008,6 +2064,27 @@ int or_renderer_end(or_renderer *r, or_stats *stats) {
 	}
 	free(rows);
 	if (stats) stats->fragments += tg.fragments;
+	if (r->color) {
+		if (debugWireframe) {
+			for (size_t i = 0; i < r->commands.count; i++) {
+				const command *c = &r->commands.items[i];
+				if (c->occluded) continue;
+				const projected *p = c->triangle.position;
+				for (int e = 0; e < 3; e++) {
+					const projected *a = &p[e], *b = &p[(e + 1) % 3];
+					draw_line(r->color, r->width, r->height, (int32_t)(a->flat.x / 256), (int32_t)(a->flat.y / 256),
+					          (int32_t)(b->flat.x / 256), (int32_t)(b->flat.y / 256), 0xFFFFFFFFu);
+				}
+			}
+		}
+		for (int32_t l = 0; l < r->debugCount; l++) {
+			const debug_line *d = &r->debugLines[l];
+			uint32_t packed = 0; /* image_saturateAndPack in the target's pack order */
+			for (int ch = 0; ch < 4; ch++) packed |= ((d->color >> (ch * 8)) & 0xFFu) << (PACK_INDEX[r->packOrder][ch] * 8);
+			draw_line(r->color, r->width, r->height, d->x1, d->y1, d->x2, d->y2, packed);
+		}
+		r->debugCount = 0;
+	}
 	r->commands.count = 0;
 	return 0;
 }

@@ -96,21 +96,22 @@ int or_model_render_depth(const or_model *model, const float modelToWorld[12], c
 
 /* ---- renderer with an occlusion grid (api/rendererAPI.cpp:141-477, modelAPI.cpp:214-275) ---- */
 typedef struct or_renderer_s or_renderer;
-typedef struct { int64_t x, y; float z; } projected_out; /* a silhouette corner: flat x, y and camera depth */
 or_renderer *or_renderer_create(void);
 void or_renderer_destroy(or_renderer *r);
 /* color (packOrder 0..3) and depth may be null; both are width x height without padding. */
 int or_renderer_begin(or_renderer *r, uint32_t *color, float *depth, int32_t width, int32_t height, int32_t packOrder);
 int or_renderer_give_task(or_renderer *r, const or_model *model, const float modelToWorld[12], const or_camera_desc *cam);
-/* silhouette (8 entries) receives the box's convex hull when not null. */
+/* debugSilhouette keeps the box's hull as cyan lines drawn at renderer_end. */
 int or_renderer_occlude_from_box(or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
-                                 const or_camera_desc *cam, projected_out *silhouette, int32_t *silhouetteCount);
+                                 const or_camera_desc *cam, int debugSilhouette);
 int or_renderer_occlude_from_existing_triangles(or_renderer *r);
 int or_renderer_occlude_from_top_rows(or_renderer *r, int perspective);
 int or_renderer_is_box_visible(const or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
                                const or_camera_desc *cam);
 int or_renderer_has_occluders(const or_renderer *r);
-int or_renderer_end(or_renderer *r, or_stats *stats);
+int or_renderer_end(or_renderer *r, or_stats *stats, int debugWireframe);
+/* draw_line (api/drawAPI.h) of a packed colour into a dense width x height image. */
+void or_draw_line(uint32_t *image, int32_t width, int32_t height, int32_t x1, int32_t y1, int32_t x2, int32_t y2, uint32_t color);
 int or_renderer_grid(const or_renderer *r, float *out, int32_t *gridWidth, int32_t *gridHeight);
 
 /* ---- deferred light passes (SDK/SpriteEngine/lightAPI.h:27-31, orthoAPI.h:41-137) and draw_higher ---- */

@@ -93,12 +93,13 @@ def lib():
         l.or_renderer_destroy.argtypes = [R]
         l.or_renderer_begin.argtypes = [R, P, P, C.c_int32, C.c_int32, C.c_int32]
         l.or_renderer_give_task.argtypes = [R, C.POINTER(Model), P, C.POINTER(CameraDesc)]
-        l.or_renderer_occlude_from_box.argtypes = [R, P, P, P, C.POINTER(CameraDesc), P, P]
+        l.or_renderer_occlude_from_box.argtypes = [R, P, P, P, C.POINTER(CameraDesc), C.c_int]
         l.or_renderer_occlude_from_existing_triangles.argtypes = [R]
         l.or_renderer_occlude_from_top_rows.argtypes = [R, C.c_int]
         l.or_renderer_is_box_visible.argtypes = [R, P, P, P, C.POINTER(CameraDesc)]
         l.or_renderer_has_occluders.argtypes = [R]
-        l.or_renderer_end.argtypes = [R, C.POINTER(Stats)]
+        l.or_renderer_end.argtypes = [R, C.POINTER(Stats), C.c_int]
+        l.or_draw_line.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint32]
         l.or_renderer_grid.argtypes = [R, P, P, P]
         _lib = l
     return _lib
@@ -335,10 +336,6 @@ def draw_higher(target, source, left, top, offset):
     return th, ta, tb
 
 
-class SilhouetteCorner(C.Structure):
-    _fields_ = [("x", C.c_int64), ("y", C.c_int64), ("z", C.c_float)]
-
-
 class OracleRenderer:
     """renderer_begin / giveTask / the occlusion grid / renderer_end on the CPU oracle
     (api/rendererAPI.cpp:141-477).  Models are PreparedModel objects; cameras CameraDesc."""
@@ -366,14 +363,10 @@ class OracleRenderer:
         self._keep.append((pm, t))
         assert lib().or_renderer_give_task(self.h, C.byref(pm.model), _ptr(t), C.byref(cam or pm.cam)) == 0
 
-    def occlude_from_box(self, mn, mx, transform, cam: CameraDesc):
+    def occlude_from_box(self, mn, mx, transform, cam: CameraDesc, debug_silhouette: bool = False):
         a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
         t = np.ascontiguousarray(transform, np.float32)
-        out = (SilhouetteCorner * 8)()
-        n = C.c_int32(0)
-        assert lib().or_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), C.byref(cam), C.cast(out, C.c_void_p),
-                                                  C.cast(C.pointer(n), C.c_void_p)) == 0
-        return [(out[i].x, out[i].y, out[i].z) for i in range(n.value)]
+        assert lib().or_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), C.byref(cam), 1 if debug_silhouette else 0) == 0
 
     def occlude_from_existing_triangles(self):
         assert lib().or_renderer_occlude_from_existing_triangles(self.h) == 0
@@ -396,12 +389,19 @@ class OracleRenderer:
         lib().or_renderer_grid(self.h, _ptr(out), C.cast(C.pointer(gw), C.c_void_p), C.cast(C.pointer(gh), C.c_void_p))
         return out
 
-    def end(self, coverage: bool = False):
+    def end(self, coverage: bool = False, debug_wireframe: bool = False):
         st = Stats()
         cov = None
         if coverage:
             img = self.color if self.color is not None else self.depth
             cov = np.zeros(img.shape, np.uint32)
         st.coverage = _ptr(cov)
-        assert lib().or_renderer_end(self.h, C.byref(st)) == 0
+        assert lib().or_renderer_end(self.h, C.byref(st), 1 if debug_wireframe else 0) == 0
         return self.color, self.depth, {"fragments": int(st.fragments), "coverage": cov}
+
+
+def draw_line(image: np.ndarray, x1: int, y1: int, x2: int, y2: int, color: int) -> np.ndarray:
+    out = np.ascontiguousarray(image, np.uint32).copy()
+    h, w = out.shape
+    lib().or_draw_line(_ptr(out), w, h, x1, y1, x2, y2, color)
+    return out

@@ -76,7 +76,8 @@ def _load(variant: str):
         l.refh_renderer_free.argtypes = [P]
         l.refh_renderer_begin.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int]
         l.refh_renderer_give_task.argtypes = [P, P, P] + cam
-        l.refh_renderer_occlude_from_box.argtypes = [P, P, P, P] + cam
+        l.refh_renderer_occlude_from_box.argtypes = [P, P, P, P] + cam + [C.c_int]
+        l.refh_draw_line.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32]
         l.refh_renderer_occlude_from_existing_triangles.argtypes = [P]
         l.refh_renderer_occlude_from_top_rows.argtypes = [P] + cam
         l.refh_renderer_is_box_visible.argtypes = [P, P, P, P] + cam
@@ -294,11 +295,11 @@ class RefRenderer:
         loc, args = _camera_args(cam)
         self.lib.refh_renderer_give_task(self.h, model.handle, _ptr(t), *args)
 
-    def occlude_from_box(self, mn, mx, transform, cam):
+    def occlude_from_box(self, mn, mx, transform, cam, debug_silhouette: bool = False):
         a, b = np.asarray(mn, np.float32), np.asarray(mx, np.float32)
         t = np.ascontiguousarray(transform, np.float32)
         loc, args = _camera_args(cam)
-        self.lib.refh_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), *args)
+        self.lib.refh_renderer_occlude_from_box(self.h, _ptr(a), _ptr(b), _ptr(t), *args, 1 if debug_silhouette else 0)
 
     def occlude_from_existing_triangles(self):
         self.lib.refh_renderer_occlude_from_existing_triangles(self.h)
@@ -319,3 +320,10 @@ class RefRenderer:
     def end(self, debug_wireframe: bool = False):
         self.lib.refh_renderer_end(self.h, 1 if debug_wireframe else 0)
         return self.color, self.depth
+
+
+def draw_line(image, x1: int, y1: int, x2: int, y2: int, color: int, variant: str = "exact"):
+    out = np.ascontiguousarray(image, np.uint32).copy()
+    h, w = out.shape
+    _load(variant).refh_draw_line(_ptr(out), w, h, x1, y1, x2, y2, color)
+    return out

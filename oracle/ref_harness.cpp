@@ -237,11 +237,19 @@ void refh_renderer_give_task(void* handle, void* modelHandle, const float* model
 
 void refh_renderer_occlude_from_box(void* handle, const float* mn, const float* mx, const float* modelToWorld,
                                     const float* cameraLocation, int perspective, float slope, float nearClip, float farClip,
-                                    int width, int height) {
+                                    int width, int height, int debugSilhouette) {
 	RendererBox* box = (RendererBox*)handle;
 	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
 	renderer_occludeFromBox(box->renderer, FVector3D(mn[0], mn[1], mn[2]), FVector3D(mx[0], mx[1], mx[2]),
-	                        makeTransform(modelToWorld), makeCamera(c), false);
+	                        makeTransform(modelToWorld), makeCamera(c), debugSilhouette != 0);
+}
+
+// draw_line (api/drawAPI.h) of a packed colour into a width x height RGBA image.
+void refh_draw_line(uint32_t* pixels, int width, int height, int x1, int y1, int x2, int y2, uint32_t color) {
+	ImageRgbaU8 image = image_create_RgbaU8(width, height);
+	copyInRgba(image, pixels, width, height);
+	draw_line(image, x1, y1, x2, y2, color);
+	copyOutRgba(image, pixels, width, height);
 }
 
 void refh_renderer_occlude_from_existing_triangles(void* handle) {

@@ -241,11 +241,12 @@ def occlusion_sessions():
     out = {}
     for name, params in OCCLUSION_CASES.items():
         sc = scenes.occlusion_scene(**params)
-        for use_color, use_depth in ((True, True), (True, False), (False, True)):
-            r = occlusion_script.play(occlusion_script.RefEngine(), sc, use_color=use_color, use_depth=use_depth)
-            out[f"{name}_c{int(use_color)}d{int(use_depth)}"] = dict(
-                params=params, use_color=use_color, use_depth=use_depth, inputs=scene_digest(sc), visible=r["visible"],
-                has_occluders=r["has_occluders"], frames=[[image_digest(f[0]), image_digest(f[1])] for f in r["frames"]])
+        for use_color, use_depth, debug in ((True, True, False), (True, False, False), (False, True, False), (True, True, True)):
+            r = occlusion_script.play(occlusion_script.RefEngine(), sc, use_color=use_color, use_depth=use_depth, debug=debug)
+            out[f"{name}_c{int(use_color)}d{int(use_depth)}{'_debug' if debug else ''}"] = dict(
+                params=params, use_color=use_color, use_depth=use_depth, debug=debug, inputs=scene_digest(sc),
+                visible=r["visible"], has_occluders=r["has_occluders"],
+                frames=[[image_digest(f[0]), image_digest(f[1])] for f in r["frames"]])
     return out
 
 

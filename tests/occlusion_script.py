@@ -39,9 +39,9 @@ class OracleEngine:
     def give(self, s, cam):
         self.r.give_task(self.model(s), s.model_to_world, cam)
 
-    def box(self, s, cam):
+    def box(self, s, cam, debug=False):
         mn, mx = scenes.OcclusionScene.bound(s)
-        self.r.occlude_from_box(mn, mx, s.model_to_world, cam)
+        self.r.occlude_from_box(mn, mx, s.model_to_world, cam, debug)
 
     def existing(self):
         self.r.occlude_from_existing_triangles()
@@ -59,8 +59,8 @@ class OracleEngine:
     def grid(self):
         return self.r.grid()
 
-    def end(self):
-        c, d, info = self.r.end(coverage=False)
+    def end(self, wireframe=False):
+        c, d, info = self.r.end(coverage=False, debug_wireframe=wireframe)
         return c, d, info["fragments"]
 
 
@@ -84,8 +84,8 @@ class RefEngine(OracleEngine):
     def grid(self):
         return None
 
-    def end(self):
-        c, d = self.r.end()
+    def end(self, wireframe=False):
+        c, d = self.r.end(wireframe)
         return c, d, None
 
 
@@ -114,9 +114,9 @@ class GpuEngine(OracleEngine):
     def give(self, s, cam):
         self.r.give_task(self.model(s), cam, s.model_to_world)
 
-    def box(self, s, cam):
+    def box(self, s, cam, debug=False):
         mn, mx = scenes.OcclusionScene.bound(s)
-        self.r.occlude_from_box(mn, mx, s.model_to_world, cam)
+        self.r.occlude_from_box(mn, mx, s.model_to_world, cam, debug)
 
     def existing(self):
         self.r.occlude_from_existing_triangles()
@@ -134,17 +134,19 @@ class GpuEngine(OracleEngine):
     def grid(self):
         return self.r.occlusion_grid()
 
-    def end(self):
+    def end(self, wireframe=False):
         self.ctx.set_counting(True, None)
         try:
-            self.r.end()
+            self.r.end(wireframe)
             fragments = self.ctx.stats()["fragments"]
         finally:
             self.ctx.set_counting(False)
         return self.images[0], self.images[1], fragments
 
 
-def play(engine, sc: scenes.OcclusionScene, *, use_color: bool = True, use_depth: bool = True) -> dict:
+def play(engine, sc: scenes.OcclusionScene, *, use_color: bool = True, use_depth: bool = True, debug: bool = False) -> dict:
+    """debug: the box occluder keeps its silhouette, frame 1 ends with the wireframe overlay, and
+    frame 2 draws a second silhouette (and the first one again when frame 1 had no colour image)."""
     cam = engine.camera(sc.camera)
     out = {"visible": [], "has_occluders": [], "grids": [], "frames": []}
     color = sc.color if use_color else None
@@ -153,7 +155,7 @@ def play(engine, sc: scenes.OcclusionScene, *, use_color: bool = True, use_depth
     # frame 1
     engine.begin(color, depth)
     out["has_occluders"].append(engine.has_occluders())
-    engine.box(sc.wall, cam)
+    engine.box(sc.wall, cam, debug)
     out["grids"].append(engine.grid())
     out["visible"] += [engine.visible(p, cam) for p in props]
     engine.give(sc.wall, cam)
@@ -170,11 +172,13 @@ def play(engine, sc: scenes.OcclusionScene, *, use_color: bool = True, use_depth
     for p in props[1::2]:
         engine.give(p, cam)
     out["has_occluders"].append(engine.has_occluders())
-    out["frames"].append(engine.end())
+    out["frames"].append(engine.end(debug))
     # frame 2: tests before any occluder read the grid the first frame left
     engine.begin(color, depth)
     out["has_occluders"].append(engine.has_occluders())
     out["visible"] += [engine.visible(p, cam) for p in props]
+    if debug:
+        engine.box(props[0], cam, True)
     if use_depth:
         engine.top_rows(cam)
         out["grids"].append(engine.grid())

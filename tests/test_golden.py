@@ -132,11 +132,11 @@ def test_oracle_occlusion_sessions(built):
     from dfpsr_gb300 import scenes
     with open(os.path.join(GOLDEN, "occlusion_sessions.json")) as f:
         sessions = json.load(f)
-    assert len(sessions) == 6
+    assert len(sessions) == 8
     for name, expect in sessions.items():
         sc = scenes.occlusion_scene(**expect["params"])
         assert make_golden.scene_digest(sc) == expect["inputs"], f"{name}: the seeded inputs changed"
-        got = o.play(o.OracleEngine(), sc, use_color=expect["use_color"], use_depth=expect["use_depth"])
+        got = o.play(o.OracleEngine(), sc, use_color=expect["use_color"], use_depth=expect["use_depth"], debug=expect["debug"])
         assert got["visible"] == expect["visible"], name
         assert got["has_occluders"] == expect["has_occluders"], name
         frames = [[make_golden.image_digest(f[0]), make_golden.image_digest(f[1])] for f in got["frames"]]

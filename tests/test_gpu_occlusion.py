@@ -16,12 +16,44 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("perspective", [True, False])
 @pytest.mark.parametrize("targets", [(True, True), (True, False), (False, True)])
-def test_occlusion_session_matches_oracle(ctx, perspective, targets):
+@pytest.mark.parametrize("debug", [False, True])
+def test_occlusion_session_matches_oracle(ctx, perspective, targets, debug):
+    """With debug, also the silhouettes of occludeFromBox and renderer_end's wireframe overlay."""
     import occlusion_script as o
     sc = scenes.occlusion_scene(perspective=perspective)
-    a = o.play(o.GpuEngine(ctx), sc, use_color=targets[0], use_depth=targets[1])
-    b = o.play(o.OracleEngine(), sc, use_color=targets[0], use_depth=targets[1])
-    o.assert_same(a, b, f"perspective {perspective} targets {targets}")
+    a = o.play(o.GpuEngine(ctx), sc, use_color=targets[0], use_depth=targets[1], debug=debug)
+    b = o.play(o.OracleEngine(), sc, use_color=targets[0], use_depth=targets[1], debug=debug)
+    o.assert_same(a, b, f"perspective {perspective} targets {targets} debug {debug}")
+
+
+def test_wireframe_of_a_large_frame_with_alpha_runs(ctx):
+    """The wireframe of a frame of solid and alpha-filtered runs (lines gathered from every run's
+    commands), at 1080p with long edges leaving the image."""
+    import dataclasses
+    import dfpsr_gb300 as d
+    from oracle import port
+    base = scenes.random_triangles(seed=91, triangles=3000, width=1920, height=1080, texture_size=64)
+    base.camera_location = scenes.camera_location((0.1, 0.2, -1.2), (0.0, 0.0, 1.0))
+    parts = [dataclasses.replace(base, filter=f) for f in (0, 1)]
+    parts[1] = dataclasses.replace(parts[1], model_to_world=np.array([0.3, 0.1, 0.2, 1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32))
+    o = port.OracleRenderer()
+    color = np.zeros((1080, 1920), np.uint32)
+    depth = np.zeros((1080, 1920), np.float32)
+    o.begin(color, depth)
+    pms = [port.PreparedModel(p) for p in parts]
+    for pm, p in zip(pms, parts):
+        o.give_task(pm, p.model_to_world, pm.cam)
+    rc, rz, _ = o.end(debug_wireframe=True)
+    r = d.Renderer(ctx)
+    c, z = color.copy(), depth.copy()
+    r.begin(c, z)
+    models = [d.Model(ctx, p) for p in parts]
+    for m, p in zip(models, parts):
+        r.give_task(m, m.camera, p.model_to_world)
+    r.end(debug_wireframe=True)
+    assert np.array_equal(c, rc), f"{int((c != rc).sum())} pixels differ"
+    assert np.array_equal(z.view(np.uint32), rz.view(np.uint32))
+    r.destroy()
 
 
 def test_occlusion_sessions_match_reference_fixtures(ctx):
@@ -35,7 +67,7 @@ def test_occlusion_sessions_match_reference_fixtures(ctx):
         sessions = json.load(f)
     for name, expect in sessions.items():
         sc = scenes.occlusion_scene(**expect["params"])
-        got = o.play(o.GpuEngine(ctx), sc, use_color=expect["use_color"], use_depth=expect["use_depth"])
+        got = o.play(o.GpuEngine(ctx), sc, use_color=expect["use_color"], use_depth=expect["use_depth"], debug=expect["debug"])
         assert got["visible"] == expect["visible"], name
         frames = [[make_golden.image_digest(f[0]), make_golden.image_digest(f[1])] for f in got["frames"]]
         assert frames == expect["frames"], name

@@ -71,13 +71,15 @@ def test_row_intervals_equal_reference(ref_lib):
 
 @pytest.mark.parametrize("perspective", [True, False])
 @pytest.mark.parametrize("targets", [(True, True), (True, False), (False, True)])
-def test_oracle_occlusion_session_equals_reference(ref_lib, perspective, targets):
+@pytest.mark.parametrize("debug", [False, True])
+def test_oracle_occlusion_session_equals_reference(ref_lib, perspective, targets, debug):
     """renderer_occludeFromBox / FromExistingTriangles / FromTopRows, isBoxVisible, hasOccluders and
-    renderer_end with completeOcclusion, two frames on one renderer (tests/occlusion_script.py)."""
+    renderer_end with completeOcclusion, two frames on one renderer (tests/occlusion_script.py);
+    with debug, the silhouettes and the wireframe overlay."""
     import occlusion_script as o
     sc = scenes.occlusion_scene(perspective=perspective)
-    a = o.play(o.OracleEngine(), sc, use_color=targets[0], use_depth=targets[1])
-    b = o.play(o.RefEngine(), sc, use_color=targets[0], use_depth=targets[1])
+    a = o.play(o.OracleEngine(), sc, use_color=targets[0], use_depth=targets[1], debug=debug)
+    b = o.play(o.RefEngine(), sc, use_color=targets[0], use_depth=targets[1], debug=debug)
     o.assert_same(a, b, f"perspective {perspective} targets {targets}")
     assert 0 < sum(a["visible"]) < len(a["visible"])  # some boxes occluded, some not
 
@@ -97,3 +99,15 @@ def test_oracle_texture_resize_equals_reference(ref_lib):
             fields, pixels = ref_lib.RefTexture(lib, img, levels).info()
             assert list(t.t.fields()) == list(fields), (w, h, levels)
             assert np.array_equal(t.t.array(), pixels), (w, h, levels)
+
+
+def test_oracle_draw_line_equals_reference(ref_lib):
+    """draw_line (api/drawAPI.cpp:176-279) on random segments, partly or wholly outside the image."""
+    from oracle import port
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        w, h = int(rng.integers(1, 40)), int(rng.integers(1, 40))
+        img = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+        x1, y1, x2, y2 = [int(v) for v in rng.integers(-20, 60, 4)]
+        color = int(rng.integers(0, 2**32))
+        assert np.array_equal(port.draw_line(img, x1, y1, x2, y2, color), ref_lib.draw_line(img, x1, y1, x2, y2, color))
