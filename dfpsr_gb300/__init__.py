@@ -36,7 +36,7 @@ EXPORTED = [
     "dsrg_draw_higher", "dsrg_batch_set_depth_only",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
-    "dsrg_renderer_end_debug",
+    "dsrg_renderer_end_debug", "dsrg_renderer_get_images", "dsrg_camera_world_to_screen", "dsrg_renderer_give_triangles",
 ]
 
 
@@ -134,6 +134,9 @@ def lib():
         l.dsrg_renderer_has_occluders.argtypes = [P]
         l.dsrg_renderer_get_occlusion_grid.argtypes = [P, P, I, C.POINTER(I), C.POINTER(I)]
         l.dsrg_renderer_end_debug.argtypes = [P, I]
+        l.dsrg_renderer_get_images.argtypes = [P, C.POINTER(Image), C.POINTER(Image)]
+        l.dsrg_camera_world_to_screen.argtypes = [C.POINTER(Camera), P, P]
+        l.dsrg_renderer_give_triangles.argtypes = [P, I, P, P, P, P, P, I, C.POINTER(Camera)]
         l.dsrg_model_render_depth_noalloc.argtypes = [P, P, P, C.POINTER(Camera), C.POINTER(Image)]
         l.dsrg_batch_create.argtypes = [P, C.POINTER(P)]
         l.dsrg_batch_destroy.argtypes = [P]
@@ -190,6 +193,24 @@ def camera_struct(scene) -> Camera:
     c.width = scene.width
     c.height = scene.height
     return c
+
+
+# dsrg_projected_point: cs[3], is[2], flat[2] (int64 at offset 24)
+PROJECTED_POINT = np.dtype({"names": ["cs", "is", "flat"], "formats": [("<f4", 3), ("<f4", 2), ("<i8", 2)],
+                            "offsets": [0, 12, 24], "itemsize": 40})
+
+
+def world_to_screen(camera: "Camera", world) -> np.ndarray:
+    """dsrg_camera_world_to_screen of (..., 3) world points; returns PROJECTED_POINT records."""
+    world = np.ascontiguousarray(world, np.float32)
+    flat = world.reshape(-1, 3)
+    out = np.zeros(len(flat), PROJECTED_POINT)
+    l = lib()
+    for i in range(len(flat)):
+        status = l.dsrg_camera_world_to_screen(C.byref(camera), flat[i].ctypes.data, out[i:i + 1].ctypes.data)
+        if status != DSRG_OK:
+            raise DsrgError(status, "dsrg_camera_world_to_screen")
+    return out.reshape(world.shape[:-1])
 
 
 def image_struct(array, pack_order: int = 0) -> Optional[Image]:
@@ -466,6 +487,23 @@ class Renderer:
     @property
     def takes_triangles(self) -> bool:
         return bool(self.ctx._l.dsrg_renderer_takes_triangles(self.handle))
+
+    def give_triangles(self, corners: np.ndarray, colors, tex_coords, diffuse: Optional["Texture"] = None,
+                       light: Optional["Texture"] = None, filter: int = 0, camera: Optional[Camera] = None):
+        """renderer_giveTask_triangle for n triangles: corners (n, 3) of PROJECTED_POINT, colors and
+        tex_coords (n, 3, 4) float32."""
+        corners = np.ascontiguousarray(corners, PROJECTED_POINT)
+        colors = np.ascontiguousarray(colors, np.float32)
+        tex = np.ascontiguousarray(tex_coords, np.float32)
+        n = corners.shape[0]
+        self.ctx._check(self.ctx._l.dsrg_renderer_give_triangles(
+            self.handle, n, corners.ctypes.data, colors.ctypes.data, tex.ctypes.data, diffuse.handle if diffuse else None,
+            light.handle if light else None, filter, C.byref(camera)))
+
+    def images(self):
+        c, dd = Image(), Image()
+        self.ctx._check(self.ctx._l.dsrg_renderer_get_images(self.handle, C.byref(c), C.byref(dd)))
+        return c, dd
 
     # the occlusion grid (renderer_occludeFromBox / FromExistingTriangles / FromTopRows, isBoxVisible)
     def occlude_from_box(self, minimum, maximum, transform, camera: Camera, debug_silhouette: bool = False):

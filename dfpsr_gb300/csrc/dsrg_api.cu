@@ -239,6 +239,13 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 	r->textures.clear();
 	r->textureHandles.clear();
 	r->tasks.clear();
+	r->givenPoints.clear();
+	r->givenPolygons.clear();
+	r->givenSource.clear();
+	r->givenTexCoords.clear();
+	r->givenColors.clear();
+	r->givenTasks.clear();
+	r->givenDirty = false;
 	CUDA_TRY(ctx, cudaEventRecord(ctx->eventStart, ctx->stream));
 	r->receiving = true;
 	return DSRG_OK;
@@ -302,7 +309,116 @@ int dsrg_renderer_give_task(dsrg_renderer r, dsrg_model m, const float *modelToW
 	return give_task(r, m, modelToWorld, camera);
 }
 
+int dsrg_renderer_get_images(dsrg_renderer r, dsrg_image *color, dsrg_image *depth) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_image none;
+	memset(&none, 0, sizeof(none));
+	if (color) *color = (r->receiving && r->hasColor) ? r->color : none;
+	if (depth) *depth = (r->receiving && r->hasDepth) ? r->depth : none;
+	return DSRG_OK;
+}
+
+int dsrg_camera_world_to_screen(const dsrg_camera *camera, const float *world, dsrg_projected_point *out) {
+	if (!camera || !world || !out || camera->width <= 0 || camera->height <= 0) return DSRG_ERROR_INVALID_ARGUMENT;
+	const CameraData c = make_camera(*camera);
+	const Projected p = camera_to_screen(c, world_to_camera(c, vec3(world[0], world[1], world[2])));
+	out->cs[0] = p.cs.x; out->cs[1] = p.cs.y; out->cs[2] = p.cs.z;
+	out->is[0] = p.isx; out->is[1] = p.isy;
+	out->flat[0] = p.flatx; out->flat[1] = p.flaty;
+	return DSRG_OK;
+}
+
+// renderer_giveTask_triangle (api/rendererAPI.cpp:503-519): one task of pre-projected triangles,
+// drawn at renderer_end in submission order with the models given around it.
+int dsrg_renderer_give_triangles(dsrg_renderer r, int32_t count, const dsrg_projected_point *corners, const float *colors,
+                                 const float *texCoords, dsrg_texture diffuse, dsrg_texture light, int32_t filter,
+                                 const dsrg_camera *camera) {
+	if (!r) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_context ctx = r->context;
+	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Cannot call renderer_giveTask before renderer_begin!");
+	if (count < 0 || !camera || (count > 0 && (!corners || !colors || !texCoords)))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: invalid argument");
+	if (camera->width <= 0 || camera->height <= 0)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: camera without image size");
+	if (filter != DSRG_FILTER_SOLID && filter != DSRG_FILTER_ALPHA)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: unknown filter");
+	if ((diffuse && diffuse->context != ctx) || (light && light->context != ctx))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: texture of another context");
+	if (r->cameraKnown && r->affine != !camera->perspective)
+		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: perspective and orthogonal cameras cannot share one frame");
+	r->affine = !camera->perspective;
+	r->cameraKnown = true;
+	if (count == 0 || (!r->hasColor && !r->hasDepth)) return DSRG_OK; // renderTriangleFromData: no target to draw on
+	TaskParams task;
+	memset(&task, 0, sizeof(task));
+	task.pointCount = 3 * count;
+	task.triangleCount = count;
+	task.orderBase = r->triangleCount;
+	task.frame = 0;
+	const float identity[12] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+	memcpy(task.modelToWorld, identity, sizeof(identity));
+	task.camera = make_camera(*camera);
+	task.filter = filter;
+	task.diffuse = r->depthOnly ? -1 : texture_slot(r, diffuse);
+	task.light = r->depthOnly ? -1 : texture_slot(r, light);
+	task.depthOnly = r->depthOnly ? 1 : 0;
+	const uint32_t first = (uint32_t)r->givenSource.size();
+	for (int32_t i = 0; i < count; i++) {
+		for (int k = 0; k < 3; k++) {
+			GivenPoint g;
+			memcpy(&g, &corners[3 * i + k], sizeof(g));
+			r->givenPoints.push_back(g);
+		}
+		const int32_t poly[4] = {3 * i, 3 * i + 1, 3 * i + 2, -1};
+		r->givenPolygons.insert(r->givenPolygons.end(), poly, poly + 4);
+		r->givenSource.push_back(2 * i); // polygon i, first fan triangle
+		for (int k = 0; k < 4; k++) {
+			for (int c = 0; c < 4; c++) {
+				r->givenTexCoords.push_back(k < 3 ? texCoords[(3 * i + k) * 4 + c] : 0.0f);
+				r->givenColors.push_back(k < 3 ? colors[(3 * i + k) * 4 + c] : 0.0f);
+			}
+		}
+	}
+	r->givenTasks.push_back(std::make_pair(r->tasks.size(), first));
+	r->tasks.push_back(task);
+	r->triangleCount += (uint32_t)count;
+	r->givenDirty = true;
+	return DSRG_OK;
+}
+
 } // extern "C"
+
+int renderer_upload_given(dsrg_renderer r) {
+	if (!r->givenDirty) return DSRG_OK;
+	dsrg_context ctx = r->context;
+	const size_t triangles = r->givenSource.size();
+	auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+	const size_t pointsAt = 0;
+	const size_t polygonsAt = align(pointsAt + triangles * 3 * sizeof(GivenPoint));
+	const size_t sourceAt = align(polygonsAt + triangles * 4 * sizeof(int32_t));
+	const size_t texAt = align(sourceAt + triangles * sizeof(int32_t));
+	const size_t colorsAt = align(texAt + triangles * 16 * sizeof(float));
+	const size_t bytes = align(colorsAt + triangles * 16 * sizeof(float));
+	CUDA_TRY(ctx, r->givenDevice.reserve(bytes));
+	unsigned char *base = r->givenDevice.ptr;
+	cudaStream_t stream = ctx->stream;
+	CUDA_TRY(ctx, cudaMemcpyAsync(base + pointsAt, r->givenPoints.data(), triangles * 3 * sizeof(GivenPoint), cudaMemcpyHostToDevice, stream));
+	CUDA_TRY(ctx, cudaMemcpyAsync(base + polygonsAt, r->givenPolygons.data(), triangles * 4 * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+	CUDA_TRY(ctx, cudaMemcpyAsync(base + sourceAt, r->givenSource.data(), triangles * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+	CUDA_TRY(ctx, cudaMemcpyAsync(base + texAt, r->givenTexCoords.data(), triangles * 16 * sizeof(float), cudaMemcpyHostToDevice, stream));
+	CUDA_TRY(ctx, cudaMemcpyAsync(base + colorsAt, r->givenColors.data(), triangles * 16 * sizeof(float), cudaMemcpyHostToDevice, stream));
+	for (const auto &gt : r->givenTasks) {
+		TaskParams &t = r->tasks[gt.first];
+		const size_t first = gt.second;
+		t.given = reinterpret_cast<const GivenPoint *>(base + pointsAt) + first * 3;
+		t.polygons = reinterpret_cast<const int32_t *>(base + polygonsAt) + first * 4;
+		t.triSource = reinterpret_cast<const int32_t *>(base + sourceAt) + first;
+		t.texCoords = reinterpret_cast<const float *>(base + texAt) + first * 16;
+		t.colors = reinterpret_cast<const float *>(base + colorsAt) + first * 16;
+	}
+	r->givenDirty = false;
+	return DSRG_OK;
+}
 
 void renderer_frame_target(dsrg_renderer r, FrameTarget &f) {
 	memset(&f, 0, sizeof(f));
@@ -329,6 +445,8 @@ static int end_frame(dsrg_renderer r, bool debugWireframe) {
 	dsrg_context ctx = r->context;
 	if (!r->receiving) return fail(ctx, DSRG_ERROR_CALL_ORDER, "Called renderer_end without renderer_begin!");
 	r->receiving = false;
+	const int uploaded = renderer_upload_given(r);
+	if (uploaded != DSRG_OK) return uploaded;
 	BatchJob &job = ctx->frameJob;
 	job.tasks.swap(r->tasks);
 	job.textures.swap(r->textures);

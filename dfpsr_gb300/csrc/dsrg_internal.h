@@ -234,6 +234,14 @@ struct dsrg_renderer_s {
 	std::vector<dsrg_texture> textureHandles;
 	std::vector<TaskParams> tasks;
 	std::vector<TaskParams> runTasks; // the frame's tasks while it runs as alpha-filtered and other runs
+	// renderer_giveTask_triangle data of this frame, uploaded before the tasks run (given tasks
+	// point into the device copy; givenTasks lists them with their first triangle)
+	std::vector<dsrg::GivenPoint> givenPoints;
+	std::vector<int32_t> givenPolygons, givenSource;
+	std::vector<float> givenTexCoords, givenColors;
+	std::vector<std::pair<size_t, uint32_t>> givenTasks;
+	bool givenDirty = false;
+	DeviceBuffer<unsigned char> givenDevice;
 	// occlusion grid (RendererImpl::depthGrid, api/rendererAPI.cpp:141-191): one float per 16x16
 	// cell, kept on the host for box occluders and box tests and on the device for the per-command
 	// work; whichever copy is stale is refreshed from the other before it is used
@@ -251,6 +259,8 @@ struct dsrg_renderer_s {
 	DeviceBuffer<int4> debugLinesDevice;
 };
 
+// Uploads the frame's renderer_giveTask_triangle data and points its tasks at it.
+int renderer_upload_given(dsrg_renderer r);
 // The frame target of a renderer's current frame (images, size, occlusion grid when in use).
 void renderer_frame_target(dsrg_renderer r, dsrg::FrameTarget &f);
 // Uploads the occlusion grid when the device copy is stale.

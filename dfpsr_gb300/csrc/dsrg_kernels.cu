@@ -62,6 +62,13 @@ __global__ void project_kernel(BatchParams b, ProjectedPoints out) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < b.totalPoints; i += gridDim.x * blockDim.x) {
 		const TaskParams &task = b.tasks[find_segment(b.taskPointBase, b.taskCount, i)];
 		const uint32_t local = i - task.pointBase;
+		if (task.given) { // renderer_giveTask_triangle: projected by the caller
+			const GivenPoint &g = task.given[local];
+			out.csx[i] = g.cs[0]; out.csy[i] = g.cs[1]; out.csz[i] = g.cs[2];
+			out.isx[i] = g.is[0]; out.isy[i] = g.is[1];
+			out.flatx[i] = g.flat[0]; out.flaty[i] = g.flat[1];
+			continue;
+		}
 		Vec3 p = vec3(task.positions[local * 3], task.positions[local * 3 + 1], task.positions[local * 3 + 2]);
 		Projected pr = camera_to_screen(task.camera, world_to_camera(task.camera, transform_point(task.modelToWorld, p)));
 		out.csx[i] = pr.cs.x; out.csy[i] = pr.cs.y; out.csz[i] = pr.cs.z;

@@ -30,6 +30,7 @@ struct TaskParams {
 	int32_t filter;           // 0 Solid, 1 Alpha
 	int32_t diffuse, light;   // indices into the batch's texture table, -1 for none
 	int32_t depthOnly;        // model_renderDepth: 1x1 alignment, no shading (renderCore.cpp:343-443)
+	const GivenPoint *given;  // renderer_giveTask_triangle: the corners come projected (positions unused)
 };
 
 // One frame of a batch: its target images, its key image and its range of tiles.

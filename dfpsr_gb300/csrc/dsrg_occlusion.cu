@@ -229,7 +229,9 @@ int dsrg_renderer_occlude_from_existing_triangles(dsrg_renderer r) {
 		return fail(ctx, DSRG_ERROR_CALL_ORDER, "Cannot call renderer_occludeFromExistingTriangles without first calling renderer_begin!");
 	prepare_for_occlusion(r);
 	if (r->tasks.empty()) return DSRG_OK;
-	int s = renderer_grid_on_device(r);
+	int s = renderer_upload_given(r);
+	if (s != DSRG_OK) return s;
+	s = renderer_grid_on_device(r);
 	if (s != DSRG_OK) return s;
 	BatchJob job;
 	job.tasks = r->tasks;

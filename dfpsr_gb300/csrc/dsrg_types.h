@@ -45,6 +45,15 @@ struct TextureData {
 	int32_t exists;
 };
 
+// A corner given already projected (ProjectedPoint, implementation/render/ProjectedPoint.h:33-49),
+// laid out as dsrg_projected_point of the C interface.
+struct GivenPoint {
+	float cs[3];
+	float is[2];
+	int64_t flat[2];
+};
+static_assert(sizeof(GivenPoint) == 40, "GivenPoint layout");
+
 // Projected corner (implementation/render/ProjectedPoint.h:33-49), structure of arrays.
 struct ProjectedPoints {
 	float *csx, *csy, *csz;

@@ -147,6 +147,26 @@ int dsrg_renderer_end(dsrg_renderer renderer);
 int dsrg_renderer_end_debug(dsrg_renderer renderer, int32_t debugWireframe);
 /* renderer_takesTriangles (api/rendererAPI.h:67): 1 between begin and end. */
 int dsrg_renderer_takes_triangles(dsrg_renderer renderer);
+/* renderer_getColorBuffer / renderer_getDepthBuffer (api/rendererAPI.h:60-63): the images given
+ * to renderer_begin while the renderer takes triangles, else images with data = NULL. */
+int dsrg_renderer_get_images(dsrg_renderer renderer, dsrg_image *color, dsrg_image *depth);
+
+/* ProjectedPoint (implementation/render/ProjectedPoint.h:33-49): camera-space position, image
+ * position and the sub-pixel position (1/256 pixel) the rasterizer uses. */
+typedef struct {
+	float cs[3];
+	float is[2];
+	int64_t flat[2];
+} dsrg_projected_point;
+/* Camera::worldToScreen (implementation/render/Camera.h:160-190), on the host. */
+int dsrg_camera_world_to_screen(const dsrg_camera *camera, const float *world, dsrg_projected_point *out);
+/* renderer_giveTask_triangle (api/rendererAPI.h:82-93) for count triangles sharing textures, filter
+ * and camera: corners[3 * i + k], colors[(3 * i + k) * 4] (RGBA, 1 = full) and
+ * texCoords[(3 * i + k) * 4] (u1, v1 for the diffuse map, u2, v2 for the light map) give corner
+ * k of triangle i, already projected with the camera.  Host memory, copied by the call. */
+int dsrg_renderer_give_triangles(dsrg_renderer renderer, int32_t count, const dsrg_projected_point *corners, const float *colors,
+                                 const float *texCoords, dsrg_texture diffuse, dsrg_texture light, int32_t filter,
+                                 const dsrg_camera *camera);
 
 /* The renderer's occlusion grid (api/rendererAPI.h:69-101, rendererAPI.cpp:141-477): one value per
  * 16x16-pixel cell, the farthest camera-space depth at which something in the cell may still be

@@ -166,6 +166,15 @@ void or_camera_to_screen(const or_camera_desc *desc, const float cs[3], float ou
 	outFlat[0] = p.flat.x; outFlat[1] = p.flat.y;
 }
 
+/* Camera::worldToScreen (Camera.h:188-190): out = cs.x, cs.y, cs.z, is.x, is.y; outFlat = flat. */
+void or_world_to_screen(const or_camera_desc *desc, const float world[3], float out[5], int64_t outFlat[2]) {
+	camera c;
+	camera_create(&c, desc);
+	projected p = camera_to_screen(&c, world_to_camera(&c, mk3(world[0], world[1], world[2])));
+	out[0] = p.cs.x; out[1] = p.cs.y; out[2] = p.cs.z; out[3] = p.is.x; out[4] = p.is.y;
+	outFlat[0] = p.flat.x; outFlat[1] = p.flat.y;
+}
+
 /* ViewFrustum::isConvexHullSeen (Camera.h:87-108). */
 static int convex_hull_seen(const plane3 *planes, int planeCount, const v3 *points, int count) {
 	int anyOutside = 0;
@@ -2028,6 +2037,32 @@ int or_renderer_give_task(or_renderer *r, const or_model *model, const float mod
 	}
 	for (size_t i = before; i < r->commands.count; i++) { r->commands.items[i].task = taskIndex; r->commands.items[i].occluded = 0; }
 	free(proj);
+	return 0;
+}
+
+/* renderer_giveTask_triangle (rendererAPI.cpp:503-519): renderTriangleFromData of corners given
+ * projected; corner k of the triangle: cs (3 floats), is (2 floats), flat (2 int64). */
+int or_renderer_give_triangle(or_renderer *r, const float cs[9], const float is[6], const int64_t flat[6], const float colors[12],
+                              const float texCoords[12], const or_texture *diffuse, const or_texture *light, int filter,
+                              const or_camera_desc *desc) {
+	if (!r->receiving) return -1;
+	if (r->camCount == r->camCapacity) {
+		r->camCapacity = r->camCapacity ? r->camCapacity * 2 : 16;
+		r->cams = (camera *)realloc(r->cams, sizeof(camera) * (size_t)r->camCapacity);
+	}
+	const int32_t taskIndex = r->camCount++;
+	camera_create(&r->cams[taskIndex], desc);
+	projected p[3];
+	for (int k = 0; k < 3; k++) {
+		p[k].cs = mk3(cs[3 * k], cs[3 * k + 1], cs[3 * k + 2]);
+		p[k].is.x = is[2 * k]; p[k].is.y = is[2 * k + 1];
+		p[k].flat.x = flat[2 * k]; p[k].flat.y = flat[2 * k + 1];
+	}
+	const size_t before = r->commands.count;
+	submit_triangle(&r->commands, &r->cams[taskIndex], r->color != NULL, r->depth != NULL, r->width, r->height, p[0], p[1], p[2],
+	                filter, diffuse, light, texCoords, texCoords + 4, texCoords + 8, colors, colors + 4, colors + 8, r->triangles);
+	r->triangles++;
+	for (size_t i = before; i < r->commands.count; i++) { r->commands.items[i].task = taskIndex; r->commands.items[i].occluded = 0; }
 	return 0;
 }
 

@@ -81,6 +81,7 @@ uint32_t or_mip_level_index(const or_texture *t, const float u[4], const float v
 
 /* ---- geometry ---- */
 void or_camera_to_screen(const or_camera_desc *cam, const float cs[3], float outIs[2], int64_t outFlat[2]);
+void or_world_to_screen(const or_camera_desc *cam, const float world[3], float out[5], int64_t outFlat[2]);
 int32_t or_triangle_rows(const int64_t flat[6], const int32_t clip[4], int32_t *startRow, int32_t *lefts, int32_t *rights, int32_t maxRows);
 
 /* ---- rendering ---- */
@@ -104,6 +105,9 @@ int or_renderer_give_task(or_renderer *r, const or_model *model, const float mod
 /* debugSilhouette keeps the box's hull as cyan lines drawn at renderer_end. */
 int or_renderer_occlude_from_box(or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],
                                  const or_camera_desc *cam, int debugSilhouette);
+int or_renderer_give_triangle(or_renderer *r, const float cs[9], const float is[6], const int64_t flat[6], const float colors[12],
+                              const float texCoords[12], const or_texture *diffuse, const or_texture *light, int filter,
+                              const or_camera_desc *cam);
 int or_renderer_occlude_from_existing_triangles(or_renderer *r);
 int or_renderer_occlude_from_top_rows(or_renderer *r, int perspective);
 int or_renderer_is_box_visible(const or_renderer *r, const float mn[3], const float mx[3], const float modelToWorld[12],

@@ -95,6 +95,9 @@ def lib():
         l.or_renderer_give_task.argtypes = [R, C.POINTER(Model), P, C.POINTER(CameraDesc)]
         l.or_renderer_occlude_from_box.argtypes = [R, P, P, P, C.POINTER(CameraDesc), C.c_int]
         l.or_renderer_occlude_from_existing_triangles.argtypes = [R]
+        l.or_renderer_give_triangle.argtypes = [R, P, P, P, P, P, C.POINTER(Texture), C.POINTER(Texture), C.c_int,
+                                                C.POINTER(CameraDesc)]
+        l.or_world_to_screen.argtypes = [C.POINTER(CameraDesc), P, P, P]
         l.or_renderer_occlude_from_top_rows.argtypes = [R, C.c_int]
         l.or_renderer_is_box_visible.argtypes = [R, P, P, P, C.POINTER(CameraDesc)]
         l.or_renderer_has_occluders.argtypes = [R]
@@ -371,6 +374,17 @@ class OracleRenderer:
     def occlude_from_existing_triangles(self):
         assert lib().or_renderer_occlude_from_existing_triangles(self.h) == 0
 
+    def give_triangles(self, cs, is_, flat, colors, tex, diffuse: Optional["OracleTexture"], light: Optional["OracleTexture"],
+                       filter_: int, cam: CameraDesc):
+        """cs (n, 3, 3) float32, is_ (n, 3, 2) float32, flat (n, 3, 2) int64, colors and tex (n, 3, 4) float32."""
+        arrays = [np.ascontiguousarray(a, dt) for a, dt in ((cs, np.float32), (is_, np.float32), (flat, np.int64),
+                                                              (colors, np.float32), (tex, np.float32))]
+        self._keep.append((arrays, diffuse, light))
+        n = arrays[0].shape[0]
+        for i in range(n):
+            assert lib().or_renderer_give_triangle(self.h, *[_ptr(a[i]) for a in arrays], diffuse.ref() if diffuse else None,
+                                                   light.ref() if light else None, filter_, C.byref(cam)) == 0
+
     def occlude_from_top_rows(self, perspective: bool):
         return lib().or_renderer_occlude_from_top_rows(self.h, 1 if perspective else 0)
 
@@ -405,3 +419,13 @@ def draw_line(image: np.ndarray, x1: int, y1: int, x2: int, y2: int, color: int)
     h, w = out.shape
     lib().or_draw_line(_ptr(out), w, h, x1, y1, x2, y2, color)
     return out
+
+
+def world_to_screen(cam: CameraDesc, world) -> tuple:
+    """Camera::worldToScreen of (n, 3) points: cs (n, 3), is (n, 2), flat (n, 2) int64."""
+    world = np.ascontiguousarray(world, np.float32).reshape(-1, 3)
+    out = np.zeros((len(world), 5), np.float32)
+    flat = np.zeros((len(world), 2), np.int64)
+    for i in range(len(world)):
+        lib().or_world_to_screen(C.byref(cam), _ptr(world[i]), _ptr(out[i]), _ptr(flat[i]))
+    return out[:, :3].copy(), out[:, 3:].copy(), flat

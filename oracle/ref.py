@@ -79,6 +79,7 @@ def _load(variant: str):
         l.refh_renderer_occlude_from_box.argtypes = [P, P, P, P] + cam + [C.c_int]
         l.refh_draw_line.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32]
         l.refh_renderer_occlude_from_existing_triangles.argtypes = [P]
+        l.refh_renderer_give_triangle.argtypes = [P, P, P, P, P, P, P, P, C.c_int] + cam
         l.refh_renderer_occlude_from_top_rows.argtypes = [P] + cam
         l.refh_renderer_is_box_visible.argtypes = [P, P, P, P] + cam
         l.refh_renderer_is_box_visible.restype = C.c_int
@@ -303,6 +304,15 @@ class RefRenderer:
 
     def occlude_from_existing_triangles(self):
         self.lib.refh_renderer_occlude_from_existing_triangles(self.h)
+
+    def give_triangles(self, cs, is_, flat, colors, tex, diffuse: Optional["RefTexture"], light: Optional["RefTexture"],
+                       filter_: int, cam):
+        arrays = [np.ascontiguousarray(a, dt) for a, dt in ((cs, np.float32), (is_, np.float32), (flat, np.int64),
+                                                              (colors, np.float32), (tex, np.float32))]
+        loc, args = _camera_args(cam)
+        for i in range(arrays[0].shape[0]):
+            self.lib.refh_renderer_give_triangle(self.h, *[_ptr(a[i]) for a in arrays], diffuse.handle if diffuse else None,
+                                                 light.handle if light else None, filter_, *args)
 
     def occlude_from_top_rows(self, cam):
         loc, args = _camera_args(cam)

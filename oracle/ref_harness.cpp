@@ -252,6 +252,25 @@ void refh_draw_line(uint32_t* pixels, int width, int height, int x1, int y1, int
 	copyOutRgba(image, pixels, width, height);
 }
 
+// renderer_giveTask_triangle for one triangle: cs 3 x 3, is 3 x 2, flat 3 x 2, colors and texCoords 3 x 4.
+void refh_renderer_give_triangle(void* handle, const float* cs, const float* is, const int64_t* flat, const float* colors,
+                                 const float* texCoords, void* diffuse, void* light, int filter, const float* cameraLocation,
+                                 int perspective, float slope, float nearClip, float farClip, int width, int height) {
+	RendererBox* box = (RendererBox*)handle;
+	CameraArgs c = {cameraLocation, perspective, slope, nearClip, farClip, width, height};
+	ProjectedPoint p[3];
+	for (int k = 0; k < 3; k++) {
+		p[k] = ProjectedPoint(FVector3D(cs[3 * k], cs[3 * k + 1], cs[3 * k + 2]), FVector2D(is[2 * k], is[2 * k + 1]),
+		                      LVector2D(flat[2 * k], flat[2 * k + 1]));
+	}
+	auto v4 = [](const float* v) { return FVector4D(v[0], v[1], v[2], v[3]); };
+	TextureRgbaU8 noTexture;
+	renderer_giveTask_triangle(box->renderer, p[0], p[1], p[2], v4(colors), v4(colors + 4), v4(colors + 8), v4(texCoords),
+	                           v4(texCoords + 4), v4(texCoords + 8), diffuse ? ((TextureBox*)diffuse)->texture : noTexture,
+	                           light ? ((TextureBox*)light)->texture : noTexture, filter ? Filter::Alpha : Filter::Solid,
+	                           makeCamera(c));
+}
+
 void refh_renderer_occlude_from_existing_triangles(void* handle) {
 	renderer_occludeFromExistingTriangles(((RendererBox*)handle)->renderer);
 }
