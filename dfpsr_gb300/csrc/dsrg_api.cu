@@ -32,7 +32,8 @@ int dsrg_context_create(int32_t device, dsrg_context *out) {
 	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
-	    ctx->control.reserve(4) != cudaSuccess || ctx->fragmentCounter.reserve(1) != cudaSuccess) {
+	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(1) != cudaSuccess ||
+	    cudaMallocHost((void **)&ctx->pinnedReadback, 16 * sizeof(uint32_t)) != cudaSuccess) {
 		delete ctx;
 		return DSRG_ERROR_CUDA;
 	}
@@ -56,6 +57,7 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	for (auto *b : ubufs) b->release();
 	ctx->records.release(); ctx->tables.release(); ctx->keys.release();
 	if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
+	if (ctx->pinnedReadback) cudaFreeHost(ctx->pinnedReadback);
 	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
 	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);

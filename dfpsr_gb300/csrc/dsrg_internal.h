@@ -171,7 +171,10 @@ struct dsrg_context_s {
 	DeviceBuffer<unsigned char> tables;  // the batch's task, frame and texture tables
 	unsigned char *pinnedTables = nullptr; // host staging of the tables (page-locked)
 	size_t pinnedCapacity = 0;
-	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag
+	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag, [4..7] a batch's gathered totals
+	uint32_t *pinnedReadback = nullptr;  // page-locked copy of the gathered totals
+	// capacities of the buffers sized before their totals are known (largest totals seen, with slack)
+	uint64_t recordCapacity = 0, rowCapacity = 0, binCapacity = 0;
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
 	DeviceBuffer<TextureData> textureTable;
 	DeviceBuffer<uint32_t> stagingColor;
@@ -277,6 +280,9 @@ int renderer_box_occluded(dsrg_renderer r, const float *minimum, const float *ma
 			return _e == cudaErrorMemoryAllocation ? DSRG_ERROR_OUT_OF_MEMORY : DSRG_ERROR_CUDA; \
 		}                                                                                        \
 	} while (0)
+
+// Internal status of a batch attempt whose buffers were too small (never returned to callers).
+const int DSRG_RETRY = 100;
 
 inline int fail(dsrg_context ctx, int code, const std::string &message) {
 	if (ctx) ctx->lastError = message;

@@ -56,6 +56,17 @@ static int grid_for(uint64_t n, int threads) {
 	return (int)(blocks > 0 ? blocks : 1);
 }
 
+// A count written on the device, bounded by the capacity the host sized the buffers for.
+__device__ __forceinline__ uint32_t device_count(uint32_t capacity, const uint32_t *countDevice) {
+	if (!countDevice) return capacity;
+	const uint32_t n = *countDevice;
+	return n < capacity ? n : capacity;
+}
+
+__device__ __forceinline__ bool overflowed(const BatchParams &b) {
+	return b.errorFlag && (*(volatile const int32_t *)b.errorFlag & ERROR_OVERFLOW_BITS) != 0;
+}
+
 // ------------------------------------------------------------------ projection
 
 __global__ void project_kernel(BatchParams b, ProjectedPoints out) {
@@ -292,78 +303,141 @@ void launch_occlusion_top_rows(float *grid, int32_t gridWidth, int32_t gridHeigh
 
 // ------------------------------------------------------------------ scan
 
-static const int SCAN_BLOCK = 1024;
+// Exclusive scan in two launches and no host round trip: the first writes one sum per chunk of
+// SCAN_CHUNK values, the second gives every chunk the sum of the chunk sums before it (read by
+// the whole block) and scans the chunk through shared memory.  The length may live on the
+// device (a count written by an earlier kernel), with `capacity` bounding it for the grid.
+static const int SCAN_THREADS = 256;
+static const int SCAN_PER_THREAD = 16;
+static const uint32_t SCAN_CHUNK = SCAN_THREADS * SCAN_PER_THREAD;
 
-__global__ void scan_blocks_kernel(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *blockSums) {
-	__shared__ uint32_t warpSums[32];
-	uint32_t i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
-	uint32_t v = i < n ? in[i] : 0u;
-	uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t x = v;
+__device__ __forceinline__ uint32_t scan_length(uint32_t n, const uint32_t *nDevice, uint32_t capacity) {
+	if (!nDevice) return n;
+	const uint32_t d = *nDevice;
+	return d < capacity ? d : capacity;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *shared) {
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+	if ((threadIdx.x & 31) == 0) shared[threadIdx.x >> 5] = v;
+	__syncthreads();
+	uint32_t total = 0;
+	for (int w = 0; w < SCAN_THREADS / 32; w++) total += shared[w];
+	__syncthreads();
+	return total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_t *__restrict__ in, uint32_t n, const uint32_t *nDevice,
+                                                                   uint32_t capacity, uint32_t *chunkSums) {
+	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
+	const uint32_t count = scan_length(n, nDevice, capacity);
+	const uint32_t begin = blockIdx.x * SCAN_CHUNK;
+	uint32_t v = 0;
+	for (uint32_t i = begin + threadIdx.x; i < begin + SCAN_CHUNK && i < count; i += SCAN_THREADS) v += in[i];
+	const uint32_t total = block_sum(v, warpSums);
+	if (threadIdx.x == 0) chunkSums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(const uint32_t *__restrict__ in, uint32_t *out, uint32_t n,
+                                                                  const uint32_t *nDevice, uint32_t capacity,
+                                                                  const uint32_t *__restrict__ chunkSums) {
+	__shared__ uint32_t values[SCAN_CHUNK + SCAN_CHUNK / 32]; // one padding word per 32: a thread's 16 values hit 16 banks
+	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
+	const uint32_t count = scan_length(n, nDevice, capacity);
+	const uint32_t begin = blockIdx.x * SCAN_CHUNK;
+	if (begin > count || (begin == count && count != 0)) return;
+	// the sum of every chunk before this one
+	uint32_t p = 0;
+	for (uint32_t c = threadIdx.x; c < blockIdx.x; c += SCAN_THREADS) p += chunkSums[c];
+	const uint32_t prefix = block_sum(p, warpSums);
+	for (int k = 0; k < SCAN_PER_THREAD; k++) {
+		const uint32_t i = begin + k * SCAN_THREADS + threadIdx.x;
+		const uint32_t at = k * SCAN_THREADS + threadIdx.x;
+		values[at + (at >> 5)] = i < count ? in[i] : 0u;
+	}
+	__syncthreads();
+	uint32_t local[SCAN_PER_THREAD];
+	uint32_t mine = 0;
+	for (int k = 0; k < SCAN_PER_THREAD; k++) {
+		local[k] = mine;
+		const uint32_t at = threadIdx.x * SCAN_PER_THREAD + k;
+		mine += values[at + (at >> 5)];
+	}
+	// exclusive scan of the threads' sums
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t x = mine;
 	for (int o = 1; o < 32; o <<= 1) {
-		uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-		if (lane >= (uint32_t)o) x += y;
+		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+		if (lane >= o) x += y;
 	}
 	if (lane == 31) warpSums[warp] = x;
 	__syncthreads();
-	if (warp == 0) {
-		uint32_t s = warpSums[lane];
-		for (int o = 1; o < 32; o <<= 1) {
-			uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
-			if (lane >= (uint32_t)o) s += y;
-		}
-		warpSums[lane] = s;
+	uint32_t before = prefix + x - mine;
+	for (int w = 0; w < warp; w++) before += warpSums[w];
+	for (int k = 0; k < SCAN_PER_THREAD; k++) {
+		const uint32_t at = threadIdx.x * SCAN_PER_THREAD + k;
+		values[at + (at >> 5)] = before + local[k];
 	}
 	__syncthreads();
-	uint32_t prefix = (warp > 0 ? warpSums[warp - 1] : 0u) + x - v;
-	if (i < n) out[i] = prefix;
-	if (threadIdx.x == SCAN_BLOCK - 1) blockSums[blockIdx.x] = prefix + v;
-}
-
-__global__ void scan_add_kernel(uint32_t *out, uint32_t n, const uint32_t *blockOffsets) {
-	uint32_t i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
-	if (i < n) out[i] += blockOffsets[blockIdx.x];
-}
-
-__global__ void scan_total_kernel(const uint32_t *blockOffsets, const uint32_t *blockSums, uint32_t blocks, uint32_t *out, uint32_t n) {
-	out[n] = blockOffsets[blocks - 1] + blockSums[blocks - 1];
-}
-
-size_t scan_scratch_elems(uint32_t n) {
-	size_t total = 0;
-	uint32_t blocks = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
-	while (true) {
-		total += 2 * (size_t)(blocks + 1);
-		if (blocks <= 1) break;
-		blocks = (blocks + SCAN_BLOCK - 1) / SCAN_BLOCK;
+	for (int k = 0; k < SCAN_PER_THREAD; k++) {
+		const uint32_t i = begin + k * SCAN_THREADS + threadIdx.x;
+		const uint32_t at = k * SCAN_THREADS + threadIdx.x;
+		if (i < count) out[i] = values[at + (at >> 5)];
 	}
-	return total + 16;
+	// the total after the last value, by the block holding it
+	if (threadIdx.x == SCAN_THREADS - 1 && (count == 0 || (count - 1) / SCAN_CHUNK == blockIdx.x)) {
+		uint32_t total = prefix;
+		for (int w = 0; w < SCAN_THREADS / 32; w++) total += warpSums[w];
+		out[count] = total;
+	}
+}
+
+size_t scan_scratch_elems(uint32_t n) { return (size_t)(n / SCAN_CHUNK) + 16; }
+
+static void scan_launch(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *nDevice, uint32_t *scratch, size_t scratchElems,
+                        cudaStream_t stream) {
+	const uint32_t blocks = n / SCAN_CHUNK + 1; // n = the length, or the capacity bounding a device length
+	if (blocks > scratchElems) {
+		cudaMemsetAsync(out, 0xFF, sizeof(uint32_t), stream); // never reached: callers size the scratch
+		return;
+	}
+	COUNT_LAUNCH();
+	scan_reduce_kernel<<<blocks, SCAN_THREADS, 0, stream>>>(in, n, nDevice, n, scratch);
+	COUNT_LAUNCH();
+	scan_apply_kernel<<<blocks, SCAN_THREADS, 0, stream>>>(in, out, n, nDevice, n, scratch);
 }
 
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream) {
-	if (n == 0) {
-		cudaMemsetAsync(out, 0, sizeof(uint32_t), stream);
-		return;
-	}
-	uint32_t blocks = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
-	uint32_t *blockSums = scratch;
-	uint32_t *blockOffsets = scratch + blocks + 1;
+	scan_launch(in, out, n, nullptr, scratch, scratchElems, stream);
+}
+
+void launch_scan_device(const uint32_t *in, uint32_t *out, const uint32_t *nDevice, uint32_t capacity, uint32_t *scratch,
+                        size_t scratchElems, cudaStream_t stream) {
+	scan_launch(in, out, capacity, nDevice, scratch, scratchElems, stream);
+}
+
+// The totals a batch's host side reads once its phases ran: records, rows, tile-list entries and
+// the error bits, gathered into one small block for a single copy.
+__global__ void gather_totals_kernel(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
+                                     const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out) {
+	const uint32_t records = triOffsets[triangles];
+	out[0] = records;
+	out[1] = rowOffsets[records < recordCapacity ? records : recordCapacity];
+	out[2] = binOffsets[binSlots];
+	out[3] = (uint32_t)*errorFlag;
+}
+
+void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
+                          const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out, cudaStream_t stream) {
 	COUNT_LAUNCH();
-	scan_blocks_kernel<<<blocks, SCAN_BLOCK, 0, stream>>>(in, out, n, blockSums);
-	if (blocks > 1) {
-		launch_scan(blockSums, blockOffsets, blocks, scratch + 2 * (blocks + 1), scratchElems - 2 * (blocks + 1), stream);
-		COUNT_LAUNCH();
-		scan_add_kernel<<<blocks, SCAN_BLOCK, 0, stream>>>(out, n, blockOffsets);
-	} else {
-		cudaMemsetAsync(blockOffsets, 0, sizeof(uint32_t), stream);
-	}
-	COUNT_LAUNCH();
-	scan_total_kernel<<<1, 1, 0, stream>>>(blockOffsets, blockSums, blocks, out, n);
+	gather_totals_kernel<<<1, 1, 0, stream>>>(triOffsets, triangles, rowOffsets, recordCapacity, binOffsets, binSlots, errorFlag, out);
 }
 
 // ------------------------------------------------------------------ row intervals
 
-__global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount, uint32_t *counts) {
+__global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t capacity, const uint32_t *countDevice,
+                                 uint32_t *counts) {
+	const uint32_t recordCount = device_count(capacity, countDevice);
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < recordCount; i += gridDim.x * blockDim.x)
 		counts[i] = (uint32_t)(records[i].bottom - records[i].top);
 }
@@ -371,9 +445,12 @@ __global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_
 void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream) {
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		row_count_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, rowCounts);
+		row_count_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, fb.recordCountDevice, rowCounts);
 	}
-	launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
+	if (fb.recordCountDevice)
+		launch_scan_device(rowCounts, fb.rowOffsets, fb.recordCountDevice, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
+	else
+		launch_scan(rowCounts, fb.rowOffsets, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 // Row interval of row y for corners held in registers (row_interval without the corner array).
@@ -390,8 +467,10 @@ __device__ __forceinline__ void row_interval_regs(int32_t x0, int32_t y0, int32_
 // 32 records and spreads the concatenation of their rows over its lanes, so tall and short
 // triangles keep every lane busy: a lane finds the record of its row by a binary search over the
 // warp's prefix sums of row counts and fetches that record's corners with shuffles.
-__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t recordCount,
-                                                   const uint32_t *__restrict__ rowOffsets, uint32_t *rows) {
+__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
+                                                   const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
+                                                   uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
+	const uint32_t recordCount = device_count(capacity, countDevice);
 	const int lane = threadIdx.x & 31;
 	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
 	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32u < recordCount; w += warps) {
@@ -430,7 +509,9 @@ __global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict_
 				const int32_t row = j - start;
 				int32_t left, right;
 				row_interval_regs(kx0, ky0, kx1, ky1, kx2, ky2, kTop + row, kL, kR, left, right);
-				rows[kOut + (uint32_t)row] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				const uint32_t at = kOut + (uint32_t)row;
+				if (at < rowCapacity) rows[at] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				else atomicOr(errorFlag, ERROR_ROW_OVERFLOW);
 			}
 		}
 	}
@@ -440,8 +521,10 @@ void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stre
 	if (recordCount == 0) return;
 	COUNT_LAUNCH();
 	// one warp per 32 records
-	rows_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(fb.records, recordCount, fb.rowOffsets,
-	                                                                                        fb.rows);
+	rows_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(fb.records, recordCount,
+	                                                                                        fb.recordCountDevice, fb.rowOffsets,
+	                                                                                        fb.rows, fb.rowCapacity ? fb.rowCapacity : 0xFFFFFFFFu,
+	                                                                                        fb.errorFlag);
 }
 
 // ------------------------------------------------------------------ binning
@@ -491,8 +574,9 @@ __device__ __forceinline__ bool tile_test_is_exact(const DrawRecord &r) {
 // ones by the whole warp, tested tile by tile.  A list keeps submission order only per warp, which
 // the order-free depth keys do not need.
 template <bool FILL>
-__global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records, uint32_t recordCount, TileBins bins,
-                           int32_t *errorFlag) {
+__global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records, uint32_t capacity, const uint32_t *countDevice,
+                           TileBins bins, int32_t *errorFlag) {
+	const uint32_t recordCount = device_count(capacity, countDevice);
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t stride = gridDim.x * blockDim.x;
 	for (uint32_t r0 = blockIdx.x * blockDim.x; r0 < recordCount; r0 += stride) {
@@ -559,7 +643,8 @@ void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t rec
 	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
+		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
+		                                                                  fb.errorFlag);
 	}
 	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
@@ -568,7 +653,8 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, bins, fb.errorFlag);
+		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
+		                                                                 fb.errorFlag);
 	}
 }
 
@@ -732,6 +818,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
                                                                          TileBins bins, const uint32_t *__restrict__ rowOffsets,
                                                                          const uint32_t *__restrict__ rows) {
 	constexpr int WARPS = THREADS / 32;
+	if (overflowed(b)) return; // the lists or rows are incomplete: the frame is redone
 	constexpr int PIXELS = TILE_W * TILE_H / THREADS; // tile pixels owned by each thread
 	__shared__ unsigned long long keys[TILE_H * TILE_STRIDE];
 	__shared__ float initialDepth[TILE_H * TILE_STRIDE];
@@ -925,6 +1012,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                             const uint32_t *__restrict__ binOffsets,
                                                             const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return; // nothing drawn: the key image was not written here
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
@@ -949,6 +1037,7 @@ __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const
 __global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                              const uint32_t *__restrict__ binOffsets,
                                                              const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
@@ -987,6 +1076,7 @@ __global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, cons
 __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                      const uint32_t *__restrict__ binOffsets,
                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
 	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
@@ -1064,6 +1154,7 @@ __global__ void tile_keys_kernel(const uint32_t *__restrict__ entryTile, const u
 __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                     const uint32_t *__restrict__ binOffsets, const uint32_t *__restrict__ sorted,
                                                     const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	const uint32_t begin = binOffsets[2 * tile], end = binOffsets[2 * tile + 2];
 	if (begin == end) return;

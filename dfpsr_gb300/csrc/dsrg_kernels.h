@@ -66,6 +66,7 @@ struct BatchParams {
 	int32_t smallWidth;               // are walked by one lane each instead of by the whole warp
 	int32_t depthOnly;                // the whole batch is model_renderDepth (1x1 walk)
 	uint32_t *tileQueue;              // work counter of the persistent tile kernel
+	const int32_t *errorFlag;         // device error bits; tile and resolve kernels return when an overflow is set
 };
 
 struct FrameBuffers {
@@ -78,6 +79,10 @@ struct FrameBuffers {
 	int32_t *errorFlag;       // device error bits
 	uint32_t *scanScratch;
 	size_t scanScratchElems;
+	// when set, the record count is read on the device (at most the host count given to the
+	// launches, which then bounds the grids), and rows hold at most rowCapacity entries
+	const uint32_t *recordCountDevice;
+	uint32_t rowCapacity;
 };
 
 // Two lists per tile: slot 2 * tile holds the records walked one lane each (small), slot
@@ -99,6 +104,10 @@ enum ErrorBits : int32_t {
 	ERROR_RECORD_OVERFLOW = 1,
 	ERROR_COORDINATE_RANGE = 2,
 	ERROR_BIN_OVERFLOW = 4,
+	ERROR_ROW_OVERFLOW = 8,
+	// a buffer sized before its count was known was too small: the frame is redone with larger
+	// buffers, and the kernels that would read past them or write the targets return at once
+	ERROR_OVERFLOW_BITS = ERROR_RECORD_OVERFLOW | ERROR_BIN_OVERFLOW | ERROR_ROW_OVERFLOW,
 };
 
 // Phase A: projection and the count of draw records per fan triangle, scanned so that the record
@@ -155,8 +164,15 @@ void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &
 void launch_wire_lines(const DrawRecord *records, uint32_t count, int4 *lines, cudaStream_t stream);
 void launch_draw_lines(uint32_t *image, int32_t stride, int32_t width, int32_t height, const int4 *lines, uint32_t count,
                        uint32_t color, cudaStream_t stream);
-// Exclusive scan of n uint32 values into out (out[n] = total).
+// out[0..3] = record count, row count, tile-list entry count, error bits of a batch.
+void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
+                          const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out, cudaStream_t stream);
+// Exclusive scan of n uint32 values into out (out[n] = total); two launches, scratch of
+// scan_scratch_elems(n) values.
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);
+// The same for a length written on the device (*nDevice, at most capacity; scratch for capacity).
+void launch_scan_device(const uint32_t *in, uint32_t *out, const uint32_t *nDevice, uint32_t capacity, uint32_t *scratch,
+                        size_t scratchElems, cudaStream_t stream);
 size_t scan_scratch_elems(uint32_t n);
 // Kernels launched by this library in this process (host-side count).
 uint64_t launch_count();

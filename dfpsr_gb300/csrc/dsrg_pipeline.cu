@@ -4,6 +4,7 @@
 // row intervals and tile-list entries) to size the next phase's buffers exactly.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -169,24 +170,37 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 			if (f.coverage) TRY(cudaMemsetAsync(f.coverage, 0, (size_t)f.width * f.height * sizeof(uint32_t), stream));
 	}
 	if (totals.triangles == 0) return DSRG_OK; // nothing reaches the tiles: the targets stay as they are
+	params.errorFlag = (const int32_t *)(ctx->control.ptr + 1);
 	RasterConfig config;
 	config.threadsPerTile = ctx->threadsPerTile;
 	config.ctasPerSm = ctx->ctasPerSm;
-	config.resolveQuads = 0; // set once the record count is known
-	PhaseKey key;
-	memset(&key, 0, sizeof(key));
-	key.resolve = job.resolve ? 1 : 0;
-	key.alpha = job.alpha ? 1 : 0;
-	key.config = config;
+	// small triangles (more than one per 8 pixels) leave most quads with several winners: resolve
+	// per pixel; otherwise a quad's pixels mostly share their winner: resolve per quad
+	config.resolveQuads = (uint64_t)totals.triangles * 8u <= (uint64_t)totals.pixels ? 1 : 0;
 
-	// phase A: projection and record counts
+	// Buffers whose sizes depend on earlier phases are sized from the context's capacities (the
+	// largest totals seen, with slack); the phases then run back to back with no host round trip.
+	// A total above its capacity sets an overflow bit, the tile and resolve kernels return at once,
+	// and batch_enqueue redoes the batch with the capacities the totals asked for.
 	const size_t np = totals.points, nt = totals.triangles;
+	const uint32_t recordCap = (uint32_t)std::max<uint64_t>(ctx->recordCapacity, nt + nt / 8 + 1024);
+	const uint32_t rowCap = (uint32_t)std::max<uint64_t>(ctx->rowCapacity, (uint64_t)recordCap * 4);
+	const uint32_t binCap = (uint32_t)std::max<uint64_t>(ctx->binCapacity, (uint64_t)recordCap * 2);
 	TRY(ctx->csx.reserve(np)); TRY(ctx->csy.reserve(np)); TRY(ctx->csz.reserve(np));
 	TRY(ctx->isx.reserve(np)); TRY(ctx->isy.reserve(np));
 	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
 	TRY(ctx->triCounts.reserve(nt + 1));
 	TRY(ctx->triOffsets.reserve(nt + 1));
-	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)(nt > 2 * (size_t)totals.tiles ? nt : 2 * (size_t)totals.tiles) + 1)));
+	TRY(ctx->records.reserve((size_t)recordCap + 1));
+	TRY(ctx->rowCounts.reserve((size_t)recordCap + 1));
+	TRY(ctx->rowOffsets.reserve((size_t)recordCap + 1));
+	TRY(ctx->rows.reserve((size_t)rowCap + 2));
+	TRY(ctx->binCounts.reserve(2 * (size_t)totals.tiles + 1));
+	TRY(ctx->binOffsets.reserve(2 * (size_t)totals.tiles + 1));
+	TRY(ctx->binCursors.reserve(2 * (size_t)totals.tiles + 1));
+	TRY(ctx->binLists.reserve((size_t)binCap + 1));
+	const uint64_t largest = std::max<uint64_t>(std::max<uint64_t>(nt, recordCap), 2 * (uint64_t)totals.tiles);
+	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)largest + 1)));
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
 	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
@@ -194,75 +208,74 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
 	fb.triCounts = ctx->triCounts.ptr;
 	fb.triOffsets = ctx->triOffsets.ptr;
+	fb.records = ctx->records.ptr;
+	fb.rowOffsets = ctx->rowOffsets.ptr;
+	fb.rows = ctx->rows.ptr;
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	fb.scanScratch = ctx->scanScratch.ptr;
 	fb.scanScratchElems = ctx->scanScratch.capacity;
-	key.phase = 0;
-	key.params = params;
-	key.fb = fb;
-	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
-		launch_project(params, fb, stream);
-		launch_setup_count(params, fb, stream);
-	}));
-	uint32_t recordCount = 0;
-	TRY(cudaMemcpyAsync(&recordCount, fb.triOffsets + nt, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	TRY(cudaStreamSynchronize(stream));
-	totals.records = recordCount;
-
-	// phase B: records, row offsets and tile counts
-	TRY(ctx->records.reserve((size_t)recordCount + 1));
-	TRY(ctx->rowCounts.reserve((size_t)recordCount + 1));
-	TRY(ctx->rowOffsets.reserve((size_t)recordCount + 1));
-	TRY(ctx->binCounts.reserve(2 * (size_t)totals.tiles + 1));
-	TRY(ctx->binOffsets.reserve(2 * (size_t)totals.tiles + 1));
-	TRY(ctx->binCursors.reserve(2 * (size_t)totals.tiles + 1));
-	const uint32_t largest = recordCount > 2 * totals.tiles ? recordCount : 2 * totals.tiles;
-	TRY(ctx->scanScratch.reserve(scan_scratch_elems(largest + 1)));
-	fb.records = ctx->records.ptr;
-	fb.rowOffsets = ctx->rowOffsets.ptr;
-	fb.scanScratch = ctx->scanScratch.ptr;
-	fb.scanScratchElems = ctx->scanScratch.capacity;
+	fb.recordCountDevice = fb.triOffsets + nt;
+	fb.rowCapacity = rowCap;
 	TileBins bins;
 	memset(&bins, 0, sizeof(bins));
 	bins.counts = ctx->binCounts.ptr;
 	bins.offsets = ctx->binOffsets.ptr;
 	bins.cursors = ctx->binCursors.ptr;
+	bins.lists = ctx->binLists.ptr;
+	bins.listCapacity = binCap;
 	uint32_t *rowCounts = ctx->rowCounts.ptr;
-	key.phase = 1;
-	key.recordCount = recordCount;
+	uint32_t *gathered = ctx->control.ptr + 4; // records, rows, bin entries, error bits
+	PhaseKey key;
+	memset(&key, 0, sizeof(key));
+	key.resolve = job.resolve ? 1 : 0;
+	key.alpha = job.alpha ? 1 : 0;
+	key.config = config;
+	key.params = params;
 	key.fb = fb;
 	key.bins = bins;
 	key.rowCounts = rowCounts;
-	TRY(run_phase(ctx, ctx->graphs[1], key, [&] {
-		launch_setup_write(params, fb, recordCount, stream);
-		launch_row_offsets(fb, recordCount, rowCounts, stream);
-		launch_bin_count(params, fb, recordCount, bins, stream);
+	key.recordCount = recordCap;
+	key.phase = 0;
+	// phases A (projection, record counts), B (records, row offsets, tile counts) and C (row
+	// intervals, tile lists) as one graph, then D (tiles and resolve) for solid batches as another
+	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
+		launch_project(params, fb, stream);
+		launch_setup_count(params, fb, stream);
+		launch_setup_write(params, fb, recordCap, stream);
+		launch_row_offsets(fb, recordCap, rowCounts, stream);
+		launch_bin_count(params, fb, recordCap, bins, stream);
+		launch_rows(fb, recordCap, stream);
+		launch_bin_fill(params, fb, recordCap, bins, stream);
+		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, 2 * totals.tiles, fb.errorFlag,
+		                     gathered, stream);
 	}));
-	uint32_t readBack[3] = {0, 0, 0};
-	TRY(cudaMemcpyAsync(&readBack[0], fb.rowOffsets + recordCount, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	TRY(cudaMemcpyAsync(&readBack[1], bins.offsets + 2 * (size_t)totals.tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-	TRY(cudaMemcpyAsync(&readBack[2], ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	if (!job.alpha) {
+		// phase D right behind, timed on the stream between the two graphs
+		TRY(cudaEventRecord(ctx->eventRasterStart, stream));
+		key.phase = 1;
+		TRY(run_phase(ctx, ctx->graphs[1], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
+		TRY(cudaEventRecord(ctx->eventRasterStop, stream));
+	}
+	TRY(cudaMemcpyAsync(ctx->pinnedReadback, gathered, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaStreamSynchronize(stream));
-	if (readBack[2] != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(readBack[2]));
-	totals.rows = readBack[0];
-	totals.binEntries = readBack[1];
-
-	// phase C: row intervals and tile lists; phase D: raster and resolve
-	TRY(ctx->rows.reserve((size_t)totals.rows + 2));
-	TRY(ctx->binLists.reserve((size_t)totals.binEntries + 1));
-	fb.rows = ctx->rows.ptr;
-	bins.lists = ctx->binLists.ptr;
-	bins.listCapacity = ctx->binLists.capacity;
-	key.phase = 2;
-	key.fb = fb;
-	key.bins = bins;
-	TRY(run_phase(ctx, ctx->graphs[2], key, [&] {
-		launch_rows(fb, recordCount, stream);
-		launch_bin_fill(params, fb, recordCount, bins, stream);
-	}));
-	TRY(cudaEventRecord(ctx->eventRasterStart, stream));
+	totals.records = ctx->pinnedReadback[0];
+	totals.rows = ctx->pinnedReadback[1];
+	totals.binEntries = ctx->pinnedReadback[2];
+	const uint32_t errorBits = ctx->pinnedReadback[3];
+	if (errorBits & ERROR_OVERFLOW_BITS) {
+		// the capacities the totals ask for; a total counted past an overflowed buffer is a lower bound
+		const bool recordsOver = totals.records > recordCap;
+		ctx->recordCapacity = std::max<uint64_t>(ctx->recordCapacity, (uint64_t)totals.records + totals.records / 4 + 1024);
+		if (!recordsOver) {
+			ctx->rowCapacity = std::max<uint64_t>(ctx->rowCapacity, (uint64_t)totals.rows + totals.rows / 4 + 1024);
+			ctx->binCapacity = std::max<uint64_t>(ctx->binCapacity, (uint64_t)totals.binEntries + totals.binEntries / 4 + 1024);
+		}
+		return DSRG_RETRY;
+	}
+	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "triangle setup reported device error bits " + std::to_string(errorBits));
 	if (job.alpha) {
-		// blending in submission order: sorted tile lists, one thread per pixel
+		// blending in submission order: sorted tile lists, one thread per pixel (needs the entry count)
+		TRY(cudaEventRecord(ctx->eventRasterStart, stream));
 		const uint64_t n = totals.binEntries;
 		const uint32_t blocks = sort_blocks(n);
 		TRY(ctx->alphaEntryTile.reserve(n + 1)); TRY(ctx->alphaTileKeys.reserve(n + 1)); TRY(ctx->alphaRecords.reserve(n + 1));
@@ -280,21 +293,10 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		key.phase = 3;
 		key.entries = totals.binEntries;
 		key.alphaBuffers = a;
-		TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_alpha(params, fb, bins, totals.binEntries, recordCount, a, stream); }));
+		key.recordCount = totals.records;
+		TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_alpha(params, fb, bins, totals.binEntries, totals.records, a, stream); }));
 		TRY(cudaEventRecord(ctx->eventRasterStop, stream));
-		if (outputs) {
-			outputs->params = params;
-			outputs->fb = fb;
-		}
-		return DSRG_OK;
 	}
-	// small triangles (more than one record per 8 pixels) leave most quads with several winners:
-	// resolve per pixel; otherwise a quad's pixels mostly share their winner: resolve per quad
-	config.resolveQuads = (uint64_t)recordCount * 8u <= (uint64_t)totals.pixels ? 1 : 0;
-	key.config = config;
-	key.phase = 3;
-	TRY(run_phase(ctx, ctx->graphs[3], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
-	TRY(cudaEventRecord(ctx->eventRasterStop, stream));
 	if (outputs) {
 		outputs->params = params;
 		outputs->fb = fb;
@@ -304,7 +306,10 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 
 int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs) {
 	if (outputs) memset(outputs, 0, sizeof(*outputs));
-	const int status = enqueue_phases(ctx, job, totals, outputs);
+	int status = DSRG_RETRY;
+	// a batch whose totals outgrow the capacities is redone once per buffer that was too small
+	for (int attempt = 0; attempt < 4 && status == DSRG_RETRY; attempt++) status = enqueue_phases(ctx, job, totals, outputs);
+	if (status == DSRG_RETRY) return fail(ctx, DSRG_ERROR_DEVICE, "batch buffers kept overflowing");
 	if (status == DSRG_OK) TRY(cudaEventRecord(ctx->eventStop, ctx->stream));
 	return status;
 }
