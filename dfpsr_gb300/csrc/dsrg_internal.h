@@ -176,6 +176,7 @@ struct dsrg_context_s {
 	// capacities of the buffers sized before their totals are known (largest totals seen, with slack)
 	uint64_t recordCapacity = 0, rowCapacity = 0, binCapacity = 0;
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
+	DeviceBuffer<uint32_t> bigList;      // records binned a warp each (their count lives in control[8])
 	DeviceBuffer<TextureData> textureTable;
 	DeviceBuffer<uint32_t> stagingColor;
 	DeviceBuffer<uint32_t> textureStaging;      // texture creation: host images and two-step resize halves

@@ -463,11 +463,104 @@ __device__ __forceinline__ void row_interval_regs(int32_t x0, int32_t y0, int32_
 	cut_row(make_edge(x2, y2, x0, y0), y, L, R, left, right);
 }
 
-// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176).  Each warp takes
-// 32 records and spreads the concatenation of their rows over its lanes, so tall and short
-// triangles keep every lane busy: a lane finds the record of its row by a binary search over the
-// warp's prefix sums of row counts and fetches that record's corners with shuffles.
-__global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
+// The row intervals of every record (rasterizeTriangle, ITriangle2D.cpp:150-176), balanced by rows:
+// each CTA takes ROWS_CHUNK consecutive rows of the concatenation of all records' rows (one warp
+// finds the records they belong to with a 32-way search over the row offsets), stages those
+// records' corners in shared memory, gives each thread ROWS_PER_THREAD consecutive rows and
+// writes the chunk back coalesced.  Every record has at least two rows (raster bounds cover row
+// pairs), so a chunk spans at most ROWS_CHUNK / 2 + 2 records.
+static const int ROWS_THREADS = 256;
+static const int ROWS_PER_THREAD = 4;
+static const uint32_t ROWS_CHUNK = ROWS_THREADS * ROWS_PER_THREAD;
+static const uint32_t ROWS_MAX_RECORDS = ROWS_CHUNK / 2 + 2;
+
+// The largest r in [0, n) with offsets[r] <= v (offsets non-decreasing, offsets[0] = 0 <= v), by one warp.
+__device__ __forceinline__ uint32_t warp_search(const uint32_t *offsets, uint32_t n, uint32_t v) {
+	const uint32_t lane = threadIdx.x & 31;
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 32) {
+		const uint32_t step = (hi - lo + 31) / 32;
+		const uint32_t probe = lo + lane * step;
+		const bool below = probe < hi && offsets[probe] <= v;
+		const uint32_t k = 31 - __clz(__ballot_sync(0xFFFFFFFFu, below));
+		lo += k * step;
+		hi = min(lo + step, hi);
+	}
+	const uint32_t probe = lo + lane;
+	const bool below = probe < hi && offsets[probe] <= v;
+	return lo + (31 - __clz(__ballot_sync(0xFFFFFFFFu, below)));
+}
+
+__global__ void __launch_bounds__(ROWS_THREADS) rows_chunk_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
+                                                            const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
+                                                            uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
+	__shared__ uint32_t first, last;
+	__shared__ uint32_t offsets[ROWS_MAX_RECORDS + 1];
+	__shared__ int4 cornersA[ROWS_MAX_RECORDS];   // flat 0..3
+	__shared__ int4 cornersB[ROWS_MAX_RECORDS];   // flat 4..5, left, top
+	__shared__ int32_t rights[ROWS_MAX_RECORDS];
+	__shared__ uint32_t out[ROWS_CHUNK + ROWS_CHUNK / 32];
+	const uint32_t n = device_count(capacity, countDevice);
+	if (n == 0) return;
+	const uint32_t total = rowOffsets[n];
+	for (uint32_t begin = blockIdx.x * ROWS_CHUNK; begin < total; begin += gridDim.x * ROWS_CHUNK) {
+		const uint32_t end = min(begin + ROWS_CHUNK, total);
+		if (threadIdx.x < 32) {
+			const uint32_t f = warp_search(rowOffsets, n, begin);
+			const uint32_t l = warp_search(rowOffsets, n, end - 1);
+			if (threadIdx.x == 0) { first = f; last = l; }
+		}
+		__syncthreads();
+		uint32_t count = last - first + 1;
+		if (count > ROWS_MAX_RECORDS) { // only records without rows could do this, and none are made
+			if (threadIdx.x == 0) atomicOr(errorFlag, ERROR_INTERNAL);
+			count = ROWS_MAX_RECORDS;
+		}
+		for (uint32_t k = threadIdx.x; k < count; k += ROWS_THREADS) {
+			const DrawRecord &r = records[first + k];
+			cornersA[k] = __ldg(reinterpret_cast<const int4 *>(&r.flat[0]));
+			cornersB[k] = __ldg(reinterpret_cast<const int4 *>(&r.flat[4]));
+			rights[k] = r.right;
+			offsets[k] = rowOffsets[first + k];
+		}
+		if (threadIdx.x == 0) offsets[count] = rowOffsets[first + count];
+		__syncthreads();
+		// this thread's rows: [j0, j0 + ROWS_PER_THREAD) within the chunk
+		const uint32_t j0 = begin + threadIdx.x * ROWS_PER_THREAD;
+		if (j0 < end) {
+			uint32_t lo = 0, hi = count; // the record holding row j0
+			while (hi - lo > 1) {
+				const uint32_t mid = (lo + hi) >> 1;
+				if (offsets[mid] <= j0) lo = mid; else hi = mid;
+			}
+			uint32_t k = lo;
+			for (int i = 0; i < ROWS_PER_THREAD; i++) {
+				const uint32_t j = j0 + i;
+				if (j >= end) break;
+				while (offsets[k + 1] <= j) k++;
+				const int4 a = cornersA[k], c = cornersB[k];
+				int32_t left, right;
+				row_interval_regs(a.x, a.y, a.z, a.w, c.x, c.y, c.w + (int32_t)(j - offsets[k]), c.z, rights[k], left, right);
+				const uint32_t at = j - begin;
+				out[at + (at >> 5)] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+			}
+		}
+		__syncthreads();
+		for (uint32_t at = threadIdx.x; at < end - begin; at += ROWS_THREADS) {
+			const uint32_t j = begin + at;
+			if (j < rowCapacity) rows[j] = out[at + (at >> 5)];
+			else atomicOr(errorFlag, ERROR_ROW_OVERFLOW);
+		}
+		__syncthreads();
+	}
+}
+
+// The row intervals of short records (a few rows each, as in dense meshes): each warp takes 32
+// records and spreads the concatenation of their rows over its lanes; a lane finds the record of
+// its row by a binary search over the warp's prefix sums of row counts and fetches that record's
+// corners with shuffles.  No search over all records is needed, but a warp's 32 records are one
+// work unit, so tall triangles are drawn by rows_chunk_kernel instead.
+__global__ void __launch_bounds__(256) rows_group_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
                                                    const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
                                                    uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
 	const uint32_t recordCount = device_count(capacity, countDevice);
@@ -517,14 +610,16 @@ __global__ void __launch_bounds__(256) rows_kernel(const DrawRecord *__restrict_
 	}
 }
 
-void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream) {
+void launch_rows(const FrameBuffers &fb, uint32_t recordCount, bool tallRecords, cudaStream_t stream) {
 	if (recordCount == 0) return;
 	COUNT_LAUNCH();
-	// one warp per 32 records
-	rows_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(fb.records, recordCount,
-	                                                                                        fb.recordCountDevice, fb.rowOffsets,
-	                                                                                        fb.rows, fb.rowCapacity ? fb.rowCapacity : 0xFFFFFFFFu,
-	                                                                                        fb.errorFlag);
+	const uint32_t rowCapacity = fb.rowCapacity ? fb.rowCapacity : 0xFFFFFFFFu;
+	if (tallRecords)
+		rows_chunk_kernel<<<sm_count() * 6, ROWS_THREADS, 0, stream>>>(fb.records, recordCount, fb.recordCountDevice, fb.rowOffsets,
+		                                                               fb.rows, rowCapacity, fb.errorFlag);
+	else
+		rows_group_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(
+			fb.records, recordCount, fb.recordCountDevice, fb.rowOffsets, fb.rows, rowCapacity, fb.errorFlag);
 }
 
 // ------------------------------------------------------------------ binning
@@ -614,6 +709,17 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 			}
 		}
 		uint32_t bigMask = __ballot_sync(0xFFFFFFFFu, big);
+		if (bins.bigList) {
+			// deferred to bin_big_kernel, which gives every big record a warp of its own
+			if (!FILL && bigMask) {
+				const uint32_t leader = __ffs(bigMask) - 1;
+				uint32_t base = 0;
+				if (lane == leader) base = atomicAdd(bins.bigCount, (uint32_t)__popc(bigMask));
+				base = __shfl_sync(0xFFFFFFFFu, base, leader);
+				if (big) bins.bigList[base + __popc(bigMask & ((1u << lane) - 1u))] = r;
+			}
+			continue;
+		}
 		while (bigMask) {
 			const uint32_t src = __ffs(bigMask) - 1;
 			bigMask &= bigMask - 1;
@@ -639,12 +745,48 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 	}
 }
 
+// The records bin_kernel deferred, one warp each over the tiles of its bound.
+template <bool FILL>
+__global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawRecord *__restrict__ records, TileBins bins,
+                                                      int32_t *errorFlag) {
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+	const uint32_t count = *bins.bigCount;
+	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += warps) {
+		const uint32_t r = bins.bigList[w];
+		const DrawRecord rec = records[r];
+		const FrameTarget &f = b.frames[rec.frame];
+		const uint32_t large = (b.depthOnly || !record_is_small(rec, b.smallRows, b.smallWidth)) ? 1u : 0u;
+		const int32_t tx0 = rec.left >> 4, ty0 = rec.top >> 4;
+		int32_t tx1 = (rec.right - 1) >> 4, ty1 = (rec.bottom - 1) >> 4;
+		if (tx1 >= f.tilesX) tx1 = f.tilesX - 1;
+		if (ty1 >= f.tilesY) ty1 = f.tilesY - 1;
+		const int32_t bw = tx1 - tx0 + 1, bt = bw * (ty1 - ty0 + 1);
+		const bool exact = tile_test_is_exact(rec);
+		for (int32_t i = (int32_t)lane; i < bt; i += 32) {
+			const int32_t tx = tx0 + i % bw, ty = ty0 + i / bw;
+			if (exact && !tile_may_overlap(rec, tx * TILE_W, ty * TILE_H)) continue;
+			const uint32_t tile = 2u * (f.tileBase + (uint32_t)(ty * f.tilesX + tx)) + large;
+			uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
+			if (FILL) {
+				slot += bins.offsets[tile];
+				if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+			}
+		}
+	}
+}
+
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
 	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+	if (bins.bigCount) cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
 		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
 		                                                                  fb.errorFlag);
+		if (bins.bigList) {
+			COUNT_LAUNCH();
+			bin_big_kernel<false><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+		}
 	}
 	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
@@ -655,6 +797,10 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 		COUNT_LAUNCH();
 		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
 		                                                                 fb.errorFlag);
+		if (bins.bigList) {
+			COUNT_LAUNCH();
+			bin_big_kernel<true><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+		}
 	}
 }
 

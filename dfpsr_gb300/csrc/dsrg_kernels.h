@@ -93,6 +93,10 @@ struct TileBins {
 	uint32_t *cursors;  // 2 * totalTiles
 	uint32_t *lists;
 	size_t listCapacity;
+	// records over more than four tiles, binned by whole warps in a second launch (room for every
+	// record; the count pass fills the list, the fill pass reads it); null: binned in the same launch
+	uint32_t *bigList;
+	uint32_t *bigCount;
 };
 
 // True when one lane walks the whole record inside a tile (small-triangle path).
@@ -105,6 +109,7 @@ enum ErrorBits : int32_t {
 	ERROR_COORDINATE_RANGE = 2,
 	ERROR_BIN_OVERFLOW = 4,
 	ERROR_ROW_OVERFLOW = 8,
+	ERROR_INTERNAL = 16,
 	// a buffer sized before its count was known was too small: the frame is redone with larger
 	// buffers, and the kernels that would read past them or write the targets return at once
 	ERROR_OVERFLOW_BITS = ERROR_RECORD_OVERFLOW | ERROR_BIN_OVERFLOW | ERROR_ROW_OVERFLOW,
@@ -126,7 +131,8 @@ void launch_occlusion_top_rows(float *grid, int32_t gridWidth, int32_t gridHeigh
 void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream);
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
 // Phase C: row intervals, tile lists, the persistent tile raster and the per-pixel resolve.
-void launch_rows(const FrameBuffers &fb, uint32_t recordCount, cudaStream_t stream);
+// tallRecords: records average many rows (large triangles); rows are then balanced by row, not by record.
+void launch_rows(const FrameBuffers &fb, uint32_t recordCount, bool tallRecords, cudaStream_t stream);
 void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream);
 // Launch shape of the persistent tile kernel.
 struct RasterConfig {

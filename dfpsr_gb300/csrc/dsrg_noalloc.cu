@@ -106,6 +106,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	fb.scanScratchElems = scan_scratch_elems(MAX_RECORDS + 2);
 	fb.scanScratch = carve.take<uint32_t>(fb.scanScratchElems);
 	TileBins bins;
+	memset(&bins, 0, sizeof(bins)); // no deferred big-record list: every record is binned in one launch
 	bins.counts = carve.take<uint32_t>(2 * MAX_TILES + 1);
 	bins.offsets = carve.take<uint32_t>(2 * MAX_TILES + 1);
 	bins.cursors = carve.take<uint32_t>(2 * MAX_TILES + 1);
@@ -172,7 +173,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles span more than DSRG_NOALLOC_MAX_ROWS (2097152) pixel rows");
 	if (totalsRead[1] > DSRG_NOALLOC_MAX_BIN_ENTRIES)
 		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_model_render_depth_noalloc: the visible triangles touch more than DSRG_NOALLOC_MAX_BIN_ENTRIES (1048576) tiles in total");
-	launch_rows(fb, recordCount, stream);
+	launch_rows(fb, recordCount, false, stream);
 	launch_bin_fill(params, fb, recordCount, bins, stream);
 
 	// depth raster (executeTriangleDrawingDepth, renderCore.cpp:343-387) and resolve

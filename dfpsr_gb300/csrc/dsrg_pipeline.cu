@@ -199,6 +199,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(ctx->binOffsets.reserve(2 * (size_t)totals.tiles + 1));
 	TRY(ctx->binCursors.reserve(2 * (size_t)totals.tiles + 1));
 	TRY(ctx->binLists.reserve((size_t)binCap + 1));
+	TRY(ctx->bigList.reserve((size_t)recordCap + 1));
 	const uint64_t largest = std::max<uint64_t>(std::max<uint64_t>(nt, recordCap), 2 * (uint64_t)totals.tiles);
 	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)largest + 1)));
 	FrameBuffers fb;
@@ -223,6 +224,8 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	bins.cursors = ctx->binCursors.ptr;
 	bins.lists = ctx->binLists.ptr;
 	bins.listCapacity = binCap;
+	bins.bigList = ctx->bigList.ptr;
+	bins.bigCount = ctx->control.ptr + 8;
 	uint32_t *rowCounts = ctx->rowCounts.ptr;
 	uint32_t *gathered = ctx->control.ptr + 4; // records, rows, bin entries, error bits
 	PhaseKey key;
@@ -244,7 +247,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_setup_write(params, fb, recordCap, stream);
 		launch_row_offsets(fb, recordCap, rowCounts, stream);
 		launch_bin_count(params, fb, recordCap, bins, stream);
-		launch_rows(fb, recordCap, stream);
+		launch_rows(fb, recordCap, config.resolveQuads != 0, stream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
 		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, 2 * totals.tiles, fb.errorFlag,
 		                     gathered, stream);
