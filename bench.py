@@ -47,6 +47,8 @@ def parse_args():
     p.add_argument("--batch-frames", type=int, default=256, help="frames of the mixed-size batch (0 skips it)")
     p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
     p.add_argument("--light-sprites", type=int, default=4096, help="sprites of the deferred-light pass (0 skips it)")
+    p.add_argument("--tuning", default="auto",
+                   help="tile kernel launch shape THREADSxCTAS_PER_SMxSMALL_ROWSxSMALL_WIDTH (e.g. 128x8x8x16), or auto")
     return p.parse_args()
 
 
@@ -468,11 +470,16 @@ def main():
 
     # the tile kernel's launch shape for this workload, chosen by the library's autotuner on a
     # one-frame batch of it (the plain path below uses the context's tuning)
-    tune_batch = ctx.batch()
-    tune_batch.add_frame(color, depth)
-    tune_batch.give_task(0, model)
-    tuning = tune_batch.autotune(rounds=3)
-    tune_batch.destroy()
+    if args.tuning == "auto":
+        tune_batch = ctx.batch()
+        tune_batch.add_frame(color, depth)
+        tune_batch.give_task(0, model)
+        tuning = tune_batch.autotune(rounds=3)
+        tune_batch.destroy()
+    else:  # a given shape (profiling runs keep the autotuner's trial launches out of the launch list)
+        threads, per_sm, rows, width = (int(v) for v in args.tuning.split("x"))
+        ctx.set_tuning(threads_per_tile=threads, ctas_per_sm=per_sm, small_rows=rows, small_width=width)
+        tuning = ctx.tuning()
 
     # fragments per frame: deterministic, counted once by the kernels themselves
     ctx.set_counting(True)

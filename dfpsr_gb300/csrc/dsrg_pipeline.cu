@@ -253,7 +253,8 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		                     gathered, stream);
 	}));
 	if (!job.alpha) {
-		// phase D right behind, timed on the stream between the two graphs
+		// phase D right behind, timed on the stream between the two graphs; after an overflow its
+		// kernels return at once and the targets stay untouched
 		TRY(cudaEventRecord(ctx->eventRasterStart, stream));
 		key.phase = 1;
 		TRY(run_phase(ctx, ctx->graphs[1], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
