@@ -951,6 +951,33 @@ __device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t 
 	return affine ? ~hi : hi;
 }
 
+// The winner of one pixel, shaded and written: the reference's running sums of its quad
+// (quad_lanes), the vertex weights, RgbaMultiply and the packed colour and depth.
+__device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameTarget &f, const DrawRecord *__restrict__ records,
+                                              const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows,
+                                              int32_t px, int32_t py, unsigned long long key) {
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
+	const uint32_t ri = key_record(key, depthTest);
+	const DrawRecord r = records[ri];
+	const int32_t y1 = py & ~1, x = px & ~1;
+	const int lane4 = ((py & 1) << 1) | (px & 1);
+	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
+	float w[3][4];
+	const int components = f.color ? 3 : 1;
+	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
+	const float depthValue = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
+	if (f.color) {
+		float wa[4], wb[4], wc[4];
+		lane_weights(w, affine, wa, wb, wc);
+		ShadeRecord shade;
+		make_shade(b.tasks[r.task], r.tri, shade);
+		float rgba[4];
+		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
+		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
+	}
+	if (depthTest) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+}
+
 // Persistent CTAs pull 16x16 tiles of the batch from a device queue.  The binning split every
 // tile's list into small and large records.  Both are dealt round-robin over the warps (warp w of
 // W takes entries w, w + W, ...): a lane walks a small record by itself (the reference's sequential
@@ -959,7 +986,7 @@ __device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t 
 // once at the tile's left edge and then walks on.
 // All fragments compete for the tile's shared keys; the winners go to the frame's key image.
 // Tiles that nothing covers write nothing: the resolve pass skips them too.
-template <bool DEPTH_ONLY_1X1, int THREADS>
+template <bool DEPTH_ONLY_1X1, int THREADS, bool RESOLVE>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                                          TileBins bins, const uint32_t *__restrict__ rowOffsets,
                                                                          const uint32_t *__restrict__ rows) {
@@ -1145,7 +1172,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 			const int me = (p >> 4) * TILE_STRIDE + (p & 15);
 			if (px < width && py < height) {
 				if (counting) coverageImage[(size_t)py * width + px] += coverage[me]; // zeroed before a frame's first run
-				keyImage[(size_t)py * width + px] = keys[me];
+				if (!RESOLVE) keyImage[(size_t)py * width + px] = keys[me];
+				// the tile's winners shaded right away (resolve_pixels_kernel fused into the tile pass)
+				else if (keys[me] != 0ull) resolve_pixel(b, f, records, rowOffsets, rows, px, py, keys[me]);
 			}
 		}
 		if (b.fragments && tid == 0) atomicAdd(b.fragments, fragmentSum);
@@ -1180,9 +1209,9 @@ __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const
 // intervals and the reference's running sums at that quad) and the pixel is shaded.  Used for
 // frames of small triangles, where the pixels of a quad mostly have different winners.  One CTA
 // of 256 threads per 16x16 tile.
-__global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, const DrawRecord *__restrict__ records,
-                                                             const uint32_t *__restrict__ binOffsets,
-                                                             const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+__global__ void __launch_bounds__(256, 4) resolve_pixels_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                                const uint32_t *__restrict__ binOffsets,
+                                                                const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
 	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
@@ -1191,27 +1220,7 @@ __global__ void __launch_bounds__(256) resolve_pixels_kernel(BatchParams b, cons
 	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
 	if (px >= f.width || py >= f.height) return;
 	const unsigned long long key = f.keys[(size_t)py * f.width + px];
-	if (key == 0ull) return;
-	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
-	const uint32_t ri = key_record(key, depthTest);
-	const DrawRecord r = records[ri];
-	const int32_t y1 = py & ~1, x = px & ~1;
-	const int lane4 = ((py & 1) << 1) | (px & 1);
-	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
-	float w[3][4];
-	const int components = f.color ? 3 : 1;
-	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
-	const float depthValue = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
-	if (f.color) {
-		float wa[4], wb[4], wc[4];
-		lane_weights(w, affine, wa, wb, wc);
-		ShadeRecord shade;
-		make_shade(b.tasks[r.task], r.tri, shade);
-		float rgba[4];
-		shade_lane(shade, b.textures, wa, wb, wc, lane4, rgba);
-		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
-	}
-	if (depthTest) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+	if (key != 0ull) resolve_pixel(b, f, records, rowOffsets, rows, px, py, key);
 }
 
 // One thread per 2x2 quad: the winners of its pixels are grouped by record, and for each record
@@ -1333,7 +1342,7 @@ __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRec
 		ShadeRecord shade;
 		make_shade(b.tasks[r.task], r.tri, shade);
 		float rgba[4];
-		shade_lane(shade, b.textures, wa, wb, wc, lane4, rgba);
+		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
 		const float opacity = fmul(rgba[3], 1.0f / 255.0f);
 		const float keep = fsub(1.0f, opacity);
 		float blended[4];
@@ -1382,17 +1391,17 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	uint32_t ctas = (uint32_t)sm_count() * (uint32_t)perSm;
 	if (ctas > b.totalTiles) ctas = b.totalTiles;
 	COUNT_LAUNCH();
-	if (threads == 64) {
-		if (b.depthOnly) raster_kernel<true, 64><<<ctas, 64, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-		else raster_kernel<false, 64><<<ctas, 64, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-	} else if (threads == 128) {
-		if (b.depthOnly) raster_kernel<true, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-		else raster_kernel<false, 128><<<ctas, 128, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-	} else {
-		if (b.depthOnly) raster_kernel<true, 256><<<ctas, 256, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-		else raster_kernel<false, 256><<<ctas, 256, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
-	}
-	if (!resolve) return;
+	// small triangles resolve per pixel inside the tile pass; the keys then never leave the chip
+	const bool fused = resolve && !b.depthOnly && !config.resolveQuads;
+#define DSRG_RASTER(T)                                                                                            \
+	if (b.depthOnly) raster_kernel<true, T, false><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	else if (fused) raster_kernel<false, T, true><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	else raster_kernel<false, T, false><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+	if (threads == 64) { DSRG_RASTER(64) }
+	else if (threads == 128) { DSRG_RASTER(128) }
+	else { DSRG_RASTER(256) }
+#undef DSRG_RASTER
+	if (!resolve || fused) return;
 	COUNT_LAUNCH();
 	if (b.depthOnly) resolve_depth_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 	else if (config.resolveQuads) resolve_quads_kernel<<<b.totalTiles, 64, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);

@@ -97,8 +97,11 @@ DSRG_HD void unpack_rgba(uint32_t c, float *out) {
 
 // getPixels_2x2 (shader/RgbaMultiply.h:74-106) for lane `lane` of a quad whose four lanes have
 // vertex weights wa/wb/wc.  The mip level of each texture comes from lanes 0..2.
-DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
-                        const float *wc, int lane, float *rgba) {
+// a[lane] by selects, so that arrays indexed by a run-time lane stay in registers
+DSRG_HD float pick4(const float *a, int lane) { return lane == 0 ? a[0] : (lane == 1 ? a[1] : (lane == 2 ? a[2] : a[3])); }
+
+DSRG_HD void shade_lane_inline(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
+                               const float *wc, int lane, float *rgba) {
 	const bool hasDiffuse = (s.flags & SHADE_DIFFUSE) != 0, hasLight = (s.flags & SHADE_LIGHT) != 0;
 	const bool colorless = (s.flags & SHADE_COLORLESS) != 0, fade = (s.flags & SHADE_VERTEX_FADE) != 0;
 	float u[4], v[4];
@@ -106,20 +109,20 @@ DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, 
 		const TextureData &t = textures[s.diffuse];
 		for (int l = 0; l < 3; l++) { u[l] = interpolate3(s.u1, wa[l], wb[l], wc[l]); v[l] = interpolate3(s.v1, wa[l], wb[l], wc[l]); }
 		u[3] = interpolate3(s.u1, wa[3], wb[3], wc[3]); v[3] = interpolate3(s.v1, wa[3], wb[3], wc[3]);
-		unpack_rgba(sample_bilinear(t, u[lane], v[lane], mip_level(t, u, v), false), rgba);
+		unpack_rgba(sample_bilinear(t, pick4(u, lane), pick4(v, lane), mip_level(t, u, v), false), rgba);
 		return;
 	}
 	if (hasLight && !hasDiffuse && colorless) {
 		const TextureData &t = textures[s.light];
-		float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
+		float uu = interpolate3(s.u2, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane)), vv = interpolate3(s.v2, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
 		unpack_rgba(sample_bilinear(t, uu, vv, 0u, true), rgba);
 		return;
 	}
 	if (fade) {
-		rgba[0] = interpolate3(s.red, wa[lane], wb[lane], wc[lane]);
-		rgba[1] = interpolate3(s.green, wa[lane], wb[lane], wc[lane]);
-		rgba[2] = interpolate3(s.blue, wa[lane], wb[lane], wc[lane]);
-		rgba[3] = interpolate3(s.alpha, wa[lane], wb[lane], wc[lane]);
+		rgba[0] = interpolate3(s.red, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
+		rgba[1] = interpolate3(s.green, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
+		rgba[2] = interpolate3(s.blue, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
+		rgba[3] = interpolate3(s.alpha, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
 	} else {
 		rgba[0] = s.red[0]; rgba[1] = s.green[0]; rgba[2] = s.blue[0]; rgba[3] = s.alpha[0];
 	}
@@ -127,16 +130,24 @@ DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, 
 	if (hasDiffuse) {
 		const TextureData &t = textures[s.diffuse];
 		for (int l = 0; l < 4; l++) { u[l] = interpolate3(s.u1, wa[l], wb[l], wc[l]); v[l] = interpolate3(s.v1, wa[l], wb[l], wc[l]); }
-		unpack_rgba(sample_bilinear(t, u[lane], v[lane], mip_level(t, u, v), false), texel);
+		unpack_rgba(sample_bilinear(t, pick4(u, lane), pick4(v, lane), mip_level(t, u, v), false), texel);
 		for (int ch = 0; ch < 4; ch++) rgba[ch] = fmul(rgba[ch], texel[ch]);
 	}
 	if (hasLight) {
 		const TextureData &t = textures[s.light];
-		float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
+		float uu = interpolate3(s.u2, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane)), vv = interpolate3(s.v2, pick4(wa, lane), pick4(wb, lane), pick4(wc, lane));
 		unpack_rgba(sample_bilinear(t, uu, vv, 0u, true), texel);
 		for (int ch = 0; ch < 4; ch++) rgba[ch] = fmul(rgba[ch], texel[ch]);
 	}
 }
+
+// shade_lane_inline kept out of line, for kernels where its code size matters more than keeping
+// its inputs in registers.
+DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
+                             const float *wc, int lane, float *rgba) {
+	shade_lane_inline(s, textures, wa, wb, wc, lane, rgba);
+}
+
 
 // shade_lane for every lane of `mask` at once: the texture coordinates of the quad's four lanes
 // and the mip levels are evaluated once and shared, each covered lane then samples on its own.
