@@ -1270,11 +1270,15 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
 			lane_weights(w, affine, wa, wb, wc);
 			ShadeRecord shade;
 			make_shade(b.tasks[r.task], r.tri, shade);
-			float rgba[4][4];
-			shade_quad(shade, b.textures, wa, wb, wc, mask, rgba);
-			for (int l = 0; l < 4; l++)
-				if (mask & (1u << l))
-					f.color[(size_t)(y1 + (l >> 1)) * f.colorStride + x + (l & 1)] = pack_saturated(rgba[l], f.packOrder);
+			float u[4], v[4];
+			const uint32_t mip = quad_diffuse_coordinates(shade, b.textures, wa, wb, wc, u, v);
+#pragma unroll
+			for (int l = 0; l < 4; l++) {
+				if (!(mask & (1u << l))) continue;
+				float rgba[4];
+				shade_quad_lane(shade, b.textures, wa, wb, wc, u, v, mip, l, rgba);
+				f.color[(size_t)(y1 + (l >> 1)) * f.colorStride + x + (l & 1)] = pack_saturated(rgba, f.packOrder);
+			}
 		}
 		if (depthTest)
 			for (int l = 0; l < 4; l++)

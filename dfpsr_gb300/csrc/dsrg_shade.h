@@ -152,47 +152,48 @@ DSRG_HD_CALL void shade_lane(const ShadeRecord &s, const TextureData *textures, 
 // shade_lane for every lane of `mask` at once: the texture coordinates of the quad's four lanes
 // and the mip levels are evaluated once and shared, each covered lane then samples on its own.
 // rgba[lane] is written for the lanes of the mask, with the same values shade_lane gives.
-DSRG_HD_CALL void shade_quad(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb, const float *wc,
-                             uint32_t mask, float (*rgba)[4]) {
+// One lane of shade_quad, given the quad's diffuse coordinates u, v and mip level (computed once
+// for the quad when the diffuse map exists); in line, so that a caller that unrolls the lanes keeps
+// every array in registers.
+DSRG_HD void shade_quad_lane(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb, const float *wc,
+                             const float *u, const float *v, uint32_t diffuseMip, int lane, float *out) {
 	const bool hasDiffuse = (s.flags & SHADE_DIFFUSE) != 0, hasLight = (s.flags & SHADE_LIGHT) != 0;
 	const bool colorless = (s.flags & SHADE_COLORLESS) != 0, fade = (s.flags & SHADE_VERTEX_FADE) != 0;
-	float u[4], v[4];
-	uint32_t diffuseMip = 0;
+	if (hasDiffuse && !hasLight && colorless) {
+		unpack_rgba(sample_bilinear(textures[s.diffuse], u[lane], v[lane], diffuseMip, false), out);
+		return;
+	}
+	if (hasLight && !hasDiffuse && colorless) {
+		const float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
+		unpack_rgba(sample_bilinear(textures[s.light], uu, vv, 0u, true), out);
+		return;
+	}
+	if (fade) {
+		out[0] = interpolate3(s.red, wa[lane], wb[lane], wc[lane]);
+		out[1] = interpolate3(s.green, wa[lane], wb[lane], wc[lane]);
+		out[2] = interpolate3(s.blue, wa[lane], wb[lane], wc[lane]);
+		out[3] = interpolate3(s.alpha, wa[lane], wb[lane], wc[lane]);
+	} else {
+		out[0] = s.red[0]; out[1] = s.green[0]; out[2] = s.blue[0]; out[3] = s.alpha[0];
+	}
+	float texel[4];
 	if (hasDiffuse) {
-		for (int l = 0; l < 4; l++) { u[l] = interpolate3(s.u1, wa[l], wb[l], wc[l]); v[l] = interpolate3(s.v1, wa[l], wb[l], wc[l]); }
-		diffuseMip = mip_level(textures[s.diffuse], u, v);
+		unpack_rgba(sample_bilinear(textures[s.diffuse], u[lane], v[lane], diffuseMip, false), texel);
+		for (int ch = 0; ch < 4; ch++) out[ch] = fmul(out[ch], texel[ch]);
 	}
-	for (int lane = 0; lane < 4; lane++) {
-		if (!(mask & (1u << lane))) continue;
-		float *out = rgba[lane];
-		if (hasDiffuse && !hasLight && colorless) {
-			unpack_rgba(sample_bilinear(textures[s.diffuse], u[lane], v[lane], diffuseMip, false), out);
-			continue;
-		}
-		if (hasLight && !hasDiffuse && colorless) {
-			const float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
-			unpack_rgba(sample_bilinear(textures[s.light], uu, vv, 0u, true), out);
-			continue;
-		}
-		if (fade) {
-			out[0] = interpolate3(s.red, wa[lane], wb[lane], wc[lane]);
-			out[1] = interpolate3(s.green, wa[lane], wb[lane], wc[lane]);
-			out[2] = interpolate3(s.blue, wa[lane], wb[lane], wc[lane]);
-			out[3] = interpolate3(s.alpha, wa[lane], wb[lane], wc[lane]);
-		} else {
-			out[0] = s.red[0]; out[1] = s.green[0]; out[2] = s.blue[0]; out[3] = s.alpha[0];
-		}
-		float texel[4];
-		if (hasDiffuse) {
-			unpack_rgba(sample_bilinear(textures[s.diffuse], u[lane], v[lane], diffuseMip, false), texel);
-			for (int ch = 0; ch < 4; ch++) out[ch] = fmul(out[ch], texel[ch]);
-		}
-		if (hasLight) {
-			const float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
-			unpack_rgba(sample_bilinear(textures[s.light], uu, vv, 0u, true), texel);
-			for (int ch = 0; ch < 4; ch++) out[ch] = fmul(out[ch], texel[ch]);
-		}
+	if (hasLight) {
+		const float uu = interpolate3(s.u2, wa[lane], wb[lane], wc[lane]), vv = interpolate3(s.v2, wa[lane], wb[lane], wc[lane]);
+		unpack_rgba(sample_bilinear(textures[s.light], uu, vv, 0u, true), texel);
+		for (int ch = 0; ch < 4; ch++) out[ch] = fmul(out[ch], texel[ch]);
 	}
+}
+
+// The diffuse coordinates and mip level of a quad (lanes 0..2 choose the level).
+DSRG_HD uint32_t quad_diffuse_coordinates(const ShadeRecord &s, const TextureData *textures, const float *wa, const float *wb,
+                                          const float *wc, float *u, float *v) {
+	if ((s.flags & SHADE_DIFFUSE) == 0) return 0;
+	for (int l = 0; l < 4; l++) { u[l] = interpolate3(s.u1, wa[l], wb[l], wc[l]); v[l] = interpolate3(s.v1, wa[l], wb[l], wc[l]); }
+	return mip_level(textures[s.diffuse], u, v);
 }
 
 // Byte index of red, green, blue, alpha for PackOrderIndex RGBA, BGRA, ARGB, ABGR (image/PackOrder.h:80-92).
