@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
     p.add_argument("--light-sprites", type=int, default=4096, help="sprites of the deferred-light pass (0 skips it)")
     p.add_argument("--tuning", default="auto",
-                   help="tile kernel launch shape THREADSxCTAS_PER_SMxSMALL_ROWSxSMALL_WIDTH (e.g. 128x8x8x16), or auto")
+                   help="tile kernel launch shape THREADSxCTAS_PER_SMxSMALL_ROWSxSMALL_WIDTH[xRESOLVE] (e.g. 128x8x8x16x1), or auto")
     return p.parse_args()
 
 
@@ -477,8 +477,9 @@ def main():
         tuning = tune_batch.autotune(rounds=3)
         tune_batch.destroy()
     else:  # a given shape (profiling runs keep the autotuner's trial launches out of the launch list)
-        threads, per_sm, rows, width = (int(v) for v in args.tuning.split("x"))
-        ctx.set_tuning(threads_per_tile=threads, ctas_per_sm=per_sm, small_rows=rows, small_width=width)
+        fields = [int(v) for v in args.tuning.split("x")]
+        ctx.set_tuning(threads_per_tile=fields[0], ctas_per_sm=fields[1], small_rows=fields[2], small_width=fields[3],
+                       resolve=fields[4] if len(fields) > 4 else 0)
         tuning = ctx.tuning()
 
     # fragments per frame: deterministic, counted once by the kernels themselves

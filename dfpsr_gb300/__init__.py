@@ -63,11 +63,11 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("threadsPerTile", C.c_int32), ("ctasPerSm", C.c_int32), ("smallRows", C.c_int32),
-                ("smallWidth", C.c_int32), ("graphs", C.c_int32)]
+                ("smallWidth", C.c_int32), ("graphs", C.c_int32), ("resolve", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {"threads_per_tile": self.threadsPerTile, "ctas_per_sm": self.ctasPerSm, "small_rows": self.smallRows,
-                "small_width": self.smallWidth, "graphs": self.graphs}
+                "small_width": self.smallWidth, "graphs": self.graphs, "resolve": self.resolve}
 
 
 class OrthoView(C.Structure):
@@ -355,7 +355,8 @@ class Context:
         return t.as_dict()
 
     def set_tuning(self, threads_per_tile: Optional[int] = None, ctas_per_sm: Optional[int] = None,
-                   small_rows: Optional[int] = None, small_width: Optional[int] = None, graphs: Optional[bool] = None):
+                   small_rows: Optional[int] = None, small_width: Optional[int] = None, graphs: Optional[bool] = None,
+                   resolve: Optional[int] = None):
         t = Tuning()
         self._check(self._l.dsrg_context_get_tuning(self.handle, C.byref(t)))
         if threads_per_tile is not None:
@@ -368,6 +369,8 @@ class Context:
             t.smallWidth = small_width
         if graphs is not None:
             t.graphs = 1 if graphs else 0
+        if resolve is not None:
+            t.resolve = resolve
         self._check(self._l.dsrg_context_set_tuning(self.handle, C.byref(t)))
 
 

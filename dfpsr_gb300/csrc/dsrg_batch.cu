@@ -235,6 +235,7 @@ int dsrg_context_get_tuning(dsrg_context ctx, dsrg_tuning *out) {
 	out->smallRows = ctx->smallRows;
 	out->smallWidth = ctx->smallWidth;
 	out->graphs = ctx->useGraphs;
+	out->resolve = ctx->resolveMode;
 	return DSRG_OK;
 }
 
@@ -250,7 +251,10 @@ int dsrg_context_set_tuning(dsrg_context ctx, const dsrg_tuning *t) {
 	ctx->ctasPerSm = t->ctasPerSm;
 	ctx->smallRows = t->smallRows;
 	ctx->smallWidth = t->smallWidth;
+	if (t->resolve < 0 || t->resolve > 2)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: resolve must be 0 or 1 (per pixel) or 2 (per quad)");
 	ctx->useGraphs = t->graphs ? 1 : 0;
+	ctx->resolveMode = t->resolve;
 	return DSRG_OK;
 }
 
@@ -263,15 +267,17 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	struct Shape { int32_t threads, perSm; };
 	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}, {64, 16}};
 	const int32_t smalls[][2] = {{8, 16}, {0, 0}, {4, 8}};
+	const int32_t resolves[] = {1, 2};
 	dsrg_tuning chosen = start;
 	double bestSeconds = -1.0;
 	for (const Shape &s : shapes) {
-		for (const auto &sm : smalls) {
+		for (const auto &sm : smalls) for (const int32_t resolve : resolves) {
 			dsrg_tuning t = start;
 			t.threadsPerTile = s.threads;
 			t.ctasPerSm = s.perSm;
 			t.smallRows = sm[0];
 			t.smallWidth = sm[1];
+			t.resolve = resolve;
 			int status = dsrg_context_set_tuning(ctx, &t);
 			if (status != DSRG_OK) return status;
 			status = dsrg_batch_render(b); // warm-up: scratch sizes and graphs for this shape

@@ -191,6 +191,7 @@ struct dsrg_context_s {
 	int32_t ctasPerSm = 4;                  // resident CTAs per SM of the persistent tile kernel
 	int32_t threadsPerTile = 256;           // threads of one tile's CTA
 	int32_t useGraphs = 1;                  // replay unchanged phases as CUDA graphs
+	int32_t resolveMode = 0;                // 0 or 1 per pixel (in the tile kernel), 2 per quad
 	dsrg::PhaseGraph graphs[4];             // phases A, B, C (lists) and D (raster)
 	int32_t counting = 0;
 	uint32_t *coverage = nullptr;

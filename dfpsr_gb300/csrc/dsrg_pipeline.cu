@@ -174,9 +174,11 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	RasterConfig config;
 	config.threadsPerTile = ctx->threadsPerTile;
 	config.ctasPerSm = ctx->ctasPerSm;
-	// small triangles (more than one per 8 pixels) leave most quads with several winners: resolve
-	// per pixel; otherwise a quad's pixels mostly share their winner: resolve per quad
-	config.resolveQuads = (uint64_t)totals.triangles * 8u <= (uint64_t)totals.pixels ? 1 : 0;
+	// fewer triangles than one per 8 pixels: tall triangles, whose rows are balanced by row
+	const bool tallTriangles = (uint64_t)totals.triangles * 8u <= (uint64_t)totals.pixels;
+	// winners are shaded per pixel inside the tile kernel unless the per-quad resolve is asked for
+	// (measured faster on both the dense terrain and the large random triangles)
+	config.resolveQuads = ctx->resolveMode == 2 ? 1 : 0;
 
 	// Buffers whose sizes depend on earlier phases are sized from the context's capacities (the
 	// largest totals seen, with slack); the phases then run back to back with no host round trip.
@@ -247,7 +249,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_setup_write(params, fb, recordCap, stream);
 		launch_row_offsets(fb, recordCap, rowCounts, stream);
 		launch_bin_count(params, fb, recordCap, bins, stream);
-		launch_rows(fb, recordCap, config.resolveQuads != 0, stream);
+		launch_rows(fb, recordCap, tallTriangles, stream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
 		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, 2 * totals.tiles, fb.errorFlag,
 		                     gathered, stream);

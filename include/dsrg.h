@@ -255,13 +255,16 @@ int dsrg_batch_render(dsrg_batch batch);
  *   ctasPerSm        persistent CTAs per SM pulling tiles from the queue (1 to 1024 / threadsPerTile)
  *   smallRows/Width  triangles whose raster bound is at most smallRows x smallWidth pixels are
  *                    walked by one lane each; larger ones by a whole warp per tile
- *   graphs           1 to replay each phase's launches as a CUDA graph, 0 to launch directly */
+ *   graphs           1 to replay each phase's launches as a CUDA graph, 0 to launch directly
+ *   resolve          how winners are shaded: 0 or 1 per pixel inside the tile kernel, 2 per 2x2
+ *                    quad in a launch of its own (same results) */
 typedef struct {
 	int32_t threadsPerTile;
 	int32_t ctasPerSm;
 	int32_t smallRows;
 	int32_t smallWidth;
 	int32_t graphs;
+	int32_t resolve;
 } dsrg_tuning;
 int dsrg_context_get_tuning(dsrg_context context, dsrg_tuning *out);
 int dsrg_context_set_tuning(dsrg_context context, const dsrg_tuning *tuning);

@@ -116,16 +116,17 @@ def test_batch_interleaved_tasks_keep_each_frames_submission_order(ctx):
         assert _same(c, ec) and _same(z, ez)
 
 
-@pytest.mark.parametrize("threads,per_sm,small", [(256, 4, (8, 16)), (256, 1, (0, 0)), (128, 8, (16, 32)), (128, 2, (4, 8)),
-                                                   (64, 16, (8, 16)), (64, 3, (0, 0))])
-def test_every_launch_shape_gives_the_same_frames(ctx, threads, per_sm, small):
+@pytest.mark.parametrize("threads,per_sm,small,resolve", [(256, 4, (8, 16), 1), (256, 1, (0, 0), 2), (128, 8, (16, 32), 2),
+                                                           (128, 2, (4, 8), 1), (64, 16, (8, 16), 2), (64, 3, (0, 0), 1),
+                                                           (128, 8, (8, 16), 0)])
+def test_every_launch_shape_gives_the_same_frames(ctx, threads, per_sm, small, resolve):
     import dfpsr_gb300 as d
     frame_scenes = _frames(seed=13, frames=4, max_triangles=2500)
     models = [d.Model(ctx, s) for s in frame_scenes]
     expected = [_alone(ctx, m, s) for m, s in zip(models, frame_scenes)]
     before = ctx.tuning()
     try:
-        ctx.set_tuning(threads_per_tile=threads, ctas_per_sm=per_sm, small_rows=small[0], small_width=small[1])
+        ctx.set_tuning(threads_per_tile=threads, ctas_per_sm=per_sm, small_rows=small[0], small_width=small[1], resolve=resolve)
         batch = d.Batch(ctx)
         imgs = []
         for i, (m, s) in enumerate(zip(models, frame_scenes)):
@@ -158,6 +159,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(ctx):
             batch.give_task(i, m)
         best = batch.autotune(rounds=1)
         assert best["threads_per_tile"] in (64, 128, 256)
+        assert best["resolve"] in (1, 2)
         assert 1 <= best["ctas_per_sm"] <= 1024 // best["threads_per_tile"]
         assert ctx.tuning() == best
         for c, z in imgs:
@@ -190,3 +192,5 @@ def test_depth_only_frame_and_errors(ctx):
         ctx.set_tuning(threads_per_tile=96)
     with pytest.raises(d.DsrgError):
         ctx.set_tuning(threads_per_tile=256, ctas_per_sm=5)
+    with pytest.raises(d.DsrgError):
+        ctx.set_tuning(resolve=3)
