@@ -234,6 +234,84 @@ DSRG_HD void cut_row(const Edge &e, int32_t y, int32_t L, int32_t R, int32_t &le
 	}
 }
 
+// cut_row for consecutive rows by exact integer stepping.  For a cutting edge the numerator of
+// the quotient changes by the same amount every row, so the floor quotient and its remainder
+// advance by a fixed quotient and remainder with at most one carry; truncation toward zero and
+// the int32 wrap of (a / b + 1) then give exactly clamp_quotient_plus_one's value.  Two int64
+// divisions per edge replace one division per edge and row.
+struct EdgeStepper {
+	int32_t kind;        // 0: cuts the left end, 1: cuts the right end, 2: empties rows (horizontal), 3: none
+	int64_t q, r, B;     // floor(A / B) and A - q * B, B > 0 (A: the numerator with the divisor's sign folded in)
+	int64_t qd, rd;      // the same for the change of A per row
+	// horizontal edges reuse q as (128 + 256 y - sy) * ny, qd as its change per row and B as the threshold
+};
+
+DSRG_HD void floor_divide(int64_t a, int64_t b, int64_t &q, int64_t &r) { // b > 0
+	q = a / b;
+	if (a % b != 0 && a < 0) q -= 1;
+	r = a - q * b;
+}
+
+DSRG_HD EdgeStepper edge_stepper(const Edge &e, int32_t y0) {
+	EdgeStepper s;
+	s.q = s.r = s.B = s.qd = s.rd = 0;
+	if (e.nx != 0) {
+		int64_t a = e.threshold - (128 - e.sx) * e.nx - (128 + 256 * (int64_t)y0 - e.sy) * e.ny;
+		if (e.nx < 0) a += 1;
+		const int64_t b = e.nx * 256, delta = -256 * e.ny;
+		const int64_t sign = b > 0 ? 1 : -1;
+		s.kind = e.nx < 0 ? 0 : 1;
+		s.B = b * sign;
+		floor_divide(a * sign, s.B, s.q, s.r);
+		floor_divide(delta * sign, s.B, s.qd, s.rd);
+	} else if (e.ny != 0) {
+		s.kind = 2;
+		s.q = (128 + 256 * (int64_t)y0 - e.sy) * e.ny;
+		s.qd = 256 * e.ny;
+		s.B = e.threshold;
+	} else {
+		s.kind = 3;
+	}
+	return s;
+}
+
+// Applies the edge to the current row's interval, then moves it to the next row.
+DSRG_HD void edge_step(EdgeStepper &s, int32_t L, int32_t R, int32_t &left, int32_t &right) {
+	if (s.kind <= 1) {
+		const int64_t t = s.q + ((s.q < 0 && s.r != 0) ? 1 : 0); // the quotient truncated toward zero
+		int32_t v = (int32_t)(uint32_t)(uint64_t)(t + 1);
+		v = v < L ? L : (v > R ? R : v);
+		if (s.kind == 0) { if (v > left) left = v; } else { if (v < right) right = v; }
+		s.q += s.qd;
+		s.r += s.rd;
+		if (s.r >= s.B) { s.r -= s.B; s.q += 1; }
+	} else if (s.kind == 2) {
+		if (s.q > s.B) { left = R; right = L; }
+		s.q += s.qd;
+	}
+}
+
+// Row intervals of rows [y0, y0 + rows) of a triangle, stepped (equal to row_interval of each row).
+DSRG_HD void row_intervals_stepped(const int32_t *flat, int32_t y0, int32_t rows, int32_t L, int32_t R, int32_t *lefts, int32_t *rights) {
+	const bool degenerate = (flat[0] == flat[2] && flat[1] == flat[3]) || (flat[2] == flat[4] && flat[3] == flat[5]) ||
+	                        (flat[4] == flat[0] && flat[5] == flat[1]);
+	if (degenerate) {
+		for (int32_t k = 0; k < rows; k++) { lefts[k] = R; rights[k] = L; }
+		return;
+	}
+	EdgeStepper s0 = edge_stepper(make_edge(flat[0], flat[1], flat[2], flat[3]), y0);
+	EdgeStepper s1 = edge_stepper(make_edge(flat[2], flat[3], flat[4], flat[5]), y0);
+	EdgeStepper s2 = edge_stepper(make_edge(flat[4], flat[5], flat[0], flat[1]), y0);
+	for (int32_t k = 0; k < rows; k++) {
+		int32_t left = L, right = R;
+		edge_step(s0, L, R, left, right);
+		edge_step(s1, L, R, left, right);
+		edge_step(s2, L, R, left, right);
+		lefts[k] = left;
+		rights[k] = right;
+	}
+}
+
 // Row interval [left, right) of pixel row y for a triangle with sub-pixel corners,
 // clamped to [L, R): rasterizeTriangle (implementation/render/ITriangle2D.cpp:150-169).
 DSRG_HD_CALL void row_interval(const int32_t *flat, int32_t y, int32_t L, int32_t R, int32_t &left, int32_t &right) {

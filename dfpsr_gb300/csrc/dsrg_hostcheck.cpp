@@ -23,4 +23,10 @@ void dsrg_host_row_intervals(const int32_t *flat, int32_t y0, int32_t rows, int3
 	for (int32_t r = 0; r < rows; r++) dsrg::row_interval(flat, y0 + r, L, R, lefts[r], rights[r]);
 }
 
+// The same rows by exact stepping (dsrg::row_intervals_stepped).
+void dsrg_host_row_intervals_stepped(const int32_t *flat, int32_t y0, int32_t rows, int32_t L, int32_t R, int32_t *lefts,
+                                     int32_t *rights) {
+	dsrg::row_intervals_stepped(flat, y0, rows, L, R, lefts, rights);
+}
+
 } // extern "C"

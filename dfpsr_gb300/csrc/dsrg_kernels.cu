@@ -555,12 +555,14 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_chunk_kernel(const DrawReco
 	}
 }
 
+static const int32_t ROWS_STEPPED_MAX = 16; // records of at most this many rows are stepped by one lane each
+
 // The row intervals of short records (a few rows each, as in dense meshes): each warp takes 32
 // records and spreads the concatenation of their rows over its lanes; a lane finds the record of
 // its row by a binary search over the warp's prefix sums of row counts and fetches that record's
 // corners with shuffles.  No search over all records is needed, but a warp's 32 records are one
 // work unit, so tall triangles are drawn by rows_chunk_kernel instead.
-__global__ void __launch_bounds__(256) rows_group_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
+__global__ void __launch_bounds__(256, 3) rows_group_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
                                                    const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
                                                    uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
 	const uint32_t recordCount = device_count(capacity, countDevice);
@@ -579,6 +581,32 @@ __global__ void __launch_bounds__(256) rows_group_kernel(const DrawRecord *__res
 			L = b.z; top = b.w; R = c.x;
 			count = c.y - top;
 			out = rowOffsets[i];
+		}
+		if (__all_sync(0xFFFFFFFFu, count <= ROWS_STEPPED_MAX)) {
+			// short records: each lane steps through its own record's rows (two divisions per edge
+			// instead of one per edge and row)
+			if (count > 0) {
+				EdgeStepper s[3];
+				const bool degenerate = (f0 == f2 && f1 == f3) || (f2 == f4 && f3 == f5) || (f4 == f0 && f5 == f1);
+				if (!degenerate) {
+					s[0] = edge_stepper(make_edge(f0, f1, f2, f3), top);
+					s[1] = edge_stepper(make_edge(f2, f3, f4, f5), top);
+					s[2] = edge_stepper(make_edge(f4, f5, f0, f1), top);
+				}
+				for (int32_t k = 0; k < count; k++) {
+					int32_t left = R, right = L;
+					if (!degenerate) {
+						left = L; right = R;
+						edge_step(s[0], L, R, left, right);
+						edge_step(s[1], L, R, left, right);
+						edge_step(s[2], L, R, left, right);
+					}
+					const uint32_t at = out + (uint32_t)k;
+					if (at < rowCapacity) rows[at] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+					else atomicOr(errorFlag, ERROR_ROW_OVERFLOW);
+				}
+			}
+			continue;
 		}
 		int32_t inclusive = count;
 		for (int o = 1; o < 32; o <<= 1) {

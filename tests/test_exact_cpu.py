@@ -102,3 +102,38 @@ def test_row_intervals_match_oracle(host, kind):
         assert np.array_equal(lefts, L) and np.array_equal(rights, R), f
         checked += 1
     assert checked > 50
+
+
+@pytest.mark.parametrize("kind", ["random", "near_horizontal", "small", "vertical", "offscreen", "far", "degenerate"])
+def test_stepped_row_intervals_equal_per_row_intervals(host, kind):
+    """row_intervals_stepped (two int64 divisions per edge, then integer steps) equals row_interval
+    of every row, including the empty rows' exact left/right values that row pairs read."""
+    r = np.random.default_rng(100 + sum(map(ord, kind)))
+    for _ in range(3000):
+        if kind == "random":
+            f = r.integers(-800 * 128, 800 * 384, 6)
+        elif kind == "near_horizontal":
+            f = r.integers(-300 * 256, 1100 * 256, 6)
+            f[1] = f[3] + r.integers(-3, 3)
+        elif kind == "small":
+            f = r.integers(0, 6 * 256, 6) + r.integers(0, 800 * 256)
+        elif kind == "vertical":
+            f = r.integers(-800 * 128, 800 * 384, 6)
+            f[0] = f[2]
+        elif kind == "offscreen":
+            f = np.array([r.integers(-800 * 256, -10), r.integers(0, 600 * 256), r.integers(-800 * 256, -10),
+                          r.integers(0, 600 * 256), r.integers(0, 800 * 256), r.integers(0, 600 * 256)])
+        elif kind == "far":  # corners up to the records' coordinate limit of 2^30
+            f = r.integers(-(1 << 30), 1 << 30, 6)
+        else:
+            f = r.integers(0, 4 * 256, 6)
+            f[2:4] = f[0:2]
+        f = np.ascontiguousarray(f.astype(np.int32))
+        y0 = int(r.integers(-40, 640))
+        rows = int(r.integers(1, 40))
+        L, R = int(r.integers(0, 400)), int(r.integers(400, 801))
+        a = _rows(host, f, y0, rows, L, R)
+        lefts, rights = np.zeros(rows, np.int32), np.zeros(rows, np.int32)
+        host.dsrg_host_row_intervals_stepped(C.c_void_p(f.ctypes.data), C.c_int32(y0), C.c_int32(rows), C.c_int32(L), C.c_int32(R),
+                                             C.c_void_p(lefts.ctypes.data), C.c_void_p(rights.ctypes.data))
+        assert np.array_equal(lefts, a[0]) and np.array_equal(rights, a[1]), (f.tolist(), y0, rows, L, R)
