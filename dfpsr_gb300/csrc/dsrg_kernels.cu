@@ -172,6 +172,21 @@ __device__ void emit_record(const TaskParams &task, uint32_t taskIndex, const Fr
 			r.task = taskIndex;
 			r.frame = (uint32_t)task.frame;
 			fb.records[index] = r;
+			if (fb.counts.rowCounts) {
+				// the record's rows, and its tiles as bin_kernel<false> counts them
+				fb.counts.rowCounts[index] = (uint32_t)(r.bottom - r.top);
+				const uint32_t large = (fb.counts.depthOnly || !record_is_small(r, fb.counts.smallRows, fb.counts.smallWidth)) ? 1u : 0u;
+				const int32_t tx0 = r.left >> 4, ty0 = r.top >> 4;
+				const int32_t tx1 = min((r.right - 1) >> 4, frame.tilesX - 1), ty1 = min((r.bottom - 1) >> 4, frame.tilesY - 1);
+				const int32_t w = tx1 - tx0 + 1, h = ty1 - ty0 + 1;
+				const int32_t tiles = (w > 0 && h > 0) ? w * h : 0;
+				if (tiles > 4) {
+					fb.counts.bigList[atomicAdd(fb.counts.bigCount, 1u)] = index;
+				} else {
+					for (int32_t i = 0; i < tiles; i++)
+						atomicAdd(&fb.counts.binCounts[2u * (frame.tileBase + (uint32_t)((ty0 + i / w) * frame.tilesX + tx0 + i % w)) + large], 1u);
+				}
+			}
 		}
 	}
 	emitted++;
@@ -802,6 +817,26 @@ __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawR
 			}
 		}
 	}
+}
+
+void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
+                                 cudaStream_t stream) {
+	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+	cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+	fb.counts.rowCounts = rowCounts;
+	fb.counts.binCounts = bins.counts;
+	fb.counts.bigList = bins.bigList;
+	fb.counts.bigCount = bins.bigCount;
+	fb.counts.smallRows = b.smallRows;
+	fb.counts.smallWidth = b.smallWidth;
+	fb.counts.depthOnly = b.depthOnly;
+	launch_setup_write(b, fb, recordCapacity, stream);
+	if (recordCapacity > 0) {
+		COUNT_LAUNCH();
+		bin_big_kernel<false><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+	}
+	launch_scan_device(rowCounts, fb.rowOffsets, fb.recordCountDevice, recordCapacity, fb.scanScratch, fb.scanScratchElems, stream);
+	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {

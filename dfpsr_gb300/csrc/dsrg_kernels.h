@@ -83,6 +83,15 @@ struct FrameBuffers {
 	// launches, which then bounds the grids), and rows hold at most rowCapacity entries
 	const uint32_t *recordCountDevice;
 	uint32_t rowCapacity;
+	// when rowCounts is set, the record-writing setup pass also writes every record's row count and
+	// counts its tiles (bins of up to four tiles; larger records go to bigList for bin_big_kernel)
+	struct {
+		uint32_t *rowCounts;
+		uint32_t *binCounts;
+		uint32_t *bigList;
+		uint32_t *bigCount;
+		int32_t smallRows, smallWidth, depthOnly;
+	} counts;
 };
 
 // Two lists per tile: slot 2 * tile holds the records walked one lane each (small), slot
@@ -122,6 +131,11 @@ void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream
 // Phase B: the records, in submission order (per frame: the order of its tasks, then of their
 // triangles), row offsets (total at rowOffsets[recordCount]) and tile counts (total at offsets[2 * totalTiles]).
 void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream);
+// launch_setup_write with the row and tile counting folded in (fb.counts is filled from rowCounts and
+// bins here), then the big records' tile counts and the scans of row counts and tile counts: the
+// work of launch_setup_write + launch_row_offsets + launch_bin_count in one pass over the records.
+void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
+                                 cudaStream_t stream);
 // occludeFromExistingTriangles (api/rendererAPI.cpp:240-255): every solid draw command of the batch
 // whose bound exceeds one cell lowers the occlusion grid of its frame over the cells it covers.
 void launch_setup_occlude(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream);

@@ -246,9 +246,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
 		launch_project(params, fb, stream);
 		launch_setup_count(params, fb, stream);
-		launch_setup_write(params, fb, recordCap, stream);
-		launch_row_offsets(fb, recordCap, rowCounts, stream);
-		launch_bin_count(params, fb, recordCap, bins, stream);
+		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
 		launch_rows(fb, recordCap, tallTriangles, stream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
 		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, 2 * totals.tiles, fb.errorFlag,
