@@ -87,22 +87,28 @@ class ClockSampler:
 
     def __enter__(self):
         try:
-            self.file = tempfile.TemporaryFile(mode="w+")
+            fd, self.file = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            # nvidia-smi appends to its own descriptor; the readers below open the file separately, so
+            # reading never moves the writer's offset
+            self.sink = open(self.file, "a")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+                                          "-lms", "200"], stdout=self.sink, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
 
+    def _lines(self):
+        try:
+            with open(self.file) as f:
+                return f.read().splitlines()
+        except Exception:
+            return []
+
     def count(self) -> int:
         if not self.file:
             return 0
-        self.file.flush()
-        pos = self.file.tell()
-        self.file.seek(0)
-        n = sum(1 for line in self.file.read().splitlines() if line.count(",") >= 8)
-        self.file.seek(pos)
-        return n
+        return sum(1 for line in self._lines() if line.count(",") >= 8)
 
     def wait_first(self, timeout: float = 5.0):
         """Waits until nvidia-smi has written its first sample (it takes a moment to start)."""
@@ -117,14 +123,19 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.sink.close()
 
     def summary(self):
         if not self.proc or not self.file:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.file.seek(0)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.file.read().splitlines():
+        lines = self._lines()
+        try:
+            os.unlink(self.file)
+        except Exception:
+            pass
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue

@@ -171,6 +171,7 @@ __device__ void emit_record(const TaskParams &task, uint32_t taskIndex, const Fr
 			r.tri = tri;
 			r.task = taskIndex;
 			r.frame = (uint32_t)task.frame;
+			r.source = task.triSource[tri];
 			fb.records[index] = r;
 			if (fb.counts.rowCounts) {
 				// the record's rows, and its tiles as bin_kernel<false> counts them
@@ -867,9 +868,9 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 	}
 }
 
-// RgbaMultiply_data and its variant (shader/RgbaMultiply.h:37-58, 110-173) for fan triangle `tri`.
-__device__ __forceinline__ void make_shade(const TaskParams &task, uint32_t tri, ShadeRecord &s) {
-	const int32_t src = task.triSource[tri];
+// RgbaMultiply_data and its variant (shader/RgbaMultiply.h:37-58, 110-173) for the fan triangle whose
+// triSource entry is `src` (polygon * 2 + fan).
+__device__ __forceinline__ void make_shade(const TaskParams &task, int32_t src, ShadeRecord &s) {
 	const int32_t p = src >> 1, k = src & 1;
 	const int corner[3] = {0, 1 + k, 2 + k};
 	float scale = 255.0f;
@@ -1033,7 +1034,7 @@ __device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameT
 		float wa[4], wb[4], wc[4];
 		lane_weights(w, affine, wa, wb, wc);
 		ShadeRecord shade;
-		make_shade(b.tasks[r.task], r.tri, shade);
+		make_shade(b.tasks[r.task], r.source, shade);
 		float rgba[4];
 		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
 		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
@@ -1229,7 +1230,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 			if (lane == 0) atomicAdd(&fragmentSum, (unsigned long long)fragments);
 		}
 		__syncthreads();
-		for (int k = 0; k < PIXELS; k++) {
+#pragma unroll 1
+		for (int k = 0; k < PIXELS; k++) { // one copy of the (inlined) resolve code, not PIXELS
 			const int p = tid + k * THREADS;
 			const int32_t px = tx0 + (p & 15), py = ty0 + (p >> 4);
 			const int me = (p >> 4) * TILE_STRIDE + (p & 15);
@@ -1332,7 +1334,7 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
 			float wa[4], wb[4], wc[4];
 			lane_weights(w, affine, wa, wb, wc);
 			ShadeRecord shade;
-			make_shade(b.tasks[r.task], r.tri, shade);
+			make_shade(b.tasks[r.task], r.source, shade);
 			float u[4], v[4];
 			const uint32_t mip = quad_diffuse_coordinates(shade, b.textures, wa, wb, wc, u, v);
 #pragma unroll
@@ -1407,7 +1409,7 @@ __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRec
 		float wa[4], wb[4], wc[4];
 		lane_weights(w, affine, wa, wb, wc);
 		ShadeRecord shade;
-		make_shade(b.tasks[r.task], r.tri, shade);
+		make_shade(b.tasks[r.task], r.source, shade);
 		float rgba[4];
 		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
 		const float opacity = fmul(rgba[3], 1.0f / 255.0f);

@@ -92,6 +92,7 @@ struct __align__(16) DrawRecord {
 	uint32_t tri;                     // fan triangle of its task (polygon data for shading)
 	uint32_t task;                    // index into the batch's task table
 	uint32_t frame;                   // index into the batch's frame table
+	int32_t source;                   // the task's triSource entry of tri (polygon * 2 + fan), for shading
 };
 // The row kernel loads corners and bounds as int4 (flat[0..3]), int4 (flat[4..5], left, top) and int2 (right, bottom).
 static_assert(sizeof(DrawRecord) == 96, "DrawRecord is 96 bytes");
