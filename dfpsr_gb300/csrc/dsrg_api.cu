@@ -212,10 +212,16 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 	size_t pixels = (size_t)r->width * r->height;
 	r->deviceColor = nullptr;
 	r->deviceDepth = nullptr;
+	r->colorDirect = r->depthDirect = false;
+	void *mapped = nullptr;
 	if (color) {
 		if (color->onDevice) {
 			r->deviceColor = (uint32_t *)color->data;
 			r->colorStride = color->strideBytes / 4;
+		} else if (host_mapped(color->data, &mapped)) {
+			r->deviceColor = (uint32_t *)mapped;
+			r->colorStride = color->strideBytes / 4;
+			r->colorDirect = true;
 		} else {
 			CUDA_TRY(ctx, ctx->stagingColor.reserve(pixels));
 			r->deviceColor = ctx->stagingColor.ptr;
@@ -228,6 +234,10 @@ static int begin_frame(dsrg_renderer r, const dsrg_image *color, const dsrg_imag
 		if (depth->onDevice) {
 			r->deviceDepth = (float *)depth->data;
 			r->depthStride = depth->strideBytes / 4;
+		} else if (host_mapped(depth->data, &mapped)) {
+			r->deviceDepth = (float *)mapped;
+			r->depthStride = depth->strideBytes / 4;
+			r->depthDirect = true;
 		} else {
 			CUDA_TRY(ctx, ctx->stagingDepth.reserve(pixels));
 			r->deviceDepth = ctx->stagingDepth.ptr;
@@ -390,6 +400,19 @@ int dsrg_renderer_give_triangles(dsrg_renderer r, int32_t count, const dsrg_proj
 
 } // extern "C"
 
+// A page-locked host image is read and written in place through its device address (over
+// NVLink-C2C on Grace-Blackwell), with no staging copy; pageable memory is staged.
+bool host_mapped(const void *p, void **devicePointer) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+	*devicePointer = a.devicePointer;
+	return true;
+}
+
 int renderer_upload_given(dsrg_renderer r) {
 	if (!r->givenDirty) return DSRG_OK;
 	dsrg_context ctx = r->context;
@@ -465,6 +488,7 @@ static int end_frame(dsrg_renderer r, bool debugWireframe) {
 	renderer_frame_target(r, f);
 	job.depthOnly = r->depthOnly;
 	job.resolve = true;
+	job.hostTargets = r->colorDirect || r->depthDirect;
 	BatchTotals totals;
 	int status = DSRG_OK;
 	// renderer_end(debugWireframe): the edges of every drawn command, collected run by run and
@@ -544,10 +568,10 @@ static int end_frame(dsrg_renderer r, bool debugWireframe) {
 			r->debugColors.clear();
 		}
 	}
-	if (r->hasColor && !r->color.onDevice)
+	if (r->hasColor && !r->color.onDevice && !r->colorDirect)
 		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->color.data, r->color.strideBytes, r->deviceColor, (size_t)r->width * 4,
 		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
-	if (r->hasDepth && !r->depth.onDevice)
+	if (r->hasDepth && !r->depth.onDevice && !r->depthDirect)
 		CUDA_TRY(ctx, cudaMemcpy2DAsync(r->depth.data, r->depth.strideBytes, r->deviceDepth, (size_t)r->width * 4,
 		                                (size_t)r->width * 4, r->height, cudaMemcpyDeviceToHost, ctx->stream));
 	return batch_finish(ctx, totals);

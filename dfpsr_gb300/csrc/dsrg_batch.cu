@@ -29,8 +29,9 @@ struct dsrg_batch_s {
 	std::vector<TaskParams> tasks;
 	std::vector<TextureData> textures;
 	std::unordered_map<dsrg_texture, int32_t> textureSlots;
-	DeviceBuffer<uint32_t> stagingColor; // frames whose images are in host memory
+	DeviceBuffer<uint32_t> stagingColor; // frames whose images are in pageable host memory
 	DeviceBuffer<float> stagingDepth;
+	std::vector<void *> mapped; // per frame: device addresses of page-locked colour and depth images
 	bool depthOnly = false; // model_renderDepth semantics for every frame
 	BatchJob job;
 };
@@ -145,11 +146,14 @@ int dsrg_batch_render(dsrg_batch b) {
 	dsrg_context ctx = b->context;
 	cudaSetDevice(ctx->device);
 	cudaStream_t stream = ctx->stream;
-	// frames in host memory are drawn in staging buffers
+	// frames in page-locked host memory are drawn in place, frames in pageable memory in staging buffers
 	size_t colorPixels = 0, depthPixels = 0;
-	for (const auto &f : b->frames) {
-		if (f.hasColor && !f.color.onDevice) colorPixels += (size_t)f.width * f.height;
-		if (f.hasDepth && !f.depth.onDevice) depthPixels += (size_t)f.width * f.height;
+	std::vector<void *> &mapped = b->mapped;
+	mapped.assign(b->frames.size() * 2, nullptr);
+	for (size_t i = 0; i < b->frames.size(); i++) {
+		const auto &f = b->frames[i];
+		if (f.hasColor && !f.color.onDevice && !host_mapped(f.color.data, &mapped[2 * i])) colorPixels += (size_t)f.width * f.height;
+		if (f.hasDepth && !f.depth.onDevice && !host_mapped(f.depth.data, &mapped[2 * i + 1])) depthPixels += (size_t)f.width * f.height;
 	}
 	if (colorPixels) DSRG_CUDA_TRY(ctx, b->stagingColor.reserve(colorPixels));
 	if (depthPixels) DSRG_CUDA_TRY(ctx, b->stagingDepth.reserve(depthPixels));
@@ -166,8 +170,8 @@ int dsrg_batch_render(dsrg_batch b) {
 		t.affine = f.affine == 1 ? 1 : 0;
 		if (f.hasColor) {
 			t.packOrder = f.color.packOrder;
-			if (f.color.onDevice) {
-				t.color = (uint32_t *)f.color.data;
+			if (f.color.onDevice || mapped[2 * i]) {
+				t.color = (uint32_t *)(f.color.onDevice ? f.color.data : mapped[2 * i]);
 				t.colorStride = f.color.strideBytes / 4;
 			} else {
 				t.color = b->stagingColor.ptr + colorPixels;
@@ -178,8 +182,8 @@ int dsrg_batch_render(dsrg_batch b) {
 			}
 		}
 		if (f.hasDepth) {
-			if (f.depth.onDevice) {
-				t.depth = (float *)f.depth.data;
+			if (f.depth.onDevice || mapped[2 * i + 1]) {
+				t.depth = (float *)(f.depth.onDevice ? f.depth.data : mapped[2 * i + 1]);
 				t.depthStride = f.depth.strideBytes / 4;
 			} else {
 				t.depth = b->stagingDepth.ptr + depthPixels;
@@ -194,6 +198,8 @@ int dsrg_batch_render(dsrg_batch b) {
 	job.textures.swap(b->textures);
 	job.depthOnly = b->depthOnly;
 	job.resolve = true;
+	job.hostTargets = false;
+	for (void *p : mapped) job.hostTargets = job.hostTargets || p != nullptr;
 	if (b->depthOnly) {
 		// renderTriangleFromDataDepth (renderCore.cpp:400-443): 1 x 1 walk, no shading, no colour target
 		for (TaskParams &t : job.tasks) { t.depthOnly = 1; t.diffuse = -1; t.light = -1; }
@@ -212,10 +218,10 @@ int dsrg_batch_render(dsrg_batch b) {
 	for (size_t i = 0; i < b->frames.size(); i++) {
 		const auto &f = b->frames[i];
 		const FrameTarget &t = job.frames[i];
-		if (f.hasColor && !f.color.onDevice)
+		if (f.hasColor && !f.color.onDevice && !mapped[2 * i])
 			DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(f.color.data, f.color.strideBytes, t.color, (size_t)f.width * 4, (size_t)f.width * 4,
 			                                     f.height, cudaMemcpyDeviceToHost, stream));
-		if (f.hasDepth && !f.depth.onDevice)
+		if (f.hasDepth && !f.depth.onDevice && !mapped[2 * i + 1])
 			DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(f.depth.data, f.depth.strideBytes, t.depth, (size_t)f.width * 4, (size_t)f.width * 4,
 			                                     f.height, cudaMemcpyDeviceToHost, stream));
 	}

@@ -126,6 +126,8 @@ struct BatchJob {
 	bool resolve = true;
 	bool alpha = false;         // every task is alpha-filtered and every frame has a colour target
 	bool clearCounters = true;  // false for the later runs of one frame: fragment counts accumulate
+	bool hostTargets = false;   // a target is page-locked host memory drawn in place: resolve per pixel,
+	                            // whose stores run along rows, even where the tuning asks for quads
 };
 
 // The launches of one phase between two host synchronisations, kept as a CUDA graph.  A phase
@@ -230,6 +232,7 @@ struct dsrg_renderer_s {
 	int32_t width = 0, height = 0;
 	uint32_t *deviceColor = nullptr;
 	float *deviceDepth = nullptr;
+	bool colorDirect = false, depthDirect = false; // page-locked host images used in place
 	int32_t colorStride = 0, depthStride = 0;
 	uint32_t triangleCount = 0;   // fan triangles submitted this frame
 	bool depthOnly = false;
@@ -266,6 +269,9 @@ struct dsrg_renderer_s {
 
 // Uploads the frame's renderer_giveTask_triangle data and points its tasks at it.
 int renderer_upload_given(dsrg_renderer r);
+// The device address of page-locked (or registered) host memory, which kernels then read and write
+// in place; false for pageable memory, which is staged through device buffers.
+bool host_mapped(const void *p, void **devicePointer);
 // The frame target of a renderer's current frame (images, size, occlusion grid when in use).
 void renderer_frame_target(dsrg_renderer r, dsrg::FrameTarget &f);
 // Uploads the occlusion grid when the device copy is stale.

@@ -176,9 +176,9 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	config.ctasPerSm = ctx->ctasPerSm;
 	// fewer triangles than one per 8 pixels: tall triangles, whose rows are balanced by row
 	const bool tallTriangles = (uint64_t)totals.triangles * 8u <= (uint64_t)totals.pixels;
-	// winners are shaded per pixel inside the tile kernel unless the per-quad resolve is asked for
-	// (measured faster on both the dense terrain and the large random triangles)
-	config.resolveQuads = ctx->resolveMode == 2 ? 1 : 0;
+	// winners are shaded per pixel inside the tile kernel unless the per-quad resolve is asked for;
+	// targets in host memory take the per-pixel stores (2x2 quads scatter small writes over the link)
+	config.resolveQuads = ctx->resolveMode == 2 && !job.hostTargets ? 1 : 0;
 
 	// Buffers whose sizes depend on earlier phases are sized from the context's capacities (the
 	// largest totals seen, with slack); the phases then run back to back with no host round trip.

@@ -60,8 +60,9 @@ typedef struct {
 /* A target image: ImageRgbaU8 (4 bytes per pixel in packOrder) or ImageF32/AlignedImageF32
  * (float per pixel) (implementation/image/Image.h:249-289).  data points to row 0;
  * strideBytes is the distance between rows.  onDevice = 1 when data is device memory of the
- * context's GPU; 0 when it is host memory (copied to the GPU and back inside the call;
- * page-locked memory makes those copies asynchronous and faster). */
+ * context's GPU; 0 when it is host memory.  Page-locked (or registered) host memory is drawn
+ * in place through its device address: the kernels read and write it over the host link, with
+ * no staging copy.  Pageable host memory is copied to a device buffer and back inside the call. */
 typedef struct {
 	void *data;
 	int32_t width;

@@ -40,9 +40,12 @@ def test_batch_frames_equal_frames_rendered_alone(ctx):
     batch = d.Batch(ctx)
     images = []
     for i, (m, s) in enumerate(zip(models, frame_scenes)):
-        if i % 2 == 0:  # host images
+        if i % 3 == 0:  # pageable host images (staged through device buffers)
             c = np.zeros((s.height, s.width), np.uint32)
             z = np.zeros((s.height, s.width), np.float32)
+        elif i % 3 == 1:  # page-locked host images with padded rows (drawn in place)
+            c = torch.zeros((s.height, s.width + 5), dtype=torch.int32).pin_memory().numpy()[:, : s.width]
+            z = torch.zeros((s.height, s.width + 3), dtype=torch.float32).pin_memory().numpy()[:, : s.width]
         else:  # device images
             c = torch.zeros((s.height, s.width), dtype=torch.int32, device="cuda")
             z = torch.zeros((s.height, s.width), dtype=torch.float32, device="cuda")

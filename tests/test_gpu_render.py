@@ -198,6 +198,43 @@ def test_device_resident_targets(ctx):
     assert np.array_equal(depth.cpu().numpy().view(np.uint32), rd.view(np.uint32))
 
 
+def test_page_locked_host_targets(ctx):
+    """Page-locked host images (drawn in place through their device addresses, no staging copies),
+    with padded rows and prefilled contents, in a frame of solid and alpha-filtered tasks with the
+    wireframe overlay (every pass that reads or writes the targets): identical to the oracle."""
+    import dataclasses
+    import torch
+    import dfpsr_gb300 as d
+    from oracle import port
+    h, w = 150, 230
+    base = scenes.random_triangles(seed=43, triangles=900, width=w, height=h, texture_size=32)
+    parts = [base, dataclasses.replace(scenes.random_triangles(seed=44, triangles=500, width=w, height=h, texture_size=32),
+                                       filter=1)]
+    rng = np.random.default_rng(45)
+    color0 = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    depth0 = rng.uniform(0.0, 0.2, size=(h, w)).astype(np.float32)
+    o = port.OracleRenderer()
+    rc, rz = color0.copy(), depth0.copy()
+    o.begin(rc, rz)
+    pms = [port.PreparedModel(p) for p in parts]
+    for pm, p in zip(pms, parts):
+        o.give_task(pm, p.model_to_world, pm.cam)
+    rc, rz, _ = o.end(debug_wireframe=True)
+    c = torch.zeros((h, w + 7), dtype=torch.int32).pin_memory().numpy()[:, :w].view(np.uint32)
+    z = torch.zeros((h, w + 1), dtype=torch.float32).pin_memory().numpy()[:, :w]
+    models = [d.Model(ctx, p) for p in parts]
+    r = d.Renderer(ctx)
+    for _ in range(2):
+        c[:], z[:] = color0, depth0
+        r.begin(c, z)
+        for m, p in zip(models, parts):
+            r.give_task(m, m.camera, p.model_to_world)
+        r.end(debug_wireframe=True)
+        assert np.array_equal(c, rc), f"{int((c != rc).sum())} colour pixels differ"
+        assert np.array_equal(z.view(np.uint32), rz.view(np.uint32))
+    r.destroy()
+
+
 def test_texture_pyramid_matches_oracle(ctx):
     import dfpsr_gb300 as d
     from oracle import port
