@@ -258,7 +258,7 @@ int dsrg_context_set_tuning(dsrg_context ctx, const dsrg_tuning *t) {
 	ctx->smallRows = t->smallRows;
 	ctx->smallWidth = t->smallWidth;
 	if (t->resolve < 0 || t->resolve > 2)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: resolve must be 0 or 1 (per pixel) or 2 (per quad)");
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: resolve must be 0 (per pixel, own pass), 1 (per pixel, in the tile kernel) or 2 (per quad)");
 	ctx->useGraphs = t->graphs ? 1 : 0;
 	ctx->resolveMode = t->resolve;
 	return DSRG_OK;
@@ -273,33 +273,47 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	struct Shape { int32_t threads, perSm; };
 	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}, {64, 16}};
 	const int32_t smalls[][2] = {{8, 16}, {0, 0}, {4, 8}};
-	const int32_t resolves[] = {1, 2};
-	dsrg_tuning chosen = start;
-	double bestSeconds = -1.0;
+	// the launch shapes with the resolve inside the tile kernel, then the other resolves with the
+	// fastest shape
+	std::vector<dsrg_tuning> candidates;
 	for (const Shape &s : shapes) {
-		for (const auto &sm : smalls) for (const int32_t resolve : resolves) {
+		for (const auto &sm : smalls) {
 			dsrg_tuning t = start;
 			t.threadsPerTile = s.threads;
 			t.ctasPerSm = s.perSm;
 			t.smallRows = sm[0];
 			t.smallWidth = sm[1];
-			t.resolve = resolve;
-			int status = dsrg_context_set_tuning(ctx, &t);
-			if (status != DSRG_OK) return status;
-			status = dsrg_batch_render(b); // warm-up: scratch sizes and graphs for this shape
+			t.resolve = 1;
+			candidates.push_back(t);
+		}
+	}
+	const size_t shapeCount = candidates.size();
+	dsrg_tuning chosen = start;
+	double bestSeconds = -1.0;
+	for (size_t c = 0; c < candidates.size(); c++) {
+		const dsrg_tuning t = candidates[c];
+		int status = dsrg_context_set_tuning(ctx, &t);
+		if (status != DSRG_OK) return status;
+		status = dsrg_batch_render(b); // warm-up: scratch sizes and graphs for this shape
+		if (status != DSRG_OK) { dsrg_context_set_tuning(ctx, &start); return status; }
+		double seconds = -1.0;
+		for (int32_t r = 0; r < rounds; r++) {
+			const auto t0 = std::chrono::steady_clock::now();
+			status = dsrg_batch_render(b);
+			const auto t1 = std::chrono::steady_clock::now();
 			if (status != DSRG_OK) { dsrg_context_set_tuning(ctx, &start); return status; }
-			double seconds = -1.0;
-			for (int32_t r = 0; r < rounds; r++) {
-				const auto t0 = std::chrono::steady_clock::now();
-				status = dsrg_batch_render(b);
-				const auto t1 = std::chrono::steady_clock::now();
-				if (status != DSRG_OK) { dsrg_context_set_tuning(ctx, &start); return status; }
-				const double d = std::chrono::duration<double>(t1 - t0).count();
-				if (seconds < 0.0 || d < seconds) seconds = d;
-			}
-			if (bestSeconds < 0.0 || seconds < bestSeconds) {
-				bestSeconds = seconds;
-				chosen = t;
+			const double d = std::chrono::duration<double>(t1 - t0).count();
+			if (seconds < 0.0 || d < seconds) seconds = d;
+		}
+		if (bestSeconds < 0.0 || seconds < bestSeconds) {
+			bestSeconds = seconds;
+			chosen = t;
+		}
+		if (c + 1 == shapeCount) {
+			for (const int32_t resolve : {0, 2}) {
+				dsrg_tuning t = chosen;
+				t.resolve = resolve;
+				candidates.push_back(t);
 			}
 		}
 	}

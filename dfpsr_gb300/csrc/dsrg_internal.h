@@ -174,7 +174,8 @@ struct dsrg_context_s {
 	unsigned char *pinnedTables = nullptr; // host staging of the tables (page-locked)
 	size_t pinnedCapacity = 0;
 	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag, [4..7] a batch's gathered totals
-	uint32_t *pinnedReadback = nullptr;  // page-locked copy of the gathered totals
+	uint32_t *pinnedReadback = nullptr;  // page-locked copy of the gathered totals (and the fragment count)
+	bool stopRecorded = false;           // the last batch recorded eventStop before its host wait
 	// capacities of the buffers sized before their totals are known (largest totals seen, with slack)
 	uint64_t recordCapacity = 0, rowCapacity = 0, binCapacity = 0;
 	DeviceBuffer<uint32_t> binCounts, binOffsets, binCursors, binLists;
@@ -193,7 +194,7 @@ struct dsrg_context_s {
 	int32_t ctasPerSm = 4;                  // resident CTAs per SM of the persistent tile kernel
 	int32_t threadsPerTile = 256;           // threads of one tile's CTA
 	int32_t useGraphs = 1;                  // replay unchanged phases as CUDA graphs
-	int32_t resolveMode = 0;                // 0 or 1 per pixel (in the tile kernel), 2 per quad
+	int32_t resolveMode = 1;                // 0 per pixel in its own pass, 1 per pixel in the tile kernel, 2 per quad
 	dsrg::PhaseGraph graphs[4];             // phases A, B, C (lists) and D (raster)
 	int32_t counting = 0;
 	uint32_t *coverage = nullptr;

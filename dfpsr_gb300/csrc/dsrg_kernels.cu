@@ -22,6 +22,9 @@
 // the records of a frame are stored in submission order.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <utility>
 
 #include "dsrg_exact.h"
 #include "dsrg_geometry.h"
@@ -56,6 +59,34 @@ static int grid_for(uint64_t n, int threads) {
 	return (int)(blocks > 0 ? blocks : 1);
 }
 
+// Programmatic dependent launch.  A kernel launched with launch_chained may be scheduled while
+// the kernel before it on the stream is still running: that kernel lets it in once all of its
+// CTAs have started (the release in chain_enter), and chain_enter, the first statement of every
+// chained kernel, holds its threads until the predecessor has completed with its writes visible.
+// Captured into a graph the pair becomes a programmatic edge, so the launch of each dependent
+// kernel overlaps the last CTAs of the one before.  Kernels launched the ordinary way pass the
+// wait at once.  Every CTA of a chained kernel runs chain_enter before anything else, so a kernel
+// completes only after its predecessor did and the chain stays ordered end to end.
+__device__ __forceinline__ void chain_enter() {
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... Params, typename... Args>
+static void launch_chained(void (*kernel)(Params...), uint32_t grid, uint32_t block, cudaStream_t stream, Args &&...args) {
+	cudaLaunchAttribute attribute[1];
+	attribute[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attribute[0].val.programmaticStreamSerializationAllowed = 1;
+	cudaLaunchConfig_t config;
+	memset(&config, 0, sizeof(config));
+	config.gridDim = dim3(grid);
+	config.blockDim = dim3(block);
+	config.stream = stream;
+	config.attrs = attribute;
+	config.numAttrs = 1;
+	cudaLaunchKernelEx(&config, kernel, std::forward<Args>(args)...);
+}
+
 // A count written on the device, bounded by the capacity the host sized the buffers for.
 __device__ __forceinline__ uint32_t device_count(uint32_t capacity, const uint32_t *countDevice) {
 	if (!countDevice) return capacity;
@@ -70,6 +101,7 @@ __device__ __forceinline__ bool overflowed(const BatchParams &b) {
 // ------------------------------------------------------------------ projection
 
 __global__ void project_kernel(BatchParams b, ProjectedPoints out) {
+	chain_enter();
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < b.totalPoints; i += gridDim.x * blockDim.x) {
 		const TaskParams &task = b.tasks[find_segment(b.taskPointBase, b.taskCount, i)];
 		const uint32_t local = i - task.pointBase;
@@ -91,7 +123,7 @@ __global__ void project_kernel(BatchParams b, ProjectedPoints out) {
 void launch_project(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
 	if (b.totalPoints == 0) return;
 	COUNT_LAUNCH();
-	project_kernel<<<grid_for(b.totalPoints, 256), 256, 0, stream>>>(b, fb.points);
+	launch_chained(project_kernel, grid_for(b.totalPoints, 256), 256, stream, b, fb.points);
 }
 
 // ------------------------------------------------------------------ triangle setup
@@ -196,6 +228,7 @@ __device__ void emit_record(const TaskParams &task, uint32_t taskIndex, const Fr
 // renderTriangleFromData / renderTriangleFromDataDepth for one fan triangle (renderCore.cpp:220-341, 400-443).
 template <int MODE>
 __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers fb, uint32_t recordCapacity) {
+	chain_enter();
 	const bool WRITE = MODE == SETUP_WRITE;
 	for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < b.totalTriangles; g += gridDim.x * blockDim.x) {
 		const uint32_t k = (uint32_t)find_segment(b.taskTriangleBase, b.taskCount, g);
@@ -267,20 +300,20 @@ void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream
 		return;
 	}
 	COUNT_LAUNCH();
-	setup_kernel<SETUP_COUNT><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
+	launch_chained(setup_kernel<SETUP_COUNT>, grid_for(b.totalTriangles, 256), 256, stream, b, fb, 0u);
 	launch_scan(fb.triCounts, fb.triOffsets, b.totalTriangles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCapacity, cudaStream_t stream) {
 	if (b.totalTriangles == 0) return;
 	COUNT_LAUNCH();
-	setup_kernel<SETUP_WRITE><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, recordCapacity);
+	launch_chained(setup_kernel<SETUP_WRITE>, grid_for(b.totalTriangles, 256), 256, stream, b, fb, recordCapacity);
 }
 
 void launch_setup_occlude(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
 	if (b.totalTriangles == 0) return;
 	COUNT_LAUNCH();
-	setup_kernel<SETUP_OCCLUDE><<<grid_for(b.totalTriangles, 256), 256, 0, stream>>>(b, fb, 0u);
+	launch_chained(setup_kernel<SETUP_OCCLUDE>, grid_for(b.totalTriangles, 256), 256, stream, b, fb, 0u);
 }
 
 // One thread per cell of the grid: the cell's run of the top pixel row of its cell row.  The
@@ -345,6 +378,7 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *shared) {
 
 __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_t *__restrict__ in, uint32_t n, const uint32_t *nDevice,
                                                                    uint32_t capacity, uint32_t *chunkSums) {
+	chain_enter();
 	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
 	const uint32_t count = scan_length(n, nDevice, capacity);
 	const uint32_t begin = blockIdx.x * SCAN_CHUNK;
@@ -357,6 +391,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_
 __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(const uint32_t *__restrict__ in, uint32_t *out, uint32_t n,
                                                                   const uint32_t *nDevice, uint32_t capacity,
                                                                   const uint32_t *__restrict__ chunkSums) {
+	chain_enter();
 	__shared__ uint32_t values[SCAN_CHUNK + SCAN_CHUNK / 32]; // one padding word per 32: a thread's 16 values hit 16 banks
 	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
 	const uint32_t count = scan_length(n, nDevice, capacity);
@@ -418,9 +453,9 @@ static void scan_launch(const uint32_t *in, uint32_t *out, uint32_t n, const uin
 		return;
 	}
 	COUNT_LAUNCH();
-	scan_reduce_kernel<<<blocks, SCAN_THREADS, 0, stream>>>(in, n, nDevice, n, scratch);
+	launch_chained(scan_reduce_kernel, blocks, SCAN_THREADS, stream, in, n, nDevice, n, scratch);
 	COUNT_LAUNCH();
-	scan_apply_kernel<<<blocks, SCAN_THREADS, 0, stream>>>(in, out, n, nDevice, n, scratch);
+	launch_chained(scan_apply_kernel, blocks, SCAN_THREADS, stream, in, out, n, nDevice, n, scratch);
 }
 
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream) {
@@ -436,6 +471,7 @@ void launch_scan_device(const uint32_t *in, uint32_t *out, const uint32_t *nDevi
 // the error bits, gathered into one small block for a single copy.
 __global__ void gather_totals_kernel(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
                                      const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out) {
+	chain_enter();
 	const uint32_t records = triOffsets[triangles];
 	out[0] = records;
 	out[1] = rowOffsets[records < recordCapacity ? records : recordCapacity];
@@ -446,13 +482,14 @@ __global__ void gather_totals_kernel(const uint32_t *triOffsets, uint32_t triang
 void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
                           const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out, cudaStream_t stream) {
 	COUNT_LAUNCH();
-	gather_totals_kernel<<<1, 1, 0, stream>>>(triOffsets, triangles, rowOffsets, recordCapacity, binOffsets, binSlots, errorFlag, out);
+	launch_chained(gather_totals_kernel, 1, 1, stream, triOffsets, triangles, rowOffsets, recordCapacity, binOffsets, binSlots, errorFlag, out);
 }
 
 // ------------------------------------------------------------------ row intervals
 
 __global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_t capacity, const uint32_t *countDevice,
                                  uint32_t *counts) {
+	chain_enter();
 	const uint32_t recordCount = device_count(capacity, countDevice);
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < recordCount; i += gridDim.x * blockDim.x)
 		counts[i] = (uint32_t)(records[i].bottom - records[i].top);
@@ -461,7 +498,7 @@ __global__ void row_count_kernel(const DrawRecord *__restrict__ records, uint32_
 void launch_row_offsets(const FrameBuffers &fb, uint32_t recordCount, uint32_t *rowCounts, cudaStream_t stream) {
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		row_count_kernel<<<grid_for(recordCount, 256), 256, 0, stream>>>(fb.records, recordCount, fb.recordCountDevice, rowCounts);
+		launch_chained(row_count_kernel, grid_for(recordCount, 256), 256, stream, fb.records, recordCount, fb.recordCountDevice, rowCounts);
 	}
 	if (fb.recordCountDevice)
 		launch_scan_device(rowCounts, fb.rowOffsets, fb.recordCountDevice, recordCount, fb.scanScratch, fb.scanScratchElems, stream);
@@ -510,6 +547,7 @@ __device__ __forceinline__ uint32_t warp_search(const uint32_t *offsets, uint32_
 __global__ void __launch_bounds__(ROWS_THREADS) rows_chunk_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
                                                             const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
                                                             uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
+	chain_enter();
 	__shared__ uint32_t first, last;
 	__shared__ uint32_t offsets[ROWS_MAX_RECORDS + 1];
 	__shared__ int4 cornersA[ROWS_MAX_RECORDS];   // flat 0..3
@@ -581,6 +619,7 @@ static const int32_t ROWS_STEPPED_MAX = 16; // records of at most this many rows
 __global__ void __launch_bounds__(256, 3) rows_group_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
                                                    const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
                                                    uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
+	chain_enter();
 	const uint32_t recordCount = device_count(capacity, countDevice);
 	const int lane = threadIdx.x & 31;
 	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -659,10 +698,10 @@ void launch_rows(const FrameBuffers &fb, uint32_t recordCount, bool tallRecords,
 	COUNT_LAUNCH();
 	const uint32_t rowCapacity = fb.rowCapacity ? fb.rowCapacity : 0xFFFFFFFFu;
 	if (tallRecords)
-		rows_chunk_kernel<<<sm_count() * 6, ROWS_THREADS, 0, stream>>>(fb.records, recordCount, fb.recordCountDevice, fb.rowOffsets,
+		launch_chained(rows_chunk_kernel, sm_count() * 6, ROWS_THREADS, stream, fb.records, recordCount, fb.recordCountDevice, fb.rowOffsets,
 		                                                               fb.rows, rowCapacity, fb.errorFlag);
 	else
-		rows_group_kernel<<<grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, 0, stream>>>(
+		launch_chained(rows_group_kernel, grid_for((uint64_t)((recordCount + 31) / 32) * 32, 256), 256, stream,
 			fb.records, recordCount, fb.recordCountDevice, fb.rowOffsets, fb.rows, rowCapacity, fb.errorFlag);
 }
 
@@ -715,6 +754,7 @@ __device__ __forceinline__ bool tile_test_is_exact(const DrawRecord &r) {
 template <bool FILL>
 __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records, uint32_t capacity, const uint32_t *countDevice,
                            TileBins bins, int32_t *errorFlag) {
+	chain_enter();
 	const uint32_t recordCount = device_count(capacity, countDevice);
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t stride = gridDim.x * blockDim.x;
@@ -793,6 +833,7 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 template <bool FILL>
 __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawRecord *__restrict__ records, TileBins bins,
                                                       int32_t *errorFlag) {
+	chain_enter();
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
 	const uint32_t count = *bins.bigCount;
@@ -820,10 +861,33 @@ __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawR
 	}
 }
 
+// Zeroes a batch's tile counters (per-tile counts and cursors, the big-record count, the tile
+// queue) in one launch at the start of its phases, so that no memset node sits in the chain of
+// dependent launches behind it.
+__global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tileQueue) {
+	chain_enter();
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+		bins.counts[i] = 0u;
+		bins.cursors[i] = 0u;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		if (bins.bigCount) *bins.bigCount = 0u;
+		if (tileQueue) *tileQueue = 0u;
+	}
+}
+
+void launch_clear_tiles(const BatchParams &b, const TileBins &bins, cudaStream_t stream) {
+	const uint32_t slots = 2 * b.totalTiles;
+	COUNT_LAUNCH();
+	launch_chained(clear_tiles_kernel, grid_for(slots, 256), 256, stream, bins, slots, b.tileQueue);
+}
+
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
                                  cudaStream_t stream) {
-	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
-	cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+	if (!bins.cleared) {
+		cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+		cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+	}
 	fb.counts.rowCounts = rowCounts;
 	fb.counts.binCounts = bins.counts;
 	fb.counts.bigList = bins.bigList;
@@ -834,36 +898,38 @@ void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t
 	launch_setup_write(b, fb, recordCapacity, stream);
 	if (recordCapacity > 0) {
 		COUNT_LAUNCH();
-		bin_big_kernel<false><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+		launch_chained(bin_big_kernel<false>, sm_count() * 8, 256, stream, b, fb.records, bins, fb.errorFlag);
 	}
 	launch_scan_device(rowCounts, fb.rowOffsets, fb.recordCountDevice, recordCapacity, fb.scanScratch, fb.scanScratchElems, stream);
 	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
-	cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
-	if (bins.bigCount) cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+	if (!bins.cleared) {
+		cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+		if (bins.bigCount) cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+	}
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		bin_kernel<false><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
+		launch_chained(bin_kernel<false>, grid_for(recordCount, 256), 256, stream, b, fb.records, recordCount, fb.recordCountDevice, bins,
 		                                                                  fb.errorFlag);
 		if (bins.bigList) {
 			COUNT_LAUNCH();
-			bin_big_kernel<false><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+			launch_chained(bin_big_kernel<false>, sm_count() * 8, 256, stream, b, fb.records, bins, fb.errorFlag);
 		}
 	}
 	launch_scan(bins.counts, bins.offsets, 2 * b.totalTiles, fb.scanScratch, fb.scanScratchElems, stream);
 }
 
 void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
-	cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+	if (!bins.cleared) cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
-		bin_kernel<true><<<grid_for(recordCount, 256), 256, 0, stream>>>(b, fb.records, recordCount, fb.recordCountDevice, bins,
+		launch_chained(bin_kernel<true>, grid_for(recordCount, 256), 256, stream, b, fb.records, recordCount, fb.recordCountDevice, bins,
 		                                                                 fb.errorFlag);
 		if (bins.bigList) {
 			COUNT_LAUNCH();
-			bin_big_kernel<true><<<sm_count() * 8, 256, 0, stream>>>(b, fb.records, bins, fb.errorFlag);
+			launch_chained(bin_big_kernel<true>, sm_count() * 8, 256, stream, b, fb.records, bins, fb.errorFlag);
 		}
 	}
 }
@@ -1054,6 +1120,7 @@ template <bool DEPTH_ONLY_1X1, int THREADS, bool RESOLVE>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                                          TileBins bins, const uint32_t *__restrict__ rowOffsets,
                                                                          const uint32_t *__restrict__ rows) {
+	chain_enter();
 	constexpr int WARPS = THREADS / 32;
 	if (overflowed(b)) return; // the lists or rows are incomplete: the frame is redone
 	constexpr int PIXELS = TILE_W * TILE_H / THREADS; // tile pixels owned by each thread
@@ -1252,6 +1319,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                             const uint32_t *__restrict__ binOffsets,
                                                             const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	chain_enter();
 	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return; // nothing drawn: the key image was not written here
@@ -1277,6 +1345,7 @@ __global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const
 __global__ void __launch_bounds__(256, 4) resolve_pixels_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                                 const uint32_t *__restrict__ binOffsets,
                                                                 const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	chain_enter();
 	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
@@ -1296,6 +1365,7 @@ __global__ void __launch_bounds__(256, 4) resolve_pixels_kernel(BatchParams b, c
 __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                      const uint32_t *__restrict__ binOffsets,
                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	chain_enter();
 	if (overflowed(b)) return;
 	const uint32_t tile = blockIdx.x;
 	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return;
@@ -1453,7 +1523,7 @@ void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,
                    cudaStream_t stream) {
 	if (b.totalTiles == 0) return;
-	cudaMemsetAsync(b.tileQueue, 0, sizeof(uint32_t), stream);
+	if (!bins.cleared) cudaMemsetAsync(b.tileQueue, 0, sizeof(uint32_t), stream);
 	const int threads = config.threadsPerTile == 64 ? 64 : (config.threadsPerTile == 128 ? 128 : 256);
 	const int maxPerSm = 1024 / threads;
 	const int perSm = config.ctasPerSm < 1 ? 1 : (config.ctasPerSm > maxPerSm ? maxPerSm : config.ctasPerSm);
@@ -1461,20 +1531,20 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	if (ctas > b.totalTiles) ctas = b.totalTiles;
 	COUNT_LAUNCH();
 	// small triangles resolve per pixel inside the tile pass; the keys then never leave the chip
-	const bool fused = resolve && !b.depthOnly && !config.resolveQuads;
+	const bool fused = resolve && !b.depthOnly && config.resolveMode == 1;
 #define DSRG_RASTER(T)                                                                                            \
-	if (b.depthOnly) raster_kernel<true, T, false><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows); \
-	else if (fused) raster_kernel<false, T, true><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows); \
-	else raster_kernel<false, T, false><<<ctas, T, 0, stream>>>(b, fb.records, bins, fb.rowOffsets, fb.rows);
+	if (b.depthOnly) launch_chained(raster_kernel<true, T, false>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	else if (fused) launch_chained(raster_kernel<false, T, true>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	else launch_chained(raster_kernel<false, T, false>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows);
 	if (threads == 64) { DSRG_RASTER(64) }
 	else if (threads == 128) { DSRG_RASTER(128) }
 	else { DSRG_RASTER(256) }
 #undef DSRG_RASTER
 	if (!resolve || fused) return;
 	COUNT_LAUNCH();
-	if (b.depthOnly) resolve_depth_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-	else if (config.resolveQuads) resolve_quads_kernel<<<b.totalTiles, 64, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-	else resolve_pixels_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	if (b.depthOnly) launch_chained(resolve_depth_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	else if (config.resolveMode == 2) launch_chained(resolve_quads_kernel, b.totalTiles, 64, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	else launch_chained(resolve_pixels_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 }
 
 } // namespace dsrg

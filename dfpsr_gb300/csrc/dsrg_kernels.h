@@ -106,6 +106,9 @@ struct TileBins {
 	// record; the count pass fills the list, the fill pass reads it); null: binned in the same launch
 	uint32_t *bigList;
 	uint32_t *bigCount;
+	// counts, cursors, bigCount and the tile queue are zeroed by launch_clear_tiles at the start of
+	// the batch's phases (0: each launcher zeroes what it uses with memsets)
+	int32_t cleared;
 };
 
 // True when one lane walks the whole record inside a tile (small-triangle path).
@@ -134,6 +137,7 @@ void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t r
 // launch_setup_write with the row and tile counting folded in (fb.counts is filled from rowCounts and
 // bins here), then the big records' tile counts and the scans of row counts and tile counts: the
 // work of launch_setup_write + launch_row_offsets + launch_bin_count in one pass over the records.
+void launch_clear_tiles(const BatchParams &b, const TileBins &bins, cudaStream_t stream);
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
                                  cudaStream_t stream);
 // occludeFromExistingTriangles (api/rendererAPI.cpp:240-255): every solid draw command of the batch
@@ -152,7 +156,8 @@ void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t reco
 struct RasterConfig {
 	int32_t threadsPerTile; // 64, 128 or 256
 	int32_t ctasPerSm;      // resident CTAs per SM pulling tiles (at most 1024 / threadsPerTile)
-	int32_t resolveQuads;   // resolve one 2x2 quad per thread (large triangles) instead of one pixel
+	int32_t resolveMode;    // 0 one pixel per thread in a pass of its own, 1 per pixel inside the tile
+	                        // kernel, 2 one 2x2 quad per thread in a pass of its own (same results)
 };
 // resolve = false leaves the winners in the key images (the differentiable renderer reads them).
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,

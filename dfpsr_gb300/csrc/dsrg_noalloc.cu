@@ -180,7 +180,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	RasterConfig config;
 	config.threadsPerTile = ctx->threadsPerTile;
 	config.ctasPerSm = ctx->ctasPerSm;
-	config.resolveQuads = 0; // depth only: the per-pixel depth resolve
+	config.resolveMode = 0; // depth only: the per-pixel depth resolve
 	launch_raster(params, fb, bins, config, true, stream);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
 	uint32_t errorBits = 0;

@@ -136,6 +136,7 @@ static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &ke
 
 static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOutputs *outputs) {
 	cudaStream_t stream = ctx->stream;
+	ctx->stopRecorded = false;
 	totals = BatchTotals();
 	BatchParams params;
 	memset(&params, 0, sizeof(params));
@@ -176,9 +177,9 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	config.ctasPerSm = ctx->ctasPerSm;
 	// fewer triangles than one per 8 pixels: tall triangles, whose rows are balanced by row
 	const bool tallTriangles = (uint64_t)totals.triangles * 8u <= (uint64_t)totals.pixels;
-	// winners are shaded per pixel inside the tile kernel unless the per-quad resolve is asked for;
-	// targets in host memory take the per-pixel stores (2x2 quads scatter small writes over the link)
-	config.resolveQuads = ctx->resolveMode == 2 && !job.hostTargets ? 1 : 0;
+	// how winners are shaded (the context's tuning); targets in host memory take the per-pixel
+	// stores inside the tile kernel (2x2 quads scatter small writes over the link)
+	config.resolveMode = ctx->resolveMode == 2 && job.hostTargets ? 1 : ctx->resolveMode;
 
 	// Buffers whose sizes depend on earlier phases are sized from the context's capacities (the
 	// largest totals seen, with slack); the phases then run back to back with no host round trip.
@@ -228,6 +229,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	bins.listCapacity = binCap;
 	bins.bigList = ctx->bigList.ptr;
 	bins.bigCount = ctx->control.ptr + 8;
+	bins.cleared = 1; // by the first launch of phase A
 	uint32_t *rowCounts = ctx->rowCounts.ptr;
 	uint32_t *gathered = ctx->control.ptr + 4; // records, rows, bin entries, error bits
 	PhaseKey key;
@@ -244,6 +246,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	// phases A (projection, record counts), B (records, row offsets, tile counts) and C (row
 	// intervals, tile lists) as one graph, then D (tiles and resolve) for solid batches as another
 	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
+		launch_clear_tiles(params, bins, stream);
 		launch_project(params, fb, stream);
 		launch_setup_count(params, fb, stream);
 		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
@@ -259,9 +262,15 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		key.phase = 1;
 		TRY(run_phase(ctx, ctx->graphs[1], key, [&] { launch_raster(params, fb, bins, config, job.resolve, stream); }));
 		TRY(cudaEventRecord(ctx->eventRasterStop, stream));
+		// the batch's own work ends here: the one host wait below also completes the timing events
+		TRY(cudaEventRecord(ctx->eventStop, stream));
+		if (ctx->counting)
+			TRY(cudaMemcpyAsync(ctx->pinnedReadback + 4, ctx->fragmentCounter.ptr, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+			                    stream));
 	}
 	TRY(cudaMemcpyAsync(ctx->pinnedReadback, gathered, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaStreamSynchronize(stream));
+	ctx->stopRecorded = !job.alpha;
 	totals.records = ctx->pinnedReadback[0];
 	totals.rows = ctx->pinnedReadback[1];
 	totals.binEntries = ctx->pinnedReadback[2];
@@ -314,7 +323,7 @@ int batch_enqueue(dsrg_context ctx, BatchJob &job, BatchTotals &totals, BatchOut
 	// a batch whose totals outgrow the capacities is redone once per buffer that was too small
 	for (int attempt = 0; attempt < 4 && status == DSRG_RETRY; attempt++) status = enqueue_phases(ctx, job, totals, outputs);
 	if (status == DSRG_RETRY) return fail(ctx, DSRG_ERROR_DEVICE, "batch buffers kept overflowing");
-	if (status == DSRG_OK) TRY(cudaEventRecord(ctx->eventStop, ctx->stream));
+	if (status == DSRG_OK && !ctx->stopRecorded) TRY(cudaEventRecord(ctx->eventStop, ctx->stream));
 	return status;
 }
 
@@ -355,14 +364,18 @@ int occlude_enqueue(dsrg_context ctx, BatchJob &job) {
 	return DSRG_OK;
 }
 
+// Only the setup, row and binning kernels raise error bits, and enqueue_phases has read them
+// after those (gather_totals_kernel): what is left is the fragment count and one wait for the
+// work the caller queued after the batch (image copies, overlays), if any.
 int batch_finish(dsrg_context ctx, const BatchTotals &totals) {
 	cudaStream_t stream = ctx->stream;
 	unsigned long long fragments = 0;
-	if (ctx->counting) TRY(cudaMemcpyAsync(&fragments, ctx->fragmentCounter.ptr, sizeof(fragments), cudaMemcpyDeviceToHost, stream));
-	uint32_t errorBits = 0;
-	TRY(cudaMemcpyAsync(&errorBits, ctx->control.ptr + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+	uint32_t *readback = ctx->pinnedReadback + 4;
+	if (ctx->counting && !ctx->stopRecorded)
+		TRY(cudaMemcpyAsync(readback, ctx->fragmentCounter.ptr, sizeof(fragments), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaStreamSynchronize(stream));
-	if (errorBits != 0) return fail(ctx, DSRG_ERROR_DEVICE, "rasterisation reported device error bits " + std::to_string(errorBits));
+	if (ctx->counting) memcpy(&fragments, readback, sizeof(fragments));
+	ctx->stopRecorded = false;
 	float ms = 0.0f, rasterMs = 0.0f;
 	cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
 	if (totals.triangles > 0) cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);

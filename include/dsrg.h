@@ -257,8 +257,9 @@ int dsrg_batch_render(dsrg_batch batch);
  *   smallRows/Width  triangles whose raster bound is at most smallRows x smallWidth pixels are
  *                    walked by one lane each; larger ones by a whole warp per tile
  *   graphs           1 to replay each phase's launches as a CUDA graph, 0 to launch directly
- *   resolve          how winners are shaded: 0 or 1 per pixel inside the tile kernel, 2 per 2x2
- *                    quad in a launch of its own (same results) */
+ *   resolve          how winners are shaded (same results): 0 one pixel per thread in a launch of
+ *                    its own, 1 per pixel inside the tile kernel (the default), 2 one 2x2 quad
+ *                    per thread in a launch of its own */
 typedef struct {
 	int32_t threadsPerTile;
 	int32_t ctasPerSm;

@@ -162,7 +162,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(ctx):
             batch.give_task(i, m)
         best = batch.autotune(rounds=1)
         assert best["threads_per_tile"] in (64, 128, 256)
-        assert best["resolve"] in (1, 2)
+        assert best["resolve"] in (0, 1, 2)
         assert 1 <= best["ctas_per_sm"] <= 1024 // best["threads_per_tile"]
         assert ctx.tuning() == best
         for c, z in imgs:
