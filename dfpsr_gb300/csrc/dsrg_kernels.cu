@@ -959,60 +959,6 @@ __device__ __forceinline__ void make_shade(const TaskParams &task, int32_t src, 
 	s.light = task.light;
 }
 
-// ------------------------------------------------------------------ the reference's walk over one record
-
-// Walks the row pairs and quads of a record exactly as fillShapeSuper does (fillerTemplates.h:246-385),
-// so every value is the reference's own running sum.  COMPONENTS = 1 for depth only, 3 for shading.
-// visit(pair, x, y1, edge, lanes[component][lane]) is called for every quad in order.
-template <int COMPONENTS, typename Visit>
-__device__ __forceinline__ void walk_record(const DrawRecord &r, const uint32_t *recordRows, int32_t rowStart, int32_t rowEnd,
-                                            int32_t height, Visit visit) {
-	for (int32_t y1 = rowStart; y1 < rowEnd; y1 += 2) {
-		const RowPair pair = record_row_pair(r, recordRows, y1, height);
-		if (!pair.any) continue;
-		float U[COMPONENTS], L[COMPONENTS], v[COMPONENTS][4];
-		for (int c = 0; c < COMPONENTS; c++) {
-			U[c] = fadd(fadd(r.start[c], fmul(r.dx[c], (float)pair.obs + 0.5f)), fmul(r.dy[c], (float)y1 + 0.5f));
-			L[c] = fadd(U[c], r.dy[c]);
-		}
-		const bool allEdge = pair.ibe <= pair.ibs;
-		const int32_t leftEnd = allEdge ? pair.obe : pair.ibs;
-		int32_t x = pair.obs;
-		for (; x < leftEnd; x += 2) {
-			for (int c = 0; c < COMPONENTS; c++) {
-				v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
-				const float d2 = fmul(r.dx[c], 2.0f);
-				U[c] = fadd(U[c], d2); L[c] = fadd(L[c], d2);
-			}
-			visit(pair, x, y1, true, v);
-		}
-		if (!allEdge) {
-			for (int c = 0; c < COMPONENTS; c++) {
-				v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
-			}
-			for (; x < pair.ibe; x += 2) {
-				visit(pair, x, y1, false, v);
-				for (int c = 0; c < COMPONENTS; c++) {
-					const float d2 = fmul(r.dx[c], 2.0f);
-					for (int l = 0; l < 4; l++) v[c][l] = fadd(v[c][l], d2);
-				}
-			}
-			for (int c = 0; c < COMPONENTS; c++) {
-				const float m = fmul(fmul(r.dx[c], 2.0f), (float)((pair.ibe - pair.ibs) >> 1));
-				U[c] = fadd(U[c], m); L[c] = fadd(L[c], m);
-			}
-			for (; x < pair.obe; x += 2) {
-				for (int c = 0; c < COMPONENTS; c++) {
-					v[c][0] = U[c]; v[c][1] = fadd(U[c], r.dx[c]); v[c][2] = L[c]; v[c][3] = fadd(L[c], r.dx[c]);
-					const float d2 = fmul(r.dx[c], 2.0f);
-					U[c] = fadd(U[c], d2); L[c] = fadd(L[c], d2);
-				}
-				visit(pair, x, y1, true, v);
-			}
-		}
-	}
-}
-
 // ------------------------------------------------------------------ tiles
 
 // Depth test of one fragment against the tile's shared keys.
@@ -1062,23 +1008,27 @@ __device__ __forceinline__ uint32_t warp_tile_threshold(const unsigned long long
 // steps is the length of the row walk.  The plane's extreme over the pixel centres of the tile
 // and record bounds lies at a corner; widening it by four times that error bound is conservative.
 // Returns 0xFFFFFFFF (never culled) for non-finite planes.
-__device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
-	const int32_t xa = max(tx0, r.left), xb = min(tx0 + TILE_W, r.right) - 1;
-	const int32_t ya = max(ty0, r.top), yb = min(ty0 + TILE_H, r.bottom) - 1;
-	const float s = r.start[0], dx = r.dx[0], dy = r.dy[0];
+__device__ __forceinline__ uint32_t bound_best_hi(int32_t left, int32_t top, int32_t right, int32_t bottom, float s, float dx, float dy,
+                                                  int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
+	const int32_t xa = max(tx0, left), xb = min(tx0 + TILE_W, right) - 1;
+	const int32_t ya = max(ty0, top), yb = min(ty0 + TILE_H, bottom) - 1;
 	const float fxa = (float)xa + 0.5f, fxb = (float)xb + 0.5f, fya = (float)ya + 0.5f, fyb = (float)yb + 0.5f;
 	const bool up = !affine; // perspective: the largest 1/W wins; orthogonal: the smallest W
 	const float px = (dx >= 0.0f) == up ? fxb : fxa;
 	const float py = (dy >= 0.0f) == up ? fyb : fya;
 	const float extreme = __fadd_rn(__fadd_rn(s, __fmul_rn(dx, px)), __fmul_rn(dy, py));
-	const float bound = __fadd_rn(__fadd_rn(fabsf(s), __fmul_rn(fabsf(dx), (float)(abs(r.right) + abs(r.left) + 2))),
-	                              __fmul_rn(fabsf(dy), (float)(abs(r.bottom) + abs(r.top) + 2)));
-	const int32_t steps = (pixelSteps ? (r.right - r.left) : ((r.right - r.left) >> 1)) + 16;
+	const float bound = __fadd_rn(__fadd_rn(fabsf(s), __fmul_rn(fabsf(dx), (float)(abs(right) + abs(left) + 2))),
+	                              __fmul_rn(fabsf(dy), (float)(abs(bottom) + abs(top) + 2)));
+	const int32_t steps = (pixelSteps ? (right - left) : ((right - left) >> 1)) + 16;
 	const float margin = __fmul_rn(__fmul_rn(bound, (float)steps), 2.384185791015625e-7f); // 2^-22 per step
 	const float best = up ? __fadd_rn(extreme, margin) : __fsub_rn(extreme, margin);
 	if (!isfinite(best) || !isfinite(margin)) return 0xFFFFFFFFu;
 	const uint32_t hi = ordered_depth(best);
 	return affine ? ~hi : hi;
+}
+
+__device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
+	return bound_best_hi(r.left, r.top, r.right, r.bottom, r.start[0], r.dx[0], r.dy[0], tx0, ty0, affine, pixelSteps);
 }
 
 // The winner of one pixel, shaded and written: the reference's running sums of its quad
@@ -1110,10 +1060,10 @@ __device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameT
 
 // Persistent CTAs pull 16x16 tiles of the batch from a device queue.  The binning split every
 // tile's list into small and large records.  Both are dealt round-robin over the warps (warp w of
-// W takes entries w, w + W, ...): a lane walks a small record by itself (the reference's sequential
-// walk; only the quads inside the tile are tested); large records are rasterised by the whole warp,
-// one lane per (row pair, position in the 2x2 quad), which evaluates the reference's running sums
-// once at the tile's left edge and then walks on.
+// W takes entries w, w + W, ...): the quads of a warp's 32 small records inside the tile are spread
+// over its lanes, one quad each (the reference's running sums at that quad, quad_lanes); large
+// records are rasterised by the whole warp, one lane per (row pair, position in the 2x2 quad),
+// which evaluates the running sums once at the tile's left edge and then walks on.
 // All fragments compete for the tile's shared keys; the winners go to the frame's key image.
 // Tiles that nothing covers write nothing: the resolve pass skips them too.
 template <bool DEPTH_ONLY_1X1, int THREADS, bool RESOLVE>
@@ -1163,28 +1113,76 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		const bool cull = depthTest && b.fragments == nullptr;
 		const int32_t validW = min(TILE_W, width - tx0), validH = min(TILE_H, height - ty0);
 		uint32_t tileMin = 0u; // this warp's view of the tile's depth threshold (0: nothing culled yet)
-		// small records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...), each
-		// walked by one lane in the reference's order; spreading them keeps a short list's walks in
-		// parallel on all warps rather than queued on a few
+		// small records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...).
+		// A warp's 32 records are cut into their quads inside the tile, (row pair, quad column)
+		// slots of each record's bound, and the slots are spread evenly over the lanes: a lane finds
+		// its record by a search over the warp's prefix sums, builds the row pair from the record's
+		// two rows and evaluates the reference's running sums at its quad (quad_lanes), so records
+		// of different sizes no longer keep lanes idle.
 		for (uint32_t chunk = smallBegin; chunk < smallEnd; chunk += (uint32_t)THREADS) {
 			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
 			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
-			if (e >= smallEnd) continue;
-			const uint32_t ri = bins.lists[e];
-			const DrawRecord r = records[ri];
-			if (cull && record_best_hi(r, tx0, ty0, affine, false) < tileMin) continue;
-			const int32_t rowStart = max(r.top, ty0), rowEnd = min(r.bottom, ty0 + TILE_H);
-			walk_record<1>(r, rows + rowOffsets[ri], rowStart, rowEnd, height,
-			               [&](const RowPair &pair, int32_t x, int32_t y1, bool edge, const float (*v)[4]) {
-				if (x + 1 < tx0 || x >= tx0 + TILE_W) return;
+			uint32_t ri = 0, rowOffset = 0;
+			int32_t slots = 0, cols = 1, rowStart = 0, colStart = 0, top = 0;
+			float s0 = 0.0f, dx0 = 0.0f, dy0 = 0.0f;
+			if (e < smallEnd) {
+				ri = bins.lists[e];
+				const DrawRecord &r = records[ri];
+				const int32_t left = r.left, right = r.right;
+				top = r.top;
+				const int32_t bottom = r.bottom;
+				s0 = r.start[0]; dx0 = r.dx[0]; dy0 = r.dy[0];
+				rowOffset = rowOffsets[ri];
+				const bool culled = cull && bound_best_hi(left, top, right, bottom, s0, dx0, dy0, tx0, ty0, affine, false) < tileMin;
+				rowStart = max(top, ty0);
+				const int32_t rowEnd = min(bottom, ty0 + TILE_H);
+				colStart = max(left & ~1, tx0);
+				const int32_t colEnd = min((right + 1) & ~1, tx0 + TILE_W);
+				if (!culled && rowEnd > rowStart && colEnd > colStart) {
+					cols = (colEnd - colStart) >> 1;
+					slots = ((rowEnd - rowStart) >> 1) * cols;
+				}
+			}
+			int32_t inclusive = slots;
+			for (int o = 1; o < 32; o <<= 1) {
+				const int32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
+				if (lane >= o) inclusive += v;
+			}
+			const int32_t total = __shfl_sync(0xFFFFFFFFu, inclusive, 31);
+			for (int32_t base = 0; base < total; base += 32) {
+				const int32_t j = base + lane;
+				int k = 0; // the first lane whose inclusive sum exceeds j
+				for (int step = 16; step >= 1; step >>= 1)
+					if (__shfl_sync(0xFFFFFFFFu, inclusive, k + step - 1) <= j) k += step;
+				const int32_t first = __shfl_sync(0xFFFFFFFFu, inclusive, k) - __shfl_sync(0xFFFFFFFFu, slots, k);
+				const int32_t kCols = __shfl_sync(0xFFFFFFFFu, cols, k);
+				const int32_t kRowStart = __shfl_sync(0xFFFFFFFFu, rowStart, k), kColStart = __shfl_sync(0xFFFFFFFFu, colStart, k);
+				const int32_t kTop = __shfl_sync(0xFFFFFFFFu, top, k);
+				const uint32_t kRecord = __shfl_sync(0xFFFFFFFFu, ri, k), kRowOffset = __shfl_sync(0xFFFFFFFFu, rowOffset, k);
+				const float kS = __shfl_sync(0xFFFFFFFFu, s0, k), kDx = __shfl_sync(0xFFFFFFFFu, dx0, k);
+				const float kDy = __shfl_sync(0xFFFFFFFFu, dy0, k);
+				if (j >= total) continue;
+				const int32_t slot = j - first;
+				const int32_t pairIndex = slot / kCols;
+				const int32_t y1 = kRowStart + 2 * pairIndex, x = kColStart + 2 * (slot - pairIndex * kCols);
+				// the record's rows y1 and y1 + 1 (row offsets are even: one 8-byte load)
+				const uint2 two = *reinterpret_cast<const uint2 *>(rows + kRowOffset + (uint32_t)(y1 - kTop));
+				int32_t uL, uR, lL, lR;
+				unpack_row(two.x, uL, uR);
+				unpack_row(two.y, lL, lR);
+				const RowPair pair = make_row_pair(uL, uR, lL, lR, y1 + 1, height);
+				if (!pair.any || x < pair.obs || x >= pair.obe) continue;
+				const bool edge = pair.ibe <= pair.ibs || x < pair.ibs || x >= pair.ibe;
+				float v[4];
+				quad_lanes(kS, kDx, kDy, pair, y1, x, v);
 				for (int l = 0; l < 4; l++) {
 					const int32_t xx = x + (l & 1), yy = y1 + (l >> 1);
-					if (xx < tx0 || xx >= tx0 + TILE_W || yy >= height || xx >= width) continue;
+					if (yy >= height || xx >= width) continue;
 					if (!lane_covered(pair, x, edge, l)) continue;
-					tile_fragment(keys, initialDepth, coverage, counting, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[0][l], ri,
+					tile_fragment(keys, initialDepth, coverage, counting, (yy - ty0) * TILE_STRIDE + (xx - tx0), v[l], kRecord,
 					              depthTest, affine, fragments);
 				}
-			});
+			}
 		}
 		// large records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...),
 		// each rasterised by the whole warp
