@@ -33,7 +33,8 @@ int dsrg_context_create(int32_t device, dsrg_context *out) {
 	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
 	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(1) != cudaSuccess ||
-	    cudaMallocHost((void **)&ctx->pinnedReadback, 16 * sizeof(uint32_t)) != cudaSuccess) {
+	    cudaMallocHost((void **)&ctx->pinnedReadback, 16 * sizeof(uint32_t)) != cudaSuccess ||
+	    cudaHostGetDevicePointer((void **)&ctx->readbackDevice, ctx->pinnedReadback, 0) != cudaSuccess) {
 		delete ctx;
 		return DSRG_ERROR_CUDA;
 	}
@@ -82,6 +83,15 @@ int dsrg_context_set_counting(dsrg_context ctx, int32_t counting, uint32_t *devi
 
 int dsrg_context_get_stats(dsrg_context ctx, dsrg_stats *out) {
 	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (ctx->timingPending) {
+		// the last call's events completed before it returned
+		float ms = 0.0f, rasterMs = 0.0f;
+		cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
+		if (ctx->timingHasRaster) cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);
+		ctx->stats.milliseconds = ms;
+		ctx->stats.rasterMilliseconds = rasterMs;
+		ctx->timingPending = false;
+	}
 	*out = ctx->stats;
 	return DSRG_OK;
 }

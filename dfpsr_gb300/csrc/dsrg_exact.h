@@ -8,6 +8,7 @@
 #ifndef DSRG_EXACT_H
 #define DSRG_EXACT_H
 
+#include <math.h>
 #include <stdint.h>
 
 #if defined(__CUDACC__)
@@ -246,7 +247,19 @@ struct EdgeStepper {
 	// horizontal edges reuse q as (128 + 256 y - sy) * ny, qd as its change per row and B as the threshold
 };
 
-DSRG_HD void floor_divide(int64_t a, int64_t b, int64_t &q, int64_t &r) { // b > 0
+// floor(a / b) and its remainder, b > 0.  Quotients below 2^22 in magnitude (every row crossing
+// inside an image) come from a binary32 estimate: a, b and their quotient each round by at most
+// 2^-24 relative, so the estimate lies within 0.75 of a / b and its floor within 1 of the answer,
+// which exact 64-bit products then correct.  Larger quotients take the 64-bit division.
+DSRG_HD void floor_divide(int64_t a, int64_t b, int64_t &q, int64_t &r) {
+	const float qf = fdiv(i64_to_float(a), i64_to_float(b));
+	if (qf > -4194304.0f && qf < 4194304.0f) {
+		q = (int64_t)floorf(qf);
+		r = a - q * b;
+		while (r < 0) { q -= 1; r += b; }
+		while (r >= b) { q += 1; r -= b; }
+		return;
+	}
 	q = a / b;
 	if (a % b != 0 && a < 0) q -= 1;
 	r = a - q * b;

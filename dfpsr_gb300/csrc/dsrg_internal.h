@@ -174,7 +174,10 @@ struct dsrg_context_s {
 	unsigned char *pinnedTables = nullptr; // host staging of the tables (page-locked)
 	size_t pinnedCapacity = 0;
 	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag, [4..7] a batch's gathered totals
-	uint32_t *pinnedReadback = nullptr;  // page-locked copy of the gathered totals (and the fragment count)
+	uint32_t *pinnedReadback = nullptr;  // page-locked: the gathered totals (written there by the GPU) and the fragment count
+	uint32_t *readbackDevice = nullptr;  // its device address
+	bool timingPending = false;          // stats' times not yet read from the events of the last call
+	bool timingHasRaster = false;
 	bool stopRecorded = false;           // the last batch recorded eventStop before its host wait
 	// capacities of the buffers sized before their totals are known (largest totals seen, with slack)
 	uint64_t recordCapacity = 0, rowCapacity = 0, binCapacity = 0;

@@ -862,9 +862,9 @@ __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawR
 }
 
 // Zeroes a batch's tile counters (per-tile counts and cursors, the big-record count, the tile
-// queue) in one launch at the start of its phases, so that no memset node sits in the chain of
-// dependent launches behind it.
-__global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tileQueue) {
+// queue) and its error bits in one launch at the start of its phases, so that no memset node sits
+// in the chain of dependent launches behind it.
+__global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tileQueue, int32_t *errorFlag) {
 	chain_enter();
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
 		bins.counts[i] = 0u;
@@ -873,13 +873,14 @@ __global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tile
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		if (bins.bigCount) *bins.bigCount = 0u;
 		if (tileQueue) *tileQueue = 0u;
+		if (errorFlag) *errorFlag = 0;
 	}
 }
 
-void launch_clear_tiles(const BatchParams &b, const TileBins &bins, cudaStream_t stream) {
+void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *errorFlag, cudaStream_t stream) {
 	const uint32_t slots = 2 * b.totalTiles;
 	COUNT_LAUNCH();
-	launch_chained(clear_tiles_kernel, grid_for(slots, 256), 256, stream, bins, slots, b.tileQueue);
+	launch_chained(clear_tiles_kernel, grid_for(slots, 256), 256, stream, bins, slots, b.tileQueue, errorFlag);
 }
 
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,

@@ -106,8 +106,8 @@ struct TileBins {
 	// record; the count pass fills the list, the fill pass reads it); null: binned in the same launch
 	uint32_t *bigList;
 	uint32_t *bigCount;
-	// counts, cursors, bigCount and the tile queue are zeroed by launch_clear_tiles at the start of
-	// the batch's phases (0: each launcher zeroes what it uses with memsets)
+	// counts, cursors, bigCount, the tile queue and the error bits are zeroed by launch_clear_tiles
+	// at the start of the batch's phases (0: each launcher zeroes what it uses with memsets)
 	int32_t cleared;
 };
 
@@ -137,7 +137,7 @@ void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t r
 // launch_setup_write with the row and tile counting folded in (fb.counts is filled from rowCounts and
 // bins here), then the big records' tile counts and the scans of row counts and tile counts: the
 // work of launch_setup_write + launch_row_offsets + launch_bin_count in one pass over the records.
-void launch_clear_tiles(const BatchParams &b, const TileBins &bins, cudaStream_t stream);
+void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *errorFlag, cudaStream_t stream);
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
                                  cudaStream_t stream);
 // occludeFromExistingTriangles (api/rendererAPI.cpp:240-255): every solid draw command of the batch

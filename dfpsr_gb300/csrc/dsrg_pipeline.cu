@@ -157,7 +157,6 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(cudaMemcpyAsync(ctx->tables.ptr, ctx->pinnedTables, tableBytes, cudaMemcpyHostToDevice, stream));
 	// without the resolve pass the caller reads every key, also where no tile was drawn
 	if (!job.resolve && totals.pixels > 0) TRY(cudaMemsetAsync(ctx->keys.ptr, 0, totals.pixels * sizeof(unsigned long long), stream));
-	TRY(cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), stream));
 	params.smallRows = ctx->smallRows;
 	params.smallWidth = ctx->smallWidth;
 	params.tileQueue = ctx->control.ptr;
@@ -231,7 +230,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	bins.bigCount = ctx->control.ptr + 8;
 	bins.cleared = 1; // by the first launch of phase A
 	uint32_t *rowCounts = ctx->rowCounts.ptr;
-	uint32_t *gathered = ctx->control.ptr + 4; // records, rows, bin entries, error bits
+	uint32_t *gathered = ctx->readbackDevice; // records, rows, bin entries, error bits: written into host memory
 	PhaseKey key;
 	memset(&key, 0, sizeof(key));
 	key.resolve = job.resolve ? 1 : 0;
@@ -246,7 +245,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	// phases A (projection, record counts), B (records, row offsets, tile counts) and C (row
 	// intervals, tile lists) as one graph, then D (tiles and resolve) for solid batches as another
 	TRY(run_phase(ctx, ctx->graphs[0], key, [&] {
-		launch_clear_tiles(params, bins, stream);
+		launch_clear_tiles(params, bins, fb.errorFlag, stream);
 		launch_project(params, fb, stream);
 		launch_setup_count(params, fb, stream);
 		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
@@ -268,7 +267,6 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 			TRY(cudaMemcpyAsync(ctx->pinnedReadback + 4, ctx->fragmentCounter.ptr, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
 			                    stream));
 	}
-	TRY(cudaMemcpyAsync(ctx->pinnedReadback, gathered, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
 	TRY(cudaStreamSynchronize(stream));
 	ctx->stopRecorded = !job.alpha;
 	totals.records = ctx->pinnedReadback[0];
@@ -376,14 +374,11 @@ int batch_finish(dsrg_context ctx, const BatchTotals &totals) {
 	TRY(cudaStreamSynchronize(stream));
 	if (ctx->counting) memcpy(&fragments, readback, sizeof(fragments));
 	ctx->stopRecorded = false;
-	float ms = 0.0f, rasterMs = 0.0f;
-	cudaEventElapsedTime(&ms, ctx->eventStart, ctx->eventStop);
-	if (totals.triangles > 0) cudaEventElapsedTime(&rasterMs, ctx->eventRasterStart, ctx->eventRasterStop);
+	ctx->timingPending = true;
+	ctx->timingHasRaster = totals.triangles > 0;
 	ctx->stats.fragments = fragments;
 	ctx->stats.drawRecords = totals.records;
 	ctx->stats.binEntries = totals.binEntries;
-	ctx->stats.milliseconds = ms;
-	ctx->stats.rasterMilliseconds = rasterMs;
 	ctx->stats.kernelLaunches = launch_count();
 	return DSRG_OK;
 }
