@@ -463,6 +463,7 @@ def main():
         return
     import torch
     import dfpsr_gb300 as d
+    from dfpsr_gb300 import replicas
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -536,13 +537,9 @@ def main():
             frame_device()
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in events]
-    total_s = sum(step_ms) / 1e3
+    total_s = replicas.max_over_ranks(sum(step_ms) / 1e3, dist)
     if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-        if dist:
-            dist.barrier()
+        dist.barrier()
 
     # end to end through the C ABI with page-locked host images
     host_color = torch.zeros((h, w), dtype=torch.int32).pin_memory().numpy()
@@ -556,11 +553,7 @@ def main():
         t0 = time.perf_counter()
         ctx.render(model, model.camera, host_color, host_depth)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(sum(e2e_times), dist)
 
     if rank == 0:
         peaks, peak_kind = measured_peaks()
