@@ -164,10 +164,13 @@ def lib():
     return _lib
 
 
-def _torch_sync():
+def _torch_sync(*images):
     """Waits for torch's current stream: device tensors handed to the library may still be being
     written there, and the library works on its own stream.  (Every library call returns with
-    its own work finished, so torch may read the results right after.)"""
+    its own work finished, so torch may read the results right after.)  Given the call's images,
+    it waits only when one of them is a device tensor."""
+    if images and all(a is None or isinstance(a, np.ndarray) for a in images):
+        return
     import sys
     torch = sys.modules.get("torch")
     if torch is not None and torch.cuda.is_available() and torch.cuda.is_initialized():
@@ -293,7 +296,7 @@ class Context:
         """dsrg_model_render into the given host (numpy) or device (torch) images, in place."""
         t = np.ascontiguousarray(model.transform if transform is None else transform, np.float32)
         ci, di = image_struct(color, pack_order), image_struct(depth)
-        _torch_sync()
+        _torch_sync(color, depth)
         self._check(self._l.dsrg_model_render(self.handle, model.handle, t.ctypes.data, C.byref(camera),
                                               C.byref(ci) if ci else None, C.byref(di) if di else None))
 
@@ -480,7 +483,7 @@ class Renderer:
         self.ctx._check(self.ctx._l.dsrg_renderer_give_task(self.handle, model.handle, t.ctypes.data, C.byref(cam)))
 
     def end(self, debug_wireframe: bool = False):
-        _torch_sync()
+        _torch_sync(*(self._images[:2] if self._images else ()))
         if debug_wireframe:
             self.ctx._check(self.ctx._l.dsrg_renderer_end_debug(self.handle, 1))
         else:
