@@ -1260,16 +1260,16 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				float R, V = 0.0f, Rb = 0.0f;
 				if (allEdge || x0 < pair.ibs) {
 					region = 0;
-					R = chain_add(R0, d2, (x0 - pair.obs) >> 1);
+					R = chain_add_short(R0, d2, (x0 - pair.obs) >> 1);
 				} else {
-					Rb = chain_add(R0, d2, nL);
+					Rb = chain_add_short(R0, d2, nL);
 					if (x0 < pair.ibe) {
 						region = 1;
 						R = Rb;
-						V = chain_add(odd ? fadd(Rb, dx) : Rb, d2, (x0 - pair.ibs) >> 1);
+						V = chain_add_short(odd ? fadd(Rb, dx) : Rb, d2, (x0 - pair.ibs) >> 1);
 					} else {
 						region = 2;
-						R = chain_add(fadd(Rb, m), d2, (x0 - pair.ibe) >> 1);
+						R = chain_add_short(fadd(Rb, m), d2, (x0 - pair.ibe) >> 1);
 					}
 				}
 				const int pixRow = (yy - ty0) * TILE_STRIDE;

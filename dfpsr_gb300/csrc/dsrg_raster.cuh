@@ -55,6 +55,18 @@ __device__ __forceinline__ RowPair record_row_pair(const DrawRecord &r, const ui
 	return make_row_pair(uL, uR, lL, lR, y1 + 1, height);
 }
 
+// chain_add for the short chains of small triangles: up to three additions straight in line
+// (predicated, no loop and no call), longer chains through chain_add.
+__device__ __forceinline__ float chain_add_short(float s, float d, int32_t n) {
+	if (n <= 3) {
+		if (n > 0) s = fadd(s, d);
+		if (n > 1) s = fadd(s, d);
+		if (n > 2) s = fadd(s, d);
+		return s;
+	}
+	return chain_add(s, d, n);
+}
+
 // The four lane values of one component (1/W or W, U/W, V/W) for the quad at x, following the
 // reference's accumulation: edge quads step pWeightUpper/Lower by 2*dx one quad at a time, the
 // run of full quads steps every lane on its own from where the left edge stopped, and the right
@@ -66,22 +78,22 @@ __device__ __forceinline__ void quad_lanes(float start, float dx, float dy, cons
 	const float d2 = fmul(dx, 2.0f);
 	if (rp.ibe <= rp.ibs || x < rp.ibs) {
 		int32_t k = (x - rp.obs) >> 1;
-		float U = chain_add(P0, d2, k), L = chain_add(L0, d2, k);
+		float U = chain_add_short(P0, d2, k), L = chain_add_short(L0, d2, k);
 		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
 		return;
 	}
 	const int32_t nL = (rp.ibs - rp.obs) >> 1;
-	const float Ub = chain_add(P0, d2, nL), Lb = chain_add(L0, d2, nL);
+	const float Ub = chain_add_short(P0, d2, nL), Lb = chain_add_short(L0, d2, nL);
 	if (x < rp.ibe) {
 		int32_t j = (x - rp.ibs) >> 1;
-		out[0] = chain_add(Ub, d2, j);
-		out[1] = chain_add(fadd(Ub, dx), d2, j);
-		out[2] = chain_add(Lb, d2, j);
-		out[3] = chain_add(fadd(Lb, dx), d2, j);
+		out[0] = chain_add_short(Ub, d2, j);
+		out[1] = chain_add_short(fadd(Ub, dx), d2, j);
+		out[2] = chain_add_short(Lb, d2, j);
+		out[3] = chain_add_short(fadd(Lb, dx), d2, j);
 	} else {
 		int32_t nI = (rp.ibe - rp.ibs) >> 1, r = (x - rp.ibe) >> 1;
 		float m = fmul(d2, (float)nI);
-		float U = chain_add(fadd(Ub, m), d2, r), L = chain_add(fadd(Lb, m), d2, r);
+		float U = chain_add_short(fadd(Ub, m), d2, r), L = chain_add_short(fadd(Lb, m), d2, r);
 		out[0] = U; out[1] = fadd(U, dx); out[2] = L; out[3] = fadd(L, dx);
 	}
 }
