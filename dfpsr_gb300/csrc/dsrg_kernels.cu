@@ -1124,7 +1124,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
 			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
 			uint32_t ri = 0, rowOffset = 0;
-			int32_t slots = 0, cols = 1, rowStart = 0, colStart = 0, top = 0;
+			int32_t slots = 0, cols = 1, rowStart = 0, colStart = 0, top = 0, colsRecip = 65536;
 			float s0 = 0.0f, dx0 = 0.0f, dy0 = 0.0f;
 			if (e < smallEnd) {
 				ri = bins.lists[e];
@@ -1143,6 +1143,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 					cols = (colEnd - colStart) >> 1;
 					slots = ((rowEnd - rowStart) >> 1) * cols;
 				}
+				colsRecip = (65536 + cols - 1) / cols;
 			}
 			int32_t inclusive = slots;
 			for (int o = 1; o < 32; o <<= 1) {
@@ -1156,7 +1157,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				for (int step = 16; step >= 1; step >>= 1)
 					if (__shfl_sync(0xFFFFFFFFu, inclusive, k + step - 1) <= j) k += step;
 				const int32_t first = __shfl_sync(0xFFFFFFFFu, inclusive, k) - __shfl_sync(0xFFFFFFFFu, slots, k);
-				const int32_t kCols = __shfl_sync(0xFFFFFFFFu, cols, k);
+				const int32_t kCols = __shfl_sync(0xFFFFFFFFu, cols, k), kRecip = __shfl_sync(0xFFFFFFFFu, colsRecip, k);
 				const int32_t kRowStart = __shfl_sync(0xFFFFFFFFu, rowStart, k), kColStart = __shfl_sync(0xFFFFFFFFu, colStart, k);
 				const int32_t kTop = __shfl_sync(0xFFFFFFFFu, top, k);
 				const uint32_t kRecord = __shfl_sync(0xFFFFFFFFu, ri, k), kRowOffset = __shfl_sync(0xFFFFFFFFu, rowOffset, k);
@@ -1164,7 +1165,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				const float kDy = __shfl_sync(0xFFFFFFFFu, dy0, k);
 				if (j >= total) continue;
 				const int32_t slot = j - first;
-				const int32_t pairIndex = slot / kCols;
+				const int32_t pairIndex = (slot * kRecip) >> 16; // slot / kCols: slots < 64, columns <= 8
 				const int32_t y1 = kRowStart + 2 * pairIndex, x = kColStart + 2 * (slot - pairIndex * kCols);
 				// the record's rows y1 and y1 + 1 (row offsets are even: one 8-byte load)
 				const uint2 two = *reinterpret_cast<const uint2 *>(rows + kRowOffset + (uint32_t)(y1 - kTop));

@@ -44,7 +44,7 @@ DSRG_HD uint32_t texel_load(const uint32_t *p, uint32_t index) {
 }
 
 // texture_sample_bilinear with MIP_INSIDE (api/textureAPI.h:320-430).
-DSRG_HD_CALL uint32_t sample_bilinear(const TextureData &t, float u, float v, uint32_t mip, bool highest) {
+DSRG_HD uint32_t sample_bilinear(const TextureData &t, float u, float v, uint32_t mip, bool highest) {
 	uint32_t scaleU = 256u << t.log2width, scaleV = 256u << t.log2height;
 	uint32_t maskX = t.maxWidthAndMask, maskY = t.maxHeightAndMask;
 	uint32_t log2Stride = t.log2width;
