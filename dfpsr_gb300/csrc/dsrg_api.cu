@@ -50,9 +50,9 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	cudaSetDevice(ctx->device);
 	cudaStreamSynchronize(ctx->stream);
 	if (ctx->implicitRenderer) dsrg_renderer_destroy(ctx->implicitRenderer);
-	DeviceBuffer<float> *fbufs[] = {&ctx->csx, &ctx->csy, &ctx->csz, &ctx->isx, &ctx->isy, &ctx->stagingDepth};
+	DeviceBuffer<float> *fbufs[] = {&ctx->pointIsy, &ctx->stagingDepth};
 	for (auto *b : fbufs) b->release();
-	ctx->flatx.release(); ctx->flaty.release();
+	ctx->pointCsis.release(); ctx->pointFlat.release();
 	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();

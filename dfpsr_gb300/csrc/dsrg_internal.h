@@ -166,8 +166,9 @@ struct dsrg_context_s {
 	cudaStream_t stream = nullptr;
 	std::string lastError;
 	// frame scratch, grown on demand and reused
-	DeviceBuffer<float> csx, csy, csz, isx, isy;
-	DeviceBuffer<int64_t> flatx, flaty;
+	DeviceBuffer<float4> pointCsis;      // projected points (ProjectedPoints)
+	DeviceBuffer<float> pointIsy;
+	DeviceBuffer<longlong2> pointFlat;
 	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
 	DeviceBuffer<DrawRecord> records;
 	DeviceBuffer<unsigned char> tables;  // the batch's task, frame and texture tables

@@ -107,16 +107,16 @@ __global__ void project_kernel(BatchParams b, ProjectedPoints out) {
 		const uint32_t local = i - task.pointBase;
 		if (task.given) { // renderer_giveTask_triangle: projected by the caller
 			const GivenPoint &g = task.given[local];
-			out.csx[i] = g.cs[0]; out.csy[i] = g.cs[1]; out.csz[i] = g.cs[2];
-			out.isx[i] = g.is[0]; out.isy[i] = g.is[1];
-			out.flatx[i] = g.flat[0]; out.flaty[i] = g.flat[1];
+			out.csis[i] = make_float4(g.cs[0], g.cs[1], g.cs[2], g.is[0]);
+			out.isy[i] = g.is[1];
+			out.flat[i] = make_longlong2(g.flat[0], g.flat[1]);
 			continue;
 		}
 		Vec3 p = vec3(task.positions[local * 3], task.positions[local * 3 + 1], task.positions[local * 3 + 2]);
 		Projected pr = camera_to_screen(task.camera, world_to_camera(task.camera, transform_point(task.modelToWorld, p)));
-		out.csx[i] = pr.cs.x; out.csy[i] = pr.cs.y; out.csz[i] = pr.cs.z;
-		out.isx[i] = pr.isx; out.isy[i] = pr.isy;
-		out.flatx[i] = pr.flatx; out.flaty[i] = pr.flaty;
+		out.csis[i] = make_float4(pr.cs.x, pr.cs.y, pr.cs.z, pr.isx);
+		out.isy[i] = pr.isy;
+		out.flat[i] = make_longlong2(pr.flatx, pr.flaty);
 	}
 }
 
@@ -244,9 +244,11 @@ __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers 
 		Corner c[3];
 		for (int i = 0; i < 3; i++) {
 			const uint32_t pi = task.pointBase + (uint32_t)task.polygons[p * 4 + corner[i]];
-			c[i].cs = vec3(fb.points.csx[pi], fb.points.csy[pi], fb.points.csz[pi]);
-			c[i].isx = fb.points.isx[pi]; c[i].isy = fb.points.isy[pi];
-			c[i].fx = fb.points.flatx[pi]; c[i].fy = fb.points.flaty[pi];
+			const float4 a = fb.points.csis[pi];
+			const longlong2 f = fb.points.flat[pi];
+			c[i].cs = vec3(a.x, a.y, a.z);
+			c[i].isx = a.w; c[i].isy = fb.points.isy[pi];
+			c[i].fx = f.x; c[i].fy = f.y;
 		}
 		const uint32_t order = (task.orderBase + t) * 8u;
 		bool visible = triangle_visibility(task.camera, c[0].cs, c[1].cs, c[2].cs, false) != 0;

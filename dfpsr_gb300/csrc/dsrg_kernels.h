@@ -69,6 +69,15 @@ struct BatchParams {
 	const int32_t *errorFlag;         // device error bits; tile and resolve kernels return when an overflow is set
 };
 
+// Projected corners (implementation/render/ProjectedPoint.h:33-49): the camera-space position and
+// the image x in one 16-byte vector, the image y, and both sub-pixel coordinates in one 16-byte
+// vector, so that the triangle setup gathers a corner with three loads.
+struct ProjectedPoints {
+	float4 *csis;     // cs.x, cs.y, cs.z, is.x
+	float *isy;       // is.y
+	longlong2 *flat;  // flat x, flat y
+};
+
 struct FrameBuffers {
 	ProjectedPoints points;
 	uint32_t *triCounts;      // per fan triangle: draw records it emits

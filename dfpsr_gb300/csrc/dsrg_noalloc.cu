@@ -92,9 +92,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	const size_t np = (size_t)DSRG_NOALLOC_MAX_POINTS;
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
-	fb.points.csx = carve.take<float>(np); fb.points.csy = carve.take<float>(np); fb.points.csz = carve.take<float>(np);
-	fb.points.isx = carve.take<float>(np); fb.points.isy = carve.take<float>(np);
-	fb.points.flatx = carve.take<int64_t>(np); fb.points.flaty = carve.take<int64_t>(np);
+	fb.points.csis = carve.take<float4>(np); fb.points.isy = carve.take<float>(np); fb.points.flat = carve.take<longlong2>(np);
 	fb.triCounts = carve.take<uint32_t>(DSRG_NOALLOC_MAX_TRIANGLES + 2);
 	fb.triOffsets = carve.take<uint32_t>(DSRG_NOALLOC_MAX_TRIANGLES + 2);
 	fb.records = carve.take<DrawRecord>(MAX_RECORDS);

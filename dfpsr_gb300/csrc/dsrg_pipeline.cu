@@ -188,9 +188,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	const uint32_t recordCap = (uint32_t)std::max<uint64_t>(ctx->recordCapacity, nt + nt / 8 + 1024);
 	const uint32_t rowCap = (uint32_t)std::max<uint64_t>(ctx->rowCapacity, (uint64_t)recordCap * 4);
 	const uint32_t binCap = (uint32_t)std::max<uint64_t>(ctx->binCapacity, (uint64_t)recordCap * 2);
-	TRY(ctx->csx.reserve(np)); TRY(ctx->csy.reserve(np)); TRY(ctx->csz.reserve(np));
-	TRY(ctx->isx.reserve(np)); TRY(ctx->isy.reserve(np));
-	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
+	TRY(ctx->pointCsis.reserve(np)); TRY(ctx->pointIsy.reserve(np)); TRY(ctx->pointFlat.reserve(np));
 	TRY(ctx->triCounts.reserve(nt + 1));
 	TRY(ctx->triOffsets.reserve(nt + 1));
 	TRY(ctx->records.reserve((size_t)recordCap + 1));
@@ -206,9 +204,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)largest + 1)));
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
-	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
-	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
-	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
+	fb.points.csis = ctx->pointCsis.ptr; fb.points.isy = ctx->pointIsy.ptr; fb.points.flat = ctx->pointFlat.ptr;
 	fb.triCounts = ctx->triCounts.ptr;
 	fb.triOffsets = ctx->triOffsets.ptr;
 	fb.records = ctx->records.ptr;
@@ -345,14 +341,10 @@ int occlude_enqueue(dsrg_context ctx, BatchJob &job) {
 	layout_tables(job, nullptr, ctx->pinnedTables, ctx->tables.ptr, params, totals);
 	TRY(cudaMemcpyAsync(ctx->tables.ptr, ctx->pinnedTables, tableBytes, cudaMemcpyHostToDevice, stream));
 	const size_t np = totals.points;
-	TRY(ctx->csx.reserve(np)); TRY(ctx->csy.reserve(np)); TRY(ctx->csz.reserve(np));
-	TRY(ctx->isx.reserve(np)); TRY(ctx->isy.reserve(np));
-	TRY(ctx->flatx.reserve(np)); TRY(ctx->flaty.reserve(np));
+	TRY(ctx->pointCsis.reserve(np)); TRY(ctx->pointIsy.reserve(np)); TRY(ctx->pointFlat.reserve(np));
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
-	fb.points.csx = ctx->csx.ptr; fb.points.csy = ctx->csy.ptr; fb.points.csz = ctx->csz.ptr;
-	fb.points.isx = ctx->isx.ptr; fb.points.isy = ctx->isy.ptr;
-	fb.points.flatx = ctx->flatx.ptr; fb.points.flaty = ctx->flaty.ptr;
+	fb.points.csis = ctx->pointCsis.ptr; fb.points.isy = ctx->pointIsy.ptr; fb.points.flat = ctx->pointFlat.ptr;
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	launch_project(params, fb, stream);
 	launch_setup_occlude(params, fb, stream);

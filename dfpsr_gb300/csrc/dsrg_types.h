@@ -54,13 +54,6 @@ struct GivenPoint {
 };
 static_assert(sizeof(GivenPoint) == 40, "GivenPoint layout");
 
-// Projected corner (implementation/render/ProjectedPoint.h:33-49), structure of arrays.
-struct ProjectedPoints {
-	float *csx, *csy, *csz;
-	float *isx, *isy;
-	int64_t *flatx, *flaty;
-};
-
 // Shader variant bits of processTriangle_RgbaMultiply (implementation/render/shader/RgbaMultiply.h:110-173).
 enum ShadeFlags : uint32_t {
 	SHADE_DIFFUSE = 1u,
