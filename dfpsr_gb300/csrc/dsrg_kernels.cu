@@ -1121,10 +1121,12 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		// slots of each record's bound, and the slots are spread evenly over the lanes: a lane finds
 		// its record by a search over the warp's prefix sums, builds the row pair from the record's
 		// two rows and evaluates the reference's running sums at its quad (quad_lanes), so records
-		// of different sizes no longer keep lanes idle.
+		// of different sizes no longer keep lanes idle.  Small records are not culled early: in dense
+		// meshes a tile's small list is walked about once per pixel, and the bound test per record
+		// cost more than it saved (large records keep the culling; a scene of small triangles with
+		// heavy overdraw can send every record down that path with a small bound of 0 x 0).
 		for (uint32_t chunk = smallBegin; chunk < smallEnd; chunk += (uint32_t)THREADS) {
 			const uint32_t e = chunk + (uint32_t)warp + (uint32_t)WARPS * (uint32_t)lane;
-			if (cull) tileMin = warp_tile_threshold(keys, initialDepth, lane, validW, validH, affine);
 			uint32_t ri = 0, rowOffset = 0;
 			int32_t slots = 0, cols = 1, rowStart = 0, colStart = 0, top = 0, colsRecip = 65536;
 			float s0 = 0.0f, dx0 = 0.0f, dy0 = 0.0f;
@@ -1136,12 +1138,11 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				const int32_t bottom = r.bottom;
 				s0 = r.start[0]; dx0 = r.dx[0]; dy0 = r.dy[0];
 				rowOffset = rowOffsets[ri];
-				const bool culled = cull && bound_best_hi(left, top, right, bottom, s0, dx0, dy0, tx0, ty0, affine, false) < tileMin;
 				rowStart = max(top, ty0);
 				const int32_t rowEnd = min(bottom, ty0 + TILE_H);
 				colStart = max(left & ~1, tx0);
 				const int32_t colEnd = min((right + 1) & ~1, tx0 + TILE_W);
-				if (!culled && rowEnd > rowStart && colEnd > colStart) {
+				if (rowEnd > rowStart && colEnd > colStart) {
 					cols = (colEnd - colStart) >> 1;
 					slots = ((rowEnd - rowStart) >> 1) * cols;
 				}
