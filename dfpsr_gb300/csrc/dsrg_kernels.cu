@@ -613,11 +613,12 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_chunk_kernel(const DrawReco
 
 static const int32_t ROWS_STEPPED_MAX = 16; // records of at most this many rows are stepped by one lane each
 
-// The row intervals of short records (a few rows each, as in dense meshes): each warp takes 32
-// records and spreads the concatenation of their rows over its lanes; a lane finds the record of
-// its row by a binary search over the warp's prefix sums of row counts and fetches that record's
-// corners with shuffles.  No search over all records is needed, but a warp's 32 records are one
-// work unit, so tall triangles are drawn by rows_chunk_kernel instead.
+// The row intervals of every record, stepped exactly (row_intervals_stepped: two floor divisions
+// per edge start a segment of rows, then one carry step per edge and row).  Each warp takes 32
+// records.  When all of them have at most ROWS_STEPPED_MAX rows (dense meshes) each lane steps its
+// own record; otherwise the records are cut into segments of up to ROWS_STEPPED_MAX rows that are
+// spread over the lanes (a lane finds its record by a search over the warp's prefix sums of
+// segment counts and fetches its corners with shuffles), so tall triangles keep every lane busy.
 __global__ void __launch_bounds__(256, 3) rows_group_kernel(const DrawRecord *__restrict__ records, uint32_t capacity,
                                                    const uint32_t *countDevice, const uint32_t *__restrict__ rowOffsets,
                                                    uint32_t *rows, uint32_t rowCapacity, int32_t *errorFlag) {
@@ -639,55 +640,54 @@ __global__ void __launch_bounds__(256, 3) rows_group_kernel(const DrawRecord *__
 			count = c.y - top;
 			out = rowOffsets[i];
 		}
-		if (__all_sync(0xFFFFFFFFu, count <= ROWS_STEPPED_MAX)) {
-			// short records: each lane steps through its own record's rows (two divisions per edge
-			// instead of one per edge and row)
-			if (count > 0) {
-				EdgeStepper s[3];
-				const bool degenerate = (f0 == f2 && f1 == f3) || (f2 == f4 && f3 == f5) || (f4 == f0 && f5 == f1);
-				if (!degenerate) {
-					s[0] = edge_stepper(make_edge(f0, f1, f2, f3), top);
-					s[1] = edge_stepper(make_edge(f2, f3, f4, f5), top);
-					s[2] = edge_stepper(make_edge(f4, f5, f0, f1), top);
-				}
-				for (int32_t k = 0; k < count; k++) {
-					int32_t left = R, right = L;
-					if (!degenerate) {
-						left = L; right = R;
-						edge_step(s[0], L, R, left, right);
-						edge_step(s[1], L, R, left, right);
-						edge_step(s[2], L, R, left, right);
-					}
-					const uint32_t at = out + (uint32_t)k;
-					if (at < rowCapacity) rows[at] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
-					else atomicOr(errorFlag, ERROR_ROW_OVERFLOW);
-				}
+		const bool short_ = __all_sync(0xFFFFFFFFu, count <= ROWS_STEPPED_MAX);
+		const int32_t segments = short_ ? 1 : (count + ROWS_STEPPED_MAX - 1) / ROWS_STEPPED_MAX;
+		int32_t inclusive = segments, total = 32;
+		if (!short_) {
+			for (int o = 1; o < 32; o <<= 1) {
+				const int32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
+				if (lane >= o) inclusive += v;
 			}
-			continue;
+			total = __shfl_sync(0xFFFFFFFFu, inclusive, 31);
 		}
-		int32_t inclusive = count;
-		for (int o = 1; o < 32; o <<= 1) {
-			const int32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
-			if (lane >= o) inclusive += v;
-		}
-		const int32_t total = __shfl_sync(0xFFFFFFFFu, inclusive, 31);
 		for (int32_t base = 0; base < total; base += 32) {
+			// this lane's segment: the rows [first, first + rowsHere) of the record held by lane k
+			int32_t x0 = f0, y0 = f1, x1 = f2, y1 = f3, x2 = f4, y2 = f5, kTop = top, kL = L, kR = R, kCount = count;
+			uint32_t kOut = out;
+			int32_t first = 0;
 			const int32_t j = base + lane;
-			int k = 0; // first lane whose inclusive sum exceeds j
-			for (int step = 16; step >= 1; step >>= 1)
-				if (__shfl_sync(0xFFFFFFFFu, inclusive, k + step - 1) <= j) k += step;
-			const int32_t start = __shfl_sync(0xFFFFFFFFu, inclusive, k) - __shfl_sync(0xFFFFFFFFu, count, k);
-			const int32_t kx0 = __shfl_sync(0xFFFFFFFFu, f0, k), ky0 = __shfl_sync(0xFFFFFFFFu, f1, k);
-			const int32_t kx1 = __shfl_sync(0xFFFFFFFFu, f2, k), ky1 = __shfl_sync(0xFFFFFFFFu, f3, k);
-			const int32_t kx2 = __shfl_sync(0xFFFFFFFFu, f4, k), ky2 = __shfl_sync(0xFFFFFFFFu, f5, k);
-			const int32_t kTop = __shfl_sync(0xFFFFFFFFu, top, k), kL = __shfl_sync(0xFFFFFFFFu, L, k);
-			const int32_t kR = __shfl_sync(0xFFFFFFFFu, R, k);
-			const uint32_t kOut = __shfl_sync(0xFFFFFFFFu, out, k);
-			if (j < total) {
-				const int32_t row = j - start;
-				int32_t left, right;
-				row_interval_regs(kx0, ky0, kx1, ky1, kx2, ky2, kTop + row, kL, kR, left, right);
-				const uint32_t at = kOut + (uint32_t)row;
+			if (!short_) {
+				int k = 0; // first lane whose inclusive sum exceeds j
+				for (int step = 16; step >= 1; step >>= 1)
+					if (__shfl_sync(0xFFFFFFFFu, inclusive, k + step - 1) <= j) k += step;
+				const int32_t start = __shfl_sync(0xFFFFFFFFu, inclusive, k) - __shfl_sync(0xFFFFFFFFu, segments, k);
+				x0 = __shfl_sync(0xFFFFFFFFu, f0, k); y0 = __shfl_sync(0xFFFFFFFFu, f1, k);
+				x1 = __shfl_sync(0xFFFFFFFFu, f2, k); y1 = __shfl_sync(0xFFFFFFFFu, f3, k);
+				x2 = __shfl_sync(0xFFFFFFFFu, f4, k); y2 = __shfl_sync(0xFFFFFFFFu, f5, k);
+				kTop = __shfl_sync(0xFFFFFFFFu, top, k); kL = __shfl_sync(0xFFFFFFFFu, L, k);
+				kR = __shfl_sync(0xFFFFFFFFu, R, k); kCount = __shfl_sync(0xFFFFFFFFu, count, k);
+				kOut = __shfl_sync(0xFFFFFFFFu, out, k);
+				first = (j - start) * ROWS_STEPPED_MAX;
+			}
+			if (j >= total) continue;
+			const int32_t rowsHere = min(ROWS_STEPPED_MAX, kCount - first);
+			if (rowsHere <= 0) continue;
+			const bool degenerate = (x0 == x1 && y0 == y1) || (x1 == x2 && y1 == y2) || (x2 == x0 && y2 == y0);
+			EdgeStepper st[3];
+			if (!degenerate) {
+				st[0] = edge_stepper(make_edge(x0, y0, x1, y1), kTop + first);
+				st[1] = edge_stepper(make_edge(x1, y1, x2, y2), kTop + first);
+				st[2] = edge_stepper(make_edge(x2, y2, x0, y0), kTop + first);
+			}
+			for (int32_t r = 0; r < rowsHere; r++) {
+				int32_t left = kR, right = kL;
+				if (!degenerate) {
+					left = kL; right = kR;
+					edge_step(st[0], kL, kR, left, right);
+					edge_step(st[1], kL, kR, left, right);
+					edge_step(st[2], kL, kR, left, right);
+				}
+				const uint32_t at = kOut + (uint32_t)(first + r);
 				if (at < rowCapacity) rows[at] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
 				else atomicOr(errorFlag, ERROR_ROW_OVERFLOW);
 			}
