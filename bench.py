@@ -178,7 +178,7 @@ def batched_section(ctx, args, flush):
                 c.zero_()
                 z.zero_()
 
-    tuning = batch.autotune(rounds=1)
+    tuning = batch.autotune(rounds=3)
     ctx.set_counting(True)
     clear()
     batch.render()

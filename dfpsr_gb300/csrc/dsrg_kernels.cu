@@ -1011,8 +1011,9 @@ __device__ __forceinline__ uint32_t warp_tile_threshold(const unsigned long long
 // steps is the length of the row walk.  The plane's extreme over the pixel centres of the tile
 // and record bounds lies at a corner; widening it by four times that error bound is conservative.
 // Returns 0xFFFFFFFF (never culled) for non-finite planes.
-__device__ __forceinline__ uint32_t bound_best_hi(int32_t left, int32_t top, int32_t right, int32_t bottom, float s, float dx, float dy,
-                                                  int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
+__device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
+	const int32_t left = r.left, top = r.top, right = r.right, bottom = r.bottom;
+	const float s = r.start[0], dx = r.dx[0], dy = r.dy[0];
 	const int32_t xa = max(tx0, left), xb = min(tx0 + TILE_W, right) - 1;
 	const int32_t ya = max(ty0, top), yb = min(ty0 + TILE_H, bottom) - 1;
 	const float fxa = (float)xa + 0.5f, fxb = (float)xb + 0.5f, fya = (float)ya + 0.5f, fyb = (float)yb + 0.5f;
@@ -1028,10 +1029,6 @@ __device__ __forceinline__ uint32_t bound_best_hi(int32_t left, int32_t top, int
 	if (!isfinite(best) || !isfinite(margin)) return 0xFFFFFFFFu;
 	const uint32_t hi = ordered_depth(best);
 	return affine ? ~hi : hi;
-}
-
-__device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t tx0, int32_t ty0, bool affine, bool pixelSteps) {
-	return bound_best_hi(r.left, r.top, r.right, r.bottom, r.start[0], r.dx[0], r.dy[0], tx0, ty0, affine, pixelSteps);
 }
 
 // The winner of one pixel, shaded and written: the reference's running sums of its quad
