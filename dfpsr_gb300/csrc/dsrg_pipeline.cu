@@ -121,9 +121,14 @@ static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &ke
 	cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
 	if (e != cudaSuccess) return e;
 	launches();
+	const cudaError_t launched = cudaGetLastError(); // a launch refused while capturing
 	cudaGraph_t graph = nullptr;
 	e = cudaStreamEndCapture(ctx->stream, &graph);
 	if (e != cudaSuccess) return e;
+	if (launched != cudaSuccess) {
+		cudaGraphDestroy(graph);
+		return launched;
+	}
 	g.launches = launch_count() - before;
 	e = cudaGraphInstantiate(&g.exec, graph, 0);
 	cudaGraphDestroy(graph);
