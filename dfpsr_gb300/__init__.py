@@ -34,6 +34,7 @@ EXPORTED = [
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
     "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
     "dsrg_draw_higher", "dsrg_batch_set_depth_only",
+    "dsrg_dense_model_create", "dsrg_dense_model_destroy", "dsrg_dense_render",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
     "dsrg_renderer_end_debug", "dsrg_renderer_get_images", "dsrg_camera_world_to_screen", "dsrg_renderer_give_triangles",
@@ -159,6 +160,10 @@ def lib():
                                         C.POINTER(PointLight), I, I]
         l.dsrg_light_blend.argtypes = [P, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image)]
         l.dsrg_draw_higher.argtypes = [P, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Sprite), I]
+        l.dsrg_dense_model_create.argtypes = [P, P, I, P, P, I, C.POINTER(P)]
+        l.dsrg_dense_model_destroy.argtypes = [P]
+        l.dsrg_dense_render.argtypes = [P, P, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
+                                        C.c_float, C.c_float, P, I]
         l.dsrg_batch_set_depth_only.argtypes = [P, I]
         _lib = l
     return _lib
@@ -352,6 +357,16 @@ class Context:
         _torch_sync()
         self._check(self._l.dsrg_draw_higher(self.handle, C.byref(hi), C.byref(ai), C.byref(bi), array.array, array.count))
 
+    def dense_render(self, model: "DenseModel", view: "OrthoView", height, diffuse, normal, origin, model_to_world,
+                     high_quality: bool = False):
+        """renderDenseModel: the dense model drawn through the ortho view into device images (height
+        F32, diffuse and normal RGBA) where it is higher; origin is the world origin in target pixels."""
+        hi, di, ni = image_struct(height), image_struct(diffuse), image_struct(normal)
+        t = np.ascontiguousarray(model_to_world, np.float32)
+        _torch_sync()
+        self._check(self._l.dsrg_dense_render(self.handle, model.handle, C.byref(view), C.byref(hi), C.byref(di), C.byref(ni),
+                                              float(origin[0]), float(origin[1]), t.ctypes.data, 1 if high_quality else 0))
+
     def tuning(self) -> dict:
         t = Tuning()
         self._check(self._l.dsrg_context_get_tuning(self.handle, C.byref(t)))
@@ -375,6 +390,32 @@ class Context:
         if resolve is not None:
             t.resolve = resolve
         self._check(self._l.dsrg_context_set_tuning(self.handle, C.byref(t)))
+
+
+class DenseModel:
+    """DenseModel_create: a model's polygons as vertex-coloured triangles with smooth normals."""
+
+    def __init__(self, ctx: Context, positions, polygons, colors):
+        self.ctx = ctx
+        pos = np.ascontiguousarray(positions, np.float32)
+        poly = np.ascontiguousarray(polygons, np.int32)
+        col = np.ascontiguousarray(colors, np.float32)
+        h = C.c_void_p()
+        ctx._check(ctx._l.dsrg_dense_model_create(ctx.handle, pos.ctypes.data, len(pos), poly.ctypes.data, col.ctypes.data, len(poly),
+                                                  C.byref(h)))
+        self.handle = h
+        ctx._adopt(self)
+
+    def destroy(self):
+        if getattr(self, "handle", None) and self.ctx.handle:
+            self.ctx._l.dsrg_dense_model_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 class Texture:

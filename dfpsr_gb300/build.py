@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdsrg.so")
-SOURCES = ["dsrg_kernels.cu", "dsrg_api.cu", "dsrg_noalloc.cu", "dsrg_pipeline.cu", "dsrg_batch.cu", "dsrg_diff.cu", "dsrg_light.cu", "dsrg_sort.cu", "dsrg_occlusion.cu", "dsrg_texture.cu", "dsrg_overlay.cu"]
+SOURCES = ["dsrg_kernels.cu", "dsrg_api.cu", "dsrg_noalloc.cu", "dsrg_pipeline.cu", "dsrg_batch.cu", "dsrg_diff.cu", "dsrg_light.cu", "dsrg_sort.cu", "dsrg_occlusion.cu", "dsrg_texture.cu", "dsrg_overlay.cu", "dsrg_dense.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-Xptxas", "-O3"]

@@ -483,3 +483,35 @@ def occlusion_scene(seed: int = 77, width: int = 320, height: int = 240, props: 
         depth = np.where(near, distance, np.float32(1000.0)).astype(np.float32)
     color = rng.integers(0, 2**32, size=(height, width), dtype=np.uint64).astype(np.uint32)
     return OcclusionScene(cam, wall, panel, field, prop_list, depth, color)
+
+
+@dataclasses.dataclass
+class DenseScene:
+    """A model drawn by the sprite engine's renderDenseModel into height, diffuse and normal images."""
+    positions: np.ndarray        # (N, 3) float32, model space in tiles
+    polygons: np.ndarray         # (P, 4) int32, index 3 is -1 for triangles
+    colors: np.ndarray           # (P, 4, 4) float32 RGBA per corner, in [0, 1]
+    camera_tilt: float
+    pixels_per_tile: int
+    view_index: int
+    origin: tuple                # the world origin in target pixels
+    model_to_world: np.ndarray   # (12,) float32
+    height: np.ndarray           # (H, W) float32 initial height image
+    diffuse: np.ndarray          # (H, W) uint32
+    normal: np.ndarray           # (H, W) uint32
+
+
+def dense_scene(seed: int = 17, width: int = 256, height: int = 192, major: int = 40, minor: int = 16, view_index: int = 0,
+                prefilled: bool = False, pixels_per_tile: int = 48) -> DenseScene:
+    """A vertex-coloured torus (quads) of one tile's radius, rotated and placed at the centre of the
+    image, seen through an ortho view; optionally over a prefilled height and colour image."""
+    rng = np.random.default_rng(seed)
+    t = torus(major_segments=major, minor_segments=minor, major_radius=1.0, minor_radius=0.35)
+    colors = rng.uniform(0.0, 1.0, size=t.colors.shape).astype(np.float32)
+    rot = random_rotation(rng)
+    model = np.concatenate([rng.uniform(-0.3, 0.3, 3), rot.reshape(-1)]).astype(np.float32)
+    h0 = (rng.uniform(-2.0, 1.0, size=(height, width)) if prefilled else np.full((height, width), -1e30)).astype(np.float32)
+    d0 = rng.integers(0, 2**32, size=(height, width), dtype=np.uint64).astype(np.uint32) if prefilled else np.zeros((height, width), np.uint32)
+    n0 = rng.integers(0, 2**32, size=(height, width), dtype=np.uint64).astype(np.uint32) if prefilled else np.zeros((height, width), np.uint32)
+    return DenseScene(t.positions, t.poly_indices, colors, -1.0, pixels_per_tile, view_index, (width * 0.5, height * 0.5), model,
+                      h0, d0, n0)

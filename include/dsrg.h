@@ -361,6 +361,22 @@ int dsrg_light_points(dsrg_context context, const dsrg_ortho_view *view, int32_t
 /* blendLight (lightAPI.cpp:287-323): target (any pack order) = diffuse * light / 128 per channel. */
 int dsrg_light_blend(dsrg_context context, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light);
 
+/* ---- dense models of the sprite engine (SDK/SpriteEngine/spriteAPI.cpp:236-262, 1143-1327) ---- */
+typedef struct dsrg_dense_model_s *dsrg_dense_model;
+/* DenseModel_create: the model's polygons (polygonIndices: polygonCount x 4, index 3 = -1 for a
+ * triangle) as vertex-coloured triangles (colors: polygonCount x 4 corners x RGBA, 1 = full) with
+ * smooth normals.  Host arrays, copied by the call. */
+int dsrg_dense_model_create(dsrg_context context, const float *positions, int32_t pointCount, const int32_t *polygonIndices,
+                            const float *colors, int32_t polygonCount, dsrg_dense_model *out);
+int dsrg_dense_model_destroy(dsrg_dense_model model);
+/* renderDenseModel<highQuality> (spriteAPI.cpp:1244-1327): the model placed by modelToWorld
+ * (position, x, y, z axes, in tiles) drawn through view into device images of one size: height
+ * (F32) where the model is higher, diffuse (vertex colour) and normal (RGBA, normals in normal
+ * space; high quality normalizes them per pixel).  originX/Y: the world origin in target pixels. */
+int dsrg_dense_render(dsrg_context context, dsrg_dense_model model, const dsrg_ortho_view *view, const dsrg_image *height,
+                      const dsrg_image *diffuse, const dsrg_image *normal, float originX, float originY, const float *modelToWorld,
+                      int32_t highQuality);
+
 /* One draw_higher source (F32 height + two RGBA images of the same size, device memory). */
 typedef struct {
 	const float *height;

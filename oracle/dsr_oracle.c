@@ -2133,3 +2133,123 @@ int or_renderer_grid(const or_renderer *r, float *out, int32_t *gridWidth, int32
 		for (int32_t x = 0; x < r->gridWidth; x++) out[(size_t)y * r->gridWidth + x] = grid_read(r, x, y);
 	return r->occluded;
 }
+
+/* ---- dense models of the sprite engine (SDK/SpriteEngine/spriteAPI.cpp:236-262, 1143-1327) ---- */
+
+int32_t or_dense_triangle_count(const int32_t *polygons, int32_t polygonCount) {
+	int32_t n = 0;
+	for (int32_t p = 0; p < polygonCount; p++) n += polygons[p * 4 + 3] < 0 ? 1 : 2;
+	return n;
+}
+
+/* DenseModelImpl::DenseModelImpl (spriteAPI.cpp:1189-1240): smooth normals (each polygon's
+ * normalized sum of its fan triangles' normals added to its points, then normalized per point),
+ * colours times 255, one dense triangle per fan triangle of every polygon in order. */
+void or_dense_model_create(const float *positions, int32_t pointCount, const int32_t *polygons, const float *colors,
+                           int32_t polygonCount, or_dense_triangle *out) {
+	v3 *normals = (v3 *)calloc((size_t)(pointCount > 0 ? pointCount : 1), sizeof(v3));
+	for (int32_t p = 0; p < polygonCount; p++) {
+		const int32_t *idx = polygons + p * 4;
+		const int32_t corners = idx[3] < 0 ? 3 : 4;
+		v3 sum = mk3(0.0f, 0.0f, 0.0f);
+		const v3 a = mk3(positions[idx[0] * 3], positions[idx[0] * 3 + 1], positions[idx[0] * 3 + 2]);
+		for (int32_t t = 0; t < corners - 2; t++) { /* getAverageNormal (spriteAPI.cpp:1160-1171) */
+			const int32_t ib = idx[t + 1], ic = idx[t + 2];
+			const v3 b = mk3(positions[ib * 3], positions[ib * 3 + 1], positions[ib * 3 + 2]);
+			const v3 c = mk3(positions[ic * 3], positions[ic * 3 + 1], positions[ic * 3 + 2]);
+			sum = add3(sum, normalize3(cross3(sub3(b, a), sub3(c, a))));
+		}
+		const v3 n = normalize3(sum);
+		for (int32_t v = 0; v < corners; v++) normals[idx[v]] = add3(normals[idx[v]], n);
+	}
+	for (int32_t i = 0; i < pointCount; i++) normals[i] = normalize3(normals[i]);
+	int32_t t = 0;
+	for (int32_t p = 0; p < polygonCount; p++) {
+		const int32_t *idx = polygons + p * 4;
+		const int32_t corners = idx[3] < 0 ? 3 : 4;
+		for (int32_t vb = 1; vb < corners - 1; vb++) {
+			const int32_t vert[3] = {0, vb, vb + 1};
+			or_dense_triangle *d = &out[t++];
+			for (int32_t k = 0; k < 3; k++) {
+				const float *col = colors + (p * 4 + vert[k]) * 4;
+				const int32_t point = idx[vert[k]];
+				d->color[k][0] = col[0] * 255.0f; d->color[k][1] = col[1] * 255.0f; d->color[k][2] = col[2] * 255.0f;
+				d->pos[k][0] = positions[point * 3]; d->pos[k][1] = positions[point * 3 + 1]; d->pos[k][2] = positions[point * 3 + 2];
+				d->normal[k][0] = normals[point].x; d->normal[k][1] = normals[point].y; d->normal[k][2] = normals[point].z;
+			}
+		}
+	}
+	free(normals);
+}
+
+static inline float dense_min3(float a, float b, float c) { const float m = a < b ? a : b; return m < c ? m : c; } /* base/noSimd.h:134-140 */
+static inline float dense_max3(float a, float b, float c) { const float m = a > b ? a : b; return m > c ? m : c; }
+/* (uint32_t)float of the reference's x86-64 build: a signed 64-bit truncation keeping the low 32 bits. */
+static inline uint32_t dense_u32(float x) { return (uint32_t)(int64_t)x; }
+
+/* renderDenseModel<HIGH_QUALITY> (spriteAPI.cpp:1244-1327) into height, diffuse and normal images
+ * (strides in elements).  The pessimistic bounding-box test only skips models that draw nothing,
+ * so it is left out. */
+void or_dense_render(const or_dense_triangle *triangles, int32_t count, const or_ortho_view *view, float *height,
+                     int32_t heightStride, uint32_t *diffuse, int32_t diffuseStride, uint32_t *normal, int32_t normalStride,
+                     int32_t width, int32_t heightPx, float originX, float originY, const float modelToWorld[12],
+                     int32_t highQuality) {
+	/* combineModelToScreenTransform (spriteAPI.cpp:29-35) with Transform3D's product (Transform3D.h:56-58) */
+	m3 tileToScreen;
+	tileToScreen.x = mk3((float)view->pixelOffsetPerTileX[0], (float)view->pixelOffsetPerTileX[1], 0.0f);
+	tileToScreen.y = mk3(0.0f, (float)(-view->yPixelsPerTile), 1.0f);
+	tileToScreen.z = mk3((float)view->pixelOffsetPerTileZ[0], (float)view->pixelOffsetPerTileZ[1], 0.0f);
+	m3 model;
+	model.x = mk3(modelToWorld[3], modelToWorld[4], modelToWorld[5]);
+	model.y = mk3(modelToWorld[6], modelToWorld[7], modelToWorld[8]);
+	model.z = mk3(modelToWorld[9], modelToWorld[10], modelToWorld[11]);
+	const v3 position = add3(m3_transform(&tileToScreen, mk3(modelToWorld[0], modelToWorld[1], modelToWorld[2])), mk3(originX, originY, 0.0f));
+	const m3 toScreen = m3_mul(&model, &tileToScreen);
+	m3 n, nt; /* transpose(normalToWorldSpace) (FMatrix3x3.h:109-120) */
+	n.x = mk3(view->normalToWorld[0], view->normalToWorld[1], view->normalToWorld[2]);
+	n.y = mk3(view->normalToWorld[3], view->normalToWorld[4], view->normalToWorld[5]);
+	n.z = mk3(view->normalToWorld[6], view->normalToWorld[7], view->normalToWorld[8]);
+	nt.x = mk3(n.x.x, n.y.x, n.z.x); nt.y = mk3(n.x.y, n.y.y, n.z.y); nt.z = mk3(n.x.z, n.y.z, n.z.z);
+	const m3 toNormal = m3_mul(&model, &nt);
+	for (int32_t t = 0; t < count; t++) {
+		const or_dense_triangle *d = &triangles[t];
+		v3 p[3], nn[3];
+		for (int32_t k = 0; k < 3; k++) {
+			p[k] = add3(m3_transform(&toScreen, mk3(d->pos[k][0], d->pos[k][1], d->pos[k][2])), position);
+		}
+		const v3 a = p[0], b = p[1], c = p[2];
+		/* getBackCulledTriangleBound (spriteAPI.cpp:1143-1155), cut to the image (IRect.h:56-66) */
+		if (((c.x - a.x) * (b.y - a.y)) + ((c.y - a.y) * (a.x - b.x)) >= 0.0f) continue;
+		const int32_t left = (int32_t)dense_min3(a.x, b.x, c.x), top = (int32_t)dense_min3(a.y, b.y, c.y);
+		const int32_t right = (int32_t)dense_max3(a.x, b.x, c.x) + 1, bottom = (int32_t)dense_max3(a.y, b.y, c.y) + 1;
+		if (!(left < width && right > 0 && top < heightPx && bottom > 0)) continue;
+		const int32_t x0 = left > 0 ? left : 0, y0 = top > 0 ? top : 0;
+		const int32_t x1 = right < width ? right : width, y1 = bottom < heightPx ? bottom : heightPx;
+		if (x1 <= x0 || y1 <= y0) continue;
+		/* inverse(FMatrix2x2(B - A, C - A)) (FMatrix2x2.h:69-76) */
+		const float mxx = b.x - a.x, mxy = b.y - a.y, myx = c.x - a.x, myy = c.y - a.y;
+		const float invDet = 1.0f / (mxx * myy - mxy * myx);
+		const float ixx = myy * invDet, ixy = -mxy * invDet, iyx = -myx * invDet, iyy = mxx * invDet;
+		for (int32_t k = 0; k < 3; k++) nn[k] = m3_transform(&toNormal, mk3(d->normal[k][0], d->normal[k][1], d->normal[k][2]));
+		for (int32_t y = y0; y < y1; y++) {
+			for (int32_t x = x0; x < x1; x++) {
+				const float ox = ((float)x + 0.5f) - a.x, oy = ((float)y + 0.5f) - a.y;
+				const float wb = ox * ixx + oy * iyx, wc = ox * ixy + oy * iyy;
+				const float wa = 1.0f - (wb + wc);
+				if (!(wa >= -0.00001f && wb >= -0.00001f && wc >= -0.00001f)) continue;
+				const float h = a.z * wa + b.z * wb + c.z * wc; /* interpolateUsingAffineWeight (ITriangle2D.h:58-61) */
+				float *target = &height[(size_t)y * heightStride + x];
+				if (!(h > *target)) continue;
+				*target = h;
+				float col[3], nv[3];
+				for (int32_t ch = 0; ch < 3; ch++) col[ch] = d->color[0][ch] * wa + d->color[1][ch] * wb + d->color[2][ch] * wc;
+				v3 nsum = mk3(nn[0].x * wa + nn[1].x * wb + nn[2].x * wc, nn[0].y * wa + nn[1].y * wb + nn[2].y * wc,
+				              nn[0].z * wa + nn[1].z * wb + nn[2].z * wc);
+				if (highQuality) nsum = normalize3(nsum);
+				nv[0] = (nsum.x + 1.0f) * 127.5f; nv[1] = (nsum.y + 1.0f) * 127.5f; nv[2] = (nsum.z + 1.0f) * 127.5f;
+				diffuse[(size_t)y * diffuseStride + x] = dense_u32(col[0]) | (dense_u32(col[1]) << 8) | (dense_u32(col[2]) << 16) | (255u << 24);
+				normal[(size_t)y * normalStride + x] = dense_u32(nv[0]) | (dense_u32(nv[1]) << 8) | (dense_u32(nv[2]) << 16) | (255u << 24);
+			}
+		}
+	}
+}

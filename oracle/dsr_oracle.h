@@ -144,6 +144,16 @@ void or_draw_higher(float *targetHeight, int32_t thStride, uint32_t *targetA, in
                     int32_t shStride, const uint32_t *sourceA, int32_t saStride, int32_t saPack, const uint32_t *sourceB,
                     int32_t sbStride, int32_t sbPack, int32_t sw, int32_t sh, int32_t left, int32_t top, float offset);
 
+/* ---- dense models of the sprite engine (SDK/SpriteEngine/spriteAPI.cpp:236-262, 1143-1327) ---- */
+typedef struct { float color[3][3]; float pos[3][3]; float normal[3][3]; } or_dense_triangle;
+int32_t or_dense_triangle_count(const int32_t *polygons, int32_t polygonCount);
+void or_dense_model_create(const float *positions, int32_t pointCount, const int32_t *polygons, const float *colors,
+                           int32_t polygonCount, or_dense_triangle *out);
+void or_dense_render(const or_dense_triangle *triangles, int32_t count, const or_ortho_view *view, float *height,
+                     int32_t heightStride, uint32_t *diffuse, int32_t diffuseStride, uint32_t *normal, int32_t normalStride,
+                     int32_t width, int32_t heightPx, float originX, float originY, const float modelToWorld[12],
+                     int32_t highQuality);
+
 #ifdef __cplusplus
 }
 #endif

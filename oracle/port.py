@@ -256,6 +256,10 @@ def _light_lib():
     if not getattr(l, "_light_ready", False):
         P, I, F = C.c_void_p, C.c_int32, C.c_float
         l.or_ortho_view_create.argtypes = [F, I, I, C.POINTER(OrthoView)]
+        l.or_dense_triangle_count.argtypes = [P, I]
+        l.or_dense_triangle_count.restype = I
+        l.or_dense_model_create.argtypes = [P, I, P, P, I, P]
+        l.or_dense_render.argtypes = [P, I, C.POINTER(OrthoView), P, I, P, I, P, I, I, I, F, F, P, I]
         l.or_shadow_side_location.argtypes = [P, I, P]
         l.or_directed_light.argtypes = [C.POINTER(OrthoView), P, I, P, I, I, I, P, F, P, I]
         l.or_point_light_bound.argtypes = [C.POINTER(OrthoView), I, I, I, I, P, F, P]
@@ -429,3 +433,36 @@ def world_to_screen(cam: CameraDesc, world) -> tuple:
     for i in range(len(world)):
         lib().or_world_to_screen(C.byref(cam), _ptr(world[i]), _ptr(out[i]), _ptr(flat[i]))
     return out[:, :3].copy(), out[:, 3:].copy(), flat
+
+
+# ---- dense models of the sprite engine (SDK/SpriteEngine/spriteAPI.cpp:1174-1327)
+
+DENSE_TRIANGLE = np.dtype([("color", np.float32, (3, 3)), ("pos", np.float32, (3, 3)), ("normal", np.float32, (3, 3))])
+
+
+def dense_model(positions, polygons, colors) -> np.ndarray:
+    """DenseModel_create: one dense triangle (colours x 255, corners, smooth normals) per fan triangle."""
+    l = _light_lib()
+    positions = np.ascontiguousarray(positions, np.float32)
+    polygons = np.ascontiguousarray(polygons, np.int32)
+    colors = np.ascontiguousarray(colors, np.float32)
+    n = l.or_dense_triangle_count(polygons.ctypes.data, len(polygons))
+    out = np.zeros(max(n, 1), DENSE_TRIANGLE)
+    l.or_dense_model_create(positions.ctypes.data, len(positions), polygons.ctypes.data, colors.ctypes.data, len(polygons),
+                            out.ctypes.data)
+    return out[:n]
+
+
+def dense_render(triangles, view: OrthoView, height, diffuse, normal, origin, model_to_world, high_quality: bool):
+    """renderDenseModel<high_quality> into copies of the images; returns (height, diffuse, normal)."""
+    l = _light_lib()
+    triangles = np.ascontiguousarray(triangles, DENSE_TRIANGLE)
+    height = np.ascontiguousarray(height, np.float32).copy()
+    diffuse = np.ascontiguousarray(diffuse, np.uint32).copy()
+    normal = np.ascontiguousarray(normal, np.uint32).copy()
+    h, w = height.shape
+    t = np.ascontiguousarray(model_to_world, np.float32)
+    l.or_dense_render(triangles.ctypes.data if len(triangles) else None, len(triangles), C.byref(view), height.ctypes.data, w,
+                      diffuse.ctypes.data, w, normal.ctypes.data, w, w, h, C.c_float(origin[0]), C.c_float(origin[1]),
+                      t.ctypes.data, 1 if high_quality else 0)
+    return height, diffuse, normal

@@ -187,6 +187,7 @@ def _light_lib(variant: str):
         l.refh_point_light.argtypes = [F, I, I, I, I, P, P, P, I, I, P, F, F, P, P, I]
         l.refh_blend_light.argtypes = [P, I, P, P, I, I]
         l.refh_draw_higher.argtypes = [P, P, I, P, I, I, I, P, P, I, P, I, I, I, I, I, F]
+        l.refh_dense_render.argtypes = [P, I, P, P, I, F, I, I, P, P, P, I, I, F, F, P, I]
         l._light_ready = True
     return l
 
@@ -259,6 +260,23 @@ def draw_higher(target, source, left, top, offset, variant: str = "exact"):
     _light_lib(variant).refh_draw_higher(_ptr(th), _ptr(ta), tap, _ptr(tb), tbp, W, H, _ptr(sh), _ptr(sa), sap, _ptr(sb), sbp,
                                          w, h, left, top, offset)
     return th, ta, tb
+
+
+def dense_render(positions, polygons, colors, tilt, pixels_per_tile, view_index, height, diffuse, normal, origin, model_to_world,
+                 high_quality: bool, variant: str = "exact"):
+    """DenseModel_create + renderDenseModel<high_quality> of the reference; returns (height, diffuse, normal)."""
+    positions = np.ascontiguousarray(positions, np.float32)
+    polygons = np.ascontiguousarray(polygons, np.int32)
+    colors = np.ascontiguousarray(colors, np.float32)
+    height = np.ascontiguousarray(height, np.float32).copy()
+    diffuse = np.ascontiguousarray(diffuse, np.uint32).copy()
+    normal = np.ascontiguousarray(normal, np.uint32).copy()
+    t = np.ascontiguousarray(model_to_world, np.float32)
+    h, w = height.shape
+    _light_lib(variant).refh_dense_render(_ptr(positions), len(positions), _ptr(polygons), _ptr(colors), len(polygons), tilt,
+                                          pixels_per_tile, view_index, _ptr(height), _ptr(diffuse), _ptr(normal), w, h,
+                                          origin[0], origin[1], _ptr(t), 1 if high_quality else 0)
+    return height, diffuse, normal
 
 
 def _camera_args(cam):
