@@ -273,6 +273,28 @@ def texture_resizes():
     return out
 
 
+DENSE_CASES = [  # (seed, view index, prefilled, high quality)
+    (60, 0, False, False), (61, 2, True, True), (62, 5, False, True), (63, 7, True, False),
+]
+
+
+def dense_renders():
+    """renderDenseModel of the reference itself on seeded dense scenes: the sha256 of the height,
+    diffuse and normal images it leaves."""
+    from dfpsr_gb300 import scenes
+    from oracle import ref
+    out = []
+    for seed, view_index, prefilled, high_quality in DENSE_CASES:
+        sc = scenes.dense_scene(seed=seed, view_index=view_index, prefilled=prefilled)
+        h, d, n = ref.dense_render(sc.positions, sc.polygons, sc.colors, sc.camera_tilt, sc.pixels_per_tile, sc.view_index,
+                                   sc.height, sc.diffuse, sc.normal, sc.origin, sc.model_to_world, high_quality)
+        out.append(dict(seed=seed, view_index=view_index, prefilled=prefilled, high_quality=high_quality,
+                        inputs=image_digest(np.concatenate([sc.positions.reshape(-1), sc.colors.reshape(-1), sc.model_to_world,
+                                                            sc.height.reshape(-1)]).view(np.uint32)),
+                        height=image_digest(h.view(np.uint32)), diffuse=image_digest(d), normal=image_digest(n)))
+    return out
+
+
 def main():
     reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DFPSR_REFERENCE", "/root/reference")
     from oracle import ref
@@ -290,6 +312,9 @@ def main():
     with open(os.path.join(HERE, "texture_resize.json"), "w") as f:
         json.dump(texture_resizes(), f, indent=1)
     print("wrote texture_resize")
+    with open(os.path.join(HERE, "dense_render.json"), "w") as f:
+        json.dump(dense_renders(), f, indent=1)
+    print("wrote dense_render")
 
 
 if __name__ == "__main__":

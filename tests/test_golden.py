@@ -158,3 +158,25 @@ def test_oracle_texture_resize_matches_reference_fixture(built):
         t = port.OracleTexture(make_golden.texture_resize_image(case["width"], case["height"]), case["resolutions"])
         assert list(t.t.fields()) == case["fields"], case
         assert hashlib.sha256(t.t.array().tobytes()).hexdigest() == case["pyramid"], case
+
+
+def test_oracle_dense_render_matches_reference_fixture(built):
+    """renderDenseModel: the oracle leaves the images the reference left (tests/golden/dense_render.json)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    from dfpsr_gb300 import scenes
+    from oracle import port
+    with open(os.path.join(GOLDEN, "dense_render.json")) as f:
+        cases = json.load(f)
+    assert len(cases) == len(make_golden.DENSE_CASES)
+    for case in cases:
+        sc = scenes.dense_scene(seed=case["seed"], view_index=case["view_index"], prefilled=case["prefilled"])
+        inputs = np.concatenate([sc.positions.reshape(-1), sc.colors.reshape(-1), sc.model_to_world, sc.height.reshape(-1)])
+        assert make_golden.image_digest(inputs.view(np.uint32)) == case["inputs"], "the seeded scene generator changed"
+        view = port.ortho_view(sc.camera_tilt, sc.pixels_per_tile, sc.view_index)
+        h, d, n = port.dense_render(port.dense_model(sc.positions, sc.polygons, sc.colors), view, sc.height, sc.diffuse,
+                                    sc.normal, sc.origin, sc.model_to_world, case["high_quality"])
+        assert make_golden.image_digest(h.view(np.uint32)) == case["height"], case
+        assert make_golden.image_digest(d) == case["diffuse"], case
+        assert make_golden.image_digest(n) == case["normal"], case

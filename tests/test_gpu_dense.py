@@ -96,3 +96,24 @@ def test_dense_model_errors(ctx):
     assert float(h.min()) == -5.0
     model.destroy()
     empty.destroy()
+
+
+def test_dense_render_matches_reference_fixture(ctx):
+    """The GPU leaves the images the reference left (tests/golden/dense_render.json)."""
+    import json
+    import os
+    import sys
+    import dfpsr_gb300 as d
+    from conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_golden
+    with open(os.path.join(ROOT, "tests", "golden", "dense_render.json")) as f:
+        cases = json.load(f)
+    for case in cases:
+        sc = scenes.dense_scene(seed=case["seed"], view_index=case["view_index"], prefilled=case["prefilled"])
+        model = d.DenseModel(ctx, sc.positions, sc.polygons, sc.colors)
+        h, di, n = _gpu(ctx, sc, model, case["high_quality"])
+        assert make_golden.image_digest(h.view(np.uint32)) == case["height"], case
+        assert make_golden.image_digest(di) == case["diffuse"], case
+        assert make_golden.image_digest(n) == case["normal"], case
+        model.destroy()
