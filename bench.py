@@ -406,7 +406,81 @@ def light_section(ctx, args):
               "cpu_oracle": {"frames_per_s": 1.0 / cpu_s, "cores": 1, "kind": "port",
                              "sample": "one frame of the same pass, oracle C restatement, one thread"}}
     gpu.destroy()
+    result["dense_models"] = dense_models_section(ctx)
     return result
+
+
+def dense_models_section(ctx, instances: int = 64):
+    """The sprite world's model instances (drawModel: renderDenseModel, low quality) at 1920x1080:
+    `instances` placements of a 3,200-triangle vertex-coloured torus drawn one after another into
+    the height, diffuse and normal images, timed with CUDA events; the images must equal the
+    oracle's after the whole sequence."""
+    import torch
+    import dfpsr_gb300 as d
+    from dfpsr_gb300 import scenes
+    from oracle import port
+    sc = scenes.dense_scene(seed=77, width=1920, height=1080, major=80, minor=20, pixels_per_tile=64)
+    rng = np.random.default_rng(5)
+    places = [((float(rng.uniform(0, 1920)), float(rng.uniform(0, 1080))),
+               np.concatenate([rng.uniform(-1, 1, 3), scenes.random_rotation(rng).reshape(-1)]).astype(np.float32))
+              for _ in range(instances)]
+    model = d.DenseModel(ctx, sc.positions, sc.polygons, sc.colors)
+    view = d.ortho_view(sc.camera_tilt, sc.pixels_per_tile, sc.view_index)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    h = torch.tensor(sc.height, device="cuda")
+    di = torch.zeros((1080, 1920), dtype=torch.int32, device="cuda")
+    n = torch.zeros_like(di)
+
+    def run():
+        h.copy_(torch.tensor(sc.height, device="cuda"))
+        di.zero_()
+        n.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for origin, transform in places:
+            ctx.dense_render(model, view, h, di, n, origin, transform, False)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    run()
+    ms = statistics.median([run() for _ in range(5)])
+    calls = {"h": h.clone(), "d": di.clone(), "n": n.clone()}
+
+    def run_many():
+        h.copy_(torch.tensor(sc.height, device="cuda"))
+        di.zero_()
+        n.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.dense_render_many([(model, origin, transform) for origin, transform in places], view, h, di, n, False)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    run_many()
+    ms_many = statistics.median([run_many() for _ in range(5)])
+    same_calls = bool(torch.equal(calls["h"], h) and torch.equal(calls["d"], di) and torch.equal(calls["n"], n))
+    tris = port.dense_model(sc.positions, sc.polygons, sc.colors)
+    pv = port.ortho_view(sc.camera_tilt, sc.pixels_per_tile, sc.view_index)
+    rh, rd, rn = sc.height, np.zeros((1080, 1920), np.uint32), np.zeros((1080, 1920), np.uint32)
+    t0 = time.perf_counter()
+    for origin, transform in places:
+        rh, rd, rn = port.dense_render(tris, pv, rh, rd, rn, origin, transform, False)
+    cpu_s = time.perf_counter() - t0
+    same = (np.array_equal(h.cpu().numpy().view(np.uint32), rh.view(np.uint32)) and
+            np.array_equal(di.cpu().numpy().view(np.uint32), rd) and np.array_equal(n.cpu().numpy().view(np.uint32), rn))
+    model.destroy()
+    count = len(tris)
+    return {"workload": f"{instances} instances of a {count}-triangle dense torus at 1920x1080 (renderDenseModel, low quality)",
+            "one_call_per_instance": {"ms_per_sequence": ms, "instances_per_s": instances / (ms / 1e3)},
+            "ms_per_sequence": ms_many, "instances_per_s": instances / (ms_many / 1e3),
+            "triangles_per_s": instances * count / (ms_many / 1e3), "parity_with_oracle": bool(same),
+            "one_call_equals_calls": same_calls,
+            "cpu_oracle": {"instances_per_s": instances / cpu_s, "cores": 1, "kind": "port",
+                           "sample": "the same sequence, oracle C restatement, one thread"}}
 
 
 def cpu_baseline(scene, seconds: float):

@@ -34,7 +34,7 @@ EXPORTED = [
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
     "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
     "dsrg_draw_higher", "dsrg_batch_set_depth_only",
-    "dsrg_dense_model_create", "dsrg_dense_model_destroy", "dsrg_dense_render",
+    "dsrg_dense_model_create", "dsrg_dense_model_destroy", "dsrg_dense_render", "dsrg_dense_render_many",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
     "dsrg_renderer_end_debug", "dsrg_renderer_get_images", "dsrg_camera_world_to_screen", "dsrg_renderer_give_triangles",
@@ -164,6 +164,7 @@ def lib():
         l.dsrg_dense_model_destroy.argtypes = [P]
         l.dsrg_dense_render.argtypes = [P, P, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
                                         C.c_float, C.c_float, P, I]
+        l.dsrg_dense_render_many.argtypes = [P, P, I, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), I]
         l.dsrg_batch_set_depth_only.argtypes = [P, I]
         _lib = l
     return _lib
@@ -367,6 +368,19 @@ class Context:
         self._check(self._l.dsrg_dense_render(self.handle, model.handle, C.byref(view), C.byref(hi), C.byref(di), C.byref(ni),
                                               float(origin[0]), float(origin[1]), t.ctypes.data, 1 if high_quality else 0))
 
+    def dense_render_many(self, instances, view: "OrthoView", height, diffuse, normal, high_quality: bool = False):
+        """instances: (DenseModel, origin, model_to_world) in drawing order, drawn as that many
+        dense_render calls would draw them, in one call."""
+        arr = (DenseInstance * max(len(instances), 1))()
+        for i, (model, origin, transform) in enumerate(instances):
+            arr[i].model = model.handle
+            arr[i].originX, arr[i].originY = float(origin[0]), float(origin[1])
+            arr[i].modelToWorld[:] = [float(v) for v in np.asarray(transform, np.float32).reshape(12)]
+        hi, di, ni = image_struct(height), image_struct(diffuse), image_struct(normal)
+        _torch_sync()
+        self._check(self._l.dsrg_dense_render_many(self.handle, arr, len(instances), C.byref(view), C.byref(hi), C.byref(di),
+                                                   C.byref(ni), 1 if high_quality else 0))
+
     def tuning(self) -> dict:
         t = Tuning()
         self._check(self._l.dsrg_context_get_tuning(self.handle, C.byref(t)))
@@ -390,6 +404,10 @@ class Context:
         if resolve is not None:
             t.resolve = resolve
         self._check(self._l.dsrg_context_set_tuning(self.handle, C.byref(t)))
+
+
+class DenseInstance(C.Structure):
+    _fields_ = [("model", C.c_void_p), ("originX", C.c_float), ("originY", C.c_float), ("modelToWorld", C.c_float * 12)]
 
 
 class DenseModel:

@@ -56,7 +56,7 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	DeviceBuffer<uint32_t> *ubufs[] = {&ctx->triCounts, &ctx->triOffsets, &ctx->scanScratch, &ctx->control, &ctx->binCounts,
 	                                   &ctx->binOffsets, &ctx->binCursors, &ctx->binLists, &ctx->stagingColor};
 	for (auto *b : ubufs) b->release();
-	ctx->records.release(); ctx->tables.release(); ctx->keys.release(); ctx->denseKeys.release();
+	ctx->records.release(); ctx->tables.release(); ctx->keys.release(); ctx->denseKeys.release(); ctx->denseInstances.release();
 	if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
 	if (ctx->pinnedReadback) cudaFreeHost(ctx->pinnedReadback);
 	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();

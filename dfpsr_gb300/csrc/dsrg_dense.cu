@@ -14,6 +14,7 @@
 // so the values are the reference's bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -29,6 +30,7 @@ struct dsrg_dense_model_s {
 	dsrg_context context = nullptr;
 	DeviceBuffer<float> triangles; // DENSE_FLOATS floats per triangle: colours (x 255), corners, normals
 	int32_t count = 0;
+	float minBound[3], maxBound[3]; // over the model's points (the model's bounding box)
 };
 
 namespace {
@@ -60,12 +62,15 @@ inline M3 product(const M3 &left, const M3 &right) {
 	return r;
 }
 
-// The per-call transforms: object to screen (position, axes) and object normals to normal space.
+// The per-call transforms: object to screen (position, axes) and object normals to normal space,
+// and the pixels the model can reach (its bounding box's screen bound, cut to the image), over
+// which the key image is laid out.
 struct DenseView {
 	V3 position;
 	M3 toScreen, toNormal;
 	int32_t width, height;
 	int32_t highQuality;
+	int32_t rx0, ry0, rw, rh;
 };
 
 // (uint32_t)float of the reference's x86-64 build: a signed 64-bit truncation keeping the low 32 bits.
@@ -113,33 +118,63 @@ __device__ __forceinline__ bool dense_weights(const DenseSetup &s, int32_t x, in
 	return wa >= -0.00001f && wb >= -0.00001f && wc >= -0.00001f;
 }
 
-__global__ void dense_keys_kernel(const float *__restrict__ triangles, int32_t count, DenseView v, const float *__restrict__ height,
-                                  int32_t heightStride, unsigned long long *keys) {
-	for (int32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+// One instance of a sequence drawn by one call: its model's triangles, its transforms and bound
+// (in the view), and the sequence number of its first triangle.
+struct DenseInstance {
+	const float *triangles;
+	uint32_t first, count;
+	DenseView v;
+};
+
+// The instance holding sequence number t (instances sorted by first).
+__device__ __forceinline__ uint32_t dense_instance_of(const DenseInstance *instances, uint32_t n, uint32_t t) {
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (instances[mid].first <= t) lo = mid; else hi = mid;
+	}
+	return lo;
+}
+
+// Keys of every instance's triangles (sequence number t = instance first + triangle): the
+// highest height wins, among equal heights the earliest in the sequence, as the reference's
+// strict test keeps it over consecutive calls.  The key image covers the rectangle (kx0, ky0, kw).
+__global__ void dense_keys_kernel(const DenseInstance *__restrict__ instances, uint32_t instanceCount, uint32_t total,
+                                  const float *__restrict__ height, int32_t heightStride, int32_t kx0, int32_t ky0, int32_t kw,
+                                  unsigned long long *keys) {
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+		const DenseInstance &ins = instances[dense_instance_of(instances, instanceCount, t)];
+		const DenseView &v = ins.v;
 		DenseSetup s;
-		if (!dense_setup(triangles + (size_t)t * DENSE_FLOATS, v, s)) continue;
-		for (int32_t y = s.y0; y < s.y1; y++) {
-			for (int32_t x = s.x0; x < s.x1; x++) {
+		if (!dense_setup(ins.triangles + (size_t)(t - ins.first) * DENSE_FLOATS, v, s)) continue;
+		// inside the key image's bound (which holds every triangle bound; the cut only keeps
+		// writes inside the buffer)
+		const int32_t ya = max(s.y0, v.ry0), yb = min(s.y1, v.ry0 + v.rh), xa = max(s.x0, v.rx0), xb = min(s.x1, v.rx0 + v.rw);
+		for (int32_t y = ya; y < yb; y++) {
+			for (int32_t x = xa; x < xb; x++) {
 				float wa, wb, wc;
 				if (!dense_weights(s, x, y, wa, wb, wc)) continue;
 				const float h = s.a.z * wa + s.b.z * wb + s.c.z * wc; // interpolateUsingAffineWeight (ITriangle2D.h:58-61)
 				if (!(h > height[(size_t)y * heightStride + x])) continue;
-				const unsigned long long key = ((unsigned long long)ordered_depth(h) << 32) | (unsigned long long)(~(uint32_t)t);
-				unsigned long long *k = &keys[(size_t)y * v.width + x];
+				const unsigned long long key = ((unsigned long long)ordered_depth(h) << 32) | (unsigned long long)(~t);
+				unsigned long long *k = &keys[(size_t)(y - ky0) * kw + (x - kx0)];
 				if (key > *k) atomicMax(k, key);
 			}
 		}
 	}
 }
 
-__global__ void dense_resolve_kernel(const float *__restrict__ triangles, DenseView v, float *height, int32_t heightStride,
-                                     uint32_t *diffuse, int32_t diffuseStride, uint32_t *normal, int32_t normalStride,
-                                     const unsigned long long *__restrict__ keys) {
-	const int32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-	if (x >= v.width) return;
-	const unsigned long long key = keys[(size_t)y * v.width + x];
+__global__ void dense_resolve_kernel(const DenseInstance *__restrict__ instances, uint32_t instanceCount, float *height,
+                                     int32_t heightStride, uint32_t *diffuse, int32_t diffuseStride, uint32_t *normal,
+                                     int32_t normalStride, int32_t kx0, int32_t ky0, int32_t kw, const unsigned long long *__restrict__ keys) {
+	const int32_t x = kx0 + blockIdx.x * blockDim.x + threadIdx.x, y = ky0 + blockIdx.y;
+	if (x >= kx0 + kw) return;
+	const unsigned long long key = keys[(size_t)(y - ky0) * kw + (x - kx0)];
 	if (key == 0ull) return;
-	const float *t = triangles + (size_t)(~(uint32_t)(key & 0xFFFFFFFFull)) * DENSE_FLOATS;
+	const uint32_t sequence = ~(uint32_t)(key & 0xFFFFFFFFull);
+	const DenseInstance &ins = instances[dense_instance_of(instances, instanceCount, sequence)];
+	const DenseView &v = ins.v;
+	const float *t = ins.triangles + (size_t)(sequence - ins.first) * DENSE_FLOATS;
 	DenseSetup s;
 	dense_setup(t, v, s);
 	float wa, wb, wc;
@@ -198,6 +233,13 @@ int dsrg_dense_model_create(dsrg_context ctx, const float *positions, int32_t po
 		for (int32_t v = 0; v < corners; v++) normals[idx[v]] = add(normals[idx[v]], n);
 	}
 	for (int32_t i = 0; i < pointCount; i++) normals[i] = normalized(normals[i]);
+	float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f};
+	for (int32_t i = 0; i < pointCount; i++)
+		for (int c = 0; c < 3; c++) {
+			const float q = positions[i * 3 + c];
+			if (i == 0 || q < mn[c]) mn[c] = q;
+			if (i == 0 || q > mx[c]) mx[c] = q;
+		}
 	std::vector<float> host((size_t)(count > 0 ? count : 1) * DENSE_FLOATS);
 	size_t at = 0;
 	for (int32_t p = 0; p < polygonCount; p++) {
@@ -219,6 +261,7 @@ int dsrg_dense_model_create(dsrg_context ctx, const float *positions, int32_t po
 	if (!m) return DSRG_ERROR_OUT_OF_MEMORY;
 	m->context = ctx;
 	m->count = count;
+	for (int c = 0; c < 3; c++) { m->minBound[c] = mn[c]; m->maxBound[c] = mx[c]; }
 	cudaSetDevice(ctx->device);
 	cudaError_t e = m->triangles.reserve(host.size());
 	if (e == cudaSuccess) e = cudaMemcpy(m->triangles.ptr, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
@@ -238,16 +281,15 @@ int dsrg_dense_model_destroy(dsrg_dense_model m) {
 	return DSRG_OK;
 }
 
-int dsrg_dense_render(dsrg_context ctx, dsrg_dense_model m, const dsrg_ortho_view *view, const dsrg_image *height,
-                      const dsrg_image *diffuse, const dsrg_image *normal, float originX, float originY, const float *modelToWorld,
-                      int32_t highQuality) {
-	if (!ctx || !m || !view || !modelToWorld) return DSRG_ERROR_INVALID_ARGUMENT;
-	if (!dense_image(height) || !dense_image(diffuse) || !dense_image(normal) || height->width != diffuse->width ||
-	    height->height != diffuse->height || height->width != normal->width || height->height != normal->height)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_dense_render: height, diffuse and normal must be device images of one size");
-	if (m->count == 0) return DSRG_OK;
-	// combineModelToScreenTransform (spriteAPI.cpp:29-35) with the product of Transform3D
-	// (Transform3D.h:56-58): tile to screen from the view's rounded axes (orthoAPI.cpp:9-13)
+} // extern "C"
+
+namespace {
+
+// The transforms and reachable pixels of one instance (combineModelToScreenTransform,
+// spriteAPI.cpp:29-35, with the product of Transform3D, Transform3D.h:56-58; tile to screen from
+// the view's rounded axes, orthoAPI.cpp:9-13).  False when the instance cannot reach the image.
+bool dense_view(const dsrg_dense_model_s *m, const dsrg_ortho_view *view, int32_t width, int32_t height, float originX, float originY,
+                const float *modelToWorld, int32_t highQuality, DenseView &v) {
 	M3 tileToScreen;
 	tileToScreen.x = v3((float)view->pixelOffsetPerTileX[0], (float)view->pixelOffsetPerTileX[1], 0.0f);
 	tileToScreen.y = v3(0.0f, (float)(-view->yPixelsPerTile), 1.0f);
@@ -256,7 +298,6 @@ int dsrg_dense_render(dsrg_context ctx, dsrg_dense_model m, const dsrg_ortho_vie
 	model.x = v3(modelToWorld[3], modelToWorld[4], modelToWorld[5]);
 	model.y = v3(modelToWorld[6], modelToWorld[7], modelToWorld[8]);
 	model.z = v3(modelToWorld[9], modelToWorld[10], modelToWorld[11]);
-	DenseView v;
 	v.position = add(transform(tileToScreen, v3(modelToWorld[0], modelToWorld[1], modelToWorld[2])), v3(originX, originY, 0.0f));
 	v.toScreen = product(model, tileToScreen);
 	const float *n = view->normalToWorld; // transpose(normalToWorldSpace) (FMatrix3x3.h:109-120)
@@ -265,24 +306,109 @@ int dsrg_dense_render(dsrg_context ctx, dsrg_dense_model m, const dsrg_ortho_vie
 	transposed.y = v3(n[1], n[4], n[7]);
 	transposed.z = v3(n[2], n[5], n[8]);
 	v.toNormal = product(model, transposed);
-	v.width = height->width;
-	v.height = height->height;
+	v.width = width;
+	v.height = height;
 	v.highQuality = highQuality ? 1 : 0;
+	// The pixels the model can reach: its bounding box's corners through the same transform
+	// (boundingBoxToRectangle, spriteAPI.cpp:1128-1141), widened by two pixels for the rounding
+	// of points inside the box, cut to the image.  Nothing outside can be drawn, as in the
+	// reference's early test.
+	int64_t bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;
+	for (int k = 0; k < 8; k++) {
+		const V3 corner = v3((k & 1) ? m->maxBound[0] : m->minBound[0], (k & 2) ? m->maxBound[1] : m->minBound[1],
+		                     (k & 4) ? m->maxBound[2] : m->minBound[2]);
+		const V3 s = add(transform(v.toScreen, corner), v.position);
+		if (!(std::isfinite(s.x) && std::isfinite(s.y) && std::fabs(s.x) < 1.0e9f && std::fabs(s.y) < 1.0e9f)) {
+			bx0 = by0 = -2000000000; bx1 = by1 = 2000000000; // no usable bound: the whole image
+			break;
+		}
+		const int64_t px = (int32_t)s.x, py = (int32_t)s.y;
+		if (k == 0 || px < bx0) bx0 = px;
+		if (k == 0 || py < by0) by0 = py;
+		if (k == 0 || px + 1 > bx1) bx1 = px + 1;
+		if (k == 0 || py + 1 > by1) by1 = py + 1;
+	}
+	v.rx0 = (int32_t)std::max<int64_t>(bx0 - 2, 0);
+	v.ry0 = (int32_t)std::max<int64_t>(by0 - 2, 0);
+	const int32_t rx1 = (int32_t)std::min<int64_t>(bx1 + 2, width), ry1 = (int32_t)std::min<int64_t>(by1 + 2, height);
+	if (rx1 <= v.rx0 || ry1 <= v.ry0 || m->count == 0) return false;
+	v.rw = rx1 - v.rx0;
+	v.rh = ry1 - v.ry0;
+	return true;
+}
+
+// Draws the instances as consecutive renderDenseModel calls would, in two launches: keys of every
+// instance's triangles over the union of their bounds, then one resolve over that union.
+int dense_draw(dsrg_context ctx, const dsrg_dense_instance *instances, int32_t count, const dsrg_ortho_view *view, const dsrg_image *height,
+               const dsrg_image *diffuse, const dsrg_image *normal, int32_t highQuality, const char *name) {
+	if (!ctx || !view || count < 0 || (count > 0 && !instances)) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!dense_image(height) || !dense_image(diffuse) || !dense_image(normal) || height->width != diffuse->width ||
+	    height->height != diffuse->height || height->width != normal->width || height->height != normal->height)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, std::string(name) + ": height, diffuse and normal must be device images of one size");
+	std::vector<DenseInstance> table;
+	table.reserve((size_t)count);
+	uint64_t total = 0;
+	int32_t kx0 = 0, ky0 = 0, kx1 = 0, ky1 = 0;
+	for (int32_t i = 0; i < count; i++) {
+		const dsrg_dense_instance &in = instances[i];
+		if (!in.model || in.model->context != ctx) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, std::string(name) + ": invalid model");
+		DenseInstance d;
+		if (!dense_view(in.model, view, height->width, height->height, in.originX, in.originY, in.modelToWorld, highQuality, d.v)) continue;
+		d.triangles = in.model->triangles.ptr;
+		d.first = (uint32_t)total;
+		d.count = (uint32_t)in.model->count;
+		total += (uint64_t)in.model->count;
+		if (total >= 0xFFFFFFFFull) return fail(ctx, DSRG_ERROR_UNSUPPORTED, std::string(name) + ": more than 2^32 - 1 triangles in one call");
+		if (table.empty()) { kx0 = d.v.rx0; ky0 = d.v.ry0; kx1 = d.v.rx0 + d.v.rw; ky1 = d.v.ry0 + d.v.rh; }
+		kx0 = std::min(kx0, d.v.rx0); ky0 = std::min(ky0, d.v.ry0);
+		kx1 = std::max(kx1, d.v.rx0 + d.v.rw); ky1 = std::max(ky1, d.v.ry0 + d.v.rh);
+		table.push_back(d);
+	}
+	if (table.empty()) return DSRG_OK;
+	const int32_t kw = kx1 - kx0, kh = ky1 - ky0;
 	cudaSetDevice(ctx->device);
-	const size_t pixels = (size_t)v.width * v.height;
-	DSRG_CUDA_TRY(ctx, ctx->denseKeys.reserve(pixels));
-	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->denseKeys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
-	const int blocks = (m->count + 127) / 128;
-	dense_keys_kernel<<<blocks, 128, 0, ctx->stream>>>(m->triangles.ptr, m->count, v, (const float *)height->data,
-	                                                   height->strideBytes / 4, ctx->denseKeys.ptr);
-	const dim3 grid((v.width + 127) / 128, v.height);
-	dense_resolve_kernel<<<grid, 128, 0, ctx->stream>>>(m->triangles.ptr, v, (float *)height->data, height->strideBytes / 4,
-	                                                    (uint32_t *)diffuse->data, diffuse->strideBytes / 4, (uint32_t *)normal->data,
-	                                                    normal->strideBytes / 4, ctx->denseKeys.ptr);
+	const size_t tableBytes = table.size() * sizeof(DenseInstance);
+	DSRG_CUDA_TRY(ctx, ctx->denseInstances.reserve(tableBytes));
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->denseInstances.ptr, table.data(), tableBytes, cudaMemcpyHostToDevice, ctx->stream));
+	const DenseInstance *deviceTable = reinterpret_cast<const DenseInstance *>(ctx->denseInstances.ptr);
+	DSRG_CUDA_TRY(ctx, ctx->denseKeys.reserve((size_t)kw * kh));
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->denseKeys.ptr, 0, (size_t)kw * kh * sizeof(unsigned long long), ctx->stream));
+	const uint64_t blocks64 = (total + 127) / 128;
+	const int blocks = (int)std::min<uint64_t>(blocks64, (uint64_t)sm_count() * 64);
+	dense_keys_kernel<<<blocks, 128, 0, ctx->stream>>>(deviceTable, (uint32_t)table.size(), (uint32_t)total,
+	                                                   (const float *)height->data, height->strideBytes / 4, kx0, ky0, kw,
+	                                                   ctx->denseKeys.ptr);
+	const dim3 grid((kw + 127) / 128, kh);
+	dense_resolve_kernel<<<grid, 128, 0, ctx->stream>>>(deviceTable, (uint32_t)table.size(), (float *)height->data,
+	                                                    height->strideBytes / 4, (uint32_t *)diffuse->data, diffuse->strideBytes / 4,
+	                                                    (uint32_t *)normal->data, normal->strideBytes / 4, kx0, ky0, kw,
+	                                                    ctx->denseKeys.ptr);
 	add_launches(2);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	// the table's copy reads the host vector: wait before it goes
 	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
 	return DSRG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int dsrg_dense_render(dsrg_context ctx, dsrg_dense_model m, const dsrg_ortho_view *view, const dsrg_image *height,
+                      const dsrg_image *diffuse, const dsrg_image *normal, float originX, float originY, const float *modelToWorld,
+                      int32_t highQuality) {
+	if (!ctx || !m || !view || !modelToWorld) return DSRG_ERROR_INVALID_ARGUMENT;
+	dsrg_dense_instance instance;
+	instance.model = m;
+	instance.originX = originX;
+	instance.originY = originY;
+	memcpy(instance.modelToWorld, modelToWorld, sizeof(instance.modelToWorld));
+	return dense_draw(ctx, &instance, 1, view, height, diffuse, normal, highQuality, "dsrg_dense_render");
+}
+
+int dsrg_dense_render_many(dsrg_context ctx, const dsrg_dense_instance *instances, int32_t count, const dsrg_ortho_view *view,
+                           const dsrg_image *height, const dsrg_image *diffuse, const dsrg_image *normal, int32_t highQuality) {
+	return dense_draw(ctx, instances, count, view, height, diffuse, normal, highQuality, "dsrg_dense_render_many");
 }
 
 } // extern "C"

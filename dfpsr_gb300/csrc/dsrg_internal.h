@@ -171,6 +171,7 @@ struct dsrg_context_s {
 	DeviceBuffer<longlong2> pointFlat;
 	DeviceBuffer<uint32_t> triCounts, triOffsets, scanScratch;
 	DeviceBuffer<unsigned long long> denseKeys; // per-pixel winners of dsrg_dense_render
+	DeviceBuffer<unsigned char> denseInstances; // the instance table of one dense-model call
 	DeviceBuffer<DrawRecord> records;
 	DeviceBuffer<unsigned char> tables;  // the batch's task, frame and texture tables
 	unsigned char *pinnedTables = nullptr; // host staging of the tables (page-locked)

@@ -376,6 +376,16 @@ int dsrg_dense_model_destroy(dsrg_dense_model model);
 int dsrg_dense_render(dsrg_context context, dsrg_dense_model model, const dsrg_ortho_view *view, const dsrg_image *height,
                       const dsrg_image *diffuse, const dsrg_image *normal, float originX, float originY, const float *modelToWorld,
                       int32_t highQuality);
+/* One model instance of the sprite world (drawModel, spriteAPI.cpp:325-327). */
+typedef struct {
+	dsrg_dense_model model;
+	float originX, originY;
+	float modelToWorld[12];
+} dsrg_dense_instance;
+/* dsrg_dense_render of every instance in order, with the same result as that many calls, in one
+ * pair of launches (heights compete across the instances; among equal heights the earlier wins). */
+int dsrg_dense_render_many(dsrg_context context, const dsrg_dense_instance *instances, int32_t count, const dsrg_ortho_view *view,
+                           const dsrg_image *height, const dsrg_image *diffuse, const dsrg_image *normal, int32_t highQuality);
 
 /* One draw_higher source (F32 height + two RGBA images of the same size, device memory). */
 typedef struct {

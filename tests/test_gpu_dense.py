@@ -117,3 +117,38 @@ def test_dense_render_matches_reference_fixture(ctx):
         assert make_golden.image_digest(di) == case["diffuse"], case
         assert make_golden.image_digest(n) == case["normal"], case
         model.destroy()
+
+
+@pytest.mark.parametrize("high_quality", [False, True])
+def test_dense_render_many_equals_calls_in_sequence(ctx, high_quality):
+    """One call for a sequence of instances of two models (some overlapping, some crossing the
+    edges, one outside) leaves what the same instances drawn one call after another leave, and
+    what the oracle leaves."""
+    import torch
+    import dfpsr_gb300 as d
+    from oracle import port
+    a = scenes.dense_scene(seed=71, width=300, height=220, prefilled=True)
+    b = scenes.dense_scene(seed=72, width=300, height=220, major=12, minor=6)
+    models = [(d.DenseModel(ctx, s.positions, s.polygons, s.colors), port.dense_model(s.positions, s.polygons, s.colors)) for s in (a, b)]
+    rng = np.random.default_rng(9)
+    instances = []
+    for k in range(10):
+        origin = (float(rng.uniform(-30, 330)), float(rng.uniform(-30, 250))) if k != 7 else (5000.0, 5000.0)
+        transform = np.concatenate([rng.uniform(-0.5, 0.5, 3), scenes.random_rotation(rng).reshape(-1)]).astype(np.float32)
+        instances.append((k % 2, origin, transform))
+    view = d.ortho_view(a.camera_tilt, a.pixels_per_tile, a.view_index)
+    dev = lambda arr, dt: torch.tensor(np.ascontiguousarray(arr).view(dt), device="cuda")
+    h, di, n = dev(a.height, np.float32), dev(a.diffuse, np.int32), dev(a.normal, np.int32)
+    ctx.dense_render_many([(models[m][0], o, t) for m, o, t in instances], view, h, di, n, high_quality)
+    got = (h.cpu().numpy(), di.cpu().numpy().view(np.uint32), n.cpu().numpy().view(np.uint32))
+    h2, d2, n2 = dev(a.height, np.float32), dev(a.diffuse, np.int32), dev(a.normal, np.int32)
+    for m, o, t in instances:
+        ctx.dense_render(models[m][0], view, h2, d2, n2, o, t, high_quality)
+    seq = (h2.cpu().numpy(), d2.cpu().numpy().view(np.uint32), n2.cpu().numpy().view(np.uint32))
+    rh, rd, rn = a.height, a.diffuse, a.normal
+    for m, o, t in instances:
+        rh, rd, rn = _oracle(a, models[m][1], high_quality, rh, rd, rn, o, t)
+    _same(got, (rh, rd, rn), "many vs oracle")
+    _same(seq, (rh, rd, rn), "calls vs oracle")
+    for m, _ in models:
+        m.destroy()
