@@ -270,9 +270,9 @@ typedef struct {
 } dsrg_tuning;
 int dsrg_context_get_tuning(dsrg_context context, dsrg_tuning *out);
 int dsrg_context_set_tuning(dsrg_context context, const dsrg_tuning *tuning);
-/* Renders the batch once per candidate configuration (rounds times each), keeps the fastest
- * for the context and returns it in *best (may be null).  The images end up holding the batch's
- * rendered frames. */
+/* Renders the batch once per candidate configuration (rounds times each, each timed render
+ * starting from a cold L2 cache), keeps the fastest for the context and returns it in *best (may
+ * be null).  The images end up holding the batch's rendered frames. */
 int dsrg_batch_autotune(dsrg_batch batch, int32_t rounds, dsrg_tuning *best);
 
 /* ---- differentiable rendering; no counterpart in the reference.
