@@ -49,12 +49,14 @@ def parse_args():
     p.add_argument("--batch-frames", type=int, default=256, help="frames of the mixed-size batch (0 skips it)")
     p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
     p.add_argument("--light-sprites", type=int, default=4096, help="sprites of the deferred-light pass (0 skips it)")
+    p.add_argument("--c0", type=int, default=1, help="also measure the 800x600 random-triangle workload (0 skips it)")
     p.add_argument("--tuning", default="auto",
                    help="tile kernel launch shape THREADSxCTAS_PER_SMxSMALL_ROWSxSMALL_WIDTH[xRESOLVE] (e.g. 128x8x8x16x1), or auto")
     return p.parse_args()
 
 
-def workload(name):
+def workload(name, world: int = 1):
+    """The scene of a plain workload and its config, the same for both arms of the benchmark."""
     from dfpsr_gb300 import scenes
     if name == "terrain":
         s = scenes.terrain(seed=1234)
@@ -65,6 +67,8 @@ def workload(name):
         s = scenes.random_triangles(seed=1234)
         cfg = {"workload": "800x600, 20,000 random triangles, 256x256 RGBA8 texture with mips, vertex colour x texture, "
                            "depth tested", "width": 800, "height": 600, "triangles": s.triangle_count, "seed": 1234}
+    cfg["l2"] = "flushed before every GPU frame (256 MB write)"
+    cfg["parallelism"] = f"replicas ({world} GPUs)" if world > 1 else "single GPU"
     return s, cfg
 
 
@@ -506,7 +510,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    scene, cfg = workload(args.workload)
+    scene, cfg = workload(args.workload, int(os.environ.get("WORLD_SIZE", "1")))
     from oracle import port, ref
     threads = os.cpu_count() or 1
     use_ref = ref.available("shipped")
@@ -541,36 +545,23 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "Mfrag/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     sys.stderr.flush()
-    # The reference library's own heap bookkeeping reports spuriously when Python tears it down.
-    os._exit(0)
+    if use_ref:
+        # the reference library's own heap bookkeeping reports spuriously when Python tears it down
+        os._exit(0)
 
 
-def main():
-    args = parse_args()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+def plain_record(ctx, scene, cfg, args, flush, dist, world, local, workload_key, with_cpu):
+    """One plain workload through dsrg_model_render: fragments/s with the targets in HBM (CUDA
+    events on the renderer's stream, L2 flushed before every frame), the same end to end with
+    page-locked host images, the tile pass's roofline and the CPU baseline."""
     import torch
     import dfpsr_gb300 as d
     from dfpsr_gb300 import replicas
-
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-
-    scene, cfg = workload(args.workload)
     h, w = scene.height, scene.width
-    ctx = d.Context(local)
     model = d.Model(ctx, scene)
     stream = torch.cuda.ExternalStream(ctx.stream)
     color = torch.zeros((h, w), dtype=torch.int32, device="cuda")
     depth = torch.zeros((h, w), dtype=torch.float32, device="cuda")
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB of L2
 
     # the tile kernel's launch shape for this workload, chosen by the library's autotuner on a
     # one-frame batch of it (the plain path below uses the context's tuning)
@@ -586,7 +577,7 @@ def main():
                        resolve=fields[4] if len(fields) > 4 else 0)
         tuning = ctx.tuning()
 
-    # fragments per frame: deterministic, counted once by the kernels themselves
+    # fragments per frame before the depth test: deterministic, counted once by the kernels themselves
     ctx.set_counting(True)
     ctx.render(model, model.camera, color, depth)
     frame_stats = ctx.stats()
@@ -614,10 +605,13 @@ def main():
     with ClockSampler(local) as clocks:
         clocks.wait_first()
         launches0 = ctx.stats()["kernel_launches"]
+        walked0 = ctx.walked_fragments()
         for _ in range(args.steps):
             events.append(frame_device())
             raster_ms.append(ctx.stats()["raster_milliseconds"])
         torch.cuda.synchronize()
+        # fragments the timed frames depth-tested (early culling on): the work actually walked
+        walked = (ctx.walked_fragments() - walked0) / args.steps
         launches = ctx.stats()["kernel_launches"] - launches0
         # the timed region can be shorter than the sampling period: keep the same load (untimed)
         # until a few samples under load exist
@@ -643,55 +637,120 @@ def main():
         ctx.render(model, model.camera, host_color, host_depth)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = replicas.max_over_ranks(sum(e2e_times), dist)
+    model.destroy()
+
+    peaks, peak_kind = measured_peaks()
+    raster_avg_s = (sum(raster_ms) / len(raster_ms)) / 1e3
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = BYTES_PER_FRAGMENT * walked / raster_avg_s / 1e9
+    achieved_counted = BYTES_PER_FRAGMENT * fragments / raster_avg_s / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get(workload_key)
+    except Exception:
+        pass
+    rec = {
+        "value": world * fragments * args.steps / total_s / 1e6, "unit": "Mfrag/s",
+        "ms_per_step": total_s * 1e3 / args.steps,
+        "frames_per_s": world * args.steps / total_s,
+        "fragments_per_frame": fragments,
+        "walked_fragments_per_frame": walked,
+        "frame_stats": {"draw_records": frame_stats["draw_records"], "bin_entries": frame_stats["bin_entries"]},
+        "e2e": {"value": world * fragments * args.steps / e2e_s / 1e6, "unit": "Mfrag/s",
+                "h2d_bytes_per_step": int(host_depth.nbytes),
+                "d2h_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
+                "frames_per_s": world * args.steps / e2e_s,
+                "transfer": "in place: the tile pass reads the host depth image and writes the host colour and "
+                            "depth images through their device addresses (page-locked memory over NVLink-C2C)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "raster_kernel (tile pass with the fused resolve)",
+                     "kernel_ms": raster_avg_s * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * walked,
+                     "model": "28 B per walked fragment (depth read + depth write + colour write + 4 RGBA8 texels); walked = "
+                              "fragments the timed frames depth-tested, after early depth culling",
+                     "pre_depth_test": {"achieved": achieved_counted, "frac": achieved_counted / peak,
+                                        "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments,
+                                        "note": "28 B per fragment counted before the depth test (the metric's unit); early "
+                                                "culling never walks most of them on high-overdraw scenes, so this can exceed 1"}},
+        "gpu_launches": launches,
+        "tuning": tuning,
+        "clocks": clocks.summary(),
+    }
+    if with_cpu:
+        rec["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+    return rec
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import dfpsr_gb300 as d
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    scene, cfg = workload(args.workload, world)
+    ctx = d.Context(local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB of L2
+    head = plain_record(ctx, scene, cfg, args, flush, dist, world, local, args.workload, with_cpu=(world == 1))
 
     if rank == 0:
-        peaks, peak_kind = measured_peaks()
-        raster_avg_s = (sum(raster_ms) / len(raster_ms)) / 1e3
-        achieved = BYTES_PER_FRAGMENT * fragments / raster_avg_s / 1e9
-        peak = float(peaks.get("hbm_gbs", 6800.0))
-        traffic = None
-        try:
-            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-                traffic = json.load(f).get(args.workload)
-        except Exception:
-            pass
-        value = world * fragments * args.steps / total_s / 1e6
-        line = {
-            "metric": METRIC, "value": value, "unit": "Mfrag/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+int64", "data": "synthetic (seeded)",
-            "config": dict(cfg, l2="flushed before every frame (256 MB write)", parallelism="replicas" if world > 1 else "single GPU"),
-            "frames_per_s": world * args.steps / total_s,
-            "fragments_per_frame": fragments,
-            "frame_stats": {"draw_records": frame_stats["draw_records"], "bin_entries": frame_stats["bin_entries"]},
-            "e2e": {"value": world * fragments * args.steps / e2e_s / 1e6, "unit": "Mfrag/s",
-                    "h2d_bytes_per_step": int(host_depth.nbytes),
-                    "d2h_bytes_per_step": int(host_color.nbytes + host_depth.nbytes),
-                    "frames_per_s": world * args.steps / e2e_s,
-                    "transfer": "in place: the tile pass reads the host depth image and writes the host colour and "
-                                "depth images through their device addresses (page-locked memory over NVLink-C2C)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": traffic, "kernel": "raster_kernel + resolve_kernel",
-                         "kernel_ms": raster_avg_s * 1e3, "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments,
-                         "model": "28 B per fragment (depth read + depth write + colour write + 4 RGBA8 texels), every "
-                                  "fragment counted before the depth test; the tile kernel's early depth culling skips "
-                                  "fragments that cannot win, so frac can exceed 1 on high-overdraw scenes"},
-            "gpu_launches": launches,
-            "tuning": tuning,
-            "clocks": clocks.summary(),
-        }
+        line = {"metric": METRIC, "value": head["value"], "unit": "Mfrag/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32+int64", "data": "synthetic (seeded)",
+                "config": cfg}
+        line.update({k: v for k, v in head.items() if k not in ("value", "unit", "ms_per_step")})
+        other = "random" if args.workload == "terrain" else None
+        if other and args.c0:
+            c0_scene, c0_cfg = workload(other)
+            sub = plain_record(ctx, c0_scene, c0_cfg, args, flush, None, 1, local, other, with_cpu=True)
+            line["c0"] = dict(config=c0_cfg, **sub)
         if args.batch_frames > 0:
             line["batch"] = batched_section(ctx, args, flush)
         if args.diff_views > 0:
             line["differentiable"] = diff_section(ctx, args)
         if args.light_sprites > 0:
             line["deferred_light"] = light_section(ctx, args)
-        if world == 1:
-            line["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def summary(line):
+    """The headline figures of every section in one short object, last on the line."""
+    out = {f"{line['config']['workload'].split(',')[0]} frames/s": line["frames_per_s"],
+           "e2e frames/s": line["e2e"]["frames_per_s"], "roofline frac (walked)": line["roofline"]["frac"],
+           "cpu_baseline frames/s": line.get("cpu_baseline", {}).get("frames_per_s")}
+    if "c0" in line:
+        c0 = line["c0"]
+        out.update({"c0 800x600 random 20k frames/s": c0["frames_per_s"], "c0 e2e frames/s": c0["e2e"]["frames_per_s"],
+                    "c0 Mfrag/s": c0["value"], "c0 walked fragments/frame": c0["walked_fragments_per_frame"],
+                    "c0 roofline frac (walked)": c0["roofline"]["frac"],
+                    "c0 cpu_baseline frames/s": c0.get("cpu_baseline", {}).get("frames_per_s")})
+    if "batch" in line:
+        b = line["batch"]
+        out.update({"batch batched frames/s": b["batched"]["frames_per_s"], "batch plain frames/s": b["plain"]["frames_per_s"],
+                    "batch batched_over_plain": b["batched_over_plain"], "batch e2e frames/s": b["e2e"]["frames_per_s"]})
+    if "differentiable" in line:
+        df = line["differentiable"]
+        out.update({"diff views/s atomic": df["atomic"]["views_per_s"],
+                    "diff views/s deterministic": df["deterministic"]["views_per_s"],
+                    "diff grad_rel_err_max": df["grad_rel_err_max"]})
+    if "deferred_light" in line:
+        dl = line["deferred_light"]
+        out.update({"deferred light ms/frame": dl["ms_per_frame"], "deferred light parity": dl["parity_with_oracle"]})
+    return out
 
 
 if __name__ == "__main__":

@@ -23,9 +23,9 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "OUT_OF_MEMORY", 4
 # Every entry point declared in include/dsrg.h.
 EXPORTED = [
     "dsrg_context_create", "dsrg_context_destroy", "dsrg_context_last_error", "dsrg_context_stream",
-    "dsrg_context_set_counting", "dsrg_context_get_stats",
-    "dsrg_texture_create", "dsrg_texture_destroy", "dsrg_texture_read", "dsrg_texture_create_many",
-    "dsrg_model_create", "dsrg_model_destroy",
+    "dsrg_context_set_counting", "dsrg_context_get_stats", "dsrg_context_walked_fragments", "dsrg_debug_fail_allocation",
+    "dsrg_texture_create", "dsrg_texture_destroy", "dsrg_texture_read", "dsrg_texture_create_many", "dsrg_texture_upload",
+    "dsrg_model_create", "dsrg_model_destroy", "dsrg_model_set_bound",
     "dsrg_model_render", "dsrg_model_render_depth",
     "dsrg_renderer_create", "dsrg_renderer_destroy", "dsrg_renderer_begin", "dsrg_renderer_give_task",
     "dsrg_renderer_end", "dsrg_renderer_takes_triangles", "dsrg_model_render_depth_noalloc",
@@ -45,6 +45,7 @@ class DsrgError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
         self.status = status
+        self.message = message
 
 
 class Camera(C.Structure):
@@ -92,7 +93,7 @@ class Sprite(C.Structure):
     _fields_ = [("height", C.c_void_p), ("colorA", C.c_void_p), ("colorB", C.c_void_p), ("width", C.c_int32),
                 ("height_", C.c_int32), ("heightStrideBytes", C.c_int32), ("colorAStrideBytes", C.c_int32),
                 ("colorBStrideBytes", C.c_int32), ("colorAPackOrder", C.c_int32), ("colorBPackOrder", C.c_int32),
-                ("left", C.c_int32), ("top", C.c_int32), ("offset", C.c_float)]
+                ("left", C.c_int32), ("top", C.c_int32), ("offset", C.c_float), ("onDevice", C.c_int32)]
 
 
 _lib = None
@@ -114,6 +115,8 @@ def lib():
         l.dsrg_context_stream.restype = P
         l.dsrg_context_set_counting.argtypes = [P, I, P]
         l.dsrg_context_get_stats.argtypes = [P, C.POINTER(Stats)]
+        l.dsrg_context_walked_fragments.argtypes = [P, C.POINTER(C.c_uint64)]
+        l.dsrg_debug_fail_allocation.argtypes = [C.c_int64]
         l.dsrg_texture_create.argtypes = [P, P, I, I, I, C.POINTER(P)]
         l.dsrg_texture_destroy.argtypes = [P]
         l.dsrg_texture_read.argtypes = [P, P, I, P, C.POINTER(I)]
@@ -189,6 +192,11 @@ def _ptr(a) -> Optional[int]:
     if isinstance(a, np.ndarray):
         return a.ctypes.data
     return int(a.data_ptr())  # torch tensor
+
+
+def _row_bytes(a) -> int:
+    """Row stride in bytes of a 2-D numpy array or torch tensor of 4-byte pixels."""
+    return int(a.strides[0]) if isinstance(a, np.ndarray) else int(a.stride(0)) * 4
 
 
 def camera_struct(scene) -> Camera:
@@ -291,6 +299,12 @@ class Context:
     def set_counting(self, on: bool, coverage=None):
         self._check(self._l.dsrg_context_set_counting(self.handle, 1 if on else 0, _ptr(coverage)))
 
+    def walked_fragments(self) -> int:
+        """Fragments the tile kernels depth-tested on this context so far (early culling skips the rest)."""
+        v = C.c_uint64()
+        self._check(self._l.dsrg_context_walked_fragments(self.handle, C.byref(v)))
+        return int(v.value)
+
     def stats(self) -> dict:
         s = Stats()
         self._check(self._l.dsrg_context_get_stats(self.handle, C.byref(s)))
@@ -318,7 +332,7 @@ class Context:
     def batch(self) -> "Batch":
         return Batch(self)
 
-    # ---- deferred light passes and draw_higher (device images: torch tensors)
+    # ---- deferred light passes and draw_higher (torch CUDA tensors, or numpy arrays in host memory)
 
     def light_directed(self, view: "OrthoView", light, normal, direction, intensity: float, color, add: bool):
         d = np.asarray(direction, np.float32)
@@ -329,7 +343,7 @@ class Context:
                                                 C.c_float(intensity), c.ctypes.data, 1 if add else 0))
 
     def light_points(self, view: "OrthoView", center, light, normal, height, lights, reference_threads: int = 0):
-        """lights: dicts with position, radius, intensity, color and optionally cube (device tensor cubeWidth*6 x cubeWidth)."""
+        """lights: dicts with position, radius, intensity, color and optionally cube (cubeWidth*6 x cubeWidth floats)."""
         arr = (PointLight * max(1, len(lights)))()
         for i, l in enumerate(lights):
             for k in range(3):
@@ -448,9 +462,10 @@ class Texture:
         ctx._adopt(self)
 
     @staticmethod
-    def create_many(ctx: Context, images, resolutions) -> list:
+    def create_many(ctx: Context, images, resolutions, pack_orders=None) -> list:
         """dsrg_texture_create_many: images are (height, width) uint32 numpy arrays (host) or int32
-        torch tensors (device); resolutions an int or one per image."""
+        torch tensors (device); resolutions an int or one per image; pack_orders None (RGBA) or one
+        per image."""
         n = len(images)
         res = [int(resolutions)] * n if np.isscalar(resolutions) else [int(r) for r in resolutions]
         structs = (Image * n)()
@@ -459,7 +474,7 @@ class Texture:
             if not hasattr(im, "data_ptr"):
                 im = np.ascontiguousarray(im, np.uint32)
             keep.append(im)
-            structs[i] = image_struct(im, 0)
+            structs[i] = image_struct(im, 0 if pack_orders is None else int(pack_orders[i]))
         r = np.array(res, np.int32)
         out = (C.c_void_p * n)()
         _torch_sync()
@@ -631,13 +646,14 @@ class SpriteArray:
             a.colorA = _ptr(sp["color_a"])
             a.colorB = _ptr(sp["color_b"])
             a.height_, a.width = int(h.shape[0]), int(h.shape[1])
-            a.heightStrideBytes = int(h.stride(0)) * 4
-            a.colorAStrideBytes = int(sp["color_a"].stride(0)) * 4
-            a.colorBStrideBytes = int(sp["color_b"].stride(0)) * 4
+            a.heightStrideBytes = _row_bytes(h)
+            a.colorAStrideBytes = _row_bytes(sp["color_a"])
+            a.colorBStrideBytes = _row_bytes(sp["color_b"])
             a.colorAPackOrder = int(sp.get("a_pack", 0))
             a.colorBPackOrder = int(sp.get("b_pack", 0))
             a.left, a.top = int(sp["left"]), int(sp["top"])
             a.offset = float(sp["offset"])
+            a.onDevice = 0 if isinstance(h, np.ndarray) else 1
             self._keep.append((h, sp["color_a"], sp["color_b"]))
 
 

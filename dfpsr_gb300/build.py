@@ -78,6 +78,25 @@ def build_hostcheck(force: bool = False) -> str:
     return HOSTCHECK_LIB
 
 
+SHIM_DIR = os.path.join(HERE, "dsr")
+
+
+def build_shim(reference_source: str, out_dir: str = BUILD) -> str:
+    """Compiles the dsr::gpu shim (dsr/dsr_gpu.cpp) against the reference's headers, as a program
+    using the reference links it: reference_source is the reference's Source/ directory.  Returns
+    the object file; link it with the reference's library and libdsrg.so."""
+    os.makedirs(out_dir, exist_ok=True)
+    src = os.path.join(SHIM_DIR, "dsr_gpu.cpp")
+    obj = os.path.join(out_dir, "dsr_gpu.o")
+    deps = [src, os.path.join(SHIM_DIR, "dsr_gpu.h"), os.path.join(os.path.dirname(HERE), "include", "dsrg.h")]
+    if _stale(obj, deps):
+        cxx = os.environ.get("CXX", "g++")
+        # the reference's own release flags (C++14, NDEBUG); no contraction, like the rest of the path
+        subprocess.check_call([cxx, "-std=c++14", "-O2", "-DNDEBUG", "-ffp-contract=off", "-fPIC", "-I", reference_source,
+                               "-I", os.path.join(os.path.dirname(HERE), "include"), "-c", src, "-o", obj])
+    return obj
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
     build_hostcheck(force="--force" in sys.argv)

@@ -2,6 +2,8 @@
 // around the kernels in dsrg_kernels.cu.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,7 +19,33 @@ using namespace dsrg;
 
 #define CUDA_TRY(ctx, expr) DSRG_CUDA_TRY(ctx, expr)
 
+namespace dsrg {
+
+// Allocations left before the one that fails (dsrg_debug_fail_allocation); negative: none fails.
+static std::atomic<int64_t> g_failAllocation(-1);
+
+cudaError_t device_alloc(void **p, size_t bytes) {
+	int64_t left = g_failAllocation.load();
+	while (left >= 0) {
+		if (g_failAllocation.compare_exchange_weak(left, left - 1)) {
+			if (left == 0) {
+				*p = nullptr;
+				return cudaErrorMemoryAllocation;
+			}
+			break;
+		}
+	}
+	return cudaMalloc(p, bytes);
+}
+
+} // namespace dsrg
+
 extern "C" {
+
+int dsrg_debug_fail_allocation(int64_t after) {
+	dsrg::g_failAllocation.store(after < 0 ? -1 : after);
+	return DSRG_OK;
+}
 
 int dsrg_context_create(int32_t device, dsrg_context *out) {
 	if (!out) return DSRG_ERROR_INVALID_ARGUMENT;
@@ -32,13 +60,17 @@ int dsrg_context_create(int32_t device, dsrg_context *out) {
 	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
-	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(1) != cudaSuccess ||
+	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(2) != cudaSuccess ||
 	    cudaMallocHost((void **)&ctx->pinnedReadback, 16 * sizeof(uint32_t)) != cudaSuccess ||
 	    cudaHostGetDevicePointer((void **)&ctx->readbackDevice, ctx->pinnedReadback, 0) != cudaSuccess) {
 		delete ctx;
 		return DSRG_ERROR_CUDA;
 	}
-	cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream);
+	if (cudaMemsetAsync(ctx->control.ptr, 0, 4 * sizeof(uint32_t), ctx->stream) != cudaSuccess ||
+	    cudaMemsetAsync(ctx->fragmentCounter.ptr, 0, 2 * sizeof(unsigned long long), ctx->stream) != cudaSuccess) {
+		dsrg_context_destroy(ctx);
+		return DSRG_ERROR_CUDA;
+	}
 	*out = ctx;
 	return DSRG_OK;
 }
@@ -60,6 +92,7 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
 	if (ctx->pinnedReadback) cudaFreeHost(ctx->pinnedReadback);
 	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
+	ctx->lightStaging.release();
 	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);
 	cudaEventDestroy(ctx->eventStop);
@@ -78,6 +111,15 @@ int dsrg_context_set_counting(dsrg_context ctx, int32_t counting, uint32_t *devi
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	ctx->counting = counting;
 	ctx->coverage = counting ? deviceCoverage : nullptr;
+	return DSRG_OK;
+}
+
+int dsrg_context_walked_fragments(dsrg_context ctx, uint64_t *out) {
+	if (!ctx || !out) return DSRG_ERROR_INVALID_ARGUMENT;
+	unsigned long long walked = 0;
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&walked, ctx->fragmentCounter.ptr + 1, sizeof(walked), cudaMemcpyDeviceToHost, ctx->stream));
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	*out = walked;
 	return DSRG_OK;
 }
 
@@ -143,11 +185,11 @@ int dsrg_model_create(dsrg_context ctx, const float *positions, int32_t pointCou
 	}
 	cudaSetDevice(ctx->device);
 	size_t np = (size_t)(pointCount > 0 ? pointCount : 1), ng = (size_t)(polygonCount > 0 ? polygonCount : 1);
-	bool ok = cudaMalloc((void **)&m->positions, np * 3 * sizeof(float)) == cudaSuccess &&
-	          cudaMalloc((void **)&m->polygons, ng * 4 * sizeof(int32_t)) == cudaSuccess &&
-	          cudaMalloc((void **)&m->texCoords, ng * 16 * sizeof(float)) == cudaSuccess &&
-	          cudaMalloc((void **)&m->colors, ng * 16 * sizeof(float)) == cudaSuccess &&
-	          cudaMalloc((void **)&m->triSource, (triSource.size() + 1) * sizeof(int32_t)) == cudaSuccess;
+	bool ok = dsrg::device_alloc((void **)&m->positions, np * 3 * sizeof(float)) == cudaSuccess &&
+	          dsrg::device_alloc((void **)&m->polygons, ng * 4 * sizeof(int32_t)) == cudaSuccess &&
+	          dsrg::device_alloc((void **)&m->texCoords, ng * 16 * sizeof(float)) == cudaSuccess &&
+	          dsrg::device_alloc((void **)&m->colors, ng * 16 * sizeof(float)) == cudaSuccess &&
+	          dsrg::device_alloc((void **)&m->triSource, (triSource.size() + 1) * sizeof(int32_t)) == cudaSuccess;
 	if (ok && pointCount > 0) ok = cudaMemcpy(m->positions, positions, (size_t)pointCount * 3 * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
 	if (ok && polygonCount > 0) {
 		ok = cudaMemcpy(m->polygons, polygonIndices, (size_t)polygonCount * 4 * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -161,6 +203,12 @@ int dsrg_model_create(dsrg_context ctx, const float *positions, int32_t pointCou
 		return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "dsrg_model_create: device allocation or copy failed");
 	}
 	*out = m;
+	return DSRG_OK;
+}
+
+int dsrg_model_set_bound(dsrg_model m, const float *minimum, const float *maximum) {
+	if (!m || !minimum || !maximum) return DSRG_ERROR_INVALID_ARGUMENT;
+	for (int a = 0; a < 3; a++) { m->minBound[a] = minimum[a]; m->maxBound[a] = maximum[a]; }
 	return DSRG_OK;
 }
 
@@ -292,9 +340,7 @@ static int give_task(dsrg_renderer r, dsrg_model m, const float *modelToWorld, c
 	if (!m || !modelToWorld || !camera) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: null argument");
 	if (camera->width <= 0 || camera->height <= 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask: camera without image size");
 	CameraData cam = make_camera(*camera);
-	if (r->cameraKnown && r->affine != !camera->perspective)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: perspective and orthogonal cameras cannot share one frame");
-	r->affine = !camera->perspective;
+	r->affine = !camera->perspective; // the last camera's projection (a frame may mix both)
 	r->cameraKnown = true;
 	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld)) return DSRG_OK;
 	if (r->occluded) { // the whole model behind the occluders so far (modelAPI.cpp:228-233)
@@ -366,9 +412,7 @@ int dsrg_renderer_give_triangles(dsrg_renderer r, int32_t count, const dsrg_proj
 		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: unknown filter");
 	if ((diffuse && diffuse->context != ctx) || (light && light->context != ctx))
 		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "renderer_giveTask_triangle: texture of another context");
-	if (r->cameraKnown && r->affine != !camera->perspective)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "renderer_giveTask: perspective and orthogonal cameras cannot share one frame");
-	r->affine = !camera->perspective;
+	r->affine = !camera->perspective; // the last camera's projection (a frame may mix both)
 	r->cameraKnown = true;
 	if (count == 0 || (!r->hasColor && !r->hasDepth)) return DSRG_OK; // renderTriangleFromData: no target to draw on
 	TaskParams task;
@@ -516,14 +560,18 @@ static int end_frame(dsrg_renderer r, bool debugWireframe) {
 		return DSRG_OK;
 	};
 	// Alpha-filtered tasks blend in submission order and write no depth (fillShape,
-	// fillerTemplates.h:387-441), so a frame runs as consecutive runs of alpha-filtered and other
-	// tasks, each through the whole pipeline, one after another on the stream.  Without a colour
-	// target an alpha-filtered task draws like a solid one.
-	auto isAlpha = [&](const TaskParams &t) { return r->hasColor && !r->depthOnly && t.filter == 1; };
-	bool anyAlpha = false;
-	for (const TaskParams &t : job.tasks) anyAlpha = anyAlpha || isAlpha(t);
-	if (!anyAlpha) {
-		job.alpha = false;
+	// fillerTemplates.h:387-441), and a task seen through an orthogonal camera tests linear depth
+	// with '<' where a perspective one tests 1/W with '>' (fillerTemplates.h:108-152), so a frame
+	// runs as consecutive runs of tasks of one kind, each through the whole pipeline, one after
+	// another on the stream.  Without a colour target an alpha-filtered task draws like a solid one.
+	auto kind = [&](const TaskParams &t) {
+		return ((r->hasColor && !r->depthOnly && t.filter == 1) ? 2 : 0) | (t.camera.perspective ? 0 : 1);
+	};
+	bool oneKind = true;
+	for (const TaskParams &t : job.tasks) oneKind = oneKind && kind(t) == kind(job.tasks[0]);
+	if (oneKind) {
+		job.alpha = !job.tasks.empty() && (kind(job.tasks[0]) & 2) != 0;
+		if (!job.tasks.empty()) f.affine = kind(job.tasks[0]) & 1;
 		job.clearCounters = true;
 		status = enqueue(totals);
 	} else {
@@ -531,11 +579,12 @@ static int end_frame(dsrg_renderer r, bool debugWireframe) {
 		all.swap(job.tasks);
 		size_t begin = 0;
 		while (begin < all.size() && status == DSRG_OK) {
-			const bool alpha = isAlpha(all[begin]);
+			const int k = kind(all[begin]);
 			size_t end = begin + 1;
-			while (end < all.size() && isAlpha(all[end]) == alpha) end++;
+			while (end < all.size() && kind(all[end]) == k) end++;
 			job.tasks.assign(all.begin() + begin, all.begin() + end);
-			job.alpha = alpha;
+			job.alpha = (k & 2) != 0;
+			job.frames[0].affine = k & 1;
 			job.clearCounters = begin == 0;
 			BatchTotals run;
 			status = enqueue(run);

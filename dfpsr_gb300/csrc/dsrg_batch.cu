@@ -5,7 +5,9 @@
 // The reference has no batched form; its renderer draws one target at a time.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <utility>
 #include <cstring>
 #include <new>
 #include <string>
@@ -23,7 +25,6 @@ struct dsrg_batch_s {
 		bool hasColor = false, hasDepth = false;
 		int32_t width = 0, height = 0;
 		uint32_t triangles = 0; // fan triangles given so far (the next task's orderBase)
-		int32_t affine = -1;    // -1 no camera yet, 0 perspective, 1 orthogonal
 	};
 	std::vector<Frame> frames;
 	std::vector<TaskParams> tasks;
@@ -34,7 +35,83 @@ struct dsrg_batch_s {
 	std::vector<void *> mapped; // per frame: device addresses of page-locked colour and depth images
 	bool depthOnly = false; // model_renderDepth semantics for every frame
 	BatchJob job;
+	BatchJob runs; // one pass of a batch whose frames draw several runs
 };
+
+// A frame's tasks in submission order form runs of consecutive tasks of one kind: alpha-filtered
+// or not (alpha-filtered tasks blend in order and write no depth, fillerTemplates.h:387-441) and
+// seen through a perspective or an orthogonal camera (the depth test compares 1/W with '>' or W
+// with '<', fillerTemplates.h:108-152).  Each run is drawn by the key-based passes of its kind,
+// and a frame's runs follow one another, which is the reference's order.  Pass p of the batch
+// draws run p of every frame that has one: the solid runs in one batch, then the alpha runs.
+static int enqueue_runs(dsrg_context ctx, BatchJob &job, BatchJob &run, BatchTotals &totals) {
+	const size_t frameCount = job.frames.size();
+	auto kind = [&](const TaskParams &t) -> int {
+		const bool alpha = !job.depthOnly && t.filter == 1 && job.frames[(size_t)t.frame].color != nullptr;
+		return (alpha ? 2 : 0) | (t.camera.perspective ? 0 : 1);
+	};
+	// each frame's runs: [first task, end) ranges over its own task list
+	std::vector<std::vector<size_t>> own(frameCount);
+	for (size_t i = 0; i < job.tasks.size(); i++) own[(size_t)job.tasks[i].frame].push_back(i);
+	std::vector<std::vector<std::pair<size_t, size_t>>> runs(frameCount);
+	size_t passes = 0;
+	bool anyAlpha = false;
+	for (size_t f = 0; f < frameCount; f++) {
+		const std::vector<size_t> &t = own[f];
+		for (size_t begin = 0; begin < t.size();) {
+			size_t end = begin + 1;
+			while (end < t.size() && kind(job.tasks[t[end]]) == kind(job.tasks[t[begin]])) end++;
+			runs[f].push_back(std::make_pair(begin, end));
+			anyAlpha = anyAlpha || (kind(job.tasks[t[begin]]) & 2) != 0;
+			begin = end;
+		}
+		passes = std::max(passes, runs[f].size());
+		job.frames[f].affine = runs[f].empty() ? 0 : (kind(job.tasks[t[0]]) & 1);
+	}
+	if (passes <= 1 && !anyAlpha) {
+		job.alpha = false;
+		job.clearCounters = true;
+		return batch_enqueue(ctx, job, totals);
+	}
+	run.textures.swap(job.textures);
+	run.depthOnly = job.depthOnly;
+	run.resolve = job.resolve;
+	run.hostTargets = job.hostTargets;
+	int status = DSRG_OK;
+	bool first = true;
+	for (size_t p = 0; p < passes && status == DSRG_OK; p++) {
+		for (int alpha = 0; alpha < 2 && status == DSRG_OK; alpha++) {
+			run.frames.clear();
+			run.tasks.clear();
+			for (size_t f = 0; f < frameCount; f++) {
+				if (p >= runs[f].size()) continue;
+				const std::vector<size_t> &t = own[f];
+				const int k = kind(job.tasks[t[runs[f][p].first]]);
+				if (((k & 2) != 0) != (alpha != 0)) continue;
+				FrameTarget target = job.frames[f];
+				target.affine = k & 1;
+				run.frames.push_back(target);
+				for (size_t i = runs[f][p].first; i < runs[f][p].second; i++) {
+					TaskParams task = job.tasks[t[i]];
+					task.frame = (int32_t)run.frames.size() - 1;
+					run.tasks.push_back(task);
+				}
+			}
+			if (run.frames.empty()) continue;
+			run.alpha = alpha != 0;
+			run.clearCounters = first;
+			first = false;
+			BatchTotals part;
+			status = batch_enqueue(ctx, run, part);
+			totals.triangles += part.triangles;
+			totals.records += part.records;
+			totals.rows += part.rows;
+			totals.binEntries += part.binEntries;
+		}
+	}
+	run.textures.swap(job.textures);
+	return status;
+}
 
 static bool image_ok(const dsrg_image *img) {
 	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 && img->strideBytes % 4 == 0;
@@ -101,12 +178,6 @@ int dsrg_batch_give_task(dsrg_batch b, int32_t frameIndex, dsrg_model m, const f
 	if (!m || !modelToWorld || !camera) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_give_task: null argument");
 	if (camera->width <= 0 || camera->height <= 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_batch_give_task: camera without image size");
 	dsrg_batch_s::Frame &f = b->frames[frameIndex];
-	if (m->filter == DSRG_FILTER_ALPHA && f.hasColor)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_batch_give_task: the alpha filter is not available on the GPU path yet");
-	const int32_t affine = camera->perspective ? 0 : 1;
-	if (f.affine >= 0 && f.affine != affine)
-		return fail(ctx, DSRG_ERROR_UNSUPPORTED, "dsrg_batch_give_task: perspective and orthogonal cameras cannot share one frame");
-	f.affine = affine;
 	CameraData cam = make_camera(*camera);
 	// ModelImpl::render skips models whose bound is outside the view (model/Model.cpp:186-197)
 	if (!box_seen(cam, m->minBound, m->maxBound, modelToWorld) || m->triangleCount == 0) return DSRG_OK;
@@ -167,7 +238,6 @@ int dsrg_batch_render(dsrg_batch b) {
 		memset(&t, 0, sizeof(t));
 		t.width = f.width;
 		t.height = f.height;
-		t.affine = f.affine == 1 ? 1 : 0;
 		if (f.hasColor) {
 			t.packOrder = f.color.packOrder;
 			if (f.color.onDevice || mapped[2 * i]) {
@@ -208,7 +278,7 @@ int dsrg_batch_render(dsrg_batch b) {
 		for (TaskParams &t : job.tasks) t.depthOnly = 0;
 	}
 	BatchTotals totals;
-	const int status = batch_enqueue(ctx, job, totals);
+	const int status = enqueue_runs(ctx, job, b->runs, totals);
 	job.tasks.swap(b->tasks);
 	job.textures.swap(b->textures);
 	if (status != DSRG_OK) {
@@ -295,7 +365,7 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	// would look faster than they are.
 	void *flush = nullptr;
 	const size_t flushBytes = (size_t)256 << 20;
-	if (cudaMalloc(&flush, flushBytes) != cudaSuccess) {
+	if (device_alloc(&flush, flushBytes) != cudaSuccess) {
 		cudaGetLastError();
 		flush = nullptr; // timed warm if the memory is not there
 	}

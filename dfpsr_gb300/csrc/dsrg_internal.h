@@ -16,6 +16,9 @@
 
 namespace dsrg {
 
+// Every device allocation of the library (cudaMalloc), so that a test can make the k-th one fail
+// as an exhausted device would (dsrg_debug_fail_allocation).
+cudaError_t device_alloc(void **p, size_t bytes);
 
 template <typename T>
 struct DeviceBuffer {
@@ -26,7 +29,7 @@ struct DeviceBuffer {
 		size_t newCapacity = capacity ? capacity : 1024;
 		while (newCapacity < n) newCapacity *= 2;
 		T *fresh = nullptr;
-		cudaError_t err = cudaMalloc((void **)&fresh, newCapacity * sizeof(T));
+		cudaError_t err = device_alloc((void **)&fresh, newCapacity * sizeof(T));
 		if (err != cudaSuccess) return err;
 		if (keep && ptr && keepCount) {
 			err = cudaMemcpyAsync(fresh, ptr, keepCount * sizeof(T), cudaMemcpyDeviceToDevice, stream);
@@ -191,6 +194,7 @@ struct dsrg_context_s {
 	DeviceBuffer<uint32_t> textureStaging;      // texture creation: host images and two-step resize halves
 	DeviceBuffer<unsigned char> textureTables;  // texture creation: work tables
 	DeviceBuffer<float> stagingDepth;
+	DeviceBuffer<uint32_t> lightStaging;        // light passes and draw_higher: pageable host images and sprites
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;
 	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;

@@ -24,6 +24,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <utility>
 
 #include "dsrg_exact.h"
@@ -36,6 +37,21 @@
 namespace dsrg {
 
 static uint64_t g_launches = 0;
+
+// The first failed enqueue of a memset inside the launchers of this thread, reported to the caller
+// of the launches by take_enqueue_error (the launchers themselves return nothing).
+static thread_local cudaError_t t_enqueueError = cudaSuccess;
+
+static void memset_async(void *p, int value, size_t bytes, cudaStream_t stream) {
+	const cudaError_t e = cudaMemsetAsync(p, value, bytes, stream);
+	if (e != cudaSuccess && t_enqueueError == cudaSuccess) t_enqueueError = e;
+}
+
+cudaError_t take_enqueue_error() {
+	const cudaError_t e = t_enqueueError;
+	t_enqueueError = cudaSuccess;
+	return e;
+}
 uint64_t launch_count() { return g_launches; }
 void add_launches(uint64_t n) { g_launches += n; }
 #define COUNT_LAUNCH() (g_launches++)
@@ -73,13 +89,13 @@ __device__ __forceinline__ void chain_enter() {
 }
 
 template <typename... Params, typename... Args>
-static void launch_chained(void (*kernel)(Params...), uint32_t grid, uint32_t block, cudaStream_t stream, Args &&...args) {
+static void launch_chained(void (*kernel)(Params...), dim3 grid, uint32_t block, cudaStream_t stream, Args &&...args) {
 	cudaLaunchAttribute attribute[1];
 	attribute[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
 	attribute[0].val.programmaticStreamSerializationAllowed = 1;
 	cudaLaunchConfig_t config;
 	memset(&config, 0, sizeof(config));
-	config.gridDim = dim3(grid);
+	config.gridDim = grid;
 	config.blockDim = dim3(block);
 	config.stream = stream;
 	config.attrs = attribute;
@@ -298,7 +314,7 @@ __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers 
 
 void launch_setup_count(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream) {
 	if (b.totalTriangles == 0) {
-		cudaMemsetAsync(fb.triOffsets, 0, sizeof(uint32_t), stream);
+		memset_async(fb.triOffsets, 0, sizeof(uint32_t), stream);
 		return;
 	}
 	COUNT_LAUNCH();
@@ -451,7 +467,7 @@ static void scan_launch(const uint32_t *in, uint32_t *out, uint32_t n, const uin
                         cudaStream_t stream) {
 	const uint32_t blocks = n / SCAN_CHUNK + 1; // n = the length, or the capacity bounding a device length
 	if (blocks > scratchElems) {
-		cudaMemsetAsync(out, 0xFF, sizeof(uint32_t), stream); // never reached: callers size the scratch
+		memset_async(out, 0xFF, sizeof(uint32_t), stream); // never reached: callers size the scratch
 		return;
 	}
 	COUNT_LAUNCH();
@@ -888,8 +904,8 @@ void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *err
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
                                  cudaStream_t stream) {
 	if (!bins.cleared) {
-		cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
-		cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+		memset_async(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+		memset_async(bins.bigCount, 0, sizeof(uint32_t), stream);
 	}
 	fb.counts.rowCounts = rowCounts;
 	fb.counts.binCounts = bins.counts;
@@ -909,8 +925,8 @@ void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t
 
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
 	if (!bins.cleared) {
-		cudaMemsetAsync(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
-		if (bins.bigCount) cudaMemsetAsync(bins.bigCount, 0, sizeof(uint32_t), stream);
+		memset_async(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+		if (bins.bigCount) memset_async(bins.bigCount, 0, sizeof(uint32_t), stream);
 	}
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
@@ -925,7 +941,7 @@ void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t rec
 }
 
 void launch_bin_fill(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {
-	if (!bins.cleared) cudaMemsetAsync(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
+	if (!bins.cleared) memset_async(bins.cursors, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 	if (recordCount > 0) {
 		COUNT_LAUNCH();
 		launch_chained(bin_kernel<true>, grid_for(recordCount, 256), 256, stream, b, fb.records, recordCount, fb.recordCountDevice, bins,
@@ -1031,31 +1047,44 @@ __device__ __forceinline__ uint32_t record_best_hi(const DrawRecord &r, int32_t 
 	return affine ? ~hi : hi;
 }
 
-// The winner of one pixel, shaded and written: the reference's running sums of its quad
-// (quad_lanes), the vertex weights, RgbaMultiply and the packed colour and depth.
-__device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameTarget &f, const DrawRecord *__restrict__ records,
-                                              const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows,
-                                              int32_t px, int32_t py, unsigned long long key) {
-	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
-	const uint32_t ri = key_record(key, depthTest);
-	const DrawRecord r = records[ri];
-	const int32_t y1 = py & ~1, x = px & ~1;
-	const int lane4 = ((py & 1) << 1) | (px & 1);
-	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
+// Lane `lane` of the record's quad at (x, y1), shaded and written to pixel (px, py): the
+// reference's running sums of the quad (quad_lanes), the vertex weights, RgbaMultiply and the
+// packed colour and depth.
+__device__ __forceinline__ void write_lane(const BatchParams &b, const FrameTarget &f, const DrawRecord &r, const RowPair &pair,
+                                           int32_t y1, int32_t x, int lane, int32_t px, int32_t py, bool affine) {
 	float w[3][4];
 	const int components = f.color ? 3 : 1;
 	for (int c = 0; c < components; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
-	const float depthValue = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
+	const float depthValue = (lane == 0) ? w[0][0] : (lane == 1) ? w[0][1] : (lane == 2) ? w[0][2] : w[0][3];
 	if (f.color) {
 		float wa[4], wb[4], wc[4];
 		lane_weights(w, affine, wa, wb, wc);
 		ShadeRecord shade;
 		make_shade(b.tasks[r.task], r.source, shade);
 		float rgba[4];
-		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
+		shade_lane_inline(shade, b.textures, wa, wb, wc, lane, rgba);
 		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
 	}
-	if (depthTest) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+	if (f.depth) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+}
+
+// The winner of one pixel, shaded and written: the reference's running sums of its quad
+// (quad_lanes), the vertex weights, RgbaMultiply and the packed colour and depth.  On the last row
+// of an odd-height target the depth-tested pixels are left to odd_row_kernel (their result depends
+// on the order of the triangles); without a depth buffer the last triangle drawn wins there as
+// anywhere, with its lower lane's value where the pixel lies in its run of full quads.
+__device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameTarget &f, const DrawRecord *__restrict__ records,
+                                              const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows,
+                                              int32_t px, int32_t py, unsigned long long key) {
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
+	const bool oddRow = odd_last_row(py, f.height);
+	if (oddRow && depthTest) return;
+	const uint32_t ri = key_record(key, depthTest);
+	const DrawRecord r = records[ri];
+	const int32_t y1 = py & ~1, x = px & ~1;
+	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
+	const int lane4 = ((py & 1) << 1) | (px & 1) | ((oddRow && full_quad(pair, x)) ? 2 : 0);
+	write_lane(b, f, r, pair, y1, x, lane4, px, py, affine);
 }
 
 // Persistent CTAs pull 16x16 tiles of the batch from a device queue.  The binning split every
@@ -1292,7 +1321,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				}
 			}
 		}
-		if (b.fragments) {
+		if (b.fragments || b.walked) {
 			for (int o = 16; o > 0; o >>= 1) fragments += __shfl_xor_sync(0xFFFFFFFFu, fragments, o);
 			if (lane == 0) atomicAdd(&fragmentSum, (unsigned long long)fragments);
 		}
@@ -1309,7 +1338,10 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 				else if (keys[me] != 0ull) resolve_pixel(b, f, records, rowOffsets, rows, px, py, keys[me]);
 			}
 		}
-		if (b.fragments && tid == 0) atomicAdd(b.fragments, fragmentSum);
+		if (tid == 0 && fragmentSum) {
+			if (b.fragments) atomicAdd(b.fragments, fragmentSum);
+			if (b.walked) atomicAdd(b.walked, fragmentSum);
+		}
 		__syncthreads();
 	}
 }
@@ -1380,7 +1412,8 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
 	for (int l = 0; l < 4; l++) {
 		const int32_t px = x + (l & 1), py = y1 + (l >> 1);
 		record[l] = 0;
-		if (px < width && py < height) {
+		// depth-tested pixels of an odd-height target's last row: odd_row_kernel
+		if (px < width && py < height && !(depthTest && odd_last_row(py, height))) {
 			const unsigned long long key = f.keys[(size_t)py * width + px];
 			if (key != 0ull) {
 				record[l] = key_record(key, depthTest);
@@ -1407,17 +1440,177 @@ __global__ void __launch_bounds__(64) resolve_quads_kernel(BatchParams b, const 
 			make_shade(b.tasks[r.task], r.source, shade);
 			float u[4], v[4];
 			const uint32_t mip = quad_diffuse_coordinates(shade, b.textures, wa, wb, wc, u, v);
+			// no depth buffer, last row of an odd height: the lower lanes of full quads are written last
+			const int lower = (odd_last_row(y1, height) && full_quad(pair, x)) ? 2 : 0;
 #pragma unroll
 			for (int l = 0; l < 4; l++) {
 				if (!(mask & (1u << l))) continue;
 				float rgba[4];
-				shade_quad_lane(shade, b.textures, wa, wb, wc, u, v, mip, l, rgba);
+				shade_quad_lane(shade, b.textures, wa, wb, wc, u, v, mip, l + lower, rgba);
 				f.color[(size_t)(y1 + (l >> 1)) * f.colorStride + x + (l & 1)] = pack_saturated(rgba, f.packOrder);
 			}
 		}
 		if (depthTest)
 			for (int l = 0; l < 4; l++)
 				if (mask & (1u << l)) f.depth[(size_t)(y1 + (l >> 1)) * f.depthStride + x + (l & 1)] = w[0][l];
+	}
+}
+
+// ------------------------------------------------------------------ last row of odd heights
+
+// Records one odd_row_kernel window holds (candidates of all 16 columns in shared memory).
+static const int ODD_WINDOW = 320;
+static const int ODD_SORT = 512; // ODD_WINDOW rounded up to a power of two, for the bitonic sort
+
+// Whether a record can touch row y of the 16 columns from tx0 (its bound, which holds every pixel
+// it writes, the lower lanes of the last row's full quads included).
+__device__ __forceinline__ bool odd_row_relevant(const DrawRecord *__restrict__ records, uint32_t ri, int32_t y, int32_t tx0) {
+	const int4 bound = *reinterpret_cast<const int4 *>(&records[ri].flat[4]); // flat[4], flat[5], left, top
+	const int2 rb = *reinterpret_cast<const int2 *>(&records[ri].right);
+	return bound.w <= y && rb.y > y && bound.z < tx0 + TILE_W && rb.x > tx0;
+}
+
+// Relevant records of the tile's list with index in [lo, hi): counted, and the largest one.
+__device__ __forceinline__ void odd_row_count(const DrawRecord *__restrict__ records, const uint32_t *__restrict__ lists,
+                                              uint32_t begin, uint32_t end, uint32_t lo, uint32_t hi, int32_t y, int32_t tx0,
+                                              uint32_t *count, uint32_t *largest) {
+	__syncthreads(); // every thread has read the previous totals
+	if (threadIdx.x == 0) { *count = 0u; *largest = 0u; }
+	__syncthreads();
+	uint32_t n = 0, m = 0;
+	for (uint32_t e = begin + threadIdx.x; e < end; e += blockDim.x) {
+		const uint32_t ri = lists[e];
+		if (ri >= lo && ri < hi && odd_row_relevant(records, ri, y, tx0)) { n++; m = max(m, ri); }
+	}
+	if (n) { atomicAdd(count, n); atomicMax(largest, m); }
+	__syncthreads();
+}
+
+// The last row of a depth-tested frame of odd height, in submission order (odd_last_row).  Along
+// the run of full quads of that row pair a triangle writes its lower lane's value over its upper
+// lane's whenever the lower lane passes the depth test, even where the upper lane is nearer, so
+// the row's result is not the nearest fragment and the max-key argument of the tile pass does not
+// hold: the tile pass leaves the row alone and this kernel replays it.  One CTA per tile of the
+// frame's bottom tile row (blockIdx.x the tile column, blockIdx.y the frame).  The tile's records
+// that reach the row are taken in windows of at most ODD_WINDOW in increasing record index (the
+// submission order); a window is sorted in shared memory, every (record, column) pair evaluates its
+// upper and lower candidates in parallel (quad_lanes, as the tile pass does), and one thread per
+// column folds them in order with the reference's strict tests: the lower lane if it beats the
+// stored depth, else the upper one if it does.  The winner is shaded once at the end.
+__global__ void __launch_bounds__(256) odd_row_kernel(BatchParams b, const DrawRecord *__restrict__ records,
+                                                      const uint32_t *__restrict__ binOffsets, const uint32_t *__restrict__ lists,
+                                                      const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
+	chain_enter();
+	if (overflowed(b)) return;
+	__shared__ uint32_t ids[ODD_SORT];
+	__shared__ float2 candidates[ODD_WINDOW * TILE_W];
+	__shared__ uint32_t count, largest;
+	// every condition that skips a frame or tile is the same for the whole CTA
+	for (int32_t frame = (int32_t)blockIdx.y; frame < b.frameCount; frame += (int32_t)gridDim.y) {
+		const FrameTarget &f = b.frames[frame];
+		if (!(f.height & 1) || f.depth == nullptr || (int32_t)blockIdx.x >= f.tilesX) continue;
+		const uint32_t tile = f.tileBase + (uint32_t)((f.tilesY - 1) * f.tilesX) + blockIdx.x;
+		const uint32_t begin = binOffsets[2 * tile], end = binOffsets[2 * tile + 2];
+		if (begin == end) continue;
+		const int32_t y = f.height - 1, tx0 = (int32_t)blockIdx.x * TILE_W, width = f.width;
+		const bool affine = f.affine != 0;
+		const int tid = threadIdx.x;
+		// fold state of column tid (threads 0..15); orthogonal depths are negated so that the nearer
+		// one is always the greater (x < y exactly when -x > -y, and NaN fails both)
+		const int32_t px = tx0 + tid;
+		float stored = 0.0f;
+		uint32_t winner = 0xFFFFFFFFu;
+		int winnerLower = 0;
+		if (tid < TILE_W && px < width) {
+			stored = f.depth[(size_t)y * f.depthStride + px];
+			if (affine) stored = -stored;
+		}
+		uint32_t lo = 0;
+		for (;;) {
+			odd_row_count(records, lists, begin, end, lo, 0xFFFFFFFFu, y, tx0, &count, &largest);
+			uint32_t n = count;
+			if (n == 0) break;
+			uint32_t hi = 0xFFFFFFFFu;
+			if (n > (uint32_t)ODD_WINDOW) {
+				// the largest hi whose window [lo, hi) holds at most ODD_WINDOW records (bisection;
+				// [lo, lo + 1) holds at most one, [lo, largest + 1) too many)
+				uint32_t good = lo + 1, bad = largest + 1;
+				while (bad - good > 1) {
+					const uint32_t mid = good + (bad - good) / 2;
+					odd_row_count(records, lists, begin, end, lo, mid, y, tx0, &count, &largest);
+					if (count <= (uint32_t)ODD_WINDOW) good = mid; else bad = mid;
+				}
+				hi = good;
+			}
+			// gather the window (any order), then sort it ascending
+			__syncthreads();
+			if (tid == 0) count = 0u;
+			__syncthreads();
+			for (uint32_t e = begin + tid; e < end; e += blockDim.x) {
+				const uint32_t ri = lists[e];
+				if (ri >= lo && ri < hi && odd_row_relevant(records, ri, y, tx0)) {
+					const uint32_t slot = atomicAdd(&count, 1u);
+					if (slot < (uint32_t)ODD_WINDOW) ids[slot] = ri; // always true: the window was sized by the same test
+				}
+			}
+			__syncthreads();
+			n = min(count, (uint32_t)ODD_WINDOW);
+			for (uint32_t i = n + tid; i < (uint32_t)ODD_SORT; i += blockDim.x) ids[i] = 0xFFFFFFFFu;
+			__syncthreads();
+			for (uint32_t k = 2; k <= (uint32_t)ODD_SORT; k <<= 1) {
+				for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+					for (uint32_t i = tid; i < (uint32_t)ODD_SORT; i += blockDim.x) {
+						const uint32_t partner = i ^ j;
+						if (partner > i) {
+							const uint32_t a = ids[i], c = ids[partner];
+							const bool ascending = (i & k) == 0;
+							if ((a > c) == ascending) { ids[i] = c; ids[partner] = a; }
+						}
+					}
+					__syncthreads();
+				}
+			}
+			// candidates of every (record, column): upper lane where covered, lower lane in full quads
+			for (uint32_t p = tid; p < n * TILE_W; p += blockDim.x) {
+				const uint32_t j = p >> 4;
+				const int32_t cx = tx0 + (int32_t)(p & 15);
+				const float none = __int_as_float(0x7FC00000); // quiet NaN: fails every depth test
+				float2 cand = make_float2(none, none);
+				if (cx < width) {
+					const uint32_t ri = ids[j];
+					const DrawRecord r = records[ri];
+					const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y, f.height);
+					const int32_t x = cx & ~1;
+					if (pair.any && x >= pair.obs && x < pair.obe) {
+						float v[4];
+						quad_lanes(r.start[0], r.dx[0], r.dy[0], pair, y, x, v);
+						const bool full = full_quad(pair, x);
+						const int l = cx & 1;
+						if (lane_covered(pair, x, !full, l)) cand.x = affine ? -v[l] : v[l];
+						if (full) cand.y = affine ? -v[l + 2] : v[l + 2];
+					}
+				}
+				candidates[p] = cand;
+			}
+			__syncthreads();
+			if (tid < TILE_W) {
+				for (uint32_t j = 0; j < n; j++) {
+					const float2 cand = candidates[j * TILE_W + tid];
+					if (cand.y > stored) { stored = cand.y; winner = ids[j]; winnerLower = 1; }
+					else if (cand.x > stored) { stored = cand.x; winner = ids[j]; winnerLower = 0; }
+				}
+			}
+			__syncthreads();
+			if (hi == 0xFFFFFFFFu) break;
+			lo = hi;
+		}
+		if (tid < TILE_W && px < width && winner != 0xFFFFFFFFu) {
+			const DrawRecord r = records[winner];
+			const int32_t x = px & ~1;
+			const RowPair pair = record_row_pair(r, rows + rowOffsets[winner], y, f.height);
+			write_lane(b, f, r, pair, y, x, (px & 1) + (winnerLower ? 2 : 0), px, y, affine);
+		}
+		__syncthreads(); // the next frame reuses the shared arrays
 	}
 }
 
@@ -1462,6 +1655,7 @@ __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRec
 	uint32_t packed = *target;
 	const int32_t y1 = py & ~1, x = px & ~1;
 	const int lane4 = ((py & 1) << 1) | (px & 1);
+	const bool oddRow = odd_last_row(py, f.height);
 	uint32_t fragments = 0;
 	for (uint32_t e = begin; e < end; e++) {
 		const uint32_t ri = sorted[e];
@@ -1475,13 +1669,20 @@ __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRec
 		float w[3][4];
 		for (int c = 0; c < 3; c++) quad_lanes(r.start[c], r.dx[c], r.dy[c], pair, y1, x, w[c]);
 		const float z = (lane4 == 0) ? w[0][0] : (lane4 == 1) ? w[0][1] : (lane4 == 2) ? w[0][2] : w[0][3];
-		if (depthTest && !(affine ? (z < stored) : (z > stored))) continue;
+		int lane = lane4;
+		if (oddRow && full_quad(pair, x)) {
+			// the lower lane reads the same target colour and is written after the upper one: it
+			// decides the pixel when it passes the depth test (odd_last_row)
+			const float zl = w[0][lane4 + 2];
+			if (!depthTest || (affine ? (zl < stored) : (zl > stored))) lane = lane4 + 2;
+		}
+		if (lane == lane4 && depthTest && !(affine ? (z < stored) : (z > stored))) continue;
 		float wa[4], wb[4], wc[4];
 		lane_weights(w, affine, wa, wb, wc);
 		ShadeRecord shade;
 		make_shade(b.tasks[r.task], r.source, shade);
 		float rgba[4];
-		shade_lane_inline(shade, b.textures, wa, wb, wc, lane4, rgba);
+		shade_lane_inline(shade, b.textures, wa, wb, wc, lane, rgba);
 		const float opacity = fmul(rgba[3], 1.0f / 255.0f);
 		const float keep = fsub(1.0f, opacity);
 		float blended[4];
@@ -1494,6 +1695,7 @@ __global__ void __launch_bounds__(256) alpha_kernel(BatchParams b, const DrawRec
 	*target = packed;
 	if (f.coverage) f.coverage[(size_t)py * f.width + px] += fragments;
 	if (b.fragments && fragments) atomicAdd(b.fragments, (unsigned long long)fragments);
+	if (b.walked && fragments) atomicAdd(b.walked, (unsigned long long)fragments);
 }
 
 void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, uint32_t entries, uint32_t recordCount,
@@ -1520,10 +1722,18 @@ void launch_alpha(const BatchParams &b, const FrameBuffers &fb, const TileBins &
 	alpha_kernel<<<b.totalTiles, 256, 0, stream>>>(b, fb.records, bins.offsets, sorted, fb.rowOffsets, fb.rows);
 }
 
+void launch_odd_rows(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, cudaStream_t stream) {
+	if (b.depthOnly || b.oddDepthFrames == 0 || b.totalTiles == 0) return;
+	COUNT_LAUNCH();
+	const unsigned frames = (unsigned)std::min<int32_t>(b.frameCount, 65535);
+	launch_chained(odd_row_kernel, dim3((unsigned)b.maxTilesX, frames), 256, stream, b, fb.records, bins.offsets,
+	               bins.lists, fb.rowOffsets, fb.rows);
+}
+
 void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins &bins, const RasterConfig &config, bool resolve,
                    cudaStream_t stream) {
 	if (b.totalTiles == 0) return;
-	if (!bins.cleared) cudaMemsetAsync(b.tileQueue, 0, sizeof(uint32_t), stream);
+	if (!bins.cleared) memset_async(b.tileQueue, 0, sizeof(uint32_t), stream);
 	const int threads = config.threadsPerTile == 64 ? 64 : (config.threadsPerTile == 128 ? 128 : 256);
 	const int maxPerSm = 1024 / threads;
 	const int perSm = config.ctasPerSm < 1 ? 1 : (config.ctasPerSm > maxPerSm ? maxPerSm : config.ctasPerSm);
@@ -1540,11 +1750,15 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	else if (threads == 128) { DSRG_RASTER(128) }
 	else { DSRG_RASTER(256) }
 #undef DSRG_RASTER
-	if (!resolve || fused) return;
-	COUNT_LAUNCH();
-	if (b.depthOnly) launch_chained(resolve_depth_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-	else if (config.resolveMode == 2) launch_chained(resolve_quads_kernel, b.totalTiles, 64, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-	else launch_chained(resolve_pixels_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	if (!resolve) return;
+	if (!fused) {
+		COUNT_LAUNCH();
+		if (b.depthOnly) launch_chained(resolve_depth_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+		else if (config.resolveMode == 2) launch_chained(resolve_quads_kernel, b.totalTiles, 64, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+		else launch_chained(resolve_pixels_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+	}
+	// the last rows of depth-tested odd-height frames, which every resolve above leaves alone
+	launch_odd_rows(b, fb, bins, stream);
 }
 
 } // namespace dsrg

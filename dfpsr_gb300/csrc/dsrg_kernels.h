@@ -62,9 +62,12 @@ struct BatchParams {
 	uint32_t totalPoints, totalTriangles, totalTiles;
 	const TextureData *textures;
 	unsigned long long *fragments;    // optional fragment total
+	unsigned long long *walked;       // optional running total of the fragments the tile kernels depth-tested
 	int32_t smallRows;                // records whose raster bound is at most smallRows x smallWidth pixels
 	int32_t smallWidth;               // are walked by one lane each instead of by the whole warp
 	int32_t depthOnly;                // the whole batch is model_renderDepth (1x1 walk)
+	int32_t oddDepthFrames;           // frames of odd height with a depth buffer (their last row: odd_row_kernel)
+	int32_t maxTilesX;                // the widest frame's tile columns
 	uint32_t *tileQueue;              // work counter of the persistent tile kernel
 	const int32_t *errorFlag;         // device error bits; tile and resolve kernels return when an overflow is set
 };
@@ -208,6 +211,9 @@ void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratc
 void launch_scan_device(const uint32_t *in, uint32_t *out, const uint32_t *nDevice, uint32_t capacity, uint32_t *scratch,
                         size_t scratchElems, cudaStream_t stream);
 size_t scan_scratch_elems(uint32_t n);
+// The first memset the launchers above failed to enqueue on this thread since the last call
+// (cudaSuccess if none), cleared by the call; callers check it with cudaGetLastError after launching.
+cudaError_t take_enqueue_error();
 // Kernels launched by this library in this process (host-side count).
 uint64_t launch_count();
 // Adds kernels launched through a replayed CUDA graph to that count.

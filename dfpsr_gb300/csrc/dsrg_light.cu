@@ -337,10 +337,70 @@ __global__ void higher_resolve_kernel(const SpriteData *__restrict__ sprites, co
 	targetB[(size_t)y * tbStride + x] = reorder(sp.colorB[(size_t)sy * sp.bStride + sx], sp.bPack, tbPack);
 }
 
-bool device_image(const dsrg_image *img) {
-	return img && img->data && img->onDevice && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 &&
-	       img->strideBytes % 4 == 0;
+bool valid_image(const dsrg_image *img) {
+	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 && img->strideBytes % 4 == 0;
 }
+
+// Memory the kernels of one call reach: device memory as given, page-locked host memory through
+// its device address (read and written in place over the host link), pageable host memory through
+// a copy in the context's staging buffer, copied back after the kernels when the call writes it.
+// The reference's light passes and draw_higher take host images (lightAPI.cpp:23-323,
+// drawAPI.cpp:872-900); this lets the same images come straight from the caller.
+struct CallMemory {
+	const void *host = nullptr; // the caller's pointer
+	size_t rowBytes = 0, strideBytes = 0, rows = 0;
+	bool onDevice = false, written = false;
+	void *device = nullptr;     // where the kernels find it
+	size_t stagedAt = SIZE_MAX; // 4-byte offset into the staging buffer, for pageable memory
+};
+
+CallMemory call_image(const dsrg_image *img, bool written) {
+	CallMemory m;
+	m.host = img->data;
+	m.rowBytes = (size_t)img->width * 4;
+	m.strideBytes = (size_t)img->strideBytes;
+	m.rows = (size_t)img->height;
+	m.onDevice = img->onDevice != 0;
+	m.written = written;
+	return m;
+}
+
+// Resolves where each block lives, stages the pageable ones (one buffer for the call) and copies them in.
+int place(dsrg_context ctx, std::vector<CallMemory> &blocks) {
+	size_t staged = 0;
+	for (CallMemory &m : blocks) {
+		if (m.onDevice || m.rowBytes * m.rows == 0) {
+			m.device = const_cast<void *>(m.host);
+		} else if (!host_mapped(m.host, &m.device)) {
+			m.stagedAt = staged;
+			staged += (m.rowBytes * m.rows + 3) / 4;
+		}
+	}
+	if (staged == 0) return DSRG_OK;
+	DSRG_CUDA_TRY(ctx, ctx->lightStaging.reserve(staged));
+	for (CallMemory &m : blocks) {
+		if (m.stagedAt == SIZE_MAX) continue;
+		m.device = ctx->lightStaging.ptr + m.stagedAt;
+		DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(m.device, m.rowBytes, m.host, m.strideBytes, m.rowBytes, m.rows, cudaMemcpyHostToDevice,
+		                                     ctx->stream));
+		m.strideBytes = m.rowBytes; // the staged copy has no row padding
+	}
+	return DSRG_OK;
+}
+
+// Copies the staged blocks the call wrote back to the caller's memory, and waits for the call.
+int finish(dsrg_context ctx, const std::vector<CallMemory> &blocks, const dsrg_image *const *images) {
+	for (size_t i = 0; i < blocks.size(); i++) {
+		const CallMemory &m = blocks[i];
+		if (m.stagedAt == SIZE_MAX || !m.written) continue;
+		DSRG_CUDA_TRY(ctx, cudaMemcpy2DAsync(const_cast<void *>(m.host), (size_t)images[i]->strideBytes, m.device, m.rowBytes, m.rowBytes,
+		                                     m.rows, cudaMemcpyDeviceToHost, ctx->stream));
+	}
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return DSRG_OK;
+}
+
+int32_t stride_of(const CallMemory &m) { return (int32_t)(m.strideBytes / 4); }
 
 int32_t hardware_threads() {
 	const unsigned n = std::thread::hardware_concurrency();
@@ -420,9 +480,13 @@ int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsr
                         const float direction[3], float intensity, const int32_t color[3], int32_t add) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (!view || !direction || !color) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: null argument");
-	if (!device_image(light) || !device_image(normal) || light->width != normal->width || light->height != normal->height)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: light and normal must be device images of one size");
+	if (!valid_image(light) || !valid_image(normal) || light->width != normal->width || light->height != normal->height)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: light and normal must be images of one size");
 	cudaSetDevice(ctx->device);
+	std::vector<CallMemory> mem = {call_image(light, true), call_image(normal, false)};
+	const dsrg_image *const images[2] = {light, normal};
+	const int placed = place(ctx, mem);
+	if (placed != DSRG_OK) return placed;
 	const M3 n = load_m3(view->normalToWorld);
 	const Vec3 d = normalize_ref(transform_transposed_ref(n, v3(direction[0], direction[1], direction[2])));
 	DirectedParams p;
@@ -435,12 +499,11 @@ int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsr
 	}
 	p.add = add ? 1 : 0;
 	const dim3 grid((light->width + 255) / 256, light->height);
-	light_directed_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)light->data, light->strideBytes / 4, (const uint32_t *)normal->data,
-	                                                     normal->strideBytes / 4, light->width, light->height, p);
+	light_directed_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)mem[0].device, stride_of(mem[0]), (const uint32_t *)mem[1].device,
+	                                                     stride_of(mem[1]), light->width, light->height, p);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	return DSRG_OK;
+	return finish(ctx, mem, images);
 }
 
 int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY, const dsrg_image *light,
@@ -448,9 +511,9 @@ int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
                       int32_t referenceThreads) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (!view || (count > 0 && !lights) || count < 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: null argument");
-	if (!device_image(light) || !device_image(normal) || !device_image(height) || light->width != normal->width ||
+	if (!valid_image(light) || !valid_image(normal) || !valid_image(height) || light->width != normal->width ||
 	    light->height != normal->height || light->width != height->width || light->height != height->height)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: light, normal and height must be device images of one size");
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: light, normal and height must be images of one size");
 	cudaSetDevice(ctx->device);
 	const int32_t width = light->width, imageHeight = light->height;
 	const int32_t threads = referenceThreads > 0 ? referenceThreads : hardware_threads();
@@ -493,6 +556,25 @@ int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
 		params.push_back(p);
 	}
 	if (params.empty()) return DSRG_OK;
+	// the images and the shadow cubes where the kernel reaches them
+	std::vector<CallMemory> mem = {call_image(light, true), call_image(normal, false), call_image(height, false)};
+	std::vector<const dsrg_image *> images = {light, normal, height};
+	for (const PointLightParams &p : params) {
+		if (!p.cube) continue;
+		CallMemory cube;
+		cube.host = p.cube;
+		cube.rowBytes = cube.strideBytes = (size_t)p.cubeWidth * 4;
+		cube.rows = (size_t)p.cubeWidth * 6;
+		cudaPointerAttributes a;
+		cube.onDevice = cudaPointerGetAttributes(&a, p.cube) == cudaSuccess && a.type == cudaMemoryTypeDevice;
+		cudaGetLastError();
+		mem.push_back(cube);
+		images.push_back(nullptr);
+	}
+	const int placed = place(ctx, mem);
+	if (placed != DSRG_OK) return placed;
+	for (size_t k = 0, c = 3; k < params.size(); k++)
+		if (params[k].cube) params[k].cube = (const float *)mem[c++].device;
 	// the light table travels in the context's table buffer
 	const size_t bytes = params.size() * sizeof(PointLightParams);
 	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(bytes));
@@ -504,41 +586,43 @@ int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
 	f.lightCount = (int32_t)params.size();
 	f.lights = reinterpret_cast<const PointLightParams *>(ctx->tables.ptr);
 	const dim3 grid((width + 255) / 256, (imageHeight + 7) / 8);
-	light_points_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)light->data, light->strideBytes / 4, (const uint32_t *)normal->data,
-	                                                   normal->strideBytes / 4, (const float *)height->data, height->strideBytes / 4,
+	light_points_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)mem[0].device, stride_of(mem[0]), (const uint32_t *)mem[1].device,
+	                                                   stride_of(mem[1]), (const float *)mem[2].device, stride_of(mem[2]),
 	                                                   width, imageHeight, f);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	return DSRG_OK;
+	return finish(ctx, mem, images.data());
 }
 
 int dsrg_light_blend(dsrg_context ctx, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
-	if (!device_image(target) || !device_image(diffuse) || !device_image(light) || target->width != diffuse->width ||
+	if (!valid_image(target) || !valid_image(diffuse) || !valid_image(light) || target->width != diffuse->width ||
 	    target->height != diffuse->height || target->width != light->width || target->height != light->height ||
 	    target->packOrder < 0 || target->packOrder > 3)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_blend: target, diffuse and light must be device images of one size");
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_blend: target, diffuse and light must be images of one size");
 	cudaSetDevice(ctx->device);
+	std::vector<CallMemory> mem = {call_image(target, true), call_image(diffuse, false), call_image(light, false)};
+	const dsrg_image *const images[3] = {target, diffuse, light};
+	const int placed = place(ctx, mem);
+	if (placed != DSRG_OK) return placed;
 	const dim3 grid((target->width + 255) / 256, target->height);
-	light_blend_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)target->data, target->strideBytes / 4, target->packOrder,
-	                                                  (const uint32_t *)diffuse->data, diffuse->strideBytes / 4,
-	                                                  (const uint32_t *)light->data, light->strideBytes / 4, target->width,
+	light_blend_kernel<<<grid, 256, 0, ctx->stream>>>((uint32_t *)mem[0].device, stride_of(mem[0]), target->packOrder,
+	                                                  (const uint32_t *)mem[1].device, stride_of(mem[1]),
+	                                                  (const uint32_t *)mem[2].device, stride_of(mem[2]), target->width,
 	                                                  target->height);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	return DSRG_OK;
+	return finish(ctx, mem, images);
 }
 
 int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsrg_image *targetA, const dsrg_image *targetB,
                      const dsrg_sprite *sprites, int32_t count) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (count < 0 || (count > 0 && !sprites)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: null sprites");
-	if (!device_image(targetHeight) || !device_image(targetA) || !device_image(targetB) || targetHeight->width != targetA->width ||
+	if (!valid_image(targetHeight) || !valid_image(targetA) || !valid_image(targetB) || targetHeight->width != targetA->width ||
 	    targetHeight->height != targetA->height || targetHeight->width != targetB->width || targetHeight->height != targetB->height ||
 	    targetA->packOrder < 0 || targetA->packOrder > 3 || targetB->packOrder < 0 || targetB->packOrder > 3)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: targets must be device images of one size");
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: targets must be images of one size");
 	cudaSetDevice(ctx->device);
 	if (count == 0) return DSRG_OK;
 	std::vector<SpriteData> table(count);
@@ -558,6 +642,33 @@ int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 		d.left = s.left; d.top = s.top; d.offset = s.offset;
 		if (s.width * s.height_ > largest) largest = s.width * s.height_;
 	}
+	// the targets and every sprite's three sources where the kernels reach them
+	std::vector<CallMemory> mem = {call_image(targetHeight, true), call_image(targetA, true), call_image(targetB, true)};
+	std::vector<const dsrg_image *> images = {targetHeight, targetA, targetB};
+	for (int32_t i = 0; i < count; i++) {
+		const dsrg_sprite &s = sprites[i];
+		const void *sources[3] = {s.height, s.colorA, s.colorB};
+		const int32_t strides[3] = {s.heightStrideBytes, s.colorAStrideBytes, s.colorBStrideBytes};
+		for (int k = 0; k < 3; k++) {
+			CallMemory m;
+			m.host = sources[k];
+			m.rowBytes = (size_t)s.width * 4;
+			m.strideBytes = (size_t)strides[k];
+			m.rows = (size_t)s.height_;
+			m.onDevice = s.onDevice != 0;
+			mem.push_back(m);
+			images.push_back(nullptr);
+		}
+	}
+	const int placed = place(ctx, mem);
+	if (placed != DSRG_OK) return placed;
+	for (int32_t i = 0; i < count; i++) {
+		SpriteData &d = table[i];
+		const CallMemory *m = &mem[3 + 3 * (size_t)i];
+		d.height = (const float *)m[0].device; d.heightStride = stride_of(m[0]);
+		d.colorA = (const uint32_t *)m[1].device; d.aStride = stride_of(m[1]);
+		d.colorB = (const uint32_t *)m[2].device; d.bStride = stride_of(m[2]);
+	}
 	const int32_t width = targetHeight->width, height = targetHeight->height;
 	const size_t pixels = (size_t)width * height;
 	DSRG_CUDA_TRY(ctx, ctx->keys.reserve(pixels));
@@ -568,19 +679,17 @@ int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	const int32_t blocksPerSprite = (largest + 255) / 256 < 64 ? (largest + 255) / 256 : 64;
 	for (int32_t first = 0; first < count; first += 65535) { // grid y is limited to 65535 sprites per launch
 		const int32_t n = count - first < 65535 ? count - first : 65535;
-		higher_keys_kernel<<<dim3(blocksPerSprite, n), 256, 0, ctx->stream>>>(deviceTable, first, count, (const float *)targetHeight->data,
-		                                                                     targetHeight->strideBytes / 4, width, height, ctx->keys.ptr);
+		higher_keys_kernel<<<dim3(blocksPerSprite, n), 256, 0, ctx->stream>>>(deviceTable, first, count, (const float *)mem[0].device,
+		                                                                     stride_of(mem[0]), width, height, ctx->keys.ptr);
 		add_launches(1);
 	}
 	const dim3 grid((width + 255) / 256, height);
-	higher_resolve_kernel<<<grid, 256, 0, ctx->stream>>>(deviceTable, ctx->keys.ptr, (float *)targetHeight->data,
-	                                                     targetHeight->strideBytes / 4, (uint32_t *)targetA->data,
-	                                                     targetA->strideBytes / 4, targetA->packOrder, (uint32_t *)targetB->data,
-	                                                     targetB->strideBytes / 4, targetB->packOrder, width, height);
+	higher_resolve_kernel<<<grid, 256, 0, ctx->stream>>>(deviceTable, ctx->keys.ptr, (float *)mem[0].device, stride_of(mem[0]),
+	                                                     (uint32_t *)mem[1].device, stride_of(mem[1]), targetA->packOrder,
+	                                                     (uint32_t *)mem[2].device, stride_of(mem[2]), targetB->packOrder, width, height);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-	return DSRG_OK;
+	return finish(ctx, mem, images.data());
 }
 
 } // extern "C"

@@ -180,6 +180,7 @@ extern "C" int dsrg_model_render_depth_noalloc(dsrg_context ctx, dsrg_model m, c
 	config.ctasPerSm = ctx->ctasPerSm;
 	config.resolveMode = 0; // depth only: the per-pixel depth resolve
 	launch_raster(params, fb, bins, config, true, stream);
+	DSRG_CUDA_TRY(ctx, take_enqueue_error());
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
 	uint32_t errorBits = 0;
 	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&errorBits, control + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));

@@ -73,6 +73,12 @@ size_t layout_tables(TaskParams *tasks, size_t taskCount, FrameTarget *frames, s
 	params.totalTriangles = triangles;
 	params.totalTiles = tiles;
 	params.depthOnly = depthOnly ? 1 : 0;
+	params.oddDepthFrames = 0;
+	params.maxTilesX = 0;
+	for (size_t i = 0; i < frameCount; i++) {
+		if ((frames[i].height & 1) && frames[i].depth) params.oddDepthFrames++;
+		params.maxTilesX = std::max(params.maxTilesX, frames[i].tilesX);
+	}
 	return bytes;
 }
 
@@ -111,7 +117,9 @@ static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &ke
 			g.key.assign(k, k + sizeof(key));
 		}
 		launches();
-		return cudaGetLastError();
+		const cudaError_t enqueued = take_enqueue_error();
+		const cudaError_t launched = cudaGetLastError();
+		return enqueued != cudaSuccess ? enqueued : launched;
 	}
 	if (g.exec) {
 		add_launches(g.launches);
@@ -121,7 +129,9 @@ static cudaError_t run_phase(dsrg_context ctx, PhaseGraph &g, const PhaseKey &ke
 	cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
 	if (e != cudaSuccess) return e;
 	launches();
-	const cudaError_t launched = cudaGetLastError(); // a launch refused while capturing
+	const cudaError_t enqueued = take_enqueue_error();
+	const cudaError_t refused = cudaGetLastError(); // a launch refused while capturing
+	const cudaError_t launched = enqueued != cudaSuccess ? enqueued : refused;
 	cudaGraph_t graph = nullptr;
 	e = cudaStreamEndCapture(ctx->stream, &graph);
 	if (e != cudaSuccess) return e;
@@ -166,6 +176,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	params.smallWidth = ctx->smallWidth;
 	params.tileQueue = ctx->control.ptr;
 	params.fragments = nullptr;
+	params.walked = ctx->fragmentCounter.ptr + 1;
 	if (ctx->counting && !job.clearCounters) {
 		params.fragments = ctx->fragmentCounter.ptr;
 	} else if (ctx->counting) {
@@ -353,6 +364,7 @@ int occlude_enqueue(dsrg_context ctx, BatchJob &job) {
 	fb.errorFlag = (int32_t *)(ctx->control.ptr + 1);
 	launch_project(params, fb, stream);
 	launch_setup_occlude(params, fb, stream);
+	TRY(take_enqueue_error());
 	TRY(cudaGetLastError());
 	// the page-locked tables are rewritten by the next batch: wait for their copy (and the grid)
 	TRY(cudaStreamSynchronize(stream));

@@ -98,6 +98,19 @@ __device__ __forceinline__ void quad_lanes(float start, float dx, float dy, cons
 	}
 }
 
+// Whether the quad at x lies in the pair's run of full quads (fillerTemplates.h:357-364).
+__device__ __forceinline__ bool full_quad(const RowPair &rp, int32_t x) {
+	return rp.ibe > rp.ibs && x >= rp.ibs && x < rp.ibe;
+}
+
+// The last row of a target of odd height.  Its row pair's lower row lies outside the image: the
+// reference empties that row's interval but bounds the run of full quads with the row as it was,
+// and points the lower row's pixels at the upper row (fillerTemplates.h:285-306).  In that run the
+// lower lanes are therefore tested against and written into the upper row, after the upper lanes.
+__device__ __forceinline__ bool odd_last_row(int32_t py, int32_t height) {
+	return (height & 1) != 0 && py == height - 1;
+}
+
 // Whether lane l of the quad at x is drawn (clipPixels, fillerTemplates.h:92-106); full quads draw all four.
 __device__ __forceinline__ bool lane_covered(const RowPair &rp, int32_t x, bool edge, int l) {
 	if (!edge) return true;

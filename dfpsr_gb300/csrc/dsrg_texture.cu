@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "dsrg_internal.h"
+#include "dsrg_shade.h"
 
 using namespace dsrg;
 
@@ -25,6 +26,7 @@ struct ResizeItem {
 	int32_t srcStride, dstStride; // in texels
 	int32_t srcWidth, srcHeight, width, height;
 	int32_t mode;                 // RESIZE_*
+	int32_t srcOrder;             // pack order of the source (the target is RGBA)
 	uint32_t first;               // first work item (target texel) of this resize in the launch
 };
 
@@ -64,6 +66,9 @@ __device__ __forceinline__ uint32_t read_clamped(const ResizeItem &r, int32_t x,
 
 __device__ __forceinline__ uint32_t channel(uint32_t c, int ch) { return (c >> (ch * 8)) & 0xFFu; }
 
+// Channel ch (0 red .. 3 alpha) of a pixel packed in the given order (image_unpack).
+__device__ __forceinline__ uint32_t channel_of(uint32_t c, int32_t order, int ch) { return (c >> pack_shift(order, ch)) & 0xFFu; }
+
 // The 16.16 sampling position of target index i: start = offset / 2 - 32768 (Sampler::Linear),
 // advanced by offset = 65536 * source / target per target pixel, clamped at 0.
 __device__ __forceinline__ uint32_t sample_position(int32_t source, int32_t target, int32_t i) {
@@ -79,9 +84,12 @@ __global__ void resize_kernel(const ResizeItem *__restrict__ items, int32_t coun
 		const int32_t x = (int32_t)(local % (uint32_t)r.width), y = (int32_t)(local / (uint32_t)r.width);
 		uint32_t out = 0;
 		if (r.mode == RESIZE_COPY) {
-			out = r.src[(size_t)y * r.srcStride + x];
+			// draw_copy, repacking another order channel by channel (imageImpl_drawCopy, drawAPI.cpp:498-520)
+			const uint32_t c = r.src[(size_t)y * r.srcStride + x];
+			for (int ch = 0; ch < 4; ch++) out |= channel_of(c, r.srcOrder, ch) << (ch * 8);
 		} else if (r.mode == RESIZE_VERTICAL) {
-			// mixColorsUniform with an 8-bit weight (the aligned branch of resize_optimized)
+			// mixColorsUniform with an 8-bit weight (the aligned branch of resize_optimized), on the
+			// packed bytes as they lie: a source of another order keeps its byte order here
 			const uint32_t sampleY = sample_position(r.srcHeight, r.height, y);
 			uint32_t upperY = sampleY >> 16, lowerY = upperY + 1;
 			if (upperY >= (uint32_t)r.srcHeight) upperY = (uint32_t)r.srcHeight - 1;
@@ -94,7 +102,7 @@ __global__ void resize_kernel(const ResizeItem *__restrict__ items, int32_t coun
 			const uint32_t leftX = sampleX >> 16, rightRatio = sampleX & 0xFFFFu, leftRatio = 65536u - rightRatio;
 			const uint32_t a = read_clamped(r, (int32_t)leftX, y), b = read_clamped(r, (int32_t)(leftX + 1), y);
 			for (int ch = 0; ch < 4; ch++) {
-				const uint32_t v = (channel(a, ch) * leftRatio + channel(b, ch) * rightRatio) >> 16;
+				const uint32_t v = (channel_of(a, r.srcOrder, ch) * leftRatio + channel_of(b, r.srcOrder, ch) * rightRatio) >> 16;
 				out |= (v > 255u ? 255u : v) << (ch * 8);
 			}
 		} else {
@@ -106,8 +114,8 @@ __global__ void resize_kernel(const ResizeItem *__restrict__ items, int32_t coun
 			const uint32_t ll = read_clamped(r, (int32_t)leftX, (int32_t)(upperY + 1));
 			const uint32_t lr = read_clamped(r, (int32_t)(leftX + 1), (int32_t)(upperY + 1));
 			for (int ch = 0; ch < 4; ch++) {
-				const uint32_t upper = (channel(ul, ch) * leftRatio + channel(ur, ch) * rightRatio) >> 16;
-				const uint32_t lower = (channel(ll, ch) * leftRatio + channel(lr, ch) * rightRatio) >> 16;
+				const uint32_t upper = (channel_of(ul, r.srcOrder, ch) * leftRatio + channel_of(ur, r.srcOrder, ch) * rightRatio) >> 16;
+				const uint32_t lower = (channel_of(ll, r.srcOrder, ch) * leftRatio + channel_of(lr, r.srcOrder, ch) * rightRatio) >> 16;
 				const uint32_t v = (upper * upperRatio + lower * lowerRatio) >> 16;
 				out |= (v > 255u ? 255u : v) << (ch * 8);
 			}
@@ -171,7 +179,7 @@ int dsrg_texture_create_many(dsrg_context ctx, int32_t count, const dsrg_image *
 			return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture of an empty image!");
 		if (im.width > 32768 || im.height > 32768)
 			return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "Tried to create a texture exceeding the maximum texture dimensions of 32768 x 32768 pixels!");
-		if (im.packOrder != 0) return fail(ctx, DSRG_ERROR_UNSUPPORTED, "texture images must be in the RGBA pack order");
+		if (im.packOrder < 0 || im.packOrder > 3) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "texture image: unknown pack order");
 		if (im.strideBytes < im.width * 4 || (im.strideBytes & 3)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "texture image: invalid stride");
 		Plan &p = plans[i];
 		p.lw = find_log2_size((uint32_t)im.width);
@@ -212,7 +220,7 @@ int dsrg_texture_create_many(dsrg_context ctx, int32_t count, const dsrg_image *
 		tex->context = ctx;
 		made.push_back(tex);
 		const Plan &p = plans[i];
-		if (cudaMalloc((void **)&tex->pixels, sizeof(uint32_t) * p.pixelCount) != cudaSuccess)
+		if (device_alloc((void **)&tex->pixels, sizeof(uint32_t) * p.pixelCount) != cudaSuccess)
 			return cleanup(DSRG_ERROR_OUT_OF_MEMORY, "cudaMalloc failed for a texture pyramid");
 		tex->pixelCount = p.pixelCount;
 		const uint32_t f[9] = {p.lw, p.lh, p.maxMip, p.startOffset, p.highest - 1, (1u << (p.lw - p.maxMip)) - 1,
@@ -263,12 +271,14 @@ int dsrg_texture_create_many(dsrg_context ctx, int32_t count, const dsrg_image *
 			h.src = source[i]; h.srcStride = sourceStride[i]; h.srcWidth = im.width; h.srcHeight = im.height;
 			h.dst = temp + p.tempOffset; h.dstStride = p.width; h.width = p.width; h.height = im.height;
 			h.mode = resize_mode(im.width, im.height, p.width, im.height);
+			h.srcOrder = im.packOrder;
 			h.first = horizontalTotal;
 			horizontalTotal += (uint32_t)(p.width * im.height);
 			horizontal.push_back(h);
 			last.src = h.dst; last.srcStride = p.width; last.srcWidth = p.width; last.srcHeight = im.height;
 		} else {
 			last.src = source[i]; last.srcStride = sourceStride[i]; last.srcWidth = im.width; last.srcHeight = im.height;
+			last.srcOrder = im.packOrder; // a two-step upscale's second step reads the RGBA half (srcOrder 0)
 		}
 		last.dst = level0Pixels; last.dstStride = p.width; last.width = p.width; last.height = p.height;
 		last.mode = resize_mode(last.srcWidth, last.srcHeight, p.width, p.height);
@@ -342,6 +352,53 @@ int dsrg_texture_create(dsrg_context ctx, const uint32_t *pixels, int32_t width,
 	image.packOrder = 0;
 	image.onDevice = 0;
 	return dsrg_texture_create_many(ctx, 1, &image, &resolutions, out);
+}
+
+int dsrg_texture_upload(dsrg_context ctx, const uint32_t *pyramid, uint32_t log2width, uint32_t log2height, uint32_t maxMipLevel,
+                        dsrg_texture *out) {
+	if (!ctx || !out || !pyramid) return DSRG_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	// the fields of the Texture constructor (implementation/image/Texture.h:66-101)
+	if (log2width > 15u || log2height > 15u || maxMipLevel > log2width || maxMipLevel > log2height || maxMipLevel > 15u)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_texture_upload: invalid pyramid dimensions");
+	Plan p;
+	memset(&p, 0, sizeof(p));
+	p.lw = log2width; p.lh = log2height; p.maxMip = maxMipLevel;
+	p.highest = 1u << (p.lw + p.lh);
+	uint64_t pixelCount = 0;
+	uint32_t levelCount = p.highest;
+	for (int32_t level = (int32_t)p.maxMip; level >= 0; level--) { pixelCount |= levelCount; levelCount >>= 2; }
+	p.pixelCount = (uint32_t)pixelCount;
+	p.startOffset = (uint32_t)pixelCount & ~p.highest;
+	cudaSetDevice(ctx->device);
+	dsrg_texture tex = new (std::nothrow) dsrg_texture_s();
+	if (!tex) return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "texture allocation failed");
+	tex->context = ctx;
+	if (device_alloc((void **)&tex->pixels, sizeof(uint32_t) * p.pixelCount) != cudaSuccess) {
+		delete tex;
+		return fail(ctx, DSRG_ERROR_OUT_OF_MEMORY, "cudaMalloc failed for a texture pyramid");
+	}
+	tex->pixelCount = p.pixelCount;
+	const uint32_t f[9] = {p.lw, p.lh, p.maxMip, p.startOffset, p.highest - 1, (1u << (p.lw - p.maxMip)) - 1,
+	                       (1u << (p.lh - p.maxMip)) - 1, (1u << p.lw) - 1, (1u << p.lh) - 1};
+	memcpy(tex->fields, f, sizeof(f));
+	TextureData &d = tex->data;
+	memset(&d, 0, sizeof(d));
+	d.pixels = tex->pixels;
+	d.log2width = p.lw; d.log2height = p.lh; d.maxMipLevel = p.maxMip; d.startOffset = p.startOffset;
+	d.maxLevelMask = p.highest - 1;
+	d.maxWidthAndMask = (1u << p.lw) - 1; d.maxHeightAndMask = (1u << p.lh) - 1;
+	d.floatMaxWidth = (float)(1u << p.lw); d.floatMaxHeight = (float)(1u << p.lh);
+	d.exists = 1;
+	const cudaError_t e1 = cudaMemcpyAsync(tex->pixels, pyramid, sizeof(uint32_t) * p.pixelCount, cudaMemcpyHostToDevice, ctx->stream);
+	const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+	if (e1 != cudaSuccess || e2 != cudaSuccess) {
+		cudaFree(tex->pixels);
+		delete tex;
+		return fail(ctx, DSRG_ERROR_CUDA, std::string("dsrg_texture_upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+	}
+	*out = tex;
+	return DSRG_OK;
 }
 
 int dsrg_texture_destroy(dsrg_texture tex) {

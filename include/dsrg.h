@@ -92,6 +92,11 @@ void *dsrg_context_stream(dsrg_context context);
  * width*height uint32, write the per-pixel fragment count there); 0 turns it off. */
 int dsrg_context_set_counting(dsrg_context context, int32_t counting, uint32_t *deviceCoverage);
 int dsrg_context_get_stats(dsrg_context context, dsrg_stats *out);
+/* Fragments the tile kernels have depth-tested on this context since it was created, counted
+ * whether or not counting is on (no reference counterpart).  With counting off, early depth
+ * culling skips fragments that cannot win, so the difference of two readings around a render is
+ * the work that render actually walked; with counting on it equals the render's fragments. */
+int dsrg_context_walked_fragments(dsrg_context context, uint64_t *out);
 
 /* ---- textures: texture_create_RgbaU8(image, resolutions) (api/textureAPI.h:450-465,
  * api/textureAPI.cpp:89-131), built on the GPU: the image is resized linearly to the next powers
@@ -105,6 +110,12 @@ int dsrg_texture_create(dsrg_context context, const uint32_t *pixels, int32_t wi
  * as one launch over all images.  On failure no texture is made and out[] is all null. */
 int dsrg_texture_create_many(dsrg_context context, int32_t count, const dsrg_image *images, const int32_t *resolutions,
                              dsrg_texture *out);
+/* A TextureRgbaU8 that already exists, as the reference holds it (implementation/image/Texture.h:42-102:
+ * impl_log2width, impl_log2height, impl_maxMipLevel and the impl_buffer pyramid, smallest level
+ * first): the pyramid is copied to the GPU as it is, so a texture made or edited by the reference's
+ * own texture API draws the same texels.  pyramid: host memory. */
+int dsrg_texture_upload(dsrg_context context, const uint32_t *pyramid, uint32_t log2width, uint32_t log2height,
+                        uint32_t maxMipLevel, dsrg_texture *out);
 int dsrg_texture_destroy(dsrg_texture texture);
 /* Copies the pyramid (smallest level first) to host memory; fields = log2width, log2height,
  * maxMipLevel, startOffset, maxLevelMask, minWidthOrMask, minHeightOrMask, maxWidthAndMask,
@@ -119,6 +130,11 @@ int dsrg_model_create(dsrg_context context, const float *positions, int32_t poin
                       const float *texCoords, const float *colors, int32_t polygonCount, dsrg_texture diffuse,
                       dsrg_texture light, int32_t filter, dsrg_model *out);
 int dsrg_model_destroy(dsrg_model model);
+/* The model's bounding box as model_getBoundingBox returns it (api/modelAPI.h:138, ModelImpl::minBound /
+ * maxBound): the box the culling and occlusion tests of model_render and renderer_giveTask use.
+ * dsrg_model_create sets it from the points as the reference grows it point by point; a caller
+ * mirroring a reference model whose points were edited passes the reference's box here. */
+int dsrg_model_set_bound(dsrg_model model, const float *minimum, const float *maximum);
 
 /* ---- rendering ---- */
 /* model_render (api/modelAPI.h:285, api/modelAPI.cpp:197-201): draws the model into the colour
@@ -197,22 +213,34 @@ int dsrg_renderer_has_occluders(dsrg_renderer renderer);
 int dsrg_renderer_get_occlusion_grid(dsrg_renderer renderer, float *out, int32_t capacity, int32_t *gridWidth,
                                      int32_t *gridHeight);
 
+/* ---- testing the failure paths (no reference counterpart) ----
+ * The device allocation `after` allocations from now (0: the next one) fails as it would on an
+ * exhausted GPU (cudaErrorMemoryAllocation), once; the call that needed it returns
+ * DSRG_ERROR_OUT_OF_MEMORY and leaves its context usable.  A negative value turns it off.
+ * Process-wide, for tests of a caller's error handling. */
+int dsrg_debug_fail_allocation(int64_t after);
+
 /* ---- depth rendering without allocation; this entry point has no counterpart in the reference.
  *
  * For callers that must not allocate GPU memory while they render: a frame loop held to a
  * no-allocation rule after start-up (cudaMalloc and cudaFree synchronise the whole device and
  * can stall unrelated work), or a host that gives the renderer a fixed memory budget up front.
- * It draws what dsrg_model_render_depth draws (model_renderDepth, api/modelAPI.h:291) and calls
- * no cudaMalloc, cudaFree or other allocating routine.  Its intermediate buffers live in one
- * static device array of DSRG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
- * until the process exits.
+ * It draws what dsrg_model_render_depth draws and calls no cudaMalloc, cudaFree or other
+ * allocating routine.  Its intermediate buffers live in one static device array of
+ * DSRG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps until the process exits.
+ * The CUDA driver reserves that array when it loads the library's device code on a device (with
+ * lazy module loading, at the first call that needs it), so a caller with a fixed budget makes
+ * one warm-up call at start-up; later calls take no device memory.
  *   - depth must be device memory (onDevice = 1) of at most DSRG_NOALLOC_MAX_SIDE pixels on a
  *     side; the model at most DSRG_NOALLOC_MAX_POINTS points and DSRG_NOALLOC_MAX_TRIANGLES fan
  *     triangles.  Larger inputs, or a view whose visible triangles need more than
  *     DSRG_NOALLOC_MAX_ROWS pixel rows or DSRG_NOALLOC_MAX_BIN_ENTRIES (tile, triangle) pairs,
  *     are rejected with DSRG_ERROR_UNSUPPORTED and a message naming the limit.
- *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress);
- *     make that first call before any stream capture.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ *     and keeps it for the life of the process; make that first call before any stream capture.
+ *     A device reset (cudaDeviceReset) inside the process is not supported afterwards.
+ *   - Each call returns with its work finished: it reads counts back to the host between its
+ *     kernels and waits for them on the context's stream.
  *   - Every call on a device shares the same array and leaves its contents behind (each call
  *     clears what it needs cleared); calls whose GPU work overlaps, from any context or thread,
  *     race on it, so they must be serialised. */
@@ -337,11 +365,17 @@ int dsrg_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t inde
  * its camera is perspective with slope 1 at the cube's resolution.  Host only. */
 int dsrg_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]);
 
-/* setDirectedLight (add = 0) / addDirectedLight (add = 1) (lightAPI.cpp:23-74). */
+/* The light passes and draw_higher take their images where the caller has them, as the
+ * reference's functions take host images (lightAPI.cpp:23-323, drawAPI.cpp:872-900): device memory
+ * (onDevice = 1), page-locked host memory (read and written in place through its device address) or
+ * pageable host memory (copied to the GPU and the written images back inside the call).  The same
+ * holds for shadow cubes and sprite sources, told apart by their pointers.
+ *
+ * setDirectedLight (add = 0) / addDirectedLight (add = 1) (lightAPI.cpp:23-74). */
 int dsrg_light_directed(dsrg_context context, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
                         const float direction[3], float intensity, const int32_t color[3], int32_t add);
 
-/* One addPointLight call (lightAPI.cpp:169-285).  shadowCube: device image of cubeWidth x 6 cubeWidth
+/* One addPointLight call (lightAPI.cpp:169-285).  shadowCube: an image of cubeWidth x 6 cubeWidth
  * floats (six reciprocal-depth faces, no row padding) or null for a light without shadows. */
 typedef struct {
 	float position[3]; /* relative to the camera, as the reference takes it */
@@ -387,7 +421,8 @@ typedef struct {
 int dsrg_dense_render_many(dsrg_context context, const dsrg_dense_instance *instances, int32_t count, const dsrg_ortho_view *view,
                            const dsrg_image *height, const dsrg_image *diffuse, const dsrg_image *normal, int32_t highQuality);
 
-/* One draw_higher source (F32 height + two RGBA images of the same size, device memory). */
+/* One draw_higher source (F32 height + two RGBA images of the same size).  onDevice = 1 when the
+ * three are device memory, 0 when they are host memory (page-locked or pageable). */
 typedef struct {
 	const float *height;
 	const uint32_t *colorA;
@@ -397,6 +432,7 @@ typedef struct {
 	int32_t colorAPackOrder, colorBPackOrder;
 	int32_t left, top;
 	float offset;
+	int32_t onDevice;
 } dsrg_sprite;
 /* draw_higher(targetHeight, sourceHeight, targetA, sourceA, targetB, sourceB, left, top, offset)
  * (api/drawAPI.cpp:872-900, 946-981) for every sprite in order, in one pass: a pixel ends with the

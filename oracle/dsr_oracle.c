@@ -481,10 +481,16 @@ void or_texture_generate_pyramid(or_texture *t) {
 	}
 }
 
-/* ---- filter_resize(image, Sampler::Linear, width, height) of RGBA images (api/filterAPI.cpp:66-311,
- * 852-859), for images that are neither sub-images nor of another pack order, as texture creation
+/* PackOrder byte indices of red, green, blue, alpha (image/PackOrder.h:80-92). */
+static const int PACK_INDEX[4][4] = {{0, 1, 2, 3}, {2, 1, 0, 3}, {1, 2, 3, 0}, {3, 2, 1, 0}};
+
+/* ---- filter_resize(image, Sampler::Linear, width, height) (api/filterAPI.cpp:66-311, 852-859) into
+ * an RGBA image, for source images in any pack order that are not sub-images, as texture creation
  * passes them.  Sampling positions are 16.16 fixed point: offset = 65536 * source / target pixels,
- * start = offset / 2 - 32768, clamped at 0, the integer part the left or upper sample. */
+ * start = offset / 2 - 32768, clamped at 0, the integer part the left or upper sample.  Every path
+ * reads the source's channels through its pack order (image_readPixel_clamp unpacks) and packs
+ * RGBA, except the vertical-only path, whose aligned branch mixes the packed bytes as they lie
+ * (mixColorsUniform), so a source of another order keeps its byte order there. */
 
 static uint32_t resize_read(const uint32_t *img, int32_t w, int32_t h, int32_t x, int32_t y) { /* image_readPixel_clamp */
 	if (x < 0) x = 0;
@@ -493,6 +499,9 @@ static uint32_t resize_read(const uint32_t *img, int32_t w, int32_t h, int32_t x
 	if (y > h - 1) y = h - 1;
 	return img[(size_t)y * w + x];
 }
+
+/* Channel ch (0 red .. 3 alpha) of a pixel packed in the given order (image_unpack). */
+static uint32_t resize_channel(uint32_t c, int order, int ch) { return (c >> (PACK_INDEX[order][ch] * 8)) & 0xFFu; }
 
 static int32_t resize_offset(int32_t source, int32_t target) { return (int32_t)((65536u * (uint32_t)source) / (uint32_t)target); }
 
@@ -523,7 +532,7 @@ static uint32_t saturate_pack(const uint32_t c[4]) { /* image_saturateAndPack, R
 }
 
 /* Horizontal only (resize_optimized): 16-bit weights per channel. */
-static void resize_horizontal(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw) {
+static void resize_horizontal(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int order) {
 	int32_t offsetX = resize_offset(sw, w);
 	int32_t startX = (int32_t)((uint32_t)(offsetX / 2) - 32768u);
 	for (int32_t y = 0; y < h; y++) {
@@ -533,7 +542,8 @@ static void resize_horizontal(uint32_t *dst, int32_t w, int32_t h, const uint32_
 			uint32_t leftX = sampleX >> 16;
 			uint32_t rightRatio = sampleX & 0xFFFFu, leftRatio = 65536u - rightRatio;
 			uint32_t l = resize_read(src, sw, h, (int32_t)leftX, y), r = resize_read(src, sw, h, (int32_t)(leftX + 1), y), c[4];
-			for (int ch = 0; ch < 4; ch++) c[ch] = (((l >> (ch * 8)) & 0xFFu) * leftRatio + ((r >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
+			for (int ch = 0; ch < 4; ch++)
+				c[ch] = (resize_channel(l, order, ch) * leftRatio + resize_channel(r, order, ch) * rightRatio) >> 16;
 			dst[(size_t)y * w + x] = saturate_pack(c);
 			readX += offsetX;
 		}
@@ -541,7 +551,7 @@ static void resize_horizontal(uint32_t *dst, int32_t w, int32_t h, const uint32_
 }
 
 /* Both dimensions (resize_reference with samplePixel<true>): bilinear with 16-bit weights. */
-static void resize_both(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+static void resize_both(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh, int order) {
 	int32_t offsetX = resize_offset(sw, w), offsetY = resize_offset(sh, h);
 	int32_t startX = (int32_t)((uint32_t)(offsetX / 2) - 32768u);
 	int32_t readY = (int32_t)((uint32_t)(offsetY / 2) - 32768u);
@@ -556,8 +566,8 @@ static void resize_both(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src
 			uint32_t ll = resize_read(src, sw, sh, (int32_t)leftX, (int32_t)(upperY + 1)), lr = resize_read(src, sw, sh, (int32_t)(leftX + 1), (int32_t)(upperY + 1));
 			uint32_t c[4];
 			for (int ch = 0; ch < 4; ch++) {
-				uint32_t upper = (((ul >> (ch * 8)) & 0xFFu) * leftRatio + ((ur >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
-				uint32_t lower = (((ll >> (ch * 8)) & 0xFFu) * leftRatio + ((lr >> (ch * 8)) & 0xFFu) * rightRatio) >> 16;
+				uint32_t upper = (resize_channel(ul, order, ch) * leftRatio + resize_channel(ur, order, ch) * rightRatio) >> 16;
+				uint32_t lower = (resize_channel(ll, order, ch) * leftRatio + resize_channel(lr, order, ch) * rightRatio) >> 16;
 				c[ch] = (upper * upperRatio + lower * lowerRatio) >> 16;
 			}
 			dst[(size_t)y * w + x] = saturate_pack(c);
@@ -567,25 +577,40 @@ static void resize_both(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src
 	}
 }
 
-/* resize_optimized's choice for one step (filterAPI.cpp:157-260). */
-static void resize_step(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
-	if (sw == w && sh == h) memcpy(dst, src, sizeof(uint32_t) * (size_t)w * (size_t)h);
+/* resize_optimized's choice for one step (filterAPI.cpp:157-260); the copy repacks another order
+ * channel by channel (imageImpl_drawCopy, drawAPI.cpp:498-520). */
+static void resize_step(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh, int order) {
+	if (sw == w && sh == h) {
+		if (order == 0) {
+			memcpy(dst, src, sizeof(uint32_t) * (size_t)w * (size_t)h);
+		} else {
+			for (size_t i = 0; i < (size_t)w * (size_t)h; i++) {
+				uint32_t out = 0;
+				for (int ch = 0; ch < 4; ch++) out |= resize_channel(src[i], order, ch) << (ch * 8);
+				dst[i] = out;
+			}
+		}
+	}
 	else if (sw == w) resize_vertical(dst, w, h, src, sh);
-	else if (sh == h) resize_horizontal(dst, w, h, src, sw);
-	else resize_both(dst, w, h, src, sw, sh);
+	else if (sh == h) resize_horizontal(dst, w, h, src, sw, order);
+	else resize_both(dst, w, h, src, sw, sh, order);
 }
 
 /* resizeToTarget (filterAPI.cpp:298-314): a wider and taller target goes through a horizontal step
- * to the target's width first. */
-void or_filter_resize_linear(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+ * to the target's width first, into an RGBA image. */
+void or_filter_resize_linear_ordered(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh, int32_t srcOrder) {
 	if (w != sw && h > sh) {
 		uint32_t *temp = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)w * (size_t)sh);
-		resize_step(temp, w, sh, src, sw, sh);
-		resize_step(dst, w, h, temp, w, sh);
+		resize_step(temp, w, sh, src, sw, sh, srcOrder);
+		resize_step(dst, w, h, temp, w, sh, 0);
 		free(temp);
 	} else {
-		resize_step(dst, w, h, src, sw, sh);
+		resize_step(dst, w, h, src, sw, sh, srcOrder);
 	}
+}
+
+void or_filter_resize_linear(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh) {
+	or_filter_resize_linear_ordered(dst, w, h, src, sw, sh, 0);
 }
 
 /* findLog2Size (textureAPI.cpp:30-40). */
@@ -596,14 +621,19 @@ static uint32_t find_log2_size(uint32_t size) {
 
 /* texture_create_RgbaU8(image, resolutions) (textureAPI.cpp:89-110, 112-131): the image resized
  * linearly to the next powers of two, then the pyramid. */
-int or_texture_create_from_image(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions) {
-	if (resolutions < 1 || width < 1 || height < 1 || width > 32768 || height > 32768) return -1;
+int or_texture_create_from_image_ordered(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions,
+                                         int32_t packOrder) {
+	if (resolutions < 1 || width < 1 || height < 1 || width > 32768 || height > 32768 || packOrder < 0 || packOrder > 3) return -1;
 	uint32_t lw = find_log2_size((uint32_t)width), lh = find_log2_size((uint32_t)height);
 	if (or_texture_init_empty(t, lw, lh, (uint32_t)(resolutions - 1))) return -1;
 	uint32_t base = or_texture_pixel_offset_to_layer(t, 0);
-	or_filter_resize_linear(t->pixels + base, (int32_t)1 << lw, (int32_t)1 << lh, level0, width, height);
+	or_filter_resize_linear_ordered(t->pixels + base, (int32_t)1 << lw, (int32_t)1 << lh, level0, width, height, packOrder);
 	or_texture_generate_pyramid(t);
 	return 0;
+}
+
+int or_texture_create_from_image(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions) {
+	return or_texture_create_from_image_ordered(t, level0, width, height, resolutions, 0);
 }
 
 /* weightColors (textureAPI.h:242-255): per channel (a*wa + b*wb) >> 8. */
@@ -776,9 +806,6 @@ static void shade_quad(const shade_data *d, const float wa[4], const float wb[4]
 	}
 }
 
-/* PackOrder byte indices of red, green, blue, alpha (image/PackOrder.h:80-92). */
-static const int PACK_INDEX[4][4] = {{0, 1, 2, 3}, {2, 1, 0, 3}, {1, 2, 3, 0}, {3, 2, 1, 0}};
-
 /* packOrder_floatToSaturatedByte with an order (PackOrder.h:204-212). */
 static uint32_t pack_saturated(const float rgba[4], int packOrder) {
 	uint32_t out = 0;
@@ -809,6 +836,10 @@ typedef struct {
 static void fill_quad(target *tg, const shade_data *sd, int clipSides, int colorWrite, int depthRead, int depthWrite,
                       int alphaFilter, int affine, int32_t x, int32_t yUpper, int32_t yLower, row_interval upper, row_interval lower,
                       const float depth[4], const float wa[4], const float wb[4], const float wc[4]) {
+	/* Lanes of a missing lower row (the last row pair of an odd height) point at the upper row: a
+	 * full quad tests and writes them there, but they add no (pixel, triangle) pair of their own to
+	 * the fragment statistics, whose upper lane already holds that pair. */
+	const int lowerAliased = (yLower == yUpper) && clipSides == 0;
 	int clip[4];
 	if (clipSides) {
 		int32_t x2 = x + 1;
@@ -833,7 +864,7 @@ static void fill_quad(target *tg, const shade_data *sd, int clipSides, int color
 			}
 		}
 		vis[l] = clip[l] && front;
-		if (clip[l]) {
+		if (clip[l] && !(lowerAliased && l >= 2)) {
 			tg->fragments++;
 			if (tg->stats && tg->stats->coverage) tg->stats->coverage[idx[l]]++;
 		}

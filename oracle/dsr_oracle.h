@@ -65,6 +65,9 @@ typedef struct {
 /* ---- textures ---- */
 int or_texture_init_empty(or_texture *t, uint32_t log2w, uint32_t log2h, uint32_t maxMipLevel);
 int or_texture_create_from_image(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions);
+/* The same from an image in pack order packOrder (0..3, PackOrder.h:37-42). */
+int or_texture_create_from_image_ordered(or_texture *t, const uint32_t *level0, int32_t width, int32_t height, int32_t resolutions,
+                                         int32_t packOrder);
 /* filter_resize(image, Sampler::Linear, w, h) of a dense RGBA image (api/filterAPI.cpp:852-859). */
 void or_filter_resize_linear(uint32_t *dst, int32_t w, int32_t h, const uint32_t *src, int32_t sw, int32_t sh);
 void or_texture_free(or_texture *t);

@@ -63,6 +63,7 @@ def lib():
         P = C.c_void_p
         l.or_texture_init_empty.argtypes = [C.POINTER(Texture), C.c_uint32, C.c_uint32, C.c_uint32]
         l.or_texture_create_from_image.argtypes = [C.POINTER(Texture), P, C.c_int32, C.c_int32, C.c_int32]
+        l.or_texture_create_from_image_ordered.argtypes = [C.POINTER(Texture), P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         l.or_texture_free.argtypes = [C.POINTER(Texture)]
         l.or_texture_generate_pyramid.argtypes = [C.POINTER(Texture)]
         for name in ("or_texture_pixel_offset_to_layer",):
@@ -113,7 +114,7 @@ def _ptr(a: Optional[np.ndarray]):
 
 
 class OracleTexture:
-    def __init__(self, pixels: Optional[np.ndarray] = None, resolutions: int = 16, empty=None):
+    def __init__(self, pixels: Optional[np.ndarray] = None, resolutions: int = 16, empty=None, pack_order: int = 0):
         self.t = Texture()
         if empty is not None:
             if lib().or_texture_init_empty(C.byref(self.t), *empty):
@@ -121,7 +122,7 @@ class OracleTexture:
         else:
             pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
             h, w = pixels.shape
-            if lib().or_texture_create_from_image(C.byref(self.t), _ptr(pixels), w, h, resolutions):
+            if lib().or_texture_create_from_image_ordered(C.byref(self.t), _ptr(pixels), w, h, resolutions, pack_order):
                 raise ValueError("texture dimensions must be powers of two")
 
     def __del__(self):

@@ -15,7 +15,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("DFPSR_REFERENCE", "/root/reference")
+# the reference checkout: $DFPSR_REFERENCE, else a directory named `reference` beside the repository
+REFERENCE_ROOT = os.environ.get("DFPSR_REFERENCE", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def lib_path(variant: str = "exact") -> str:
@@ -57,6 +58,8 @@ def _load(variant: str):
         P = C.c_void_p
         l.refh_texture_create.argtypes = [P, C.c_int, C.c_int, C.c_int]
         l.refh_texture_create.restype = P
+        l.refh_texture_create_ordered.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
+        l.refh_texture_create_ordered.restype = P
         l.refh_texture_info.argtypes = [P, P, P, C.c_int]
         l.refh_texture_info.restype = C.c_int
         l.refh_texture_free.argtypes = [P]
@@ -96,11 +99,14 @@ def _ptr(a: Optional[np.ndarray]):
 
 
 class RefTexture:
-    def __init__(self, lib, pixels: np.ndarray, resolutions: int):
+    def __init__(self, lib, pixels: np.ndarray, resolutions: int, pack_order: int = 0):
         self.lib = lib
         self.pixels = np.ascontiguousarray(pixels, np.uint32)
         h, w = self.pixels.shape
-        self.handle = lib.refh_texture_create(_ptr(self.pixels), w, h, resolutions)
+        if pack_order:
+            self.handle = lib.refh_texture_create_ordered(_ptr(self.pixels), w, h, resolutions, pack_order)
+        else:
+            self.handle = lib.refh_texture_create(_ptr(self.pixels), w, h, resolutions)
 
     def info(self):
         fields = np.zeros(9, np.uint32)

@@ -100,6 +100,16 @@ int refh_texture_info(void* handle, uint32_t* fields, uint32_t* pixels, int maxP
 	return count;
 }
 
+// The same from an image in pack order packOrder (0..3, PackOrderIndex), created with
+// image_create_RgbaU8_native as a program's own image would be; pixels are the packed values.
+void* refh_texture_create_ordered(const uint32_t* pixels, int width, int height, int resolutions, int packOrder) {
+	AlignedImageRgbaU8 image = image_create_RgbaU8_native(width, height, (PackOrderIndex)packOrder);
+	copyInRgba(image, pixels, width, height);
+	TextureBox* box = new TextureBox();
+	box->texture = texture_create_RgbaU8(image, resolutions);
+	return box;
+}
+
 void refh_texture_free(void* handle) { delete (TextureBox*)handle; }
 
 // polyIndices: polyCount x 4 (index 3 = -1 for triangles); texCoords, colors: polyCount x 4 x 4 floats.

@@ -17,7 +17,8 @@ render_*.npz
     from its sources as the exact (scalar, no-FMA) variant by oracle/Makefile.ref, through
     model_render / renderer_* / model_renderDepth.
 
-Usage: python tests/golden/make_golden.py [reference root, default $DFPSR_REFERENCE or /root/reference]
+Usage: python tests/golden/make_golden.py [reference root, default $DFPSR_REFERENCE or a
+`reference` checkout beside the repository]
 """
 import json
 import os
@@ -296,7 +297,8 @@ def dense_renders():
 
 
 def main():
-    reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DFPSR_REFERENCE", "/root/reference")
+    reference_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(
+        "DFPSR_REFERENCE", os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "..", "reference"))
     from oracle import ref
     os.environ["DFPSR_REFERENCE"] = reference_root
     if not ref.build():

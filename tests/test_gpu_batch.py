@@ -197,3 +197,47 @@ def test_depth_only_frame_and_errors(ctx):
         ctx.set_tuning(threads_per_tile=256, ctas_per_sm=5)
     with pytest.raises(d.DsrgError):
         ctx.set_tuning(resolve=3)
+
+
+def test_benchmarked_batch_frames_match_oracle(ctx):
+    """Frames of the benchmarked mixed-size batch itself (scenes.batch_frames(seed=4321): 256 frames,
+    resolutions 64x64 to 1024x768, 1k-200k random triangles each): the 12 frames with the most
+    triangles at 1024x768 and 640x480 and two of each smaller resolution, rendered together in one
+    batch after the autotuner, each compared bit for bit with the oracle (12 row bands on all
+    host cores, which equals the single-band oracle)."""
+    import os
+    import dfpsr_gb300 as d
+    from oracle import port
+    frames = scenes.batch_frames(seed=4321)
+    by_size = {}
+    for i, s in enumerate(frames):
+        by_size.setdefault((s.width, s.height), []).append(i)
+    chosen = []
+    for size, count in (((1024, 768), 4), ((640, 480), 4), ((256, 256), 2), ((64, 64), 2)):
+        chosen += sorted(by_size[size], key=lambda i: -frames[i].triangle_count)[:count]
+    assert any(frames[i].width == 1024 and frames[i].triangle_count > 100_000 for i in chosen)
+    before = ctx.tuning()
+    try:
+        batch = d.Batch(ctx)
+        imgs = []
+        for k, i in enumerate(chosen):
+            s = frames[i]
+            m = d.Model(ctx, s)
+            imgs.append((np.zeros((s.height, s.width), np.uint32), np.zeros((s.height, s.width), np.float32)))
+            batch.add_frame(*imgs[-1])
+            batch.give_task(k, m)
+        batch.autotune(rounds=1)
+        for c, z in imgs:
+            c[:] = 0
+            z[:] = 0
+        batch.render()
+        threads = os.cpu_count() or 1
+        for (c, z), i in zip(imgs, chosen):
+            s = frames[i]
+            rc, rd, _ = port.render(s, bands=12, threads=threads)
+            label = f"frame {i} ({s.width}x{s.height}, {s.triangle_count} triangles)"
+            assert np.array_equal(c, rc), f"{label}: {int((c != rc).sum())} colour pixels differ"
+            assert np.array_equal(z.view(np.uint32), rd.view(np.uint32)), f"{label}: depth differs"
+        batch.destroy()
+    finally:
+        ctx.set_tuning(**{k: v for k, v in before.items()})

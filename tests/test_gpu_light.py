@@ -126,3 +126,68 @@ def test_deferred_light_pass_end_to_end(ctx):
     assert np.array_equal(host(got, np.uint32), out)
     assert (out != 0).mean() > 0.3
     gpu.destroy()
+
+
+def _pinned(a, pad=3):
+    """A page-locked copy of a 2-D array of 4-byte pixels, with padded rows."""
+    import torch
+    h, w = a.shape
+    dtype = torch.float32 if a.dtype == np.float32 else torch.int32
+    buf = torch.zeros((h, w + pad), dtype=dtype).pin_memory().numpy()[:, :w]
+    buf[:] = a.view(buf.dtype)
+    return buf
+
+
+@pytest.mark.parametrize("memory", ["pageable", "page-locked"])
+def test_light_calls_and_draw_higher_take_host_images(ctx, memory):
+    """The reference's light functions and draw_higher take host images: the same calls with
+    pageable (staged) and page-locked (read and written in place) host images, shadow cubes and
+    sprite sources give the oracle's results."""
+    import dfpsr_gb300 as d
+    from oracle import port
+    place = (lambda a: np.ascontiguousarray(a).copy()) if memory == "pageable" else _pinned
+    rng = np.random.default_rng(11)
+    h, w = 300, 240
+    normal, light, height = random_images(rng, h, w)
+    view, oview = d.ortho_view(-0.8, 64, 1), port.ortho_view(-0.8, 64, 1)
+    # directed light
+    want = port.directed_light(oview, light, normal, (0.3, -1.0, 0.2), 0.9, (255, 200, 100), True)
+    got = place(light)
+    ctx.light_directed(view, got, place(normal), (0.3, -1.0, 0.2), 0.9, (255, 200, 100), True)
+    assert np.array_equal(got.view(np.uint32), want)
+    # point lights with shadow cubes
+    lights = [{"position": (rng.uniform(-2, 2), rng.uniform(0, 2), rng.uniform(-2, 2)), "radius": float(rng.uniform(2, 6)),
+               "intensity": float(rng.uniform(0.5, 1.5)), "color": tuple(int(c) for c in rng.integers(64, 256, 3))} for _ in range(3)]
+    cubes = [rng.uniform(0, 0.6, size=(6 * 32, 32)).astype(np.float32) for _ in lights]
+    want = light
+    for l, cube in zip(lights, cubes):
+        want = port.point_light(oview, (w // 2, h // 2), want, normal, height, l["position"], l["radius"], l["intensity"], l["color"],
+                                cube, THREADS)
+    got = place(light)
+    host_cubes = [np.ascontiguousarray(c) if memory == "pageable" else _pinned(c, pad=0) for c in cubes]
+    ctx.light_points(view, (w // 2, h // 2), got, place(normal), place(height),
+                     [dict(l, cube=c) for l, c in zip(lights, host_cubes)], THREADS)
+    assert np.array_equal(got.view(np.uint32), want)
+    # blendLight
+    target = place(np.zeros((h, w), np.uint32))
+    ctx.light_blend(target, place(normal), place(light), 2)
+    assert np.array_equal(target.view(np.uint32), port.blend_light(2, normal, light))
+    # draw_higher with host sprites
+    th = rng.uniform(-1, 0.5, size=(h, w)).astype(np.float32)
+    ta = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    tb = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    sprites, expected = [], (th, ta, tb)
+    for k in range(12):
+        sh_, sw_ = int(rng.integers(8, 40)), int(rng.integers(8, 40))
+        hgt = rng.uniform(-1, 1, size=(sh_, sw_)).astype(np.float32)
+        a = rng.integers(0, 2**32, size=(sh_, sw_), dtype=np.uint64).astype(np.uint32)
+        b = rng.integers(0, 2**32, size=(sh_, sw_), dtype=np.uint64).astype(np.uint32)
+        left, top = int(rng.integers(-20, w)), int(rng.integers(-20, h))
+        expected = port.draw_higher((expected[0], expected[1], 0, expected[2], 0), (hgt, a, 0, b, 0), left, top, 0.0)
+        sprites.append({"height": place(hgt), "color_a": place(a), "color_b": place(b), "left": left, "top": top, "offset": 0.0,
+                        "a_pack": 0, "b_pack": 0})
+    gh, ga, gb = place(th), place(ta), place(tb)
+    ctx.draw_higher(gh, ga, gb, sprites)
+    assert np.array_equal(gh.view(np.uint32), expected[0].view(np.uint32))
+    assert np.array_equal(ga.view(np.uint32), expected[1])
+    assert np.array_equal(gb.view(np.uint32), expected[2])

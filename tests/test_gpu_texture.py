@@ -73,9 +73,29 @@ def test_texture_create_errors(ctx):
         d.Texture(ctx, np.zeros((4, 4), np.uint32), 0)
     with pytest.raises(d.DsrgError):
         d.Texture(ctx, np.zeros((4, 40000), np.uint32), 1)
-    img = d.image_struct(np.zeros((4, 4), np.uint32), 1)  # BGRA is rejected
+    img = d.image_struct(np.zeros((4, 4), np.uint32), 7)  # no such pack order
     import ctypes as C
     out = (C.c_void_p * 1)()
     r = np.array([1], np.int32)
-    assert ctx._l.dsrg_texture_create_many(ctx.handle, 1, (d.Image * 1)(img), r.ctypes.data, out) == 5
+    assert ctx._l.dsrg_texture_create_many(ctx.handle, 1, (d.Image * 1)(img), r.ctypes.data, out) == 1
     assert out[0] is None
+
+
+def test_texture_create_from_every_pack_order(ctx):
+    """Images in BGRA, ARGB and ABGR order (and RGBA) through every resize path: the GPU texture
+    equals the oracle's, which the CPU tests pin to the reference's texture_create_RgbaU8."""
+    import dfpsr_gb300 as d
+    from oracle import port
+    sizes = [(16, 16, 16), (16, 10, 16), (16, 20, 4), (10, 16, 16), (20, 16, 16), (12, 20, 3), (100, 60, 16), (33, 2, 16)]
+    images, orders, levels = [], [], []
+    for i, (w, h, lv) in enumerate(sizes):
+        for order in range(4):
+            images.append(_image(w, h, 300 + 4 * i + order))
+            orders.append(order)
+            levels.append(lv)
+    textures = d.Texture.create_many(ctx, images, levels, pack_orders=orders)
+    for tex, pixels, order, lv in zip(textures, images, orders, levels):
+        fields, pyramid = tex.read()
+        ot = port.OracleTexture(pixels, lv, pack_order=order)
+        assert list(fields) == ot.t.fields(), (pixels.shape, order)
+        assert np.array_equal(pyramid, ot.t.array()), (pixels.shape, order)

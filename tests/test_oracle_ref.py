@@ -111,3 +111,110 @@ def test_oracle_draw_line_equals_reference(ref_lib):
         x1, y1, x2, y2 = [int(v) for v in rng.integers(-20, 60, 4)]
         color = int(rng.integers(0, 2**32))
         assert np.array_equal(port.draw_line(img, x1, y1, x2, y2, color), ref_lib.draw_line(img, x1, y1, x2, y2, color))
+
+
+def _odd(w, h, n, seed=11, **kw):
+    import dataclasses
+    s = scenes.random_triangles(seed=seed, triangles=n, width=w, height=h, texture_size=32)
+    if kw.get("ortho"):
+        s.perspective = False
+        s.slope = 1.3
+    if kw.get("alpha"):
+        s = dataclasses.replace(s, filter=1)
+    return s
+
+
+ODD_CASES = {
+    "1x57": lambda: _odd(1, 57, 300),
+    "64x1": lambda: _odd(64, 1, 300),
+    "97x3": lambda: _odd(97, 3, 400),
+    "199x151": lambda: _odd(199, 151, 2000),
+    "199x151_ortho": lambda: _odd(199, 151, 2000, seed=12, ortho=True),
+    "199x151_alpha": lambda: _odd(199, 151, 1500, seed=13, alpha=True),
+    "48x33_dense": lambda: _odd(48, 33, 3000, seed=14),
+    "800x601": lambda: scenes.random_triangles(seed=1234, width=800, height=601),
+}
+
+
+@pytest.mark.parametrize("name", sorted(ODD_CASES))
+def test_oracle_equals_reference_odd_heights(ref_lib, name):
+    """Targets of odd height: the last row pair's missing lower row points at the upper row, so
+    the run of full quads writes its lower lanes there (fillerTemplates.h:285-306).  Prefilled
+    targets, colour-only and depth-only targets and the threaded renderer, bit for bit."""
+    from oracle import port
+    scene = ODD_CASES[name]()
+    h, w = scene.height, scene.width
+    model = ref_lib.RefModel(scene, "exact")
+    rng = np.random.default_rng(7)
+    color0 = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    depth0 = rng.uniform(0.0, 0.3, size=(h, w)).astype(np.float32)
+    for kw in (dict(), dict(color=color0, depth=depth0), dict(use_depth=False), dict(use_color=False)):
+        rc, rd = model.render(**kw)
+        oc, od, _ = port.render(scene, **kw)
+        if rc is not None:
+            assert np.array_equal(rc, oc), (name, kw.keys(), int((rc != oc).sum()))
+        if rd is not None:
+            assert np.array_equal(rd.view(np.uint32), od.view(np.uint32)), (name, kw.keys())
+    tc, td = model.render(threaded=True)
+    bc, bd, _ = port.render(scene, bands=12, threads=4)
+    assert np.array_equal(tc, bc) and np.array_equal(td.view(np.uint32), bd.view(np.uint32))
+
+
+def _mixed_frame_tasks():
+    """Tasks of one frame in order: perspective solid, orthogonal solid, perspective alpha,
+    orthogonal alpha, perspective solid (each task with its own camera)."""
+    import dataclasses
+    out = []
+    for i, (perspective, alpha) in enumerate([(True, False), (False, False), (True, True), (False, True), (True, False)]):
+        s = scenes.random_triangles(seed=140 + i, triangles=700, width=211, height=143, texture_size=32)
+        if not perspective:
+            s.perspective = False
+            s.slope = 1.3
+        if alpha:
+            s = dataclasses.replace(s, filter=1)
+        s.model_to_world = np.array([0.1 * i, -0.05 * i, 0.2 * i, 1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32)
+        out.append(s)
+    return out
+
+
+def test_oracle_equals_reference_on_frames_mixing_projections_and_filters(ref_lib):
+    """renderer_giveTask with perspective and orthogonal cameras and solid and alpha-filtered models
+    in one frame: every triangle tests depth with its own projection's comparison
+    (fillerTemplates.h:108-152) in submission order."""
+    from oracle import port
+    tasks = _mixed_frame_tasks()
+    h, w = tasks[0].height, tasks[0].width
+    rng = np.random.default_rng(3)
+    color0 = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+    depth0 = rng.uniform(0.0, 0.3, size=(h, w)).astype(np.float32)
+    r = ref_lib.RefRenderer()
+    o = port.OracleRenderer()
+    for eng in (r, o):
+        eng.begin(color0, depth0)
+    models = [ref_lib.RefModel(s) for s in tasks]
+    pms = [port.PreparedModel(s) for s in tasks]
+    for s, m, pm in zip(tasks, models, pms):
+        r.give_task(m, s.model_to_world, pm.cam)
+        o.give_task(pm, s.model_to_world, pm.cam)
+    rc, rd = r.end(False)
+    oc, od, _ = o.end()
+    assert np.array_equal(rc, oc)
+    assert np.array_equal(rd.view(np.uint32), od.view(np.uint32))
+    assert (rc != color0).sum() > 1000
+
+
+def test_oracle_texture_from_other_pack_orders_equals_reference(ref_lib):
+    """texture_create_RgbaU8 of BGRA, ARGB and ABGR images: the copy and the horizontal and bilinear
+    paths unpack the source's order, the aligned vertical-only path mixes its bytes as they lie
+    (filterAPI.cpp:157-260), a two-step upscale unpacks in its first step."""
+    from oracle import port
+    lib = ref_lib._load("exact")
+    rng = np.random.default_rng(15)
+    for w, h in [(16, 16), (16, 10), (16, 20), (10, 16), (20, 16), (12, 20), (100, 60), (60, 100), (33, 2), (2, 33), (5, 3)]:
+        img = rng.integers(0, 2**32, size=(h, w), dtype=np.uint64).astype(np.uint32)
+        for order in (1, 2, 3):
+            for levels in (1, 16):
+                t = port.OracleTexture(img, levels, pack_order=order)
+                fields, pixels = ref_lib.RefTexture(lib, img, levels, pack_order=order).info()
+                assert list(t.t.fields()) == list(fields), (w, h, order, levels)
+                assert np.array_equal(t.t.array(), pixels), (w, h, order, levels)
