@@ -33,7 +33,7 @@ EXPORTED = [
     "dsrg_batch_render", "dsrg_context_get_tuning", "dsrg_context_set_tuning", "dsrg_batch_autotune",
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
     "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
-    "dsrg_draw_higher", "dsrg_batch_set_depth_only",
+    "dsrg_draw_higher", "dsrg_sprite_frame", "dsrg_check_float_roots", "dsrg_batch_set_depth_only",
     "dsrg_dense_model_create", "dsrg_dense_model_destroy", "dsrg_dense_render", "dsrg_dense_render_many",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
@@ -94,6 +94,17 @@ class Sprite(C.Structure):
                 ("height_", C.c_int32), ("heightStrideBytes", C.c_int32), ("colorAStrideBytes", C.c_int32),
                 ("colorBStrideBytes", C.c_int32), ("colorAPackOrder", C.c_int32), ("colorBPackOrder", C.c_int32),
                 ("left", C.c_int32), ("top", C.c_int32), ("offset", C.c_float), ("onDevice", C.c_int32)]
+
+
+class SpriteFrame(C.Structure):
+    """dsrg_sprite_frame_desc: one frame of the deferred-light pass."""
+    _fields_ = [("view", C.POINTER(OrthoView)), ("centerX", C.c_int32), ("centerY", C.c_int32),
+                ("height", C.POINTER(Image)), ("diffuse", C.POINTER(Image)), ("normal", C.POINTER(Image)),
+                ("light", C.POINTER(Image)), ("output", C.POINTER(Image)), ("clearHeight", C.c_float),
+                ("clearDiffuse", C.c_uint32), ("clearNormal", C.c_uint32), ("sprites", C.POINTER(Sprite)),
+                ("spriteCount", C.c_int32), ("sunDirection", C.c_float * 3), ("sunIntensity", C.c_float),
+                ("sunColor", C.c_int32 * 3), ("shadows", C.c_void_p), ("lights", C.POINTER(PointLight)),
+                ("lightCount", C.c_int32), ("referenceThreads", C.c_int32)]
 
 
 _lib = None
@@ -169,6 +180,8 @@ def lib():
                                         C.c_float, C.c_float, P, I]
         l.dsrg_dense_render_many.argtypes = [P, P, I, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), I]
         l.dsrg_batch_set_depth_only.argtypes = [P, I]
+        l.dsrg_sprite_frame.argtypes = [P, C.POINTER(SpriteFrame)]
+        l.dsrg_check_float_roots.argtypes = [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64)]
         _lib = l
     return _lib
 
@@ -342,8 +355,10 @@ class Context:
         self._check(self._l.dsrg_light_directed(self.handle, C.byref(view), C.byref(li), C.byref(ni), d.ctypes.data,
                                                 C.c_float(intensity), c.ctypes.data, 1 if add else 0))
 
-    def light_points(self, view: "OrthoView", center, light, normal, height, lights, reference_threads: int = 0):
-        """lights: dicts with position, radius, intensity, color and optionally cube (cubeWidth*6 x cubeWidth floats)."""
+    @staticmethod
+    def point_lights(lights):
+        """A dsrg_point_light array from dicts with position, radius, intensity, color and optionally
+        cube (cubeWidth*6 x cubeWidth floats)."""
         arr = (PointLight * max(1, len(lights)))()
         for i, l in enumerate(lights):
             for k in range(3):
@@ -354,6 +369,11 @@ class Context:
             cube = l.get("cube")
             arr[i].shadowCube = _ptr(cube) if cube is not None else None
             arr[i].cubeWidth = int(cube.shape[1]) if cube is not None else 0
+        return arr
+
+    def light_points(self, view: "OrthoView", center, light, normal, height, lights, reference_threads: int = 0):
+        """lights: dicts with position, radius, intensity, color and optionally cube (cubeWidth*6 x cubeWidth floats)."""
+        arr = self.point_lights(lights)
         li, ni, hi = image_struct(light), image_struct(normal), image_struct(height)
         _torch_sync()
         self._check(self._l.dsrg_light_points(self.handle, C.byref(view), int(center[0]), int(center[1]), C.byref(li),
@@ -371,6 +391,34 @@ class Context:
         hi, ai, bi = image_struct(target_height), image_struct(target_a, a_pack), image_struct(target_b, b_pack)
         _torch_sync()
         self._check(self._l.dsrg_draw_higher(self.handle, C.byref(hi), C.byref(ai), C.byref(bi), array.array, array.count))
+
+    def check_float_roots(self, first_bits: int, count: int) -> int:
+        """dsrg_check_float_roots: floats whose double-precision roots, rounded, differ from the
+        correctly rounded single-precision ones."""
+        out = C.c_uint64()
+        self._check(self._l.dsrg_check_float_roots(self.handle, first_bits, count, C.byref(out)))
+        return int(out.value)
+
+    def sprite_frame(self, view: "OrthoView", center, images, clear, sprites, sun, shadows, lights, reference_threads: int = 0):
+        """dsrg_sprite_frame: images = (height, diffuse, normal, light, output); clear = (height value,
+        diffuse word, normal word); sprites a SpriteArray; sun = (direction, intensity, colour); shadows
+        a depth-only Batch of cube faces or None; lights as for light_points."""
+        structs = [image_struct(i) for i in images]
+        lights_array = self.point_lights(lights)
+        f = SpriteFrame()
+        f.view = C.pointer(view)
+        f.centerX, f.centerY = int(center[0]), int(center[1])
+        f.height, f.diffuse, f.normal, f.light, f.output = [C.pointer(s) for s in structs]
+        f.clearHeight, f.clearDiffuse, f.clearNormal = float(clear[0]), int(clear[1]), int(clear[2])
+        f.sprites, f.spriteCount = sprites.array, sprites.count
+        for k in range(3):
+            f.sunDirection[k] = float(sun[0][k])
+            f.sunColor[k] = int(sun[2][k])
+        f.sunIntensity = float(sun[1])
+        f.shadows = shadows.handle if shadows is not None else None
+        f.lights, f.lightCount, f.referenceThreads = lights_array, len(lights), int(reference_threads)
+        _torch_sync()
+        self._check(self._l.dsrg_sprite_frame(self.handle, C.byref(f)))
 
     def dense_render(self, model: "DenseModel", view: "OrthoView", height, diffuse, normal, origin, model_to_world,
                      high_quality: bool = False):

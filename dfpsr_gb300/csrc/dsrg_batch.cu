@@ -117,6 +117,24 @@ static bool image_ok(const dsrg_image *img) {
 	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 && img->strideBytes % 4 == 0;
 }
 
+bool batch_depth_in_place(dsrg_batch b) {
+	void *mappedPointer = nullptr;
+	for (const auto &f : b->frames)
+		if (f.hasDepth && !f.depth.onDevice && !host_mapped(f.depth.data, &mappedPointer)) return false;
+	return true;
+}
+
+void batch_clear_depth(dsrg_batch b) {
+	for (const auto &f : b->frames) {
+		if (!f.hasDepth) continue;
+		void *at = f.depth.data;
+		if (!f.depth.onDevice && !host_mapped(f.depth.data, &at)) continue; // excluded by batch_depth_in_place
+		enqueue_fill_words(at, f.depth.strideBytes / 4, f.width, f.height, 0u, b->context->stream);
+	}
+}
+
+dsrg_context batch_context(dsrg_batch b) { return b->context; }
+
 extern "C" {
 
 int dsrg_batch_create(dsrg_context ctx, dsrg_batch *out) {

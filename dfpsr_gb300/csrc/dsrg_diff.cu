@@ -135,7 +135,7 @@ __global__ void normals_kernel(DiffModel m, const float *__restrict__ modelToWor
 		const float bx = p[2].x - p[0].x, by = p[2].y - p[0].y, bz = p[2].z - p[0].z;
 		const float nx = fmul(ay, bz) - fmul(az, by), ny = fmul(az, bx) - fmul(ax, bz), nz = fmul(ax, by) - fmul(ay, bx);
 		const float len = __fsqrt_rn(fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz)));
-		const float inv = len > 0.0f ? fdiv(1.0f, len) : 0.0f;
+		const float inv = len > 0.0f ? frcp(len) : 0.0f;
 		normals[tri * 3] = fmul(nx, inv);
 		normals[tri * 3 + 1] = fmul(ny, inv);
 		normals[tri * 3 + 2] = fmul(nz, inv);

@@ -50,6 +50,29 @@ DSRG_HD float fdiv(float a, float b) {
 	return a / b;
 #endif
 }
+// 1 / x correctly rounded: the same value as fdiv(1.0f, x) for every x (IEEE 754 defines both as
+// the rounded exact quotient), in fewer instructions on the device.
+DSRG_HD float frcp(float x) {
+#if defined(__CUDA_ARCH__)
+	return __frcp_rn(x);
+#else
+	return 1.0f / x;
+#endif
+}
+// An estimate of a / b for quotients that exact integer products correct afterwards: within 2 ulp
+// on the device (|b| < 2^126, which int64 operands satisfy).  A host build may define
+// DSRG_HOST_ESTIMATE_ERROR to push its estimates that far off, so that host checks exercise the
+// corrections as the device does.
+DSRG_HD float fdiv_estimate(float a, float b) {
+#if defined(__CUDA_ARCH__)
+	return __fdividef(a, b);
+#elif defined(DSRG_HOST_ESTIMATE_ERROR)
+	const float q = a / b;
+	return q + q * DSRG_HOST_ESTIMATE_ERROR;
+#else
+	return a / b;
+#endif
+}
 DSRG_HD uint32_t fbits(float f) {
 #if defined(__CUDA_ARCH__)
 	return __float_as_uint(f);
@@ -179,7 +202,7 @@ DSRG_HD_CALL float chain_add(float s, float d, int32_t n) {
 // quotients beyond +-2^30 (where the int32 cast may wrap) take the 64-bit division.
 // Requires b != 0 and -2^20 < L <= R < 2^20.
 DSRG_HD int32_t clamp_quotient_plus_one(int64_t a, int64_t b, int32_t L, int32_t R) {
-	float qf = fdiv(i64_to_float(a), i64_to_float(b));
+	float qf = fdiv_estimate(i64_to_float(a), i64_to_float(b));
 	int32_t v;
 	if (qf > -1.0e9f && qf < 1.0e9f) {
 		if (qf < -2097152.0f) return L;
@@ -248,11 +271,11 @@ struct EdgeStepper {
 };
 
 // floor(a / b) and its remainder, b > 0.  Quotients below 2^22 in magnitude (every row crossing
-// inside an image) come from a binary32 estimate: a, b and their quotient each round by at most
-// 2^-24 relative, so the estimate lies within 0.75 of a / b and its floor within 1 of the answer,
-// which exact 64-bit products then correct.  Larger quotients take the 64-bit division.
+// inside an image) come from a binary32 estimate: a and b round by at most 2^-24 relative and the
+// estimated quotient by 2 ulp, so the estimate lies within 2 of a / b, and exact 64-bit products
+// step its floor to the answer.  Larger quotients take the 64-bit division.
 DSRG_HD void floor_divide(int64_t a, int64_t b, int64_t &q, int64_t &r) {
-	const float qf = fdiv(i64_to_float(a), i64_to_float(b));
+	const float qf = fdiv_estimate(i64_to_float(a), i64_to_float(b));
 	if (qf > -4194304.0f && qf < 4194304.0f) {
 		q = (int64_t)floorf(qf);
 		r = a - q * b;

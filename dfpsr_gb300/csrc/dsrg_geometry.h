@@ -43,7 +43,7 @@ DSRG_HD Projected camera_to_screen(const CameraData &c, const Vec3 &cs) {
 	Projected p;
 	p.cs = cs;
 	if (c.perspective) {
-		float invDepth = (cs.z > 0.0f) ? fdiv(1.0f, cs.z) : 0.0f;
+		float invDepth = (cs.z > 0.0f) ? frcp(cs.z) : 0.0f;
 		float centerShear = fmul(cs.z, 0.5f);
 		float preX = fmul(fadd(fmul(cs.x, c.invWidthSlope), centerShear), c.imageWidth);
 		float preY = fmul(fadd(fmul(-cs.y, c.invHeightSlope), centerShear), c.imageHeight);
@@ -108,7 +108,7 @@ DSRG_HD void triangle_projection(const float *isx, const float *isy, const float
 	for (int i = 0; i < 3; i++) {
 		int o = (i + 2) % 3;
 		float other = fadd(fmul(isx[o] - isx[i], offsetX[i]), fmul(isy[o] - isy[i], offsetY[i]));
-		weightMultiplier[o] = (other == 0.0f) ? 0.0f : fdiv(1.0f, other);
+		weightMultiplier[o] = (other == 0.0f) ? 0.0f : frcp(other);
 	}
 	for (int i = 0; i < 3; i++) {
 		normalX[i] = fmul(offsetX[i], weightMultiplier[i]);
@@ -132,7 +132,7 @@ DSRG_HD void triangle_projection(const float *isx, const float *isy, const float
 		dy[1] = fadd(fadd(fmul(awdy[0], subB[0]), fmul(awdy[1], subB[1])), fmul(awdy[2], subB[2]));
 		dy[2] = fadd(fadd(fmul(awdy[0], subC[0]), fmul(awdy[1], subC[1])), fmul(awdy[2], subC[2]));
 	} else {
-		const float IW[3] = {fdiv(1.0f, csz[0]), fdiv(1.0f, csz[1]), fdiv(1.0f, csz[2])};
+		const float IW[3] = {frcp(csz[0]), frcp(csz[1]), frcp(csz[2])};
 		start[0] = fadd(fadd(fmul(IW[0], targetWeight[0]), fmul(IW[1], targetWeight[1])), fmul(IW[2], targetWeight[2]));
 		start[1] = fadd(fadd(fmul(fmul(IW[0], targetWeight[0]), subB[0]), fmul(fmul(IW[1], targetWeight[1]), subB[1])),
 		                fmul(fmul(IW[2], targetWeight[2]), subB[2]));

@@ -3,6 +3,9 @@
 // Built with -ffp-contract=off so that it computes the same bits as the device code.
 #include <stdint.h>
 
+// Estimates of integer quotients 2^-21 off, at least as far as the device's: the host checks then
+// exercise the exact corrections that follow them.
+#define DSRG_HOST_ESTIMATE_ERROR 4.76837158203125e-7f
 #include "dsrg_exact.h"
 #include "dsrg_geometry.h"
 

@@ -283,6 +283,14 @@ int renderer_upload_given(dsrg_renderer r);
 // The device address of page-locked (or registered) host memory, which kernels then read and write
 // in place; false for pageable memory, which is staged through device buffers.
 bool host_mapped(const void *p, void **devicePointer);
+// Queues a fill of a rectangle of 32-bit words (device or mapped memory) with one value.
+void enqueue_fill_words(void *image, int32_t strideWords, int32_t width, int32_t height, uint32_t value, cudaStream_t stream);
+// Whether every depth image of a batch is reachable by kernels without staging (device or page-locked memory).
+bool batch_depth_in_place(dsrg_batch b);
+// Queues zeroing of every depth image of a batch (CubeMapF32::clear for a batch of cube faces).
+void batch_clear_depth(dsrg_batch b);
+// The context a batch belongs to.
+dsrg_context batch_context(dsrg_batch b);
 // The frame target of a renderer's current frame (images, size, occlusion grid when in use).
 void renderer_frame_target(dsrg_renderer r, dsrg::FrameTarget &f);
 // Uploads the occlusion grid when the device copy is stale.

@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(256) setup_kernel(BatchParams b, FrameBuffers 
 		const uint32_t t = g - task.triangleBase;
 		uint32_t emitted = 0;
 		const uint32_t base = WRITE ? fb.triOffsets[g] : 0u;
+		if (WRITE && fb.triOffsets[g + 1] == base) continue; // the count pass emitted nothing for it
 		const int32_t src = task.triSource[t];
 		const int32_t p = src >> 1, fan = src & 1;
 		const int corner[3] = {0, 1 + fan, 2 + fan}; // fan 0-1-2, 0-2-3 (model/Model.cpp:135-162, 164-183)
@@ -1087,6 +1088,42 @@ __device__ __forceinline__ void resolve_pixel(const BatchParams &b, const FrameT
 	write_lane(b, f, r, pair, y1, x, lane4, px, py, affine);
 }
 
+// The winner of pixel (px, py) when all four pixels of its 2x2 quad have that winner, evaluated by
+// the four lanes of the quad together (lanes 4q..4q+3 of `quadLanes` hold quad q, lane l4 its
+// position): each lane computes the running sums of its own position only (quad_lane), and the
+// vertex weights of positions 0..2, which every position's mip level needs, come from the other
+// lanes by shuffles.  The values are those of resolve_pixel; the quad's sums are evaluated once
+// instead of four times.
+__device__ __forceinline__ void resolve_shared_quad(const BatchParams &b, const FrameTarget &f, const DrawRecord *__restrict__ records,
+                                                    const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows,
+                                                    int32_t px, int32_t py, unsigned long long key, int l4, unsigned quadLanes) {
+	const bool depthTest = f.depth != nullptr, affine = f.affine != 0;
+	const uint32_t ri = key_record(key, depthTest);
+	const DrawRecord r = records[ri];
+	const int32_t y1 = py & ~1, x = px & ~1;
+	const RowPair pair = record_row_pair(r, rows + rowOffsets[ri], y1, f.height);
+	const float depthValue = quad_lane(r.start[0], r.dx[0], r.dy[0], pair, y1, x, l4);
+	if (f.color) {
+		float a, bw, c;
+		lane_weight(depthValue, quad_lane(r.start[1], r.dx[1], r.dy[1], pair, y1, x, l4),
+		            quad_lane(r.start[2], r.dx[2], r.dy[2], pair, y1, x, l4), affine, a, bw, c);
+		const int base = (int)(threadIdx.x & 31u) & ~3;
+		float wa[4], wb[4], wc[4];
+		for (int l = 0; l < 3; l++) {
+			wa[l] = __shfl_sync(quadLanes, a, base + l);
+			wb[l] = __shfl_sync(quadLanes, bw, base + l);
+			wc[l] = __shfl_sync(quadLanes, c, base + l);
+		}
+		wa[3] = a; wb[3] = bw; wc[3] = c; // position 3 reads only its own weights
+		ShadeRecord shade;
+		make_shade(b.tasks[r.task], r.source, shade);
+		float rgba[4];
+		shade_lane_inline(shade, b.textures, wa, wb, wc, l4, rgba);
+		f.color[(size_t)py * f.colorStride + px] = pack_saturated(rgba, f.packOrder);
+	}
+	if (f.depth) f.depth[(size_t)py * f.depthStride + px] = depthValue;
+}
+
 // Persistent CTAs pull 16x16 tiles of the batch from a device queue.  The binning split every
 // tile's list into small and large records.  Both are dealt round-robin over the warps (warp w of
 // W takes entries w, w + W, ...): the quads of a warp's 32 small records inside the tile are spread
@@ -1328,14 +1365,30 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		__syncthreads();
 #pragma unroll 1
 		for (int k = 0; k < PIXELS; k++) { // one copy of the (inlined) resolve code, not PIXELS
-			const int p = tid + k * THREADS;
-			const int32_t px = tx0 + (p & 15), py = ty0 + (p >> 4);
-			const int me = (p >> 4) * TILE_STRIDE + (p & 15);
-			if (px < width && py < height) {
+			// quad-major: lanes 4q..4q+3 hold the four pixels of quad q, and a warp holds a 16 x 2 strip
+			const int p = tid + k * THREADS, q = p >> 2, l4 = p & 3;
+			const int lx = 2 * (q & 7) + (l4 & 1), ly = 2 * (q >> 3) + (l4 >> 1);
+			const int32_t px = tx0 + lx, py = ty0 + ly;
+			const int me = ly * TILE_STRIDE + lx;
+			const bool inside = px < width && py < height;
+			const unsigned long long key = inside ? keys[me] : 0ull;
+			if (inside) {
 				if (counting) coverageImage[(size_t)py * width + px] += coverage[me]; // zeroed before a frame's first run
-				if (!RESOLVE) keyImage[(size_t)py * width + px] = keys[me];
-				// the tile's winners shaded right away (resolve_pixels_kernel fused into the tile pass)
-				else if (keys[me] != 0ull) resolve_pixel(b, f, records, rowOffsets, rows, px, py, keys[me]);
+				if (!RESOLVE) keyImage[(size_t)py * width + px] = key;
+			}
+			if (!RESOLVE) continue;
+			// the tile's winners shaded right away (resolve_pixels_kernel fused into the tile pass): a
+			// warp whose quads each have one winner (or none) shares each quad's sums among its lanes;
+			// other warps, and every quad touching the image's edge or an odd height's last row (whose
+			// missing pixels have no key), resolve pixel by pixel
+			const int same = key == __shfl_sync(0xFFFFFFFFu, key, lane & ~3) ? 1 : 0;
+			const bool quadSame = (same & __shfl_xor_sync(0xFFFFFFFFu, same, 1) & __shfl_xor_sync(0xFFFFFFFFu, same, 2) &
+			                       __shfl_xor_sync(0xFFFFFFFFu, same, 3)) != 0;
+			const unsigned drawn = __ballot_sync(0xFFFFFFFFu, key != 0ull);
+			if (__all_sync(0xFFFFFFFFu, quadSame || key == 0ull)) {
+				if (key != 0ull) resolve_shared_quad(b, f, records, rowOffsets, rows, px, py, key, l4, drawn);
+			} else if (key != 0ull) {
+				resolve_pixel(b, f, records, rowOffsets, rows, px, py, key);
 			}
 		}
 		if (tid == 0 && fragmentSum) {

@@ -19,6 +19,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "dsrg_internal.h"
@@ -157,7 +158,7 @@ __device__ __forceinline__ float shadow_transparency(const float *cube, int32_t 
 		slopeSide = -slopeSide;
 		viewOffset += width;
 	}
-	const float reciDepth = fdiv(1.0f, depth);
+	const float reciDepth = frcp(depth);
 	const float scale = fmul(halfWidth, reciDepth);
 	int32_t sampleX = (int32_t)fadd(halfWidth, fmul(slopeSide, scale));
 	int32_t sampleY = (int32_t)fsub(halfWidth, fmul(slopeUp, scale));
@@ -175,11 +176,15 @@ __device__ __forceinline__ void point_light_bytes(const PointLightParams &p, con
 	                       fmul(fadd((float)((normalWord >> 16) & 0xFFu), -128.0f), -0.0078125f)};
 	const float squareLength = fadd(fadd(fmul(o[0], o[0]), fmul(o[1], o[1])), fmul(o[2], o[2]));
 	// squareRoot and reciprocalSquareRoot of the scalar build go through the double overload of sqrt
-	const double root = __dsqrt_rn((double)squareLength);
-	const float length = __double2float_rn(root);
+	// (simd.h:4084-4146): (float)sqrt((double)x) and (float)(1.0 / sqrt((double)x)).  Both equal the
+	// correctly rounded single-precision results, so no double arithmetic is needed: the square root
+	// because rounding first to 53 and then to 24 bits is innocuous for sqrt (53 >= 2 * 24 + 2), the
+	// reciprocal square root as checked for every float of [1, 4) on the device (dsrg_check_float_roots;
+	// both sides scale exactly by 2 when x scales by 4).
+	const float length = __fsqrt_rn(squareLength);
 	const float ratio = vmin_ref(1.0f, fmul(length, p.reciprocalRadius));
 	const float distanceIntensity = fadd(fsub(1.0f, fmul(2.0f, ratio)), fmul(ratio, ratio));
-	const float rs = __double2float_rn(__ddiv_rn(1.0, root));
+	const float rs = __frsqrt_rn(squareLength);
 	const float angle = vmax_ref(0.0f, fadd(fadd(fmul(fmul(o[0], rs), negN[0]), fmul(fmul(o[1], rs), negN[1])),
 	                                        fmul(fmul(o[2], rs), negN[2])));
 	float intensity = fmul(angle, distanceIntensity);
@@ -337,6 +342,37 @@ __global__ void higher_resolve_kernel(const SpriteData *__restrict__ sprites, co
 	targetB[(size_t)y * tbStride + x] = reorder(sp.colorB[(size_t)sy * sp.bStride + sx], sp.bPack, tbPack);
 }
 
+// The scalar build's float square roots through double precision against the correctly rounded
+// single-precision operations, for `count` consecutive float bit patterns from firstBits: counts
+// the inputs where either differs (NaN results compare equal to NaN).
+__global__ void root_check_kernel(uint32_t firstBits, uint32_t count, unsigned long long *mismatches) {
+	unsigned long long bad = 0;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+		const float x = __uint_as_float(firstBits + i);
+		const double root = __dsqrt_rn((double)x);
+		const float viaDouble[2] = {__double2float_rn(root), __double2float_rn(__ddiv_rn(1.0, root))};
+		const float single[2] = {__fsqrt_rn(x), __frsqrt_rn(x)};
+		for (int k = 0; k < 2; k++) {
+			const bool bothNaN = viaDouble[k] != viaDouble[k] && single[k] != single[k];
+			if (!bothNaN && __float_as_uint(viaDouble[k]) != __float_as_uint(single[k])) bad++;
+		}
+	}
+	if (bad) atomicAdd(mismatches, bad);
+}
+
+// A rectangle of 32-bit words set to one value (the frame's clears).
+__global__ void fill_words_kernel(uint32_t *image, int32_t stride, int32_t width, int32_t height, uint32_t value) {
+	const int32_t x = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x), y = (int32_t)blockIdx.y;
+	if (x < width && y < height) image[(size_t)y * stride + x] = value;
+}
+
+bool sprite_ok(const dsrg_sprite &s) {
+	return s.height && s.colorA && s.colorB && s.width >= 0 && s.height_ >= 0 && s.heightStrideBytes >= s.width * 4 &&
+	       s.colorAStrideBytes >= s.width * 4 && s.colorBStrideBytes >= s.width * 4 && s.heightStrideBytes % 4 == 0 &&
+	       s.colorAStrideBytes % 4 == 0 && s.colorBStrideBytes % 4 == 0 && s.colorAPackOrder >= 0 && s.colorAPackOrder <= 3 &&
+	       s.colorBPackOrder >= 0 && s.colorBPackOrder <= 3;
+}
+
 bool valid_image(const dsrg_image *img) {
 	return img && img->data && img->width > 0 && img->height > 0 && img->strideBytes >= img->width * 4 && img->strideBytes % 4 == 0;
 }
@@ -389,7 +425,14 @@ int place(dsrg_context ctx, std::vector<CallMemory> &blocks) {
 }
 
 // Copies the staged blocks the call wrote back to the caller's memory, and waits for the call.
-int finish(dsrg_context ctx, const std::vector<CallMemory> &blocks, const dsrg_image *const *images) {
+// Inside a sprite frame (wait = false) every image comes placed already, so nothing is staged and
+// the frame waits once at its end.
+int finish(dsrg_context ctx, const std::vector<CallMemory> &blocks, const dsrg_image *const *images, bool wait = true) {
+	if (!wait) {
+		for (const CallMemory &m : blocks)
+			if (m.stagedAt != SIZE_MAX) return fail(ctx, DSRG_ERROR_CUDA, "sprite frame: an image of a step was not placed");
+		return DSRG_OK;
+	}
 	for (size_t i = 0; i < blocks.size(); i++) {
 		const CallMemory &m = blocks[i];
 		if (m.stagedAt == SIZE_MAX || !m.written) continue;
@@ -407,77 +450,8 @@ int32_t hardware_threads() {
 	return n > 0 ? (int32_t)n : 1;
 }
 
-} // namespace
-
-extern "C" {
-
-int dsrg_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, dsrg_ortho_view *out) {
-	if (!out || index < 0 || index > 7 || pixelsPerTile < 1) return DSRG_ERROR_INVALID_ARGUMENT;
-	const float diag = 0.707106781f;
-	// the reference's unqualified sqrt of a float argument resolves to the double overload
-	const int32_t yPixelsPerTile = (int32_t)((double)(float)pixelsPerTile / sqrt((double)(cameraTilt * cameraTilt + 1)));
-	const Vec3 forward[8] = {v3(diag, cameraTilt, diag), v3(-diag, cameraTilt, diag), v3(-diag, cameraTilt, -diag),
-	                         v3(diag, cameraTilt, -diag), v3(0.0f, cameraTilt, 1.0f), v3(-1.0f, cameraTilt, 0.0f),
-	                         v3(0.0f, cameraTilt, -1.0f), v3(1.0f, cameraTilt, 0.0f)};
-	const M3 system = axis_system(forward[index], v3(0.0f, 1.0f, 0.0f));
-	Vec3 normalDirection = system.z;
-	normalDirection.y = 0.0f;
-	const M3 normalToWorld = axis_system(normalDirection, v3(0.0f, 1.0f, 0.0f));
-	// Camera::createOrthogonal(Transform3D(origin, system), ppt, ppt, 0.5) and worldToScreen of the x and z axes
-	dsrg_camera cam;
-	memset(&cam, 0, sizeof(cam));
-	const float loc[12] = {0.0f, 0.0f, 0.0f, system.x.x, system.x.y, system.x.z, system.y.x, system.y.y, system.y.z,
-	                       system.z.x, system.z.y, system.z.z};
-	memcpy(cam.location, loc, sizeof(loc));
-	cam.perspective = 0;
-	cam.slope = 0.5f;
-	cam.width = pixelsPerTile;
-	cam.height = pixelsPerTile;
-	const CameraData c = make_camera(cam);
-	const float halfTile = (float)pixelsPerTile * 0.5f;
-	const Projected px = camera_to_screen(c, world_to_camera(c, v3(1.0f, 0.0f, 0.0f)));
-	const Projected pz = camera_to_screen(c, world_to_camera(c, v3(0.0f, 0.0f, 1.0f)));
-	const int32_t xAxis[2] = {(int32_t)(px.isx - halfTile), (int32_t)(px.isy - halfTile)};
-	const int32_t zAxis[2] = {(int32_t)(pz.isx - halfTile), (int32_t)(pz.isy - halfTile)};
-	// OrthoView::OrthoView (orthoAPI.cpp:6-37)
-	M3 tileToScreen;
-	tileToScreen.x = v3((float)xAxis[0], (float)xAxis[1], 0.0f);
-	tileToScreen.y = v3(0.0f, (float)(-yPixelsPerTile), 1.0f);
-	tileToScreen.z = v3((float)zAxis[0], (float)zAxis[1], 0.0f);
-	const M3 screenToTile = inverse_ref(tileToScreen);
-	M3 toLight;
-	toLight.x = transform_transposed_ref(normalToWorld, screenToTile.x);
-	toLight.y = transform_transposed_ref(normalToWorld, screenToTile.y);
-	toLight.z = transform_transposed_ref(normalToWorld, screenToTile.z);
-	const M3 fromLight = inverse_ref(toLight);
-	store_m3(normalToWorld, out->normalToWorld);
-	store_m3(toLight, out->screenDepthToLightSpace);
-	store_m3(fromLight, out->lightSpaceToScreenDepth);
-	out->pixelOffsetPerTileX[0] = xAxis[0]; out->pixelOffsetPerTileX[1] = xAxis[1];
-	out->pixelOffsetPerTileZ[0] = zAxis[0]; out->pixelOffsetPerTileZ[1] = zAxis[1];
-	out->yPixelsPerTile = yPixelsPerTile;
-	return DSRG_OK;
-}
-
-int dsrg_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]) {
-	if (!normalToWorld || !location || side < 0 || side > 5) return DSRG_ERROR_INVALID_ARGUMENT;
-	const Vec3 forward[6] = {v3(1.0f, 0.0f, 0.0f), v3(-1.0f, 0.0f, 0.0f), v3(0.0f, 1.0f, 0.0f),
-	                         v3(0.0f, -1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f), v3(0.0f, 0.0f, -1.0f)};
-	const Vec3 up[6] = {v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f),
-	                    v3(0.0f, 0.0f, 1.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f)};
-	const M3 s = axis_system(forward[side], up[side]);
-	const M3 n = load_m3(normalToWorld);
-	M3 r; // FMatrix3x3 product (FMatrix3x3.h:50-52)
-	r.x = transform_ref(n, s.x);
-	r.y = transform_ref(n, s.y);
-	r.z = transform_ref(n, s.z);
-	location[0] = 0.0f; location[1] = 0.0f; location[2] = 0.0f;
-	store_m3(r, location + 3);
-	return DSRG_OK;
-}
-
-int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
-                        const float direction[3], float intensity, const int32_t color[3], int32_t add) {
+int light_directed_impl(dsrg_context ctx, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
+                        const float direction[3], float intensity, const int32_t color[3], int32_t add, bool wait) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (!view || !direction || !color) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_directed: null argument");
 	if (!valid_image(light) || !valid_image(normal) || light->width != normal->width || light->height != normal->height)
@@ -503,12 +477,12 @@ int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsr
 	                                                     stride_of(mem[1]), light->width, light->height, p);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	return finish(ctx, mem, images);
+	return finish(ctx, mem, images, wait);
 }
 
-int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY, const dsrg_image *light,
+int light_points_impl(dsrg_context ctx, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY, const dsrg_image *light,
                       const dsrg_image *normal, const dsrg_image *height, const dsrg_point_light *lights, int32_t count,
-                      int32_t referenceThreads) {
+                      int32_t referenceThreads, bool wait) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (!view || (count > 0 && !lights) || count < 0) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_light_points: null argument");
 	if (!valid_image(light) || !valid_image(normal) || !valid_image(height) || light->width != normal->width ||
@@ -591,10 +565,10 @@ int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
 	                                                   width, imageHeight, f);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	return finish(ctx, mem, images.data());
+	return finish(ctx, mem, images.data(), wait);
 }
 
-int dsrg_light_blend(dsrg_context ctx, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light) {
+int light_blend_impl(dsrg_context ctx, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light, bool wait) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (!valid_image(target) || !valid_image(diffuse) || !valid_image(light) || target->width != diffuse->width ||
 	    target->height != diffuse->height || target->width != light->width || target->height != light->height ||
@@ -612,11 +586,11 @@ int dsrg_light_blend(dsrg_context ctx, const dsrg_image *target, const dsrg_imag
 	                                                  target->height);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	return finish(ctx, mem, images);
+	return finish(ctx, mem, images, wait);
 }
 
-int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsrg_image *targetA, const dsrg_image *targetB,
-                     const dsrg_sprite *sprites, int32_t count) {
+int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsrg_image *targetA, const dsrg_image *targetB,
+                     const dsrg_sprite *sprites, int32_t count, bool wait) {
 	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
 	if (count < 0 || (count > 0 && !sprites)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: null sprites");
 	if (!valid_image(targetHeight) || !valid_image(targetA) || !valid_image(targetB) || targetHeight->width != targetA->width ||
@@ -629,11 +603,7 @@ int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	int32_t largest = 1;
 	for (int32_t i = 0; i < count; i++) {
 		const dsrg_sprite &s = sprites[i];
-		if (!s.height || !s.colorA || !s.colorB || s.width < 0 || s.height_ < 0 || s.heightStrideBytes < s.width * 4 ||
-		    s.colorAStrideBytes < s.width * 4 || s.colorBStrideBytes < s.width * 4 || s.heightStrideBytes % 4 ||
-		    s.colorAStrideBytes % 4 || s.colorBStrideBytes % 4 || s.colorAPackOrder < 0 || s.colorAPackOrder > 3 ||
-		    s.colorBPackOrder < 0 || s.colorBPackOrder > 3)
-			return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: invalid sprite " + std::to_string(i));
+		if (!sprite_ok(s)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: invalid sprite " + std::to_string(i));
 		SpriteData &d = table[i];
 		d.height = s.height; d.colorA = s.colorA; d.colorB = s.colorB;
 		d.width = s.width; d.height_ = s.height_;
@@ -689,7 +659,239 @@ int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	                                                     (uint32_t *)mem[2].device, stride_of(mem[2]), targetB->packOrder, width, height);
 	add_launches(1);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	return finish(ctx, mem, images.data());
+	return finish(ctx, mem, images.data(), wait);
+}
+
+// Where a shadow cube's words are for the kernels: device memory as given, page-locked memory
+// through its device address; null for pageable memory.
+const float *cube_in_place(const float *cube) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, cube) == cudaSuccess && a.type == cudaMemoryTypeDevice) return cube;
+	cudaGetLastError();
+	void *mappedPointer = nullptr;
+	return host_mapped(cube, &mappedPointer) ? (const float *)mappedPointer : nullptr;
+}
+
+// The steps of one sprite frame after its images were placed (see dsrg_sprite_frame).
+int sprite_frame_steps(dsrg_context ctx, const dsrg_sprite_frame_desc &d, const dsrg_image *img, const dsrg_sprite *sprites,
+                       const dsrg_point_light *lights) {
+	const dsrg_image &height = img[0], &diffuse = img[1], &normal = img[2], &light = img[3], &output = img[4];
+	uint32_t clearHeight;
+	memcpy(&clearHeight, &d.clearHeight, 4);
+	enqueue_fill_words(height.data, height.strideBytes / 4, height.width, height.height, clearHeight, ctx->stream);
+	enqueue_fill_words(diffuse.data, diffuse.strideBytes / 4, diffuse.width, diffuse.height, d.clearDiffuse, ctx->stream);
+	enqueue_fill_words(normal.data, normal.strideBytes / 4, normal.width, normal.height, d.clearNormal, ctx->stream);
+	add_launches(3);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	int status = draw_higher_impl(ctx, &height, &diffuse, &normal, sprites, d.spriteCount, false);
+	if (status != DSRG_OK) return status;
+	status = light_directed_impl(ctx, d.view, &light, &normal, d.sunDirection, d.sunIntensity, d.sunColor, 0, false);
+	if (status != DSRG_OK) return status;
+	if (d.shadows) {
+		batch_clear_depth(d.shadows);
+		DSRG_CUDA_TRY(ctx, cudaGetLastError());
+		status = dsrg_batch_render(d.shadows); // checks its buffers on the host: the frame's first wait
+		if (status != DSRG_OK) return status;
+	}
+	status = light_points_impl(ctx, d.view, d.centerX, d.centerY, &light, &normal, &height, lights, d.lightCount, d.referenceThreads,
+	                           false);
+	if (status != DSRG_OK) return status;
+	return light_blend_impl(ctx, &output, &diffuse, &light, false);
+}
+
+} // namespace
+
+void enqueue_fill_words(void *image, int32_t strideWords, int32_t width, int32_t height, uint32_t value, cudaStream_t stream) {
+	if (width <= 0 || height <= 0) return;
+	for (int32_t first = 0; first < height; first += 65535) { // grid y is limited to 65535 rows per launch
+		const int32_t rows = height - first < 65535 ? height - first : 65535;
+		fill_words_kernel<<<dim3((width + 255) / 256, rows), 256, 0, stream>>>((uint32_t *)image + (size_t)first * strideWords,
+		                                                                      strideWords, width, rows, value);
+	}
+}
+
+extern "C" {
+
+int dsrg_ortho_view_create(float cameraTilt, int32_t pixelsPerTile, int32_t index, dsrg_ortho_view *out) {
+	if (!out || index < 0 || index > 7 || pixelsPerTile < 1) return DSRG_ERROR_INVALID_ARGUMENT;
+	const float diag = 0.707106781f;
+	// the reference's unqualified sqrt of a float argument resolves to the double overload
+	const int32_t yPixelsPerTile = (int32_t)((double)(float)pixelsPerTile / sqrt((double)(cameraTilt * cameraTilt + 1)));
+	const Vec3 forward[8] = {v3(diag, cameraTilt, diag), v3(-diag, cameraTilt, diag), v3(-diag, cameraTilt, -diag),
+	                         v3(diag, cameraTilt, -diag), v3(0.0f, cameraTilt, 1.0f), v3(-1.0f, cameraTilt, 0.0f),
+	                         v3(0.0f, cameraTilt, -1.0f), v3(1.0f, cameraTilt, 0.0f)};
+	const M3 system = axis_system(forward[index], v3(0.0f, 1.0f, 0.0f));
+	Vec3 normalDirection = system.z;
+	normalDirection.y = 0.0f;
+	const M3 normalToWorld = axis_system(normalDirection, v3(0.0f, 1.0f, 0.0f));
+	// Camera::createOrthogonal(Transform3D(origin, system), ppt, ppt, 0.5) and worldToScreen of the x and z axes
+	dsrg_camera cam;
+	memset(&cam, 0, sizeof(cam));
+	const float loc[12] = {0.0f, 0.0f, 0.0f, system.x.x, system.x.y, system.x.z, system.y.x, system.y.y, system.y.z,
+	                       system.z.x, system.z.y, system.z.z};
+	memcpy(cam.location, loc, sizeof(loc));
+	cam.perspective = 0;
+	cam.slope = 0.5f;
+	cam.width = pixelsPerTile;
+	cam.height = pixelsPerTile;
+	const CameraData c = make_camera(cam);
+	const float halfTile = (float)pixelsPerTile * 0.5f;
+	const Projected px = camera_to_screen(c, world_to_camera(c, v3(1.0f, 0.0f, 0.0f)));
+	const Projected pz = camera_to_screen(c, world_to_camera(c, v3(0.0f, 0.0f, 1.0f)));
+	const int32_t xAxis[2] = {(int32_t)(px.isx - halfTile), (int32_t)(px.isy - halfTile)};
+	const int32_t zAxis[2] = {(int32_t)(pz.isx - halfTile), (int32_t)(pz.isy - halfTile)};
+	// OrthoView::OrthoView (orthoAPI.cpp:6-37)
+	M3 tileToScreen;
+	tileToScreen.x = v3((float)xAxis[0], (float)xAxis[1], 0.0f);
+	tileToScreen.y = v3(0.0f, (float)(-yPixelsPerTile), 1.0f);
+	tileToScreen.z = v3((float)zAxis[0], (float)zAxis[1], 0.0f);
+	const M3 screenToTile = inverse_ref(tileToScreen);
+	M3 toLight;
+	toLight.x = transform_transposed_ref(normalToWorld, screenToTile.x);
+	toLight.y = transform_transposed_ref(normalToWorld, screenToTile.y);
+	toLight.z = transform_transposed_ref(normalToWorld, screenToTile.z);
+	const M3 fromLight = inverse_ref(toLight);
+	store_m3(normalToWorld, out->normalToWorld);
+	store_m3(toLight, out->screenDepthToLightSpace);
+	store_m3(fromLight, out->lightSpaceToScreenDepth);
+	out->pixelOffsetPerTileX[0] = xAxis[0]; out->pixelOffsetPerTileX[1] = xAxis[1];
+	out->pixelOffsetPerTileZ[0] = zAxis[0]; out->pixelOffsetPerTileZ[1] = zAxis[1];
+	out->yPixelsPerTile = yPixelsPerTile;
+	return DSRG_OK;
+}
+
+int dsrg_shadow_side_location(const float normalToWorld[9], int32_t side, float location[12]) {
+	if (!normalToWorld || !location || side < 0 || side > 5) return DSRG_ERROR_INVALID_ARGUMENT;
+	const Vec3 forward[6] = {v3(1.0f, 0.0f, 0.0f), v3(-1.0f, 0.0f, 0.0f), v3(0.0f, 1.0f, 0.0f),
+	                         v3(0.0f, -1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f), v3(0.0f, 0.0f, -1.0f)};
+	const Vec3 up[6] = {v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 0.0f, 1.0f),
+	                    v3(0.0f, 0.0f, 1.0f), v3(0.0f, 1.0f, 0.0f), v3(0.0f, 1.0f, 0.0f)};
+	const M3 s = axis_system(forward[side], up[side]);
+	const M3 n = load_m3(normalToWorld);
+	M3 r; // FMatrix3x3 product (FMatrix3x3.h:50-52)
+	r.x = transform_ref(n, s.x);
+	r.y = transform_ref(n, s.y);
+	r.z = transform_ref(n, s.z);
+	location[0] = 0.0f; location[1] = 0.0f; location[2] = 0.0f;
+	store_m3(r, location + 3);
+	return DSRG_OK;
+}
+
+int dsrg_light_directed(dsrg_context ctx, const dsrg_ortho_view *view, const dsrg_image *light, const dsrg_image *normal,
+                        const float direction[3], float intensity, const int32_t color[3], int32_t add) {
+	return light_directed_impl(ctx, view, light, normal, direction, intensity, color, add, true);
+}
+
+int dsrg_light_points(dsrg_context ctx, const dsrg_ortho_view *view, int32_t centerX, int32_t centerY, const dsrg_image *light,
+                      const dsrg_image *normal, const dsrg_image *height, const dsrg_point_light *lights, int32_t count,
+                      int32_t referenceThreads) {
+	return light_points_impl(ctx, view, centerX, centerY, light, normal, height, lights, count, referenceThreads, true);
+}
+
+int dsrg_light_blend(dsrg_context ctx, const dsrg_image *target, const dsrg_image *diffuse, const dsrg_image *light) {
+	return light_blend_impl(ctx, target, diffuse, light, true);
+}
+
+int dsrg_draw_higher(dsrg_context ctx, const dsrg_image *targetHeight, const dsrg_image *targetA, const dsrg_image *targetB,
+                     const dsrg_sprite *sprites, int32_t count) {
+	return draw_higher_impl(ctx, targetHeight, targetA, targetB, sprites, count, true);
+}
+
+int dsrg_check_float_roots(dsrg_context ctx, uint32_t firstBits, uint32_t count, uint64_t *mismatches) {
+	if (!ctx || !mismatches) return DSRG_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	*mismatches = 0;
+	if (count == 0) return DSRG_OK;
+	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(sizeof(unsigned long long)));
+	unsigned long long *counter = reinterpret_cast<unsigned long long *>(ctx->tables.ptr);
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+	root_check_kernel<<<sm_count() * 8, 256, 0, ctx->stream>>>(firstBits, count, counter);
+	add_launches(1);
+	DSRG_CUDA_TRY(ctx, cudaGetLastError());
+	unsigned long long found = 0;
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(&found, counter, sizeof(found), cudaMemcpyDeviceToHost, ctx->stream));
+	DSRG_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	*mismatches = found;
+	return DSRG_OK;
+}
+
+int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
+	if (!ctx) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!frame || !frame->view) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: null argument");
+	const dsrg_sprite_frame_desc &d = *frame;
+	const dsrg_image *given[5] = {d.height, d.diffuse, d.normal, d.light, d.output};
+	for (const dsrg_image *g : given)
+		if (!valid_image(g) || g->width != d.height->width || g->height != d.height->height)
+			return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: height, diffuse, normal, light and output must be images of one size");
+	if (d.spriteCount < 0 || (d.spriteCount > 0 && !d.sprites) || d.lightCount < 0 || (d.lightCount > 0 && !d.lights))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: null sprites or lights");
+	for (int32_t i = 0; i < d.spriteCount; i++)
+		if (!sprite_ok(d.sprites[i])) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: invalid sprite " + std::to_string(i));
+	if (d.shadows && batch_context(d.shadows) != ctx)
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: the shadow batch belongs to another context");
+	cudaSetDevice(ctx->device);
+	if (d.shadows && !batch_depth_in_place(d.shadows))
+		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: shadow cubes must be device or page-locked memory");
+	std::vector<dsrg_point_light> lights(d.lights, d.lights + d.lightCount);
+	for (dsrg_point_light &l : lights) {
+		if (!l.shadowCube) continue;
+		l.shadowCube = cube_in_place(l.shadowCube);
+		if (!l.shadowCube) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_sprite_frame: shadow cubes must be device or page-locked memory");
+	}
+	// every image of the frame placed once: the five frame images (written) and each distinct sprite source (read)
+	std::vector<CallMemory> mem;
+	std::vector<const dsrg_image *> images;
+	for (const dsrg_image *g : given) {
+		mem.push_back(call_image(g, true));
+		images.push_back(g);
+	}
+	std::vector<dsrg_sprite> sprites(d.sprites, d.sprites + d.spriteCount);
+	std::unordered_map<const void *, size_t> sourceBlock;
+	std::vector<size_t> spriteBlocks(sprites.size() * 3);
+	for (size_t i = 0; i < sprites.size(); i++) {
+		const dsrg_sprite &s = sprites[i];
+		const void *sources[3] = {s.height, s.colorA, s.colorB};
+		const int32_t strides[3] = {s.heightStrideBytes, s.colorAStrideBytes, s.colorBStrideBytes};
+		for (int k = 0; k < 3; k++) {
+			auto found = sourceBlock.find(sources[k]);
+			if (found == sourceBlock.end()) {
+				CallMemory m;
+				m.host = sources[k];
+				m.rowBytes = (size_t)s.width * 4;
+				m.strideBytes = (size_t)(strides[k] > 0 ? strides[k] : 0);
+				m.rows = (size_t)(s.height_ > 0 ? s.height_ : 0);
+				m.onDevice = s.onDevice != 0;
+				found = sourceBlock.emplace(sources[k], mem.size()).first;
+				mem.push_back(m);
+				images.push_back(nullptr);
+			}
+			spriteBlocks[3 * i + k] = found->second;
+		}
+	}
+	int status = place(ctx, mem);
+	if (status != DSRG_OK) return status;
+	dsrg_image placed[5];
+	for (int i = 0; i < 5; i++) {
+		placed[i] = *given[i];
+		placed[i].data = mem[i].device;
+		placed[i].strideBytes = (int32_t)mem[i].strideBytes;
+		placed[i].onDevice = 1;
+	}
+	for (size_t i = 0; i < sprites.size(); i++) {
+		dsrg_sprite &s = sprites[i];
+		const CallMemory &h = mem[spriteBlocks[3 * i]], &a = mem[spriteBlocks[3 * i + 1]], &b = mem[spriteBlocks[3 * i + 2]];
+		s.height = (const float *)h.device; s.heightStrideBytes = (int32_t)h.strideBytes;
+		s.colorA = (const uint32_t *)a.device; s.colorAStrideBytes = (int32_t)a.strideBytes;
+		s.colorB = (const uint32_t *)b.device; s.colorBStrideBytes = (int32_t)b.strideBytes;
+		s.onDevice = 1;
+	}
+	status = sprite_frame_steps(ctx, d, placed, sprites.data(), lights.data());
+	if (status != DSRG_OK) {
+		cudaStreamSynchronize(ctx->stream); // nothing of the frame stays in flight
+		cudaGetLastError();
+		return status;
+	}
+	return finish(ctx, mem, images.data()); // the staged frame images back to the caller, and the frame's last wait
 }
 
 } // extern "C"

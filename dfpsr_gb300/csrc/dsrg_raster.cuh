@@ -98,6 +98,24 @@ __device__ __forceinline__ void quad_lanes(float start, float dx, float dy, cons
 	}
 }
 
+// Position `lane` of quad_lanes alone: the same operations on the same values, for the one chain
+// that position's value comes from.
+__device__ __forceinline__ float quad_lane(float start, float dx, float dy, const RowPair &rp, int32_t y1, int32_t x, int lane) {
+	const float P0 = fadd(fadd(start, fmul(dx, (float)rp.obs + 0.5f)), fmul(dy, (float)y1 + 0.5f));
+	const float R0 = (lane < 2) ? P0 : fadd(P0, dy);
+	const float d2 = fmul(dx, 2.0f);
+	const bool odd = (lane & 1) != 0;
+	if (rp.ibe <= rp.ibs || x < rp.ibs) {
+		const float v = chain_add_short(R0, d2, (x - rp.obs) >> 1);
+		return odd ? fadd(v, dx) : v;
+	}
+	const float B = chain_add_short(R0, d2, (rp.ibs - rp.obs) >> 1);
+	if (x < rp.ibe) return chain_add_short(odd ? fadd(B, dx) : B, d2, (x - rp.ibs) >> 1);
+	const float m = fmul(d2, (float)((rp.ibe - rp.ibs) >> 1));
+	const float v = chain_add_short(fadd(B, m), d2, (x - rp.ibe) >> 1);
+	return odd ? fadd(v, dx) : v;
+}
+
 // Whether the quad at x lies in the pair's run of full quads (fillerTemplates.h:357-364).
 __device__ __forceinline__ bool full_quad(const RowPair &rp, int32_t x) {
 	return rp.ibe > rp.ibs && x >= rp.ibs && x < rp.ibe;
@@ -135,6 +153,19 @@ __device__ __forceinline__ uint32_t key_record(unsigned long long key, bool dept
 	return depthTest ? ~(uint32_t)(key & 0xFFFFFFFFull) : (uint32_t)key - 1u;
 }
 
+// Vertex weights of one position from its (1/W, U/W, V/W) or (W, U, V), as lane_weights gives them.
+__device__ __forceinline__ void lane_weight(float w0, float w1, float w2, bool affine, float &wa, float &wb, float &wc) {
+	if (affine) {
+		wb = w1;
+		wc = w2;
+	} else {
+		const float linearDepth = frcp(w0); // reciprocal of the scalar build (noSimd.h:187)
+		wb = fmul(w1, linearDepth);
+		wc = fmul(w2, linearDepth);
+	}
+	wa = 1.0f - fadd(wb, wc);
+}
+
 // Vertex weights of the four lanes from (1/W, U/W, V/W) or (W, U, V) (fillerTemplates.h:197-233).
 __device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, float *wa, float *wb, float *wc) {
 	for (int l = 0; l < 4; l++) {
@@ -142,7 +173,7 @@ __device__ __forceinline__ void lane_weights(const float (*w)[4], bool affine, f
 			wb[l] = w[1][l];
 			wc[l] = w[2][l];
 		} else {
-			const float linearDepth = fdiv(1.0f, w[0][l]); // reciprocal of the scalar build (noSimd.h:187)
+			const float linearDepth = frcp(w[0][l]); // reciprocal of the scalar build (noSimd.h:187)
 			wb[l] = fmul(w[1][l], linearDepth);
 			wc[l] = fmul(w[2][l], linearDepth);
 		}

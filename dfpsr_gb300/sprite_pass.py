@@ -55,7 +55,15 @@ class DeferredLightPass:
         self.light_list = [dict(l, cube=self.cubes[k]) for k, l in enumerate(scene.lights)]
 
     def run(self):
-        """One frame; returns the output image (device)."""
+        """One frame in one call (dsrg_sprite_frame); returns the output image (device)."""
+        s = self.scene
+        self.ctx.sprite_frame(self.view, s.center, (self.height, self.diffuse, self.normal, self.light, self.output),
+                              (BACKGROUND_HEIGHT, 0, 0), self.sprites, (s.sun_direction, s.sun_intensity, s.sun_color),
+                              self.shadows, self.light_list, self.threads)
+        return self.output
+
+    def run_steps(self):
+        """The same frame as one call per step; returns the output image (device)."""
         s = self.scene
         self.height.fill_(BACKGROUND_HEIGHT)
         self.diffuse.zero_()

@@ -440,6 +440,44 @@ typedef struct {
 int dsrg_draw_higher(dsrg_context context, const dsrg_image *targetHeight, const dsrg_image *targetA,
                      const dsrg_image *targetB, const dsrg_sprite *sprites, int32_t count);
 
+/* One frame of the sprite engine's deferred-light pass (the frame of spriteAPI.cpp:770-816 with
+ * its background cleared as BackgroundBlock::draw does, spriteAPI.cpp:525-527), in one call:
+ *   1. height = clearHeight, diffuse = clearDiffuse, normal = clearNormal;
+ *   2. draw_higher of every sprite into height, diffuse (colour A) and normal (colour B);
+ *   3. setDirectedLight with the sun into light (sunIntensity 0 and sunColor 0 give a black light);
+ *   4. the shadow batch (a depth-only batch of cube faces), its depth images cleared to 0 first
+ *      (CubeMapF32::clear, spriteAPI.cpp:361-363); null for no shadows;
+ *   5. addPointLight for every light (dsrg_light_points, with referenceThreads);
+ *   6. blendLight(output, diffuse, light).
+ * Every step runs on the context's stream in this order and the call waits twice: once inside the
+ * shadow batch (which checks its buffers) and once at its end.  The images are those of the steps
+ * above (device, page-locked or pageable host memory; each pageable image is copied in once and,
+ * if written, out once).  Shadow cubes (the batch's depth images and the lights' shadowCube) must
+ * be device or page-locked memory.  The result equals that of the six calls made one by one. */
+typedef struct {
+	const dsrg_ortho_view *view;
+	int32_t centerX, centerY;
+	const dsrg_image *height, *diffuse, *normal, *light, *output;
+	float clearHeight;
+	uint32_t clearDiffuse, clearNormal;
+	const dsrg_sprite *sprites;
+	int32_t spriteCount;
+	float sunDirection[3];
+	float sunIntensity;
+	int32_t sunColor[3];
+	dsrg_batch shadows;
+	const dsrg_point_light *lights;
+	int32_t lightCount;
+	int32_t referenceThreads;
+} dsrg_sprite_frame_desc;
+int dsrg_sprite_frame(dsrg_context context, const dsrg_sprite_frame_desc *frame);
+
+/* A self-check with no reference counterpart: the point lights compute the scalar build's
+ * (float)sqrt((double)x) and (float)(1.0 / sqrt((double)x)) as the correctly rounded float square
+ * root and reciprocal square root.  This counts, on the device, the floats x with bit patterns
+ * firstBits .. firstBits + count - 1 for which either pair differs (0 expected). */
+int dsrg_check_float_roots(dsrg_context context, uint32_t firstBits, uint32_t count, uint64_t *mismatches);
+
 /* model_renderDepth semantics for every frame of a batch (1 x 1 depth walk, no colour), for
  * shadow cube maps and other depth-only views: depthOnly = 1.  Frames need depth images only. */
 int dsrg_batch_set_depth_only(dsrg_batch batch, int32_t depthOnly);

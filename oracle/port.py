@@ -330,10 +330,19 @@ def blend_light(target_pack_order, diffuse, light):
 
 def draw_higher(target, source, left, top, offset):
     th, ta, tap, tb, tbp = target
-    sh, sa, sap, sb, sbp = source
     th = np.ascontiguousarray(th, np.float32).copy()
     ta = np.ascontiguousarray(ta, np.uint32).copy()
     tb = np.ascontiguousarray(tb, np.uint32).copy()
+    draw_higher_in_place((th, ta, tap, tb, tbp), source, left, top, offset)
+    return th, ta, tb
+
+
+def draw_higher_in_place(target, source, left, top, offset):
+    """draw_higher into target images that are C-contiguous float32 / uint32 arrays, changed in place."""
+    th, ta, tap, tb, tbp = target
+    sh, sa, sap, sb, sbp = source
+    assert th.flags.c_contiguous and ta.flags.c_contiguous and tb.flags.c_contiguous
+    assert th.dtype == np.float32 and ta.dtype == np.uint32 and tb.dtype == np.uint32
     sh = np.ascontiguousarray(sh, np.float32)
     sa = np.ascontiguousarray(sa, np.uint32)
     sb = np.ascontiguousarray(sb, np.uint32)
@@ -341,7 +350,6 @@ def draw_higher(target, source, left, top, offset):
     h, w = sh.shape
     _light_lib().or_draw_higher(th.ctypes.data, W, ta.ctypes.data, W, tap, tb.ctypes.data, W, tbp, W, H, sh.ctypes.data, w,
                                 sa.ctypes.data, w, sap, sb.ctypes.data, w, sbp, w, h, left, top, offset)
-    return th, ta, tb
 
 
 class OracleRenderer:

@@ -194,6 +194,8 @@ def _light_lib(variant: str):
         l.refh_blend_light.argtypes = [P, I, P, P, I, I]
         l.refh_draw_higher.argtypes = [P, P, I, P, I, I, I, P, P, I, P, I, I, I, I, I, F]
         l.refh_dense_render.argtypes = [P, I, P, P, I, F, I, I, P, P, P, I, I, F, F, P, I]
+        l.refh_light_frame.argtypes = [F, I, I, I, I, I, I, F, I, P, P, P, P, I, P, P, I, P, P, I, P, P, I, P, P, P, P]
+        l.refh_light_frame.restype = C.c_double
         l._light_ready = True
     return l
 
@@ -266,6 +268,33 @@ def draw_higher(target, source, left, top, offset, variant: str = "exact"):
     _light_lib(variant).refh_draw_higher(_ptr(th), _ptr(ta), tap, _ptr(tb), tbp, W, H, _ptr(sh), _ptr(sa), sap, _ptr(sb), sbp,
                                          w, h, left, top, offset)
     return th, ta, tb
+
+
+def light_frame(scene, frames: int = 1, background_height: float = -1000.0, variant: str = "exact"):
+    """One frame of the deferred-light pass (scenes.light_scene) through the reference's own
+    functions (refh_light_frame): returns (seconds of the fastest of `frames` runs, output, light,
+    height, cubes)."""
+    l = _light_lib(variant)
+    caster = RefModel(scene.caster, variant)
+    sources = [(np.ascontiguousarray(h, np.float32), np.ascontiguousarray(c, np.uint32), np.ascontiguousarray(n, np.uint32))
+               for h, c, n in zip(scene.sprite_heights, scene.sprite_diffuse, scene.sprite_normals)]
+    types = np.array([[h.shape[1], h.shape[0]] for h, _, _ in sources], np.int32)
+    ptrs = [(C.c_void_p * len(sources))(*[_ptr(s[k]) for s in sources]) for k in range(3)]
+    placements = np.ascontiguousarray(scene.placements, np.int32)
+    sun = np.array([*scene.sun_direction, scene.sun_intensity], np.float32)
+    sun_color = np.array(scene.sun_color, np.int32)
+    lights = np.array([[*x["position"], x["radius"], x["intensity"]] for x in scene.lights], np.float32).reshape(-1, 5)
+    colors = np.array([x["color"] for x in scene.lights], np.int32).reshape(-1, 3)
+    H, W, res = scene.height, scene.width, scene.cube_resolution
+    output = np.zeros((H, W), np.uint32)
+    light = np.zeros((H, W), np.uint32)
+    height = np.zeros((H, W), np.float32)
+    cubes = np.zeros((len(scene.lights), 6 * res, res), np.float32)
+    seconds = l.refh_light_frame(scene.camera_tilt, scene.pixels_per_tile, scene.view_index, W, H, int(scene.center[0]),
+                                 int(scene.center[1]), background_height, len(sources), _ptr(types), ptrs[0], ptrs[1], ptrs[2],
+                                 len(placements), _ptr(placements), caster.handle, res, _ptr(sun), _ptr(sun_color), len(lights),
+                                 _ptr(lights), _ptr(colors), frames, _ptr(output), _ptr(light), _ptr(height), _ptr(cubes))
+    return float(seconds), output, light, height, list(cubes)
 
 
 def dense_render(positions, polygons, colors, tilt, pixels_per_tile, view_index, height, diffuse, normal, origin, model_to_world,

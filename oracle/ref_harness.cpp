@@ -20,6 +20,7 @@
 #include "DFPSR/base/threading.h"
 #include <cstring>
 #include <cstdint>
+#include <vector>
 
 using namespace dsr;
 
@@ -449,6 +450,91 @@ void refh_draw_higher(float* targetHeight, uint32_t* targetA, int targetAPack, u
 	ImageRgbaU8 targetAImage = ta, targetBImage = tb;
 	draw_higher(targetHeightImage, sh_, targetAImage, sa, targetBImage, sb, left, top, offset);
 	copyOutF32(th_, targetHeight, tw, th); copyOutRgba(ta, targetA, tw, th); copyOutRgba(tb, targetB, tw, th);
+}
+
+
+// One frame of the sprite engine's deferred-light pass through the reference's own functions, on
+// images made once: height, diffuse and normal cleared (image_fill), draw_higher of every placement,
+// each light's cube map cleared and drawn with model_renderDepth of the caster on its six faces
+// (the sub-images of one 6 x res image, as CubeMapF32 and PointLight::renderModelShadow do,
+// spriteAPI.cpp:340-401), setDirectedLight, addPointLight per light (threadedSplit over the
+// hardware threads, lightAPI.cpp:186) and blendLight (spriteAPI.cpp:770-816).  The frame runs
+// `frames` times; returns the seconds of the fastest and leaves its images in the outputs.
+//   types: per sprite type w, h; typeHeights / typeDiffuse / typeNormals: per type image pointers
+//   placements: per sprite type, left, top and the offset's float bits
+//   sun: direction xyz, intensity; lights: per light x, y, z, radius, intensity; lightColors: rgb
+double refh_light_frame(float cameraTilt, int pixelsPerTile, int viewIndex, int width, int height, int centerX, int centerY,
+                        float backgroundHeight, int typeCount, const int* types, const float* const* typeHeights,
+                        const uint32_t* const* typeDiffuse, const uint32_t* const* typeNormals, int placementCount,
+                        const int* placements, void* casterHandle, int cubeResolution, const float* sun, const int* sunColor,
+                        int lightCount, const float* lights, const int* lightColors, int frames, uint32_t* output, uint32_t* lightOut,
+                        float* heightOut, float* cubesOut) {
+	OrthoSystem system(cameraTilt, pixelsPerTile);
+	const OrthoView& view = system.view[viewIndex];
+	Model& caster = ((ModelBox*)casterHandle)->model;
+	std::vector<AlignedImageF32> spriteHeights;
+	std::vector<OrderedImageRgbaU8> spriteDiffuse, spriteNormals;
+	for (int t = 0; t < typeCount; t++) {
+		const int w = types[2 * t], h = types[2 * t + 1];
+		spriteHeights.push_back(image_create_F32(w, h));
+		spriteDiffuse.push_back(image_create_RgbaU8(w, h));
+		spriteNormals.push_back(image_create_RgbaU8(w, h));
+		copyInF32(spriteHeights.back(), typeHeights[t], w, h);
+		copyInRgba(spriteDiffuse.back(), typeDiffuse[t], w, h);
+		copyInRgba(spriteNormals.back(), typeNormals[t], w, h);
+	}
+	AlignedImageF32 heightImage = image_create_F32(width, height);
+	OrderedImageRgbaU8 diffuseImage = image_create_RgbaU8(width, height);
+	OrderedImageRgbaU8 normalImage = image_create_RgbaU8(width, height);
+	OrderedImageRgbaU8 lightImage = image_create_RgbaU8(width, height);
+	AlignedImageRgbaU8 outputImage = image_create_RgbaU8_native(width, height, PackOrderIndex::RGBA);
+	std::vector<AlignedImageF32> cubes;
+	for (int k = 0; k < lightCount; k++) cubes.push_back(image_create_F32(cubeResolution, cubeResolution * 6));
+	float normalToWorld[9];
+	storeMatrix(view.normalToWorldSpace, normalToWorld);
+	double best = 1e30;
+	for (int f = 0; f < frames; f++) {
+		const double start = time_getSeconds();
+		image_fill(heightImage, backgroundHeight);
+		image_fill(diffuseImage, ColorRgbaI32(0));
+		image_fill(normalImage, ColorRgbaI32(0));
+		for (int i = 0; i < placementCount; i++) {
+			const int* p = placements + 4 * i;
+			float offset;
+			std::memcpy(&offset, &p[3], 4);
+			ImageF32 targetHeight = heightImage;
+			ImageRgbaU8 targetA = diffuseImage, targetB = normalImage;
+			draw_higher(targetHeight, spriteHeights[p[0]], targetA, spriteDiffuse[p[0]], targetB, spriteNormals[p[0]], p[1], p[2], offset);
+		}
+		for (int k = 0; k < lightCount; k++) {
+			image_fill(cubes[k], 0.0f);
+			const float* l = lights + 5 * k;
+			const Transform3D transform(FVector3D(-l[0], -l[1], -l[2]), FMatrix3x3());
+			for (int side = 0; side < 6; side++) {
+				float location[12];
+				refh_shadow_side(normalToWorld, side, location);
+				const Camera camera = makeCamera(location, 1, 1.0f, cubeResolution, cubeResolution, 0.01f, 1000.0f);
+				ImageF32 face = image_getSubImage(cubes[k], IRect(0, side * cubeResolution, cubeResolution, cubeResolution));
+				model_renderDepth(caster, transform, face, camera);
+			}
+		}
+		setDirectedLight(view, lightImage, normalImage, FVector3D(sun[0], sun[1], sun[2]), sun[3],
+		                 ColorRgbI32(sunColor[0], sunColor[1], sunColor[2]));
+		for (int k = 0; k < lightCount; k++) {
+			const float* l = lights + 5 * k;
+			addPointLight(view, IVector2D(centerX, centerY), lightImage, normalImage, heightImage, FVector3D(l[0], l[1], l[2]), l[3], l[4],
+			              ColorRgbI32(lightColors[3 * k], lightColors[3 * k + 1], lightColors[3 * k + 2]), cubes[k]);
+		}
+		blendLight(outputImage, diffuseImage, lightImage);
+		const double seconds = time_getSeconds() - start;
+		if (seconds < best) best = seconds;
+	}
+	if (output) copyOutRgba(outputImage, output, width, height);
+	if (lightOut) copyOutRgba(lightImage, lightOut, width, height);
+	if (heightOut) copyOutF32(heightImage, heightOut, width, height);
+	for (int k = 0; k < lightCount && cubesOut; k++)
+		copyOutF32(cubes[k], cubesOut + (size_t)k * cubeResolution * cubeResolution * 6, cubeResolution, cubeResolution * 6);
+	return best;
 }
 
 } // extern "C"

@@ -28,7 +28,7 @@ int main(void) {
 		(any_function)dsrg_diff_destroy, (any_function)dsrg_diff_forward, (any_function)dsrg_diff_l2_loss,
 		(any_function)dsrg_diff_adjoint, (any_function)dsrg_ortho_view_create, (any_function)dsrg_shadow_side_location,
 		(any_function)dsrg_light_directed, (any_function)dsrg_light_points, (any_function)dsrg_light_blend,
-		(any_function)dsrg_draw_higher, (any_function)dsrg_dense_model_create, (any_function)dsrg_dense_model_destroy,
+		(any_function)dsrg_draw_higher, (any_function)dsrg_sprite_frame, (any_function)dsrg_check_float_roots, (any_function)dsrg_dense_model_create, (any_function)dsrg_dense_model_destroy,
 		(any_function)dsrg_dense_render, (any_function)dsrg_dense_render_many,
 	};
 	size_t i, missing = 0;

@@ -191,3 +191,79 @@ def test_light_calls_and_draw_higher_take_host_images(ctx, memory):
     assert np.array_equal(gh.view(np.uint32), expected[0].view(np.uint32))
     assert np.array_equal(ga.view(np.uint32), expected[1])
     assert np.array_equal(gb.view(np.uint32), expected[2])
+
+
+@pytest.mark.parametrize("memory", ["device", "pageable", "page-locked"])
+def test_sprite_frame_in_one_call(ctx, memory):
+    """dsrg_sprite_frame (clears, draw_higher, directed light, the shadow batch, point lights and
+    blendLight queued on the library's stream with two waits) gives the oracle's frame, with the
+    frame images and sprite sources in device, pageable or page-locked memory, and equals the same
+    frame made one call per step."""
+    import dfpsr_gb300 as d
+    from dfpsr_gb300.sprite_pass import BACKGROUND_HEIGHT, DeferredLightPass
+    from oracle import light_pass
+    m, _ = d.ortho_view(-0.7, 64, 2).arrays()
+    scene = scenes.light_scene(seed=8, width=256, height=200, sprites=90, sprite_types=5, lights=3, radius_px=(50, 120),
+                               caster_triangles=200, cube_resolution=32, light_space=(m[9:18], m[0:9]))
+    out, light, height, diffuse, normal, cubes = light_pass.run(scene, THREADS)
+    gpu = DeferredLightPass(ctx, scene, THREADS)
+    steps_out = host(gpu.run_steps(), np.uint32).copy()
+    assert np.array_equal(steps_out, out)
+    if memory == "device":
+        got = host(gpu.run(), np.uint32)
+        assert np.array_equal(host(gpu.height, np.uint32), height.view(np.uint32))
+        assert np.array_equal(host(gpu.light, np.uint32), light)
+        assert np.array_equal(got, out)
+    else:
+        place = (lambda a: np.ascontiguousarray(a).copy()) if memory == "pageable" else _pinned
+        H, W = scene.height, scene.width
+        images = [place(np.full((H, W), 7.0, np.float32))] + [place(np.full((H, W), 0x01020304, np.uint32)) for _ in range(4)]
+        sprites = d.SpriteArray([dict(s, height=place(host(s["height"], np.float32)), color_a=place(host(s["color_a"], np.uint32)),
+                                      color_b=place(host(s["color_b"], np.uint32))) for s in _sprite_dicts(gpu)])
+        ctx.sprite_frame(gpu.view, scene.center, images, (BACKGROUND_HEIGHT, 0, 0), sprites,
+                         (scene.sun_direction, scene.sun_intensity, scene.sun_color), gpu.shadows, gpu.light_list, THREADS)
+        assert np.array_equal(images[0].view(np.uint32), height.view(np.uint32))
+        assert np.array_equal(images[1].view(np.uint32), diffuse)
+        assert np.array_equal(images[2].view(np.uint32), normal)
+        assert np.array_equal(images[3].view(np.uint32), light)
+        assert np.array_equal(images[4].view(np.uint32), out)
+    gpu.destroy()
+
+
+def _sprite_dicts(gpu):
+    out = []
+    for i in range(gpu.sprites.count):
+        s = gpu.sprites.array[i]
+        h, a, b = gpu.sprites._keep[i]
+        out.append({"height": h, "color_a": a, "color_b": b, "left": s.left, "top": s.top, "offset": s.offset})
+    return out
+
+
+def test_sprite_frame_rejects_pageable_shadow_cubes(ctx):
+    """Shadow cubes are read by the point lights after the shadow batch drew them: the frame takes
+    them in device or page-locked memory only, and says so."""
+    import dfpsr_gb300 as d
+    from dfpsr_gb300.sprite_pass import BACKGROUND_HEIGHT, DeferredLightPass
+    m, _ = d.ortho_view(-0.7, 64, 0).arrays()
+    scene = scenes.light_scene(seed=9, width=64, height=64, sprites=4, sprite_types=2, lights=1, radius_px=(20, 30),
+                               caster_triangles=20, cube_resolution=16, light_space=(m[9:18], m[0:9]))
+    gpu = DeferredLightPass(ctx, scene, THREADS)
+    pageable_cube = np.zeros((6 * 16, 16), np.float32)
+    lights = [dict(l, cube=pageable_cube) for l in gpu.light_list]
+    images = (gpu.height, gpu.diffuse, gpu.normal, gpu.light, gpu.output)
+    with pytest.raises(d.DsrgError) as e:
+        ctx.sprite_frame(gpu.view, scene.center, images, (BACKGROUND_HEIGHT, 0, 0), gpu.sprites,
+                         (scene.sun_direction, scene.sun_intensity, scene.sun_color), None, lights, THREADS)
+    assert e.value.status == 1 and "page-locked" in str(e.value)
+    gpu.destroy()
+
+
+def test_float_roots_equal_the_scalar_builds_double_roots(ctx):
+    """The point lights take the scalar build's (float)sqrt((double)x) and (float)(1.0 / sqrt((double)x))
+    as the correctly rounded float square root and reciprocal square root.  Checked on the device for
+    every float of [1, 4), which covers every positive input (x -> 4x scales both sides by exactly 2,
+    subnormal inputs included), and directly for zero and the subnormals, the largest floats up to
+    infinity and the first NaNs, and negative inputs."""
+    assert ctx.check_float_roots(0x3F800000, 1 << 24) == 0
+    for first, count in ((0x00000000, 1 << 23), (0x7F000000, (1 << 23) + 2), (0x80000000, 1 << 16), (0xBF800000, 1 << 16)):
+        assert ctx.check_float_roots(first, count) == 0, hex(first)
