@@ -125,12 +125,30 @@ bool batch_depth_in_place(dsrg_batch b) {
 }
 
 void batch_clear_depth(dsrg_batch b) {
+	// frames whose images follow one another in memory with one width and stride (the six faces of
+	// a cube map) are cleared as one rectangle
+	char *first = nullptr;
+	int32_t strideBytes = 0, width = 0, rows = 0;
+	auto flush = [&]() {
+		if (first) enqueue_fill_words(first, strideBytes / 4, width, rows, 0u, b->context->stream);
+		first = nullptr;
+	};
 	for (const auto &f : b->frames) {
 		if (!f.hasDepth) continue;
 		void *at = f.depth.data;
 		if (!f.depth.onDevice && !host_mapped(f.depth.data, &at)) continue; // excluded by batch_depth_in_place
-		enqueue_fill_words(at, f.depth.strideBytes / 4, f.width, f.height, 0u, b->context->stream);
+		char *p = static_cast<char *>(at);
+		if (first && p == first + (size_t)rows * strideBytes && f.depth.strideBytes == strideBytes && f.width == width) {
+			rows += f.height;
+			continue;
+		}
+		flush();
+		first = p;
+		strideBytes = f.depth.strideBytes;
+		width = f.width;
+		rows = f.height;
 	}
+	flush();
 }
 
 dsrg_context batch_context(dsrg_batch b) { return b->context; }

@@ -850,6 +850,7 @@ int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
 	std::vector<size_t> spriteBlocks(sprites.size() * 3);
 	for (size_t i = 0; i < sprites.size(); i++) {
 		const dsrg_sprite &s = sprites[i];
+		if (s.onDevice) continue; // device sources are used as given
 		const void *sources[3] = {s.height, s.colorA, s.colorB};
 		const int32_t strides[3] = {s.heightStrideBytes, s.colorAStrideBytes, s.colorBStrideBytes};
 		for (int k = 0; k < 3; k++) {
@@ -879,6 +880,7 @@ int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
 	}
 	for (size_t i = 0; i < sprites.size(); i++) {
 		dsrg_sprite &s = sprites[i];
+		if (s.onDevice) continue;
 		const CallMemory &h = mem[spriteBlocks[3 * i]], &a = mem[spriteBlocks[3 * i + 1]], &b = mem[spriteBlocks[3 * i + 2]];
 		s.height = (const float *)h.device; s.heightStrideBytes = (int32_t)h.strideBytes;
 		s.colorA = (const uint32_t *)a.device; s.colorAStrideBytes = (int32_t)a.strideBytes;
