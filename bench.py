@@ -571,6 +571,11 @@ def plain_record(ctx, scene, cfg, args, flush, dist, world, local, workload_key,
     from dfpsr_gb300 import replicas
     h, w = scene.height, scene.width
     model = d.Model(ctx, scene)
+    # the model's device arrays, which a frame reads at least once: positions (12 B per point),
+    # polygon indices (16 B), corner colours and texture coordinates (2 x 64 B per polygon) and
+    # the fan table (4 B per fan triangle)
+    model_bytes = (12 * int(np.asarray(scene.positions).shape[0]) + (16 + 128) * int(np.asarray(scene.poly_indices).shape[0])
+                   + 4 * int(scene.triangle_count))
     stream = torch.cuda.ExternalStream(ctx.stream)
     color = torch.zeros((h, w), dtype=torch.int32, device="cuda")
     depth = torch.zeros((h, w), dtype=torch.float32, device="cuda")
@@ -684,6 +689,13 @@ def plain_record(ctx, scene, cfg, args, flush, dist, world, local, workload_key,
                                         "algorithmic_bytes_per_launch": BYTES_PER_FRAGMENT * fragments,
                                         "note": "28 B per fragment counted before the depth test (the metric's unit); early "
                                                 "culling never walks most of them on high-overdraw scenes, so this can exceed 1"}},
+        "frame_roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_kind,
+                           "algorithmic_bytes": model_bytes + BYTES_PER_FRAGMENT * walked,
+                           "achieved": (model_bytes + BYTES_PER_FRAGMENT * walked) / (total_s / args.steps) / 1e9,
+                           "frac": (model_bytes + BYTES_PER_FRAGMENT * walked) / (total_s / args.steps) / 1e9 / peak,
+                           "model": "the whole frame: the model's device arrays read once (positions, polygon indices, corner "
+                                    "colours and texture coordinates, fan table) plus 28 B per walked fragment, over the "
+                                    "frame's CUDA-event time"},
         "gpu_launches": launches,
         "tuning": tuning,
         "clocks": clocks.summary(),
@@ -743,6 +755,7 @@ def summary(line):
     """The headline figures of every section in one short object, last on the line."""
     out = {f"{line['config']['workload'].split(',')[0]} frames/s": line["frames_per_s"],
            "e2e frames/s": line["e2e"]["frames_per_s"], "roofline frac (walked)": line["roofline"]["frac"],
+           "frame roofline frac": line["frame_roofline"]["frac"],
            "cpu_baseline frames/s": line.get("cpu_baseline", {}).get("frames_per_s")}
     if "c0" in line:
         c0 = line["c0"]

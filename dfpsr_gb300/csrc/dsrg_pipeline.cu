@@ -217,7 +217,9 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	TRY(ctx->binLists.reserve((size_t)binCap + 1));
 	TRY(ctx->bigList.reserve((size_t)recordCap + 1));
 	const uint64_t largest = std::max<uint64_t>(std::max<uint64_t>(nt, recordCap), 2 * (uint64_t)totals.tiles);
-	TRY(ctx->scanScratch.reserve(scan_scratch_elems((uint32_t)largest + 1)));
+	// the row and tile-list scans share one launch pair, with both arrays' chunk sums in the scratch
+	TRY(ctx->scanScratch.reserve(std::max(scan_scratch_elems((uint32_t)largest + 1),
+	                                      scan_scratch_elems(recordCap + 1) + scan_scratch_elems(2 * (uint32_t)totals.tiles + 1))));
 	FrameBuffers fb;
 	memset(&fb, 0, sizeof(fb));
 	fb.points.csis = ctx->pointCsis.ptr; fb.points.isy = ctx->pointIsy.ptr; fb.points.flat = ctx->pointFlat.ptr;
