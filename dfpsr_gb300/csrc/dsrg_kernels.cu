@@ -584,21 +584,39 @@ void launch_scan_device(const uint32_t *in, uint32_t *out, const uint32_t *nDevi
 }
 
 // The totals a batch's host side reads once its phases ran: records, rows, tile-list entries and
-// the error bits, gathered into one small block for a single copy.
+// the error bits, gathered into one small block for a single copy.  The same launch lists the
+// tiles that have entries (one thread per tile, warp-aggregated appends), so that the persistent
+// tile kernel pulls only those: frames that are mostly empty (shadow-cube faces) no longer send
+// every CTA through thousands of empty tiles.
 __global__ void gather_totals_kernel(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
-                                     const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out) {
+                                     const uint32_t *binOffsets, uint32_t tiles, const int32_t *errorFlag, uint32_t *out,
+                                     uint32_t *tileList, uint32_t *tileListCount) {
 	chain_enter();
-	const uint32_t records = triOffsets[triangles];
-	out[0] = records;
-	out[1] = rowOffsets[records < recordCapacity ? records : recordCapacity];
-	out[2] = binOffsets[binSlots];
-	out[3] = (uint32_t)*errorFlag;
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		const uint32_t records = triOffsets[triangles];
+		out[0] = records;
+		out[1] = rowOffsets[records < recordCapacity ? records : recordCapacity];
+		out[2] = binOffsets[2 * tiles];
+		out[3] = (uint32_t)*errorFlag;
+	}
+	if (!tileList) return;
+	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool drawn = t < tiles && binOffsets[2 * t] != binOffsets[2 * t + 2];
+	const uint32_t mask = __ballot_sync(0xFFFFFFFFu, drawn);
+	if (!mask) return;
+	const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1;
+	uint32_t base = 0;
+	if (lane == leader) base = atomicAdd(tileListCount, (uint32_t)__popc(mask));
+	base = __shfl_sync(0xFFFFFFFFu, base, leader);
+	if (drawn) tileList[base + __popc(mask & ((1u << lane) - 1u))] = t;
 }
 
 void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
-                          const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out, cudaStream_t stream) {
+                          const uint32_t *binOffsets, uint32_t tiles, const int32_t *errorFlag, uint32_t *out, uint32_t *tileList,
+                          uint32_t *tileListCount, cudaStream_t stream) {
 	COUNT_LAUNCH();
-	launch_chained(gather_totals_kernel, 1, 1, stream, triOffsets, triangles, rowOffsets, recordCapacity, binOffsets, binSlots, errorFlag, out);
+	launch_chained(gather_totals_kernel, tileList ? grid_for(tiles, 256) : 1u, tileList ? 256u : 1u, stream, triOffsets, triangles, rowOffsets,
+	               recordCapacity, binOffsets, tiles, errorFlag, out, tileList, tileListCount);
 }
 
 // ------------------------------------------------------------------ row intervals
@@ -980,7 +998,7 @@ __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawR
 // Zeroes a batch's tile counters (per-tile counts and cursors, the big-record count, the tile
 // queue) and its error bits in one launch at the start of its phases, so that no memset node sits
 // in the chain of dependent launches behind it.
-__global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tileQueue, int32_t *errorFlag) {
+__global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tileQueue, uint32_t *tileListCount, int32_t *errorFlag) {
 	chain_enter();
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
 		bins.counts[i] = 0u;
@@ -989,6 +1007,7 @@ __global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tile
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		if (bins.bigCount) *bins.bigCount = 0u;
 		if (tileQueue) *tileQueue = 0u;
+		if (tileListCount) *tileListCount = 0u;
 		if (errorFlag) *errorFlag = 0;
 	}
 }
@@ -996,7 +1015,7 @@ __global__ void clear_tiles_kernel(TileBins bins, uint32_t slots, uint32_t *tile
 void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *errorFlag, cudaStream_t stream) {
 	const uint32_t slots = 2 * b.totalTiles;
 	COUNT_LAUNCH();
-	launch_chained(clear_tiles_kernel, grid_for(slots, 256), 256, stream, bins, slots, b.tileQueue, errorFlag);
+	launch_chained(clear_tiles_kernel, grid_for(slots, 256), 256, stream, bins, slots, b.tileQueue, b.tileListCount, errorFlag);
 }
 
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
@@ -1167,6 +1186,29 @@ __device__ __forceinline__ void write_lane(const BatchParams &b, const FrameTarg
 	if (f.depth) f.depth[(size_t)py * f.depthStride + px] = depthValue;
 }
 
+// The depth model_renderDepth leaves at (px, py) when record ri wins the pixel: the reference's
+// 1 x 1 walk from its row's left end (executeTriangleDrawingDepth, renderCore.cpp:343-387).
+__device__ __forceinline__ float depth_walk_value(const DrawRecord *__restrict__ records, const uint32_t *__restrict__ rowOffsets,
+                                                  const uint32_t *__restrict__ rows, uint32_t ri, int32_t px, int32_t py) {
+	const DrawRecord r = records[ri];
+	int32_t left, right;
+	unpack_row(rows[rowOffsets[ri] + (py - r.top)], left, right);
+	const float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
+	return chain_add(value, r.dx[0], px - left);
+}
+
+// The depth of a depth-only winner from its key: the key's upper word is the ordered bits of the
+// very value the walk wrote (make_key), so it decodes to that value, except that +0 and -0 share
+// one key word; that word is walked again.
+__device__ __forceinline__ float depth_from_key(unsigned long long key, bool affine, const DrawRecord *__restrict__ records,
+                                                const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows,
+                                                int32_t px, int32_t py) {
+	uint32_t hi = (uint32_t)(key >> 32);
+	if (affine) hi = ~hi;
+	if (hi == 0x80000000u) return depth_walk_value(records, rowOffsets, rows, key_record(key, true), px, py);
+	return bitsf((hi & 0x80000000u) ? (hi & 0x7FFFFFFFu) : ~hi);
+}
+
 // The winner of one pixel, shaded and written: the reference's running sums of its quad
 // (quad_lanes), the vertex weights, RgbaMultiply and the packed colour and depth.  On the last row
 // of an odd-height target the depth-tested pixels are left to odd_row_kernel (their result depends
@@ -1246,7 +1288,12 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 	const int tid = threadIdx.x;
 	const int warp = tid >> 5, lane = tid & 31;
 	for (;;) {
-		if (tid == 0) { sharedTile = atomicAdd(b.tileQueue, 1u); fragmentSum = 0ull; }
+		if (tid == 0) {
+			const uint32_t next = atomicAdd(b.tileQueue, 1u);
+			// the listed tiles (those with entries), or every tile
+			sharedTile = !b.tileList ? next : (next < *b.tileListCount ? b.tileList[next] : 0xFFFFFFFFu);
+			fragmentSum = 0ull;
+		}
 		__syncthreads();
 		const uint32_t tile = sharedTile;
 		if (tile >= b.totalTiles) break;
@@ -1473,8 +1520,11 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 			if (inside) {
 				if (counting) coverageImage[(size_t)py * width + px] += coverage[me]; // zeroed before a frame's first run
 				if (!RESOLVE) keyImage[(size_t)py * width + px] = key;
+				// model_renderDepth: the winner's depth straight from its key, written by the tile pass itself
+				else if (DEPTH_ONLY_1X1 && key != 0ull)
+					f.depth[(size_t)py * f.depthStride + px] = depth_from_key(key, affine, records, rowOffsets, rows, px, py);
 			}
-			if (!RESOLVE) continue;
+			if (!RESOLVE || DEPTH_ONLY_1X1) continue;
 			// the tile's winners shaded right away (resolve_pixels_kernel fused into the tile pass): a
 			// warp whose quads each have one winner (or none) shares each quad's sums among its lanes;
 			// other warps, and every quad touching the image's edge or an odd height's last row (whose
@@ -1495,30 +1545,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		}
 		__syncthreads();
 	}
-}
-
-// model_renderDepth resolve, one thread per pixel: the winner's depth is the reference's 1 x 1
-// walk from its row's left end (executeTriangleDrawingDepth, renderCore.cpp:343-387).
-__global__ void __launch_bounds__(256) resolve_depth_kernel(BatchParams b, const DrawRecord *__restrict__ records,
-                                                            const uint32_t *__restrict__ binOffsets,
-                                                            const uint32_t *__restrict__ rowOffsets, const uint32_t *__restrict__ rows) {
-	chain_enter();
-	if (overflowed(b)) return;
-	const uint32_t tile = blockIdx.x;
-	if (binOffsets[2 * tile] == binOffsets[2 * tile + 2]) return; // nothing drawn: the key image was not written here
-	const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
-	const int32_t local = (int32_t)(tile - f.tileBase);
-	const int32_t px = (local % f.tilesX) * TILE_W + (threadIdx.x & 15), py = (local / f.tilesX) * TILE_H + (threadIdx.x >> 4);
-	if (px >= f.width || py >= f.height) return;
-	const unsigned long long key = f.keys[(size_t)py * f.width + px];
-	if (key == 0ull) return;
-	const uint32_t ri = key_record(key, true);
-	const DrawRecord r = records[ri];
-	int32_t left, right;
-	unpack_row(rows[rowOffsets[ri] + (py - r.top)], left, right);
-	float value = fadd(fadd(r.start[0], fmul(r.dx[0], (float)left + 0.5f)), fmul(r.dy[0], (float)py + 0.5f));
-	value = chain_add(value, r.dx[0], px - left);
-	f.depth[(size_t)py * f.depthStride + px] = value;
 }
 
 // One thread per pixel: the winning fragment's quad is re-evaluated exactly (its row pair's
@@ -1894,7 +1920,8 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	// small triangles resolve per pixel inside the tile pass; the keys then never leave the chip
 	const bool fused = resolve && !b.depthOnly && config.resolveMode == 1;
 #define DSRG_RASTER(T)                                                                                            \
-	if (b.depthOnly) launch_chained(raster_kernel<true, T, false>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	if (b.depthOnly && resolve) launch_chained(raster_kernel<true, T, true>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
+	else if (b.depthOnly) launch_chained(raster_kernel<true, T, false>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
 	else if (fused) launch_chained(raster_kernel<false, T, true>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows); \
 	else launch_chained(raster_kernel<false, T, false>, ctas, T, stream, b, fb.records, bins, fb.rowOffsets, fb.rows);
 	if (threads == 64) { DSRG_RASTER(64) }
@@ -1902,10 +1929,9 @@ void launch_raster(const BatchParams &b, const FrameBuffers &fb, const TileBins 
 	else { DSRG_RASTER(256) }
 #undef DSRG_RASTER
 	if (!resolve) return;
-	if (!fused) {
+	if (!fused && !b.depthOnly) { // depth-only batches resolve inside the tile pass (depth_from_key)
 		COUNT_LAUNCH();
-		if (b.depthOnly) launch_chained(resolve_depth_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
-		else if (config.resolveMode == 2) launch_chained(resolve_quads_kernel, b.totalTiles, 64, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
+		if (config.resolveMode == 2) launch_chained(resolve_quads_kernel, b.totalTiles, 64, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 		else launch_chained(resolve_pixels_kernel, b.totalTiles, 256, stream, b, fb.records, bins.offsets, fb.rowOffsets, fb.rows);
 	}
 	// the last rows of depth-tested odd-height frames, which every resolve above leaves alone

@@ -69,6 +69,8 @@ struct BatchParams {
 	int32_t oddDepthFrames;           // frames of odd height with a depth buffer (their last row: odd_row_kernel)
 	int32_t maxTilesX;                // the widest frame's tile columns
 	uint32_t *tileQueue;              // work counter of the persistent tile kernel
+	uint32_t *tileList;               // the tiles that have list entries (written at the end of phase C), or null: every tile
+	uint32_t *tileListCount;          // their number
 	const int32_t *errorFlag;         // device error bits; tile and resolve kernels return when an overflow is set
 };
 
@@ -203,7 +205,8 @@ void launch_draw_lines(uint32_t *image, int32_t stride, int32_t width, int32_t h
                        uint32_t color, cudaStream_t stream);
 // out[0..3] = record count, row count, tile-list entry count, error bits of a batch.
 void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,
-                          const uint32_t *binOffsets, uint32_t binSlots, const int32_t *errorFlag, uint32_t *out, cudaStream_t stream);
+                          const uint32_t *binOffsets, uint32_t tiles, const int32_t *errorFlag, uint32_t *out, uint32_t *tileList,
+                          uint32_t *tileListCount, cudaStream_t stream);
 // Exclusive scan of n uint32 values into out (out[n] = total); two launches, scratch of
 // scan_scratch_elems(n) values.
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream);

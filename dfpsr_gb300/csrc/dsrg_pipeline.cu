@@ -159,6 +159,7 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	const size_t tableBytes = layout_tables(job, nullptr, nullptr, nullptr, params, totals);
 	if (totals.pixels > 0) TRY(ctx->keys.reserve(totals.pixels));
 	TRY(ctx->tables.reserve(tableBytes));
+	TRY(ctx->tileList.reserve((size_t)totals.tiles + 1));
 	if (ctx->pinnedCapacity < tableBytes) {
 		if (ctx->pinnedTables) cudaFreeHost(ctx->pinnedTables);
 		ctx->pinnedTables = nullptr;
@@ -175,6 +176,11 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 	params.smallRows = ctx->smallRows;
 	params.smallWidth = ctx->smallWidth;
 	params.tileQueue = ctx->control.ptr;
+	// depth-only batches (shadow-cube faces) are mostly empty tiles: their tile kernel pulls only
+	// the listed ones.  Colour frames pull every tile in order, which measured faster for them
+	// (the listed order is not the tile order, and the list costs a wider totals launch).
+	params.tileList = job.depthOnly ? ctx->tileList.ptr : nullptr;
+	params.tileListCount = job.depthOnly ? ctx->control.ptr + 9 : nullptr;
 	params.fragments = nullptr;
 	params.walked = ctx->fragmentCounter.ptr + 1;
 	if (ctx->counting && !job.clearCounters) {
@@ -265,8 +271,8 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
 		launch_rows(fb, recordCap, tallTriangles, stream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
-		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, 2 * totals.tiles, fb.errorFlag,
-		                     gathered, stream);
+		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, totals.tiles, fb.errorFlag,
+		                     gathered, params.tileList, params.tileListCount, stream);
 	}));
 	if (!job.alpha) {
 		// phase D right behind, timed on the stream between the two graphs; after an overflow its
