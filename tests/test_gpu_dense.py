@@ -152,3 +152,33 @@ def test_dense_render_many_equals_calls_in_sequence(ctx, high_quality):
     _same(seq, (rh, rd, rn), "calls vs oracle")
     for m, _ in models:
         m.destroy()
+
+
+def test_benchmarked_dense_instances_full_size(ctx):
+    """The benchmarked dense-model sequence itself: 64 placements of a 3,200-triangle torus at
+    1920x1080 in one dsrg_dense_render_many call, against the oracle's 64 renderDenseModel calls."""
+    import torch
+    import dfpsr_gb300 as d
+    from dfpsr_gb300 import scenes
+    from oracle import port
+    sc = scenes.dense_scene(seed=77, width=1920, height=1080, major=80, minor=20, pixels_per_tile=64)
+    rng = np.random.default_rng(5)
+    places = [((float(rng.uniform(0, 1920)), float(rng.uniform(0, 1080))),
+               np.concatenate([rng.uniform(-1, 1, 3), scenes.random_rotation(rng).reshape(-1)]).astype(np.float32))
+              for _ in range(64)]
+    model = d.DenseModel(ctx, sc.positions, sc.polygons, sc.colors)
+    view = d.ortho_view(sc.camera_tilt, sc.pixels_per_tile, sc.view_index)
+    h = torch.tensor(sc.height, device="cuda")
+    di = torch.zeros((1080, 1920), dtype=torch.int32, device="cuda")
+    n = torch.zeros_like(di)
+    ctx.dense_render_many([(model, origin, transform) for origin, transform in places], view, h, di, n, False)
+    tris = port.dense_model(sc.positions, sc.polygons, sc.colors)
+    pv = port.ortho_view(sc.camera_tilt, sc.pixels_per_tile, sc.view_index)
+    rh, rd, rn = sc.height, np.zeros((1080, 1920), np.uint32), np.zeros((1080, 1920), np.uint32)
+    for origin, transform in places:
+        rh, rd, rn = port.dense_render(tris, pv, rh, rd, rn, origin, transform, False)
+    assert np.array_equal(h.cpu().numpy().view(np.uint32), rh.view(np.uint32))
+    assert np.array_equal(di.cpu().numpy().view(np.uint32), rd)
+    assert np.array_equal(n.cpu().numpy().view(np.uint32), rn)
+    assert (rd != 0).sum() > 10000
+    model.destroy()

@@ -267,3 +267,27 @@ def test_float_roots_equal_the_scalar_builds_double_roots(ctx):
     assert ctx.check_float_roots(0x3F800000, 1 << 24) == 0
     for first, count in ((0x00000000, 1 << 23), (0x7F000000, (1 << 23) + 2), (0x80000000, 1 << 16), (0xBF800000, 1 << 16)):
         assert ctx.check_float_roots(first, count) == 0, hex(first)
+
+
+def test_benchmarked_light_pass_full_size(ctx):
+    """The benchmarked deferred-light frame itself (scenes.light_scene(seed=2024): 1920x1080, 4096
+    sprites, 16 shadowed point lights with 6 x 512 x 512 cube maps from a 2,000-triangle caster), as
+    one dsrg_sprite_frame call, against the oracle's whole pass, image by image, bit for bit."""
+    import os
+    import dfpsr_gb300 as d
+    from dfpsr_gb300.sprite_pass import DeferredLightPass
+    from oracle import light_pass
+    m, _ = d.ortho_view(-0.7, 64, 0).arrays()
+    scene = scenes.light_scene(seed=2024, sprites=4096, light_space=(m[9:18], m[0:9]))
+    workers = os.cpu_count() or 1
+    out, light, height, diffuse, normal, cubes = light_pass.run(scene, THREADS, workers=workers)
+    gpu = DeferredLightPass(ctx, scene, THREADS)
+    got = host(gpu.run(), np.uint32)
+    assert np.array_equal(host(gpu.height, np.uint32), height.view(np.uint32))
+    assert np.array_equal(host(gpu.diffuse, np.uint32), diffuse)
+    assert np.array_equal(host(gpu.normal, np.uint32), normal)
+    for k, cube in enumerate(cubes):
+        assert np.array_equal(host(gpu.cubes[k], np.uint32), cube.view(np.uint32)), f"shadow cube {k}"
+    assert np.array_equal(host(gpu.light, np.uint32), light)
+    assert np.array_equal(got, out)
+    gpu.destroy()
