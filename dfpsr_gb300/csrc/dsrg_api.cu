@@ -93,6 +93,8 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	if (ctx->pinnedReadback) cudaFreeHost(ctx->pinnedReadback);
 	ctx->rowCounts.release(); ctx->rowOffsets.release(); ctx->rows.release(); ctx->textureTable.release(); ctx->fragmentCounter.release();
 	ctx->lightStaging.release();
+	ctx->spriteTableHost.release();
+	ctx->lightTableHost.release();
 	ctx->tileList.release();
 	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);

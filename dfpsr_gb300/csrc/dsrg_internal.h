@@ -48,6 +48,30 @@ struct DeviceBuffer {
 	}
 };
 
+// Page-locked host memory that a call fills and copies to the device asynchronously: a copy from
+// pageable memory would first wait for everything queued on the stream.  Grown as needed; the
+// call that filled it must be finished before the next one refills it.
+struct HostStaging {
+	unsigned char *ptr = nullptr;
+	size_t capacity = 0;
+	cudaError_t reserve(size_t n) {
+		if (n <= capacity) return cudaSuccess;
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		capacity = 0;
+		size_t c = 4096;
+		while (c < n) c *= 2;
+		const cudaError_t e = cudaMallocHost((void **)&ptr, c);
+		if (e == cudaSuccess) capacity = c;
+		return e;
+	}
+	void release() {
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		capacity = 0;
+	}
+};
+
 // Camera::createPerspective / createOrthogonal and ViewFrustum (implementation/render/Camera.h:55-156),
 // computed on the host in the reference's order (this file is built with -ffp-contract=off).
 inline Plane make_plane(float x, float y, float z, float offset) {
@@ -157,6 +181,7 @@ struct BatchTotals {
 } // namespace dsrg
 
 using dsrg::DeviceBuffer;
+using dsrg::HostStaging;
 using dsrg::DrawRecord;
 using dsrg::TaskParams;
 using dsrg::FrameTarget;
@@ -196,6 +221,7 @@ struct dsrg_context_s {
 	DeviceBuffer<unsigned char> textureTables;  // texture creation: work tables
 	DeviceBuffer<float> stagingDepth;
 	DeviceBuffer<uint32_t> lightStaging;        // light passes and draw_higher: pageable host images and sprites
+	HostStaging spriteTableHost, lightTableHost; // draw_higher's sprite table and the point lights' table on their way to the GPU
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;
 	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;

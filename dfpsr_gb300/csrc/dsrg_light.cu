@@ -552,7 +552,9 @@ int light_points_impl(dsrg_context ctx, const dsrg_ortho_view *view, int32_t cen
 	// the light table travels in the context's table buffer
 	const size_t bytes = params.size() * sizeof(PointLightParams);
 	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(bytes));
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, params.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+	DSRG_CUDA_TRY(ctx, ctx->lightTableHost.reserve(bytes));
+	memcpy(ctx->lightTableHost.ptr, params.data(), bytes);
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, ctx->lightTableHost.ptr, bytes, cudaMemcpyHostToDevice, ctx->stream));
 	PointFrame f;
 	memcpy(f.toLight, view->screenDepthToLightSpace, sizeof(f.toLight));
 	f.centerX = centerX;
@@ -612,11 +614,13 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 		d.left = s.left; d.top = s.top; d.offset = s.offset;
 		if (s.width * s.height_ > largest) largest = s.width * s.height_;
 	}
-	// the targets and every sprite's three sources where the kernels reach them
+	// the targets and every host sprite's three sources where the kernels reach them (device
+	// sources are used as given)
 	std::vector<CallMemory> mem = {call_image(targetHeight, true), call_image(targetA, true), call_image(targetB, true)};
 	std::vector<const dsrg_image *> images = {targetHeight, targetA, targetB};
 	for (int32_t i = 0; i < count; i++) {
 		const dsrg_sprite &s = sprites[i];
+		if (s.onDevice) continue;
 		const void *sources[3] = {s.height, s.colorA, s.colorB};
 		const int32_t strides[3] = {s.heightStrideBytes, s.colorAStrideBytes, s.colorBStrideBytes};
 		for (int k = 0; k < 3; k++) {
@@ -632,9 +636,10 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	}
 	const int placed = place(ctx, mem);
 	if (placed != DSRG_OK) return placed;
-	for (int32_t i = 0; i < count; i++) {
+	for (int32_t i = 0, placedSprite = 0; i < count; i++) {
+		if (sprites[i].onDevice) continue;
 		SpriteData &d = table[i];
-		const CallMemory *m = &mem[3 + 3 * (size_t)i];
+		const CallMemory *m = &mem[3 + 3 * (size_t)placedSprite++];
 		d.height = (const float *)m[0].device; d.heightStride = stride_of(m[0]);
 		d.colorA = (const uint32_t *)m[1].device; d.aStride = stride_of(m[1]);
 		d.colorB = (const uint32_t *)m[2].device; d.bStride = stride_of(m[2]);
@@ -643,7 +648,10 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	const size_t pixels = (size_t)width * height;
 	DSRG_CUDA_TRY(ctx, ctx->keys.reserve(pixels));
 	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(sizeof(SpriteData) * table.size()));
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, table.data(), sizeof(SpriteData) * table.size(), cudaMemcpyHostToDevice, ctx->stream));
+	DSRG_CUDA_TRY(ctx, ctx->spriteTableHost.reserve(sizeof(SpriteData) * table.size()));
+	memcpy(ctx->spriteTableHost.ptr, table.data(), sizeof(SpriteData) * table.size());
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, ctx->spriteTableHost.ptr, sizeof(SpriteData) * table.size(), cudaMemcpyHostToDevice,
+	                                   ctx->stream));
 	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
 	const SpriteData *deviceTable = reinterpret_cast<const SpriteData *>(ctx->tables.ptr);
 	const int32_t blocksPerSprite = (largest + 255) / 256 < 64 ? (largest + 255) / 256 : 64;
