@@ -600,15 +600,18 @@ __global__ void gather_totals_kernel(const uint32_t *triOffsets, uint32_t triang
 		out[3] = (uint32_t)*errorFlag;
 	}
 	if (!tileList) return;
-	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-	const bool drawn = t < tiles && binOffsets[2 * t] != binOffsets[2 * t + 2];
-	const uint32_t mask = __ballot_sync(0xFFFFFFFFu, drawn);
-	if (!mask) return;
-	const uint32_t lane = threadIdx.x & 31u, leader = __ffs(mask) - 1;
-	uint32_t base = 0;
-	if (lane == leader) base = atomicAdd(tileListCount, (uint32_t)__popc(mask));
-	base = __shfl_sync(0xFFFFFFFFu, base, leader);
-	if (drawn) tileList[base + __popc(mask & ((1u << lane) - 1u))] = t;
+	const uint32_t lane = threadIdx.x & 31u;
+	for (uint32_t first = blockIdx.x * blockDim.x; first < tiles; first += gridDim.x * blockDim.x) { // uniform per block
+		const uint32_t t = first + threadIdx.x;
+		const bool drawn = t < tiles && binOffsets[2 * t] != binOffsets[2 * t + 2];
+		const uint32_t mask = __ballot_sync(0xFFFFFFFFu, drawn);
+		if (!mask) continue;
+		const uint32_t leader = __ffs(mask) - 1;
+		uint32_t at = 0;
+		if (lane == leader) at = atomicAdd(tileListCount, (uint32_t)__popc(mask));
+		at = __shfl_sync(0xFFFFFFFFu, at, leader);
+		if (drawn) tileList[at + __popc(mask & ((1u << lane) - 1u))] = t;
+	}
 }
 
 void launch_gather_totals(const uint32_t *triOffsets, uint32_t triangles, const uint32_t *rowOffsets, uint32_t recordCapacity,

@@ -16,10 +16,11 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
 #include <thread>
-#include <unordered_map>
+#include <tuple>
 #include <vector>
 
 #include "dsrg_internal.h"
@@ -854,7 +855,8 @@ int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
 		images.push_back(g);
 	}
 	std::vector<dsrg_sprite> sprites(d.sprites, d.sprites + d.spriteCount);
-	std::unordered_map<const void *, size_t> sourceBlock;
+	// one block per distinct source (the same memory seen with the same size and stride)
+	std::map<std::tuple<const void *, int32_t, int32_t, int32_t>, size_t> sourceBlock;
 	std::vector<size_t> spriteBlocks(sprites.size() * 3);
 	for (size_t i = 0; i < sprites.size(); i++) {
 		const dsrg_sprite &s = sprites[i];
@@ -862,7 +864,8 @@ int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
 		const void *sources[3] = {s.height, s.colorA, s.colorB};
 		const int32_t strides[3] = {s.heightStrideBytes, s.colorAStrideBytes, s.colorBStrideBytes};
 		for (int k = 0; k < 3; k++) {
-			auto found = sourceBlock.find(sources[k]);
+			const auto key = std::make_tuple(sources[k], s.width, s.height_, strides[k]);
+			auto found = sourceBlock.find(key);
 			if (found == sourceBlock.end()) {
 				CallMemory m;
 				m.host = sources[k];
@@ -870,7 +873,7 @@ int dsrg_sprite_frame(dsrg_context ctx, const dsrg_sprite_frame_desc *frame) {
 				m.strideBytes = (size_t)(strides[k] > 0 ? strides[k] : 0);
 				m.rows = (size_t)(s.height_ > 0 ? s.height_ : 0);
 				m.onDevice = s.onDevice != 0;
-				found = sourceBlock.emplace(sources[k], mem.size()).first;
+				found = sourceBlock.emplace(key, mem.size()).first;
 				mem.push_back(m);
 				images.push_back(nullptr);
 			}

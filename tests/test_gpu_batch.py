@@ -241,3 +241,31 @@ def test_benchmarked_batch_frames_match_oracle(ctx):
         batch.destroy()
     finally:
         ctx.set_tuning(**{k: v for k, v in before.items()})
+
+
+def test_depth_only_batch_with_more_tiles_than_one_launch_covers(ctx):
+    """A depth-only batch (the shadow-map form) of 40 frames of 2048 x 2048: 655,360 tiles, more than
+    one pass of the totals launch's grid lists, so the listing of the tiles that have entries must
+    stride over them.  Every frame against the oracle's model_renderDepth, bit for bit."""
+    import torch
+    import dfpsr_gb300 as d
+    from oracle import port
+    batch = d.Batch(ctx)
+    batch.set_depth_only(True)
+    scenes_, images, models = [], [], []
+    for k in range(40):
+        s = scenes.random_triangles(seed=700 + k, triangles=60, width=2048, height=2048, texture_size=0)
+        scenes_.append(s)
+        m = d.Model(ctx, s)
+        models.append(m)
+        images.append(torch.zeros((2048, 2048), dtype=torch.float32, device="cuda"))
+        batch.add_frame(None, images[-1])
+        batch.give_task(k, m)
+    batch.render()
+    for k in (0, 13, 26, 39):  # frames from the start, the middle and the end of the tile range
+        want, _ = port.render_depth(scenes_[k])
+        assert np.array_equal(images[k].cpu().numpy().view(np.uint32), want.view(np.uint32)), f"frame {k}"
+        assert (want != 0).sum() > 1000
+    batch.destroy()
+    for m in models:
+        m.destroy()
