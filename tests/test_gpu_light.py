@@ -291,3 +291,28 @@ def test_benchmarked_light_pass_full_size(ctx):
     assert np.array_equal(host(gpu.light, np.uint32), light)
     assert np.array_equal(got, out)
     gpu.destroy()
+
+
+def test_sprite_frame_without_sprites_lights_or_shadows(ctx):
+    """A frame with no sprites, no point lights and no shadow batch: the clears, the directed light
+    over the cleared normals and the blend, as the calls one by one make them."""
+    import torch
+    import dfpsr_gb300 as d
+    H, W = 64, 96
+    view = d.ortho_view(-0.7, 64, 3)
+    images = [torch.zeros((H, W), dtype=torch.float32, device="cuda")] + \
+             [torch.zeros((H, W), dtype=torch.int32, device="cuda") for _ in range(4)]
+    sun = ((0.3, -1.0, 0.2), 0.8, (255, 220, 180))
+    normal_word = 0x00C08040
+    ctx.sprite_frame(view, (W // 2, H // 2), images, (-5.0, 0x11223344, normal_word), d.SpriteArray([]), sun, None, [], THREADS)
+    assert (host(images[0], np.float32) == -5.0).all()
+    assert (host(images[1], np.uint32) == 0x11223344).all()
+    assert (host(images[2], np.uint32) == normal_word).all()
+    normal = torch.full((H, W), normal_word, dtype=torch.int32, device="cuda")
+    light = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    ctx.light_directed(view, light, normal, sun[0], sun[1], sun[2], False)
+    assert np.array_equal(host(images[3], np.uint32), host(light, np.uint32))
+    out = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    ctx.light_blend(out, images[1], light)
+    assert np.array_equal(host(images[4], np.uint32), host(out, np.uint32))
+    assert ctx.check_float_roots(0x3F800000, 0) == 0
