@@ -966,35 +966,69 @@ __global__ void bin_kernel(BatchParams b, const DrawRecord *__restrict__ records
 	}
 }
 
-// The records bin_kernel deferred, one warp each over the tiles of its bound.
+// The records bin_kernel deferred.  A block takes BIG_GROUP of them at a time and its threads share
+// the (record, tile) pairs of their bounds evenly, so that one record spanning a whole frame is
+// spread over the block instead of keeping a single warp busy while the rest of the grid idles.
+static const int BIG_GROUP = 8;
+
+struct BigRecord {
+	DrawRecord rec;
+	uint32_t index, tileBase, large;
+	int32_t tx0, ty0, bw, tilesX, exact;
+};
+
 template <bool FILL>
 __global__ void __launch_bounds__(256) bin_big_kernel(BatchParams b, const DrawRecord *__restrict__ records, TileBins bins,
                                                       int32_t *errorFlag) {
 	chain_enter();
-	const uint32_t lane = threadIdx.x & 31;
-	const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+	__shared__ BigRecord held[BIG_GROUP];
+	__shared__ int32_t firstPair[BIG_GROUP + 1];
 	const uint32_t count = *bins.bigCount;
-	for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += warps) {
-		const uint32_t r = bins.bigList[w];
-		const DrawRecord rec = records[r];
-		const FrameTarget &f = b.frames[rec.frame];
-		const uint32_t large = (b.depthOnly || !record_is_small(rec, b.smallRows, b.smallWidth)) ? 1u : 0u;
-		const int32_t tx0 = rec.left >> 4, ty0 = rec.top >> 4;
-		int32_t tx1 = (rec.right - 1) >> 4, ty1 = (rec.bottom - 1) >> 4;
-		if (tx1 >= f.tilesX) tx1 = f.tilesX - 1;
-		if (ty1 >= f.tilesY) ty1 = f.tilesY - 1;
-		const int32_t bw = tx1 - tx0 + 1, bt = bw * (ty1 - ty0 + 1);
-		const bool exact = tile_test_is_exact(rec);
-		for (int32_t i = (int32_t)lane; i < bt; i += 32) {
-			const int32_t tx = tx0 + i % bw, ty = ty0 + i / bw;
-			if (exact && !tile_may_overlap(rec, tx * TILE_W, ty * TILE_H)) continue;
-			const uint32_t tile = 2u * (f.tileBase + (uint32_t)(ty * f.tilesX + tx)) + large;
+	for (uint32_t first = blockIdx.x * BIG_GROUP; first < count; first += gridDim.x * BIG_GROUP) { // uniform per block
+		if (threadIdx.x < BIG_GROUP) {
+			const uint32_t w = first + threadIdx.x;
+			int32_t pairs = 0;
+			if (w < count) {
+				BigRecord &h = held[threadIdx.x];
+				h.index = bins.bigList[w];
+				h.rec = records[h.index];
+				const FrameTarget &f = b.frames[h.rec.frame];
+				h.large = (b.depthOnly || !record_is_small(h.rec, b.smallRows, b.smallWidth)) ? 1u : 0u;
+				h.tx0 = h.rec.left >> 4;
+				h.ty0 = h.rec.top >> 4;
+				const int32_t tx1 = min((h.rec.right - 1) >> 4, f.tilesX - 1), ty1 = min((h.rec.bottom - 1) >> 4, f.tilesY - 1);
+				h.bw = tx1 - h.tx0 + 1;
+				h.tilesX = f.tilesX;
+				h.tileBase = f.tileBase;
+				h.exact = tile_test_is_exact(h.rec) ? 1 : 0;
+				pairs = (h.bw > 0 && ty1 >= h.ty0) ? h.bw * (ty1 - h.ty0 + 1) : 0;
+			}
+			// prefix sums of the group's pair counts within the first BIG_GROUP lanes
+			int32_t inclusive = pairs;
+			for (int o = 1; o < BIG_GROUP; o <<= 1) {
+				const int32_t v = __shfl_up_sync((1u << BIG_GROUP) - 1u, inclusive, o);
+				if ((int)threadIdx.x >= o) inclusive += v;
+			}
+			firstPair[threadIdx.x + 1] = inclusive;
+			if (threadIdx.x == 0) firstPair[0] = 0;
+		}
+		__syncthreads();
+		const int32_t total = firstPair[BIG_GROUP];
+		for (int32_t i = (int32_t)threadIdx.x; i < total; i += (int32_t)blockDim.x) {
+			int k = 0;
+			while (firstPair[k + 1] <= i) k++;
+			const BigRecord &h = held[k];
+			const int32_t local = i - firstPair[k];
+			const int32_t tx = h.tx0 + local % h.bw, ty = h.ty0 + local / h.bw;
+			if (h.exact && !tile_may_overlap(h.rec, tx * TILE_W, ty * TILE_H)) continue;
+			const uint32_t tile = 2u * (h.tileBase + (uint32_t)(ty * h.tilesX + tx)) + h.large;
 			uint32_t slot = atomicAdd(FILL ? &bins.cursors[tile] : &bins.counts[tile], 1u);
 			if (FILL) {
 				slot += bins.offsets[tile];
-				if (slot < bins.listCapacity) bins.lists[slot] = r; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
+				if (slot < bins.listCapacity) bins.lists[slot] = h.index; else atomicOr(errorFlag, ERROR_BIN_OVERFLOW);
 			}
 		}
+		__syncthreads(); // the group is done with before the next one is loaded
 	}
 }
 
@@ -1275,6 +1309,8 @@ __device__ __forceinline__ void resolve_shared_quad(const BatchParams &b, const 
 // which evaluates the running sums once at the tile's left edge and then walks on.
 // All fragments compete for the tile's shared keys; the winners go to the frame's key image.
 // Tiles that nothing covers write nothing: the resolve pass skips them too.
+static const int SHARED_FRAMES = 256;
+
 template <bool DEPTH_ONLY_1X1, int THREADS, bool RESOLVE>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchParams b, const DrawRecord *__restrict__ records,
                                                                          TileBins bins, const uint32_t *__restrict__ rowOffsets,
@@ -1288,13 +1324,19 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 	__shared__ uint32_t coverage[TILE_H * TILE_STRIDE];
 	__shared__ uint32_t sharedTile;
 	__shared__ unsigned long long fragmentSum;
+	__shared__ uint32_t frameBases[SHARED_FRAMES]; // the frames' first tiles, for batches of up to SHARED_FRAMES frames
 	const int tid = threadIdx.x;
 	const int warp = tid >> 5, lane = tid & 31;
+	const bool framesShared = b.frameCount <= SHARED_FRAMES;
+	if (framesShared)
+		for (int i = tid; i < b.frameCount; i += THREADS) frameBases[i] = b.frameTileBase[i];
+	const uint32_t listed = (tid == 0 && b.tileList) ? *b.tileListCount : 0u;
 	for (;;) {
 		if (tid == 0) {
-			const uint32_t next = atomicAdd(b.tileQueue, 1u);
-			// the listed tiles (those with entries), or every tile
-			sharedTile = !b.tileList ? next : (next < *b.tileListCount ? b.tileList[next] : 0xFFFFFFFFu);
+			// the listed tiles (those with entries), or every tile.  (A ticket taken one tile ahead
+			// hides the atomic's round trip but holds a tile back from idle CTAs: slower overall.)
+			const uint32_t ticket = atomicAdd(b.tileQueue, 1u);
+			sharedTile = !b.tileList ? ticket : (ticket < listed ? b.tileList[ticket] : 0xFFFFFFFFu);
 			fragmentSum = 0ull;
 		}
 		__syncthreads();
@@ -1302,7 +1344,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		if (tile >= b.totalTiles) break;
 		const uint32_t smallBegin = bins.offsets[2 * tile], smallEnd = bins.offsets[2 * tile + 1], end = bins.offsets[2 * tile + 2];
 		if (smallBegin == end) { __syncthreads(); continue; }
-		const FrameTarget &f = b.frames[find_segment(b.frameTileBase, b.frameCount, tile)];
+		const FrameTarget &f = b.frames[framesShared ? find_segment_shared(frameBases, b.frameCount, tile)
+		                                             : find_segment(b.frameTileBase, b.frameCount, tile)];
 		const int32_t width = f.width, height = f.height;
 		const float *depthImage = f.depth;
 		const bool depthTest = depthImage != nullptr;
@@ -1323,8 +1366,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) raster_kernel(BatchPa
 		__syncthreads();
 
 		uint32_t fragments = 0;
-		// early depth culling needs a depth buffer and is off while fragments are being counted
-		const bool cull = depthTest && b.fragments == nullptr;
+		// early depth culling needs a depth buffer and is off while fragments are being counted; the
+		// 1x1 depth walk of depth-only frames is cheaper than the culling test itself
+		const bool cull = depthTest && b.fragments == nullptr && !DEPTH_ONLY_1X1;
 		const int32_t validW = min(TILE_W, width - tx0), validH = min(TILE_H, height - ty0);
 		uint32_t tileMin = 0u; // this warp's view of the tile's depth threshold (0: nothing culled yet)
 		// small records: dealt round-robin over the warps (warp w of W takes entries w, w + W, ...).

@@ -19,6 +19,16 @@ __device__ __forceinline__ int32_t find_segment(const uint32_t *base, int32_t co
 	return lo;
 }
 
+// find_segment over a copy of the bases in shared memory.
+__device__ __forceinline__ int32_t find_segment_shared(const uint32_t *base, int32_t count, uint32_t i) {
+	int32_t lo = 0, hi = count - 1;
+	while (lo < hi) {
+		const int32_t mid = (lo + hi + 1) >> 1;
+		if (base[mid] <= i) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
 __device__ __forceinline__ void unpack_row(uint32_t packed, int32_t &left, int32_t &right) {
 	left = (int32_t)(packed & 0xFFFFu);
 	right = (int32_t)(packed >> 16);
