@@ -369,6 +369,8 @@ def light_section(ctx, args):
     scene = scenes.light_scene(seed=2024, sprites=args.light_sprites, light_space=(m[9:18], m[0:9]))
     threads = os.cpu_count() or 1
     gpu = DeferredLightPass(ctx, scene, threads)
+    # the shadow batch's own tile-kernel shape, chosen by the autotuner on it (the context's stays)
+    shadow_tuning = gpu.tune_shadows(rounds=2)
     stream = torch.cuda.ExternalStream(ctx.stream)
     steps = max(1, min(args.steps, 20))
 
@@ -415,6 +417,7 @@ def light_section(ctx, args):
               "frame_call": "dsrg_sprite_frame: every step on the library's stream, a host wait inside the shadow batch "
                             "and one at the end; CUDA events on that stream",
               "ms_per_frame_one_call_per_step": ms_steps,
+              "shadow_batch_tuning": "{threads_per_tile}x{ctas_per_sm}x{small_rows}x{small_width}x{resolve}".format(**shadow_tuning),
               "point_lights_ms": statistics.median(lt), "lit_pixel_lights": bounds,
               "point_lights_GB_per_s": 20.0 * bounds / (statistics.median(lt) / 1e3) / 1e9,
               "parity_with_oracle": bool(np.array_equal(got, out)),

@@ -33,7 +33,7 @@ EXPORTED = [
     "dsrg_batch_render", "dsrg_context_get_tuning", "dsrg_context_set_tuning", "dsrg_batch_autotune",
     "dsrg_diff_create", "dsrg_diff_destroy", "dsrg_diff_forward", "dsrg_diff_l2_loss", "dsrg_diff_adjoint",
     "dsrg_ortho_view_create", "dsrg_shadow_side_location", "dsrg_light_directed", "dsrg_light_points", "dsrg_light_blend",
-    "dsrg_draw_higher", "dsrg_sprite_frame", "dsrg_check_float_roots", "dsrg_batch_set_depth_only",
+    "dsrg_draw_higher", "dsrg_sprite_frame", "dsrg_check_float_roots", "dsrg_batch_set_depth_only", "dsrg_batch_set_tuning",
     "dsrg_dense_model_create", "dsrg_dense_model_destroy", "dsrg_dense_render", "dsrg_dense_render_many",
     "dsrg_renderer_occlude_from_box", "dsrg_renderer_occlude_from_existing_triangles", "dsrg_renderer_occlude_from_top_rows",
     "dsrg_renderer_is_box_visible", "dsrg_renderer_has_occluders", "dsrg_renderer_get_occlusion_grid",
@@ -180,6 +180,7 @@ def lib():
                                         C.c_float, C.c_float, P, I]
         l.dsrg_dense_render_many.argtypes = [P, P, I, C.POINTER(OrthoView), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), I]
         l.dsrg_batch_set_depth_only.argtypes = [P, I]
+        l.dsrg_batch_set_tuning.argtypes = [P, C.POINTER(Tuning)]
         l.dsrg_sprite_frame.argtypes = [P, C.POINTER(SpriteFrame)]
         l.dsrg_check_float_roots.argtypes = [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64)]
         _lib = l
@@ -742,6 +743,16 @@ class Batch:
 
     def set_depth_only(self, on: bool):
         self.ctx._check(self.ctx._l.dsrg_batch_set_depth_only(self.handle, 1 if on else 0))
+
+    def set_tuning(self, tuning: Optional[dict] = None):
+        """dsrg_batch_set_tuning: this batch's own tile-kernel configuration (a dict as
+        Context.tuning() returns; None: the context's)."""
+        if tuning is None:
+            self.ctx._check(self.ctx._l.dsrg_batch_set_tuning(self.handle, None))
+            return
+        t = Tuning(tuning["threads_per_tile"], tuning["ctas_per_sm"], tuning["small_rows"], tuning["small_width"],
+                   int(tuning.get("graphs", 1)), tuning.get("resolve", 1))
+        self.ctx._check(self.ctx._l.dsrg_batch_set_tuning(self.handle, C.byref(t)))
 
     def clear(self):
         self.ctx._check(self.ctx._l.dsrg_batch_clear(self.handle))

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <utility>
 #include <cstring>
 #include <new>
@@ -34,6 +35,8 @@ struct dsrg_batch_s {
 	DeviceBuffer<float> stagingDepth;
 	std::vector<void *> mapped; // per frame: device addresses of page-locked colour and depth images
 	bool depthOnly = false; // model_renderDepth semantics for every frame
+	bool hasTuning = false; // the batch's own tile-kernel configuration (else the context's)
+	dsrg_tuning tuning;
 	BatchJob job;
 	BatchJob runs; // one pass of a batch whose frames draw several runs
 };
@@ -248,8 +251,22 @@ int dsrg_batch_give_task(dsrg_batch b, int32_t frameIndex, dsrg_model m, const f
 	return DSRG_OK;
 }
 
+static int batch_render_with_context_tuning(dsrg_batch b);
+
 int dsrg_batch_render(dsrg_batch b) {
 	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!b->hasTuning) return batch_render_with_context_tuning(b);
+	// the batch's own configuration for this render, the context's back afterwards
+	dsrg_context ctx = b->context;
+	dsrg_tuning saved;
+	dsrg_context_get_tuning(ctx, &saved);
+	int status = dsrg_context_set_tuning(ctx, &b->tuning);
+	if (status == DSRG_OK) status = batch_render_with_context_tuning(b);
+	dsrg_context_set_tuning(ctx, &saved);
+	return status;
+}
+
+static int batch_render_with_context_tuning(dsrg_batch b) {
 	dsrg_context ctx = b->context;
 	cudaSetDevice(ctx->device);
 	cudaStream_t stream = ctx->stream;
@@ -351,22 +368,45 @@ int dsrg_context_get_tuning(dsrg_context ctx, dsrg_tuning *out) {
 	return DSRG_OK;
 }
 
+static int check_tuning(dsrg_context ctx, const dsrg_tuning *t, const char *caller) {
+	char message[200];
+	const char *problem = nullptr;
+	if (t->threadsPerTile != 64 && t->threadsPerTile != 128 && t->threadsPerTile != 256)
+		problem = "threadsPerTile must be 64, 128 or 256";
+	else if (t->ctasPerSm < 1 || t->ctasPerSm > 1024 / t->threadsPerTile)
+		problem = "ctasPerSm must be between 1 and 1024 / threadsPerTile";
+	else if (t->smallRows < 0 || t->smallWidth < 0 || t->smallRows > 16 || t->smallWidth > 64)
+		problem = "small-triangle bound out of range (rows 0..16, width 0..64)";
+	else if (t->resolve < 0 || t->resolve > 2)
+		problem = "resolve must be 0 (per pixel, own pass), 1 (per pixel, in the tile kernel) or 2 (per quad)";
+	if (!problem) return DSRG_OK;
+	snprintf(message, sizeof(message), "%s: %s", caller, problem);
+	return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, message);
+}
+
 int dsrg_context_set_tuning(dsrg_context ctx, const dsrg_tuning *t) {
 	if (!ctx || !t) return DSRG_ERROR_INVALID_ARGUMENT;
-	if (t->threadsPerTile != 64 && t->threadsPerTile != 128 && t->threadsPerTile != 256)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: threadsPerTile must be 64, 128 or 256");
-	if (t->ctasPerSm < 1 || t->ctasPerSm > 1024 / t->threadsPerTile)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: ctasPerSm must be between 1 and 1024 / threadsPerTile");
-	if (t->smallRows < 0 || t->smallWidth < 0 || t->smallRows > 16 || t->smallWidth > 64)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: small-triangle bound out of range (rows 0..16, width 0..64)");
+	const int status = check_tuning(ctx, t, "dsrg_context_set_tuning");
+	if (status != DSRG_OK) return status;
 	ctx->threadsPerTile = t->threadsPerTile;
 	ctx->ctasPerSm = t->ctasPerSm;
 	ctx->smallRows = t->smallRows;
 	ctx->smallWidth = t->smallWidth;
-	if (t->resolve < 0 || t->resolve > 2)
-		return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_context_set_tuning: resolve must be 0 (per pixel, own pass), 1 (per pixel, in the tile kernel) or 2 (per quad)");
 	ctx->useGraphs = t->graphs ? 1 : 0;
 	ctx->resolveMode = t->resolve;
+	return DSRG_OK;
+}
+
+int dsrg_batch_set_tuning(dsrg_batch b, const dsrg_tuning *t) {
+	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
+	if (!t) {
+		b->hasTuning = false;
+		return DSRG_OK;
+	}
+	const int status = check_tuning(b->context, t, "dsrg_batch_set_tuning");
+	if (status != DSRG_OK) return status;
+	b->tuning = *t;
+	b->hasTuning = true;
 	return DSRG_OK;
 }
 
@@ -374,8 +414,22 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 	if (!b) return DSRG_ERROR_INVALID_ARGUMENT;
 	dsrg_context ctx = b->context;
 	if (rounds < 1) rounds = 1;
+	// a batch with a configuration of its own is searched from it and keeps the result; the
+	// context's configuration is then left as it was
+	dsrg_tuning contextTuning;
+	dsrg_context_get_tuning(ctx, &contextTuning);
+	const bool own = b->hasTuning;
+	if (own) dsrg_context_set_tuning(ctx, &b->tuning);
+	b->hasTuning = false; // the candidates are set on the context while searching
 	dsrg_tuning start;
 	dsrg_context_get_tuning(ctx, &start);
+	struct Restore { // whatever the search's outcome
+		dsrg_batch batch; dsrg_context context; dsrg_tuning tuning; bool own;
+		~Restore() {
+			batch->hasTuning = own;
+			if (own) dsrg_context_set_tuning(context, &tuning);
+		}
+	} restore{b, ctx, contextTuning, own};
 	struct Shape { int32_t threads, perSm; };
 	const Shape shapes[] = {{256, 4}, {256, 2}, {128, 8}, {128, 4}, {64, 16}};
 	const int32_t smalls[][2] = {{8, 16}, {0, 0}, {4, 8}};
@@ -448,7 +502,8 @@ int dsrg_batch_autotune(dsrg_batch b, int32_t rounds, dsrg_tuning *best) {
 		}
 	}
 	if (flush) cudaFree(flush);
-	dsrg_context_set_tuning(ctx, &chosen);
+	if (own) b->tuning = chosen; // the context gets its own configuration back (Restore)
+	else dsrg_context_set_tuning(ctx, &chosen);
 	if (best) *best = chosen;
 	return DSRG_OK;
 }

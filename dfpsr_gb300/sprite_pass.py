@@ -54,6 +54,13 @@ class DeferredLightPass:
                 self.shadows.give_task(frame, self.caster, cam, transform)
         self.light_list = [dict(l, cube=self.cubes[k]) for k, l in enumerate(scene.lights)]
 
+    def tune_shadows(self, rounds: int = 2) -> dict:
+        """Gives the shadow batch a tile-kernel configuration of its own, the autotuner's choice for
+        it (cube faces of large triangles suit other shapes than the frames drawn with the
+        context's configuration, which stays as it is)."""
+        self.shadows.set_tuning(self.ctx.tuning())
+        return self.shadows.autotune(rounds)
+
     def run(self):
         """One frame in one call (dsrg_sprite_frame); returns the output image (device)."""
         s = self.scene

@@ -299,9 +299,16 @@ typedef struct {
 int dsrg_context_get_tuning(dsrg_context context, dsrg_tuning *out);
 int dsrg_context_set_tuning(dsrg_context context, const dsrg_tuning *tuning);
 /* Renders the batch once per candidate configuration (rounds times each, each timed render
- * starting from a cold L2 cache), keeps the fastest for the context and returns it in *best (may
- * be null).  The images end up holding the batch's rendered frames. */
+ * starting from a cold L2 cache), keeps the fastest and returns it in *best (may be null): for the
+ * batch when it has a configuration of its own (dsrg_batch_set_tuning), the context's staying as
+ * it was, else for the context.  The images end up holding the batch's rendered frames. */
 int dsrg_batch_autotune(dsrg_batch batch, int32_t rounds, dsrg_tuning *best);
+
+/* A tile-kernel configuration for this batch alone (no counterpart in the reference): its renders
+ * use *tuning and leave the context's configuration as it is, so that batches of different
+ * workloads (a frame of small triangles, shadow faces of large ones) each keep the shape that
+ * suits them.  tuning = null returns the batch to the context's configuration. */
+int dsrg_batch_set_tuning(dsrg_batch batch, const dsrg_tuning *tuning);
 
 /* ---- differentiable rendering; no counterpart in the reference.
  *

@@ -23,7 +23,7 @@ int main(void) {
 		(any_function)dsrg_renderer_has_occluders, (any_function)dsrg_renderer_get_occlusion_grid,
 		(any_function)dsrg_model_render_depth_noalloc, (any_function)dsrg_batch_create, (any_function)dsrg_batch_destroy,
 		(any_function)dsrg_batch_clear, (any_function)dsrg_batch_add_frame, (any_function)dsrg_batch_give_task,
-		(any_function)dsrg_batch_set_depth_only, (any_function)dsrg_batch_render, (any_function)dsrg_batch_autotune,
+		(any_function)dsrg_batch_set_depth_only, (any_function)dsrg_batch_set_tuning, (any_function)dsrg_batch_render, (any_function)dsrg_batch_autotune,
 		(any_function)dsrg_context_get_tuning, (any_function)dsrg_context_set_tuning, (any_function)dsrg_diff_create,
 		(any_function)dsrg_diff_destroy, (any_function)dsrg_diff_forward, (any_function)dsrg_diff_l2_loss,
 		(any_function)dsrg_diff_adjoint, (any_function)dsrg_ortho_view_create, (any_function)dsrg_shadow_side_location,

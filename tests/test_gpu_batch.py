@@ -269,3 +269,47 @@ def test_depth_only_batch_with_more_tiles_than_one_launch_covers(ctx):
     batch.destroy()
     for m in models:
         m.destroy()
+
+
+def test_batch_with_a_tuning_of_its_own(ctx):
+    """dsrg_batch_set_tuning: the batch renders with its own configuration, the context's is left
+    as it was (also by the autotuner, which then keeps its choice for the batch), the images are
+    those of the frames drawn one by one, and a configuration out of range is refused."""
+    import dfpsr_gb300 as d
+    frame_scenes = _frames(seed=15, frames=4, max_triangles=2000)
+    models = [d.Model(ctx, s) for s in frame_scenes]
+    expected = [_alone(ctx, m, s) for m, s in zip(models, frame_scenes)]
+    before = ctx.tuning()
+    try:
+        batch = d.Batch(ctx)
+        imgs = []
+        for i, (m, s) in enumerate(zip(models, frame_scenes)):
+            imgs.append((np.zeros((s.height, s.width), np.uint32), np.zeros((s.height, s.width), np.float32)))
+            batch.add_frame(*imgs[-1])
+            batch.give_task(i, m)
+        own = dict(before, threads_per_tile=64, ctas_per_sm=16, resolve=2)
+        batch.set_tuning(own)
+        batch.render()
+        assert ctx.tuning() == before
+        for (c, z), (ec, ez) in zip(imgs, expected):
+            assert _same(c, ec) and _same(z, ez)
+        best = batch.autotune(rounds=1)
+        assert ctx.tuning() == before
+        assert best["threads_per_tile"] in (64, 128, 256)
+        for c, z in imgs:
+            c[:] = 0
+            z[:] = 0
+        batch.render()
+        assert ctx.tuning() == before
+        for (c, z), (ec, ez) in zip(imgs, expected):
+            assert _same(c, ec) and _same(z, ez)
+        with pytest.raises(d.DsrgError, match="threadsPerTile"):
+            batch.set_tuning(dict(before, threads_per_tile=96))
+        batch.set_tuning(None)
+        batch.render()
+        assert ctx.tuning() == before
+        batch.destroy()
+    finally:
+        ctx.set_tuning(**{k: v for k, v in before.items()})
+        for m in models:
+            m.destroy()
