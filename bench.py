@@ -50,6 +50,8 @@ def parse_args():
     p.add_argument("--diff-views", type=int, default=64, help="views of the differentiable render (0 skips it)")
     p.add_argument("--light-sprites", type=int, default=4096, help="sprites of the deferred-light pass (0 skips it)")
     p.add_argument("--c0", type=int, default=1, help="also measure the 800x600 random-triangle workload (0 skips it)")
+    p.add_argument("--shadow-tuning", default="auto",
+                   help="the light pass's shadow batch: auto (the autotuner on that batch) or TxCxRxWxM like --tuning")
     p.add_argument("--tuning", default="auto",
                    help="tile kernel launch shape THREADSxCTAS_PER_SMxSMALL_ROWSxSMALL_WIDTH[xRESOLVE] (e.g. 128x8x8x16x1), or auto")
     return p.parse_args()
@@ -370,7 +372,13 @@ def light_section(ctx, args):
     threads = os.cpu_count() or 1
     gpu = DeferredLightPass(ctx, scene, threads)
     # the shadow batch's own tile-kernel shape, chosen by the autotuner on it (the context's stays)
-    shadow_tuning = gpu.tune_shadows(rounds=2)
+    if args.shadow_tuning == "auto":
+        shadow_tuning = gpu.tune_shadows(rounds=2)
+    else:  # a given shape (profiling runs keep the autotuner's trial launches out of the launch list)
+        fields = [int(v) for v in args.shadow_tuning.split("x")]
+        shadow_tuning = dict(ctx.tuning(), threads_per_tile=fields[0], ctas_per_sm=fields[1], small_rows=fields[2],
+                             small_width=fields[3], resolve=fields[4] if len(fields) > 4 else 1)
+        gpu.shadows.set_tuning(shadow_tuning)
     stream = torch.cuda.ExternalStream(ctx.stream)
     steps = max(1, min(args.steps, 20))
 
