@@ -239,6 +239,28 @@ def _sprite_dicts(gpu):
     return out
 
 
+def test_sprite_frame_first_call_on_a_fresh_context(built):
+    """On a fresh context the large shadow triangles of 256 x 256 cube faces outgrow the row and
+    tile-list buffers the shadow batch starts with; the batch is redone with grown buffers inside
+    the call, and the first call already gives the oracle's frame (and so does the next one)."""
+    import dfpsr_gb300 as d
+    from dfpsr_gb300.sprite_pass import DeferredLightPass
+    from oracle import light_pass
+    m, _ = d.ortho_view(-0.7, 64, 1).arrays()
+    scene = scenes.light_scene(seed=10, width=256, height=200, sprites=40, sprite_types=4, lights=2, radius_px=(60, 120),
+                               caster_triangles=100, cube_resolution=256, light_space=(m[9:18], m[0:9]))
+    out, *_ = light_pass.run(scene, THREADS)
+    fresh = d.Context(0)
+    try:
+        gpu = DeferredLightPass(fresh, scene, THREADS)
+        assert np.array_equal(host(gpu.run(), np.uint32), out)
+        assert fresh.stats()["draw_records"] > 0  # the statistics of the checked shadow batch
+        assert np.array_equal(host(gpu.run(), np.uint32), out)
+        gpu.destroy()
+    finally:
+        fresh.close()
+
+
 def test_sprite_frame_rejects_pageable_shadow_cubes(ctx):
     """Shadow cubes are read by the point lights after the shadow batch drew them: the frame takes
     them in device or page-locked memory only, and says so."""
