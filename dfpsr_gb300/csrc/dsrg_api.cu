@@ -57,7 +57,11 @@ int dsrg_context_create(int32_t device, dsrg_context *out) {
 	if (!ctx) return DSRG_ERROR_OUT_OF_MEMORY;
 	ctx->device = device;
 	memset(&ctx->stats, 0, sizeof(ctx->stats));
-	if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+	// the context's stream at the device's highest priority: a sprite frame's side stream (lowest)
+	// then only fills what the shadow batch on this stream leaves free
+	int leastPriority = 0, greatestPriority = 0;
+	if (cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority) != cudaSuccess) greatestPriority = 0;
+	if (cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatestPriority) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
 	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(2) != cudaSuccess ||
@@ -95,6 +99,11 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	ctx->lightStaging.release();
 	ctx->spriteTableHost.release();
 	ctx->lightTableHost.release();
+	ctx->spriteKeys.release();
+	ctx->spriteTables.release();
+	if (ctx->sideStart) cudaEventDestroy(ctx->sideStart);
+	if (ctx->sideDone) cudaEventDestroy(ctx->sideDone);
+	if (ctx->sideStream) cudaStreamDestroy(ctx->sideStream);
 	ctx->tileList.release();
 	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);

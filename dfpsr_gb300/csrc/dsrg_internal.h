@@ -222,6 +222,10 @@ struct dsrg_context_s {
 	DeviceBuffer<float> stagingDepth;
 	DeviceBuffer<uint32_t> lightStaging;        // light passes and draw_higher: pageable host images and sprites
 	HostStaging spriteTableHost, lightTableHost; // draw_higher's sprite table and the point lights' table on their way to the GPU
+	DeviceBuffer<unsigned long long> spriteKeys; // draw_higher's per-pixel keys and its sprite table, apart from the
+	DeviceBuffer<unsigned char> spriteTables;    // pipeline's, so that a sprite frame can draw sprites beside its shadows
+	cudaStream_t sideStream = nullptr;           // a sprite frame's second stream (created on first use)
+	cudaEvent_t sideStart = nullptr, sideDone = nullptr;
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;
 	DeviceBuffer<uint32_t> rowCounts, rowOffsets, rows;

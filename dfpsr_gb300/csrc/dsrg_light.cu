@@ -297,23 +297,30 @@ __device__ __forceinline__ uint32_t ordered_height(float h) {
 }
 
 // Every source pixel raised above the initial target height bids (height, ~sprite) for its pixel.
-__global__ void higher_keys_kernel(const SpriteData *__restrict__ sprites, int32_t first, int32_t count,
-                                   const float *__restrict__ targetHeight, int32_t thStride, int32_t width, int32_t height,
-                                   unsigned long long *keys) {
+// Blocks of 64 x 4 threads: columns over threadIdx.x, rows over threadIdx.y and the sprite's blocks
+// (blockIdx.x; blockIdx.y is the sprite).  Keys only grow, so a bid that a key already in place
+// beats (read without the atomic; a stale read is only smaller) is dropped before the atomic.
+__global__ void __launch_bounds__(256) higher_keys_kernel(const SpriteData *__restrict__ sprites, int32_t first, int32_t count,
+                                                          const float *__restrict__ targetHeight, int32_t thStride, int32_t width,
+                                                          int32_t height, unsigned long long *keys) {
 	const int32_t s = first + (int32_t)blockIdx.y;
 	if (s >= count) return;
 	const SpriteData sp = sprites[s];
-	const int32_t pixels = sp.width * sp.height_;
-	for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += gridDim.x * blockDim.x) {
-		const int32_t sx = i % sp.width, sy = i / sp.width;
-		const int32_t x = sp.left + sx, y = sp.top + sy;
-		if (x < 0 || y < 0 || x >= width || y >= height) continue;
-		float h = sp.height[(size_t)sy * sp.heightStride + sx];
-		if (!(h > -INFINITY)) continue;
-		h = fadd(h, sp.offset);
-		if (!(h > targetHeight[(size_t)y * thStride + x])) continue;
-		const unsigned long long key = ((unsigned long long)ordered_height(h) << 32) | (unsigned long long)(~(uint32_t)s);
-		atomicMax(&keys[(size_t)y * width + x], key);
+	const unsigned long long low = (unsigned long long)(~(uint32_t)s);
+	for (int32_t sy = (int32_t)(blockIdx.x * blockDim.y + threadIdx.y); sy < sp.height_; sy += (int32_t)(gridDim.x * blockDim.y)) {
+		const int32_t y = sp.top + sy;
+		if (y < 0 || y >= height) continue;
+		for (int32_t sx = (int32_t)threadIdx.x; sx < sp.width; sx += (int32_t)blockDim.x) {
+			const int32_t x = sp.left + sx;
+			if (x < 0 || x >= width) continue;
+			float h = sp.height[(size_t)sy * sp.heightStride + sx];
+			if (!(h > -INFINITY)) continue;
+			h = fadd(h, sp.offset);
+			if (!(h > targetHeight[(size_t)y * thStride + x])) continue;
+			const unsigned long long key = ((unsigned long long)ordered_height(h) << 32) | low;
+			unsigned long long *slot = &keys[(size_t)y * width + x];
+			if (key > *slot) atomicMax(slot, key);
+		}
 	}
 }
 
@@ -603,7 +610,7 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	cudaSetDevice(ctx->device);
 	if (count == 0) return DSRG_OK;
 	std::vector<SpriteData> table(count);
-	int32_t largest = 1;
+	int32_t tallest = 1;
 	for (int32_t i = 0; i < count; i++) {
 		const dsrg_sprite &s = sprites[i];
 		if (!sprite_ok(s)) return fail(ctx, DSRG_ERROR_INVALID_ARGUMENT, "dsrg_draw_higher: invalid sprite " + std::to_string(i));
@@ -613,7 +620,7 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 		d.heightStride = s.heightStrideBytes / 4; d.aStride = s.colorAStrideBytes / 4; d.bStride = s.colorBStrideBytes / 4;
 		d.aPack = s.colorAPackOrder; d.bPack = s.colorBPackOrder;
 		d.left = s.left; d.top = s.top; d.offset = s.offset;
-		if (s.width * s.height_ > largest) largest = s.width * s.height_;
+		if (s.height_ > tallest) tallest = s.height_;
 	}
 	// the targets and every host sprite's three sources where the kernels reach them (device
 	// sources are used as given)
@@ -647,23 +654,24 @@ int draw_higher_impl(dsrg_context ctx, const dsrg_image *targetHeight, const dsr
 	}
 	const int32_t width = targetHeight->width, height = targetHeight->height;
 	const size_t pixels = (size_t)width * height;
-	DSRG_CUDA_TRY(ctx, ctx->keys.reserve(pixels));
-	DSRG_CUDA_TRY(ctx, ctx->tables.reserve(sizeof(SpriteData) * table.size()));
+	DSRG_CUDA_TRY(ctx, ctx->spriteKeys.reserve(pixels));
+	DSRG_CUDA_TRY(ctx, ctx->spriteTables.reserve(sizeof(SpriteData) * table.size()));
 	DSRG_CUDA_TRY(ctx, ctx->spriteTableHost.reserve(sizeof(SpriteData) * table.size()));
 	memcpy(ctx->spriteTableHost.ptr, table.data(), sizeof(SpriteData) * table.size());
-	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tables.ptr, ctx->spriteTableHost.ptr, sizeof(SpriteData) * table.size(), cudaMemcpyHostToDevice,
+	DSRG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->spriteTables.ptr, ctx->spriteTableHost.ptr, sizeof(SpriteData) * table.size(), cudaMemcpyHostToDevice,
 	                                   ctx->stream));
-	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->keys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
-	const SpriteData *deviceTable = reinterpret_cast<const SpriteData *>(ctx->tables.ptr);
-	const int32_t blocksPerSprite = (largest + 255) / 256 < 64 ? (largest + 255) / 256 : 64;
+	DSRG_CUDA_TRY(ctx, cudaMemsetAsync(ctx->spriteKeys.ptr, 0, pixels * sizeof(unsigned long long), ctx->stream));
+	const SpriteData *deviceTable = reinterpret_cast<const SpriteData *>(ctx->spriteTables.ptr);
+	// about four rows per thread: 16 rows per block of 64 x 4 threads
+	const int32_t blocksPerSprite = (tallest + 15) / 16 < 64 ? (tallest + 15) / 16 : 64;
 	for (int32_t first = 0; first < count; first += 65535) { // grid y is limited to 65535 sprites per launch
 		const int32_t n = count - first < 65535 ? count - first : 65535;
-		higher_keys_kernel<<<dim3(blocksPerSprite, n), 256, 0, ctx->stream>>>(deviceTable, first, count, (const float *)mem[0].device,
-		                                                                     stride_of(mem[0]), width, height, ctx->keys.ptr);
+		higher_keys_kernel<<<dim3(blocksPerSprite, n), dim3(64, 4), 0, ctx->stream>>>(deviceTable, first, count, (const float *)mem[0].device,
+		                                                                             stride_of(mem[0]), width, height, ctx->spriteKeys.ptr);
 		add_launches(1);
 	}
 	const dim3 grid((width + 255) / 256, height);
-	higher_resolve_kernel<<<grid, 256, 0, ctx->stream>>>(deviceTable, ctx->keys.ptr, (float *)mem[0].device, stride_of(mem[0]),
+	higher_resolve_kernel<<<grid, 256, 0, ctx->stream>>>(deviceTable, ctx->spriteKeys.ptr, (float *)mem[0].device, stride_of(mem[0]),
 	                                                     (uint32_t *)mem[1].device, stride_of(mem[1]), targetA->packOrder,
 	                                                     (uint32_t *)mem[2].device, stride_of(mem[2]), targetB->packOrder, width, height);
 	add_launches(1);
@@ -682,9 +690,10 @@ const float *cube_in_place(const float *cube) {
 }
 
 // The steps of one sprite frame after its images were placed (see dsrg_sprite_frame).
-int sprite_frame_steps(dsrg_context ctx, const dsrg_sprite_frame_desc &d, const dsrg_image *img, const dsrg_sprite *sprites,
-                       const dsrg_point_light *lights) {
-	const dsrg_image &height = img[0], &diffuse = img[1], &normal = img[2], &light = img[3], &output = img[4];
+// The clears, draw_higher and the directed light of a sprite frame: they touch neither the shadow
+// cubes nor the buffers of the shadow batch.
+int sprite_frame_images(dsrg_context ctx, const dsrg_sprite_frame_desc &d, const dsrg_image *img, const dsrg_sprite *sprites) {
+	const dsrg_image &height = img[0], &diffuse = img[1], &normal = img[2], &light = img[3];
 	uint32_t clearHeight;
 	memcpy(&clearHeight, &d.clearHeight, 4);
 	enqueue_fill_words(height.data, height.strideBytes / 4, height.width, height.height, clearHeight, ctx->stream);
@@ -692,14 +701,44 @@ int sprite_frame_steps(dsrg_context ctx, const dsrg_sprite_frame_desc &d, const 
 	enqueue_fill_words(normal.data, normal.strideBytes / 4, normal.width, normal.height, d.clearNormal, ctx->stream);
 	add_launches(3);
 	DSRG_CUDA_TRY(ctx, cudaGetLastError());
-	int status = draw_higher_impl(ctx, &height, &diffuse, &normal, sprites, d.spriteCount, false);
+	const int status = draw_higher_impl(ctx, &height, &diffuse, &normal, sprites, d.spriteCount, false);
 	if (status != DSRG_OK) return status;
-	status = light_directed_impl(ctx, d.view, &light, &normal, d.sunDirection, d.sunIntensity, d.sunColor, 0, false);
-	if (status != DSRG_OK) return status;
+	return light_directed_impl(ctx, d.view, &light, &normal, d.sunDirection, d.sunIntensity, d.sunColor, 0, false);
+}
+
+int sprite_frame_steps(dsrg_context ctx, const dsrg_sprite_frame_desc &d, const dsrg_image *img, const dsrg_sprite *sprites,
+                       const dsrg_point_light *lights) {
+	const dsrg_image &height = img[0], &diffuse = img[1], &normal = img[2], &light = img[3], &output = img[4];
+	int status = DSRG_OK;
 	if (d.shadows) {
-		batch_clear_depth(d.shadows);
-		DSRG_CUDA_TRY(ctx, cudaGetLastError());
-		status = dsrg_batch_render(d.shadows); // checks its buffers on the host: the frame's first wait
+		// the sprite images on a second stream beside the shadow batch (whose short, latency-bound
+		// launches leave most of the GPU's issue slots free), joined before the point lights
+		if (!ctx->sideStream) {
+			int leastPriority = 0, greatestPriority = 0;
+			DSRG_CUDA_TRY(ctx, cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority));
+			DSRG_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->sideStream, cudaStreamNonBlocking, leastPriority));
+			DSRG_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->sideStart, cudaEventDisableTiming));
+			DSRG_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->sideDone, cudaEventDisableTiming));
+		}
+		cudaStream_t mainStream = ctx->stream;
+		DSRG_CUDA_TRY(ctx, cudaEventRecord(ctx->sideStart, mainStream)); // after the frame's images were placed
+		DSRG_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->sideStream, ctx->sideStart, 0));
+		ctx->stream = ctx->sideStream;
+		status = sprite_frame_images(ctx, d, img, sprites);
+		ctx->stream = mainStream;
+		// the main stream waits for the side stream whatever happens next, so that a wait for the
+		// main stream covers both
+		const cudaError_t recorded = cudaEventRecord(ctx->sideDone, ctx->sideStream);
+		if (status == DSRG_OK && recorded == cudaSuccess) {
+			batch_clear_depth(d.shadows);
+			status = cudaGetLastError() == cudaSuccess ? dsrg_batch_render(d.shadows) // its host wait is for the main stream
+			                                           : fail(ctx, DSRG_ERROR_CUDA, "sprite frame: clearing the shadow cubes failed");
+		}
+		const cudaError_t joined = recorded == cudaSuccess ? cudaStreamWaitEvent(mainStream, ctx->sideDone, 0) : recorded;
+		if (status != DSRG_OK) return status;
+		DSRG_CUDA_TRY(ctx, joined);
+	} else {
+		status = sprite_frame_images(ctx, d, img, sprites);
 		if (status != DSRG_OK) return status;
 	}
 	status = light_points_impl(ctx, d.view, d.centerX, d.centerY, &light, &normal, &height, lights, d.lightCount, d.referenceThreads,
