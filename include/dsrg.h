@@ -237,7 +237,7 @@ int dsrg_debug_fail_allocation(int64_t after);
  *     DSRG_NOALLOC_MAX_ROWS pixel rows or DSRG_NOALLOC_MAX_BIN_ENTRIES (tile, triangle) pairs,
  *     are rejected with DSRG_ERROR_UNSUPPORTED and a message naming the limit.
  *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- *     and keeps it for the life of the process; make that first call before any stream capture.
+ *     and keeps it for the life of the process.
  *     A device reset (cudaDeviceReset) inside the process is not supported afterwards.
  *   - Each call returns with its work finished: it reads counts back to the host between its
  *     kernels and waits for them on the context's stream.
