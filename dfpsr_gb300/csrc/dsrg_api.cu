@@ -62,6 +62,9 @@ int dsrg_context_create(int32_t device, dsrg_context *out) {
 	int leastPriority = 0, greatestPriority = 0;
 	if (cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority) != cudaSuccess) greatestPriority = 0;
 	if (cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatestPriority) != cudaSuccess ||
+	    cudaStreamCreateWithPriority(&ctx->branchStream, cudaStreamNonBlocking, greatestPriority) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&ctx->branchFork, cudaEventDisableTiming) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&ctx->branchJoin, cudaEventDisableTiming) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventStart) != cudaSuccess || cudaEventCreate(&ctx->eventStop) != cudaSuccess ||
 	    cudaEventCreate(&ctx->eventRasterStart) != cudaSuccess || cudaEventCreate(&ctx->eventRasterStop) != cudaSuccess ||
 	    ctx->control.reserve(16) != cudaSuccess || ctx->fragmentCounter.reserve(2) != cudaSuccess ||
@@ -104,6 +107,9 @@ int dsrg_context_destroy(dsrg_context ctx) {
 	if (ctx->sideStart) cudaEventDestroy(ctx->sideStart);
 	if (ctx->sideDone) cudaEventDestroy(ctx->sideDone);
 	if (ctx->sideStream) cudaStreamDestroy(ctx->sideStream);
+	if (ctx->branchFork) cudaEventDestroy(ctx->branchFork);
+	if (ctx->branchJoin) cudaEventDestroy(ctx->branchJoin);
+	if (ctx->branchStream) cudaStreamDestroy(ctx->branchStream);
 	ctx->tileList.release();
 	for (PhaseGraph &g : ctx->graphs) g.reset();
 	cudaEventDestroy(ctx->eventStart);

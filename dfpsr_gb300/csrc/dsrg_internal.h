@@ -225,6 +225,8 @@ struct dsrg_context_s {
 	DeviceBuffer<unsigned long long> spriteKeys; // draw_higher's per-pixel keys and its sprite table, apart from the
 	DeviceBuffer<unsigned char> spriteTables;    // pipeline's, so that a sprite frame can draw sprites beside its shadows
 	cudaStream_t sideStream = nullptr;           // a sprite frame's second stream (created on first use)
+	cudaStream_t branchStream = nullptr;         // a batch's second branch: the row intervals beside the tile lists
+	cudaEvent_t branchFork = nullptr, branchJoin = nullptr;
 	cudaEvent_t sideStart = nullptr, sideDone = nullptr;
 	DeviceBuffer<unsigned long long> fragmentCounter;
 	DeviceBuffer<unsigned long long> keys;

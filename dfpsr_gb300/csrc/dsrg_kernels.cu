@@ -47,6 +47,12 @@ static void memset_async(void *p, int value, size_t bytes, cudaStream_t stream) 
 	if (e != cudaSuccess && t_enqueueError == cudaSuccess) t_enqueueError = e;
 }
 
+void enqueue_join(cudaStream_t from, cudaStream_t to, cudaEvent_t event) {
+	cudaError_t e = cudaEventRecord(event, from);
+	if (e == cudaSuccess) e = cudaStreamWaitEvent(to, event, 0);
+	if (e != cudaSuccess && t_enqueueError == cudaSuccess) t_enqueueError = e;
+}
+
 cudaError_t take_enqueue_error() {
 	const cudaError_t e = t_enqueueError;
 	t_enqueueError = cudaSuccess;

@@ -217,6 +217,9 @@ size_t scan_scratch_elems(uint32_t n);
 // The first memset the launchers above failed to enqueue on this thread since the last call
 // (cudaSuccess if none), cleared by the call; callers check it with cudaGetLastError after launching.
 cudaError_t take_enqueue_error();
+// Makes `to` wait for what `from` has queued so far (an event recorded on `from`); inside a stream
+// capture this forks or joins branches of the graph.  A failure is kept for take_enqueue_error.
+void enqueue_join(cudaStream_t from, cudaStream_t to, cudaEvent_t event);
 // Kernels launched by this library in this process (host-side count).
 uint64_t launch_count();
 // Adds kernels launched through a replayed CUDA graph to that count.

@@ -269,8 +269,12 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_project(params, fb, stream);
 		launch_setup_count(params, fb, stream);
 		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
-		launch_rows(fb, recordCap, tallTriangles, stream);
+		// the row intervals and the tile lists both follow the scans above and not each other: two
+		// branches, joined before the totals
+		enqueue_join(stream, ctx->branchStream, ctx->branchFork);
+		launch_rows(fb, recordCap, tallTriangles, ctx->branchStream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
+		enqueue_join(ctx->branchStream, stream, ctx->branchJoin);
 		launch_gather_totals(fb.triOffsets, (uint32_t)nt, fb.rowOffsets, recordCap, bins.offsets, totals.tiles, fb.errorFlag,
 		                     gathered, params.tileList, params.tileListCount, stream);
 	}));
