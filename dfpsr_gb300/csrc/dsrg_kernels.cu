@@ -731,15 +731,32 @@ __global__ void __launch_bounds__(ROWS_THREADS) rows_chunk_kernel(const DrawReco
 				if (offsets[mid] <= j0) lo = mid; else hi = mid;
 			}
 			uint32_t k = lo;
-			for (int i = 0; i < ROWS_PER_THREAD; i++) {
-				const uint32_t j = j0 + i;
-				if (j >= end) break;
-				while (offsets[k + 1] <= j) k++;
+			const uint32_t jEnd = min(j0 + (uint32_t)ROWS_PER_THREAD, end);
+			if (offsets[k + 1] >= jEnd) {
+				// all of this thread's rows belong to one record: stepped from the first (two divisions
+				// per edge instead of one per edge and row; rows past jEnd are stepped but not kept)
 				const int4 a = cornersA[k], c = cornersB[k];
-				int32_t left, right;
-				row_interval_regs(a.x, a.y, a.z, a.w, c.x, c.y, c.w + (int32_t)(j - offsets[k]), c.z, rights[k], left, right);
-				const uint32_t at = j - begin;
-				out[at + (at >> 5)] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				const int32_t flat[6] = {a.x, a.y, a.z, a.w, c.x, c.y};
+				int32_t lefts[ROWS_PER_THREAD], rightsOut[ROWS_PER_THREAD];
+				row_intervals_stepped(flat, c.w + (int32_t)(j0 - offsets[k]), ROWS_PER_THREAD, c.z, rights[k], lefts, rightsOut);
+#pragma unroll
+				for (int i = 0; i < ROWS_PER_THREAD; i++) {
+					const uint32_t j = j0 + i;
+					if (j >= jEnd) break;
+					const uint32_t at = j - begin;
+					out[at + (at >> 5)] = (uint32_t)(lefts[i] & 0xFFFF) | ((uint32_t)rightsOut[i] << 16);
+				}
+			} else {
+				for (int i = 0; i < ROWS_PER_THREAD; i++) {
+					const uint32_t j = j0 + i;
+					if (j >= end) break;
+					while (offsets[k + 1] <= j) k++;
+					const int4 a = cornersA[k], c = cornersB[k];
+					int32_t left, right;
+					row_interval_regs(a.x, a.y, a.z, a.w, c.x, c.y, c.w + (int32_t)(j - offsets[k]), c.z, rights[k], left, right);
+					const uint32_t at = j - begin;
+					out[at + (at >> 5)] = (uint32_t)(left & 0xFFFF) | ((uint32_t)right << 16);
+				}
 			}
 		}
 		__syncthreads();
