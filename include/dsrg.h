@@ -456,8 +456,10 @@ int dsrg_draw_higher(dsrg_context context, const dsrg_image *targetHeight, const
  *      (CubeMapF32::clear, spriteAPI.cpp:361-363); null for no shadows;
  *   5. addPointLight for every light (dsrg_light_points, with referenceThreads);
  *   6. blendLight(output, diffuse, light).
- * Every step runs on the context's stream in this order and the call waits twice: once inside the
- * shadow batch (which checks its buffers) and once at its end.  The images are those of the steps
+ * With a shadow batch, steps 1-3 run on a second stream of the context beside step 4 (they touch
+ * neither the cubes nor the batch's buffers) and step 5 waits for both; otherwise every step runs
+ * on the context's stream in this order.  The call waits twice: once inside the shadow batch
+ * (which checks its buffers) and once at its end.  The images are those of the steps
  * above (device, page-locked or pageable host memory; each pageable image is copied in once and,
  * if written, out once).  Shadow cubes (the batch's depth images and the lights' shadowCube) must
  * be device or page-locked memory.  The result equals that of the six calls made one by one. */
