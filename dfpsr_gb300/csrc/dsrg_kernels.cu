@@ -1079,7 +1079,7 @@ void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *err
 }
 
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
-                                 cudaStream_t stream) {
+                                 cudaStream_t stream, cudaStream_t rowStream, cudaEvent_t fork) {
 	if (!bins.cleared) {
 		memset_async(bins.counts, 0, sizeof(uint32_t) * 2 * b.totalTiles, stream);
 		memset_async(bins.bigCount, 0, sizeof(uint32_t), stream);
@@ -1092,13 +1092,26 @@ void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t
 	fb.counts.smallWidth = b.smallWidth;
 	fb.counts.depthOnly = b.depthOnly;
 	launch_setup_write(b, fb, recordCapacity, stream);
+	const uint32_t rowBlocks = recordCapacity / SCAN_CHUNK + 1, tileBlocks = (2 * b.totalTiles) / SCAN_CHUNK + 1;
+	if (rowStream && (size_t)rowBlocks + tileBlocks <= fb.scanScratchElems) {
+		// the row offsets on the second stream right after the records (each scan with its own part
+		// of the scratch), the big records' tile counts and the tile-list offsets on this one
+		enqueue_join(stream, rowStream, fork);
+		scan_launch(rowCounts, fb.rowOffsets, recordCapacity, fb.recordCountDevice, fb.scanScratch, rowBlocks, rowStream);
+	}
 	if (recordCapacity > 0) {
 		COUNT_LAUNCH();
 		launch_chained(bin_big_kernel<false>, sm_count() * 8, 256, stream, b, fb.records, bins, fb.errorFlag);
 	}
-	// the row offsets and the tile-list offsets in one pair of launches
+	if (rowStream && (size_t)rowBlocks + tileBlocks <= fb.scanScratchElems) {
+		scan_launch(bins.counts, bins.offsets, 2 * b.totalTiles, nullptr, fb.scanScratch + rowBlocks, fb.scanScratchElems - rowBlocks, stream);
+		return;
+	}
+	// the row offsets and the tile-list offsets in one pair of launches (rowStream, if given, waits
+	// for them)
 	scan_pair_launch(rowCounts, fb.rowOffsets, recordCapacity, fb.recordCountDevice, bins.counts, bins.offsets, 2 * b.totalTiles,
 	                 fb.scanScratch, fb.scanScratchElems, stream);
+	if (rowStream) enqueue_join(stream, rowStream, fork);
 }
 
 void launch_bin_count(const BatchParams &b, const FrameBuffers &fb, uint32_t recordCount, TileBins &bins, cudaStream_t stream) {

@@ -152,8 +152,10 @@ void launch_setup_write(const BatchParams &b, const FrameBuffers &fb, uint32_t r
 // bins here), then the big records' tile counts and the scans of row counts and tile counts: the
 // work of launch_setup_write + launch_row_offsets + launch_bin_count in one pass over the records.
 void launch_clear_tiles(const BatchParams &b, const TileBins &bins, int32_t *errorFlag, cudaStream_t stream);
+// With rowStream, the row-offset scan runs there (forked with `fork` right after the records) and
+// the caller's row-interval launch on rowStream follows it; the tile counts stay on `stream`.
 void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t recordCapacity, uint32_t *rowCounts, TileBins &bins,
-                                 cudaStream_t stream);
+                                 cudaStream_t stream, cudaStream_t rowStream = nullptr, cudaEvent_t fork = nullptr);
 // occludeFromExistingTriangles (api/rendererAPI.cpp:240-255): every solid draw command of the batch
 // whose bound exceeds one cell lowers the occlusion grid of its frame over the cells it covers.
 void launch_setup_occlude(const BatchParams &b, const FrameBuffers &fb, cudaStream_t stream);

@@ -268,10 +268,9 @@ static int enqueue_phases(dsrg_context ctx, BatchJob &job, BatchTotals &totals, 
 		launch_clear_tiles(params, bins, fb.errorFlag, stream);
 		launch_project(params, fb, stream);
 		launch_setup_count(params, fb, stream);
-		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream);
-		// the row intervals and the tile lists both follow the scans above and not each other: two
-		// branches, joined before the totals
-		enqueue_join(stream, ctx->branchStream, ctx->branchFork);
+		// the row offsets and intervals on a second branch right after the records, the tile counts,
+		// offsets and lists on this one: neither needs the other; joined before the totals
+		launch_setup_write_counting(params, fb, recordCap, rowCounts, bins, stream, ctx->branchStream, ctx->branchFork);
 		launch_rows(fb, recordCap, tallTriangles, ctx->branchStream);
 		launch_bin_fill(params, fb, recordCap, bins, stream);
 		enqueue_join(ctx->branchStream, stream, ctx->branchJoin);
