@@ -224,37 +224,29 @@ __global__ void fixed_order_sum_kernel(const float *blockSums, int32_t blocks, i
 
 // ------------------------------------------------------------------ adjoint
 
-// Position of the set bit of `mask` with the given rank (0 = lowest).
-__device__ __forceinline__ int nth_set_bit(uint32_t mask, int rank) {
-	int pos = 0;
-	for (int step = 16; step >= 1; step >>= 1) {
-		const int p = pos + step - 1;
-		const uint32_t below = p >= 31 ? mask : (mask & ((2u << p) - 1u));
-		if (__popc(below) <= rank) pos += step;
-	}
-	return pos;
-}
-
-// Adds `value` to base[key] (a float4), once per distinct key in the warp: the lanes holding the
-// same key sum their values in a tree by rank, and the lowest of them issues one vector atomic.
-__device__ __forceinline__ void warp_aggregated_add(float4 *base, uint32_t key, float4 value, bool active) {
+// Adds `value` to base[key] (a float4) once per run of consecutive lanes holding the same key:
+// a segmented scan over the run (shuffles up, only within the run) and one vector atomic from
+// its last lane.  Consecutive pixels mostly share their triangle's corners and often a texel, so
+// runs catch nearly all repeats; equal keys in separate runs each add their own sum.
+__device__ __forceinline__ void warp_run_add(float4 *base, uint32_t key, float4 value, bool active) {
 	const uint32_t k = active ? key : 0xFFFFFFFFu;
-	const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
 	const int lane = threadIdx.x & 31;
-	const int rank = __popc(peers & ((1u << lane) - 1u)), n = __popc(peers);
-	if (__any_sync(0xFFFFFFFFu, n > 1)) {
+	const uint32_t previous = __shfl_up_sync(0xFFFFFFFFu, k, 1);
+	const bool head = lane == 0 || previous != k;
+	const uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
+	const int start = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane))); // this lane's run begins here
+	if (heads != 0xFFFFFFFFu) { // some run holds more than one lane
 		for (int d = 1; d < 32; d <<= 1) {
-			const int srcRank = rank + d;
-			const int src = srcRank < n ? nth_set_bit(peers, srcRank) : lane;
-			const float ox = __shfl_sync(0xFFFFFFFFu, value.x, src), oy = __shfl_sync(0xFFFFFFFFu, value.y, src);
-			const float oz = __shfl_sync(0xFFFFFFFFu, value.z, src), ow = __shfl_sync(0xFFFFFFFFu, value.w, src);
-			if ((rank & (2 * d - 1)) == 0 && srcRank < n) {
+			const float ox = __shfl_up_sync(0xFFFFFFFFu, value.x, d), oy = __shfl_up_sync(0xFFFFFFFFu, value.y, d);
+			const float oz = __shfl_up_sync(0xFFFFFFFFu, value.z, d), ow = __shfl_up_sync(0xFFFFFFFFu, value.w, d);
+			if (lane - d >= start) {
 				value.x = fadd(value.x, ox); value.y = fadd(value.y, oy);
 				value.z = fadd(value.z, oz); value.w = fadd(value.w, ow);
 			}
 		}
 	}
-	if (active && rank == 0) atomicAdd(base + key, value);
+	const bool last = lane == 31 || ((heads >> (lane + 1)) & 1u) != 0;
+	if (active && last) atomicAdd(base + key, value);
 }
 
 // Per-pixel gradients: texture (4 taps), vertex colours (3 corners) and light.
@@ -319,8 +311,8 @@ __global__ void __launch_bounds__(256) adjoint_atomic_kernel(DiffModel m, DiffPa
 		PixelShade s;
 		PixelGrad pg;
 		const bool active = i < pixels && pixel_gradient(m, q, visibility, i, grad[i < pixels ? i : 0], s, pg);
-		for (int k = 0; k < 4; k++) warp_aggregated_add(gradTexture, active ? s.taps[k] : 0u, pg.tex[k], active);
-		for (int c = 0; c < 3; c++) warp_aggregated_add(gradVertex, active ? (uint32_t)s.point[c] : 0u, pg.vertex[c], active);
+		for (int k = 0; k < 4; k++) warp_run_add(gradTexture, active ? s.taps[k] : 0u, pg.tex[k], active);
+		for (int c = 0; c < 3; c++) warp_run_add(gradVertex, active ? (uint32_t)s.point[c] : 0u, pg.vertex[c], active);
 		if (active)
 			for (int j = 0; j < 4; j++) light[j] = fadd(light[j], pg.light[j]);
 	}
