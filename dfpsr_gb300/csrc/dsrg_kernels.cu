@@ -483,102 +483,6 @@ static void scan_launch(const uint32_t *in, uint32_t *out, uint32_t n, const uin
 	launch_chained(scan_apply_kernel, blocks, SCAN_THREADS, stream, in, out, n, nDevice, n, scratch);
 }
 
-// Two exclusive scans in one launch pair: blocks [0, firstBlocks) scan array 0, the rest array 1,
-// each with its own run of chunk sums in the scratch.
-struct ScanPairJobs {
-	const uint32_t *in0, *in1;
-	uint32_t *out0, *out1;
-	const uint32_t *nDevice0, *nDevice1;
-	uint32_t n0, n1, firstBlocks;
-};
-
-__global__ void __launch_bounds__(SCAN_THREADS) scan_pair_reduce_kernel(ScanPairJobs p, uint32_t *chunkSums) {
-	chain_enter();
-	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
-	const bool second = blockIdx.x >= p.firstBlocks;
-	const uint32_t block = second ? blockIdx.x - p.firstBlocks : blockIdx.x;
-	const uint32_t *in = second ? p.in1 : p.in0;
-	const uint32_t n = second ? p.n1 : p.n0;
-	const uint32_t count = scan_length(n, second ? p.nDevice1 : p.nDevice0, n);
-	const uint32_t begin = block * SCAN_CHUNK;
-	uint32_t v = 0;
-	for (uint32_t i = begin + threadIdx.x; i < begin + SCAN_CHUNK && i < count; i += SCAN_THREADS) v += in[i];
-	const uint32_t total = block_sum(v, warpSums);
-	if (threadIdx.x == 0) chunkSums[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) scan_pair_apply_kernel(ScanPairJobs p, const uint32_t *__restrict__ chunkSums) {
-	chain_enter();
-	__shared__ uint32_t values[SCAN_CHUNK + SCAN_CHUNK / 32];
-	__shared__ uint32_t warpSums[SCAN_THREADS / 32];
-	const bool second = blockIdx.x >= p.firstBlocks;
-	const uint32_t block = second ? blockIdx.x - p.firstBlocks : blockIdx.x;
-	const uint32_t sumsBase = second ? p.firstBlocks : 0u;
-	const uint32_t *in = second ? p.in1 : p.in0;
-	uint32_t *out = second ? p.out1 : p.out0;
-	const uint32_t n = second ? p.n1 : p.n0;
-	const uint32_t count = scan_length(n, second ? p.nDevice1 : p.nDevice0, n);
-	const uint32_t begin = block * SCAN_CHUNK;
-	if (begin > count || (begin == count && count != 0)) return;
-	uint32_t q = 0;
-	for (uint32_t c = threadIdx.x; c < block; c += SCAN_THREADS) q += chunkSums[sumsBase + c];
-	const uint32_t prefix = block_sum(q, warpSums);
-	for (int k = 0; k < SCAN_PER_THREAD; k++) {
-		const uint32_t i = begin + k * SCAN_THREADS + threadIdx.x;
-		const uint32_t at = k * SCAN_THREADS + threadIdx.x;
-		values[at + (at >> 5)] = i < count ? in[i] : 0u;
-	}
-	__syncthreads();
-	uint32_t local[SCAN_PER_THREAD];
-	uint32_t mine = 0;
-	for (int k = 0; k < SCAN_PER_THREAD; k++) {
-		local[k] = mine;
-		const uint32_t at = threadIdx.x * SCAN_PER_THREAD + k;
-		mine += values[at + (at >> 5)];
-	}
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t x = mine;
-	for (int o = 1; o < 32; o <<= 1) {
-		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-		if (lane >= o) x += y;
-	}
-	if (lane == 31) warpSums[warp] = x;
-	__syncthreads();
-	uint32_t before = prefix + x - mine;
-	for (int w = 0; w < warp; w++) before += warpSums[w];
-	for (int k = 0; k < SCAN_PER_THREAD; k++) {
-		const uint32_t at = threadIdx.x * SCAN_PER_THREAD + k;
-		values[at + (at >> 5)] = before + local[k];
-	}
-	__syncthreads();
-	for (int k = 0; k < SCAN_PER_THREAD; k++) {
-		const uint32_t i = begin + k * SCAN_THREADS + threadIdx.x;
-		const uint32_t at = k * SCAN_THREADS + threadIdx.x;
-		if (i < count) out[i] = values[at + (at >> 5)];
-	}
-	if (threadIdx.x == SCAN_THREADS - 1 && (count == 0 || (count - 1) / SCAN_CHUNK == block)) {
-		uint32_t total = prefix;
-		for (int w = 0; w < SCAN_THREADS / 32; w++) total += warpSums[w];
-		out[count] = total;
-	}
-}
-
-static void scan_pair_launch(const uint32_t *in0, uint32_t *out0, uint32_t n0, const uint32_t *nDevice0, const uint32_t *in1,
-                             uint32_t *out1, uint32_t n1, uint32_t *scratch, size_t scratchElems, cudaStream_t stream) {
-	const uint32_t blocks0 = n0 / SCAN_CHUNK + 1, blocks1 = n1 / SCAN_CHUNK + 1;
-	if ((size_t)blocks0 + blocks1 > scratchElems) {
-		scan_launch(in0, out0, n0, nDevice0, scratch, scratchElems, stream);
-		scan_launch(in1, out1, n1, nullptr, scratch, scratchElems, stream);
-		return;
-	}
-	ScanPairJobs p;
-	p.in0 = in0; p.in1 = in1; p.out0 = out0; p.out1 = out1; p.nDevice0 = nDevice0; p.nDevice1 = nullptr;
-	p.n0 = n0; p.n1 = n1; p.firstBlocks = blocks0;
-	COUNT_LAUNCH();
-	launch_chained(scan_pair_reduce_kernel, blocks0 + blocks1, SCAN_THREADS, stream, p, scratch);
-	COUNT_LAUNCH();
-	launch_chained(scan_pair_apply_kernel, blocks0 + blocks1, SCAN_THREADS, stream, p, (const uint32_t *)scratch);
-}
 
 void launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *scratch, size_t scratchElems, cudaStream_t stream) {
 	scan_launch(in, out, n, nullptr, scratch, scratchElems, stream);
@@ -1107,10 +1011,9 @@ void launch_setup_write_counting(const BatchParams &b, FrameBuffers fb, uint32_t
 		scan_launch(bins.counts, bins.offsets, 2 * b.totalTiles, nullptr, fb.scanScratch + rowBlocks, fb.scanScratchElems - rowBlocks, stream);
 		return;
 	}
-	// the row offsets and the tile-list offsets in one pair of launches (rowStream, if given, waits
-	// for them)
-	scan_pair_launch(rowCounts, fb.rowOffsets, recordCapacity, fb.recordCountDevice, bins.counts, bins.offsets, 2 * b.totalTiles,
-	                 fb.scanScratch, fb.scanScratchElems, stream);
+	// one after the other on this stream, sharing the scratch (rowStream, if given, waits for both)
+	scan_launch(rowCounts, fb.rowOffsets, recordCapacity, fb.recordCountDevice, fb.scanScratch, fb.scanScratchElems, stream);
+	scan_launch(bins.counts, bins.offsets, 2 * b.totalTiles, nullptr, fb.scanScratch, fb.scanScratchElems, stream);
 	if (rowStream) enqueue_join(stream, rowStream, fork);
 }
 
