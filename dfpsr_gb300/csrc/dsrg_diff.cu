@@ -425,9 +425,64 @@ static int reserve_segmented_sum(dsrg_diff d, uint64_t n, uint32_t keyEnd) {
 	return DSRG_OK;
 }
 
+// Entries a block of compact_count_kernel / compact_write_kernel takes (256 threads x 16).
+static const int COMPACT_ITEMS = 16;
+static const uint64_t COMPACT_CHUNK = 256 * COMPACT_ITEMS;
+
+// The entries of each block's chunk with a key below keyEnd (the others are pixels without a
+// triangle), counted.
+__global__ void __launch_bounds__(256) compact_count_kernel(const uint32_t *__restrict__ keys, uint64_t n, uint32_t keyEnd,
+                                                            uint32_t *blockCounts) {
+	__shared__ uint32_t warpSums[8];
+	const uint64_t begin = (uint64_t)blockIdx.x * COMPACT_CHUNK;
+	uint32_t c = 0;
+	for (int r = 0; r < COMPACT_ITEMS; r++) {
+		const uint64_t i = begin + (uint64_t)r * 256 + threadIdx.x;
+		if (i < n && keys[i] < keyEnd) c++;
+	}
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+	if ((threadIdx.x & 31) == 0) warpSums[threadIdx.x >> 5] = c;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		uint32_t total = 0;
+		for (int w = 0; w < 8; w++) total += warpSums[w];
+		blockCounts[blockIdx.x] = total;
+	}
+}
+
+// Those entries as (key, entry index) pairs, in entry order, each block from its scanned offset.
+__global__ void __launch_bounds__(256) compact_write_kernel(const uint32_t *__restrict__ keys, uint64_t n, uint32_t keyEnd,
+                                                            const uint32_t *__restrict__ blockOffsets, uint32_t *outKeys,
+                                                            uint32_t *outIds) {
+	__shared__ uint32_t warpCounts[8];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint64_t begin = (uint64_t)blockIdx.x * COMPACT_CHUNK;
+	uint32_t running = blockOffsets[blockIdx.x];
+	for (int r = 0; r < COMPACT_ITEMS; r++) {
+		const uint64_t i = begin + (uint64_t)r * 256 + threadIdx.x;
+		const uint32_t k = i < n ? keys[i] : keyEnd;
+		const bool keep = k < keyEnd;
+		const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);
+		if (lane == 0) warpCounts[warp] = __popc(kept);
+		__syncthreads();
+		uint32_t before = running, total = 0;
+		for (int w = 0; w < 8; w++) {
+			if (w < warp) before += warpCounts[w];
+			total += warpCounts[w];
+		}
+		if (keep) {
+			const uint32_t at = before + __popc(kept & ((1u << lane) - 1u));
+			outKeys[at] = k;
+			outIds[at] = (uint32_t)i;
+		}
+		running += total;
+		__syncthreads(); // warpCounts is read before the next round writes it
+	}
+}
+
 // Sums `values` per key in [0, keyEnd) into out (keyEnd float4), in the order of the entries:
-// count and scan the keys, stable-sort the entry ids by key, then one ordered sum per key.
-// Its scratch must have been reserved (reserve_segmented_sum).
+// count and scan the keys, keep the entries with a key (in entry order), stable-sort their ids by
+// key, then one ordered sum per key.  Its scratch must have been reserved (reserve_segmented_sum).
 static int segmented_sum(dsrg_diff d, const uint32_t *keys, const float4 *values, uint64_t n, uint32_t keyEnd, float4 *out) {
 	dsrg_context ctx = d->context;
 	cudaStream_t stream = ctx->stream;
@@ -438,13 +493,27 @@ static int segmented_sum(dsrg_diff d, const uint32_t *keys, const float4 *values
 	key_count_kernel<<<grid_for(n, 256), 256, 0, stream>>>(keys, n, keyEnd, d->counts.ptr);
 	add_launches(1);
 	launch_scan(d->counts.ptr, d->segments.ptr, keyEnd, ctx->scanScratch.ptr, ctx->scanScratch.capacity, stream);
-	// the entry ids sorted by key, entries of one key in entry order
+	// the entries with a key, in entry order, into the sort's second buffers (its first pass reads
+	// them from there); their number comes back to the host for the sort's launch shape
+	const uint32_t blocks = (uint32_t)((n + COMPACT_CHUNK - 1) / COMPACT_CHUNK);
+	uint32_t kept = 0;
+	if (blocks > 0) {
+		compact_count_kernel<<<blocks, 256, 0, stream>>>(keys, n, keyEnd, d->hist.ptr);
+		launch_scan(d->hist.ptr, d->offsets.ptr, blocks, ctx->scanScratch.ptr, ctx->scanScratch.capacity, stream);
+		compact_write_kernel<<<blocks, 256, 0, stream>>>(keys, n, keyEnd, d->offsets.ptr, d->keysB.ptr, d->idsB.ptr);
+		add_launches(2);
+		TRY(cudaGetLastError());
+		TRY(cudaMemcpyAsync(ctx->pinnedReadback + 8, d->offsets.ptr + blocks, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+		TRY(cudaStreamSynchronize(stream));
+		kept = ctx->pinnedReadback[8];
+	}
+	// the kept entries' ids sorted by key, entries of one key in entry order
 	SortBuffers sb;
 	sb.keysA = d->keysA.ptr; sb.keysB = d->keysB.ptr; sb.idsA = d->idsA.ptr; sb.idsB = d->idsB.ptr;
 	sb.hist = d->hist.ptr; sb.offsets = d->offsets.ptr;
 	sb.scanScratch = ctx->scanScratch.ptr; sb.scanScratchElems = ctx->scanScratch.capacity;
 	const uint32_t *sortedKeys = nullptr, *iin = nullptr;
-	launch_stable_sort(keys, nullptr, n, bits, sb, stream, &sortedKeys, &iin);
+	launch_stable_sort(d->keysB.ptr, d->idsB.ptr, kept, bits, sb, stream, &sortedKeys, &iin);
 	segment_sum_kernel<<<grid_for((uint64_t)keyEnd * 32, 256), 256, 0, stream>>>(d->segments.ptr, iin, values, keyEnd, out);
 	add_launches(1);
 	TRY(cudaGetLastError());

@@ -206,7 +206,8 @@ struct dsrg_context_s {
 	size_t pinnedCapacity = 0;
 	DeviceBuffer<uint32_t> control;      // [0] tile queue, [1] error flag, [4..7] a batch's gathered totals, [9] listed tiles
 	DeviceBuffer<uint32_t> tileList;     // the tiles of a batch that have tile-list entries
-	uint32_t *pinnedReadback = nullptr;  // page-locked: the gathered totals (written there by the GPU) and the fragment count
+	uint32_t *pinnedReadback = nullptr;  // page-locked: the gathered totals (written there by the GPU), the fragment count,
+	                                     // [8] the entries a deterministic adjoint's sums keep
 	uint32_t *readbackDevice = nullptr;  // its device address
 	bool timingPending = false;          // stats' times not yet read from the events of the last call
 	bool timingHasRaster = false;
